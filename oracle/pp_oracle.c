@@ -1,0 +1,695 @@
+/*
+ * pp_oracle.c -- CPU restatement of the PatchyParticles roto-translation MC path. TEST INFRASTRUCTURE:
+ * see pp_oracle.h for who may use it and how it is pinned. Each routine names the reference routine it
+ * restates (file:line inside the reference project) and keeps its floating-point operation order; the
+ * build uses -ffp-contract=off. Parity is pinned against the reference built from source (oracle/_ref)
+ * and against tests/golden/ outputs of that build.
+ */
+#include "pp_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+struct orc_system {
+	orc_params prm;
+	int N;
+	double box[3];
+	double V;
+	double energy;
+	double kf_sqr_rcut;
+	double r_cut;
+	int overlap;
+	long long tries[ORC_N_MOVES];
+	long long accepted[ORC_N_MOVES];
+	double *r, *r_old;  /* N x 3 */
+	double *R, *R_old;  /* N x 9, row-major: R[i*9 + 3*row + col] */
+	double *patch;      /* N x 12 */
+	double base[4][3];
+	/* linked-list cells (cells.h:16-21) */
+	int nside[3];
+	int ncells;
+	int *head, *next, *cell, *cell_old;
+	/* drand48 state X (48 bits) */
+	unsigned long long X;
+};
+
+/* ---------------------------------------------------------------- drand48 (POSIX recurrence) */
+/* X <- (0x5DEECE66D X + 0xB) mod 2^48, returned as X / 2^48; srand48(s) sets X = (s & 0xffffffff) << 16 | 0x330E. */
+static void orc_seed(orc_system *s, int seed) {
+	s->X = ((unsigned long long) (unsigned int) seed << 16) | 0x330EULL;
+}
+
+static double orc_drand(orc_system *s) {
+	s->X = (0x5DEECE66DULL * s->X + 0xBULL) & 0xFFFFFFFFFFFFULL;
+	return (double) s->X * 0x1p-48;
+}
+
+void orc_drand48_sequence(int seed, int n, double *out) {
+	orc_system tmp;
+	orc_seed(&tmp, seed);
+	for(int i = 0; i < n; i++) out[i] = orc_drand(&tmp);
+}
+
+/* ---------------------------------------------------------------- vector helpers (utils.c, utils.h) */
+#define O_SCALAR(x, y) ((x)[0] * (y)[0] + (x)[1] * (y)[1] + (x)[2] * (y)[2]) /* utils.h:16 */
+
+static void o_normalize(double *v) { /* utils.c:31-36 */
+	double norm = sqrt(O_SCALAR(v, v));
+	v[0] /= norm;
+	v[1] /= norm;
+	v[2] /= norm;
+}
+
+static void o_cross(const double *a, const double *b, double *res) { /* utils.c:25-29 */
+	res[0] = a[1] * b[2] - a[2] * b[1];
+	res[1] = a[2] * b[0] - a[0] * b[2];
+	res[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+static void o_gram_schmidt(double *v1, double *v2, double *v3) { /* utils.c:91-113 */
+	double v1_norm2 = O_SCALAR(v1, v1);
+	double v2_v1 = O_SCALAR(v2, v1);
+	double b1 = v2_v1 / v1_norm2;
+	for(int k = 0; k < 3; k++) v2[k] -= b1 * v1[k];
+	double v3_v1 = O_SCALAR(v3, v1);
+	double v3_v2 = O_SCALAR(v3, v2);
+	double v2_norm2 = O_SCALAR(v2, v2);
+	b1 = v3_v1 / v1_norm2;
+	double b2 = v3_v2 / v2_norm2;
+	for(int k = 0; k < 3; k++) v3[k] -= b1 * v1[k] + b2 * v2[k];
+	o_normalize(v1);
+	o_normalize(v2);
+	o_normalize(v3);
+}
+
+/* patches[i] = R . base[i] with the MATRIX_VECTOR_MULTIPLICATION order (utils.h:18-22) */
+static void o_set_patches(orc_system *s, int p) {
+	const double *R = s->R + 9 * p;
+	double *P = s->patch + 12 * p;
+	for(int i = 0; i < 4; i++) {
+		const double *b = s->base[i];
+		P[3 * i + 0] = R[0] * b[0] + R[1] * b[1] + R[2] * b[2];
+		P[3 * i + 1] = R[3] * b[0] + R[4] * b[1] + R[5] * b[2];
+		P[3 * i + 2] = R[6] * b[0] + R[7] * b[1] + R[8] * b[2];
+	}
+}
+
+/* random_vector_on_sphere (utils.c:115-131): Marsaglia (1972) rejection on the unit disc */
+static void o_random_vector_on_sphere(orc_system *s, double *res) {
+	double ran1, ran2, ransq;
+	do {
+		ran1 = 1. - 2. * orc_drand(s);
+		ran2 = 1. - 2. * orc_drand(s);
+		ransq = ran1 * ran1 + ran2 * ran2;
+	} while(ransq >= 1.);
+	double ranh = 2. * sqrt(1. - ransq);
+	res[0] = ran1 * ranh;
+	res[1] = ran2 * ranh;
+	res[2] = 1. - 2. * ransq;
+}
+
+/* utils_rotate_matrix (utils.c:204-209): new = old . Rot(axis, t), Rot from get_rotation_matrix (utils.c:186-202) */
+static void o_rotate_matrix(const double *old, double *out, const double *a, double t) {
+	double st = sin(t);
+	double ct = cos(t);
+	double uct = 1. - ct;
+	double m[9];
+	m[0] = a[0] * a[0] + (1. - a[0] * a[0]) * ct;
+	m[1] = a[0] * a[1] * uct - a[2] * st;
+	m[2] = a[0] * a[2] * uct + a[1] * st;
+	m[3] = a[0] * a[1] * uct + a[2] * st;
+	m[4] = a[1] * a[1] + (1. - a[1] * a[1]) * ct;
+	m[5] = a[1] * a[2] * uct - a[0] * st;
+	m[6] = a[0] * a[2] * uct - a[1] * st;
+	m[7] = a[1] * a[2] * uct + a[0] * st;
+	m[8] = a[2] * a[2] + (1. - a[2] * a[2]) * ct;
+	/* matrix_matrix_multiplication (utils.c:172-184) */
+	for(int i = 0; i < 3; i++)
+		for(int j = 0; j < 3; j++) out[3 * i + j] = old[3 * i + 0] * m[0 + j] + old[3 * i + 1] * m[3 + j] + old[3 * i + 2] * m[6 + j];
+}
+
+void orc_base_patches(double base[4][3]) { /* _init_tetrahedral_patches, system.c:20-31 */
+	double h = 0.5 / sqrt(3.);
+	double v[4][3] = { { -h, -h, h }, { h, -h, -h }, { h, h, h }, { -h, h, -h } };
+	for(int i = 0; i < 4; i++) {
+		o_normalize(v[i]);
+		memcpy(base[i], v[i], sizeof(v[i]));
+	}
+}
+
+/* ---------------------------------------------------------------- cells (cells.c) */
+static int o_cell_index(const orc_system *s, const double *r, int idx[3]) { /* cells.c:43-49 */
+	for(int k = 0; k < 3; k++) idx[k] = (int) ((r[k] / s->box[k] - floor(r[k] / s->box[k])) * (1. - DBL_EPSILON) * s->nside[k]);
+	return (idx[0] * s->nside[1] + idx[1]) * s->nside[2] + idx[2];
+}
+
+static int o_cells_init(orc_system *s) { /* cells.c:17-37 */
+	for(int k = 0; k < 3; k++) {
+		s->nside[k] = floor(s->box[k] / s->r_cut);
+		if(s->nside[k] < 3) s->nside[k] = 3;
+	}
+	s->ncells = s->nside[0] * s->nside[1] * s->nside[2];
+	free(s->head);
+	s->head = malloc(sizeof(int) * s->ncells);
+	if(s->head == NULL) return -1;
+	for(int i = 0; i < s->ncells; i++) s->head[i] = -1;
+	for(int i = 0; i < s->N; i++) s->next[i] = -1;
+	return 0;
+}
+
+static void o_cells_fill(orc_system *s) { /* cells.c:51-63 */
+	int ind[3];
+	for(int i = 0; i < s->N; i++) {
+		int c = o_cell_index(s, s->r + 3 * i, ind);
+		s->next[i] = s->head[c];
+		s->head[c] = i;
+		s->cell[i] = c;
+		s->cell_old[i] = c;
+	}
+}
+
+static void o_unlink(orc_system *s, int p, int c) {
+	if(s->head[c] == p) s->head[c] = s->next[p];
+	else {
+		int q = s->head[c];
+		while(s->next[q] != p) q = s->next[q];
+		s->next[q] = s->next[p];
+	}
+}
+
+static void o_change_cell(orc_system *s, int p) { /* MC_change_cell, MC.c:180-206 */
+	int ind[3];
+	int c = o_cell_index(s, s->r + 3 * p, ind);
+	if(c == s->cell[p]) {
+		s->cell_old[p] = s->cell[p];
+		return;
+	}
+	o_unlink(s, p, s->cell[p]);
+	s->next[p] = s->head[c];
+	s->head[c] = p;
+	s->cell_old[p] = s->cell[p];
+	s->cell[p] = c;
+}
+
+/* ---------------------------------------------------------------- pair interaction and energy (MC.c) */
+/* MC_would_interact (MC.c:232-266): q's position r and patches qp, seen from particle p */
+static int o_would_interact(const orc_system *s, int p, const double *r, const double *qp) {
+	const double *rp = s->r + 3 * p;
+	double d[3] = { r[0] - rp[0], r[1] - rp[1], r[2] - rp[2] };
+	d[0] -= s->box[0] * rint(d[0] / s->box[0]);
+	d[1] -= s->box[1] * rint(d[1] / s->box[1]);
+	d[2] -= s->box[2] * rint(d[2] / s->box[2]);
+	double dist2 = O_SCALAR(d, d);
+	if(dist2 < 1.) return ORC_OVERLAP;
+	if(dist2 < s->kf_sqr_rcut) {
+		double norm = sqrt(dist2);
+		d[0] /= norm;
+		d[1] /= norm;
+		d[2] /= norm;
+		const double *pp = s->patch + 12 * p;
+		for(int a = 0; a < 4; a++) {
+			double p_cos = O_SCALAR(d, pp + 3 * a);
+			if(p_cos > s->prm.kf_cosmax) {
+				for(int b = 0; b < 4; b++) {
+					double q_cos = -O_SCALAR(d, qp + 3 * b);
+					if(q_cos > s->prm.kf_cosmax) return ORC_PATCH_BOND;
+				}
+			}
+		}
+	}
+	return ORC_NO_BOND;
+}
+
+int orc_interact(orc_system *s, int i, int j) { /* MC_interact, MC.c:268-270 */
+	return o_would_interact(s, i, s->r + 3 * j, s->patch + 12 * j);
+}
+
+static double o_energy(orc_system *s, int p) { /* MC_energy, MC.c:272-309 */
+	s->overlap = 0;
+	double E = 0.;
+	int ind[3];
+	o_cell_index(s, s->r + 3 * p, ind);
+	for(int j = -1; j < 2; j++) {
+		int cx = (ind[0] + j + s->nside[0]) % s->nside[0];
+		for(int k = -1; k < 2; k++) {
+			int cy = (ind[1] + k + s->nside[1]) % s->nside[1];
+			for(int l = -1; l < 2; l++) {
+				int cz = (ind[2] + l + s->nside[2]) % s->nside[2];
+				int q = s->head[(cx * s->nside[1] + cy) * s->nside[2] + cz];
+				while(q != -1) {
+					if(q != p) {
+						int val = orc_interact(s, p, q);
+						if(val == ORC_PATCH_BOND) E -= 1.;
+						else if(val == ORC_OVERLAP) {
+							s->overlap = 1;
+							return 0.;
+						}
+					}
+					q = s->next[q];
+				}
+			}
+		}
+	}
+	return E;
+}
+
+double orc_particle_energy(orc_system *s, int i, int *overlap) {
+	double E = o_energy(s, i);
+	if(overlap) *overlap = s->overlap;
+	return E;
+}
+
+/* full 27-cell walk of particle p without early exit (as output_print_bonds, output.c:213-268) */
+static void o_partners(orc_system *s, int p, int *nb, int *no, int *bonded, int cap) {
+	int ind[3];
+	*nb = *no = 0;
+	o_cell_index(s, s->r + 3 * p, ind);
+	for(int j = -1; j < 2; j++) {
+		int cx = (ind[0] + j + s->nside[0]) % s->nside[0];
+		for(int k = -1; k < 2; k++) {
+			int cy = (ind[1] + k + s->nside[1]) % s->nside[1];
+			for(int l = -1; l < 2; l++) {
+				int cz = (ind[2] + l + s->nside[2]) % s->nside[2];
+				int q = s->head[(cx * s->nside[1] + cy) * s->nside[2] + cz];
+				while(q != -1) {
+					if(q != p) {
+						int val = orc_interact(s, p, q);
+						if(val == ORC_PATCH_BOND) {
+							if(bonded != NULL && *nb < cap) bonded[*nb] = q;
+							(*nb)++;
+						}
+						else if(val == ORC_OVERLAP) (*no)++;
+					}
+					q = s->next[q];
+				}
+			}
+		}
+	}
+}
+
+double orc_energies(orc_system *s, double *E, int *overlap, int *n_bonds, int *n_overlaps) {
+	double tot = 0.;
+	for(int i = 0; i < s->N; i++) {
+		double e = o_energy(s, i);
+		if(E) E[i] = e;
+		if(overlap) overlap[i] = s->overlap;
+		tot += e;
+		if(n_bonds || n_overlaps) {
+			int nb, no;
+			o_partners(s, i, &nb, &no, NULL, 0);
+			if(n_bonds) n_bonds[i] = nb;
+			if(n_overlaps) n_overlaps[i] = no;
+		}
+	}
+	return tot * 0.5;
+}
+
+static int cmp_int(const void *a, const void *b) {
+	int x = *(const int *) a, y = *(const int *) b;
+	return (x > y) - (x < y);
+}
+
+int orc_bond_lists(orc_system *s, int *offsets, int *partners, int cap) {
+	int total = 0;
+	for(int i = 0; i < s->N; i++) {
+		int nb, no;
+		offsets[i] = total;
+		o_partners(s, i, &nb, &no, partners + total, cap - total);
+		if(total + nb > cap) return -1;
+		qsort(partners + total, nb, sizeof(int), cmp_int);
+		total += nb;
+	}
+	offsets[s->N] = total;
+	return total;
+}
+
+/* ---------------------------------------------------------------- moves (MC.c) */
+static void o_rototranslate(orc_system *s, int p, const double *disp, const double *newR) { /* MC.c:208-230 */
+	double *r = s->r + 3 * p, *ro = s->r_old + 3 * p;
+	for(int k = 0; k < 3; k++) {
+		ro[k] = r[k];
+		r[k] += disp[k];
+	}
+	memcpy(s->R_old + 9 * p, s->R + 9 * p, 9 * sizeof(double));
+	memcpy(s->R + 9 * p, newR, 9 * sizeof(double));
+	o_set_patches(s, p);
+	o_change_cell(s, p);
+}
+
+static void o_rollback(orc_system *s, int p) { /* MC_rollback_particle, MC.c:146-178 */
+	memcpy(s->r + 3 * p, s->r_old + 3 * p, 3 * sizeof(double));
+	memcpy(s->R + 9 * p, s->R_old + 9 * p, 9 * sizeof(double));
+	o_set_patches(s, p);
+	if(s->cell[p] != s->cell_old[p]) {
+		o_unlink(s, p, s->cell[p]);
+		s->next[p] = s->head[s->cell_old[p]];
+		s->head[s->cell_old[p]] = p;
+		int c = s->cell[p];
+		s->cell[p] = s->cell_old[p];
+		s->cell_old[p] = c;
+	}
+}
+
+static void o_move_rototranslate(orc_system *s) { /* MC_move_rototranslate, MC.c:311-340 */
+	int p = (int) (orc_drand(s) * s->N);
+	s->tries[ORC_ROTO_TRASL]++;
+	double disp[3];
+	disp[0] = (orc_drand(s) - 0.5) * s->prm.disp_max;
+	disp[1] = (orc_drand(s) - 0.5) * s->prm.disp_max;
+	disp[2] = (orc_drand(s) - 0.5) * s->prm.disp_max;
+	double theta = orc_drand(s) * s->prm.theta_max;
+	double axis[3], newR[9];
+	o_random_vector_on_sphere(s, axis);
+	o_rotate_matrix(s->R + 9 * p, newR, axis, theta);
+
+	double dE = -o_energy(s, p);
+	o_rototranslate(s, p, disp, newR);
+	dE += o_energy(s, p);
+
+	if(!s->overlap && (dE < 0. || orc_drand(s) < exp(-dE / s->prm.T))) {
+		s->energy += dE;
+		s->accepted[ORC_ROTO_TRASL]++;
+	}
+	else {
+		o_rollback(s, p);
+		s->overlap = 0;
+	}
+}
+
+static void o_change_volume(orc_system *s) { /* MC_change_volume, MC.c:450-513 */
+	s->tries[ORC_VOLUME]++;
+	double dE = -s->energy;
+	double V0 = s->box[0] * s->box[1] * s->box[2];
+	int dir = orc_drand(s) * 3;
+	double lnV = log(V0) + (orc_drand(s) - 0.5) * s->prm.rescale_factor_max;
+	double V1 = exp(lnV);
+	double old_side = s->box[dir];
+	double new_side = V1;
+	for(int i = 0; i < 3; i++)
+		if(i != dir) new_side /= s->box[i];
+	s->box[dir] = new_side;
+	double f = new_side / old_side;
+	for(int i = 0; i < s->N; i++) s->r[3 * i + dir] *= f;
+
+	if((s->box[dir] / s->nside[dir]) < s->r_cut) {
+		o_cells_init(s);
+		o_cells_fill(s);
+	}
+
+	int overlap_found = 0;
+	for(int i = 0; i < s->N && !overlap_found; i++) {
+		dE += o_energy(s, i) * 0.5;
+		if(s->overlap) overlap_found = 1;
+	}
+
+	double dV = V1 - V0;
+	double arg = -(s->prm.P * dV + dE) / s->prm.T + (s->N + 1) * log(f);
+	if(!overlap_found && orc_drand(s) < exp(arg)) {
+		s->V = V1;
+		s->energy += dE;
+		s->accepted[ORC_VOLUME]++;
+	}
+	else {
+		for(int i = 0; i < s->N; i++) s->r[3 * i + dir] /= f;
+		s->box[dir] = old_side;
+		s->overlap = 0;
+	}
+}
+
+/* one iteration of the do_NVT (MC.c:19-29) or do_NPT (MC.c:60-68) loop body */
+static void o_attempt(orc_system *s) {
+	if(s->prm.ensemble == ORC_NPT) {
+		if(orc_drand(s) < 1. / s->N) o_change_volume(s);
+		else if(s->N > 0) o_move_rototranslate(s);
+	}
+	else {
+		o_move_rototranslate(s);
+		/* do_NVT always draws the Lx-move number (MC.c:24), even with Lx_move = 0 */
+		(void) orc_drand(s);
+	}
+}
+
+void orc_sweep(orc_system *s) {
+	for(int i = 0; i < s->N; i++) o_attempt(s);
+}
+
+void orc_sweeps(orc_system *s, long long n) {
+	for(long long k = 0; k < n; k++) orc_sweep(s);
+}
+
+int orc_check_energy(orc_system *s) { /* MC_check_energy, MC.c:766-784 */
+	double E = 0.;
+	s->overlap = 0;
+	for(int i = 0; i < s->N; i++) {
+		E += o_energy(s, i);
+		double *R = s->R + 9 * i;
+		o_gram_schmidt(R, R + 3, R + 6);
+	}
+	E *= 0.5;
+	/* as in the reference, only the last particle's overlap flag survives the loop */
+	if(s->overlap) return -1;
+	if(fabs(s->energy) > 1e-5 && fabs((E - s->energy) / s->energy) > 1e-5) return -2;
+	s->energy = E;
+	return 0;
+}
+
+/* ---------------------------------------------------------------- construction / IO */
+static orc_system *o_alloc(int N, const orc_params *prm) {
+	orc_system *s = calloc(1, sizeof(orc_system));
+	if(s == NULL) return NULL;
+	s->prm = *prm;
+	s->N = N;
+	size_t n = N > 0 ? (size_t) N : 1;
+	s->r = calloc(3 * n, sizeof(double));
+	s->r_old = calloc(3 * n, sizeof(double));
+	s->R = calloc(9 * n, sizeof(double));
+	s->R_old = calloc(9 * n, sizeof(double));
+	s->patch = calloc(12 * n, sizeof(double));
+	s->next = malloc(n * sizeof(int));
+	s->cell = malloc(n * sizeof(int));
+	s->cell_old = malloc(n * sizeof(int));
+	if(!s->r || !s->r_old || !s->R || !s->R_old || !s->patch || !s->next || !s->cell || !s->cell_old) {
+		orc_free(s);
+		return NULL;
+	}
+	orc_base_patches(s->base);
+	s->kf_sqr_rcut = (1. + prm->kf_delta) * (1. + prm->kf_delta); /* system.c:86 */
+	s->r_cut = 1. + prm->kf_delta;                                /* system.c:249 */
+	orc_seed(s, prm->seed);
+	/* system_init seeds (system.c:75) and then _init_tetrahedral_patches builds base_orient through
+	 * set_orientation_around_vector (system.c:48), which draws two random unit vectors
+	 * (utils.c:232-233). base_orient is not used by roto-translations, but the draws move the stream. */
+	double unused[3];
+	o_random_vector_on_sphere(s, unused);
+	o_random_vector_on_sphere(s, unused);
+	return s;
+}
+
+static int o_finish(orc_system *s) {
+	s->V = s->box[0] * s->box[1] * s->box[2];
+	for(int i = 0; i < s->N; i++) o_set_patches(s, i);
+	if(o_cells_init(s) != 0) return -1;
+	o_cells_fill(s);
+	s->energy = 0.;
+	return 0;
+}
+
+orc_system *orc_load_rrr(const char *path, const orc_params *prm, char *err, int err_len) {
+	FILE *f = fopen(path, "r");
+	if(f == NULL) {
+		snprintf(err, err_len, "Initial_conditions_file '%s' is not readable", path);
+		return NULL;
+	}
+	int N;
+	double box[3];
+	/* header "step N Lx Ly Lz" (system.c:80-81) */
+	if(fscanf(f, "%*d %d %lf %lf %lf\n", &N, box, box + 1, box + 2) != 4 || N < 0) {
+		snprintf(err, err_len, "The initial configuration file '%s' is empty or its headers are malformed", path);
+		fclose(f);
+		return NULL;
+	}
+	orc_system *s = o_alloc(N, prm);
+	if(s == NULL) {
+		fclose(f);
+		snprintf(err, err_len, "out of memory");
+		return NULL;
+	}
+	memcpy(s->box, box, sizeof(box));
+	/* three lines per particle: orientation row 0, row 1, position (system.c:213-243) */
+	int i = 0;
+	double p1[3] = { 0., 0., 0. }, p2[3] = { 0., 0., 0. }, p3[3];
+	char line[512];
+	char *sr = fgets(line, sizeof(line), f);
+	while(sr != NULL) {
+		if(i >= N) {
+			i++;
+			break;
+		}
+		if(sscanf(line, "%lf %lf %lf\n", p1, p1 + 1, p1 + 2)) {
+		}
+		if(fscanf(f, "%lf %lf %lf\n", p2, p2 + 1, p2 + 2)) {
+		}
+		double *r = s->r + 3 * i;
+		if(fscanf(f, "%lf %lf %lf\n", r, r + 1, r + 2)) {
+		}
+		o_normalize(p1);
+		o_normalize(p2);
+		o_cross(p1, p2, p3);
+		double *R = s->R + 9 * i;
+		memcpy(R, p1, sizeof(p1));
+		memcpy(R + 3, p2, sizeof(p2));
+		memcpy(R + 6, p3, sizeof(p3));
+		o_gram_schmidt(R, R + 3, R + 6);
+		i++;
+		sr = fgets(line, sizeof(line), f);
+	}
+	fclose(f);
+	if(i != N) {
+		snprintf(err, err_len, "Number of particles found in configuration (%d) is different from the value found in the header (%d)", i, N);
+		orc_free(s);
+		return NULL;
+	}
+	if(o_finish(s) != 0) {
+		snprintf(err, err_len, "out of memory");
+		orc_free(s);
+		return NULL;
+	}
+	return s;
+}
+
+orc_system *orc_from_arrays(int N, const double *r, const double *R, const double box[3], const orc_params *prm) {
+	orc_system *s = o_alloc(N, prm);
+	if(s == NULL) return NULL;
+	memcpy(s->box, box, 3 * sizeof(double));
+	memcpy(s->r, r, 3 * sizeof(double) * N);
+	memcpy(s->R, R, 9 * sizeof(double) * N);
+	if(o_finish(s) != 0) {
+		orc_free(s);
+		return NULL;
+	}
+	return s;
+}
+
+void orc_free(orc_system *s) {
+	if(s == NULL) return;
+	free(s->r);
+	free(s->r_old);
+	free(s->R);
+	free(s->R_old);
+	free(s->patch);
+	free(s->head);
+	free(s->next);
+	free(s->cell);
+	free(s->cell_old);
+	free(s);
+}
+
+int orc_N(const orc_system *s) { return s->N; }
+void orc_box(const orc_system *s, double box[3]) { memcpy(box, s->box, 3 * sizeof(double)); }
+double orc_volume(const orc_system *s) { return s->V; }
+double orc_get_energy(const orc_system *s) { return s->energy; }
+void orc_set_energy(orc_system *s, double E) { s->energy = E; }
+
+void orc_get_state(const orc_system *s, double *r, double *R) {
+	if(r) memcpy(r, s->r, 3 * sizeof(double) * s->N);
+	if(R) memcpy(R, s->R, 9 * sizeof(double) * s->N);
+}
+
+void orc_get_patches(const orc_system *s, double *patches) { memcpy(patches, s->patch, 12 * sizeof(double) * s->N); }
+
+void orc_counters(const orc_system *s, long long tries[ORC_N_MOVES], long long accepted[ORC_N_MOVES]) {
+	memcpy(tries, s->tries, sizeof(s->tries));
+	memcpy(accepted, s->accepted, sizeof(s->accepted));
+}
+
+void orc_reset_counters(orc_system *s) { /* utils_reset_acceptance_counters, utils.c:276-282 */
+	memset(s->tries, 0, sizeof(s->tries));
+	memset(s->accepted, 0, sizeof(s->accepted));
+}
+
+int orc_save_rrr(const orc_system *s, long long step, const char *path) { /* output_save, output.c:302-317 */
+	FILE *out = fopen(path, "w");
+	if(out == NULL) return -1;
+	fprintf(out, "%lld %d %.12lf %.12lf %.12lf\n", step, s->N, s->box[0], s->box[1], s->box[2]);
+	for(int i = 0; i < s->N; i++) {
+		const double *R = s->R + 9 * i, *r = s->r + 3 * i;
+		fprintf(out, "%lf %lf %lf\n", R[0], R[1], R[2]);
+		fprintf(out, "%lf %lf %lf\n", R[3], R[4], R[5]);
+		fprintf(out, "%.12lf %.12lf %.12lf\n", r[0], r[1], r[2]);
+	}
+	fclose(out);
+	return 0;
+}
+
+/* ---------------------------------------------------------------- bounded multi-core throughput sample */
+typedef struct {
+	int N;
+	const double *r, *R;
+	double box[3];
+	orc_params prm;
+	double seconds;
+	long long attempts;
+	double elapsed;
+	int initial_energy_ok;
+} o_job;
+
+static double o_now(void) {
+	struct timespec ts;
+	clock_gettime(CLOCK_MONOTONIC, &ts);
+	return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
+static void *o_worker(void *arg) {
+	o_job *j = arg;
+	orc_system *s = orc_from_arrays(j->N, j->r, j->R, j->box, &j->prm);
+	if(s == NULL) return NULL;
+	int ov = 0;
+	double E = 0.;
+	for(int i = 0; i < s->N && !ov; i++) E += orc_particle_energy(s, i, &ov);
+	s->energy = 0.5 * E;
+	j->initial_energy_ok = !ov;
+	double t0 = o_now();
+	long long n = 0;
+	const int chunk = 4096;
+	do {
+		for(int k = 0; k < chunk; k++) o_attempt(s);
+		n += chunk;
+	} while(o_now() - t0 < j->seconds);
+	j->elapsed = o_now() - t0;
+	j->attempts = n;
+	orc_free(s);
+	return NULL;
+}
+
+double orc_parallel_throughput(int N, const double *r, const double *R, const double box[3], const orc_params *prm,
+		int threads, double seconds, long long *attempts_out) {
+	if(threads < 1) threads = 1;
+	o_job *jobs = calloc(threads, sizeof(o_job));
+	pthread_t *tid = calloc(threads, sizeof(pthread_t));
+	for(int t = 0; t < threads; t++) {
+		jobs[t].N = N;
+		jobs[t].r = r;
+		jobs[t].R = R;
+		memcpy(jobs[t].box, box, 3 * sizeof(double));
+		jobs[t].prm = *prm;
+		jobs[t].prm.seed = prm->seed + t;
+		jobs[t].seconds = seconds;
+		pthread_create(&tid[t], NULL, o_worker, &jobs[t]);
+	}
+	double rate = 0.;
+	long long total = 0;
+	for(int t = 0; t < threads; t++) {
+		pthread_join(tid[t], NULL);
+		if(jobs[t].elapsed > 0) rate += jobs[t].attempts / jobs[t].elapsed;
+		total += jobs[t].attempts;
+	}
+	free(jobs);
+	free(tid);
+	if(attempts_out) *attempts_out = total;
+	return rate;
+}

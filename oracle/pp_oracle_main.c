@@ -1,0 +1,196 @@
+/*
+ * pp_oracle_main.c -- TEST INFRASTRUCTURE: command-line driver of the oracle restatement, mirroring the
+ * reference main loop (main.c:26-143) for Dynamics = 0 in the NVT and NPT ensembles, with the reference
+ * input-file rules (parse_input.c:18-104) and output files (output.c:19-211, 302-317). Used to show that
+ * the restatement reproduces the reference trajectory: same input file -> same energy.dat,
+ * acceptance.dat, density.dat, stdout and configuration files.
+ *
+ *   pporacle input_file
+ */
+#include "pp_oracle.h"
+
+#include <ctype.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <unistd.h>
+
+#define MAXKEYS 256
+#define KEYLEN 256
+
+typedef struct {
+	int n;
+	char key[MAXKEYS][KEYLEN];
+	char val[MAXKEYS][KEYLEN];
+} inp_t;
+
+static void trim(char *s) {
+	size_t n = strlen(s);
+	while(n > 0 && isspace((unsigned char) s[n - 1])) s[--n] = '\0';
+	size_t b = 0;
+	while(s[b] && isspace((unsigned char) s[b])) b++;
+	if(b) memmove(s, s + b, strlen(s + b) + 1);
+}
+
+/* loadInput (parse_input.c:30-87): "key = value" lines, '#' comments, surrounding blanks trimmed */
+static int load_input(inp_t *in, const char *path) {
+	FILE *f = fopen(path, "r");
+	if(f == NULL) {
+		fprintf(stderr, "Input file not found\n");
+		return -1;
+	}
+	in->n = 0;
+	char line[4096];
+	while(fgets(line, sizeof(line), f)) {
+		trim(line);
+		if(line[0] == '\0' || line[0] == '#') continue;
+		char *eq = strchr(line, '=');
+		if(eq == NULL) {
+			fprintf(stderr, "WARNING: malformed line '%s'\n", line);
+			continue;
+		}
+		*eq = '\0';
+		if(in->n == MAXKEYS) break;
+		snprintf(in->key[in->n], KEYLEN, "%s", line);
+		snprintf(in->val[in->n], KEYLEN, "%s", eq + 1);
+		trim(in->key[in->n]);
+		trim(in->val[in->n]);
+		in->n++;
+	}
+	fclose(f);
+	return 0;
+}
+
+/* getInputKeyIndex (parse_input.c:89-104): first key with a non-empty value; missing mandatory -> exit(-1) */
+static const char *get(inp_t *in, const char *key, int mandatory) {
+	for(int i = 0; i < in->n; i++)
+		if(strcmp(in->key[i], key) == 0 && strlen(in->val[i]) > 0) return in->val[i];
+	if(mandatory) {
+		fprintf(stderr, "Mandatory key '%s' not found, exiting\n", key);
+		exit(-1);
+	}
+	return NULL;
+}
+
+static void die(const char *msg) {
+	fprintf(stderr, "%s\n", msg);
+	exit(1);
+}
+
+int main(int argc, char *argv[]) {
+	if(argc < 2) {
+		fprintf(stderr, "Usage is %s input\n", argv[0]);
+		return 1;
+	}
+	inp_t *in = calloc(1, sizeof(inp_t));
+	if(load_input(in, argv[1]) != 0) return 1;
+
+	/* output_init (output.c:19-109), the parts that Dynamics = 0 with NVT/NPT reads */
+	int restart = 1;
+	const char *v;
+	if((v = get(in, "Restart_step_counter", 0))) restart = atoi(v);
+	const char *mode = restart ? "w" : "a";
+	long long start_from = 0;
+	if(!restart) {
+		FILE *c = fopen(get(in, "Initial_conditions_file", 1), "r");
+		if(c == NULL || fscanf(c, "%lld", &start_from) != 1) die("Invalid initial configuration: the first value in the first row should be the time step of the configuration");
+		fclose(c);
+	}
+	long long print_every = atol(get(in, "Print_every", 1));
+	long long save_every = atol(get(in, "Save_every", 1));
+	const char *ename = (v = get(in, "Energy_file", 0)) ? v : "energy.dat";
+	const char *aname = (v = get(in, "Acceptance_file", 0)) ? v : "acceptance.dat";
+	FILE *fe = fopen(ename, mode), *fa = fopen(aname, mode), *fd = NULL;
+	if(fe == NULL || fa == NULL) die("output file not writable");
+	const char *folder = get(in, "Configuration_folder", 1);
+	if(access(folder, W_OK) != 0) die("Cannot create files in the configuration folder");
+	const char *last = (v = get(in, "Configuration_last", 0)) ? v : "last.rrr";
+	int ensemble = atoi(get(in, "Ensemble", 1));
+	if(ensemble != 0) {
+		const char *dname = (v = get(in, "Density_file", 0)) ? v : "density.dat";
+		fd = fopen(dname, mode);
+		if(fd == NULL) die("Density file not writable");
+	}
+
+	/* system_init (system.c:58-252), Dynamics = 0, NVT or NPT */
+	orc_params prm;
+	memset(&prm, 0, sizeof(prm));
+	int dynamics = atoi(get(in, "Dynamics", 1));
+	prm.ensemble = ensemble;
+	prm.disp_max = atof(get(in, "Disp_max", 1));
+	prm.theta_max = atof(get(in, "Theta_max", 1));
+	prm.T = atof(get(in, "Temperature", 1));
+	const char *conf = get(in, "Initial_conditions_file", 1);
+	if(!(v = get(in, "Seed", 0))) die("this driver needs an explicit Seed");
+	prm.seed = atoi(v);
+	prm.kf_delta = atof(get(in, "KF_delta", 1));
+	prm.kf_cosmax = atof(get(in, "KF_cosmax", 1));
+	if(ensemble == ORC_NPT) {
+		prm.rescale_factor_max = atof(get(in, "rescale_factor_max", 1));
+		prm.P = atof(get(in, "P", 1));
+	}
+	if(dynamics != 0 || (ensemble != ORC_NVT && ensemble != ORC_NPT)) die("only Dynamics = 0 with Ensemble 0 or 5 is restated");
+	char err[512];
+	orc_system *s = orc_load_rrr(conf, &prm, err, sizeof(err));
+	if(s == NULL) die(err);
+
+	/* initial energy and overlap check (main.c:55-64) */
+	int N = orc_N(s), ov;
+	double E0 = 0.;
+	for(int i = 0; i < N; i++) {
+		E0 += orc_particle_energy(s, i, &ov);
+		if(ov) die("Initial configuration contains an overlap, aborting");
+	}
+	orc_set_energy(s, 0.5 * E0);
+
+	long long steps = atol(get(in, "Steps", 1)) + start_from, step;
+	long long tries[ORC_N_MOVES], acc[ORC_N_MOVES];
+	char name[1100];
+	for(step = start_from; step < steps; step++) {
+		if(step % print_every == 0) { /* output_print (output.c:119-211) */
+			double energy = orc_get_energy(s);
+			double E = N > 0 ? energy / N : 0;
+			double V = orc_volume(s);
+			fprintf(fe, "%lld %lf\n", step, E);
+			fflush(fe);
+			if(ensemble != 0) {
+				fprintf(fd, "%lld %lf %d\n", step, N / V, N);
+				fflush(fd);
+			}
+			orc_counters(s, tries, acc);
+			fprintf(fa, "%lld", step);
+			fprintf(fa, " %e", acc[ORC_ROTO_TRASL] / (double) tries[ORC_ROTO_TRASL]);
+			if(ensemble == ORC_NPT) fprintf(fa, " %e", acc[ORC_VOLUME] / (double) tries[ORC_VOLUME]);
+			fprintf(fa, "\n");
+			fflush(fa);
+			orc_reset_counters(s);
+			printf("%lld %lf %lf", step, E, energy);
+			if(ensemble != 0) printf(" %lf", N / V);
+			printf("\n");
+			orc_save_rrr(s, step, last);
+			if(step != 0) {
+				int rc = orc_check_energy(s);
+				if(rc == -1) die("\nComputing energy from scratch resulted in an overlap, aborting");
+				if(rc == -2) die("\nEnergy check failed");
+			}
+		}
+		if(step > 0 && step % save_every == 0) {
+			snprintf(name, sizeof(name), "%s/conf_%lld.rrr", folder, step);
+			orc_save_rrr(s, step, name);
+			orc_save_rrr(s, step, last);
+		}
+		orc_sweep(s);
+	}
+	orc_save_rrr(s, step, last);
+	double energy = orc_get_energy(s);
+	printf("%lld %lf %lf", step, N > 0 ? energy / N : 0, energy);
+	if(ensemble != 0) printf(" %lf", N / orc_volume(s));
+	printf("\n");
+	fclose(fe);
+	fclose(fa);
+	if(fd) fclose(fd);
+	orc_free(s);
+	free(in);
+	return 0;
+}
