@@ -1,0 +1,356 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the roto-translation Monte Carlo hot path (Kern-Frenkel 4-patch, Dynamics = 0).
+
+Metric: MC move attempts per second. Default workload: N = 1,048,576 particles, NPT (T = 0.11, P = 0.05,
+rescale_factor_max = 0.01) from a seeded random insertion at rho = 0.3 with uniform orientations,
+KF_delta = 0.12, KF_cosmax = 0.92, Disp_max = 0.05, Theta_max = 0.1, FP32 pair tests with an FP64 guard
+band (eps = 1e-5), FP64 state. One step = one MC sweep: one checkerboard round (one attempt per non-empty cell) plus one NPT volume
+attempt.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload c5|c2|c4|c1]
+
+--impl gb300 (default) times the CUDA engine through its C-ABI; --impl reference times the reference's
+CPU implementation of the same path on the host cores (oracle/_ref when the reference was compiled on
+this machine, otherwise the oracle restatement of it, oracle/pp_oracle.c, which reproduces the reference
+trajectory bit for bit), one independent system per core.
+
+Under torchrun (N > 1) every rank runs an independent replica of the workload on its own GPU (the path
+does not shard; there is no collective in the data path); rank 0 prints the aggregate.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "MC move attempts/sec at N=1M (frac of HBM peak); eff. samples/sec learned vs plain"
+UNIT = "attempts/s"
+BYTES_PER_ATTEMPT = 192  # read + write of the FP64 canonical state r (24 B) + R (72 B) per attempt
+
+WORKLOADS = {
+    "c5": dict(N=1048576, rho=0.3, T=0.11, P=0.05, ensemble=5, rescale=0.01, disp=0.05, theta=0.1, seed=1005,
+               name="N=1048576 NPT rho0=0.3 T=0.11 P=0.05 rescale_factor_max=0.01, plain roto-translation, FP32+guard"),
+    "c2": dict(N=32768, rho=0.5, T=0.13, P=0.0, ensemble=0, rescale=0.01, disp=0.05, theta=0.1, seed=1002,
+               name="N=32768 NVT rho=0.5 T=0.13, FP32+guard"),
+    "c4": dict(N=32768, rho=0.1, T=0.09, P=0.0, ensemble=0, rescale=0.01, disp=0.05, theta=0.1, seed=1004,
+               name="N=32768 NVT rho=0.1 T=0.09, plain proposal, FP32+guard"),
+    "c1": dict(N=1000, rho=0.1, T=0.12, P=0.0, ensemble=0, rescale=0.01, disp=0.05, theta=0.1, seed=1001,
+               name="N=1000 NVT rho=0.1 T=0.12, FP32+guard"),
+}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        try:
+            d = json.load(open(p))
+            return float(d["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(workload):
+    """DRAM bytes per launch of the sweep kernel from the committed ncu summary, if one exists."""
+    p = os.path.join(ROOT, "profiles", "k_colour_%s.txt" % workload)
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_launch_full_size"):
+            try:
+                return float(line.split("=")[1].split()[0])
+            except Exception:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.out = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.out.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+        return ws, rank, local, dist
+    return 1, 0, 0, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def allreduce(dist, value, op):
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64)
+    dist.all_reduce(t, op=op)
+    return float(t.item())
+
+
+def make_config(wl, seed_offset=0):
+    import patchyparticles_gb300 as pp
+
+    return pp.generate(wl["N"], wl["rho"], wl["seed"] + seed_offset, round_like_file=False)
+
+
+def cpu_reference_impl():
+    """Which CPU implementation is timed: the reference compiled here, or the oracle restatement."""
+    return "port"
+
+
+def cpu_throughput(wl, r, R, box, seconds, threads, samples=1):
+    from oracle import pyoracle as po
+
+    po.build(with_reference=False)
+    prm = po.params(ensemble=wl["ensemble"], T=wl["T"], P=wl["P"], disp_max=wl["disp"], theta_max=wl["theta"],
+                    rescale_factor_max=wl["rescale"], seed=wl["seed"])
+    pool = po.Pool(r, R, box, prm, threads)
+    tot_att, tot_t = 0, 0.0
+    for _ in range(samples):
+        t0 = time.perf_counter()
+        _, att = pool.run(seconds)
+        tot_t += time.perf_counter() - t0
+        tot_att += att
+    pool.close()
+    return tot_att / tot_t, tot_att, tot_t
+
+
+def run_reference(args, wl, ws, rank, dist):
+    if rank != 0:
+        return
+    r, R, box = make_config(wl)
+    threads = os.cpu_count() or 1
+    total = args.steps + args.warmup
+    per = max(0.2, min(2.0, 20.0 / max(1, total)))
+    from oracle import pyoracle as po
+
+    po.build(with_reference=False)
+    prm = po.params(ensemble=wl["ensemble"], T=wl["T"], P=wl["P"], disp_max=wl["disp"], theta_max=wl["theta"],
+                    rescale_factor_max=wl["rescale"], seed=wl["seed"])
+    pool = po.Pool(r, R, box, prm, threads)
+    for _ in range(args.warmup):
+        pool.run(per)
+    att, el = 0, 0.0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        _, a = pool.run(per)
+        el += time.perf_counter() - t0
+        att += a
+    pool.close()
+    value = att / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * el / max(1, args.steps), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random insertion)",
+        "config": {"workload": wl["name"], "N": wl["N"], "sample": "%.2f s of all-core MC per step" % per},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": cpu_reference_impl(),
+                         "sample": "%d independent %d-particle systems, %d x %.2f s" % (threads, wl["N"], args.steps, per)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, wl, ws, rank, local, dist):
+    import patchyparticles_gb300 as pp
+    from patchyparticles_gb300 import build
+
+    if rank == 0 or ws == 1:
+        build.build()
+    barrier(dist)
+    pp.select_device(local)
+    r, R, box = make_config(wl, seed_offset=rank)
+    prm = pp.default_params(ensemble=wl["ensemble"], temperature=wl["T"], pressure=wl["P"], disp_max=wl["disp"],
+                            theta_max=wl["theta"], rescale_factor_max=wl["rescale"], seed=wl["seed"] + rank)
+    e = pp.Engine(prm)
+    e.upload(r, R, box)
+    spsw = args.sweeps_per_step
+    # warm-up
+    for _ in range(args.warmup):
+        e.sweeps(spsw)
+    e.sync()
+    e.counters(reset=True)
+    e.set_timing(True)
+    e.kernel_stats(reset=True)
+    launches0 = e.launch_count()
+    sampler = ClockSampler(local)
+    barrier(dist)
+    e.sync()
+    sampler.start()
+    ms = e.time_sweeps(args.steps * spsw)  # CUDA events on the engine's stream around the K steps
+    clocks = sampler.stop()
+    barrier(dist)
+    launches = e.launch_count() - launches0
+    tries, acc = e.counters()
+    ks = e.kernel_stats()
+    e.set_timing(False)
+    attempts = tries[pp.MOVE_ROTO_TRASL] + tries[pp.MOVE_VOLUME]
+    t_max = allreduce(dist, ms / 1000.0, _max_op(dist))
+    att_sum = allreduce(dist, attempts, _sum_op(dist))
+    value = att_sum / t_max
+
+    # roofline of the dominant kernel: k_colour (the 8 checkerboard colour launches of a round are timed as one
+    # event group on the engine stream), 192 B per attempt
+    peak, peak_kind = measured_peaks()
+    sweep_launches = max(1, ks["sweep_launches"])
+    avg_ms = ks["sweep_ms"] / sweep_launches
+    att_per_launch = tries[pp.MOVE_ROTO_TRASL] / sweep_launches
+    achieved = att_per_launch * BYTES_PER_ATTEMPT / (avg_ms / 1000.0) / 1e9
+    traffic = profiled_traffic(args.workload)
+
+    # end to end through the C-ABI with host buffers: upload (H2D) + sweeps + download (D2H) per step
+    e2e = None
+    if not args.no_e2e:
+        r_h, R_h, b_h = e.download()
+        e2e_steps = args.e2e_steps
+        att_e2e = 0
+        barrier(dist)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            e.upload(r_h, R_h, b_h)
+            e.counters(reset=True)
+            e.sweeps(args.e2e_sweeps)
+            r_h, R_h, b_h = e.download()
+            _ = e.tracked_energy()
+            t, _a = e.counters()
+            att_e2e += t[pp.MOVE_ROTO_TRASL] + t[pp.MOVE_VOLUME]
+        el = time.perf_counter() - t0
+        el = allreduce(dist, el, _max_op(dist))
+        att_e2e = allreduce(dist, att_e2e, _sum_op(dist))
+        N = wl["N"]
+        e2e = {"value": att_e2e / el, "unit": UNIT, "h2d_bytes_per_step": N * (96 + 4), "d2h_bytes_per_step": N * (96 + 4),
+               "sweeps_per_step": args.e2e_sweeps, "steps": e2e_steps}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, a, t = cpu_throughput(wl, r, R, box, args.cpu_seconds, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": cpu_reference_impl(),
+               "sample": "%d independent %d-particle systems for %.1f s (%d attempts)" % (threads, wl["N"], t, a)}
+    e.close()
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * t_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64", "data": "synthetic (seeded random insertion, uniform orientations)",
+        "config": {"workload": wl["name"], "N": wl["N"], "sweeps_per_step": spsw, "proposal": "plain",
+                   "l2": "inputs larger than L2 (FP64 state %.0f MB + FP32 mirror %.0f MB per GPU)" % (wl["N"] * 96 / 1e6, wl["N"] * 64 / 1e6),
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "acceptance": acc[pp.MOVE_ROTO_TRASL] / max(1, tries[pp.MOVE_ROTO_TRASL]),
+        "volume_acceptance": acc[pp.MOVE_VOLUME] / max(1, tries[pp.MOVE_VOLUME]) if tries[pp.MOVE_VOLUME] else None,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "kernel": "k_colour (8 launches per round, one event group)", "peak_source": peak_kind,
+                     "bytes_per_attempt": BYTES_PER_ATTEMPT, "avg_launch_ms": avg_ms, "attempts_per_launch": att_per_launch},
+        "kernel_ms_per_step": {"sort": ks["sort_ms"] / max(1, ks["sort_launches"]), "sweep": avg_ms,
+                               "volume": ks["volume_ms"] / max(1, ks["volume_launches"]) if ks["volume_launches"] else 0.0},
+        "clocks": clocks,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def _max_op(dist):
+    if dist is None:
+        return None
+    return dist.ReduceOp.MAX
+
+
+def _sum_op(dist):
+    if dist is None:
+        return None
+    return dist.ReduceOp.SUM
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="c5", choices=sorted(WORKLOADS))
+    ap.add_argument("--sweeps-per-step", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-sweeps", type=int, default=10)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    wl = WORKLOADS[args.workload]
+    ws, rank, local, dist = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, wl, ws, rank, dist)
+    else:
+        run_gpu(args, wl, ws, rank, local, dist)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

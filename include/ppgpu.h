@@ -1,0 +1,193 @@
+/*
+ * ppgpu.h -- C-ABI of the GB300 roto-translation Monte Carlo engine for Kern-Frenkel four-patch hard
+ * spheres (PatchyParticles, Dynamics = 0, NVT and NPT).
+ *
+ * The boundary is the reference's per-step ensemble hook: `System::do_ensemble` (defs.h:78), selected by
+ * MC_init (MC.c:85-131) and called once per MC step from the driver loop (main.c:119). One engine call
+ * `pp_gpu_sweeps(e, n)` replaces n calls of do_NVT (MC.c:19-29) or do_NPT (MC.c:60-68) with
+ * MC_move_rototranslate (MC.c:311-340) as do_dynamics. Host <-> device traffic happens only where the
+ * reference driver needs host state: the print/save cadence (main.c:82-104, output.c:119-211).
+ *
+ * Plain C types only: no CUDA or torch types cross this boundary. Every function returns PP_OK (0) or a
+ * negative PP_ERR_* code and never exits the process; pp_gpu_last_error gives the message. The
+ * reference's fatal paths (output_exit, output.c:374-388) become these codes; the command-line driver
+ * maps them back to exit(1).
+ *
+ * Particle state crosses the boundary as the reference stores it (defs.h:47-56): positions r as N x 3
+ * doubles (unwrapped, as MC_rototraslate_particle leaves them, MC.c:213-215) and orientations R as N x 9
+ * doubles, row-major, rows = the three rows of PatchyParticle::orientation.
+ */
+#ifndef PPGPU_H_
+#define PPGPU_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status codes */
+#define PP_OK 0
+#define PP_ERR_ARG -1      /* invalid argument or parameter */
+#define PP_ERR_CUDA -2     /* CUDA runtime failure (message carries the CUDA error string) */
+#define PP_ERR_OVERLAP -3  /* configuration contains an overlap (main.c:57-60, MC.c:778) */
+#define PP_ERR_CAPACITY -4 /* a device-side capacity was exceeded (tile particle capacity, cell grid) */
+#define PP_ERR_IO -5       /* file unreadable / malformed (system.c:77-81, 245) */
+#define PP_ERR_STATE -6    /* call order violated (e.g. sweeps before upload) */
+#define PP_ERR_DRIFT -7    /* energy check failed: relative drift > 1e-5 (MC.c:779-781) */
+
+/* ------------------------------------------------------------------ constants shared with the reference */
+#define PP_NVT 0 /* Ensemble = 0 (defs.h:21) */
+#define PP_NPT 5 /* Ensemble = 5 (defs.h:24) */
+
+#define PP_MOVE_ROTO_TRASL 0 /* tries/accepted slots as System::tries/accepted (defs.h:11-19, 95-96) */
+#define PP_MOVE_VOLUME 6
+#define PP_N_MOVES 8
+
+#define PP_PREC_FP32_GUARD 0 /* FP32 pair tests, FP64 re-evaluation inside the guard band (default) */
+#define PP_PREC_FP64 1       /* every pair test in FP64 with the reference's operation order */
+
+typedef struct pp_params {
+	int ensemble;              /* Ensemble (system.c:62): PP_NVT or PP_NPT */
+	double temperature;        /* Temperature (system.c:66) */
+	double pressure;           /* P (system.c:168), NPT only */
+	double disp_max;           /* Disp_max (system.c:64): translation drawn uniformly in [-Disp_max/2, Disp_max/2)^3 */
+	double theta_max;          /* Theta_max (system.c:65): rotation angle uniform in [0, Theta_max) */
+	double rescale_factor_max; /* rescale_factor_max (system.c:167), NPT only */
+	double kf_delta;           /* KF_delta (system.c:83) */
+	double kf_cosmax;          /* KF_cosmax (system.c:84) */
+	uint64_t seed;             /* Seed (system.c:71): keys the counter-based Philox4x32-10 streams */
+	int precision;             /* PP_PREC_FP32_GUARD or PP_PREC_FP64 */
+	double guard_eps;          /* guard half-width on r^2 and on patch cosines; <= 0 selects 1e-5 */
+	int resort_every;          /* checkerboard rounds between cell-grid re-sorts from the FP64 state; 0 = 4 */
+	int audit;                 /* nonzero: re-check every FP32 decision in FP64 and count mismatches */
+} pp_params;
+
+typedef struct pp_counters {
+	long long tries[PP_N_MOVES];    /* System::tries (defs.h:95) */
+	long long accepted[PP_N_MOVES]; /* System::accepted (defs.h:96) */
+} pp_counters;
+
+typedef struct pp_guard_stats {
+	long long pairs;       /* pair tests performed by the FP32 path */
+	long long fallbacks;   /* pairs inside the guard band, re-evaluated in FP64 */
+	long long mismatches;  /* audit mode: FP32 decisions outside the band that FP64 contradicts (must be 0) */
+	double max_err_r2;     /* audit mode: largest |r^2_fp32 - r^2_fp64| seen */
+	double max_err_cos;    /* audit mode: largest |cos_fp32 - cos_fp64| seen */
+} pp_guard_stats;
+
+typedef struct pp_engine pp_engine;
+
+/* Fills *p with the reference defaults this engine assumes (NVT, FP32 + guard band, eps = 1e-5). */
+void pp_default_params(pp_params *p);
+
+/* Creates an engine for one system (replaces System setup for the MC step, system_init/MC_init,
+ * system.c:58-252 and MC.c:85-131). */
+int pp_gpu_create(const pp_params *prm, pp_engine **out);
+
+/* Creates an engine holding n_replicas independent systems that every sweep call advances together
+ * (the batched-replica layout; no reference counterpart beyond running n copies of the reference). */
+int pp_gpu_create_batch(const pp_params *prms, int n_replicas, pp_engine **out);
+
+/* Copies one system's state to the device (the System the reference builds in system_init,
+ * system.c:213-251, plus the initial energy and overlap check of main.c:55-64: returns PP_ERR_OVERLAP
+ * if the configuration contains an overlap). r: N x 3, R: N x 9 row-major, box: Lx Ly Lz. */
+int pp_gpu_upload(pp_engine *e, int N, const double *r, const double *R, const double box[3]);
+int pp_gpu_upload_replica(pp_engine *e, int replica, int N, const double *r, const double *R, const double box[3]);
+
+/* Enqueues n MC steps (sweeps) for every replica: n calls of do_NVT (MC.c:19-29) / do_NPT (MC.c:60-68).
+ * Asynchronous: returns once the work is queued; pp_gpu_sync waits for it and reports device errors. */
+int pp_gpu_sweeps(pp_engine *e, long long n);
+int pp_gpu_sync(pp_engine *e);
+
+/* Tracked total energy of a replica (System::energy, updated by every accepted move, MC.c:333,501). */
+int pp_gpu_get_energy(pp_engine *e, int replica, double *E);
+
+/* Energy recomputed from scratch: 0.5 * sum_i MC_energy(i) (main.c:55-64); *overlap = 1 if any pair overlaps. */
+int pp_gpu_energy(pp_engine *e, int replica, double *E, int *overlap);
+
+/* MC_check_energy (MC.c:766-784): recompute from scratch, re-orthonormalise every orientation with
+ * gram_schmidt (MC.c:774), fail with PP_ERR_OVERLAP / PP_ERR_DRIFT as the reference aborts, and
+ * replace the tracked energy with the recomputed one. */
+int pp_gpu_check_energy(pp_engine *e, int replica);
+
+/* gram_schmidt on every orientation (MC.c:774, utils.c:91-113), bit-identical to the reference's. */
+int pp_gpu_orthonormalise(pp_engine *e, int replica);
+
+/* Acceptance counters (System::tries / accepted, defs.h:95-96); reset = 1 clears them afterwards as
+ * output_print does (output.c:189). */
+int pp_gpu_counters(pp_engine *e, int replica, pp_counters *out, int reset);
+
+/* Copies a replica's state back: r (N x 3), R (N x 9), box, in the particle order of the upload. */
+int pp_gpu_download(pp_engine *e, double *r, double *R, double box[3]);
+int pp_gpu_download_replica(pp_engine *e, int replica, double *r, double *R, double box[3]);
+
+/* Per-particle bond and overlap counts over all partners (the per-particle results of
+ * output_print_bonds, output.c:213-268), in upload order. Either pointer may be NULL. */
+int pp_gpu_bonds(pp_engine *e, int replica, int *n_bonds, int *n_overlaps);
+
+/* Bonded partner lists in upload order: offsets has N+1 entries, partners capacity `cap`.
+ * Returns the total number of entries (sum of n_bonds) or a negative error (PP_ERR_CAPACITY if cap is short).
+ * Partners of each particle are sorted ascending (output_print_bonds lists them in cell-walk order). */
+int pp_gpu_bond_lists(pp_engine *e, int replica, int *offsets, int *partners, int cap);
+
+/* Guard-band statistics accumulated since the last call (reset = 1 clears them). */
+int pp_gpu_guard_stats(pp_engine *e, pp_guard_stats *out, int reset);
+
+/* Per-group device times collected with CUDA events on the engine's stream (pp_gpu_set_timing). */
+typedef struct pp_kernel_stats {
+	double sweep_ms;          /* tile sweep kernel (the checkerboard moves) */
+	long long sweep_launches;
+	double sort_ms;           /* grid plan + cell assignment + bin scan + scatter */
+	long long sort_launches;  /* number of timed sort groups */
+	double volume_ms;         /* NPT: candidate-box energy, acceptance, rescale */
+	long long volume_launches;
+} pp_kernel_stats;
+
+/* Selects the CUDA device used by engines created afterwards in this thread (one process per GPU). */
+int pp_gpu_select_device(int device);
+
+/* Enables (1) or disables (0) per-group event timing of every following sweep. */
+int pp_gpu_set_timing(pp_engine *e, int enable);
+int pp_gpu_kernel_stats(pp_engine *e, pp_kernel_stats *out, int reset);
+
+/* Enqueues n sweeps between two CUDA events recorded on the engine's stream, waits, and returns the
+ * elapsed device time in *ms. */
+int pp_gpu_time_sweeps(pp_engine *e, long long n, double *ms);
+
+/* Number of replicas, particles of a replica, current box of a replica. */
+int pp_gpu_num_replicas(const pp_engine *e);
+int pp_gpu_num_particles(const pp_engine *e, int replica);
+int pp_gpu_box(pp_engine *e, int replica, double box[3]);
+
+/* Number of kernel launches the engine has enqueued since creation (its own kernels only). */
+long long pp_gpu_launch_count(const pp_engine *e);
+
+const char *pp_gpu_last_error(const pp_engine *e);
+void pp_gpu_destroy(pp_engine *e);
+
+/* ------------------------------------------------------------------ reference file formats (host only) */
+/* .rrr header "step N Lx Ly Lz" (system.c:80; output.c:306). Returns PP_OK or PP_ERR_IO. */
+int pp_rrr_header(const char *path, long long *step, int *N, double box[3]);
+
+/* Reads a .rrr configuration exactly as system_init does (system.c:213-243): each particle's two stored
+ * orientation rows are normalised, the third row is their cross product and the matrix is passed through
+ * gram_schmidt, so R is bit-identical to the reference's. r: N x 3, R: N x 9. */
+int pp_rrr_read(const char *path, int N, double *r, double *R, double box[3], char *err, int err_len);
+
+/* Writes a .rrr configuration in output_save's format (output.c:302-317). */
+int pp_rrr_write(const char *path, long long step, int N, const double *r, const double *R, const double box[3]);
+
+/* Seeded random sequential insertion of N non-overlapping unit spheres at the given density in a cubic box,
+ * with uniformly random orientations: the algorithm of the reference generator (generator.c:43-68,
+ * 86-124; random_orientation, utils.c:133-169), drawing from the drand48 recurrence seeded as
+ * srand48(seed). Returns PP_ERR_ARG for density > 0.7 (generator.c:99-102). If round_like_file is
+ * nonzero, orientations pass through the same "%lf" text rounding and re-orthonormalisation that writing
+ * and reading a .rrr file applies, so the result equals loading the generator's file. */
+int pp_generate(int N, double density, int seed, int round_like_file, double *r, double *R, double box[3]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PPGPU_H_ */

@@ -693,3 +693,102 @@ double orc_parallel_throughput(int N, const double *r, const double *R, const do
 	if(attempts_out) *attempts_out = total;
 	return rate;
 }
+
+/* ---------------------------------------------------------------- persistent pool */
+struct orc_pool {
+	int threads;
+	orc_system **sys;
+	double seconds;
+	long long *att;
+	double *el;
+};
+
+typedef struct {
+	orc_pool *pool;
+	int t;
+} o_pool_arg;
+
+static void *o_pool_init(void *arg) {
+	o_pool_arg *a = arg;
+	orc_system *s = a->pool->sys[a->t];
+	int ov = 0;
+	double E = 0.;
+	for(int i = 0; i < s->N && !ov; i++) E += orc_particle_energy(s, i, &ov);
+	s->energy = 0.5 * E;
+	return NULL;
+}
+
+static void *o_pool_work(void *arg) {
+	o_pool_arg *a = arg;
+	orc_system *s = a->pool->sys[a->t];
+	double t0 = o_now();
+	long long n = 0;
+	const int chunk = 4096;
+	do {
+		for(int k = 0; k < chunk; k++) o_attempt(s);
+		n += chunk;
+	} while(o_now() - t0 < a->pool->seconds);
+	a->pool->el[a->t] = o_now() - t0;
+	a->pool->att[a->t] = n;
+	return NULL;
+}
+
+orc_pool *orc_pool_create(int N, const double *r, const double *R, const double box[3], const orc_params *prm, int threads) {
+	if(threads < 1) threads = 1;
+	orc_pool *p = calloc(1, sizeof(orc_pool));
+	p->threads = threads;
+	p->sys = calloc(threads, sizeof(orc_system *));
+	p->att = calloc(threads, sizeof(long long));
+	p->el = calloc(threads, sizeof(double));
+	for(int t = 0; t < threads; t++) {
+		orc_params q = *prm;
+		q.seed = prm->seed + t;
+		p->sys[t] = orc_from_arrays(N, r, R, box, &q);
+		if(p->sys[t] == NULL) {
+			orc_pool_free(p);
+			return NULL;
+		}
+	}
+	pthread_t *tid = calloc(threads, sizeof(pthread_t));
+	o_pool_arg *args = calloc(threads, sizeof(o_pool_arg));
+	for(int t = 0; t < threads; t++) {
+		args[t].pool = p;
+		args[t].t = t;
+		pthread_create(&tid[t], NULL, o_pool_init, &args[t]);
+	}
+	for(int t = 0; t < threads; t++) pthread_join(tid[t], NULL);
+	free(tid);
+	free(args);
+	return p;
+}
+
+double orc_pool_run(orc_pool *p, double seconds, long long *attempts_out) {
+	p->seconds = seconds;
+	pthread_t *tid = calloc(p->threads, sizeof(pthread_t));
+	o_pool_arg *args = calloc(p->threads, sizeof(o_pool_arg));
+	for(int t = 0; t < p->threads; t++) {
+		args[t].pool = p;
+		args[t].t = t;
+		pthread_create(&tid[t], NULL, o_pool_work, &args[t]);
+	}
+	double rate = 0.;
+	long long tot = 0;
+	for(int t = 0; t < p->threads; t++) {
+		pthread_join(tid[t], NULL);
+		if(p->el[t] > 0) rate += p->att[t] / p->el[t];
+		tot += p->att[t];
+	}
+	free(tid);
+	free(args);
+	if(attempts_out) *attempts_out = tot;
+	return rate;
+}
+
+void orc_pool_free(orc_pool *p) {
+	if(p == NULL) return;
+	for(int t = 0; t < p->threads; t++) orc_free(p->sys[t]);
+	free(p->sys);
+	free(p->att);
+	free(p->el);
+	free(p);
+}

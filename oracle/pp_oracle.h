@@ -92,6 +92,14 @@ void orc_drand48_sequence(int seed, int n, double *out);
 double orc_parallel_throughput(int N, const double *r, const double *R, const double box[3], const orc_params *prm,
 		int threads, double seconds, long long *attempts_out);
 
+/* Persistent pool for repeated bounded samples: `threads` independent clones (seeds seed+t), initial
+ * energy computed once; each orc_pool_run lets every clone continue for `seconds` and returns the
+ * aggregate attempts per second of that interval. */
+typedef struct orc_pool orc_pool;
+orc_pool *orc_pool_create(int N, const double *r, const double *R, const double box[3], const orc_params *prm, int threads);
+double orc_pool_run(orc_pool *pool, double seconds, long long *attempts_out);
+void orc_pool_free(orc_pool *pool);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,1134 @@
+/*
+ * ppgpu_host.c -- C host side of the engine behind include/ppgpu.h: engine lifecycle, state upload /
+ * download, the per-sweep launch sequence, energy checks, and the reference file formats (.rrr reader
+ * and writer, seeded initial-configuration generator).
+ *
+ * Compiled with -ffp-contract=off: the .rrr reader must produce orientations bit-identical to the
+ * reference's system_init (system.c:213-243), and the generator must reproduce generator.c.
+ */
+#define _GNU_SOURCE
+#include "ppgpu.h"
+#include "ppgpu_internal.h"
+
+#include <cuda_runtime_api.h>
+#include <float.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+struct pp_engine {
+	int nrep;
+	pp_params *prm;
+	/* host-side staging of uploads until the device layout exists */
+	int *N;
+	double **h_r, **h_R;
+	double (*h_box)[3];
+	int *uploaded;
+	int committed;
+	/* device */
+	ppi_dev d;
+	ppi_rparams *h_rp;
+	ppi_rstate *h_rs;
+	int ntot_alloc;
+	cudaStream_t stream;
+	int threads;
+	long long sweep_counter;
+	long long round_counter;
+	long long epoch;
+	long long launches;
+	int resort_every;     /* rounds between cell-grid re-sorts (new random shift, records rebuilt from FP64) */
+	int rounds_per_sweep; /* checkerboard rounds per MC step */
+	int reorder_every;    /* re-sorts between physical reorders of the FP64 state */
+	int any_npt;
+	/* event timing */
+	int timing;
+	int n_ev;
+	cudaEvent_t *ev;   /* groups of 2 events: start, stop */
+	int *ev_kind;      /* 0 sort, 1 sweep, 2 volume */
+	int ev_cap;
+	pp_kernel_stats kstats;
+	/* pinned staging */
+	double *pin_rec;
+	int *pin_id;
+	int *pin_i1, *pin_i2;
+	size_t pin_n;
+	char err[512];
+};
+
+static int set_err(pp_engine *e, int code, const char *fmt, ...) {
+	if(e) {
+		va_list ap;
+		va_start(ap, fmt);
+		vsnprintf(e->err, sizeof(e->err), fmt, ap);
+		va_end(ap);
+	}
+	return code;
+}
+
+#define CU(call)                                                                                        \
+	do {                                                                                                \
+		cudaError_t _c = (call);                                                                        \
+		if(_c != cudaSuccess) return set_err(e, PP_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(_c)); \
+	} while(0)
+
+#define CK(rc)                                                                                            \
+	do {                                                                                                  \
+		int _c = (rc);                                                                                    \
+		if(_c != 0) return set_err(e, PP_ERR_CUDA, "kernel launch: %s", cudaGetErrorString((cudaError_t) _c)); \
+	} while(0)
+
+/* ------------------------------------------------------------------------------------------------ */
+/* small vector helpers with the reference's operation order (utils.c)                              */
+/* ------------------------------------------------------------------------------------------------ */
+#define H_SCALAR(x, y) ((x)[0] * (y)[0] + (x)[1] * (y)[1] + (x)[2] * (y)[2])
+
+static void h_normalize(double *v) { /* utils.c:31-36 */
+	double norm = sqrt(H_SCALAR(v, v));
+	v[0] /= norm;
+	v[1] /= norm;
+	v[2] /= norm;
+}
+
+static void h_cross(const double *a, const double *b, double *r) { /* utils.c:25-29 */
+	r[0] = a[1] * b[2] - a[2] * b[1];
+	r[1] = a[2] * b[0] - a[0] * b[2];
+	r[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+static void h_gram_schmidt(double *v1, double *v2, double *v3) { /* utils.c:91-113 */
+	double v1n = H_SCALAR(v1, v1);
+	double b1 = H_SCALAR(v2, v1) / v1n;
+	for(int k = 0; k < 3; k++) v2[k] -= b1 * v1[k];
+	double v3v1 = H_SCALAR(v3, v1), v3v2 = H_SCALAR(v3, v2), v2n = H_SCALAR(v2, v2);
+	b1 = v3v1 / v1n;
+	double b2 = v3v2 / v2n;
+	for(int k = 0; k < 3; k++) v3[k] -= b1 * v1[k] + b2 * v2[k];
+	h_normalize(v1);
+	h_normalize(v2);
+	h_normalize(v3);
+}
+
+static void h_base_patches(double base[4][3]) { /* system.c:20-31 */
+	double h = 0.5 / sqrt(3.);
+	double v[4][3] = { { -h, -h, h }, { h, -h, -h }, { h, h, h }, { -h, h, -h } };
+	for(int i = 0; i < 4; i++) {
+		h_normalize(v[i]);
+		memcpy(base[i], v[i], sizeof(v[i]));
+	}
+}
+
+/* ------------------------------------------------------------------------------------------------ */
+/* parameters                                                                                       */
+/* ------------------------------------------------------------------------------------------------ */
+void pp_default_params(pp_params *p) {
+	memset(p, 0, sizeof(*p));
+	p->ensemble = PP_NVT;
+	p->temperature = 0.12;
+	p->pressure = 0.;
+	p->disp_max = 0.05;
+	p->theta_max = 0.1;
+	p->rescale_factor_max = 0.01;
+	p->kf_delta = 0.12;
+	p->kf_cosmax = 0.92;
+	p->seed = 1;
+	p->precision = PP_PREC_FP32_GUARD;
+	p->guard_eps = 1e-5;
+	p->resort_every = 0;
+	p->audit = 0;
+}
+
+static int check_params(pp_engine *e, const pp_params *p) {
+	if(p->ensemble != PP_NVT && p->ensemble != PP_NPT) return set_err(e, PP_ERR_ARG, "Ensemble %d not supported (0 = NVT, 5 = NPT)", p->ensemble);
+	if(!(p->temperature > 0.)) return set_err(e, PP_ERR_ARG, "Temperature must be > 0");
+	if(!(p->disp_max >= 0.) || !(p->theta_max >= 0.)) return set_err(e, PP_ERR_ARG, "Disp_max and Theta_max must be >= 0");
+	if(!(p->kf_delta > 0.) || !(p->kf_delta < 1.)) return set_err(e, PP_ERR_ARG, "KF_delta must lie in (0, 1)");
+	if(!(p->kf_cosmax > -1.) || !(p->kf_cosmax < 1.)) return set_err(e, PP_ERR_ARG, "KF_cosmax must lie in (-1, 1)");
+	if(p->precision != PP_PREC_FP32_GUARD && p->precision != PP_PREC_FP64) return set_err(e, PP_ERR_ARG, "unknown precision %d", p->precision);
+	if(p->guard_eps > 1e-2) return set_err(e, PP_ERR_ARG, "guard_eps too large");
+	if(p->resort_every < 0 || p->resort_every > 64) return set_err(e, PP_ERR_ARG, "resort_every (re-sort period in rounds) must be 0 or in [1, 64]");
+	if(p->ensemble == PP_NPT && !(p->rescale_factor_max > 0. && p->rescale_factor_max < 1.)) return set_err(e, PP_ERR_ARG, "rescale_factor_max must lie in (0, 1)");
+	return PP_OK;
+}
+
+static int create_common(const pp_params *prms, int n, pp_engine **out) {
+	*out = NULL;
+	if(n < 1 || prms == NULL) return PP_ERR_ARG;
+	pp_engine *e = calloc(1, sizeof(pp_engine));
+	if(e == NULL) return PP_ERR_ARG;
+	for(int i = 0; i < n; i++) {
+		int rc = check_params(e, prms + i);
+		if(rc != PP_OK) {
+			*out = e; /* let the caller read the message */
+			e->nrep = 0;
+			return rc;
+		}
+	}
+	e->nrep = n;
+	e->prm = calloc(n, sizeof(pp_params));
+	memcpy(e->prm, prms, sizeof(pp_params) * n);
+	e->N = calloc(n, sizeof(int));
+	e->h_r = calloc(n, sizeof(double *));
+	e->h_R = calloc(n, sizeof(double *));
+	e->h_box = calloc(n, sizeof(double[3]));
+	e->uploaded = calloc(n, sizeof(int));
+	e->threads = 128;
+	e->resort_every = 4;
+	e->rounds_per_sweep = 1;
+	e->reorder_every = 16;
+	for(int i = 0; i < n; i++) {
+		if(e->prm[i].guard_eps <= 0.) e->prm[i].guard_eps = 1e-5;
+		if(e->prm[i].ensemble == PP_NPT) e->any_npt = 1;
+	}
+	if(e->prm[0].resort_every > 0) e->resort_every = e->prm[0].resort_every;
+	cudaError_t c = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
+	*out = e;
+	if(c != cudaSuccess) return set_err(e, PP_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(c));
+	return PP_OK;
+}
+
+int pp_gpu_create(const pp_params *prm, pp_engine **out) { return create_common(prm, 1, out); }
+int pp_gpu_create_batch(const pp_params *prms, int n, pp_engine **out) { return create_common(prms, n, out); }
+
+const char *pp_gpu_last_error(const pp_engine *e) { return e ? e->err : "no engine"; }
+int pp_gpu_num_replicas(const pp_engine *e) { return e ? e->nrep : 0; }
+int pp_gpu_num_particles(const pp_engine *e, int r) { return (e && r >= 0 && r < e->nrep) ? e->N[r] : -1; }
+long long pp_gpu_launch_count(const pp_engine *e) { return e ? e->launches : 0; }
+
+static void free_device(pp_engine *e) {
+	void **ptrs[] = { (void **) &e->d.rec, (void **) &e->d.srec, (void **) &e->d.id, (void **) &e->d.rep, (void **) &e->d.cellof,
+		(void **) &e->d.cell_count, (void **) &e->d.cell_start, (void **) &e->d.cell_cursor, (void **) &e->d.cell_rep, (void **) &e->d.scan_aux,
+		(void **) &e->d.clist, (void **) &e->d.ccount, (void **) &e->d.rp, (void **) &e->d.rs, (void **) &e->d.grid, (void **) &e->d.out_bonds,
+		(void **) &e->d.out_overlaps, (void **) &e->d.out_partners, (void **) &e->d.tmp_rec, (void **) &e->d.tmp_id };
+	for(size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); i++) {
+		if(*ptrs[i]) cudaFree(*ptrs[i]);
+		*ptrs[i] = NULL;
+	}
+	if(e->pin_rec) cudaFreeHost(e->pin_rec);
+	if(e->pin_id) cudaFreeHost(e->pin_id);
+	if(e->pin_i1) cudaFreeHost(e->pin_i1);
+	if(e->pin_i2) cudaFreeHost(e->pin_i2);
+	e->pin_rec = NULL;
+	e->pin_id = e->pin_i1 = e->pin_i2 = NULL;
+	e->pin_n = 0;
+}
+
+void pp_gpu_destroy(pp_engine *e) {
+	if(e == NULL) return;
+	if(e->stream) cudaStreamSynchronize(e->stream);
+	free_device(e);
+	if(e->stream) cudaStreamDestroy(e->stream);
+	for(int i = 0; i < e->nrep; i++) {
+		free(e->h_r[i]);
+		free(e->h_R[i]);
+	}
+	free(e->h_r);
+	free(e->h_R);
+	free(e->h_box);
+	free(e->uploaded);
+	free(e->N);
+	free(e->prm);
+	free(e->h_rp);
+	free(e->h_rs);
+	if(e->ev) {
+		for(int i = 0; i < 2 * e->ev_cap; i++) cudaEventDestroy(e->ev[i]);
+		free(e->ev);
+		free(e->ev_kind);
+	}
+	free(e);
+}
+
+/* ------------------------------------------------------------------------------------------------ */
+/* layout                                                                                           */
+/* ------------------------------------------------------------------------------------------------ */
+/* fills per-replica derived parameters; returns PP_OK or an error */
+static int derive_rparams(pp_engine *e, int r, ppi_rparams *rp) {
+	const pp_params *p = e->prm + r;
+	memset(rp, 0, sizeof(*rp));
+	rp->N = e->N[r];
+	rp->ensemble = p->ensemble;
+	rp->precision = p->precision;
+	rp->audit = p->audit;
+	rp->T = p->temperature;
+	rp->P = p->pressure;
+	rp->disp_max = p->disp_max;
+	rp->theta_max = p->theta_max;
+	rp->rescale_max = p->rescale_factor_max;
+	rp->cosmax = p->kf_cosmax;
+	rp->sqr_rcut = (1. + p->kf_delta) * (1. + p->kf_delta); /* system.c:86 */
+	rp->r_cut = 1. + p->kf_delta;                           /* system.c:249 */
+	h_base_patches(rp->base);
+	/* cell edge: r_cut plus a margin for FP32 rounding of cell-local coordinates; NPT also leaves room for
+	 * the accepted compressions between two re-sorts (each shrinks one side by at most exp(-max/2)) */
+	double wm = rp->r_cut + 1e-5;
+	if(p->ensemble == PP_NPT) wm /= exp(-0.5 * p->rescale_factor_max * (e->resort_every + 1));
+	rp->w_min = wm;
+	for(int k = 0; k < 32; k++) {
+		double pk = exp(-(double) k / p->temperature);
+		double t = ceil(pk * 9007199254740992.0);
+		if(t > 9007199254740992.0) t = 9007199254740992.0;
+		rp->acc_thr[k] = (uint64_t) t;
+	}
+	rp->cosmax_f = (float) rp->cosmax;
+	rp->sqr_rcut_f = (float) rp->sqr_rcut;
+	rp->eps_f = (float) p->guard_eps;
+	rp->disp_max_f = (float) p->disp_max;
+	rp->theta_max_f = (float) p->theta_max;
+	rp->base_f = (float) fabs(rp->base[0][0]);
+	rp->seed = p->seed;
+	const double *box = e->h_box[r];
+	double grow = (p->ensemble == PP_NPT) ? 1.15 : 1.0; /* a larger box is served by coarser cells */
+	long long cap = 1;
+	for(int a = 0; a < 3; a++) {
+		int n = ((int) floor(box[a] / wm)) & ~1;
+		if(n < 4) return set_err(e, PP_ERR_CAPACITY, "replica %d: box side %g is too small for the cell grid (needs >= 4 cells of edge %g)", r, box[a], wm);
+		if(n > PPI_MAX_AXIS_CELLS) return set_err(e, PP_ERR_CAPACITY, "replica %d: box side %g needs more than %d cells", r, box[a], PPI_MAX_AXIS_CELLS);
+		int nc = ((int) floor(box[a] * grow / wm)) & ~1;
+		if(nc > PPI_MAX_AXIS_CELLS) nc = PPI_MAX_AXIS_CELLS;
+		cap *= nc;
+	}
+	if(cap > (1LL << 28)) return set_err(e, PP_ERR_CAPACITY, "replica %d: too many cells", r);
+	rp->cell_cap = (int) cap;
+	return PP_OK;
+}
+
+static int ensure_pinned(pp_engine *e, size_t n) {
+	if(e->pin_n >= n && e->pin_rec) return PP_OK;
+	if(e->pin_rec) cudaFreeHost(e->pin_rec);
+	if(e->pin_id) cudaFreeHost(e->pin_id);
+	if(e->pin_i1) cudaFreeHost(e->pin_i1);
+	if(e->pin_i2) cudaFreeHost(e->pin_i2);
+	e->pin_rec = NULL;
+	e->pin_id = e->pin_i1 = e->pin_i2 = NULL;
+	CU(cudaMallocHost((void **) &e->pin_rec, sizeof(double) * PPI_REC * (n ? n : 1)));
+	CU(cudaMallocHost((void **) &e->pin_id, sizeof(int) * (n ? n : 1)));
+	CU(cudaMallocHost((void **) &e->pin_i1, sizeof(int) * PPI_MAX_PARTNERS * (n ? n : 1)));
+	CU(cudaMallocHost((void **) &e->pin_i2, sizeof(int) * (n ? n : 1)));
+	e->pin_n = n;
+	return PP_OK;
+}
+
+static int read_states(pp_engine *e) {
+	CU(cudaMemcpyAsync(e->h_rs, e->d.rs, sizeof(ppi_rstate) * e->nrep, cudaMemcpyDeviceToHost, e->stream));
+	CU(cudaStreamSynchronize(e->stream));
+	for(int r = 0; r < e->nrep; r++)
+		if(e->h_rs[r].error) return set_err(e, PP_ERR_CAPACITY, "replica %d: the box no longer fits an even cell grid of edge >= r_cut (device error %d)", r, e->h_rs[r].error);
+	return PP_OK;
+}
+
+static int write_states(pp_engine *e) {
+	CU(cudaMemcpyAsync(e->d.rs, e->h_rs, sizeof(ppi_rstate) * e->nrep, cudaMemcpyHostToDevice, e->stream));
+	return PP_OK;
+}
+
+static int do_resort(pp_engine *e) {
+	long long nl = 0;
+	if(e->reorder_every > 0 && e->epoch % e->reorder_every == 0) {
+		/* physical reorder into the current cell order keeps the FP64 updates of a cell's particles local */
+		CK(ppi_resort(&e->d, e->epoch, e->stream, &nl));
+		CK(ppi_reorder(&e->d, e->stream, &nl));
+	}
+	CK(ppi_resort(&e->d, e->epoch, e->stream, &nl));
+	e->launches += nl;
+	e->epoch++;
+	return PP_OK;
+}
+
+/* energy of every replica from scratch into rs.vol_bonds / vol_overlap (per-slot counts in out_*) */
+static int run_energy(pp_engine *e, int mode) {
+	long long nl = 0;
+	CK(ppi_energy(&e->d, mode, e->stream, &nl));
+	e->launches += nl;
+	return read_states(e);
+}
+
+static int commit(pp_engine *e) {
+	int ntot = 0;
+	for(int r = 0; r < e->nrep; r++) ntot += e->N[r];
+	free_device(e);
+	free(e->h_rp);
+	free(e->h_rs);
+	e->h_rp = calloc(e->nrep, sizeof(ppi_rparams));
+	e->h_rs = calloc(e->nrep, sizeof(ppi_rstate));
+	long long cells = 0;
+	int p0 = 0;
+	for(int r = 0; r < e->nrep; r++) {
+		ppi_rparams *rp = e->h_rp + r;
+		int rc = derive_rparams(e, r, rp);
+		if(rc != PP_OK) return rc;
+		rp->p0 = p0;
+		p0 += rp->N;
+		rp->cell_base = (int) cells;
+		cells += rp->cell_cap;
+	}
+	if(cells > (1LL << 30)) return set_err(e, PP_ERR_CAPACITY, "too many cells in total");
+	ppi_dev *d = &e->d;
+	d->nrep = e->nrep;
+	d->ntot = ntot;
+	d->total_cells = (int) cells;
+	d->clist_cap = (int) (cells / 8 + e->nrep + 8);
+	size_t n1 = ntot > 0 ? (size_t) ntot : 1;
+	CU(cudaMalloc((void **) &d->rec, sizeof(double) * PPI_REC * n1));
+	CU(cudaMalloc((void **) &d->srec, sizeof(float) * 16 * n1));
+	CU(cudaMalloc((void **) &d->id, sizeof(int) * n1));
+	CU(cudaMalloc((void **) &d->rep, sizeof(int) * n1));
+	CU(cudaMalloc((void **) &d->cellof, sizeof(int) * n1));
+	CU(cudaMalloc((void **) &d->out_bonds, sizeof(int) * n1));
+	CU(cudaMalloc((void **) &d->out_overlaps, sizeof(int) * n1));
+	CU(cudaMalloc((void **) &d->out_partners, sizeof(int) * PPI_MAX_PARTNERS * n1));
+	CU(cudaMalloc((void **) &d->tmp_rec, sizeof(double) * PPI_REC * n1));
+	CU(cudaMalloc((void **) &d->tmp_id, sizeof(int) * n1));
+	CU(cudaMalloc((void **) &d->cell_count, sizeof(int) * cells));
+	CU(cudaMalloc((void **) &d->cell_start, sizeof(int) * (cells + 1)));
+	CU(cudaMalloc((void **) &d->cell_cursor, sizeof(int) * cells));
+	CU(cudaMalloc((void **) &d->cell_rep, sizeof(int) * cells));
+	CU(cudaMalloc((void **) &d->scan_aux, sizeof(int) * ((cells + 1023) / 1024 + 1)));
+	CU(cudaMalloc((void **) &d->clist, sizeof(int) * 8 * (size_t) d->clist_cap));
+	CU(cudaMalloc((void **) &d->ccount, sizeof(int) * 8));
+	CU(cudaMalloc((void **) &d->rp, sizeof(ppi_rparams) * e->nrep));
+	CU(cudaMalloc((void **) &d->rs, sizeof(ppi_rstate) * e->nrep));
+	CU(cudaMalloc((void **) &d->grid, sizeof(ppi_grid) * e->nrep));
+	CU(cudaMemsetAsync(d->out_bonds, 0, sizeof(int) * n1, e->stream));
+	CU(cudaMemsetAsync(d->out_overlaps, 0, sizeof(int) * n1, e->stream));
+	CU(cudaMemsetAsync(d->grid, 0, sizeof(ppi_grid) * e->nrep, e->stream));
+	int rc = ensure_pinned(e, n1);
+	if(rc != PP_OK) return rc;
+	int *crep = malloc(sizeof(int) * (cells > 0 ? cells : 1));
+	int *rep = malloc(sizeof(int) * n1);
+	for(int r = 0; r < e->nrep; r++) {
+		ppi_rparams *rp = e->h_rp + r;
+		for(int c = 0; c < rp->cell_cap; c++) crep[rp->cell_base + c] = r;
+		for(int i = 0; i < rp->N; i++) rep[rp->p0 + i] = r;
+	}
+	cudaError_t c1 = cudaMemcpy(d->cell_rep, crep, sizeof(int) * cells, cudaMemcpyHostToDevice);
+	cudaError_t c2 = cudaMemcpy(d->rep, rep, sizeof(int) * ntot, cudaMemcpyHostToDevice);
+	free(crep);
+	free(rep);
+	if(c1 != cudaSuccess || c2 != cudaSuccess) return set_err(e, PP_ERR_CUDA, "layout upload failed");
+	CU(cudaMemcpy(d->rp, e->h_rp, sizeof(ppi_rparams) * e->nrep, cudaMemcpyHostToDevice));
+	e->ntot_alloc = ntot;
+	e->committed = 1;
+	return PP_OK;
+}
+
+/* copies replica r's host arrays into its device slots */
+static int push_replica(pp_engine *e, int r, const double *rr, const double *RR) {
+	ppi_rparams *rp = e->h_rp + r;
+	int N = rp->N;
+	for(int i = 0; i < N; i++) {
+		double *dst = e->pin_rec + (size_t) i * PPI_REC;
+		dst[0] = rr[3 * i];
+		dst[1] = rr[3 * i + 1];
+		dst[2] = rr[3 * i + 2];
+		memcpy(dst + 3, RR + 9 * (size_t) i, 9 * sizeof(double));
+		e->pin_id[i] = i;
+	}
+	CU(cudaMemcpyAsync(e->d.rec + (size_t) rp->p0 * PPI_REC, e->pin_rec, sizeof(double) * PPI_REC * N, cudaMemcpyHostToDevice, e->stream));
+	CU(cudaMemcpyAsync(e->d.id + rp->p0, e->pin_id, sizeof(int) * N, cudaMemcpyHostToDevice, e->stream));
+	/* the pinned buffer is reused by the next replica: wait for this copy */
+	CU(cudaStreamSynchronize(e->stream));
+	return PP_OK;
+}
+
+/* state uploaded: cell sort (with a physical reorder), initial energy and overlap check (main.c:55-64) */
+static int finish_upload(pp_engine *e, int only) {
+	int rc;
+	long long nl = 0;
+	CK(ppi_resort(&e->d, e->epoch, e->stream, &nl));
+	CK(ppi_reorder(&e->d, e->stream, &nl));
+	e->launches += nl;
+	rc = do_resort(e);
+	if(rc != PP_OK) return rc;
+	rc = run_energy(e, PPI_EN_BONDS);
+	if(rc != PP_OK) return rc;
+	int bad = -1;
+	for(int r = 0; r < e->nrep; r++) {
+		if(only >= 0 && r != only) continue;
+		ppi_rstate *s = e->h_rs + r;
+		if(s->vol_overlap && bad < 0) bad = r;
+		s->bonds = s->vol_bonds / 2;
+		s->pairs = s->fallbacks = 0;
+	}
+	rc = write_states(e);
+	if(rc != PP_OK) return rc;
+	CU(cudaStreamSynchronize(e->stream));
+	if(bad >= 0) return set_err(e, PP_ERR_OVERLAP, "Initial configuration contains an overlap, aborting (replica %d)", bad);
+	return PP_OK;
+}
+
+int pp_gpu_upload_replica(pp_engine *e, int r, int N, const double *rr, const double *RR, const double box[3]) {
+	if(e == NULL || r < 0 || r >= e->nrep || N < 0 || (N > 0 && (rr == NULL || RR == NULL)) || box == NULL) return set_err(e, PP_ERR_ARG, "invalid upload arguments");
+	for(int a = 0; a < 3; a++)
+		if(!(box[a] > 0.)) return set_err(e, PP_ERR_ARG, "box sides must be positive");
+	/* fast path: same layout already on the device -> copy straight into the replica's slots */
+	if(e->committed && e->N[r] == N) {
+		double grow = (e->prm[r].ensemble == PP_NPT) ? 1.15 : 1.0;
+		long long cap = 1;
+		for(int a = 0; a < 3; a++) {
+			int nc = ((int) floor(box[a] * grow / e->h_rp[r].w_min)) & ~1;
+			cap *= nc < 4 ? 4 : nc;
+		}
+		if(cap <= e->h_rp[r].cell_cap) {
+			int rc = read_states(e);
+			if(rc != PP_OK) return rc;
+			memcpy(e->h_box[r], box, sizeof(double) * 3);
+			ppi_rstate *s = e->h_rs + r;
+			memset(s, 0, sizeof(*s));
+			memcpy(s->box, box, sizeof(s->box));
+			s->V = box[0] * box[1] * box[2];
+			rc = write_states(e);
+			if(rc != PP_OK) return rc;
+			rc = push_replica(e, r, rr, RR);
+			if(rc != PP_OK) return rc;
+			return finish_upload(e, r);
+		}
+	}
+	free(e->h_r[r]);
+	free(e->h_R[r]);
+	e->h_r[r] = malloc(sizeof(double) * 3 * (N > 0 ? N : 1));
+	e->h_R[r] = malloc(sizeof(double) * 9 * (N > 0 ? N : 1));
+	if(N > 0) {
+		memcpy(e->h_r[r], rr, sizeof(double) * 3 * N);
+		memcpy(e->h_R[r], RR, sizeof(double) * 9 * N);
+	}
+	memcpy(e->h_box[r], box, sizeof(double) * 3);
+	e->N[r] = N;
+	e->uploaded[r] = 1;
+	e->committed = 0;
+	for(int q = 0; q < e->nrep; q++)
+		if(!e->uploaded[q]) return PP_OK; /* wait for the rest of the batch */
+	int rc = commit(e);
+	if(rc != PP_OK) return rc;
+	for(int q = 0; q < e->nrep; q++) {
+		ppi_rstate *s = e->h_rs + q;
+		memset(s, 0, sizeof(*s));
+		memcpy(s->box, e->h_box[q], sizeof(s->box));
+		s->V = s->box[0] * s->box[1] * s->box[2];
+	}
+	rc = write_states(e);
+	if(rc != PP_OK) return rc;
+	for(int q = 0; q < e->nrep; q++) {
+		rc = push_replica(e, q, e->h_r[q], e->h_R[q]);
+		if(rc != PP_OK) return rc;
+	}
+	return finish_upload(e, -1);
+}
+
+int pp_gpu_upload(pp_engine *e, int N, const double *r, const double *R, const double box[3]) { return pp_gpu_upload_replica(e, 0, N, r, R, box); }
+
+static int ready(pp_engine *e) {
+	if(e == NULL) return PP_ERR_ARG;
+	if(!e->committed) return set_err(e, PP_ERR_STATE, "no configuration uploaded for every replica");
+	return PP_OK;
+}
+
+/* ------------------------------------------------------------------------------------------------ */
+/* event timing                                                                                     */
+/* ------------------------------------------------------------------------------------------------ */
+static int collect_events(pp_engine *e) {
+	if(e->n_ev == 0) return PP_OK;
+	CU(cudaStreamSynchronize(e->stream));
+	for(int i = 0; i < e->n_ev; i++) {
+		float ms = 0.f;
+		CU(cudaEventElapsedTime(&ms, e->ev[2 * i], e->ev[2 * i + 1]));
+		if(e->ev_kind[i] == 0) {
+			e->kstats.sort_ms += ms;
+			e->kstats.sort_launches++;
+		}
+		else if(e->ev_kind[i] == 1) {
+			e->kstats.sweep_ms += ms;
+			e->kstats.sweep_launches++;
+		}
+		else {
+			e->kstats.volume_ms += ms;
+			e->kstats.volume_launches++;
+		}
+	}
+	e->n_ev = 0;
+	return PP_OK;
+}
+
+static int ev_begin(pp_engine *e, int kind, int *slot) {
+	*slot = -1;
+	if(!e->timing) return PP_OK;
+	if(e->n_ev == e->ev_cap) {
+		int rc = collect_events(e);
+		if(rc != PP_OK) return rc;
+	}
+	int i = e->n_ev++;
+	e->ev_kind[i] = kind;
+	CU(cudaEventRecord(e->ev[2 * i], e->stream));
+	*slot = i;
+	return PP_OK;
+}
+
+static int ev_end(pp_engine *e, int slot) {
+	if(slot < 0) return PP_OK;
+	CU(cudaEventRecord(e->ev[2 * slot + 1], e->stream));
+	return PP_OK;
+}
+
+int pp_gpu_set_timing(pp_engine *e, int enable) {
+	if(e == NULL) return PP_ERR_ARG;
+	if(enable && e->ev == NULL) {
+		e->ev_cap = 3072;
+		e->ev = calloc(2 * e->ev_cap, sizeof(cudaEvent_t));
+		e->ev_kind = calloc(e->ev_cap, sizeof(int));
+		for(int i = 0; i < 2 * e->ev_cap; i++) CU(cudaEventCreate(&e->ev[i]));
+	}
+	if(!enable) {
+		int rc = collect_events(e);
+		if(rc != PP_OK) return rc;
+	}
+	e->timing = enable ? 1 : 0;
+	return PP_OK;
+}
+
+int pp_gpu_kernel_stats(pp_engine *e, pp_kernel_stats *out, int reset) {
+	if(e == NULL) return PP_ERR_ARG;
+	int rc = collect_events(e);
+	if(rc != PP_OK) return rc;
+	if(out) *out = e->kstats;
+	if(reset) memset(&e->kstats, 0, sizeof(e->kstats));
+	return PP_OK;
+}
+
+int pp_gpu_select_device(int device) {
+	cudaError_t c = cudaSetDevice(device);
+	return c == cudaSuccess ? PP_OK : PP_ERR_CUDA;
+}
+
+/* ------------------------------------------------------------------------------------------------ */
+/* sweeps                                                                                           */
+/* ------------------------------------------------------------------------------------------------ */
+/* order of the 8 checkerboard colours in a round: a Fisher-Yates shuffle driven by splitmix64 of the round
+ * index. It depends on no replica's seed, so a replica's trajectory does not depend on its batch. */
+static void colour_order(long long round, int col[8]) {
+	uint64_t z = (uint64_t) round * 0x9E3779B97F4A7C15ULL + 0x632BE59BD9B4E019ULL;
+	for(int i = 0; i < 8; i++) col[i] = i;
+	for(int i = 7; i > 0; i--) {
+		z += 0x9E3779B97F4A7C15ULL;
+		uint64_t x = z;
+		x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
+		x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
+		x ^= x >> 31;
+		int j = (int) (x % (uint64_t) (i + 1));
+		int t = col[i];
+		col[i] = col[j];
+		col[j] = t;
+	}
+}
+
+/* One MC step: `rounds_per_sweep` checkerboard rounds (one attempt per non-empty cell per round, the
+ * grid re-sorted from the FP64 state every resort_every rounds), then one NPT volume attempt. */
+int pp_gpu_sweeps(pp_engine *e, long long n) {
+	int rc = ready(e);
+	if(rc != PP_OK) return rc;
+	if(n < 0) return set_err(e, PP_ERR_ARG, "negative sweep count");
+	for(long long k = 0; k < n; k++) {
+		long long s = e->sweep_counter++;
+		int ev;
+		for(int rr = 0; rr < e->rounds_per_sweep; rr++) {
+			if(e->round_counter % e->resort_every == 0) {
+				if((rc = ev_begin(e, 0, &ev)) != PP_OK) return rc;
+				if((rc = do_resort(e)) != PP_OK) return rc;
+				if((rc = ev_end(e, ev)) != PP_OK) return rc;
+			}
+			long long nl = 0;
+			int colours[8];
+			colour_order(e->round_counter, colours);
+			if((rc = ev_begin(e, 1, &ev)) != PP_OK) return rc;
+			CK(ppi_round(&e->d, e->round_counter, colours, e->stream, &nl));
+			if((rc = ev_end(e, ev)) != PP_OK) return rc;
+			e->round_counter++;
+			e->launches += nl;
+		}
+		if(e->any_npt) {
+			long long nl = 0;
+			if((rc = ev_begin(e, 2, &ev)) != PP_OK) return rc;
+			CK(ppi_volume(&e->d, s, e->stream, &nl));
+			if((rc = ev_end(e, ev)) != PP_OK) return rc;
+			e->launches += nl;
+		}
+	}
+	return PP_OK;
+}
+
+int pp_gpu_time_sweeps(pp_engine *e, long long n, double *ms) {
+	int rc = ready(e);
+	if(rc != PP_OK) return rc;
+	cudaEvent_t a, b;
+	CU(cudaEventCreate(&a));
+	CU(cudaEventCreate(&b));
+	CU(cudaEventRecord(a, e->stream));
+	rc = pp_gpu_sweeps(e, n);
+	if(rc != PP_OK) return rc;
+	CU(cudaEventRecord(b, e->stream));
+	CU(cudaEventSynchronize(b));
+	float t = 0.f;
+	CU(cudaEventElapsedTime(&t, a, b));
+	cudaEventDestroy(a);
+	cudaEventDestroy(b);
+	if(ms) *ms = t;
+	return read_states(e);
+}
+
+int pp_gpu_sync(pp_engine *e) {
+	int rc = ready(e);
+	if(rc != PP_OK) return rc;
+	CU(cudaStreamSynchronize(e->stream));
+	CU(cudaGetLastError());
+	return read_states(e);
+}
+
+int pp_gpu_get_energy(pp_engine *e, int r, double *E) {
+	int rc = ready(e);
+	if(rc != PP_OK) return rc;
+	if(r < 0 || r >= e->nrep || E == NULL) return set_err(e, PP_ERR_ARG, "bad replica");
+	rc = read_states(e);
+	if(rc != PP_OK) return rc;
+	*E = -(double) e->h_rs[r].bonds;
+	return PP_OK;
+}
+
+int pp_gpu_box(pp_engine *e, int r, double box[3]) {
+	int rc = ready(e);
+	if(rc != PP_OK) return rc;
+	if(r < 0 || r >= e->nrep) return set_err(e, PP_ERR_ARG, "bad replica");
+	rc = read_states(e);
+	if(rc != PP_OK) return rc;
+	memcpy(box, e->h_rs[r].box, sizeof(double) * 3);
+	return PP_OK;
+}
+
+int pp_gpu_energy(pp_engine *e, int r, double *E, int *overlap) {
+	int rc = ready(e);
+	if(rc != PP_OK) return rc;
+	if(r < 0 || r >= e->nrep) return set_err(e, PP_ERR_ARG, "bad replica");
+	rc = run_energy(e, PPI_EN_BONDS);
+	if(rc != PP_OK) return rc;
+	if(E) *E = -0.5 * (double) e->h_rs[r].vol_bonds;
+	if(overlap) *overlap = e->h_rs[r].vol_overlap;
+	return PP_OK;
+}
+
+int pp_gpu_orthonormalise(pp_engine *e, int r) {
+	int rc = ready(e);
+	if(rc != PP_OK) return rc;
+	if(r < 0 || r >= e->nrep) return set_err(e, PP_ERR_ARG, "bad replica");
+	long long nl = 0;
+	ppi_rparams *rp = e->h_rp + r;
+	CK(ppi_gram_schmidt(&e->d, rp->p0, rp->N, e->stream, &nl));
+	e->launches += nl;
+	/* the FP32 working records are rebuilt from the re-orthonormalised FP64 state */
+	rc = do_resort(e);
+	if(rc != PP_OK) return rc;
+	e->round_counter += e->resort_every - e->round_counter % e->resort_every; /* start a fresh epoch */
+	CU(cudaStreamSynchronize(e->stream));
+	return PP_OK;
+}
+
+int pp_gpu_check_energy(pp_engine *e, int r) {
+	double E;
+	int ov;
+	int rc = pp_gpu_energy(e, r, &E, &ov);
+	if(rc != PP_OK) return rc;
+	double tracked = -(double) e->h_rs[r].bonds;
+	rc = pp_gpu_orthonormalise(e, r);
+	if(rc != PP_OK) return rc;
+	if(ov) return set_err(e, PP_ERR_OVERLAP, "Computing energy from scratch resulted in an overlap, aborting");
+	if(fabs(tracked) > 1e-5 && fabs((E - tracked) / tracked) > 1e-5)
+		return set_err(e, PP_ERR_DRIFT, "Energy check failed, old energy = %lf, new energy = %lf", tracked, E);
+	rc = read_states(e);
+	if(rc != PP_OK) return rc;
+	e->h_rs[r].bonds = (long long) llround(-E);
+	return write_states(e);
+}
+
+int pp_gpu_counters(pp_engine *e, int r, pp_counters *out, int reset) {
+	int rc = ready(e);
+	if(rc != PP_OK) return rc;
+	if(r < 0 || r >= e->nrep) return set_err(e, PP_ERR_ARG, "bad replica");
+	rc = read_states(e);
+	if(rc != PP_OK) return rc;
+	if(out) {
+		for(int k = 0; k < PP_N_MOVES; k++) {
+			out->tries[k] = (long long) e->h_rs[r].tries[k];
+			out->accepted[k] = (long long) e->h_rs[r].accepted[k];
+		}
+	}
+	if(reset) {
+		memset(e->h_rs[r].tries, 0, sizeof(e->h_rs[r].tries));
+		memset(e->h_rs[r].accepted, 0, sizeof(e->h_rs[r].accepted));
+		rc = write_states(e);
+		if(rc != PP_OK) return rc;
+		CU(cudaStreamSynchronize(e->stream));
+	}
+	return PP_OK;
+}
+
+int pp_gpu_guard_stats(pp_engine *e, pp_guard_stats *out, int reset) {
+	int rc = ready(e);
+	if(rc != PP_OK) return rc;
+	rc = read_states(e);
+	if(rc != PP_OK) return rc;
+	pp_guard_stats g;
+	memset(&g, 0, sizeof(g));
+	for(int r = 0; r < e->nrep; r++) {
+		ppi_rstate *s = e->h_rs + r;
+		g.pairs += (long long) s->pairs;
+		g.fallbacks += (long long) s->fallbacks;
+		g.mismatches += (long long) s->mismatches;
+		float a, b;
+		memcpy(&a, &s->max_err_r2_bits, 4);
+		memcpy(&b, &s->max_err_cos_bits, 4);
+		if(a > g.max_err_r2) g.max_err_r2 = a;
+		if(b > g.max_err_cos) g.max_err_cos = b;
+		if(reset) {
+			s->pairs = s->fallbacks = s->mismatches = 0;
+			s->max_err_r2_bits = s->max_err_cos_bits = 0;
+		}
+	}
+	if(out) *out = g;
+	if(reset) {
+		rc = write_states(e);
+		if(rc != PP_OK) return rc;
+		CU(cudaStreamSynchronize(e->stream));
+	}
+	return PP_OK;
+}
+
+int pp_gpu_download_replica(pp_engine *e, int r, double *rr, double *RR, double box[3]) {
+	int rc = ready(e);
+	if(rc != PP_OK) return rc;
+	if(r < 0 || r >= e->nrep) return set_err(e, PP_ERR_ARG, "bad replica");
+	rc = read_states(e);
+	if(rc != PP_OK) return rc;
+	ppi_rparams *rp = e->h_rp + r;
+	int N = rp->N;
+	CU(cudaMemcpyAsync(e->pin_rec, e->d.rec + (size_t) rp->p0 * PPI_REC, sizeof(double) * PPI_REC * N, cudaMemcpyDeviceToHost, e->stream));
+	CU(cudaMemcpyAsync(e->pin_id, e->d.id + rp->p0, sizeof(int) * N, cudaMemcpyDeviceToHost, e->stream));
+	CU(cudaStreamSynchronize(e->stream));
+	for(int k = 0; k < N; k++) {
+		int i = e->pin_id[k];
+		if(i < 0 || i >= N) return set_err(e, PP_ERR_STATE, "corrupt particle ids");
+		const double *src = e->pin_rec + (size_t) k * PPI_REC;
+		if(rr) memcpy(rr + 3 * (size_t) i, src, 3 * sizeof(double));
+		if(RR) memcpy(RR + 9 * (size_t) i, src + 3, 9 * sizeof(double));
+	}
+	if(box) memcpy(box, e->h_rs[r].box, sizeof(double) * 3);
+	return PP_OK;
+}
+
+int pp_gpu_download(pp_engine *e, double *r, double *R, double box[3]) { return pp_gpu_download_replica(e, 0, r, R, box); }
+
+static int fetch_counts(pp_engine *e, int r, int mode) {
+	int rc = run_energy(e, mode);
+	if(rc != PP_OK) return rc;
+	ppi_rparams *rp = e->h_rp + r;
+	int N = rp->N;
+	CU(cudaMemcpyAsync(e->pin_i2, e->d.out_bonds + rp->p0, sizeof(int) * N, cudaMemcpyDeviceToHost, e->stream));
+	CU(cudaMemcpyAsync(e->pin_id, e->d.id + rp->p0, sizeof(int) * N, cudaMemcpyDeviceToHost, e->stream));
+	CU(cudaStreamSynchronize(e->stream));
+	return PP_OK;
+}
+
+int pp_gpu_bonds(pp_engine *e, int r, int *n_bonds, int *n_overlaps) {
+	int rc = ready(e);
+	if(rc != PP_OK) return rc;
+	if(r < 0 || r >= e->nrep) return set_err(e, PP_ERR_ARG, "bad replica");
+	rc = fetch_counts(e, r, PPI_EN_BONDS);
+	if(rc != PP_OK) return rc;
+	ppi_rparams *rp = e->h_rp + r;
+	int N = rp->N;
+	CU(cudaMemcpyAsync(e->pin_i1, e->d.out_overlaps + rp->p0, sizeof(int) * N, cudaMemcpyDeviceToHost, e->stream));
+	CU(cudaStreamSynchronize(e->stream));
+	for(int k = 0; k < N; k++) {
+		int i = e->pin_id[k];
+		if(i < 0 || i >= N) return set_err(e, PP_ERR_STATE, "corrupt particle ids");
+		if(n_bonds) n_bonds[i] = e->pin_i2[k];
+		if(n_overlaps) n_overlaps[i] = e->pin_i1[k];
+	}
+	return PP_OK;
+}
+
+static int cmp_int(const void *a, const void *b) {
+	int x = *(const int *) a, y = *(const int *) b;
+	return (x > y) - (x < y);
+}
+
+int pp_gpu_bond_lists(pp_engine *e, int r, int *offsets, int *partners, int cap) {
+	int rc = ready(e);
+	if(rc != PP_OK) return rc;
+	if(r < 0 || r >= e->nrep || offsets == NULL) return set_err(e, PP_ERR_ARG, "bad arguments");
+	rc = fetch_counts(e, r, PPI_EN_PARTNERS);
+	if(rc != PP_OK) return rc;
+	ppi_rparams *rp = e->h_rp + r;
+	int N = rp->N;
+	CU(cudaMemcpyAsync(e->pin_i1, e->d.out_partners + (size_t) rp->p0 * PPI_MAX_PARTNERS, sizeof(int) * PPI_MAX_PARTNERS * N, cudaMemcpyDeviceToHost, e->stream));
+	CU(cudaStreamSynchronize(e->stream));
+	/* counts in upload order, then offsets, then the lists */
+	int *cnt = calloc(N > 0 ? N : 1, sizeof(int));
+	int *where = calloc(N > 0 ? N : 1, sizeof(int));
+	for(int k = 0; k < N; k++) {
+		int i = e->pin_id[k];
+		if(i < 0 || i >= N) {
+			free(cnt);
+			free(where);
+			return set_err(e, PP_ERR_STATE, "corrupt particle ids");
+		}
+		cnt[i] = e->pin_i2[k];
+		where[i] = k;
+		if(cnt[i] > PPI_MAX_PARTNERS) {
+			free(cnt);
+			free(where);
+			return set_err(e, PP_ERR_CAPACITY, "particle %d has more than %d bonds", i, PPI_MAX_PARTNERS);
+		}
+	}
+	int total = 0;
+	for(int i = 0; i < N; i++) {
+		offsets[i] = total;
+		total += cnt[i];
+	}
+	offsets[N] = total;
+	if(total > cap || (total > 0 && partners == NULL)) {
+		free(cnt);
+		free(where);
+		return set_err(e, PP_ERR_CAPACITY, "partner buffer holds %d entries, %d needed", cap, total);
+	}
+	for(int i = 0; i < N; i++) {
+		memcpy(partners + offsets[i], e->pin_i1 + (size_t) where[i] * PPI_MAX_PARTNERS, sizeof(int) * cnt[i]);
+		qsort(partners + offsets[i], cnt[i], sizeof(int), cmp_int);
+	}
+	free(cnt);
+	free(where);
+	return total;
+}
+
+/* ------------------------------------------------------------------------------------------------ */
+/* .rrr format                                                                                      */
+/* ------------------------------------------------------------------------------------------------ */
+int pp_rrr_header(const char *path, long long *step, int *N, double box[3]) {
+	FILE *f = fopen(path, "r");
+	if(f == NULL) return PP_ERR_IO;
+	long long st;
+	int n;
+	double b[3];
+	int res = fscanf(f, "%lld %d %lf %lf %lf", &st, &n, b, b + 1, b + 2);
+	fclose(f);
+	if(res != 5 || n < 0) return PP_ERR_IO;
+	if(step) *step = st;
+	if(N) *N = n;
+	if(box) memcpy(box, b, sizeof(b));
+	return PP_OK;
+}
+
+static void set_msg(char *err, int len, const char *fmt, ...) {
+	if(err == NULL || len <= 0) return;
+	va_list ap;
+	va_start(ap, fmt);
+	vsnprintf(err, len, fmt, ap);
+	va_end(ap);
+}
+
+/* system.c:77-245: header "%*d %d %lf %lf %lf", then per particle: row 0 via fgets + sscanf, row 1 and the
+ * position via fscanf; rows normalised, row 2 = row0 x row1, gram_schmidt. */
+int pp_rrr_read(const char *path, int N, double *r, double *R, double box[3], char *err, int err_len) {
+	FILE *f = fopen(path, "r");
+	if(f == NULL) {
+		set_msg(err, err_len, "Initial_conditions_file '%s' is not readable", path);
+		return PP_ERR_IO;
+	}
+	int n;
+	double b[3];
+	if(fscanf(f, "%*d %d %lf %lf %lf\n", &n, b, b + 1, b + 2) != 4) {
+		fclose(f);
+		set_msg(err, err_len, "The initial configuration file '%s' is empty or its headers are malformed", path);
+		return PP_ERR_IO;
+	}
+	if(n != N) {
+		fclose(f);
+		set_msg(err, err_len, "header of '%s' announces %d particles, caller expected %d", path, n, N);
+		return PP_ERR_IO;
+	}
+	if(box) memcpy(box, b, sizeof(b));
+	int i = 0;
+	double p1[3] = { 0., 0., 0. }, p2[3] = { 0., 0., 0. }, p3[3], rp[3] = { 0., 0., 0. };
+	char line[512];
+	char *sr = fgets(line, sizeof(line), f);
+	while(sr != NULL) {
+		if(i >= N) {
+			i++;
+			break;
+		}
+		if(sscanf(line, "%lf %lf %lf\n", p1, p1 + 1, p1 + 2) < 0) {
+		}
+		if(fscanf(f, "%lf %lf %lf\n", p2, p2 + 1, p2 + 2) < 0) {
+		}
+		if(fscanf(f, "%lf %lf %lf\n", rp, rp + 1, rp + 2) < 0) {
+		}
+		h_normalize(p1);
+		h_normalize(p2);
+		h_cross(p1, p2, p3);
+		double *Ri = R + 9 * (size_t) i;
+		memcpy(Ri, p1, sizeof(p1));
+		memcpy(Ri + 3, p2, sizeof(p2));
+		memcpy(Ri + 6, p3, sizeof(p3));
+		h_gram_schmidt(Ri, Ri + 3, Ri + 6);
+		memcpy(r + 3 * (size_t) i, rp, sizeof(rp));
+		i++;
+		sr = fgets(line, sizeof(line), f);
+	}
+	fclose(f);
+	if(i != N) {
+		set_msg(err, err_len, "Number of particles found in configuration (%d) is different from the value found in the header (%d)", i, N);
+		return PP_ERR_IO;
+	}
+	return PP_OK;
+}
+
+int pp_rrr_write(const char *path, long long step, int N, const double *r, const double *R, const double box[3]) {
+	FILE *out = fopen(path, "w");
+	if(out == NULL) return PP_ERR_IO;
+	fprintf(out, "%lld %d %.12lf %.12lf %.12lf\n", step, N, box[0], box[1], box[2]); /* output.c:306 */
+	for(int i = 0; i < N; i++) {
+		const double *Ri = R + 9 * (size_t) i, *ri = r + 3 * (size_t) i;
+		fprintf(out, "%lf %lf %lf\n", Ri[0], Ri[1], Ri[2]);
+		fprintf(out, "%lf %lf %lf\n", Ri[3], Ri[4], Ri[5]);
+		fprintf(out, "%.12lf %.12lf %.12lf\n", ri[0], ri[1], ri[2]);
+	}
+	fclose(out);
+	return PP_OK;
+}
+
+/* ------------------------------------------------------------------------------------------------ */
+/* generator (generator.c)                                                                          */
+/* ------------------------------------------------------------------------------------------------ */
+typedef struct {
+	unsigned long long X;
+} g_rng;
+
+static double g_drand(g_rng *g) { /* POSIX drand48 recurrence */
+	g->X = (0x5DEECE66DULL * g->X + 0xBULL) & 0xFFFFFFFFFFFFULL;
+	return (double) g->X * 0x1p-48;
+}
+
+static void g_sphere(g_rng *g, double *res) { /* random_vector_on_sphere, utils.c:115-131 */
+	double a, b, s;
+	do {
+		a = 1. - 2. * g_drand(g);
+		b = 1. - 2. * g_drand(g);
+		s = a * a + b * b;
+	} while(s >= 1.);
+	double h = 2. * sqrt(1. - s);
+	res[0] = a * h;
+	res[1] = b * h;
+	res[2] = 1. - 2. * s;
+}
+
+static double g_det(const double *m) { /* determinant, utils.c:78-89 */
+	double det = 0.;
+	det += m[0] * m[4] * m[8];
+	det += m[1] * m[5] * m[6];
+	det += m[2] * m[3] * m[7];
+	det -= m[2] * m[4] * m[6];
+	det -= m[0] * m[5] * m[7];
+	det -= m[1] * m[3] * m[8];
+	return det;
+}
+
+static void g_orientation(g_rng *g, double *R) { /* random_orientation, utils.c:133-169 */
+	double x[3], y[3], z[3];
+	g_sphere(g, x);
+	g_sphere(g, y);
+	g_sphere(g, z);
+	h_gram_schmidt(x, y, z);
+	memcpy(R, z, sizeof(z));
+	memcpy(R + 3, x, sizeof(x));
+	memcpy(R + 6, y, sizeof(y));
+	if(g_det(R) < 0) {
+		memcpy(R, x, sizeof(x));
+		memcpy(R + 3, z, sizeof(z));
+	}
+}
+
+static double round_text(const char *fmt, double v) {
+	char buf[64];
+	snprintf(buf, sizeof(buf), fmt, v);
+	return strtod(buf, NULL);
+}
+
+int pp_generate(int N, double density, int seed, int round_like_file, double *r, double *R, double box[3]) {
+	if(N < 0 || !(density > 0.) || density > 0.7 || r == NULL || R == NULL || box == NULL) return PP_ERR_ARG; /* generator.c:99-102 */
+	double L = pow(N / density, 1. / 3.); /* generator.c:103-105 */
+	g_rng g = { ((unsigned long long) (unsigned int) seed << 16) | 0x330EULL };
+	/* cells of edge >= 1 (cells_init with rcut = 1, cells.c:17-37) */
+	int ns = (int) floor(L / 1.);
+	if(ns < 3) ns = 3;
+	long long nc = (long long) ns * ns * ns;
+	int *head = malloc(sizeof(int) * nc);
+	int *next = malloc(sizeof(int) * (N > 0 ? N : 1));
+	if(head == NULL || next == NULL) {
+		free(head);
+		free(next);
+		return PP_ERR_ARG;
+	}
+	for(long long c = 0; c < nc; c++) head[c] = -1;
+	double bx[3] = { L, L, L };
+	int inserted = 0;
+	while(inserted < N) { /* make_initial_conf, generator.c:43-68 */
+		double p[3] = { g_drand(&g) * L, g_drand(&g) * L, g_drand(&g) * L };
+		int ind[3];
+		for(int k = 0; k < 3; k++) ind[k] = (int) ((p[k] / bx[k] - floor(p[k] / bx[k])) * (1. - DBL_EPSILON) * ns);
+		int over = 0;
+		for(int j = -1; j < 2 && !over; j++)
+			for(int k = -1; k < 2 && !over; k++)
+				for(int l = -1; l < 2 && !over; l++) {
+					int cx = (ind[0] + j + ns) % ns, cy = (ind[1] + k + ns) % ns, cz = (ind[2] + l + ns) % ns;
+					int q = head[((long long) cx * ns + cy) * ns + cz];
+					while(q != -1) {
+						const double *rq = r + 3 * (size_t) q;
+						double d[3] = { rq[0] - p[0], rq[1] - p[1], rq[2] - p[2] };
+						for(int a = 0; a < 3; a++) d[a] -= bx[a] * rint(d[a] / bx[a]);
+						if(H_SCALAR(d, d) < 1.) {
+							over = 1;
+							break;
+						}
+						q = next[q];
+					}
+				}
+		if(over) continue;
+		g_orientation(&g, R + 9 * (size_t) inserted);
+		memcpy(r + 3 * (size_t) inserted, p, sizeof(p));
+		int c = (ind[0] * ns + ind[1]) * ns + ind[2];
+		next[inserted] = head[c];
+		head[c] = inserted;
+		inserted++;
+	}
+	free(head);
+	free(next);
+	box[0] = box[1] = box[2] = L;
+	if(round_like_file) {
+		/* what writing generated.rrr (generator.c:70-82) and reading it back (system.c:80-243) gives */
+		double Lr = round_text("%lf", L);
+		box[0] = box[1] = box[2] = Lr;
+		for(int i = 0; i < N; i++) {
+			double *Ri = R + 9 * (size_t) i, *ri = r + 3 * (size_t) i;
+			double p1[3], p2[3], p3[3];
+			for(int k = 0; k < 3; k++) {
+				p1[k] = round_text("%lf", Ri[k]);
+				p2[k] = round_text("%lf", Ri[3 + k]);
+				ri[k] = round_text("%.12lf", ri[k]);
+			}
+			h_normalize(p1);
+			h_normalize(p2);
+			h_cross(p1, p2, p3);
+			memcpy(Ri, p1, sizeof(p1));
+			memcpy(Ri + 3, p2, sizeof(p2));
+			memcpy(Ri + 6, p3, sizeof(p3));
+			h_gram_schmidt(Ri, Ri + 3, Ri + 6);
+		}
+	}
+	return PP_OK;
+}

@@ -1,0 +1,133 @@
+/*
+ * ppgpu_internal.h -- data layout shared by the C host code (ppgpu_host.c) and the CUDA kernels
+ * (ppgpu_kernels.cu). Plain C structs; no torch types.
+ *
+ * Device memory (one engine = R replicas; particle "slots" are global over replicas):
+ *   rec[slot]   12 doubles: canonical FP64 state, x y z (unwrapped) then orientation rows R00..R22
+ *               (96 B = three 32-B sectors). Only FP64 arithmetic ever writes it.
+ *   srec[k]     64-B FP32 working record of the particle at cell-sorted position k:
+ *                 a = (lx, ly, lz, slot)       cell-local position, 0 <= l < w
+ *                 b = (c0x, c0y, c0z, c1x)     orientation columns c_j = (R0j, R1j, R2j)
+ *                 c = (c1y, c1z, c2x, c2y)
+ *                 d = (c2z, id, cell, -)       particle id (upload order), global cell index
+ *               Rebuilt from rec every `resort_every` rounds; updated in FP32 by accepted moves in between.
+ *   cell_start  per replica n_x*n_y*n_z + 1 entries (global cell index = replica cell base + local index,
+ *               local index = (cz * n_y + cy) * n_x + cx), particles of a cell contiguous in srec.
+ *   clist       per colour (8), the non-empty cells of that checkerboard colour (global cell indices).
+ */
+#ifndef PPGPU_INTERNAL_H_
+#define PPGPU_INTERNAL_H_
+
+#include <stdint.h>
+#include <cuda_runtime_api.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PPI_REC 12
+#define PPI_MAX_AXIS_CELLS 1024
+
+/* error codes written by kernels into ppi_rstate.error */
+#define PPI_E_GRID 2 /* the box became too small for an even cell grid of edge >= r_cut */
+
+typedef struct ppi_rparams {
+	int N;           /* particles of this replica */
+	int p0;          /* first slot */
+	int ensemble;    /* 0 NVT, 5 NPT */
+	int precision;   /* 0 FP32 + guard, 1 FP64 */
+	int audit;
+	int cell_base;   /* first global cell index of this replica */
+	int cell_cap;    /* cells reserved for this replica */
+	int pad0;
+	double T, P, disp_max, theta_max, rescale_max;
+	double cosmax, sqr_rcut, r_cut, w_min;
+	double base[4][3];     /* tetrahedral base patches, bit-identical to system.c:20-31 */
+	uint64_t acc_thr[32];  /* accept a move with dE = +k iff U53 < acc_thr[k], U53 uniform in [0, 2^53) */
+	float cosmax_f, sqr_rcut_f, eps_f, disp_max_f, theta_max_f, base_f;
+	float pad1[2];
+	uint64_t seed;
+} ppi_rparams;
+
+typedef struct ppi_rstate {
+	double box[3];
+	double V;                    /* System::V (updated by accepted volume moves, MC.c:500) */
+	long long bonds;             /* tracked bonded pairs: energy = -bonds */
+	unsigned long long tries[8];
+	unsigned long long accepted[8];
+	long long vol_bonds;         /* bonds counted by the last energy pass (candidate box for NPT) */
+	int vol_overlap;
+	int vol_accept;
+	int error;
+	int error_info;
+	unsigned long long pairs, fallbacks, mismatches;
+	unsigned int max_err_r2_bits, max_err_cos_bits;
+} ppi_rstate;
+
+typedef struct ppi_grid {
+	int n[3];          /* cells per axis (even) */
+	int ncells;
+	double w[3];       /* cell edge */
+	double shift[3];   /* grid origin offset, uniform in [0, w) at every re-sort */
+	double inv_w[3], inv_L[3];
+	float wf[3];
+	float pad;
+	/* NPT candidate of the current sweep (MC.c:456-472) */
+	int vol_dir;
+	int pad2;
+	double vol_f, vol_side, vol_V1, vol_V0;
+	float vol_ff;
+	float pad3;
+} ppi_grid;
+
+/* all device pointers, passed by value to every kernel */
+typedef struct ppi_dev {
+	int nrep;
+	int ntot;          /* total slots */
+	int total_cells;   /* sum of cell caps */
+	int pad;
+	double *rec;
+	float4 *srec;      /* 4 x float4 per particle */
+	int *id;           /* slot -> particle index in its replica */
+	int *rep;          /* slot -> replica */
+	int *cellof;       /* slot -> global cell (current grid) */
+	int *cell_count;
+	int *cell_start;   /* total_cells + 1 */
+	int *cell_cursor;
+	int *cell_rep;     /* global cell -> replica */
+	int *scan_aux;
+	int *clist;        /* 8 lists of capacity total_cells / 8 + nrep each */
+	int *ccount;       /* 8 counters */
+	int clist_cap;
+	int pad1;
+	ppi_rparams *rp;
+	ppi_rstate *rs;
+	ppi_grid *grid;
+	int *out_bonds;    /* per slot */
+	int *out_overlaps;
+	int *out_partners; /* bond lists: per slot up to PPI_MAX_PARTNERS */
+	double *tmp_rec;   /* reorder scratch */
+	int *tmp_id;
+} ppi_dev;
+
+#define PPI_MAX_PARTNERS 24
+
+/* launchers (ppgpu_kernels.cu); each returns a cudaError_t value as int and adds its launches to *nl */
+int ppi_resort(const ppi_dev *d, long long epoch, cudaStream_t s, long long *nl);
+int ppi_round(const ppi_dev *d, long long round, const int *colours, cudaStream_t s, long long *nl);
+int ppi_energy(const ppi_dev *d, int mode, cudaStream_t s, long long *nl);
+int ppi_volume(const ppi_dev *d, long long sweep, cudaStream_t s, long long *nl);
+int ppi_gram_schmidt(const ppi_dev *d, int first, int count, cudaStream_t s, long long *nl);
+int ppi_reorder(const ppi_dev *d, cudaStream_t s, long long *nl);
+int ppi_sm_count(void);
+
+/* energy kernel modes */
+#define PPI_EN_BONDS 0    /* per-slot bond/overlap counts + per-replica sum into rs.vol_bonds */
+#define PPI_EN_VOLUME 1   /* NPT candidate box: per-replica sums only */
+#define PPI_EN_PARTNERS 2 /* as BONDS, and bonded partner ids per slot into out_partners */
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PPGPU_INTERNAL_H_ */

@@ -1,0 +1,66 @@
+"""The reference file formats and the seeded generator of the product (include/ppgpu.h, host-only functions)."""
+import gzip
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+from tests import helpers
+import patchyparticles_gb300 as pp
+from oracle import pyoracle as po
+
+
+@pytest.mark.parametrize("N,rho,seed", [(300, 0.3, 4242), (1000, 0.1, 1001)])
+def test_generator_reproduces_reference_generator(built, N, rho, seed):
+    p = helpers.unpack_golden("generator_%d_%s_%d.rrr" % (N, rho, seed))
+    _, r, R, box = pp.read_rrr(p)
+    g_r, g_R, g_box = pp.generate(N, rho, seed, round_like_file=True)
+    assert np.array_equal(r, g_r) and np.array_equal(R, g_R) and np.array_equal(box, g_box)
+
+
+def test_generator_rejects_dense(built):
+    with pytest.raises(pp.PPError):
+        pp.generate(100, 0.75, 1)
+
+
+def test_generated_config_has_no_overlap(built):
+    r, R, box = pp.generate(2000, 0.6, 3, round_like_file=False)
+    s = po.System(po.params(), arrays=(r, R, box))
+    _, ov = s.init_energy()
+    assert not ov
+    M = R.reshape(-1, 3, 3)
+    assert np.allclose(np.linalg.det(M), 1.0, atol=1e-12)
+
+
+@pytest.mark.parametrize("name", ["fcc", "bcc", "adversarial"])
+def test_reader_bit_identical_to_reference_loader(built, name):
+    path = helpers.unpack_golden(name + ".rrr")
+    _, r, R, box = pp.read_rrr(path)
+    s = po.System(po.params(), path=path)
+    orr, oR = s.state()
+    assert np.array_equal(r, orr) and np.array_equal(R, oR) and np.array_equal(box, s.box())
+
+
+def test_rrr_write_format_and_roundtrip(built):
+    r, R, box = helpers.config("small")
+    d = tempfile.mkdtemp()
+    p = os.path.join(d, "x.rrr")
+    pp.write_rrr(p, 123, r, R, box)
+    s = po.System(po.params(), arrays=(r, R, box))
+    q = os.path.join(d, "y.rrr")
+    s.save(q, 123)
+    assert open(p).read() == open(q).read()
+    step, N, b = pp.rrr_header(p)
+    assert step == 123 and N == len(r)
+
+
+def test_reader_rejects_short_file(built):
+    d = tempfile.mkdtemp()
+    p = os.path.join(d, "bad.rrr")
+    open(p, "w").write("0 3 10 10 10\n1 0 0\n0 1 0\n1 1 1\n")
+    with pytest.raises(pp.PPError):
+        pp.read_rrr(p)
+    open(p, "w").write("")
+    with pytest.raises(pp.PPError):
+        pp.rrr_header(p)
