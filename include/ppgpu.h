@@ -155,6 +155,29 @@ int pp_gpu_kernel_stats(pp_engine *e, pp_kernel_stats *out, int reset);
  * elapsed device time in *ms. */
 int pp_gpu_time_sweeps(pp_engine *e, long long n, double *ms);
 
+/* Allocation-free energy of one configuration (no counterpart in the reference: an addition for callers
+ * that may not allocate device memory themselves -- hosts that run the engine inside a device-memory
+ * budget or pool owned by someone else, and latency-sensitive loops, where cudaMalloc/cudaFree could
+ * fail or stall the whole device with their implicit synchronisation).
+ *
+ * The caller passes device pointers: r_dev (N x 3 doubles) and R_dev (N x 9 doubles, orientation rows),
+ * and optionally n_bonds_dev / n_overlaps_dev (N ints each, may be NULL), which receive the per-particle
+ * bond and overlap counts in input order, as pp_gpu_bonds does. *E receives 0.5 * sum_i MC_energy(i)
+ * (main.c:55-64 semantics; -bonds) and *overlap whether any pair overlaps. Model: KF_delta, KF_cosmax,
+ * FP32 pair tests with the FP64 guard band (eps = 1e-5), bit-identical decisions to the reference.
+ *
+ * Nothing is allocated: all scratch (cell grid, sort buffers, working records) lives in one static
+ * device array of about 8.8 MB, which every GPU that loads the library holds until the process exits.
+ * Limits: N <= 32768 particles and at most 131072 cells (even cell count >= 4 per axis, cell edge >=
+ * 1 + KF_delta, i.e. roughly a 57^3 box at delta = 0.12); larger inputs return PP_ERR_CAPACITY with a
+ * message in err (err may be NULL). The first call on a device looks up the array's device address with
+ * cudaGetSymbolAddress (once per device); make that first call before any stream capture. Calls share
+ * the array and run on the legacy default stream and return after the result is on the host: calls that
+ * overlap on the GPU (from several host threads) race on the shared scratch and must be serialised by
+ * the caller. Returns PP_OK, PP_ERR_ARG, PP_ERR_CAPACITY or PP_ERR_CUDA. */
+int pp_gpu_energy_noalloc(int N, const double *r_dev, const double *R_dev, const double box[3], double kf_delta, double kf_cosmax,
+		int *n_bonds_dev, int *n_overlaps_dev, double *E, int *overlap, char *err, int err_len);
+
 /* Number of replicas, particles of a replica, current box of a replica. */
 int pp_gpu_num_replicas(const pp_engine *e);
 int pp_gpu_num_particles(const pp_engine *e, int replica);

@@ -93,6 +93,7 @@ EXPORTED = [
     "pp_gpu_bond_lists", "pp_gpu_guard_stats", "pp_gpu_num_replicas", "pp_gpu_num_particles", "pp_gpu_box",
     "pp_gpu_launch_count", "pp_gpu_last_error", "pp_gpu_destroy", "pp_rrr_header", "pp_rrr_read", "pp_rrr_write",
     "pp_generate", "pp_gpu_select_device", "pp_gpu_set_timing", "pp_gpu_kernel_stats", "pp_gpu_time_sweeps",
+    "pp_gpu_energy_noalloc",
 ]
 
 

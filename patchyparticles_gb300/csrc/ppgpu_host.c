@@ -243,6 +243,23 @@ void pp_gpu_destroy(pp_engine *e) {
 /* layout                                                                                           */
 /* ------------------------------------------------------------------------------------------------ */
 /* fills per-replica derived parameters; returns PP_OK or an error */
+void ppi_model_params(int N, double kf_delta, double kf_cosmax, ppi_rparams *rp) {
+	memset(rp, 0, sizeof(*rp));
+	rp->N = N;
+	rp->ensemble = PP_NVT;
+	rp->T = 1.0;
+	rp->cosmax = kf_cosmax;
+	rp->sqr_rcut = (1. + kf_delta) * (1. + kf_delta); /* system.c:86 */
+	rp->r_cut = 1. + kf_delta;                        /* system.c:249 */
+	h_base_patches(rp->base);
+	rp->w_min = rp->r_cut + 1e-5;
+	rp->cosmax_f = (float) rp->cosmax;
+	rp->sqr_rcut_f = (float) rp->sqr_rcut;
+	rp->eps_f = 1e-5f;
+	rp->base_f = (float) fabs(rp->base[0][0]);
+	rp->seed = 1;
+}
+
 static int derive_rparams(pp_engine *e, int r, ppi_rparams *rp) {
 	const pp_params *p = e->prm + r;
 	memset(rp, 0, sizeof(*rp));

@@ -121,6 +121,10 @@ int ppi_gram_schmidt(const ppi_dev *d, int first, int count, cudaStream_t s, lon
 int ppi_reorder(const ppi_dev *d, cudaStream_t s, long long *nl);
 int ppi_sm_count(void);
 
+/* model parameters of one NVT system of N particles (exact FP64 base patches, FP32 thresholds),
+ * without cell capacities; defined in ppgpu_host.c (compiled with -ffp-contract=off) */
+void ppi_model_params(int N, double kf_delta, double kf_cosmax, ppi_rparams *rp);
+
 /* energy kernel modes */
 #define PPI_EN_BONDS 0    /* per-slot bond/overlap counts + per-replica sum into rs.vol_bonds */
 #define PPI_EN_VOLUME 1   /* NPT candidate box: per-replica sums only */

@@ -15,11 +15,14 @@
  * k_energy: energy from scratch (per-particle bonds/overlaps, output.c:213-268) or of the NPT candidate
  * box (MC.c:487-495); k_vol_*: the NPT volume move (MC.c:450-513).
  */
+#include "ppgpu.h"
 #include "ppgpu_internal.h"
 
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
+#include <stdio.h>
+#include <string.h>
 
 /* ------------------------------------------------------------------------------------------------ */
 /* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3", SC'11)   */
@@ -1040,4 +1043,146 @@ extern "C" int ppi_reorder(const ppi_dev *d, cudaStream_t s, long long *nl) {
 	cudaMemcpyAsync(d->rec, d->tmp_rec, sizeof(double) * PPI_REC * (size_t) d->ntot, cudaMemcpyDeviceToDevice, s);
 	cudaMemcpyAsync(d->id, d->tmp_id, sizeof(int) * (size_t) d->ntot, cudaMemcpyDeviceToDevice, s);
 	return (int) cudaGetLastError();
+}
+
+/* ------------------------------------------------------------------------------------------------ */
+/* allocation-free energy of one configuration (pp_gpu_energy_noalloc)                               */
+/*                                                                                                  */
+/* For callers that may not allocate device memory: every scratch buffer of the energy pass (cell     */
+/* grid, counting sort, FP32 working records, FP64 records) is carved out of one file-scope device    */
+/* array of fixed size, so a call allocates nothing. The kernels are the engine's own (k_grid ...    */
+/* k_energy), given a ppi_dev view whose pointers lie inside the array.                               */
+/* ------------------------------------------------------------------------------------------------ */
+#define NOALLOC_N 32768      /* particles */
+#define NOALLOC_CELLS 131072 /* cells of the grid (even count >= 4 per axis, edge >= r_cut) */
+#define NA_ALIGN(x) ((((size_t) (x)) + 255) & ~(size_t) 255)
+#define NA_REC ((size_t) 0)
+#define NA_STAGE (NA_REC + NA_ALIGN((size_t) NOALLOC_N * PPI_REC * sizeof(double)))
+#define NA_SREC (NA_STAGE + NA_ALIGN((size_t) NOALLOC_N * sizeof(float4)))
+#define NA_ID (NA_SREC + NA_ALIGN((size_t) NOALLOC_N * 4 * sizeof(float4)))
+#define NA_REP (NA_ID + NA_ALIGN((size_t) NOALLOC_N * sizeof(int)))
+#define NA_CELLOF (NA_REP + NA_ALIGN((size_t) NOALLOC_N * sizeof(int)))
+#define NA_BONDS (NA_CELLOF + NA_ALIGN((size_t) NOALLOC_N * sizeof(int)))
+#define NA_OVER (NA_BONDS + NA_ALIGN((size_t) NOALLOC_N * sizeof(int)))
+#define NA_CCOUNT (NA_OVER + NA_ALIGN((size_t) NOALLOC_N * sizeof(int)))
+#define NA_CSTART (NA_CCOUNT + NA_ALIGN((size_t) NOALLOC_CELLS * sizeof(int)))
+#define NA_CCURSOR (NA_CSTART + NA_ALIGN((size_t) (NOALLOC_CELLS + 1) * sizeof(int)))
+#define NA_CREP (NA_CCURSOR + NA_ALIGN((size_t) NOALLOC_CELLS * sizeof(int)))
+#define NA_AUX (NA_CREP + NA_ALIGN((size_t) NOALLOC_CELLS * sizeof(int)))
+#define NA_CLIST (NA_AUX + NA_ALIGN((size_t) (NOALLOC_CELLS / 1024 + 2) * sizeof(int)))
+#define NA_COLCOUNT (NA_CLIST + NA_ALIGN((size_t) 8 * (NOALLOC_CELLS / 8 + 8) * sizeof(int)))
+#define NA_RP (NA_COLCOUNT + NA_ALIGN(8 * sizeof(int)))
+#define NA_RS (NA_RP + NA_ALIGN(sizeof(ppi_rparams)))
+#define NA_GRID (NA_RS + NA_ALIGN(sizeof(ppi_rstate)))
+#define NA_TOTAL (NA_GRID + NA_ALIGN(sizeof(ppi_grid)))
+
+/* The scratch. Host code must not use its name as an address: the device address comes from
+ * cudaGetSymbolAddress (g_noalloc_base, once per device). */
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_TOTAL];
+
+#define NOALLOC_MAX_DEVICES 64
+static void *g_noalloc_base[NOALLOC_MAX_DEVICES];
+
+__global__ void k_noalloc_pack(ppi_dev d, const double *r, const double *R) {
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= d.ntot) return;
+	double *o = d.rec + (size_t) i * PPI_REC;
+	o[0] = r[3 * (size_t) i];
+	o[1] = r[3 * (size_t) i + 1];
+	o[2] = r[3 * (size_t) i + 2];
+	for(int k = 0; k < 9; k++) o[3 + k] = R[9 * (size_t) i + k];
+	d.id[i] = i;
+	d.rep[i] = 0;
+}
+
+static int na_fail(char *err, int err_len, int code, const char *msg, const char *detail) {
+	if(err && err_len > 0) snprintf(err, err_len, "%s%s%s", msg, detail ? ": " : "", detail ? detail : "");
+	return code;
+}
+
+extern "C" int pp_gpu_energy_noalloc(int N, const double *r_dev, const double *R_dev, const double box[3], double kf_delta, double kf_cosmax,
+		int *n_bonds_dev, int *n_overlaps_dev, double *E, int *overlap, char *err, int err_len) {
+	if(err && err_len > 0) err[0] = '\0';
+	if(box == NULL || E == NULL || overlap == NULL || N < 0 || (N > 0 && (r_dev == NULL || R_dev == NULL)))
+		return na_fail(err, err_len, PP_ERR_ARG, "invalid arguments", NULL);
+	if(!(kf_delta > 0. && kf_delta < 1.) || !(kf_cosmax > -1. && kf_cosmax < 1.)) return na_fail(err, err_len, PP_ERR_ARG, "KF_delta or KF_cosmax out of range", NULL);
+	if(N > NOALLOC_N) {
+		char b[96];
+		snprintf(b, sizeof(b), "N = %d exceeds the static capacity of %d particles", N, NOALLOC_N);
+		return na_fail(err, err_len, PP_ERR_CAPACITY, "pp_gpu_energy_noalloc", b);
+	}
+	ppi_rparams rp;
+	ppi_model_params(N, kf_delta, kf_cosmax, &rp);
+	long long cells = 1;
+	for(int a = 0; a < 3; a++) {
+		if(!(box[a] > 0.)) return na_fail(err, err_len, PP_ERR_ARG, "box sides must be positive", NULL);
+		int n = (int) floor(box[a] / rp.w_min);
+		if(n > PPI_MAX_AXIS_CELLS) n = PPI_MAX_AXIS_CELLS;
+		n &= ~1;
+		if(n < 4) return na_fail(err, err_len, PP_ERR_CAPACITY, "pp_gpu_energy_noalloc", "a box side is shorter than 4 cells of edge 1 + KF_delta");
+		cells *= n;
+	}
+	if(cells > NOALLOC_CELLS) {
+		char b[96];
+		snprintf(b, sizeof(b), "the box needs %lld cells, the static capacity is %d", cells, NOALLOC_CELLS);
+		return na_fail(err, err_len, PP_ERR_CAPACITY, "pp_gpu_energy_noalloc", b);
+	}
+	rp.cell_base = 0;
+	rp.cell_cap = (int) cells;
+	rp.p0 = 0;
+	/* device address of the scratch, looked up once per device with that device current */
+	int dev = 0;
+	cudaError_t c = cudaGetDevice(&dev);
+	if(c != cudaSuccess) return na_fail(err, err_len, PP_ERR_CUDA, "cudaGetDevice", cudaGetErrorString(c));
+	if(dev < 0 || dev >= NOALLOC_MAX_DEVICES) return na_fail(err, err_len, PP_ERR_CUDA, "device ordinal out of range", NULL);
+	if(g_noalloc_base[dev] == NULL) {
+		void *p = NULL;
+		c = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+		if(c != cudaSuccess || p == NULL) return na_fail(err, err_len, PP_ERR_CUDA, "cudaGetSymbolAddress", cudaGetErrorString(c));
+		g_noalloc_base[dev] = p;
+	}
+	unsigned char *base = (unsigned char *) g_noalloc_base[dev];
+	ppi_dev d;
+	memset(&d, 0, sizeof(d));
+	d.nrep = 1;
+	d.ntot = N;
+	d.total_cells = (int) cells;
+	d.clist_cap = (int) (cells / 8 + 8);
+	d.rec = (double *) (base + NA_REC);
+	d.tmp_rec = (double *) (base + NA_STAGE); /* float4 staging of the cell assignment */
+	d.srec = (float4 *) (base + NA_SREC);
+	d.id = (int *) (base + NA_ID);
+	d.rep = (int *) (base + NA_REP);
+	d.cellof = (int *) (base + NA_CELLOF);
+	d.out_bonds = n_bonds_dev ? n_bonds_dev : (int *) (base + NA_BONDS);
+	d.out_overlaps = n_overlaps_dev ? n_overlaps_dev : (int *) (base + NA_OVER);
+	d.cell_count = (int *) (base + NA_CCOUNT);
+	d.cell_start = (int *) (base + NA_CSTART);
+	d.cell_cursor = (int *) (base + NA_CCURSOR);
+	d.cell_rep = (int *) (base + NA_CREP);
+	d.scan_aux = (int *) (base + NA_AUX);
+	d.clist = (int *) (base + NA_CLIST);
+	d.ccount = (int *) (base + NA_COLCOUNT);
+	d.rp = (ppi_rparams *) (base + NA_RP);
+	d.rs = (ppi_rstate *) (base + NA_RS);
+	d.grid = (ppi_grid *) (base + NA_GRID);
+	/* the array keeps the previous call's contents: everything this call reads is written first */
+	ppi_rstate rs;
+	memset(&rs, 0, sizeof(rs));
+	for(int a = 0; a < 3; a++) rs.box[a] = box[a];
+	rs.V = box[0] * box[1] * box[2];
+	if((c = cudaMemcpy(d.rp, &rp, sizeof(rp), cudaMemcpyHostToDevice)) != cudaSuccess ||
+			(c = cudaMemcpy(d.rs, &rs, sizeof(rs), cudaMemcpyHostToDevice)) != cudaSuccess ||
+			(c = cudaMemset(d.grid, 0, sizeof(ppi_grid))) != cudaSuccess || (c = cudaMemset(d.cell_rep, 0, sizeof(int) * (size_t) cells)) != cudaSuccess)
+		return na_fail(err, err_len, PP_ERR_CUDA, "scratch set-up", cudaGetErrorString(c));
+	long long nl = 0;
+	if(N > 0) k_noalloc_pack<<<(N + 255) / 256, 256>>>(d, r_dev, R_dev);
+	int rc = ppi_resort(&d, 0, 0, &nl);
+	if(rc == 0) rc = ppi_energy(&d, PPI_EN_BONDS, 0, &nl);
+	if(rc != 0) return na_fail(err, err_len, PP_ERR_CUDA, "kernel launch", cudaGetErrorString((cudaError_t) rc));
+	if((c = cudaMemcpy(&rs, d.rs, sizeof(rs), cudaMemcpyDeviceToHost)) != cudaSuccess) return na_fail(err, err_len, PP_ERR_CUDA, "result copy", cudaGetErrorString(c));
+	if(rs.error) return na_fail(err, err_len, PP_ERR_CAPACITY, "pp_gpu_energy_noalloc", "cell grid error on the device");
+	*E = -0.5 * (double) rs.vol_bonds;
+	*overlap = rs.vol_overlap;
+	return PP_OK;
 }
