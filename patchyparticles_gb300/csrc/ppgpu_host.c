@@ -42,6 +42,7 @@ struct pp_engine {
 	int rounds_per_sweep; /* checkerboard rounds per MC step */
 	int reorder_every;    /* re-sorts between physical reorders of the FP64 state */
 	int any_npt;
+	int any_audit;
 	/* event timing */
 	int timing;
 	int n_ev;
@@ -180,6 +181,7 @@ static int create_common(const pp_params *prms, int n, pp_engine **out) {
 	for(int i = 0; i < n; i++) {
 		if(e->prm[i].guard_eps <= 0.) e->prm[i].guard_eps = 1e-5;
 		if(e->prm[i].ensemble == PP_NPT) e->any_npt = 1;
+		if(e->prm[i].audit) e->any_audit = 1;
 	}
 	if(e->prm[0].resort_every > 0) e->resort_every = e->prm[0].resort_every;
 	cudaError_t c = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
@@ -197,7 +199,7 @@ int pp_gpu_num_particles(const pp_engine *e, int r) { return (e && r >= 0 && r <
 long long pp_gpu_launch_count(const pp_engine *e) { return e ? e->launches : 0; }
 
 static void free_device(pp_engine *e) {
-	void **ptrs[] = { (void **) &e->d.rec, (void **) &e->d.srec, (void **) &e->d.id, (void **) &e->d.rep, (void **) &e->d.cellof,
+	void **ptrs[] = { (void **) &e->d.rec, (void **) &e->d.spos, (void **) &e->d.sori, (void **) &e->d.id, (void **) &e->d.rep, (void **) &e->d.cellof,
 		(void **) &e->d.cell_count, (void **) &e->d.cell_start, (void **) &e->d.cell_cursor, (void **) &e->d.cell_rep, (void **) &e->d.scan_aux,
 		(void **) &e->d.clist, (void **) &e->d.ccount, (void **) &e->d.rp, (void **) &e->d.rs, (void **) &e->d.grid, (void **) &e->d.out_bonds,
 		(void **) &e->d.out_overlaps, (void **) &e->d.out_partners, (void **) &e->d.tmp_rec, (void **) &e->d.tmp_id };
@@ -387,7 +389,8 @@ static int commit(pp_engine *e) {
 	d->clist_cap = (int) (cells / 8 + e->nrep + 8);
 	size_t n1 = ntot > 0 ? (size_t) ntot : 1;
 	CU(cudaMalloc((void **) &d->rec, sizeof(double) * PPI_REC * n1));
-	CU(cudaMalloc((void **) &d->srec, sizeof(float) * 16 * n1));
+	CU(cudaMalloc((void **) &d->spos, sizeof(float) * 4 * n1));
+	CU(cudaMalloc((void **) &d->sori, sizeof(float) * 12 * n1));
 	CU(cudaMalloc((void **) &d->id, sizeof(int) * n1));
 	CU(cudaMalloc((void **) &d->rep, sizeof(int) * n1));
 	CU(cudaMalloc((void **) &d->cellof, sizeof(int) * n1));
@@ -401,8 +404,13 @@ static int commit(pp_engine *e) {
 	CU(cudaMalloc((void **) &d->cell_cursor, sizeof(int) * cells));
 	CU(cudaMalloc((void **) &d->cell_rep, sizeof(int) * cells));
 	CU(cudaMalloc((void **) &d->scan_aux, sizeof(int) * ((cells + 1023) / 1024 + 1)));
-	CU(cudaMalloc((void **) &d->clist, sizeof(int) * 8 * (size_t) d->clist_cap));
+	CU(cudaMalloc((void **) &d->clist, sizeof(int4) * 8 * (size_t) d->clist_cap));
 	CU(cudaMalloc((void **) &d->ccount, sizeof(int) * 8));
+	d->audit_any = e->any_audit;
+	{ /* lanes per attempt: a tuning override for measurements (4 by default) */
+		const char *v = getenv("PPGPU_LANES");
+		d->lanes = (v && atoi(v) == 8) ? 8 : 4;
+	}
 	CU(cudaMalloc((void **) &d->rp, sizeof(ppi_rparams) * e->nrep));
 	CU(cudaMalloc((void **) &d->rs, sizeof(ppi_rstate) * e->nrep));
 	CU(cudaMalloc((void **) &d->grid, sizeof(ppi_grid) * e->nrep));
@@ -438,7 +446,11 @@ static int push_replica(pp_engine *e, int r, const double *rr, const double *RR)
 		dst[0] = rr[3 * i];
 		dst[1] = rr[3 * i + 1];
 		dst[2] = rr[3 * i + 2];
-		memcpy(dst + 3, RR + 9 * (size_t) i, 9 * sizeof(double));
+		dst[PPI_Q] = 1.0; /* accumulated rotation: identity, so R = R0 is the uploaded matrix bit for bit */
+		dst[PPI_Q + 1] = 0.0;
+		dst[PPI_Q + 2] = 0.0;
+		dst[PPI_Q + 3] = 0.0;
+		memcpy(dst + PPI_R0, RR + 9 * (size_t) i, 9 * sizeof(double));
 		e->pin_id[i] = i;
 	}
 	CU(cudaMemcpyAsync(e->d.rec + (size_t) rp->p0 * PPI_REC, e->pin_rec, sizeof(double) * PPI_REC * N, cudaMemcpyHostToDevice, e->stream));
@@ -656,7 +668,7 @@ int pp_gpu_sweeps(pp_engine *e, long long n) {
 			int colours[8];
 			colour_order(e->round_counter, colours);
 			if((rc = ev_begin(e, 1, &ev)) != PP_OK) return rc;
-			CK(ppi_round(&e->d, e->round_counter, colours, e->stream, &nl));
+			CK(ppi_round(&e->d, e->round_counter, colours, e->any_audit, e->stream, &nl));
 			if((rc = ev_end(e, ev)) != PP_OK) return rc;
 			e->round_counter++;
 			e->launches += nl;
@@ -824,13 +836,16 @@ int pp_gpu_download_replica(pp_engine *e, int r, double *rr, double *RR, double 
 	if(rc != PP_OK) return rc;
 	ppi_rparams *rp = e->h_rp + r;
 	int N = rp->N;
-	CU(cudaMemcpyAsync(e->pin_rec, e->d.rec + (size_t) rp->p0 * PPI_REC, sizeof(double) * PPI_REC * N, cudaMemcpyDeviceToHost, e->stream));
+	long long nl = 0;
+	CK(ppi_export(&e->d, rp->p0, N, e->stream, &nl)); /* x y z R = R0 . Q(q), 12 doubles per slot */
+	e->launches += nl;
+	CU(cudaMemcpyAsync(e->pin_rec, e->d.tmp_rec, sizeof(double) * 12 * N, cudaMemcpyDeviceToHost, e->stream));
 	CU(cudaMemcpyAsync(e->pin_id, e->d.id + rp->p0, sizeof(int) * N, cudaMemcpyDeviceToHost, e->stream));
 	CU(cudaStreamSynchronize(e->stream));
 	for(int k = 0; k < N; k++) {
 		int i = e->pin_id[k];
 		if(i < 0 || i >= N) return set_err(e, PP_ERR_STATE, "corrupt particle ids");
-		const double *src = e->pin_rec + (size_t) k * PPI_REC;
+		const double *src = e->pin_rec + (size_t) k * 12;
 		if(rr) memcpy(rr + 3 * (size_t) i, src, 3 * sizeof(double));
 		if(RR) memcpy(RR + 9 * (size_t) i, src + 3, 9 * sizeof(double));
 	}

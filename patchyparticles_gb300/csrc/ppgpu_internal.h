@@ -3,17 +3,24 @@
  * (ppgpu_kernels.cu). Plain C structs; no torch types.
  *
  * Device memory (one engine = R replicas; particle "slots" are global over replicas):
- *   rec[slot]   12 doubles: canonical FP64 state, x y z (unwrapped) then orientation rows R00..R22
- *               (96 B = three 32-B sectors). Only FP64 arithmetic ever writes it.
- *   srec[k]     64-B FP32 working record of the particle at cell-sorted position k:
- *                 a = (lx, ly, lz, slot)       cell-local position, 0 <= l < w
- *                 b = (c0x, c0y, c0z, c1x)     orientation columns c_j = (R0j, R1j, R2j)
- *                 c = (c1y, c1z, c2x, c2y)
- *                 d = (c2z, id, cell, -)       particle id (upload order), global cell index
- *               Rebuilt from rec every `resort_every` rounds; updated in FP32 by accepted moves in between.
+ *   rec[slot]   16 doubles, the canonical FP64 state:
+ *                 [0..2]  x y z (unwrapped position)
+ *                 [3..6]  q = (w, x, y, z), accumulated rotation quaternion (not normalised)
+ *                 [7..15] R0, orientation rows at upload (or at the last orthonormalisation)
+ *               The orientation is R = R0 . Q(q) with Q the rotation matrix of q / |q| (orient64), so an
+ *               accepted rotation costs one FP64 quaternion product instead of a 3x3 matrix product, and
+ *               an uploaded orientation is reproduced bit for bit while q is the identity.
+ *               Only FP64 arithmetic ever writes it.
+ *   spos[k]     float4 (lx, ly, lz, slot) of the particle at cell-sorted position k, cell-local, 0 <= l < w
+ *   sori[3k..]  3 x float4 orientation columns c_j = (R0j, R1j, R2j) of the same particle:
+ *                 (c0x, c0y, c0z, c1x) (c1y, c1z, c2x, c2y) (c2z, id, cell, -)
+ *               id = particle index in its replica, cell = global cell index.
+ *               spos/sori are rebuilt from rec every `resort_every` rounds and updated in FP32 by accepted
+ *               moves in between; the distance filter reads only spos (16 B per candidate).
  *   cell_start  per replica n_x*n_y*n_z + 1 entries (global cell index = replica cell base + local index,
- *               local index = (cz * n_y + cy) * n_x + cx), particles of a cell contiguous in srec.
- *   clist       per colour (8), the non-empty cells of that checkerboard colour (global cell indices).
+ *               local index = (cz * n_y + cy) * n_x + cx), particles of a cell contiguous in spos/sori.
+ *   clist       per colour (8), the non-empty cells of that checkerboard colour as int4 (global cell,
+ *               first sorted position, particle count, replica).
  */
 #ifndef PPGPU_INTERNAL_H_
 #define PPGPU_INTERNAL_H_
@@ -25,7 +32,9 @@
 extern "C" {
 #endif
 
-#define PPI_REC 12
+#define PPI_REC 16
+#define PPI_Q 3   /* offset of q in rec */
+#define PPI_R0 7  /* offset of R0 in rec */
 #define PPI_MAX_AXIS_CELLS 1024
 
 /* error codes written by kernels into ppi_rstate.error */
@@ -87,7 +96,8 @@ typedef struct ppi_dev {
 	int total_cells;   /* sum of cell caps */
 	int pad;
 	double *rec;
-	float4 *srec;      /* 4 x float4 per particle */
+	float4 *spos;      /* 1 x float4 per particle */
+	float4 *sori;      /* 3 x float4 per particle */
 	int *id;           /* slot -> particle index in its replica */
 	int *rep;          /* slot -> replica */
 	int *cellof;       /* slot -> global cell (current grid) */
@@ -96,8 +106,10 @@ typedef struct ppi_dev {
 	int *cell_cursor;
 	int *cell_rep;     /* global cell -> replica */
 	int *scan_aux;
-	int *clist;        /* 8 lists of capacity total_cells / 8 + nrep each */
+	int4 *clist;       /* 8 lists of capacity clist_cap each */
 	int *ccount;       /* 8 counters */
+	int audit_any;     /* some replica audits: every pass runs in audit mode */
+	int lanes;         /* lanes per attempt of the colour and energy passes (4 or 8; 0 = default) */
 	int clist_cap;
 	int pad1;
 	ppi_rparams *rp;
@@ -106,7 +118,7 @@ typedef struct ppi_dev {
 	int *out_bonds;    /* per slot */
 	int *out_overlaps;
 	int *out_partners; /* bond lists: per slot up to PPI_MAX_PARTNERS */
-	double *tmp_rec;   /* reorder scratch */
+	double *tmp_rec;   /* reorder / export scratch (ntot records) */
 	int *tmp_id;
 } ppi_dev;
 
@@ -114,11 +126,13 @@ typedef struct ppi_dev {
 
 /* launchers (ppgpu_kernels.cu); each returns a cudaError_t value as int and adds its launches to *nl */
 int ppi_resort(const ppi_dev *d, long long epoch, cudaStream_t s, long long *nl);
-int ppi_round(const ppi_dev *d, long long round, const int *colours, cudaStream_t s, long long *nl);
+int ppi_round(const ppi_dev *d, long long round, const int *colours, int audit, cudaStream_t s, long long *nl);
 int ppi_energy(const ppi_dev *d, int mode, cudaStream_t s, long long *nl);
 int ppi_volume(const ppi_dev *d, long long sweep, cudaStream_t s, long long *nl);
 int ppi_gram_schmidt(const ppi_dev *d, int first, int count, cudaStream_t s, long long *nl);
 int ppi_reorder(const ppi_dev *d, cudaStream_t s, long long *nl);
+/* writes x y z R00..R22 (12 doubles) of slots [first, first + count) into d->tmp_rec */
+int ppi_export(const ppi_dev *d, int first, int count, cudaStream_t s, long long *nl);
 int ppi_sm_count(void);
 
 /* model parameters of one NVT system of N particles (exact FP64 base patches, FP32 thresholds),

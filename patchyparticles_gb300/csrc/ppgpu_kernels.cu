@@ -2,16 +2,17 @@
  * ppgpu_kernels.cu -- sm_103a kernels of the roto-translation Monte Carlo engine (global checkerboard).
  *
  * Every `resort_every` rounds each replica gets a new cell grid (even number of cells per axis, edge >=
- * r_cut, random origin shift) and the particles are counting-sorted into cell order as 64-B FP32 working
- * records rebuilt from the FP64 canonical state:
+ * r_cut, random origin shift) and the particles are counting-sorted into cell order as FP32 working
+ * records (spos 16 B + sori 48 B) rebuilt from the FP64 canonical state:
  *   k_grid, k_assign, k_scan_*, k_scatter, k_cellfin (deterministic in-cell order, colour lists)
  * One round = the 8 colours of the 2x2x2 checkerboard, one launch each (k_colour): every non-empty
- * cell of the colour is one thread that performs one roto-translation attempt on a uniformly chosen
- * particle of the cell (MC_move_rototranslate, MC.c:311-340). Same-colour cells are never adjacent and a
- * move that leaves its cell is rejected, so concurrent moves never interact and the cell lists stay
- * valid for the whole epoch. The pair test is FP32 with an FP64 re-evaluation inside the guard band,
- * bit-identical to MC_would_interact (MC.c:232-266). Accepted moves update the FP64 state with FP64
- * arithmetic and the FP32 record in place.
+ * cell of the colour gets one roto-translation attempt on a uniformly chosen particle of the cell
+ * (MC_move_rototranslate, MC.c:311-340), run by a group of 4 (or 8) lanes that share the 27-cell
+ * neighbourhood. Same-colour cells are never adjacent and a move that leaves its cell is rejected, so
+ * concurrent moves never interact and the cell lists stay valid for the whole epoch. The pair test is
+ * FP32 with an FP64 re-evaluation inside the guard band, bit-identical to MC_would_interact
+ * (MC.c:232-266). Accepted moves update the FP64 state with FP64 arithmetic (r + disp, q (x) dq) and
+ * the FP32 record in place.
  * k_energy: energy from scratch (per-particle bonds/overlaps, output.c:213-268) or of the NPT candidate
  * box (MC.c:487-495); k_vol_*: the NPT volume move (MC.c:450-513).
  */
@@ -62,24 +63,24 @@ __device__ __forceinline__ double u01d(uint32_t a, uint32_t b) { return (double)
 /* MATRIX_VECTOR_MULTIPLICATION (utils.h:18-22). Every operation is an explicitly rounded IEEE        */
 /* operation, so nothing is contracted into an FMA and the result equals the reference's bit for bit. */
 /* ------------------------------------------------------------------------------------------------ */
-__device__ __forceinline__ void patches64(const double *R, const double (*b)[3], double *P) {
+/* patch i of an orientation: R . base_i with the MATRIX_VECTOR_MULTIPLICATION order (utils.h:18-22) */
+__device__ __forceinline__ void patch64(const double *R, const double *b, double *P) {
 #pragma unroll
-	for(int i = 0; i < 4; i++) {
-#pragma unroll
-		for(int k = 0; k < 3; k++)
-			P[3 * i + k] = __dadd_rn(__dadd_rn(__dmul_rn(R[3 * k + 0], b[i][0]), __dmul_rn(R[3 * k + 1], b[i][1])), __dmul_rn(R[3 * k + 2], b[i][2]));
-	}
+	for(int k = 0; k < 3; k++) P[k] = __dadd_rn(__dadd_rn(__dmul_rn(R[3 * k + 0], b[0]), __dmul_rn(R[3 * k + 1], b[1])), __dmul_rn(R[3 * k + 2], b[2]));
 }
 
 __device__ __forceinline__ double scalar64(const double *a, const double *b) {
 	return __dadd_rn(__dadd_rn(__dmul_rn(a[0], b[0]), __dmul_rn(a[1], b[1])), __dmul_rn(a[2], b[2]));
 }
 
-/* returns -1 overlap, 0 no bond, 1 bond; optional diagnostics (dist2, max p cosine, max q cosine) */
-__device__ int interact64(const double *rp, const double *Pp, const double *rq, const double *Pq, const double *box, double sqr_rcut, double cosmax,
-		double *o_dist2, double *o_pmax, double *o_qmax) {
+/* MC_would_interact (MC.c:232-266) for p = (rp, Rp) and q = (rq, Rq): returns -1 overlap, 0 no bond,
+ * 1 bond; optional diagnostics (dist2, max p cosine, max q cosine). Patches are formed one at a time
+ * from the orientations (same operations as the stored patches of the reference), which keeps this cold
+ * path light on registers. */
+__device__ __noinline__ int interact64(const double *rp, const double *Rp, const double *rq, const double *Rq, const double (*base)[3], const double *box, double sqr_rcut,
+		double cosmax, double *o_dist2, double *o_pmax, double *o_qmax) {
 	double d[3];
-#pragma unroll
+#pragma unroll 1
 	for(int k = 0; k < 3; k++) {
 		d[k] = __dsub_rn(rq[k], rp[k]);
 		d[k] = __dsub_rn(d[k], __dmul_rn(box[k], rint(__ddiv_rn(d[k], box[k]))));
@@ -93,15 +94,19 @@ __device__ int interact64(const double *rp, const double *Pp, const double *rq, 
 		d[0] = __ddiv_rn(d[0], norm);
 		d[1] = __ddiv_rn(d[1], norm);
 		d[2] = __ddiv_rn(d[2], norm);
-		double pmax = -2., qmax = -2.;
+		double pmax = -2., qmax = -2., P[3];
 		int pok = 0;
+#pragma unroll 1
 		for(int a = 0; a < 4; a++) {
-			double pc = scalar64(d, Pp + 3 * a);
+			patch64(Rp, base[a], P);
+			double pc = scalar64(d, P);
 			pmax = fmax(pmax, pc);
 			if(pc > cosmax) pok = 1;
 		}
+#pragma unroll 1
 		for(int b = 0; b < 4; b++) {
-			double qc = -scalar64(d, Pq + 3 * b);
+			patch64(Rq, base[b], P);
+			double qc = -scalar64(d, P);
 			qmax = fmax(qmax, qc);
 			if(pok && qc > cosmax) res = 1;
 		}
@@ -111,39 +116,104 @@ __device__ int interact64(const double *rp, const double *Pp, const double *rq, 
 	return res;
 }
 
-/* candidate FP64 state of a move: r + disp, R . Q with Q the rotation of the quaternion (w, x, y, z)
- * given in FP32 and normalised in FP64. This is the engine's definition of the proposed state;
- * FP32 tests approximate it, FP64 re-evaluations and the accepted update use exactly these bits. */
-__device__ __forceinline__ void candidate64(const double *rec, float4 q, float3 disp, double *r, double *R) {
-	double w = q.x, x = q.y, y = q.z, z = q.w;
-	double n = w * w + x * x + y * y + z * z;
-	double inv = (double) (1.0f / (float) n);
-	inv = inv * (2.0 - n * inv);
-	inv = inv * (2.0 - n * inv);
-	double s = 2.0 * inv;
+/* ------------------------------------------------------------------------------------------------ */
+/* Canonical state arithmetic                                                                       */
+/* ------------------------------------------------------------------------------------------------ */
+/* exact FP32 -> FP64 widening by bit manipulation (integer pipe; the FP64 pipe is the scarce one);
+ * equal to (double) f for every finite f */
+__device__ __forceinline__ double f2d(float f) {
+	uint32_t b = __float_as_uint(f);
+	uint32_t e = (b >> 23) & 0xffu;
+	if(e == 0u) return (double) f; /* zero or subnormal */
+	uint32_t hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
+	return __hiloint2double((int) hi, (int) (b << 29));
+}
+
+/* FP64 -> FP32 rounded to nearest (ties away from zero) by bit manipulation; magnitudes below the FP32
+ * normal range become zero. Used only for the FP32 working copies, whose error budget is ~1e-7. */
+__device__ __forceinline__ float d2f(double x) {
+	unsigned long long u = (unsigned long long) __double_as_longlong(x);
+	uint32_t s = (uint32_t) (u >> 32) & 0x80000000u;
+	u = (u & 0x7fffffffffffffffull) + 0x10000000ull;
+	int e = (int) (u >> 52) - 896;
+	if(e <= 0) return __uint_as_float(s);
+	return __uint_as_float(s | ((uint32_t) e << 23) | ((uint32_t) (u >> 29) & 0x7fffffu));
+}
+
+/* Component c of the Hamilton product a (x) b, with a_{c^k} given as ac[k]:
+ *   w' = aw bw - ax bx - ay by - az bz      x' = ax bw + aw bx - az by + ay bz
+ *   y' = ay bw + az bx + aw by - ax bz      z' = az bw - ay bx + ax by + aw bz
+ * i.e. c' = sum_k s(c, k) a_{c^k} b_k with the sign pattern 0x284E (one nibble per c, bit k = minus).
+ * One fixed sequence of explicitly rounded operations for every c, so the lanes of a group compute
+ * their components without divergence and the full product (qmul64) is bit-identical. */
+__device__ __forceinline__ double qcomp64(double a0, double a1, double a2, double a3, const double *b, int c) {
+	const int m = (0x284E >> (4 * c)) & 0xF;
+	double v = __dmul_rn(a0, b[0]);
+	v = __fma_rn((m & 2) ? -a1 : a1, b[1], v);
+	v = __fma_rn((m & 4) ? -a2 : a2, b[2], v);
+	v = __fma_rn((m & 8) ? -a3 : a3, b[3], v);
+	return v;
+}
+
+__device__ __forceinline__ void qmul64(const double *a, const double *b, double *out) {
+#pragma unroll 1
+	for(int c = 0; c < 4; c++) out[c] = qcomp64(a[c], a[c ^ 1], a[c ^ 2], a[c ^ 3], b, c);
+}
+
+/* rotation matrix of q / |q| (rows), q = (w, x, y, z); the identity quaternion gives exactly I */
+__device__ __forceinline__ void quatmat64(const double *q, double *Q) {
+	const double w = q[0], x = q[1], y = q[2], z = q[3];
+	const double xx = __dmul_rn(x, x), yy = __dmul_rn(y, y), zz = __dmul_rn(z, z), ww = __dmul_rn(w, w);
+	const double xy = __dmul_rn(x, y), xz = __dmul_rn(x, z), yz = __dmul_rn(y, z);
+	const double wx = __dmul_rn(w, x), wy = __dmul_rn(w, y), wz = __dmul_rn(w, z);
+	const double s = __ddiv_rn(2.0, __dadd_rn(__dadd_rn(ww, xx), __dadd_rn(yy, zz)));
+	Q[0] = __dsub_rn(1.0, __dmul_rn(s, __dadd_rn(yy, zz)));
+	Q[1] = __dmul_rn(s, __dsub_rn(xy, wz));
+	Q[2] = __dmul_rn(s, __dadd_rn(xz, wy));
+	Q[3] = __dmul_rn(s, __dadd_rn(xy, wz));
+	Q[4] = __dsub_rn(1.0, __dmul_rn(s, __dadd_rn(xx, zz)));
+	Q[5] = __dmul_rn(s, __dsub_rn(yz, wx));
+	Q[6] = __dmul_rn(s, __dsub_rn(xz, wy));
+	Q[7] = __dmul_rn(s, __dadd_rn(yz, wx));
+	Q[8] = __dsub_rn(1.0, __dmul_rn(s, __dadd_rn(xx, yy)));
+}
+
+/* orientation R = R0 . Q(q) of a canonical record. With q the identity (every particle after upload or
+ * orthonormalisation) the result is R0 bit for bit (up to the sign of zero entries, which no test of
+ * MC_would_interact can see). */
+__device__ __noinline__ void orient64(const double *R0, const double *q, double *R) {
 	double Q[9];
-	Q[0] = 1.0 - s * (y * y + z * z);
-	Q[1] = s * (x * y - w * z);
-	Q[2] = s * (x * z + w * y);
-	Q[3] = s * (x * y + w * z);
-	Q[4] = 1.0 - s * (x * x + z * z);
-	Q[5] = s * (y * z - w * x);
-	Q[6] = s * (x * z - w * y);
-	Q[7] = s * (y * z + w * x);
-	Q[8] = 1.0 - s * (x * x + y * y);
-#pragma unroll
-	for(int k = 0; k < 3; k++) {
-#pragma unroll
-		for(int j = 0; j < 3; j++) {
-			double acc = rec[3 + 3 * k + 0] * Q[0 + j];
-			acc = fma(rec[3 + 3 * k + 1], Q[3 + j], acc);
-			acc = fma(rec[3 + 3 * k + 2], Q[6 + j], acc);
-			R[3 * k + j] = acc;
-		}
+	quatmat64(q, Q);
+#pragma unroll 1
+	for(int i = 0; i < 3; i++)
+#pragma unroll 1
+		for(int j = 0; j < 3; j++)
+			R[3 * i + j] = __dadd_rn(__dadd_rn(__dmul_rn(R0[3 * i], Q[j]), __dmul_rn(R0[3 * i + 1], Q[3 + j])), __dmul_rn(R0[3 * i + 2], Q[6 + j]));
+}
+
+/* Canonical state of particle slot ps as (x y z R00..R22): kind 0 = stored state, kind 1 = the candidate
+ * of the current move, r + disp and q (x) dq with disp and dq the FP32 proposal widened exactly. This is
+ * the engine's definition of the proposed state: FP32 tests approximate it, FP64 re-evaluations use it
+ * and an accepted move stores exactly these q and r bits (k_colour's commit uses the same qcomp64). */
+__device__ __noinline__ void state64(const double *__restrict__ rec_all, int ps, int kind, float4 dq, float3 disp, double *P) {
+	const double *rec = rec_all + (size_t) ps * PPI_REC;
+	double q[4] = { rec[PPI_Q], rec[PPI_Q + 1], rec[PPI_Q + 2], rec[PPI_Q + 3] };
+	P[0] = rec[0];
+	P[1] = rec[1];
+	P[2] = rec[2];
+	if(kind == 1) {
+		const double b[4] = { f2d(dq.x), f2d(dq.y), f2d(dq.z), f2d(dq.w) };
+		double qn[4];
+		qmul64(q, b, qn);
+		q[0] = qn[0];
+		q[1] = qn[1];
+		q[2] = qn[2];
+		q[3] = qn[3];
+		P[0] = __dadd_rn(P[0], f2d(disp.x));
+		P[1] = __dadd_rn(P[1], f2d(disp.y));
+		P[2] = __dadd_rn(P[2], f2d(disp.z));
 	}
-	r[0] = rec[0] + (double) disp.x;
-	r[1] = rec[1] + (double) disp.y;
-	r[2] = rec[2] + (double) disp.z;
+	orient64(rec + PPI_R0, q, P + 3);
 }
 
 /* Exact re-evaluation of one pair. p is the probing particle: kind 0 = its stored state, kind 1 = the
@@ -151,26 +221,17 @@ __device__ __forceinline__ void candidate64(const double *rec, float4 q, float3 
  * vol_f and uses box[vol_dir] = vol_side (the NPT candidate box, MC.c:471-478). */
 __device__ __noinline__ int exact_pair(const double *__restrict__ rec_all, const ppi_rparams *rp, const double *box_in, int ps, int kind, float4 q,
 		float3 disp, int qs, int vol_dir, double vol_f, double vol_side, double *o_dist2, double *o_pmax, double *o_qmax) {
-	double rp_[3], Rp[9], rq[3], Pp[12], Pq[12], box[3];
-	const double *recp = rec_all + (size_t) ps * PPI_REC;
-	const double *recq = rec_all + (size_t) qs * PPI_REC;
-	if(kind == 1) candidate64(recp, q, disp, rp_, Rp);
-	else {
-		for(int k = 0; k < 3; k++) rp_[k] = recp[k];
-		for(int k = 0; k < 9; k++) Rp[k] = recp[3 + k];
-	}
-	for(int k = 0; k < 3; k++) {
-		rq[k] = recq[k];
-		box[k] = box_in[k];
-	}
+	double P[12], Qr[12], box[3];
+	state64(rec_all, ps, kind, q, disp, P);
+	state64(rec_all, qs, 0, q, disp, Qr);
+#pragma unroll 1
+	for(int k = 0; k < 3; k++) box[k] = box_in[k];
 	if(vol_dir >= 0) {
-		rp_[vol_dir] = __dmul_rn(rp_[vol_dir], vol_f);
-		rq[vol_dir] = __dmul_rn(rq[vol_dir], vol_f);
+		P[vol_dir] = __dmul_rn(P[vol_dir], vol_f);
+		Qr[vol_dir] = __dmul_rn(Qr[vol_dir], vol_f);
 		box[vol_dir] = vol_side;
 	}
-	patches64(Rp, rp->base, Pp);
-	patches64(recq + 3, rp->base, Pq);
-	return interact64(rp_, Pp, rq, Pq, box, rp->sqr_rcut, rp->cosmax, o_dist2, o_pmax, o_qmax);
+	return interact64(P, P + 3, Qr, Qr + 3, rp->base, box, rp->sqr_rcut, rp->cosmax, o_dist2, o_pmax, o_qmax);
 }
 
 /* ------------------------------------------------------------------------------------------------ */
@@ -366,52 +427,110 @@ __global__ void k_scan_add(int *out, const int *aux, int n) {
 	if(i < n) out[i] += aux[blockIdx.x];
 }
 
+/* FP32 working record of slot s at sorted position pos: cell-local position from k_assign, orientation
+ * columns of R0 . Q(q) evaluated in FP32 (error ~1e-7, far inside the guard band) */
 __global__ void k_scatter(ppi_dev d, const float4 *tmp) {
 	int s = blockIdx.x * blockDim.x + threadIdx.x;
 	if(s >= d.ntot) return;
 	int gc = d.cellof[s];
 	int pos = d.cell_start[gc] + atomicAdd(d.cell_cursor + gc, 1);
-	const double *R = d.rec + (size_t) s * PPI_REC + 3;
+	const double *rec = d.rec + (size_t) s * PPI_REC;
 	float4 a = tmp[s];
-	a.w = __int_as_float(s);
-	float4 *o = d.srec + 4 * (size_t) pos;
-	o[0] = a;
-	o[1] = make_float4((float) R[0], (float) R[3], (float) R[6], (float) R[1]); /* c0 = (R00, R10, R20), c1.x = R01 */
-	o[2] = make_float4((float) R[4], (float) R[7], (float) R[2], (float) R[5]); /* c1.y, c1.z, c2.x = R02, c2.y = R12 */
-	o[3] = make_float4((float) R[8], __int_as_float(d.id[s]), __int_as_float(gc), 0.f);
+	{ /* .w = the cell's x index (neighbour offsets in the colour pass) */
+		const int r = d.rep[s];
+		a.w = __int_as_float((gc - d.rp[r].cell_base) % d.grid[r].n[0]);
+	}
+	float R0[9], Q[9];
+#pragma unroll
+	for(int k = 0; k < 9; k++) R0[k] = d2f(rec[PPI_R0 + k]);
+	const float w = d2f(rec[PPI_Q]), x = d2f(rec[PPI_Q + 1]), y = d2f(rec[PPI_Q + 2]), z = d2f(rec[PPI_Q + 3]);
+	const float sc = 2.f / (w * w + x * x + y * y + z * z);
+	Q[0] = 1.f - sc * (y * y + z * z);
+	Q[1] = sc * (x * y - w * z);
+	Q[2] = sc * (x * z + w * y);
+	Q[3] = sc * (x * y + w * z);
+	Q[4] = 1.f - sc * (x * x + z * z);
+	Q[5] = sc * (y * z - w * x);
+	Q[6] = sc * (x * z - w * y);
+	Q[7] = sc * (y * z + w * x);
+	Q[8] = 1.f - sc * (x * x + y * y);
+	float c[9]; /* c[3 j + i] = R_ij */
+#pragma unroll
+	for(int i = 0; i < 3; i++)
+#pragma unroll
+		for(int j = 0; j < 3; j++) c[3 * j + i] = fmaf(R0[3 * i], Q[j], fmaf(R0[3 * i + 1], Q[3 + j], R0[3 * i + 2] * Q[6 + j]));
+	d.spos[pos] = a;
+	float4 *o = d.sori + 3 * (size_t) pos;
+	o[0] = make_float4(c[0], c[1], c[2], c[3]);
+	o[1] = make_float4(c[4], c[5], c[6], c[7]);
+	o[2] = make_float4(c[8], __int_as_float(d.id[s]), __int_as_float(gc), __int_as_float(s));
 }
 
-/* per cell: deterministic order (ascending particle id), and the colour lists of non-empty cells */
-__global__ void k_cellfin(ppi_dev d) {
-	int gc = blockIdx.x * blockDim.x + threadIdx.x;
-	if(gc >= d.total_cells) return;
-	int r = d.cell_rep[gc];
-	const ppi_grid &g = d.grid[r];
-	int local = gc - d.rp[r].cell_base;
-	if(local >= g.ncells) return;
-	int a = d.cell_start[gc], b = d.cell_start[gc + 1];
-	if(b <= a) return;
-	float4 *v = d.srec;
-	for(int i = a + 1; i < b; i++) {
-		float4 x0 = v[4 * i], x1 = v[4 * i + 1], x2 = v[4 * i + 2], x3 = v[4 * i + 3];
-		int key = __float_as_int(x3.y);
-		int j = i - 1;
-		while(j >= a && __float_as_int(v[4 * j + 3].y) > key) {
-			v[4 * (j + 1)] = v[4 * j];
-			v[4 * (j + 1) + 1] = v[4 * j + 1];
-			v[4 * (j + 1) + 2] = v[4 * j + 2];
-			v[4 * (j + 1) + 3] = v[4 * j + 3];
-			j--;
+/* per cell: deterministic order (ascending particle id); the colour lists of non-empty cells, built per
+ * CTA (ballot ranks inside each warp, one global atomic per colour and CTA). A list entry carries what an
+ * attempt needs first: (global cell, first sorted position, particle count, replica). */
+#define CELLFIN_B 256
+__global__ void __launch_bounds__(CELLFIN_B) k_cellfin(ppi_dev d) {
+	__shared__ int s_cnt[CELLFIN_B / 32][8];
+	__shared__ int s_base[8];
+	const int gc = blockIdx.x * blockDim.x + threadIdx.x;
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	int col = -1, a_out = 0, b_out = 0, rep_out = 0;
+	if(gc < d.total_cells) {
+		const int r = d.cell_rep[gc];
+		const ppi_grid &g = d.grid[r];
+		const int local = gc - d.rp[r].cell_base;
+		if(local < g.ncells) {
+			const int a = d.cell_start[gc], b = d.cell_start[gc + 1];
+			a_out = a;
+			b_out = b;
+			rep_out = r;
+			if(b > a) {
+				float4 *P = d.spos, *O = d.sori;
+				for(int i = a + 1; i < b; i++) {
+					const float4 x0 = P[i], x1 = O[3 * i], x2 = O[3 * i + 1], x3 = O[3 * i + 2];
+					const int key = __float_as_int(x3.y);
+					int j = i - 1;
+					while(j >= a && __float_as_int(O[3 * j + 2].y) > key) {
+						P[j + 1] = P[j];
+						O[3 * (j + 1)] = O[3 * j];
+						O[3 * (j + 1) + 1] = O[3 * j + 1];
+						O[3 * (j + 1) + 2] = O[3 * j + 2];
+						j--;
+					}
+					P[j + 1] = x0;
+					O[3 * (j + 1)] = x1;
+					O[3 * (j + 1) + 1] = x2;
+					O[3 * (j + 1) + 2] = x3;
+				}
+				const int cx = local % g.n[0], cy = (local / g.n[0]) % g.n[1], cz = local / (g.n[0] * g.n[1]);
+				col = (cx & 1) | ((cy & 1) << 1) | ((cz & 1) << 2);
+			}
 		}
-		v[4 * (j + 1)] = x0;
-		v[4 * (j + 1) + 1] = x1;
-		v[4 * (j + 1) + 2] = x2;
-		v[4 * (j + 1) + 3] = x3;
 	}
-	int cx = local % g.n[0], cy = (local / g.n[0]) % g.n[1], cz = local / (g.n[0] * g.n[1]);
-	int col = (cx & 1) | ((cy & 1) << 1) | ((cz & 1) << 2);
-	int idx = atomicAdd(d.ccount + col, 1);
-	if(idx < d.clist_cap) d.clist[col * d.clist_cap + idx] = gc;
+	int rank = 0;
+#pragma unroll
+	for(int c = 0; c < 8; c++) {
+		const unsigned m = __ballot_sync(0xffffffffu, col == c);
+		if(col == c) rank = __popc(m & ((1u << lane) - 1u));
+		if(lane == 0) s_cnt[warp][c] = __popc(m);
+	}
+	__syncthreads();
+	if(threadIdx.x < 8) {
+		const int c = threadIdx.x;
+		int tot = 0;
+		for(int w = 0; w < CELLFIN_B / 32; w++) {
+			const int v = s_cnt[w][c];
+			s_cnt[w][c] = tot;
+			tot += v;
+		}
+		s_base[c] = tot ? atomicAdd(d.ccount + c, tot) : 0;
+	}
+	__syncthreads();
+	if(col >= 0) {
+		const int idx = s_base[col] + s_cnt[warp][col] + rank;
+		if(idx < d.clist_cap) d.clist[(size_t) col * d.clist_cap + idx] = make_int4(gc, a_out, b_out - a_out, rep_out);
+	}
 }
 
 /* ------------------------------------------------------------------------------------------------ */
@@ -479,197 +598,428 @@ __device__ __forceinline__ void flush_block(const ppi_dev &d, Acc &A) {
 	}
 }
 
-struct Probe {
-	float4 po;      /* old cell-local position */
-	float3 pn;      /* candidate cell-local position */
-	float cpo[9], cpn[9];
-	int i, pslot;
-	float4 q;
-	float3 disp;
+/* ------------------------------------------------------------------------------------------------ */
+/* one checkerboard colour: one attempt per non-empty cell of that colour, 32 attempts per warp      */
+/* ------------------------------------------------------------------------------------------------ */
+/* Kernel modes of the colour and energy passes:
+ *   MODE_FAST  pair tests in FP32; a pair inside the guard band is re-evaluated exactly (FP64, out of
+ *              line, rare)
+ *   MODE_AUDIT every pair additionally re-evaluated in FP64 and compared (test mode) */
+#define MODE_FAST 0
+#define MODE_AUDIT 2
+#ifndef PPI_FAST_MIN_BLOCKS
+#define PPI_FAST_MIN_BLOCKS 6 /* resident 128-thread CTAs per SM the energy kernels are compiled for */
+#endif
+#define TILE_WARPS 3 /* warps per CTA of the colour kernel (shared memory: ~12 KB per warp) */
+#ifndef PPI_TILE_MIN_BLOCKS
+#define PPI_TILE_MIN_BLOCKS 6 /* resident CTAs per SM of the colour kernel */
+#endif
+
+__device__ __forceinline__ int wrapi(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
+
+/* the FP32 decision for one pair and one state of p, made exact in the guard band (cold paths) */
+template <int MODE>
+__device__ __forceinline__ int pair_state(const ppi_dev &d, const ppi_rparams &rp, ppi_rstate *rs, int pslot, int kind, float4 q, float3 disp, int qslot,
+		float dx, float dy, float dz, const float *cp, const float *cq, float sqr_rcut, float cosmax, float basef, float eps, int vol_dir, double vol_f,
+		double vol_side, Acc &A) {
+	PairF f;
+	int cl = classify(dx, dy, dz, cp, cq, sqr_rcut, cosmax, basef, eps, MODE == MODE_AUDIT ? &f : nullptr);
+	if(MODE == MODE_AUDIT) audit_pair(d.rec, &rp, rs, rs->box, pslot, kind, q, disp, qslot, vol_dir, vol_f, vol_side, cl, f);
+	if(cl == CL_UNSURE) {
+		A.fallbacks++;
+		int ex = exact_pair(d.rec, &rp, rs->box, pslot, kind, q, disp, qslot, vol_dir, vol_f, vol_side, nullptr, nullptr, nullptr);
+		cl = ex == -1 ? CL_OVER : (ex == 1 ? CL_BOND : CL_NONE);
+	}
+	return cl;
+}
+
+/* Colour pass design. A warp takes 32 list entries at a time and each lane owns one attempt for the
+ * per-attempt work (draws, proposal, decision, commit). The neighbour pairs of the 32 attempts are
+ * flattened, one neighbour row (dy, dz) at a time, into a shared pair list (a warp scan of the lanes'
+ * row lengths gives each attempt its slice), and the lanes then walk that list 32 pairs per step: every
+ * lane executes the same instructions on its own pair, so the warp does not serialise the attempts'
+ * differently sized neighbourhoods, and each step has 32 independent candidate loads in flight. Pairs
+ * within the bonding range are compacted (ballot) into a second list whose steps run the patch tests.
+ * Guard-band pairs go to a third list resolved after the rows by the out-of-line FP64 test, so no call
+ * site sits in the hot loops. Per-attempt bond counts and flags live in shared memory. */
+#define TILE_PCAP 384 /* pair list capacity per neighbour plane (32 attempts x 3 rows x 3 cells) */
+#define TILE_CCAP 96  /* close-pair list capacity (flushed before it can overflow) */
+#define TILE_UCAP 32  /* guard-band list capacity (overflow -> the attempt is rescanned exactly) */
+#define TF_OVER 1     /* the candidate state overlaps: rejected */
+#define TF_RESCAN 2   /* evaluate the whole neighbourhood again with the exact fallback inline */
+#define TF_CLOSED 4   /* no attempt (empty slot or move out of the cell) */
+
+struct __align__(16) TileSmem {
+	double rq[32][8];  /* canonical x y z, q of the mover (cp.async target), for the commit */
+	float4 pos[32];    /* old cell-local position, .w = cell x index */
+	float4 npos[32];   /* candidate position */
+	float4 wv[32];     /* cell edges (wx, wy, wz), .w = number of x cells */
+	float4 mq[32];     /* proposed rotation quaternion */
+	float4 md[32];     /* displacement, .w = mover slot */
+	float cp[32][19];  /* mover columns: [0..8] old, [9..17] candidate */
+	int mi[32];        /* mover sorted position */
+	int bo[32], bn[32], flag[32];
+	int2 pbuf[TILE_PCAP]; /* (sorted position, attempt << 4 | row) */
+	int2 cbuf[TILE_CCAP]; /* (sorted position, attempt << 4 | row) */
+	int2 uns[TILE_UCAP];  /* (sorted position, attempt << 1 | kind) */
+	int rep[32];          /* replica of the attempt */
+	int loc[32];          /* local cell index of the attempt (its draws' counter) */
+	int nc, nu;
 };
 
-/* tests candidate jq (smem-free: records read from the global cell-sorted array) against the old and new
- * state of the moving particle; returns 1 if the new state overlaps */
-__device__ __forceinline__ int test_candidate(const ppi_dev &d, const ppi_rparams &rp, ppi_rstate *rs, const double *box, const Probe &P, int jq, float ox,
-		float oy, float oz, float sqr_rcut, float cosmax, float basef, float eps, int &bo, int &bn, Acc &A) {
-	float4 qa = d.srec[4 * (size_t) jq];
-	float dxo = (qa.x - P.po.x) + ox, dyo = (qa.y - P.po.y) + oy, dzo = (qa.z - P.po.z) + oz;
-	float dxn = (qa.x - P.pn.x) + ox, dyn = (qa.y - P.pn.y) + oy, dzn = (qa.z - P.pn.z) + oz;
-	float r2o = fmaf(dxo, dxo, fmaf(dyo, dyo, dzo * dzo));
-	float r2n = fmaf(dxn, dxn, fmaf(dyn, dyn, dzn * dzn));
-	A.pairs += 2;
-	int qslot = __float_as_int(qa.w);
-	if(r2o >= sqr_rcut + eps && r2n >= sqr_rcut + eps) {
-		if(rp.audit) {
-			PairF f;
-			f.pmax = f.qmax = -2.f;
-			f.r2 = r2o;
-			audit_pair(d.rec, &rp, rs, box, P.pslot, 0, P.q, P.disp, qslot, -1, 1., 0., CL_NONE, f);
-			f.r2 = r2n;
-			audit_pair(d.rec, &rp, rs, box, P.pslot, 1, P.q, P.disp, qslot, -1, 1., 0., CL_NONE, f);
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
+	const unsigned s = (unsigned) __cvta_generic_to_shared(smem);
+	asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+/* pair geometry: d = q - p in p's cell frame for the old (o) and candidate (n) state of attempt a */
+struct PairGeo {
+	float dxo, dyo, dzo, dxn, dyn, dzn;
+};
+
+__device__ __forceinline__ PairGeo pair_geo(const TileSmem &S, int a, int t, float4 qa) {
+	const float4 p = S.pos[a], n = S.npos[a], w = S.wv[a];
+	const int nxc = __float_as_int(w.w);
+	int dxc = __float_as_int(qa.w) - __float_as_int(p.w);
+	dxc = dxc > 1 ? dxc - nxc : (dxc < -1 ? dxc + nxc : dxc);
+	const float ox = dxc * w.x, oy = (t % 3 - 1) * w.y, oz = (t / 3 - 1) * w.z;
+	PairGeo G;
+	G.dxo = (qa.x - p.x) + ox;
+	G.dyo = (qa.y - p.y) + oy;
+	G.dzo = (qa.z - p.z) + oz;
+	G.dxn = (qa.x - n.x) + ox;
+	G.dyn = (qa.y - n.y) + oy;
+	G.dzn = (qa.z - n.z) + oz;
+	return G;
+}
+
+/* patch tests of the listed close pairs, 32 per step */
+template <int MODE>
+__device__ __forceinline__ void tile_close(const ppi_dev &d, TileSmem &S, int lane, Acc &A) {
+	const int nc = S.nc;
+	for(int c = lane; c < nc; c += 32) {
+		const int2 en = S.cbuf[c];
+		const int jq = en.x, a = en.y >> 4, t = en.y & 15;
+		if(S.flag[a] & (TF_OVER | TF_RESCAN)) continue;
+		const int r = S.rep[a];
+		const ppi_rparams &rp = d.rp[r];
+		const float4 qa = d.spos[jq], qb = d.sori[3 * (size_t) jq], qc = d.sori[3 * (size_t) jq + 1], qd = d.sori[3 * (size_t) jq + 2];
+		const float cq[9] = { qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w, qd.x };
+		const PairGeo G = pair_geo(S, a, t, qa);
+		const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
+		int clo, cln;
+		if(MODE == MODE_AUDIT) {
+			ppi_rstate *rs = d.rs + r;
+			const float4 mq = S.mq[a], md = S.md[a];
+			const int pslot = __float_as_int(md.w), qslot = __float_as_int(qd.w);
+			const float3 disp = make_float3(md.x, md.y, md.z);
+			clo = pair_state<MODE>(d, rp, rs, pslot, 0, mq, disp, qslot, G.dxo, G.dyo, G.dzo, S.cp[a], cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0., A);
+			cln = pair_state<MODE>(d, rp, rs, pslot, 1, mq, disp, qslot, G.dxn, G.dyn, G.dzn, S.cp[a] + 9, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0., A);
 		}
-		return 0;
+		else {
+			clo = classify(G.dxo, G.dyo, G.dzo, S.cp[a], cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, nullptr);
+			cln = classify(G.dxn, G.dyn, G.dzn, S.cp[a] + 9, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, nullptr);
+			const int nu = (clo == CL_UNSURE) + (cln == CL_UNSURE);
+			if(nu) {
+				const int k = atomicAdd(&S.nu, nu);
+				if(k + nu > TILE_UCAP) atomicOr(&S.flag[a], TF_RESCAN);
+				else {
+					int kk = k;
+					if(clo == CL_UNSURE) S.uns[kk++] = make_int2(jq, a << 1);
+					if(cln == CL_UNSURE) S.uns[kk] = make_int2(jq, (a << 1) | 1);
+				}
+			}
+		}
+		if(clo == CL_BOND) atomicAdd(&S.bo[a], 1);
+		if(cln == CL_BOND) atomicAdd(&S.bn[a], 1);
+		if(cln == CL_OVER) atomicOr(&S.flag[a], TF_OVER);
 	}
-	float4 qb = d.srec[4 * (size_t) jq + 1], qc = d.srec[4 * (size_t) jq + 2];
-	float qd = d.srec[4 * (size_t) jq + 3].x;
-	float cq[9] = { qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w, qd };
-	PairF fo, fn;
-	int clo = classify(dxo, dyo, dzo, P.cpo, cq, sqr_rcut, cosmax, basef, eps, &fo);
-	int cln = classify(dxn, dyn, dzn, P.cpn, cq, sqr_rcut, cosmax, basef, eps, &fn);
-	if(rp.audit) {
-		audit_pair(d.rec, &rp, rs, box, P.pslot, 0, P.q, P.disp, qslot, -1, 1., 0., clo, fo);
-		audit_pair(d.rec, &rp, rs, box, P.pslot, 1, P.q, P.disp, qslot, -1, 1., 0., cln, fn);
-	}
-	if(clo == CL_UNSURE) {
-		A.fallbacks++;
-		int ex = exact_pair(d.rec, &rp, box, P.pslot, 0, P.q, P.disp, qslot, -1, 1., 0., nullptr, nullptr, nullptr);
-		clo = ex == -1 ? CL_OVER : (ex == 1 ? CL_BOND : CL_NONE);
-	}
-	if(cln == CL_UNSURE) {
-		A.fallbacks++;
-		int ex = exact_pair(d.rec, &rp, box, P.pslot, 1, P.q, P.disp, qslot, -1, 1., 0., nullptr, nullptr, nullptr);
-		cln = ex == -1 ? CL_OVER : (ex == 1 ? CL_BOND : CL_NONE);
-	}
-	bo += (clo == CL_BOND);
-	bn += (cln == CL_BOND);
-	return cln == CL_OVER;
+	__syncwarp();
+	if(lane == 0) S.nc = 0;
+	__syncwarp();
 }
 
-/* accepted move: FP64 update of the canonical state (candidate64) and the FP32 working record */
-__device__ __noinline__ void commit_move(const ppi_dev &d, int i, int pslot, float4 q, float3 disp, float3 pn, float pw, const float *cpn) {
-	double *rec = d.rec + (size_t) pslot * PPI_REC;
-	double old[PPI_REC], nr[3], nR[9];
-#pragma unroll
-	for(int k = 0; k < PPI_REC; k++) old[k] = rec[k];
-	candidate64(old, q, disp, nr, nR);
-	rec[0] = nr[0];
-	rec[1] = nr[1];
-	rec[2] = nr[2];
-#pragma unroll
-	for(int k = 0; k < 9; k++) rec[3 + k] = nR[k];
-	float4 *o = d.srec + 4 * (size_t) i;
-	o[0] = make_float4(pn.x, pn.y, pn.z, pw);
-	o[1] = make_float4(cpn[0], cpn[1], cpn[2], cpn[3]);
-	o[2] = make_float4(cpn[4], cpn[5], cpn[6], cpn[7]);
-	o[3].x = cpn[8];
-}
-
-__device__ void attempt(const ppi_dev &d, int gc, long long round, Acc &A) {
-	int r = d.cell_rep[gc];
-	if(r != A.r) {
-		flush_thread(d, A);
-		A.r = r;
-	}
-
+/* cold path: attempt a's neighbourhood again, every guard-band pair decided exactly on the spot */
+__device__ __noinline__ void tile_rescan(const ppi_dev &d, TileSmem &S, int a, Acc &A) {
+	const float4 md = S.md[a];
+	const int mslot = __float_as_int(md.w);
+	const int i = S.mi[a];
+	const int gc = __float_as_int(d.sori[3 * (size_t) i + 2].z);
+	const int r = d.cell_rep[gc];
 	const ppi_rparams &rp = d.rp[r];
 	const ppi_grid &g = d.grid[r];
 	ppi_rstate *rs = d.rs + r;
 	const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
 	const int local = gc - rp.cell_base;
 	const int cx = local % nx, cy = (local / nx) % ny, cz = local / (nx * ny);
-	const int c0 = d.cell_start[gc], cnt = d.cell_start[gc + 1] - c0;
-	U4 r1 = rng(rp, round, r, TAG_MOVE, (uint32_t) local, 0);
-	U4 r2 = rng(rp, round, r, TAG_MOVE, (uint32_t) local, 1);
-	Probe P;
-	P.i = c0 + (int) __umulhi(r1.x, (uint32_t) cnt);
-	A.tries++;
-	P.disp = make_float3((u01(r1.y) - 0.5f) * rp.disp_max_f, (u01(r1.z) - 0.5f) * rp.disp_max_f, (u01(r1.w) - 0.5f) * rp.disp_max_f);
-	const float wx = g.wf[0], wy = g.wf[1], wz = g.wf[2];
-	P.po = d.srec[4 * (size_t) P.i];
-	P.pn = make_float3(P.po.x + P.disp.x, P.po.y + P.disp.y, P.po.z + P.disp.z);
-	/* a move that leaves the cell is rejected: cells stay valid and same-colour cells stay independent */
-	if(!(P.pn.x >= 0.f && P.pn.x < wx && P.pn.y >= 0.f && P.pn.y < wy && P.pn.z >= 0.f && P.pn.z < wz)) return;
-	/* rotation: angle uniform in [0, Theta_max), axis uniform on the sphere (inversion method) */
-	float theta = u01(r2.x) * rp.theta_max_f;
-	float zc = 1.f - 2.f * u01(r2.y);
-	float phi = 6.283185307179586f * u01(r2.z);
-	float sr = sqrtf(fmaxf(0.f, 1.f - zc * zc));
-	float sp, cp, sh, ch;
-	__sincosf(phi, &sp, &cp);
-	__sincosf(0.5f * theta, &sh, &ch);
-	P.q = make_float4(ch, sh * sr * cp, sh * sr * sp, sh * zc);
-	{
-		float4 b = d.srec[4 * (size_t) P.i + 1], c = d.srec[4 * (size_t) P.i + 2];
-		float dd = d.srec[4 * (size_t) P.i + 3].x;
-		P.cpo[0] = b.x;
-		P.cpo[1] = b.y;
-		P.cpo[2] = b.z;
-		P.cpo[3] = b.w;
-		P.cpo[4] = c.x;
-		P.cpo[5] = c.y;
-		P.cpo[6] = c.z;
-		P.cpo[7] = c.w;
-		P.cpo[8] = dd;
-		float w = P.q.x, x = P.q.y, y = P.q.z, z = P.q.w;
-		float Q[9];
-		Q[0] = 1.f - 2.f * (y * y + z * z);
-		Q[1] = 2.f * (x * y - w * z);
-		Q[2] = 2.f * (x * z + w * y);
-		Q[3] = 2.f * (x * y + w * z);
-		Q[4] = 1.f - 2.f * (x * x + z * z);
-		Q[5] = 2.f * (y * z - w * x);
-		Q[6] = 2.f * (x * z - w * y);
-		Q[7] = 2.f * (y * z + w * x);
-		Q[8] = 1.f - 2.f * (x * x + y * y);
-#pragma unroll
-		for(int jj = 0; jj < 3; jj++)
-#pragma unroll
-			for(int k3 = 0; k3 < 3; k3++) P.cpn[3 * jj + k3] = fmaf(P.cpo[k3], Q[jj], fmaf(P.cpo[3 + k3], Q[3 + jj], P.cpo[6 + k3] * Q[6 + jj]));
-	}
-	P.pslot = __float_as_int(P.po.w);
 	const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
-	const float sqr_rcut = rp.sqr_rcut_f, cosmax = rp.cosmax_f, basef = rp.base_f;
-	double box[3] = { rs->box[0], rs->box[1], rs->box[2] };
-	const int *cs = d.cell_start;
+	const float rc2e = rp.sqr_rcut_f + eps;
+	const float4 mq = S.mq[a];
+	const float3 disp = make_float3(md.x, md.y, md.z);
 	int bo = 0, bn = 0, over = 0;
-	for(int rr = 0; rr < 9 && !over; rr++) {
-		int dy = rr % 3 - 1, dz = rr / 3 - 1;
-		int yy = cy + dy, zz = cz + dz;
-		yy = yy < 0 ? yy + ny : (yy >= ny ? yy - ny : yy);
-		zz = zz < 0 ? zz + nz : (zz >= nz ? zz - nz : zz);
-		int rowbase = rp.cell_base + (zz * ny + yy) * nx;
-		float oy = dy * wy, oz = dz * wz;
-		if(cx >= 1 && cx <= nx - 2) {
-			/* the three x-neighbours are consecutive cells: one contiguous range */
-			int j0 = cs[rowbase + cx - 1], b1 = cs[rowbase + cx], b2 = cs[rowbase + cx + 1], j3 = cs[rowbase + cx + 2];
-			for(int jq = j0; jq < j3; jq++) {
-				if(jq == P.i) continue;
-				float ox = jq < b1 ? -wx : (jq < b2 ? 0.f : wx);
-				if(test_candidate(d, rp, rs, box, P, jq, ox, oy, oz, sqr_rcut, cosmax, basef, eps, bo, bn, A)) {
+	for(int t = 0; t < 9 && !over; t++) {
+		const int row = rp.cell_base + (wrapi(cz + t / 3 - 1, nz) * ny + wrapi(cy + t % 3 - 1, ny)) * nx;
+		for(int c = 0; c < 3 && !over; c++) {
+			const int cell = row + wrapi(cx + c - 1, nx);
+			for(int jq = d.cell_start[cell]; jq < d.cell_start[cell + 1]; jq++) {
+				if(jq == i) continue;
+				const float4 qa = d.spos[jq];
+				const PairGeo G = pair_geo(S, a, t, qa);
+				const float r2o = fmaf(G.dxo, G.dxo, fmaf(G.dyo, G.dyo, G.dzo * G.dzo)), r2n = fmaf(G.dxn, G.dxn, fmaf(G.dyn, G.dyn, G.dzn * G.dzn));
+				if(!(r2o < rc2e || r2n < rc2e)) continue;
+				const float4 qb = d.sori[3 * (size_t) jq], qc = d.sori[3 * (size_t) jq + 1], qd = d.sori[3 * (size_t) jq + 2];
+				const float cq[9] = { qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w, qd.x };
+				const int qslot = __float_as_int(qd.w);
+				const int clo = pair_state<MODE_FAST>(d, rp, rs, mslot, 0, mq, disp, qslot, G.dxo, G.dyo, G.dzo, S.cp[a], cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0., A);
+				const int cln = pair_state<MODE_FAST>(d, rp, rs, mslot, 1, mq, disp, qslot, G.dxn, G.dyn, G.dzn, S.cp[a] + 9, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0., A);
+				bo += (clo == CL_BOND);
+				bn += (cln == CL_BOND);
+				if(cln == CL_OVER) {
 					over = 1;
 					break;
 				}
 			}
 		}
-		else {
-			for(int dx = -1; dx <= 1 && !over; dx++) {
-				int xx = cx + dx;
-				xx = xx < 0 ? xx + nx : (xx >= nx ? xx - nx : xx);
-				int j0 = cs[rowbase + xx], j1 = cs[rowbase + xx + 1];
-				float ox = dx * wx;
-				for(int jq = j0; jq < j1; jq++) {
-					if(jq == P.i) continue;
-					if(test_candidate(d, rp, rs, box, P, jq, ox, oy, oz, sqr_rcut, cosmax, basef, eps, bo, bn, A)) {
-						over = 1;
-						break;
+	}
+	S.bo[a] = bo;
+	S.bn[a] = bn;
+	S.flag[a] = over ? TF_OVER : 0;
+}
+
+/* the 32 attempts of list entries ent (one per lane; ent.x < 0: none) */
+template <int MODE>
+__device__ __forceinline__ void tile_round(const ppi_dev &d, TileSmem &S, const int lane, const int4 ent, long long round, Acc &A) {
+	int flag = TF_CLOSED;
+	int i = 0, cx = 0, cy = 0, cz = 0, nx = 4, ny = 4, nz = 4, cbase = 0;
+	float4 po = make_float4(0.f, 0.f, 0.f, 0.f), pn = po, q = make_float4(1.f, 0.f, 0.f, 0.f);
+	float3 disp = make_float3(0.f, 0.f, 0.f);
+	int r = 0, pslot = 0, local = 0;
+	if(ent.x >= 0) {
+		const int gc = ent.x, c0 = ent.y, cnt = ent.z;
+		r = ent.w;
+		if(r != A.r) {
+			flush_thread(d, A);
+			A.r = r;
+		}
+		const ppi_rparams &rp = d.rp[r];
+		const ppi_grid &g = d.grid[r];
+		nx = g.n[0];
+		ny = g.n[1];
+		nz = g.n[2];
+		cbase = rp.cell_base;
+		local = gc - cbase;
+		cx = local % nx;
+		cy = (local / nx) % ny;
+		cz = local / (nx * ny);
+		A.tries++;
+		/* the attempt's Philox draws: particle + displacement, rotation (acceptance only when needed) */
+		const U4 r1 = rng(rp, round, r, TAG_MOVE, (uint32_t) local, 0u), r2 = rng(rp, round, r, TAG_MOVE, (uint32_t) local, 1u);
+		i = c0 + (int) __umulhi(r1.x, (uint32_t) cnt);
+		po = d.spos[i];
+		const float dm = rp.disp_max_f;
+		disp = make_float3((u01(r1.y) - 0.5f) * dm, (u01(r1.z) - 0.5f) * dm, (u01(r1.w) - 0.5f) * dm);
+		pn = make_float4(po.x + disp.x, po.y + disp.y, po.z + disp.z, po.w);
+		S.wv[lane] = make_float4(g.wf[0], g.wf[1], g.wf[2], __int_as_float(nx));
+		/* a move that leaves the cell is rejected: cells stay valid and same-colour cells stay independent */
+		if(pn.x >= 0.f && pn.x < g.wf[0] && pn.y >= 0.f && pn.y < g.wf[1] && pn.z >= 0.f && pn.z < g.wf[2]) {
+			flag = 0;
+			const float4 ob = d.sori[3 * (size_t) i], oc = d.sori[3 * (size_t) i + 1], od = d.sori[3 * (size_t) i + 2];
+			pslot = __float_as_int(od.w);
+			/* the canonical x y z and q the commit needs, copied asynchronously into shared memory */
+			const double *rec = d.rec + (size_t) pslot * PPI_REC;
+#pragma unroll
+			for(int k = 0; k < 7; k++) cp_async8(&S.rq[lane][k], rec + k);
+			/* rotation: angle uniform in [0, Theta_max), axis uniform on the sphere (inversion method) */
+			const float theta = u01(r2.x) * rp.theta_max_f;
+			const float zc = 1.f - 2.f * u01(r2.y);
+			const float phi = 6.283185307179586f * u01(r2.z);
+			const float sr = sqrtf(fmaxf(0.f, 1.f - zc * zc));
+			float sp, cph, sh, ch;
+			__sincosf(phi, &sp, &cph);
+			__sincosf(0.5f * theta, &sh, &ch);
+			q = make_float4(ch, sh * sr * cph, sh * sr * sp, sh * zc);
+			const float cpo[9] = { ob.x, ob.y, ob.z, ob.w, oc.x, oc.y, oc.z, oc.w, od.x };
+			const float w = q.x, x = q.y, y = q.z, z = q.w;
+			float Q[9];
+			Q[0] = 1.f - 2.f * (y * y + z * z);
+			Q[1] = 2.f * (x * y - w * z);
+			Q[2] = 2.f * (x * z + w * y);
+			Q[3] = 2.f * (x * y + w * z);
+			Q[4] = 1.f - 2.f * (x * x + z * z);
+			Q[5] = 2.f * (y * z - w * x);
+			Q[6] = 2.f * (x * z - w * y);
+			Q[7] = 2.f * (y * z + w * x);
+			Q[8] = 1.f - 2.f * (x * x + y * y);
+			float *cp = S.cp[lane];
+#pragma unroll
+			for(int k = 0; k < 9; k++) cp[k] = cpo[k];
+#pragma unroll
+			for(int jj = 0; jj < 3; jj++)
+#pragma unroll
+				for(int k3 = 0; k3 < 3; k3++) cp[9 + 3 * jj + k3] = fmaf(cpo[k3], Q[jj], fmaf(cpo[3 + k3], Q[3 + jj], cpo[6 + k3] * Q[6 + jj]));
+		}
+	}
+	S.pos[lane] = po;
+	S.npos[lane] = pn;
+	S.mq[lane] = q;
+	S.md[lane] = make_float4(disp.x, disp.y, disp.z, __int_as_float(pslot));
+	S.mi[lane] = i;
+	S.rep[lane] = r;
+	S.loc[lane] = local;
+	S.bo[lane] = 0;
+	S.bn[lane] = 0;
+	S.flag[lane] = flag;
+	if(lane == 0) {
+		S.nc = 0;
+		S.nu = 0;
+	}
+	__syncwarp();
+	/* the neighbour planes dz = -1, 0, 1, one at a time for all 32 attempts (3 rows each) */
+	{
+		const ppi_rparams &rpl = d.rp[r];
+		const float eps = rpl.precision == 1 ? 1e30f : rpl.eps_f;
+		const float rc2e = rpl.sqr_rcut_f + eps, ovl = 1.f - eps;
+		/* x ranges of a row: cells xm, cx, xp as one or two contiguous ranges of sorted positions */
+		const int xa0 = (cx >= 1 && cx <= nx - 2) ? cx - 1 : (cx == 0 ? nx - 1 : nx - 2);
+		const int xa1 = (cx >= 1 && cx <= nx - 2) ? cx + 2 : nx;
+		const int xb1 = (cx >= 1 && cx <= nx - 2) ? 0 : (cx == 0 ? 2 : 1);
+		const unsigned lt = (1u << lane) - 1u;
+#pragma unroll 1
+		for(int pz = 0; pz < 3; pz++) {
+			int sa[3], ea[3], sb[3], eb[3];
+			int n = 0;
+			const int live = !(S.flag[lane] & (TF_OVER | TF_CLOSED | TF_RESCAN));
+#pragma unroll
+			for(int ry = 0; ry < 3; ry++) {
+				sa[ry] = ea[ry] = sb[ry] = eb[ry] = 0;
+				if(live) {
+					const int *cs = d.cell_start + cbase + (wrapi(cz + pz - 1, nz) * ny + wrapi(cy + ry - 1, ny)) * nx;
+					sa[ry] = cs[xa0];
+					ea[ry] = cs[xa1];
+					sb[ry] = cs[0];
+					eb[ry] = cs[xb1];
+				}
+				n += (ea[ry] - sa[ry]) + (eb[ry] - sb[ry]);
+			}
+			int incl = n;
+#pragma unroll
+			for(int o = 1; o < 32; o <<= 1) {
+				const int v = __shfl_up_sync(0xffffffffu, incl, o);
+				if(lane >= o) incl += v;
+			}
+			if(__shfl_sync(0xffffffffu, incl, 31) == 0) continue;
+			/* the lanes whose slices fit into the list; the others are rescanned exactly (dense corner case) */
+			const unsigned fit = __ballot_sync(0xffffffffu, incl <= TILE_PCAP);
+			const int np = fit ? __shfl_sync(0xffffffffu, incl, 31 - __clz(fit)) : 0;
+			if(incl > TILE_PCAP) {
+				if(n) atomicOr(&S.flag[lane], TF_RESCAN);
+			}
+			else {
+				int pos = incl - n;
+#pragma unroll
+				for(int ry = 0; ry < 3; ry++) {
+					const int tag = (lane << 4) | (3 * pz + ry);
+					for(int jq = sa[ry]; jq < ea[ry]; jq++) S.pbuf[pos++] = make_int2(jq, tag);
+					for(int jq = sb[ry]; jq < eb[ry]; jq++) S.pbuf[pos++] = make_int2(jq, tag);
+				}
+			}
+			__syncwarp();
+			for(int p0 = 0; p0 < np; p0 += 32) {
+				const int p = p0 + lane;
+				int close = 0;
+				int2 en = make_int2(0, 0);
+				if(p < np) {
+					en = S.pbuf[p];
+					const int jq = en.x, a = en.y >> 4;
+					if(jq != S.mi[a] && !(S.flag[a] & (TF_OVER | TF_RESCAN))) {
+						const float4 qa = d.spos[jq];
+						const PairGeo G = pair_geo(S, a, en.y & 15, qa);
+						const float r2o = fmaf(G.dxo, G.dxo, fmaf(G.dyo, G.dyo, G.dzo * G.dzo));
+						const float r2n = fmaf(G.dxn, G.dxn, fmaf(G.dyn, G.dyn, G.dzn * G.dzn));
+						A.pairs += 2;
+						if(MODE != MODE_AUDIT && r2n < ovl) atomicOr(&S.flag[a], TF_OVER); /* certain overlap of the candidate state */
+						else close = MODE == MODE_AUDIT || r2o < rc2e || r2n < rc2e;
 					}
+				}
+				/* compact the close pairs into the patch-test list */
+				const unsigned m = __ballot_sync(0xffffffffu, close);
+				if(m) {
+					if(S.nc + __popc(m) > TILE_CCAP) tile_close<MODE>(d, S, lane, A);
+					if(close) S.cbuf[S.nc + __popc(m & lt)] = en;
+					__syncwarp();
+					if(lane == 0) S.nc += __popc(m);
+					__syncwarp();
 				}
 			}
 		}
 	}
-	if(over) return;
-	int dE = bo - bn; /* E = -bonds */
+	if(S.nc) tile_close<MODE>(d, S, lane, A);
+	/* guard-band pairs: exact decisions */
+	const int nu = S.nu < TILE_UCAP ? S.nu : TILE_UCAP;
+	for(int u = lane; u < nu; u += 32) {
+		const int2 v = S.uns[u];
+		const int jq = v.x, a = v.y >> 1, kind = v.y & 1;
+		if(S.flag[a] & (TF_OVER | TF_RESCAN)) continue;
+		const float4 md = S.md[a];
+		const int rr = S.rep[a];
+		A.fallbacks++;
+		const int ex = exact_pair(d.rec, d.rp + rr, d.rs[rr].box, __float_as_int(md.w), kind, S.mq[a], make_float3(md.x, md.y, md.z),
+				__float_as_int(d.sori[3 * (size_t) jq + 2].w), -1, 1., 0., nullptr, nullptr, nullptr);
+		if(ex == 1) atomicAdd(kind ? &S.bn[a] : &S.bo[a], 1);
+		else if(ex == -1 && kind) atomicOr(&S.flag[a], TF_OVER);
+	}
+	__syncwarp();
+	flag = S.flag[lane];
+	if(flag & TF_RESCAN) {
+		tile_rescan(d, S, lane, A);
+		flag = S.flag[lane];
+	}
+	if(flag & (TF_OVER | TF_CLOSED)) return;
+	/* Metropolis on dE = -(bn - bo) (MC.c:330-339); the attempt's state comes back from shared memory */
+	r = S.rep[lane];
+	const ppi_rparams &rp = d.rp[r];
+	const int bo = S.bo[lane], bn = S.bn[lane];
+	const int dE = bo - bn;
 	if(dE > 0) {
-		U4 r3 = rng(rp, round, r, TAG_MOVE, (uint32_t) local, 2);
-		uint64_t U = ((uint64_t) r3.x << 21) | (r3.y >> 11);
+		const U4 u3 = rng(rp, round, r, TAG_MOVE, (uint32_t) S.loc[lane], 2u);
+		const uint64_t U = ((uint64_t) u3.x << 21) | (u3.y >> 11);
 		if(!(U < rp.acc_thr[dE < 31 ? dE : 31])) return;
 	}
 	A.acc++;
 	A.dbonds += bn - bo;
-	commit_move(d, P.i, P.pslot, P.q, P.disp, P.pn, P.po.w, P.cpn);
+	/* commit: FP64 q' = q (x) dq and r' = r + disp (state64 defines the same bits), FP32 record */
+	const float4 mq = S.mq[lane], md = S.md[lane];
+	i = S.mi[lane];
+	cp_async_wait_all();
+	const double *rq = S.rq[lane];
+	const double qv[4] = { rq[3], rq[4], rq[5], rq[6] };
+	const double b[4] = { f2d(mq.x), f2d(mq.y), f2d(mq.z), f2d(mq.w) };
+	double *rec = d.rec + (size_t) __float_as_int(md.w) * PPI_REC;
+	double qn[4];
+#pragma unroll
+	for(int c = 0; c < 4; c++) qn[c] = qcomp64(qv[c], qv[c ^ 1], qv[c ^ 2], qv[c ^ 3], b, c);
+	rec[0] = __dadd_rn(rq[0], f2d(md.x));
+	rec[1] = __dadd_rn(rq[1], f2d(md.y));
+	rec[2] = __dadd_rn(rq[2], f2d(md.z));
+	rec[PPI_Q] = qn[0];
+	rec[PPI_Q + 1] = qn[1];
+	rec[PPI_Q + 2] = qn[2];
+	rec[PPI_Q + 3] = qn[3];
+	d.spos[i] = S.npos[lane];
+	const float *cp = S.cp[lane];
+	d.sori[3 * (size_t) i] = make_float4(cp[9], cp[10], cp[11], cp[12]);
+	d.sori[3 * (size_t) i + 1] = make_float4(cp[13], cp[14], cp[15], cp[16]);
+	((float *) (d.sori + 3 * (size_t) i + 2))[0] = cp[17];
 }
 
-__global__ void __launch_bounds__(128) k_colour(ppi_dev d, long long round, int col) {
+/* one colour of a round: the colour's non-empty cells, 32 per warp and iteration */
+template <int MODE>
+__global__ void __launch_bounds__(32 * TILE_WARPS, MODE == MODE_FAST ? PPI_TILE_MIN_BLOCKS : 1) k_colour(ppi_dev d, long long round, int col) {
+	__shared__ TileSmem s_tile[TILE_WARPS];
+	TileSmem &S = s_tile[threadIdx.x >> 5];
+	const int lane = threadIdx.x & 31;
+	const int4 *list = d.clist + (size_t) col * d.clist_cap;
 	int cnt = d.ccount[col];
 	if(cnt > d.clist_cap) cnt = d.clist_cap;
 	if(blockIdx.x * blockDim.x >= cnt) return; /* the whole CTA has no entry: leave before any reduction */
@@ -677,9 +1027,62 @@ __global__ void __launch_bounds__(128) k_colour(ppi_dev d, long long round, int 
 	A.r = -1;
 	A.tries = A.acc = A.pairs = A.fallbacks = 0;
 	A.dbonds = 0;
-	int stride = gridDim.x * blockDim.x;
-	for(int e = blockIdx.x * blockDim.x + threadIdx.x; e < cnt; e += stride) attempt(d, d.clist[col * d.clist_cap + e], round, A);
+	const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarp = (gridDim.x * blockDim.x) >> 5;
+	int b = warp * 32;
+	int4 ent = (b + lane < cnt) ? list[b + lane] : make_int4(-1, 0, 0, 0);
+	for(; b < cnt; b += nwarp * 32) {
+		const int en = b + nwarp * 32 + lane;
+		const int4 next = (en < cnt) ? list[en] : make_int4(-1, 0, 0, 0); /* next entry requested early */
+		tile_round<MODE>(d, S, lane, ent, round, A);
+		cp_async_wait_all(); /* no copy may still target this warp's shared memory */
+		__syncwarp();
+		ent = next;
+	}
 	flush_block(d, A);
+}
+
+/* ------------------------------------------------------------------------------------------------ */
+/* lane groups (energy pass)                                                                        */
+/* ------------------------------------------------------------------------------------------------ */
+#define PPI_DEFAULT_LANES 4
+template <int G>
+__device__ __forceinline__ unsigned group_mask() {
+	if(G >= 32) return 0xffffffffu;
+	return ((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1));
+}
+
+template <int G>
+__device__ __forceinline__ int group_sum(unsigned gm, int v) {
+#pragma unroll
+	for(int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(gm, v, o);
+	return v;
+}
+
+/* Guard-band pairs met in the hot loops are not evaluated there: a call to the out-of-line FP64 test
+ * inside the loop would make the compiler keep the loop's state in local memory around it. Each lane
+ * records up to UNS_CAP of them in registers (a shift register, no indexed arrays) and resolves them
+ * after its loop; a lane with more re-runs its share of the neighbourhood on a cold path. */
+#define UNS_CAP 4
+struct Unsure {
+	int n;
+	int v0, v1, v2, v3; /* (sorted position << 1) | kind */
+	__device__ __forceinline__ void push(int v) {
+		v3 = v2;
+		v2 = v1;
+		v1 = v0;
+		v0 = v;
+		n++;
+	}
+};
+
+/* exact decision of a recorded pair: p's state `kind` against the particle at sorted position jq */
+__device__ __forceinline__ int resolve_exact(const ppi_dev &d, const ppi_rparams &rp, ppi_rstate *rs, int pslot, int v, float4 q, float3 disp, int vol_dir,
+		double vol_f, double vol_side, Acc &A) {
+	const int jq = v >> 1, kind = v & 1;
+	const int qslot = __float_as_int(d.sori[3 * (size_t) jq + 2].w);
+	A.fallbacks++;
+	const int ex = exact_pair(d.rec, &rp, rs->box, pslot, kind, q, disp, qslot, vol_dir, vol_f, vol_side, nullptr, nullptr, nullptr);
+	return ex == -1 ? CL_OVER : (ex == 1 ? CL_BOND : CL_NONE);
 }
 
 /* ------------------------------------------------------------------------------------------------ */
@@ -728,105 +1131,223 @@ __device__ __forceinline__ void energy_flush_block(const ppi_dev &d, Acc &A) {
 	}
 }
 
-__global__ void __launch_bounds__(128) k_energy(ppi_dev d, int mode) {
-	int stride = gridDim.x * blockDim.x;
-	if(blockIdx.x * blockDim.x >= d.ntot) return;
-	Acc A; /* A.tries = bonds counted, pairs, fallbacks */
-	A.r = -1;
-	A.tries = A.acc = A.pairs = A.fallbacks = 0;
-	A.dbonds = 0;
-	float4 qz = make_float4(1.f, 0.f, 0.f, 0.f);
-	float3 dz0 = make_float3(0.f, 0.f, 0.f);
-	for(int k = blockIdx.x * blockDim.x + threadIdx.x; k < d.ntot; k += stride) {
-		float4 pa = d.srec[4 * (size_t) k];
-		float4 pb = d.srec[4 * (size_t) k + 1], pc = d.srec[4 * (size_t) k + 2], pd = d.srec[4 * (size_t) k + 3];
-		int gc = __float_as_int(pd.z);
-		int r = d.cell_rep[gc];
-		if(r != A.r) {
-			energy_flush_thread(d, A);
-			A.r = r;
-		}
-		const ppi_rparams &rp = d.rp[r];
-		const ppi_grid &g = d.grid[r];
-		ppi_rstate *rs = d.rs + r;
-		int sdir = -1;
-		float sf = 1.f;
-		double vf = 1.0, vside = 0.0;
-		if(mode == PPI_EN_VOLUME) {
-			if(g.vol_dir < 0 || rs->vol_overlap) continue;
-			sdir = g.vol_dir;
-			sf = g.vol_ff;
-			vf = g.vol_f;
-			vside = g.vol_side;
-		}
-		float w[3] = { g.wf[0], g.wf[1], g.wf[2] };
-		float pl[3] = { pa.x, pa.y, pa.z };
-		if(sdir >= 0) {
-			w[sdir] *= sf;
-			pl[sdir] *= sf;
-		}
-		float cp[9] = { pb.x, pb.y, pb.z, pb.w, pc.x, pc.y, pc.z, pc.w, pd.x };
-		const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
-		const int local = gc - rp.cell_base;
-		const int cx = local % nx, cy = (local / nx) % ny, cz = local / (nx * ny);
-		const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
-		const float sqr_rcut = rp.sqr_rcut_f, cosmax = rp.cosmax_f, basef = rp.base_f;
-		double box[3] = { rs->box[0], rs->box[1], rs->box[2] };
-		int pslot = __float_as_int(pa.w);
-		int nb = 0, no = 0;
-		int *partners = (mode == PPI_EN_PARTNERS) ? d.out_partners + (size_t) pslot * PPI_MAX_PARTNERS : nullptr;
-		for(int dz = -1; dz <= 1; dz++)
-			for(int dy = -1; dy <= 1; dy++)
-				for(int dx = -1; dx <= 1; dx++) {
-					int xx = cx + dx, yy = cy + dy, zz = cz + dz;
-					xx = xx < 0 ? xx + nx : (xx >= nx ? xx - nx : xx);
-					yy = yy < 0 ? yy + ny : (yy >= ny ? yy - ny : yy);
-					zz = zz < 0 ? zz + nz : (zz >= nz ? zz - nz : zz);
-					int cell = rp.cell_base + (zz * ny + yy) * nx + xx;
-					int j0 = d.cell_start[cell], j1 = d.cell_start[cell + 1];
-					float ox = dx * w[0], oy = dy * w[1], oz = dz * w[2];
-					for(int jq = j0; jq < j1; jq++) {
-						if(jq == k) continue;
-						float4 qa = d.srec[4 * (size_t) jq];
-						float ql[3] = { qa.x, qa.y, qa.z };
-						if(sdir >= 0) ql[sdir] *= sf;
-						float ddx = (ql[0] - pl[0]) + ox, ddy = (ql[1] - pl[1]) + oy, ddz = (ql[2] - pl[2]) + oz;
-						float r2 = fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz));
-						A.pairs++;
-						int qslot = __float_as_int(qa.w);
-						if(r2 >= sqr_rcut + eps) {
-							if(rp.audit) {
-								PairF f;
-								f.r2 = r2;
-								f.pmax = f.qmax = -2.f;
-								audit_pair(d.rec, &rp, rs, box, pslot, 0, qz, dz0, qslot, sdir, vf, vside, CL_NONE, f);
-							}
-							continue;
-						}
-						float4 qb = d.srec[4 * (size_t) jq + 1], qc = d.srec[4 * (size_t) jq + 2];
-						float qd = d.srec[4 * (size_t) jq + 3].x;
-						float cq[9] = { qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w, qd };
-						PairF f;
-						int cl = classify(ddx, ddy, ddz, cp, cq, sqr_rcut, cosmax, basef, eps, &f);
-						if(rp.audit) audit_pair(d.rec, &rp, rs, box, pslot, 0, qz, dz0, qslot, sdir, vf, vside, cl, f);
-						if(cl == CL_UNSURE) {
-							A.fallbacks++;
-							int ex = exact_pair(d.rec, &rp, box, pslot, 0, qz, dz0, qslot, sdir, vf, vside, nullptr, nullptr, nullptr);
-							cl = ex == -1 ? CL_OVER : (ex == 1 ? CL_BOND : CL_NONE);
-						}
-						if(cl == CL_BOND) {
-							if(partners && nb < PPI_MAX_PARTNERS) partners[nb] = __float_as_int(d.srec[4 * (size_t) jq + 3].y);
-							nb++;
-						}
-						no += (cl == CL_OVER);
-					}
+/* what a lane needs to re-run its share of a particle's neighbourhood in the energy pass */
+struct EnergyCtx {
+	float pl[3], w[3], cp[9];
+	float sf;
+	int k, pslot, cx, cy, cz, nx, ny, nz, cell_base, sdir;
+	double vf, vside;
+	int *partners;
+};
+
+/* cold path of a lane that met more than UNS_CAP guard-band pairs in the energy pass: its rows again,
+ * every guard-band pair decided exactly on the spot. Returns the overlap count; bonds in *nb_out. */
+template <int G>
+__device__ __noinline__ int energy_lane_exact(const ppi_dev &d, const ppi_rparams &rp, ppi_rstate *rs, const EnergyCtx &E, int sub, Acc &A, int *nb_out) {
+	const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
+	const float sqr_rcut = rp.sqr_rcut_f, cosmax = rp.cosmax_f, basef = rp.base_f, rc2e = sqr_rcut + eps;
+	const int *cs = d.cell_start;
+	const float4 q0 = make_float4(1.f, 0.f, 0.f, 0.f);
+	const float3 d0 = make_float3(0.f, 0.f, 0.f);
+	int nb = 0, no = 0;
+	for(int t = sub; t < 9; t += G) {
+		const int dy = t % 3 - 1, dz = t / 3 - 1;
+		const int row = E.cell_base + (wrapi(E.cz + dz, E.nz) * E.ny + wrapi(E.cy + dy, E.ny)) * E.nx;
+		for(int c = 0; c < 3; c++) {
+			const int cell = row + wrapi(E.cx + c - 1, E.nx);
+			const float ox = (c - 1) * E.w[0], oy = dy * E.w[1], oz = dz * E.w[2];
+			for(int jq = cs[cell]; jq < cs[cell + 1]; jq++) {
+				if(jq == E.k) continue;
+				const float4 qa = d.spos[jq];
+				float ql[3] = { qa.x, qa.y, qa.z };
+				if(E.sdir >= 0) ql[E.sdir] *= E.sf;
+				const float ddx = (ql[0] - E.pl[0]) + ox, ddy = (ql[1] - E.pl[1]) + oy, ddz = (ql[2] - E.pl[2]) + oz;
+				const float r2 = fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz));
+				if(r2 >= rc2e) continue;
+				const float4 qb = d.sori[3 * (size_t) jq], qc = d.sori[3 * (size_t) jq + 1], qd = d.sori[3 * (size_t) jq + 2];
+				const float cq[9] = { qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w, qd.x };
+				const int cl = pair_state<MODE_FAST>(d, rp, rs, E.pslot, 0, q0, d0, __float_as_int(qd.w), ddx, ddy, ddz, E.cp, cq, sqr_rcut, cosmax, basef, eps, E.sdir,
+						E.vf, E.vside, A);
+				if(cl == CL_BOND) {
+					if(E.partners && nb < PPI_MAX_PARTNERS) E.partners[nb] = __float_as_int(qd.y);
+					nb++;
 				}
+				no += (cl == CL_OVER);
+			}
+		}
+	}
+	*nb_out = nb;
+	return no;
+}
+
+/* energy of one particle from scratch, G lanes: bond and overlap counts over all partners (MC_energy,
+ * MC.c:272-309, without the early exit, as output_print_bonds counts them, output.c:213-268), or its
+ * share of the NPT candidate box's energy (MC.c:487-495). G = 1 in PPI_EN_PARTNERS mode, which also
+ * lists the bonded partners. */
+template <int MODE, int G>
+__device__ __forceinline__ void energy_particle(const ppi_dev &d, int mode, int k, Acc &A, const int sub, const unsigned gm) {
+	const float4 pa = d.spos[k];
+	const float4 pd = d.sori[3 * (size_t) k + 2];
+	const int gc = __float_as_int(pd.z);
+	const int r = d.cell_rep[gc];
+	if(r != A.r) {
+		energy_flush_thread(d, A);
+		A.r = r;
+	}
+	const ppi_rparams &rp = d.rp[r];
+	const ppi_grid &g = d.grid[r];
+	ppi_rstate *rs = d.rs + r;
+	int sdir = -1;
+	float sf = 1.f;
+	double vf = 1.0, vside = 0.0;
+	if(mode == PPI_EN_VOLUME) {
+		if(g.vol_dir < 0) return;
+		/* one overlap already rejects the candidate box: skip (one read per group, shared) */
+		int skip = sub == 0 ? *(volatile int *) &rs->vol_overlap : 0;
+		skip = __shfl_sync(gm, skip, 0, G);
+		if(skip) return;
+		sdir = g.vol_dir;
+		sf = g.vol_ff;
+		vf = g.vol_f;
+		vside = g.vol_side;
+	}
+	float w[3] = { g.wf[0], g.wf[1], g.wf[2] };
+	float pl[3] = { pa.x, pa.y, pa.z };
+	if(sdir >= 0) {
+		w[sdir] *= sf;
+		pl[sdir] *= sf;
+	}
+	const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+	const int local = gc - rp.cell_base;
+	const int cx = local % nx, cy = (local / nx) % ny, cz = local / (nx * ny);
+	const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
+	const float sqr_rcut = rp.sqr_rcut_f, cosmax = rp.cosmax_f, basef = rp.base_f, rc2e = sqr_rcut + eps, ovl = 1.f - eps;
+	const int pslot = __float_as_int(pd.w);
+	int nb = 0, no = 0;
+	int *partners = (mode == PPI_EN_PARTNERS) ? d.out_partners + (size_t) pslot * PPI_MAX_PARTNERS : nullptr;
+	const int *cs = d.cell_start;
+	float cp[9];
+	{
+		const float4 pb = d.sori[3 * (size_t) k], pc = d.sori[3 * (size_t) k + 1];
+		cp[0] = pb.x;
+		cp[1] = pb.y;
+		cp[2] = pb.z;
+		cp[3] = pb.w;
+		cp[4] = pc.x;
+		cp[5] = pc.y;
+		cp[6] = pc.z;
+		cp[7] = pc.w;
+		cp[8] = pd.x;
+	}
+	const float4 q0 = make_float4(1.f, 0.f, 0.f, 0.f);
+	const float3 d0 = make_float3(0.f, 0.f, 0.f);
+	const int xm = wrapi(cx - 1, nx), xp = wrapi(cx + 1, nx);
+	const int stop_on_overlap = (mode == PPI_EN_VOLUME);
+	Unsure U;
+	U.n = U.v0 = U.v1 = U.v2 = U.v3 = 0;
+	for(int t = sub; t < 9 && !(stop_on_overlap && no); t += G) {
+		const int dy = t % 3 - 1, dz = t / 3 - 1;
+		const int row = rp.cell_base + (wrapi(cz + dz, nz) * ny + wrapi(cy + dy, ny)) * nx;
+		const int a0 = cs[row + xm], a1 = cs[row + xm + 1], m0 = cs[row + cx], m1 = cs[row + cx + 1], p0 = cs[row + xp], p1 = cs[row + xp + 1];
+		const float oy = dy * w[1], oz = dz * w[2];
+#pragma unroll 1
+		for(int c = 0; c < 3 && !(stop_on_overlap && no); c++) {
+			const float ox = (c - 1) * w[0];
+			const int j1 = c == 0 ? a1 : (c == 1 ? m1 : p1);
+			for(int jq = (c == 0 ? a0 : (c == 1 ? m0 : p0)); jq < j1; jq++) {
+				if(jq == k) continue;
+				const float4 qa = d.spos[jq];
+				float ql[3] = { qa.x, qa.y, qa.z };
+				if(sdir >= 0) ql[sdir] *= sf;
+				const float ddx = (ql[0] - pl[0]) + ox, ddy = (ql[1] - pl[1]) + oy, ddz = (ql[2] - pl[2]) + oz;
+				const float r2 = fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz));
+				A.pairs++;
+				int cl;
+				if(MODE != MODE_AUDIT && r2 < ovl) cl = CL_OVER;
+				else if(MODE != MODE_AUDIT && r2 >= rc2e) continue;
+				else {
+					const float4 qb = d.sori[3 * (size_t) jq], qc = d.sori[3 * (size_t) jq + 1];
+					const float4 qd = d.sori[3 * (size_t) jq + 2];
+					const float cq[9] = { qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w, qd.x };
+					if(MODE == MODE_AUDIT)
+						cl = pair_state<MODE>(d, rp, rs, pslot, 0, q0, d0, __float_as_int(qd.w), ddx, ddy, ddz, cp, cq, sqr_rcut, cosmax, basef, eps, sdir, vf, vside, A);
+					else {
+						cl = classify(ddx, ddy, ddz, cp, cq, sqr_rcut, cosmax, basef, eps, nullptr);
+						if(cl == CL_UNSURE) U.push(jq << 1);
+					}
+					if(cl == CL_BOND && partners && nb < PPI_MAX_PARTNERS) partners[nb] = __float_as_int(qd.y);
+				}
+				nb += (cl == CL_BOND);
+				if(cl == CL_OVER) {
+					no++;
+					if(stop_on_overlap) break;
+				}
+			}
+		}
+	}
+	if(MODE == MODE_FAST && U.n && !(stop_on_overlap && no)) {
+		if(U.n > UNS_CAP) {
+			EnergyCtx E;
+			for(int a = 0; a < 3; a++) {
+				E.pl[a] = pl[a];
+				E.w[a] = w[a];
+			}
+			for(int a = 0; a < 9; a++) E.cp[a] = cp[a];
+			E.sf = sf;
+			E.k = k;
+			E.pslot = pslot;
+			E.cx = cx;
+			E.cy = cy;
+			E.cz = cz;
+			E.nx = nx;
+			E.ny = ny;
+			E.nz = nz;
+			E.cell_base = rp.cell_base;
+			E.sdir = sdir;
+			E.vf = vf;
+			E.vside = vside;
+			E.partners = partners;
+			no = energy_lane_exact<G>(d, rp, rs, E, sub, A, &nb);
+		}
+		else {
+#pragma unroll 1
+			for(int kk = 0; kk < U.n; kk++) {
+				const int v = kk == 0 ? U.v0 : (kk == 1 ? U.v1 : (kk == 2 ? U.v2 : U.v3));
+				const int cl = resolve_exact(d, rp, rs, pslot, v, q0, d0, sdir, vf, vside, A);
+				if(cl == CL_BOND) {
+					if(partners && nb < PPI_MAX_PARTNERS) partners[nb] = __float_as_int(d.sori[3 * (size_t) (v >> 1) + 2].y);
+					nb++;
+				}
+				no += (cl == CL_OVER);
+			}
+		}
+	}
+	nb = group_sum<G>(gm, nb);
+	no = group_sum<G>(gm, no);
+	if(sub == 0) {
 		if(mode != PPI_EN_VOLUME) {
 			d.out_bonds[pslot] = nb;
 			d.out_overlaps[pslot] = no;
 		}
-		A.tries += nb;
 		if(no && !rs->vol_overlap) atomicExch(&rs->vol_overlap, 1); /* visible at once: lets the others skip work */
+		if(!(mode == PPI_EN_VOLUME && no)) A.tries += nb;
+	}
+}
+
+template <int MODE, int G>
+__global__ void __launch_bounds__(128, MODE == MODE_FAST ? PPI_FAST_MIN_BLOCKS : 1) k_energy(ppi_dev d, int mode) {
+	constexpr int PW = 32 / G;
+	if(blockIdx.x * (blockDim.x / G) >= d.ntot) return;
+	Acc A; /* A.tries = bonds counted, pairs, fallbacks */
+	A.r = -1;
+	A.tries = A.acc = A.pairs = A.fallbacks = 0;
+	A.dbonds = 0;
+	const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarp = (gridDim.x * blockDim.x) >> 5;
+	const int sub = threadIdx.x & (G - 1), slot = (threadIdx.x & 31) / G;
+	const unsigned gm = group_mask<G>();
+	for(int b = warp * PW; b < d.ntot; b += nwarp * PW) {
+		const int k = b + slot;
+		if(k < d.ntot) energy_particle<MODE, G>(d, mode, k, A, sub, gm);
 	}
 	energy_flush_block(d, A);
 }
@@ -911,21 +1432,20 @@ __global__ void k_vol_apply(ppi_dev d) {
 		rec[g.vol_dir] = __dmul_rn(rec[g.vol_dir], g.vol_f); /* p->r[dir] *= rescale_factor (MC.c:477) */
 	}
 	/* working record (sorted position k) */
-	float4 *o = d.srec + 4 * (size_t) k;
-	int gc = __float_as_int(o[3].z);
+	int gc = __float_as_int(d.sori[3 * (size_t) k + 2].z);
 	int r2 = d.cell_rep[gc];
 	if(d.rs[r2].vol_accept) {
 		const ppi_grid &g = d.grid[r2];
-		float4 a = o[0];
+		float4 a = d.spos[k];
 		if(g.vol_dir == 0) a.x *= g.vol_ff;
 		else if(g.vol_dir == 1) a.y *= g.vol_ff;
 		else a.z *= g.vol_ff;
-		o[0] = a;
+		d.spos[k] = a;
 	}
 }
 
 /* ------------------------------------------------------------------------------------------------ */
-/* gram_schmidt, reorder                                                                            */
+/* gram_schmidt, reorder, export                                                                    */
 /* ------------------------------------------------------------------------------------------------ */
 __device__ void normalize64(double *v) {
 	double norm = __dsqrt_rn(scalar64(v, v));
@@ -934,11 +1454,14 @@ __device__ void normalize64(double *v) {
 	v[2] = __ddiv_rn(v[2], norm);
 }
 
-/* gram_schmidt (utils.c:91-113) on the orientation rows, with explicitly rounded operations */
+/* gram_schmidt (utils.c:91-113) on the orientation rows R = R0 . Q(q), with explicitly rounded
+ * operations; the result becomes the new R0 and q the identity */
 __global__ void k_gram_schmidt(ppi_dev d, int first, int count) {
 	int k = blockIdx.x * blockDim.x + threadIdx.x;
 	if(k >= count) return;
-	double *R = d.rec + (size_t) (first + k) * PPI_REC + 3;
+	double *rec = d.rec + (size_t) (first + k) * PPI_REC;
+	double R[9];
+	orient64(rec + PPI_R0, rec + PPI_Q, R);
 	double v1[3] = { R[0], R[1], R[2] }, v2[3] = { R[3], R[4], R[5] }, v3[3] = { R[6], R[7], R[8] };
 	double b1 = __ddiv_rn(scalar64(v2, v1), scalar64(v1, v1));
 	for(int i = 0; i < 3; i++) v2[i] = __dsub_rn(v2[i], __dmul_rn(b1, v1[i]));
@@ -950,23 +1473,39 @@ __global__ void k_gram_schmidt(ppi_dev d, int first, int count) {
 	normalize64(v2);
 	normalize64(v3);
 	for(int i = 0; i < 3; i++) {
-		R[i] = v1[i];
-		R[3 + i] = v2[i];
-		R[6 + i] = v3[i];
+		rec[PPI_R0 + i] = v1[i];
+		rec[PPI_R0 + 3 + i] = v2[i];
+		rec[PPI_R0 + 6 + i] = v3[i];
 	}
+	rec[PPI_Q] = 1.0;
+	rec[PPI_Q + 1] = 0.0;
+	rec[PPI_Q + 2] = 0.0;
+	rec[PPI_Q + 3] = 0.0;
 }
 
 /* physical reorder of the canonical state into the current cell order (locality of the FP64 updates) */
 __global__ void k_gather(ppi_dev d) {
 	int k = blockIdx.x * blockDim.x + threadIdx.x;
 	if(k >= d.ntot) return;
-	float4 *o = d.srec + 4 * (size_t) k;
-	int s = __float_as_int(o[0].w);
-	const double *src = d.rec + (size_t) s * PPI_REC;
-	double *dst = d.tmp_rec + (size_t) k * PPI_REC;
-	for(int j = 0; j < PPI_REC; j++) dst[j] = src[j];
+	int s = __float_as_int(d.sori[3 * (size_t) k + 2].w);
+	const double2 *src = (const double2 *) (d.rec + (size_t) s * PPI_REC);
+	double2 *dst = (double2 *) (d.tmp_rec + (size_t) k * PPI_REC);
+#pragma unroll
+	for(int j = 0; j < PPI_REC / 2; j++) dst[j] = src[j];
 	d.tmp_id[k] = d.id[s];
-	o[0].w = __int_as_float(k);
+	d.sori[3 * (size_t) k + 2].w = __int_as_float(k);
+}
+
+/* x y z R00..R22 of slots [first, first + count) into tmp_rec (12 doubles each) */
+__global__ void k_export(ppi_dev d, int first, int count) {
+	int k = blockIdx.x * blockDim.x + threadIdx.x;
+	if(k >= count) return;
+	const double *rec = d.rec + (size_t) (first + k) * PPI_REC;
+	double *o = d.tmp_rec + (size_t) k * 12;
+	o[0] = rec[0];
+	o[1] = rec[1];
+	o[2] = rec[2];
+	orient64(rec + PPI_R0, rec + PPI_Q, o + 3);
 }
 
 /* ------------------------------------------------------------------------------------------------ */
@@ -984,6 +1523,17 @@ extern "C" int ppi_sm_count(void) {
 	return g_sms;
 }
 
+/* one full wave of resident 128-thread CTAs of kernel f (the passes loop over their work) */
+template <typename F>
+static int resident_grid(F f, int *cache, int block = 128) {
+	if(*cache == 0) {
+		int nb = 0;
+		if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f, block, 0) != cudaSuccess || nb <= 0) nb = 1;
+		*cache = nb * ppi_sm_count();
+	}
+	return *cache;
+}
+
 extern "C" int ppi_resort(const ppi_dev *d, long long epoch, cudaStream_t s, long long *nl) {
 	float4 *tmp = (float4 *) d->tmp_rec; /* ntot float4 fit in the reorder scratch */
 	cudaMemsetAsync(d->cell_count, 0, sizeof(int) * (size_t) d->total_cells, s);
@@ -996,16 +1546,38 @@ extern "C" int ppi_resort(const ppi_dev *d, long long epoch, cudaStream_t s, lon
 	k_scan_top<<<1, SCAN_B, 0, s>>>(d->scan_aux, sb, d->cell_start + d->total_cells);
 	k_scan_add<<<sb, SCAN_B, 0, s>>>(d->cell_start, d->scan_aux, d->total_cells);
 	if(nb > 0) k_scatter<<<nb, 256, 0, s>>>(*d, tmp);
-	k_cellfin<<<(d->total_cells + 255) / 256, 256, 0, s>>>(*d);
+	k_cellfin<<<(d->total_cells + CELLFIN_B - 1) / CELLFIN_B, CELLFIN_B, 0, s>>>(*d);
 	*nl += 5 + (nb > 0 ? 2 : 0);
 	return (int) cudaGetLastError();
 }
 
-extern "C" int ppi_round(const ppi_dev *d, long long round, const int *colours, cudaStream_t s, long long *nl) {
-	int grid = ppi_sm_count() * 8;
-	for(int ci = 0; ci < 8; ci++) k_colour<<<grid, 128, 0, s>>>(*d, round, colours[ci]);
+static int lanes_of(const ppi_dev *d) { return d->lanes == 8 ? 8 : PPI_DEFAULT_LANES; }
+
+extern "C" int ppi_round(const ppi_dev *d, long long round, const int *colours, int audit, cudaStream_t s, long long *nl) {
+	static int g_audit = 0, g_fast = 0;
+	if(audit || d->audit_any) {
+		int grid = resident_grid(k_colour<MODE_AUDIT>, &g_audit, 32 * TILE_WARPS);
+		for(int ci = 0; ci < 8; ci++) k_colour<MODE_AUDIT><<<grid, 32 * TILE_WARPS, 0, s>>>(*d, round, colours[ci]);
+	}
+	else {
+		int grid = resident_grid(k_colour<MODE_FAST>, &g_fast, 32 * TILE_WARPS);
+		for(int ci = 0; ci < 8; ci++) k_colour<MODE_FAST><<<grid, 32 * TILE_WARPS, 0, s>>>(*d, round, colours[ci]);
+	}
 	*nl += 8;
 	return (int) cudaGetLastError();
+}
+
+static void launch_energy(const ppi_dev *d, int mode, cudaStream_t s, long long *nl) {
+	static int g_a1 = 0, g_a4 = 0, g_f1 = 0, g_f4 = 0, g_f8 = 0;
+	const int audit = d->audit_any;
+	if(mode == PPI_EN_PARTNERS) { /* one lane per particle: the partner list is written in order */
+		if(audit) k_energy<MODE_AUDIT, 1><<<resident_grid(k_energy<MODE_AUDIT, 1>, &g_a1), 128, 0, s>>>(*d, mode);
+		else k_energy<MODE_FAST, 1><<<resident_grid(k_energy<MODE_FAST, 1>, &g_f1), 128, 0, s>>>(*d, mode);
+	}
+	else if(audit) k_energy<MODE_AUDIT, 4><<<resident_grid(k_energy<MODE_AUDIT, 4>, &g_a4), 128, 0, s>>>(*d, mode);
+	else if(lanes_of(d) == 8) k_energy<MODE_FAST, 8><<<resident_grid(k_energy<MODE_FAST, 8>, &g_f8), 128, 0, s>>>(*d, mode);
+	else k_energy<MODE_FAST, 4><<<resident_grid(k_energy<MODE_FAST, 4>, &g_f4), 128, 0, s>>>(*d, mode);
+	*nl += 1;
 }
 
 extern "C" int ppi_energy(const ppi_dev *d, int mode, cudaStream_t s, long long *nl) {
@@ -1013,19 +1585,16 @@ extern "C" int ppi_energy(const ppi_dev *d, int mode, cudaStream_t s, long long 
 		k_energy_reset<<<(d->nrep + 63) / 64, 64, 0, s>>>(*d);
 		*nl += 1;
 	}
-	int grid = ppi_sm_count() * 8;
-	k_energy<<<grid, 128, 0, s>>>(*d, mode);
-	*nl += 1;
+	launch_energy(d, mode, s, nl);
 	return (int) cudaGetLastError();
 }
 
 extern "C" int ppi_volume(const ppi_dev *d, long long sweep, cudaStream_t s, long long *nl) {
 	k_vol_plan<<<(d->nrep + 63) / 64, 64, 0, s>>>(*d, sweep);
-	int grid = ppi_sm_count() * 8;
-	k_energy<<<grid, 128, 0, s>>>(*d, PPI_EN_VOLUME);
+	launch_energy(d, PPI_EN_VOLUME, s, nl);
 	k_vol_decide<<<(d->nrep + 63) / 64, 64, 0, s>>>(*d, sweep);
 	if(d->ntot > 0) k_vol_apply<<<(d->ntot + 255) / 256, 256, 0, s>>>(*d);
-	*nl += 4;
+	*nl += 3;
 	return (int) cudaGetLastError();
 }
 
@@ -1045,6 +1614,13 @@ extern "C" int ppi_reorder(const ppi_dev *d, cudaStream_t s, long long *nl) {
 	return (int) cudaGetLastError();
 }
 
+extern "C" int ppi_export(const ppi_dev *d, int first, int count, cudaStream_t s, long long *nl) {
+	if(count <= 0) return 0;
+	k_export<<<(count + 255) / 256, 256, 0, s>>>(*d, first, count);
+	*nl += 1;
+	return (int) cudaGetLastError();
+}
+
 /* ------------------------------------------------------------------------------------------------ */
 /* allocation-free energy of one configuration (pp_gpu_energy_noalloc)                               */
 /*                                                                                                  */
@@ -1058,8 +1634,9 @@ extern "C" int ppi_reorder(const ppi_dev *d, cudaStream_t s, long long *nl) {
 #define NA_ALIGN(x) ((((size_t) (x)) + 255) & ~(size_t) 255)
 #define NA_REC ((size_t) 0)
 #define NA_STAGE (NA_REC + NA_ALIGN((size_t) NOALLOC_N * PPI_REC * sizeof(double)))
-#define NA_SREC (NA_STAGE + NA_ALIGN((size_t) NOALLOC_N * sizeof(float4)))
-#define NA_ID (NA_SREC + NA_ALIGN((size_t) NOALLOC_N * 4 * sizeof(float4)))
+#define NA_SPOS (NA_STAGE + NA_ALIGN((size_t) NOALLOC_N * sizeof(float4)))
+#define NA_SORI (NA_SPOS + NA_ALIGN((size_t) NOALLOC_N * sizeof(float4)))
+#define NA_ID (NA_SORI + NA_ALIGN((size_t) NOALLOC_N * 3 * sizeof(float4)))
 #define NA_REP (NA_ID + NA_ALIGN((size_t) NOALLOC_N * sizeof(int)))
 #define NA_CELLOF (NA_REP + NA_ALIGN((size_t) NOALLOC_N * sizeof(int)))
 #define NA_BONDS (NA_CELLOF + NA_ALIGN((size_t) NOALLOC_N * sizeof(int)))
@@ -1070,7 +1647,7 @@ extern "C" int ppi_reorder(const ppi_dev *d, cudaStream_t s, long long *nl) {
 #define NA_CREP (NA_CCURSOR + NA_ALIGN((size_t) NOALLOC_CELLS * sizeof(int)))
 #define NA_AUX (NA_CREP + NA_ALIGN((size_t) NOALLOC_CELLS * sizeof(int)))
 #define NA_CLIST (NA_AUX + NA_ALIGN((size_t) (NOALLOC_CELLS / 1024 + 2) * sizeof(int)))
-#define NA_COLCOUNT (NA_CLIST + NA_ALIGN((size_t) 8 * (NOALLOC_CELLS / 8 + 8) * sizeof(int)))
+#define NA_COLCOUNT (NA_CLIST + NA_ALIGN((size_t) 8 * (NOALLOC_CELLS / 8 + 8) * sizeof(int4)))
 #define NA_RP (NA_COLCOUNT + NA_ALIGN(8 * sizeof(int)))
 #define NA_RS (NA_RP + NA_ALIGN(sizeof(ppi_rparams)))
 #define NA_GRID (NA_RS + NA_ALIGN(sizeof(ppi_rstate)))
@@ -1090,7 +1667,11 @@ __global__ void k_noalloc_pack(ppi_dev d, const double *r, const double *R) {
 	o[0] = r[3 * (size_t) i];
 	o[1] = r[3 * (size_t) i + 1];
 	o[2] = r[3 * (size_t) i + 2];
-	for(int k = 0; k < 9; k++) o[3 + k] = R[9 * (size_t) i + k];
+	o[PPI_Q] = 1.0;
+	o[PPI_Q + 1] = 0.0;
+	o[PPI_Q + 2] = 0.0;
+	o[PPI_Q + 3] = 0.0;
+	for(int k = 0; k < 9; k++) o[PPI_R0 + k] = R[9 * (size_t) i + k];
 	d.id[i] = i;
 	d.rep[i] = 0;
 }
@@ -1150,7 +1731,8 @@ extern "C" int pp_gpu_energy_noalloc(int N, const double *r_dev, const double *R
 	d.clist_cap = (int) (cells / 8 + 8);
 	d.rec = (double *) (base + NA_REC);
 	d.tmp_rec = (double *) (base + NA_STAGE); /* float4 staging of the cell assignment */
-	d.srec = (float4 *) (base + NA_SREC);
+	d.spos = (float4 *) (base + NA_SPOS);
+	d.sori = (float4 *) (base + NA_SORI);
 	d.id = (int *) (base + NA_ID);
 	d.rep = (int *) (base + NA_REP);
 	d.cellof = (int *) (base + NA_CELLOF);
@@ -1161,8 +1743,10 @@ extern "C" int pp_gpu_energy_noalloc(int N, const double *r_dev, const double *R
 	d.cell_cursor = (int *) (base + NA_CCURSOR);
 	d.cell_rep = (int *) (base + NA_CREP);
 	d.scan_aux = (int *) (base + NA_AUX);
-	d.clist = (int *) (base + NA_CLIST);
+	d.clist = (int4 *) (base + NA_CLIST);
 	d.ccount = (int *) (base + NA_COLCOUNT);
+	d.audit_any = 0;
+	d.lanes = 0;
 	d.rp = (ppi_rparams *) (base + NA_RP);
 	d.rs = (ppi_rstate *) (base + NA_RS);
 	d.grid = (ppi_grid *) (base + NA_GRID);
