@@ -617,61 +617,63 @@ __device__ __forceinline__ void flush_block(const ppi_dev &d, Acc &A) {
 
 __device__ __forceinline__ int wrapi(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
 
-/* the FP32 decision for one pair and one state of p, made exact in the guard band (cold paths) */
+/* the FP32 decision for one pair and one state of p, made exact in the guard band */
 template <int MODE>
-__device__ __forceinline__ int pair_state(const ppi_dev &d, const ppi_rparams &rp, ppi_rstate *rs, int pslot, int kind, float4 q, float3 disp, int qslot,
+__device__ __forceinline__ int pair_state(const double *rec, const ppi_rparams &rp, ppi_rstate *rs, int pslot, int kind, float4 q, float3 disp, int qslot,
 		float dx, float dy, float dz, const float *cp, const float *cq, float sqr_rcut, float cosmax, float basef, float eps, int vol_dir, double vol_f,
-		double vol_side, Acc &A) {
+		double vol_side, unsigned &fallbacks) {
 	PairF f;
 	int cl = classify(dx, dy, dz, cp, cq, sqr_rcut, cosmax, basef, eps, MODE == MODE_AUDIT ? &f : nullptr);
-	if(MODE == MODE_AUDIT) audit_pair(d.rec, &rp, rs, rs->box, pslot, kind, q, disp, qslot, vol_dir, vol_f, vol_side, cl, f);
+	if(MODE == MODE_AUDIT) audit_pair(rec, &rp, rs, rs->box, pslot, kind, q, disp, qslot, vol_dir, vol_f, vol_side, cl, f);
 	if(cl == CL_UNSURE) {
-		A.fallbacks++;
-		int ex = exact_pair(d.rec, &rp, rs->box, pslot, kind, q, disp, qslot, vol_dir, vol_f, vol_side, nullptr, nullptr, nullptr);
+		fallbacks++;
+		int ex = exact_pair(rec, &rp, rs->box, pslot, kind, q, disp, qslot, vol_dir, vol_f, vol_side, nullptr, nullptr, nullptr);
 		cl = ex == -1 ? CL_OVER : (ex == 1 ? CL_BOND : CL_NONE);
 	}
 	return cl;
 }
 
-/* Colour pass design. A warp takes 32 list entries at a time and each lane owns one attempt for the
- * per-attempt work (draws, proposal, decision, commit). The neighbour pairs of the 32 attempts are
- * flattened, one neighbour row (dy, dz) at a time, into a shared pair list (a warp scan of the lanes'
- * row lengths gives each attempt its slice), and the lanes then walk that list 32 pairs per step: every
- * lane executes the same instructions on its own pair, so the warp does not serialise the attempts'
- * differently sized neighbourhoods, and each step has 32 independent candidate loads in flight. Pairs
- * within the bonding range are compacted (ballot) into a second list whose steps run the patch tests.
- * Guard-band pairs go to a third list resolved after the rows by the out-of-line FP64 test, so no call
- * site sits in the hot loops. Per-attempt bond counts and flags live in shared memory. */
-#define TILE_PCAP 384 /* pair list capacity per neighbour plane (32 attempts x 3 rows x 3 cells) */
-#define TILE_CCAP 96  /* close-pair list capacity (flushed before it can overflow) */
-#define TILE_UCAP 32  /* guard-band list capacity (overflow -> the attempt is rescanned exactly) */
-#define TF_OVER 1     /* the candidate state overlaps: rejected */
-#define TF_RESCAN 2   /* evaluate the whole neighbourhood again with the exact fallback inline */
-#define TF_CLOSED 4   /* no attempt (empty slot or move out of the cell) */
+/* The rare exact paths (rescans of an attempt or of a particle) are inline code that receives the
+ * device pointers it needs one by one (COLD_PARAMS / COLD_ARGS) and returns its counts; the only
+ * out-of-line call of the hot kernels is exact_pair, whose arguments are scalars and pointers. */
+#define COLD_PARAMS const float4 *__restrict__ c_spos, const float4 *__restrict__ c_sori, const int *__restrict__ c_cs, const double *c_rec, const ppi_rparams *c_rp, \
+		const ppi_grid *c_grid, ppi_rstate *c_rs
+#define COLD_ARGS(d) (d).spos, (d).sori, (d).cell_start, (d).rec, (d).rp, (d).grid, (d).rs
+
+/* Colour pass design. A warp takes TA = 64 list entries at a time; lane l owns attempts l and l + 32
+ * for the per-attempt work (draws, proposal, decision, commit). The neighbour pairs of the 64 attempts
+ * are flattened, one neighbour plane (dz) at a time, into a shared pair list (a warp scan of the lanes'
+ * plane lengths gives each attempt its slice), and the lanes then walk that list 32 pairs per step:
+ * every lane executes the same instructions on its own pair, so the warp does not serialise the
+ * attempts' differently sized neighbourhoods, and each step has 32 independent candidate loads in
+ * flight. Pairs within the bonding range are compacted (ballot) into a second list whose steps run the
+ * patch tests. Guard-band pairs go to a third list resolved after the planes by the out-of-line FP64
+ * test, so no call site sits in the hot loops. The per-attempt state kept in shared memory is small
+ * (~120 B), so that a colour of a million-particle system fits into one wave of resident warps. */
+#define TA 64          /* attempts per warp and iteration (2 per lane) */
+#define TILE_PCAP 768  /* pair list capacity per neighbour plane */
+#define TILE_CCAP 128  /* close-pair list capacity (flushed before it can overflow) */
+#define TILE_UCAP 32   /* guard-band list capacity (overflow -> the attempt is rescanned exactly) */
+#define TILE_OFF_MAX (1 << 21) /* |candidate - mover| sorted-position distance that a packed entry holds */
+#define TF_OVER 1      /* the candidate state overlaps: rejected */
+#define TF_RESCAN 2    /* evaluate the whole neighbourhood again with the exact fallback inline */
+#define TF_CLOSED 4    /* no attempt (empty slot or move out of the cell) */
 
 struct __align__(16) TileSmem {
-	double rq[32][8];  /* canonical x y z, q of the mover (cp.async target), for the commit */
-	float4 pos[32];    /* old cell-local position, .w = cell x index */
-	float4 npos[32];   /* candidate position */
-	float4 wv[32];     /* cell edges (wx, wy, wz), .w = number of x cells */
-	float4 mq[32];     /* proposed rotation quaternion */
-	float4 md[32];     /* displacement, .w = mover slot */
-	float cp[32][19];  /* mover columns: [0..8] old, [9..17] candidate */
-	int mi[32];        /* mover sorted position */
-	int bo[32], bn[32], flag[32];
-	int2 pbuf[TILE_PCAP]; /* (sorted position, attempt << 4 | row) */
-	int2 cbuf[TILE_CCAP]; /* (sorted position, attempt << 4 | row) */
-	int2 uns[TILE_UCAP];  /* (sorted position, attempt << 1 | kind) */
-	int rep[32];          /* replica of the attempt */
-	int loc[32];          /* local cell index of the attempt (its draws' counter) */
+	float4 pos[TA];   /* old cell-local position, .w = cell x index */
+	float4 md[TA];    /* displacement, .w = mover slot */
+	float4 wv[TA];    /* cell edges (wx, wy, wz), .w = number of x cells */
+	float4 qr[TA];    /* proposed rotation quaternion */
+	float cpo[9][TA]; /* mover's old orientation columns */
+	int mi[TA];       /* mover sorted position */
+	int rep[TA];      /* replica */
+	int cc[TA];       /* mover cell coordinates cx | cy << 10 | cz << 20 */
+	int flag[TA], bo[TA], bn[TA];
+	int pbuf[TILE_PCAP]; /* (candidate - mover) << 10 | attempt << 4 | row */
+	int cbuf[TILE_CCAP]; /* same packing, pairs within the bonding range */
+	int2 uns[TILE_UCAP]; /* (sorted position, attempt << 1 | kind) */
 	int nc, nu;
 };
-
-__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
-	const unsigned s = (unsigned) __cvta_generic_to_shared(smem);
-	asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 /* pair geometry: d = q - p in p's cell frame for the old (o) and candidate (n) state of attempt a */
 struct PairGeo {
@@ -679,7 +681,7 @@ struct PairGeo {
 };
 
 __device__ __forceinline__ PairGeo pair_geo(const TileSmem &S, int a, int t, float4 qa) {
-	const float4 p = S.pos[a], n = S.npos[a], w = S.wv[a];
+	const float4 p = S.pos[a], m = S.md[a], w = S.wv[a];
 	const int nxc = __float_as_int(w.w);
 	int dxc = __float_as_int(qa.w) - __float_as_int(p.w);
 	dxc = dxc > 1 ? dxc - nxc : (dxc < -1 ? dxc + nxc : dxc);
@@ -688,10 +690,36 @@ __device__ __forceinline__ PairGeo pair_geo(const TileSmem &S, int a, int t, flo
 	G.dxo = (qa.x - p.x) + ox;
 	G.dyo = (qa.y - p.y) + oy;
 	G.dzo = (qa.z - p.z) + oz;
-	G.dxn = (qa.x - n.x) + ox;
-	G.dyn = (qa.y - n.y) + oy;
-	G.dzn = (qa.z - n.z) + oz;
+	G.dxn = (qa.x - (p.x + m.x)) + ox;
+	G.dyn = (qa.y - (p.y + m.y)) + oy;
+	G.dzn = (qa.z - (p.z + m.z)) + oz;
 	return G;
+}
+
+/* FP32 rotation matrix of a unit quaternion (w, x, y, z), rows */
+__device__ __forceinline__ void quatmat32(float4 q, float *Q) {
+	const float w = q.x, x = q.y, y = q.z, z = q.w;
+	Q[0] = 1.f - 2.f * (y * y + z * z);
+	Q[1] = 2.f * (x * y - w * z);
+	Q[2] = 2.f * (x * z + w * y);
+	Q[3] = 2.f * (x * y + w * z);
+	Q[4] = 1.f - 2.f * (x * x + z * z);
+	Q[5] = 2.f * (y * z - w * x);
+	Q[6] = 2.f * (x * z - w * y);
+	Q[7] = 2.f * (y * z + w * x);
+	Q[8] = 1.f - 2.f * (x * x + y * y);
+}
+
+/* old (cpo) and candidate (cpn = R . Q) orientation columns of attempt a */
+__device__ __forceinline__ void mover_cols(const TileSmem &S, int a, float *cpo, float *cpn) {
+#pragma unroll
+	for(int k = 0; k < 9; k++) cpo[k] = S.cpo[k][a];
+	float Q[9];
+	quatmat32(S.qr[a], Q);
+#pragma unroll
+	for(int jj = 0; jj < 3; jj++)
+#pragma unroll
+		for(int k3 = 0; k3 < 3; k3++) cpn[3 * jj + k3] = fmaf(cpo[k3], Q[jj], fmaf(cpo[3 + k3], Q[3 + jj], cpo[6 + k3] * Q[6 + jj]));
 }
 
 /* patch tests of the listed close pairs, 32 per step */
@@ -699,27 +727,29 @@ template <int MODE>
 __device__ __forceinline__ void tile_close(const ppi_dev &d, TileSmem &S, int lane, Acc &A) {
 	const int nc = S.nc;
 	for(int c = lane; c < nc; c += 32) {
-		const int2 en = S.cbuf[c];
-		const int jq = en.x, a = en.y >> 4, t = en.y & 15;
+		const int en = S.cbuf[c];
+		const int a = (en >> 4) & 63, t = en & 15;
 		if(S.flag[a] & (TF_OVER | TF_RESCAN)) continue;
-		const int r = S.rep[a];
-		const ppi_rparams &rp = d.rp[r];
+		const int jq = S.mi[a] + (en >> 10);
+		const ppi_rparams &rp = d.rp[S.rep[a]];
 		const float4 qa = d.spos[jq], qb = d.sori[3 * (size_t) jq], qc = d.sori[3 * (size_t) jq + 1], qd = d.sori[3 * (size_t) jq + 2];
 		const float cq[9] = { qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w, qd.x };
 		const PairGeo G = pair_geo(S, a, t, qa);
 		const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
+		float cpo[9], cpn[9];
+		mover_cols(S, a, cpo, cpn);
 		int clo, cln;
 		if(MODE == MODE_AUDIT) {
-			ppi_rstate *rs = d.rs + r;
-			const float4 mq = S.mq[a], md = S.md[a];
+			ppi_rstate *rs = d.rs + S.rep[a];
+			const float4 md = S.md[a];
 			const int pslot = __float_as_int(md.w), qslot = __float_as_int(qd.w);
 			const float3 disp = make_float3(md.x, md.y, md.z);
-			clo = pair_state<MODE>(d, rp, rs, pslot, 0, mq, disp, qslot, G.dxo, G.dyo, G.dzo, S.cp[a], cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0., A);
-			cln = pair_state<MODE>(d, rp, rs, pslot, 1, mq, disp, qslot, G.dxn, G.dyn, G.dzn, S.cp[a] + 9, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0., A);
+			clo = pair_state<MODE>(d.rec, rp, rs, pslot, 0, S.qr[a], disp, qslot, G.dxo, G.dyo, G.dzo, cpo, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0., A.fallbacks);
+			cln = pair_state<MODE>(d.rec, rp, rs, pslot, 1, S.qr[a], disp, qslot, G.dxn, G.dyn, G.dzn, cpn, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0., A.fallbacks);
 		}
 		else {
-			clo = classify(G.dxo, G.dyo, G.dzo, S.cp[a], cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, nullptr);
-			cln = classify(G.dxn, G.dyn, G.dzn, S.cp[a] + 9, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, nullptr);
+			clo = classify(G.dxo, G.dyo, G.dzo, cpo, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, nullptr);
+			cln = classify(G.dxn, G.dyn, G.dzn, cpn, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, nullptr);
 			const int nu = (clo == CL_UNSURE) + (cln == CL_UNSURE);
 			if(nu) {
 				const int k = atomicAdd(&S.nu, nu);
@@ -740,39 +770,44 @@ __device__ __forceinline__ void tile_close(const ppi_dev &d, TileSmem &S, int la
 	__syncwarp();
 }
 
-/* cold path: attempt a's neighbourhood again, every guard-band pair decided exactly on the spot */
-__device__ __noinline__ void tile_rescan(const ppi_dev &d, TileSmem &S, int a, Acc &A) {
+/* cold path: attempt a's neighbourhood again, every guard-band pair decided exactly on the spot;
+ * returns the number of exact re-evaluations */
+__device__ __forceinline__ unsigned tile_rescan(COLD_PARAMS, TileSmem &S, int a) {
 	const float4 md = S.md[a];
 	const int mslot = __float_as_int(md.w);
 	const int i = S.mi[a];
-	const int gc = __float_as_int(d.sori[3 * (size_t) i + 2].z);
-	const int r = d.cell_rep[gc];
-	const ppi_rparams &rp = d.rp[r];
-	const ppi_grid &g = d.grid[r];
-	ppi_rstate *rs = d.rs + r;
+	const int r = S.rep[a];
+	const ppi_rparams &rp = c_rp[r];
+	const ppi_grid &g = c_grid[r];
+	ppi_rstate *rs = c_rs + r;
 	const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
-	const int local = gc - rp.cell_base;
-	const int cx = local % nx, cy = (local / nx) % ny, cz = local / (nx * ny);
+	const int ccp = S.cc[a];
+	const int cx = ccp & 1023, cy = (ccp >> 10) & 1023, cz = ccp >> 20;
 	const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
 	const float rc2e = rp.sqr_rcut_f + eps;
-	const float4 mq = S.mq[a];
+	const float4 mq = S.qr[a];
 	const float3 disp = make_float3(md.x, md.y, md.z);
+	float cpo[9], cpn[9];
+	mover_cols(S, a, cpo, cpn);
 	int bo = 0, bn = 0, over = 0;
+	unsigned fallbacks = 0;
 	for(int t = 0; t < 9 && !over; t++) {
 		const int row = rp.cell_base + (wrapi(cz + t / 3 - 1, nz) * ny + wrapi(cy + t % 3 - 1, ny)) * nx;
 		for(int c = 0; c < 3 && !over; c++) {
 			const int cell = row + wrapi(cx + c - 1, nx);
-			for(int jq = d.cell_start[cell]; jq < d.cell_start[cell + 1]; jq++) {
+			for(int jq = c_cs[cell]; jq < c_cs[cell + 1]; jq++) {
 				if(jq == i) continue;
-				const float4 qa = d.spos[jq];
+				const float4 qa = c_spos[jq];
 				const PairGeo G = pair_geo(S, a, t, qa);
 				const float r2o = fmaf(G.dxo, G.dxo, fmaf(G.dyo, G.dyo, G.dzo * G.dzo)), r2n = fmaf(G.dxn, G.dxn, fmaf(G.dyn, G.dyn, G.dzn * G.dzn));
 				if(!(r2o < rc2e || r2n < rc2e)) continue;
-				const float4 qb = d.sori[3 * (size_t) jq], qc = d.sori[3 * (size_t) jq + 1], qd = d.sori[3 * (size_t) jq + 2];
+				const float4 qb = c_sori[3 * (size_t) jq], qc = c_sori[3 * (size_t) jq + 1], qd = c_sori[3 * (size_t) jq + 2];
 				const float cq[9] = { qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w, qd.x };
 				const int qslot = __float_as_int(qd.w);
-				const int clo = pair_state<MODE_FAST>(d, rp, rs, mslot, 0, mq, disp, qslot, G.dxo, G.dyo, G.dzo, S.cp[a], cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0., A);
-				const int cln = pair_state<MODE_FAST>(d, rp, rs, mslot, 1, mq, disp, qslot, G.dxn, G.dyn, G.dzn, S.cp[a] + 9, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0., A);
+				const int clo = pair_state<MODE_FAST>(c_rec, rp, rs, mslot, 0, mq, disp, qslot, G.dxo, G.dyo, G.dzo, cpo, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0.,
+						fallbacks);
+				const int cln = pair_state<MODE_FAST>(c_rec, rp, rs, mslot, 1, mq, disp, qslot, G.dxn, G.dyn, G.dzn, cpn, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0.,
+						fallbacks);
 				bo += (clo == CL_BOND);
 				bn += (cln == CL_BOND);
 				if(cln == CL_OVER) {
@@ -785,16 +820,40 @@ __device__ __noinline__ void tile_rescan(const ppi_dev &d, TileSmem &S, int a, A
 	S.bo[a] = bo;
 	S.bn[a] = bn;
 	S.flag[a] = over ? TF_OVER : 0;
+	return fallbacks;
 }
 
-/* the 32 attempts of list entries ent (one per lane; ent.x < 0: none) */
-template <int MODE>
-__device__ __forceinline__ void tile_round(const ppi_dev &d, TileSmem &S, const int lane, const int4 ent, long long round, Acc &A) {
-	int flag = TF_CLOSED;
-	int i = 0, cx = 0, cy = 0, cz = 0, nx = 4, ny = 4, nz = 4, cbase = 0;
-	float4 po = make_float4(0.f, 0.f, 0.f, 0.f), pn = po, q = make_float4(1.f, 0.f, 0.f, 0.f);
+/* the rare exact work of a tile iteration: guard-band pairs of the list, then attempts to rescan */
+__device__ __forceinline__ unsigned tile_exact(COLD_PARAMS, TileSmem &S, int lane) {
+	unsigned fallbacks = 0;
+	const int nu = S.nu < TILE_UCAP ? S.nu : TILE_UCAP;
+	for(int u = lane; u < nu; u += 32) {
+		const int2 v = S.uns[u];
+		const int jq = v.x, a = v.y >> 1, kind = v.y & 1;
+		if(S.flag[a] & (TF_OVER | TF_RESCAN)) continue;
+		const float4 md = S.md[a];
+		const int rr = S.rep[a];
+		fallbacks++;
+		const int ex = exact_pair(c_rec, c_rp + rr, c_rs[rr].box, __float_as_int(md.w), kind, S.qr[a], make_float3(md.x, md.y, md.z),
+				__float_as_int(c_sori[3 * (size_t) jq + 2].w), -1, 1., 0., nullptr, nullptr, nullptr);
+		if(ex == 1) atomicAdd(kind ? &S.bn[a] : &S.bo[a], 1);
+		else if(ex == -1 && kind) atomicOr(&S.flag[a], TF_OVER);
+	}
+	__syncwarp();
+	for(int k = 0; k < 2; k++) {
+		const int a = lane + 32 * k;
+		if(S.flag[a] & TF_RESCAN) fallbacks += tile_rescan(c_spos, c_sori, c_cs, c_rec, c_rp, c_grid, c_rs, S, a);
+	}
+	__syncwarp();
+	return fallbacks;
+}
+
+/* proposal of attempt a = (list entry ent): mover, displacement, rotation; returns the attempt's local
+ * cell index (its draws' counter) */
+__device__ __forceinline__ int tile_setup(const ppi_dev &d, TileSmem &S, int a, const int4 ent, long long round, Acc &A) {
+	int flag = TF_CLOSED, i = 0, r = 0, local = 0, pslot = 0;
+	float4 po = make_float4(0.f, 0.f, 0.f, 0.f), q = make_float4(1.f, 0.f, 0.f, 0.f), wv = make_float4(1.f, 1.f, 1.f, __int_as_float(4));
 	float3 disp = make_float3(0.f, 0.f, 0.f);
-	int r = 0, pslot = 0, local = 0;
 	if(ent.x >= 0) {
 		const int gc = ent.x, c0 = ent.y, cnt = ent.z;
 		r = ent.w;
@@ -804,14 +863,11 @@ __device__ __forceinline__ void tile_round(const ppi_dev &d, TileSmem &S, const 
 		}
 		const ppi_rparams &rp = d.rp[r];
 		const ppi_grid &g = d.grid[r];
-		nx = g.n[0];
-		ny = g.n[1];
-		nz = g.n[2];
-		cbase = rp.cell_base;
-		local = gc - cbase;
-		cx = local % nx;
-		cy = (local / nx) % ny;
-		cz = local / (nx * ny);
+		local = gc - rp.cell_base;
+		{
+			const int cx = local % g.n[0], cy = (local / g.n[0]) % g.n[1], cz = local / (g.n[0] * g.n[1]);
+			S.cc[a] = cx | (cy << 10) | (cz << 20);
+		}
 		A.tries++;
 		/* the attempt's Philox draws: particle + displacement, rotation (acceptance only when needed) */
 		const U4 r1 = rng(rp, round, r, TAG_MOVE, (uint32_t) local, 0u), r2 = rng(rp, round, r, TAG_MOVE, (uint32_t) local, 1u);
@@ -819,17 +875,13 @@ __device__ __forceinline__ void tile_round(const ppi_dev &d, TileSmem &S, const 
 		po = d.spos[i];
 		const float dm = rp.disp_max_f;
 		disp = make_float3((u01(r1.y) - 0.5f) * dm, (u01(r1.z) - 0.5f) * dm, (u01(r1.w) - 0.5f) * dm);
-		pn = make_float4(po.x + disp.x, po.y + disp.y, po.z + disp.z, po.w);
-		S.wv[lane] = make_float4(g.wf[0], g.wf[1], g.wf[2], __int_as_float(nx));
+		wv = make_float4(g.wf[0], g.wf[1], g.wf[2], __int_as_float(g.n[0]));
+		const float nx = po.x + disp.x, ny = po.y + disp.y, nz = po.z + disp.z;
 		/* a move that leaves the cell is rejected: cells stay valid and same-colour cells stay independent */
-		if(pn.x >= 0.f && pn.x < g.wf[0] && pn.y >= 0.f && pn.y < g.wf[1] && pn.z >= 0.f && pn.z < g.wf[2]) {
+		if(nx >= 0.f && nx < wv.x && ny >= 0.f && ny < wv.y && nz >= 0.f && nz < wv.z) {
 			flag = 0;
 			const float4 ob = d.sori[3 * (size_t) i], oc = d.sori[3 * (size_t) i + 1], od = d.sori[3 * (size_t) i + 2];
 			pslot = __float_as_int(od.w);
-			/* the canonical x y z and q the commit needs, copied asynchronously into shared memory */
-			const double *rec = d.rec + (size_t) pslot * PPI_REC;
-#pragma unroll
-			for(int k = 0; k < 7; k++) cp_async8(&S.rq[lane][k], rec + k);
 			/* rotation: angle uniform in [0, Theta_max), axis uniform on the sphere (inversion method) */
 			const float theta = u01(r2.x) * rp.theta_max_f;
 			const float zc = 1.f - 2.f * u01(r2.y);
@@ -839,181 +891,199 @@ __device__ __forceinline__ void tile_round(const ppi_dev &d, TileSmem &S, const 
 			__sincosf(phi, &sp, &cph);
 			__sincosf(0.5f * theta, &sh, &ch);
 			q = make_float4(ch, sh * sr * cph, sh * sr * sp, sh * zc);
-			const float cpo[9] = { ob.x, ob.y, ob.z, ob.w, oc.x, oc.y, oc.z, oc.w, od.x };
-			const float w = q.x, x = q.y, y = q.z, z = q.w;
-			float Q[9];
-			Q[0] = 1.f - 2.f * (y * y + z * z);
-			Q[1] = 2.f * (x * y - w * z);
-			Q[2] = 2.f * (x * z + w * y);
-			Q[3] = 2.f * (x * y + w * z);
-			Q[4] = 1.f - 2.f * (x * x + z * z);
-			Q[5] = 2.f * (y * z - w * x);
-			Q[6] = 2.f * (x * z - w * y);
-			Q[7] = 2.f * (y * z + w * x);
-			Q[8] = 1.f - 2.f * (x * x + y * y);
-			float *cp = S.cp[lane];
-#pragma unroll
-			for(int k = 0; k < 9; k++) cp[k] = cpo[k];
-#pragma unroll
-			for(int jj = 0; jj < 3; jj++)
-#pragma unroll
-				for(int k3 = 0; k3 < 3; k3++) cp[9 + 3 * jj + k3] = fmaf(cpo[k3], Q[jj], fmaf(cpo[3 + k3], Q[3 + jj], cpo[6 + k3] * Q[6 + jj]));
+			S.cpo[0][a] = ob.x;
+			S.cpo[1][a] = ob.y;
+			S.cpo[2][a] = ob.z;
+			S.cpo[3][a] = ob.w;
+			S.cpo[4][a] = oc.x;
+			S.cpo[5][a] = oc.y;
+			S.cpo[6][a] = oc.z;
+			S.cpo[7][a] = oc.w;
+			S.cpo[8][a] = od.x;
 		}
 	}
-	S.pos[lane] = po;
-	S.npos[lane] = pn;
-	S.mq[lane] = q;
-	S.md[lane] = make_float4(disp.x, disp.y, disp.z, __int_as_float(pslot));
-	S.mi[lane] = i;
-	S.rep[lane] = r;
-	S.loc[lane] = local;
-	S.bo[lane] = 0;
-	S.bn[lane] = 0;
-	S.flag[lane] = flag;
+	S.pos[a] = po;
+	S.md[a] = make_float4(disp.x, disp.y, disp.z, __int_as_float(pslot));
+	S.wv[a] = wv;
+	S.qr[a] = q;
+	S.mi[a] = i;
+	S.rep[a] = r;
+	S.bo[a] = 0;
+	S.bn[a] = 0;
+	S.flag[a] = flag;
+	return local;
+}
+
+/* the three rows (dy = -1, 0, 1) of plane dz of attempt a's neighbourhood: each row is one or two
+ * contiguous ranges of sorted positions (two where the x range wraps around the box) */
+struct PlaneRanges {
+	int s[6], e[6];
+};
+
+__device__ __forceinline__ int plane_ranges(const ppi_dev &d, const TileSmem &S, int a, int pz, PlaneRanges &P) {
+	int n = 0;
+#pragma unroll
+	for(int k = 0; k < 6; k++) P.s[k] = P.e[k] = 0;
+	if(S.flag[a] & (TF_OVER | TF_CLOSED | TF_RESCAN)) return 0;
+	const int r = S.rep[a];
+	const ppi_grid &g = d.grid[r];
+	const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+	const int cb = d.rp[r].cell_base;
+	const int ccp = S.cc[a];
+	const int cx = ccp & 1023, cy = (ccp >> 10) & 1023, cz = ccp >> 20;
+	const bool inner = cx >= 1 && cx <= nx - 2;
+	const int xa0 = inner ? cx - 1 : (cx == 0 ? nx - 1 : nx - 2), xa1 = inner ? cx + 2 : nx;
+	const int xb1 = cx == 0 ? 2 : 1;
+#pragma unroll
+	for(int ry = 0; ry < 3; ry++) {
+		const int *cs = d.cell_start + cb + (wrapi(cz + pz - 1, nz) * ny + wrapi(cy + ry - 1, ny)) * nx;
+		P.s[2 * ry] = cs[xa0];
+		P.e[2 * ry] = cs[xa1];
+		if(!inner) {
+			P.s[2 * ry + 1] = cs[0];
+			P.e[2 * ry + 1] = cs[xb1];
+		}
+	}
+#pragma unroll
+	for(int k = 0; k < 6; k++) n += P.e[k] - P.s[k];
+	return n;
+}
+
+/* attempt a's pairs of plane pz into the pair list from position pos */
+__device__ __forceinline__ void write_pairs(TileSmem &S, int a, int pz, const PlaneRanges &P, int pos) {
+	const int i = S.mi[a];
+#pragma unroll
+	for(int sg = 0; sg < 6; sg++) {
+		const int tag = (a << 4) | (3 * pz + (sg >> 1));
+		for(int jq = P.s[sg]; jq < P.e[sg]; jq++) {
+			const int off = jq - i;
+			if(off >= TILE_OFF_MAX || off <= -TILE_OFF_MAX) {
+				atomicOr(&S.flag[a], TF_RESCAN);
+				S.pbuf[pos++] = tag; /* offset 0 = the mover itself: skipped */
+			}
+			else S.pbuf[pos++] = (int) ((unsigned) off << 10) | tag;
+		}
+	}
+}
+
+/* the TA attempts of list entries e0 (lane's first) and e1 (lane's second); ent.x < 0: none */
+template <int MODE>
+__device__ __forceinline__ void tile_round(const ppi_dev &d, TileSmem &S, const int lane, const int4 e0, const int4 e1, long long round, Acc &A) {
+	const int loc0 = tile_setup(d, S, lane, e0, round, A);
+	const int loc1 = tile_setup(d, S, lane + 32, e1, round, A);
 	if(lane == 0) {
 		S.nc = 0;
 		S.nu = 0;
 	}
 	__syncwarp();
-	/* the neighbour planes dz = -1, 0, 1, one at a time for all 32 attempts (3 rows each) */
-	{
-		const ppi_rparams &rpl = d.rp[r];
-		const float eps = rpl.precision == 1 ? 1e30f : rpl.eps_f;
-		const float rc2e = rpl.sqr_rcut_f + eps, ovl = 1.f - eps;
-		/* x ranges of a row: cells xm, cx, xp as one or two contiguous ranges of sorted positions */
-		const int xa0 = (cx >= 1 && cx <= nx - 2) ? cx - 1 : (cx == 0 ? nx - 1 : nx - 2);
-		const int xa1 = (cx >= 1 && cx <= nx - 2) ? cx + 2 : nx;
-		const int xb1 = (cx >= 1 && cx <= nx - 2) ? 0 : (cx == 0 ? 2 : 1);
-		const unsigned lt = (1u << lane) - 1u;
+	const unsigned lt = (1u << lane) - 1u;
 #pragma unroll 1
-		for(int pz = 0; pz < 3; pz++) {
-			int sa[3], ea[3], sb[3], eb[3];
-			int n = 0;
-			const int live = !(S.flag[lane] & (TF_OVER | TF_CLOSED | TF_RESCAN));
+	for(int pz = 0; pz < 3; pz++) {
+		PlaneRanges P0, P1;
+		const int n0 = plane_ranges(d, S, lane, pz, P0);
+		const int n1 = plane_ranges(d, S, lane + 32, pz, P1);
+		const int n = n0 + n1;
+		int incl = n;
 #pragma unroll
-			for(int ry = 0; ry < 3; ry++) {
-				sa[ry] = ea[ry] = sb[ry] = eb[ry] = 0;
-				if(live) {
-					const int *cs = d.cell_start + cbase + (wrapi(cz + pz - 1, nz) * ny + wrapi(cy + ry - 1, ny)) * nx;
-					sa[ry] = cs[xa0];
-					ea[ry] = cs[xa1];
-					sb[ry] = cs[0];
-					eb[ry] = cs[xb1];
+		for(int o = 1; o < 32; o <<= 1) {
+			const int v = __shfl_up_sync(0xffffffffu, incl, o);
+			if(lane >= o) incl += v;
+		}
+		if(__shfl_sync(0xffffffffu, incl, 31) == 0) continue;
+		/* the lanes whose slices fit into the list; the others are rescanned exactly (dense corner case) */
+		const unsigned fit = __ballot_sync(0xffffffffu, incl <= TILE_PCAP);
+		const int np = fit ? __shfl_sync(0xffffffffu, incl, 31 - __clz(fit)) : 0;
+		if(incl > TILE_PCAP) {
+			if(n0) atomicOr(&S.flag[lane], TF_RESCAN);
+			if(n1) atomicOr(&S.flag[lane + 32], TF_RESCAN);
+		}
+		else {
+			const int pos = incl - n;
+			write_pairs(S, lane, pz, P0, pos);
+			write_pairs(S, lane + 32, pz, P1, pos + n0);
+		}
+		__syncwarp();
+		for(int p0 = 0; p0 < np; p0 += 32) {
+			const int p = p0 + lane;
+			int close = 0, en = 0;
+			if(p < np) {
+				en = S.pbuf[p];
+				const int a = (en >> 4) & 63, off = en >> 10;
+				if(off != 0 && !(S.flag[a] & (TF_OVER | TF_RESCAN))) {
+					const int jq = S.mi[a] + off;
+					const float4 qa = d.spos[jq];
+					const PairGeo G = pair_geo(S, a, en & 15, qa);
+					const float r2o = fmaf(G.dxo, G.dxo, fmaf(G.dyo, G.dyo, G.dzo * G.dzo));
+					const float r2n = fmaf(G.dxn, G.dxn, fmaf(G.dyn, G.dyn, G.dzn * G.dzn));
+					const ppi_rparams &rp = d.rp[S.rep[a]];
+					const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
+					A.pairs += 2;
+					if(MODE != MODE_AUDIT && r2n < 1.f - eps) atomicOr(&S.flag[a], TF_OVER); /* certain overlap of the candidate state */
+					else close = MODE == MODE_AUDIT || r2o < rp.sqr_rcut_f + eps || r2n < rp.sqr_rcut_f + eps;
 				}
-				n += (ea[ry] - sa[ry]) + (eb[ry] - sb[ry]);
 			}
-			int incl = n;
-#pragma unroll
-			for(int o = 1; o < 32; o <<= 1) {
-				const int v = __shfl_up_sync(0xffffffffu, incl, o);
-				if(lane >= o) incl += v;
-			}
-			if(__shfl_sync(0xffffffffu, incl, 31) == 0) continue;
-			/* the lanes whose slices fit into the list; the others are rescanned exactly (dense corner case) */
-			const unsigned fit = __ballot_sync(0xffffffffu, incl <= TILE_PCAP);
-			const int np = fit ? __shfl_sync(0xffffffffu, incl, 31 - __clz(fit)) : 0;
-			if(incl > TILE_PCAP) {
-				if(n) atomicOr(&S.flag[lane], TF_RESCAN);
-			}
-			else {
-				int pos = incl - n;
-#pragma unroll
-				for(int ry = 0; ry < 3; ry++) {
-					const int tag = (lane << 4) | (3 * pz + ry);
-					for(int jq = sa[ry]; jq < ea[ry]; jq++) S.pbuf[pos++] = make_int2(jq, tag);
-					for(int jq = sb[ry]; jq < eb[ry]; jq++) S.pbuf[pos++] = make_int2(jq, tag);
-				}
-			}
-			__syncwarp();
-			for(int p0 = 0; p0 < np; p0 += 32) {
-				const int p = p0 + lane;
-				int close = 0;
-				int2 en = make_int2(0, 0);
-				if(p < np) {
-					en = S.pbuf[p];
-					const int jq = en.x, a = en.y >> 4;
-					if(jq != S.mi[a] && !(S.flag[a] & (TF_OVER | TF_RESCAN))) {
-						const float4 qa = d.spos[jq];
-						const PairGeo G = pair_geo(S, a, en.y & 15, qa);
-						const float r2o = fmaf(G.dxo, G.dxo, fmaf(G.dyo, G.dyo, G.dzo * G.dzo));
-						const float r2n = fmaf(G.dxn, G.dxn, fmaf(G.dyn, G.dyn, G.dzn * G.dzn));
-						A.pairs += 2;
-						if(MODE != MODE_AUDIT && r2n < ovl) atomicOr(&S.flag[a], TF_OVER); /* certain overlap of the candidate state */
-						else close = MODE == MODE_AUDIT || r2o < rc2e || r2n < rc2e;
-					}
-				}
-				/* compact the close pairs into the patch-test list */
-				const unsigned m = __ballot_sync(0xffffffffu, close);
-				if(m) {
-					if(S.nc + __popc(m) > TILE_CCAP) tile_close<MODE>(d, S, lane, A);
-					if(close) S.cbuf[S.nc + __popc(m & lt)] = en;
-					__syncwarp();
-					if(lane == 0) S.nc += __popc(m);
-					__syncwarp();
-				}
+			/* compact the close pairs into the patch-test list */
+			const unsigned m = __ballot_sync(0xffffffffu, close);
+			if(m) {
+				if(S.nc + __popc(m) > TILE_CCAP) tile_close<MODE>(d, S, lane, A);
+				if(close) S.cbuf[S.nc + __popc(m & lt)] = en;
+				__syncwarp();
+				if(lane == 0) S.nc += __popc(m);
+				__syncwarp();
 			}
 		}
 	}
 	if(S.nc) tile_close<MODE>(d, S, lane, A);
-	/* guard-band pairs: exact decisions */
-	const int nu = S.nu < TILE_UCAP ? S.nu : TILE_UCAP;
-	for(int u = lane; u < nu; u += 32) {
-		const int2 v = S.uns[u];
-		const int jq = v.x, a = v.y >> 1, kind = v.y & 1;
-		if(S.flag[a] & (TF_OVER | TF_RESCAN)) continue;
-		const float4 md = S.md[a];
-		const int rr = S.rep[a];
-		A.fallbacks++;
-		const int ex = exact_pair(d.rec, d.rp + rr, d.rs[rr].box, __float_as_int(md.w), kind, S.mq[a], make_float3(md.x, md.y, md.z),
-				__float_as_int(d.sori[3 * (size_t) jq + 2].w), -1, 1., 0., nullptr, nullptr, nullptr);
-		if(ex == 1) atomicAdd(kind ? &S.bn[a] : &S.bo[a], 1);
-		else if(ex == -1 && kind) atomicOr(&S.flag[a], TF_OVER);
-	}
-	__syncwarp();
-	flag = S.flag[lane];
-	if(flag & TF_RESCAN) {
-		tile_rescan(d, S, lane, A);
-		flag = S.flag[lane];
-	}
-	if(flag & (TF_OVER | TF_CLOSED)) return;
-	/* Metropolis on dE = -(bn - bo) (MC.c:330-339); the attempt's state comes back from shared memory */
-	r = S.rep[lane];
-	const ppi_rparams &rp = d.rp[r];
-	const int bo = S.bo[lane], bn = S.bn[lane];
-	const int dE = bo - bn;
-	if(dE > 0) {
-		const U4 u3 = rng(rp, round, r, TAG_MOVE, (uint32_t) S.loc[lane], 2u);
-		const uint64_t U = ((uint64_t) u3.x << 21) | (u3.y >> 11);
-		if(!(U < rp.acc_thr[dE < 31 ? dE : 31])) return;
-	}
-	A.acc++;
-	A.dbonds += bn - bo;
-	/* commit: FP64 q' = q (x) dq and r' = r + disp (state64 defines the same bits), FP32 record */
-	const float4 mq = S.mq[lane], md = S.md[lane];
-	i = S.mi[lane];
-	cp_async_wait_all();
-	const double *rq = S.rq[lane];
-	const double qv[4] = { rq[3], rq[4], rq[5], rq[6] };
-	const double b[4] = { f2d(mq.x), f2d(mq.y), f2d(mq.z), f2d(mq.w) };
-	double *rec = d.rec + (size_t) __float_as_int(md.w) * PPI_REC;
-	double qn[4];
+	/* guard-band pairs and rescans: exact decisions, out of line */
+	const int need = (S.nu > 0) | ((S.flag[lane] | S.flag[lane + 32]) & TF_RESCAN);
+	if(__any_sync(0xffffffffu, need)) A.fallbacks += tile_exact(COLD_ARGS(d), S, lane);
+#pragma unroll 1
+	for(int k = 0; k < 2; k++) {
+		const int a = lane + 32 * k;
+		const int flag = S.flag[a];
+		if(flag & (TF_OVER | TF_CLOSED)) continue;
+		/* Metropolis on dE = -(bn - bo) (MC.c:330-339) */
+		const int r = S.rep[a];
+		const ppi_rparams &rp = d.rp[r];
+		const int bo = S.bo[a], bn = S.bn[a];
+		const int dE = bo - bn;
+		if(dE > 0) {
+			const U4 u3 = rng(rp, round, r, TAG_MOVE, (uint32_t) (k ? loc1 : loc0), 2u);
+			const uint64_t U = ((uint64_t) u3.x << 21) | (u3.y >> 11);
+			if(!(U < rp.acc_thr[dE < 31 ? dE : 31])) continue;
+		}
+		if(r != A.r) {
+			flush_thread(d, A);
+			A.r = r;
+		}
+		A.acc++;
+		A.dbonds += bn - bo;
+		/* commit: FP64 q' = q (x) dq and r' = r + disp (state64 defines the same bits), FP32 record */
+		const float4 mq = S.qr[a], md = S.md[a];
+		const int i = S.mi[a];
+		double *rec = d.rec + (size_t) __float_as_int(md.w) * PPI_REC;
+		const double2 r01 = *(const double2 *) rec, r23 = *(const double2 *) (rec + 2), r45 = *(const double2 *) (rec + 4);
+		const double r6 = rec[6];
+		const double qv[4] = { r23.y, r45.x, r45.y, r6 };
+		const double b[4] = { f2d(mq.x), f2d(mq.y), f2d(mq.z), f2d(mq.w) };
+		double qn[4];
 #pragma unroll
-	for(int c = 0; c < 4; c++) qn[c] = qcomp64(qv[c], qv[c ^ 1], qv[c ^ 2], qv[c ^ 3], b, c);
-	rec[0] = __dadd_rn(rq[0], f2d(md.x));
-	rec[1] = __dadd_rn(rq[1], f2d(md.y));
-	rec[2] = __dadd_rn(rq[2], f2d(md.z));
-	rec[PPI_Q] = qn[0];
-	rec[PPI_Q + 1] = qn[1];
-	rec[PPI_Q + 2] = qn[2];
-	rec[PPI_Q + 3] = qn[3];
-	d.spos[i] = S.npos[lane];
-	const float *cp = S.cp[lane];
-	d.sori[3 * (size_t) i] = make_float4(cp[9], cp[10], cp[11], cp[12]);
-	d.sori[3 * (size_t) i + 1] = make_float4(cp[13], cp[14], cp[15], cp[16]);
-	((float *) (d.sori + 3 * (size_t) i + 2))[0] = cp[17];
+		for(int c = 0; c < 4; c++) qn[c] = qcomp64(qv[c], qv[c ^ 1], qv[c ^ 2], qv[c ^ 3], b, c);
+		*(double2 *) rec = make_double2(__dadd_rn(r01.x, f2d(md.x)), __dadd_rn(r01.y, f2d(md.y)));
+		*(double2 *) (rec + 2) = make_double2(__dadd_rn(r23.x, f2d(md.z)), qn[0]);
+		*(double2 *) (rec + 4) = make_double2(qn[1], qn[2]);
+		rec[6] = qn[3];
+		const float4 po = S.pos[a];
+		d.spos[i] = make_float4(po.x + md.x, po.y + md.y, po.z + md.z, po.w);
+		float cpo[9], cpn[9];
+		mover_cols(S, a, cpo, cpn);
+		d.sori[3 * (size_t) i] = make_float4(cpn[0], cpn[1], cpn[2], cpn[3]);
+		d.sori[3 * (size_t) i + 1] = make_float4(cpn[4], cpn[5], cpn[6], cpn[7]);
+		((float *) (d.sori + 3 * (size_t) i + 2))[0] = cpn[8];
+	}
 }
 
-/* one colour of a round: the colour's non-empty cells, 32 per warp and iteration */
+/* one colour of a round: the colour's non-empty cells, TA per warp and iteration */
 template <int MODE>
 __global__ void __launch_bounds__(32 * TILE_WARPS, MODE == MODE_FAST ? PPI_TILE_MIN_BLOCKS : 1) k_colour(ppi_dev d, long long round, int col) {
 	__shared__ TileSmem s_tile[TILE_WARPS];
@@ -1022,21 +1092,20 @@ __global__ void __launch_bounds__(32 * TILE_WARPS, MODE == MODE_FAST ? PPI_TILE_
 	const int4 *list = d.clist + (size_t) col * d.clist_cap;
 	int cnt = d.ccount[col];
 	if(cnt > d.clist_cap) cnt = d.clist_cap;
-	if(blockIdx.x * blockDim.x >= cnt) return; /* the whole CTA has no entry: leave before any reduction */
 	Acc A;
 	A.r = -1;
 	A.tries = A.acc = A.pairs = A.fallbacks = 0;
 	A.dbonds = 0;
 	const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarp = (gridDim.x * blockDim.x) >> 5;
-	int b = warp * 32;
-	int4 ent = (b + lane < cnt) ? list[b + lane] : make_int4(-1, 0, 0, 0);
-	for(; b < cnt; b += nwarp * 32) {
-		const int en = b + nwarp * 32 + lane;
-		const int4 next = (en < cnt) ? list[en] : make_int4(-1, 0, 0, 0); /* next entry requested early */
-		tile_round<MODE>(d, S, lane, ent, round, A);
-		cp_async_wait_all(); /* no copy may still target this warp's shared memory */
+	/* every resident warp gets an equal share of the list (the CTA scheduler does not spread the
+	 * working CTAs of a partly filled grid evenly over the SMs) */
+	const int lo = (int) ((long long) warp * cnt / nwarp), hi = (int) ((long long) (warp + 1) * cnt / nwarp);
+	const int4 none = make_int4(-1, 0, 0, 0);
+	for(int b = lo; b < hi; b += TA) {
+		const int4 e0 = (b + lane < hi) ? list[b + lane] : none;
+		const int4 e1 = (b + 32 + lane < hi) ? list[b + 32 + lane] : none;
+		tile_round<MODE>(d, S, lane, e0, e1, round, A);
 		__syncwarp();
-		ent = next;
 	}
 	flush_block(d, A);
 }
@@ -1141,12 +1210,16 @@ struct EnergyCtx {
 };
 
 /* cold path of a lane that met more than UNS_CAP guard-band pairs in the energy pass: its rows again,
- * every guard-band pair decided exactly on the spot. Returns the overlap count; bonds in *nb_out. */
+ * every guard-band pair decided exactly on the spot. Returns bonds | overlaps << 16 | exact
+ * re-evaluations << 32. */
 template <int G>
-__device__ __noinline__ int energy_lane_exact(const ppi_dev &d, const ppi_rparams &rp, ppi_rstate *rs, const EnergyCtx &E, int sub, Acc &A, int *nb_out) {
+__device__ __forceinline__ unsigned long long energy_lane_exact(COLD_PARAMS, int r, const EnergyCtx &E, int sub) {
+	const ppi_rparams &rp = c_rp[r];
+	ppi_rstate *rs = c_rs + r;
 	const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
 	const float sqr_rcut = rp.sqr_rcut_f, cosmax = rp.cosmax_f, basef = rp.base_f, rc2e = sqr_rcut + eps;
-	const int *cs = d.cell_start;
+	const int *cs = c_cs;
+	unsigned fallbacks = 0;
 	const float4 q0 = make_float4(1.f, 0.f, 0.f, 0.f);
 	const float3 d0 = make_float3(0.f, 0.f, 0.f);
 	int nb = 0, no = 0;
@@ -1158,16 +1231,16 @@ __device__ __noinline__ int energy_lane_exact(const ppi_dev &d, const ppi_rparam
 			const float ox = (c - 1) * E.w[0], oy = dy * E.w[1], oz = dz * E.w[2];
 			for(int jq = cs[cell]; jq < cs[cell + 1]; jq++) {
 				if(jq == E.k) continue;
-				const float4 qa = d.spos[jq];
+				const float4 qa = c_spos[jq];
 				float ql[3] = { qa.x, qa.y, qa.z };
 				if(E.sdir >= 0) ql[E.sdir] *= E.sf;
 				const float ddx = (ql[0] - E.pl[0]) + ox, ddy = (ql[1] - E.pl[1]) + oy, ddz = (ql[2] - E.pl[2]) + oz;
 				const float r2 = fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz));
 				if(r2 >= rc2e) continue;
-				const float4 qb = d.sori[3 * (size_t) jq], qc = d.sori[3 * (size_t) jq + 1], qd = d.sori[3 * (size_t) jq + 2];
+				const float4 qb = c_sori[3 * (size_t) jq], qc = c_sori[3 * (size_t) jq + 1], qd = c_sori[3 * (size_t) jq + 2];
 				const float cq[9] = { qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w, qd.x };
-				const int cl = pair_state<MODE_FAST>(d, rp, rs, E.pslot, 0, q0, d0, __float_as_int(qd.w), ddx, ddy, ddz, E.cp, cq, sqr_rcut, cosmax, basef, eps, E.sdir,
-						E.vf, E.vside, A);
+				const int cl = pair_state<MODE_FAST>(c_rec, rp, rs, E.pslot, 0, q0, d0, __float_as_int(qd.w), ddx, ddy, ddz, E.cp, cq, sqr_rcut, cosmax, basef, eps, E.sdir,
+						E.vf, E.vside, fallbacks);
 				if(cl == CL_BOND) {
 					if(E.partners && nb < PPI_MAX_PARTNERS) E.partners[nb] = __float_as_int(qd.y);
 					nb++;
@@ -1176,8 +1249,7 @@ __device__ __noinline__ int energy_lane_exact(const ppi_dev &d, const ppi_rparam
 			}
 		}
 	}
-	*nb_out = nb;
-	return no;
+	return (unsigned long long) (nb & 0xffff) | ((unsigned long long) (no & 0xffff) << 16) | ((unsigned long long) fallbacks << 32);
 }
 
 /* energy of one particle from scratch, G lanes: bond and overlap counts over all partners (MC_energy,
@@ -1270,7 +1342,7 @@ __device__ __forceinline__ void energy_particle(const ppi_dev &d, int mode, int 
 					const float4 qd = d.sori[3 * (size_t) jq + 2];
 					const float cq[9] = { qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w, qd.x };
 					if(MODE == MODE_AUDIT)
-						cl = pair_state<MODE>(d, rp, rs, pslot, 0, q0, d0, __float_as_int(qd.w), ddx, ddy, ddz, cp, cq, sqr_rcut, cosmax, basef, eps, sdir, vf, vside, A);
+						cl = pair_state<MODE>(d.rec, rp, rs, pslot, 0, q0, d0, __float_as_int(qd.w), ddx, ddy, ddz, cp, cq, sqr_rcut, cosmax, basef, eps, sdir, vf, vside, A.fallbacks);
 					else {
 						cl = classify(ddx, ddy, ddz, cp, cq, sqr_rcut, cosmax, basef, eps, nullptr);
 						if(cl == CL_UNSURE) U.push(jq << 1);
@@ -1307,7 +1379,10 @@ __device__ __forceinline__ void energy_particle(const ppi_dev &d, int mode, int 
 			E.vf = vf;
 			E.vside = vside;
 			E.partners = partners;
-			no = energy_lane_exact<G>(d, rp, rs, E, sub, A, &nb);
+			const unsigned long long res = energy_lane_exact<G>(COLD_ARGS(d), r, E, sub);
+			nb = (int) (res & 0xffff);
+			no = (int) ((res >> 16) & 0xffff);
+			A.fallbacks += (unsigned) (res >> 32);
 		}
 		else {
 #pragma unroll 1
