@@ -201,7 +201,7 @@ long long pp_gpu_launch_count(const pp_engine *e) { return e ? e->launches : 0; 
 static void free_device(pp_engine *e) {
 	void **ptrs[] = { (void **) &e->d.rec, (void **) &e->d.spos, (void **) &e->d.sori, (void **) &e->d.id, (void **) &e->d.rep, (void **) &e->d.cellof,
 		(void **) &e->d.cell_count, (void **) &e->d.cell_start, (void **) &e->d.cell_cursor, (void **) &e->d.cell_rep, (void **) &e->d.scan_aux,
-		(void **) &e->d.clist, (void **) &e->d.ccount, (void **) &e->d.rp, (void **) &e->d.rs, (void **) &e->d.grid, (void **) &e->d.out_bonds,
+		(void **) &e->d.clist, (void **) &e->d.ccount, (void **) &e->d.dflag, (void **) &e->d.eflag, (void **) &e->d.rp, (void **) &e->d.rs, (void **) &e->d.grid, (void **) &e->d.out_bonds,
 		(void **) &e->d.out_overlaps, (void **) &e->d.out_partners, (void **) &e->d.tmp_rec, (void **) &e->d.tmp_id };
 	for(size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); i++) {
 		if(*ptrs[i]) cudaFree(*ptrs[i]);
@@ -406,6 +406,10 @@ static int commit(pp_engine *e) {
 	CU(cudaMalloc((void **) &d->scan_aux, sizeof(int) * ((cells + 1023) / 1024 + 1)));
 	CU(cudaMalloc((void **) &d->clist, sizeof(int4) * 8 * (size_t) d->clist_cap));
 	CU(cudaMalloc((void **) &d->ccount, sizeof(int) * 8));
+	CU(cudaMalloc((void **) &d->dflag, 8 * (size_t) d->clist_cap));
+	CU(cudaMemsetAsync(d->dflag, 0, 8 * (size_t) d->clist_cap, e->stream));
+	CU(cudaMalloc((void **) &d->eflag, n1));
+	CU(cudaMemsetAsync(d->eflag, 0, n1, e->stream));
 	d->audit_any = e->any_audit;
 	{ /* lanes per attempt: a tuning override for measurements (4 by default) */
 		const char *v = getenv("PPGPU_LANES");

@@ -108,6 +108,8 @@ typedef struct ppi_dev {
 	int *scan_aux;
 	int4 *clist;       /* 8 lists of capacity clist_cap each */
 	int *ccount;       /* 8 counters */
+	unsigned char *dflag; /* 8 x clist_cap: deferred attempts a warp could not keep in shared memory */
+	unsigned char *eflag; /* ntot: the same for particles of the energy pass */
 	int audit_any;     /* some replica audits: every pass runs in audit mode */
 	int lanes;         /* lanes per attempt of the colour and energy passes (4 or 8; 0 = default) */
 	int clist_cap;

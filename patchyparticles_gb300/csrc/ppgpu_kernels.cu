@@ -234,6 +234,124 @@ __device__ __noinline__ int exact_pair(const double *__restrict__ rec_all, const
 	return interact64(P, P + 3, Qr, Qr + 3, rp->base, box, rp->sqr_rcut, rp->cosmax, o_dist2, o_pmax, o_qmax);
 }
 
+/* Certified FP64 decision of one pair without the reference's division and square root chain.
+ * The distance test is the reference's own operation sequence (MC.c:232-245), so it is bit-identical:
+ * d = q - p, minimum image d - box * rint(d / box), dist2 = d . d. Only rint's argument is formed with
+ * the reciprocal of the box; it can round differently from d / box only within ~1e-15 of a half
+ * integer, which is checked. The patch test (MC.c:246-265) is evaluated to ~1e-15 with Newton
+ * reciprocals (norm of d, norm of q); a cosine farther than DEC64_TOL from KF_cosmax is then on the same
+ * side of it as the reference's FP64 value. Anything closer returns DEC64_EXACT and the caller runs the
+ * bit-identical exact_pair. Returns -1 overlap, 0 no bond, 1 bond. */
+#define DEC64_TOL 1e-12
+#define DEC64_EXACT 2
+
+__device__ __forceinline__ double rcp64(double x) { /* 1 / x to ~1e-16, x > 0 */
+	double r = (double) (1.0f / (float) x);
+	r = r * (2.0 - x * r);
+	r = r * (2.0 - x * r);
+	return r;
+}
+
+__device__ __forceinline__ double rsqrt64(double x) { /* 1 / sqrt(x) to ~1e-16, x > 0 */
+	double y = (double) rsqrtf((float) x);
+	y = y * (1.5 - 0.5 * x * y * y);
+	y = y * (1.5 - 0.5 * x * y * y);
+	y = y * (1.5 - 0.5 * x * y * y);
+	return y;
+}
+
+/* orientation R0 . Q(q) to ~1e-15 (the canonical value is orient64's; this is only compared with a margin) */
+__device__ __forceinline__ void orient64_fast(const double *R0, const double *q, double *R) {
+	const double w = q[0], x = q[1], y = q[2], z = q[3];
+	const double s = 2.0 * rcp64(w * w + x * x + y * y + z * z);
+	double Q[9];
+	Q[0] = 1.0 - s * (y * y + z * z);
+	Q[1] = s * (x * y - w * z);
+	Q[2] = s * (x * z + w * y);
+	Q[3] = s * (x * y + w * z);
+	Q[4] = 1.0 - s * (x * x + z * z);
+	Q[5] = s * (y * z - w * x);
+	Q[6] = s * (x * z - w * y);
+	Q[7] = s * (y * z + w * x);
+	Q[8] = 1.0 - s * (x * x + y * y);
+#pragma unroll
+	for(int i = 0; i < 3; i++)
+#pragma unroll
+		for(int j = 0; j < 3; j++) R[3 * i + j] = fma(R0[3 * i], Q[j], fma(R0[3 * i + 1], Q[3 + j], R0[3 * i + 2] * Q[6 + j]));
+}
+
+/* canonical position (bit-exact, as state64) and approximate orientation of slot ps, state kind */
+__device__ __forceinline__ void state64_fast(const double *__restrict__ rec_all, int ps, int kind, float4 dq, float3 disp, double *r, double *R) {
+	const double *rec = rec_all + (size_t) ps * PPI_REC;
+	double q[4] = { rec[PPI_Q], rec[PPI_Q + 1], rec[PPI_Q + 2], rec[PPI_Q + 3] };
+	r[0] = rec[0];
+	r[1] = rec[1];
+	r[2] = rec[2];
+	if(kind == 1) {
+		const double b[4] = { f2d(dq.x), f2d(dq.y), f2d(dq.z), f2d(dq.w) };
+		double qn[4];
+#pragma unroll
+		for(int c = 0; c < 4; c++) qn[c] = qcomp64(q[c], q[c ^ 1], q[c ^ 2], q[c ^ 3], b, c);
+#pragma unroll
+		for(int c = 0; c < 4; c++) q[c] = qn[c];
+		r[0] = __dadd_rn(r[0], f2d(disp.x));
+		r[1] = __dadd_rn(r[1], f2d(disp.y));
+		r[2] = __dadd_rn(r[2], f2d(disp.z));
+	}
+	double R0[9];
+#pragma unroll
+	for(int k = 0; k < 9; k++) R0[k] = rec[PPI_R0 + k];
+	orient64_fast(R0, q, R);
+}
+
+__device__ __forceinline__ int decide64(const double *__restrict__ rec_all, const ppi_rparams &rp, const double *box_in, const double *inv_box_in, int ps, int kind, float4 dq,
+		float3 disp, int qs, int vol_dir, double vol_f, double vol_side) {
+	double rp_[3], Rp[9], rq_[3], Rq[9];
+	state64_fast(rec_all, ps, kind, dq, disp, rp_, Rp);
+	state64_fast(rec_all, qs, 0, dq, disp, rq_, Rq);
+	double box[3] = { box_in[0], box_in[1], box_in[2] }, ib[3] = { inv_box_in[0], inv_box_in[1], inv_box_in[2] };
+	if(vol_dir >= 0) {
+		rp_[vol_dir] = __dmul_rn(rp_[vol_dir], vol_f);
+		rq_[vol_dir] = __dmul_rn(rq_[vol_dir], vol_f);
+		box[vol_dir] = vol_side;
+		ib[vol_dir] = rcp64(vol_side);
+	}
+	double d[3];
+#pragma unroll
+	for(int k = 0; k < 3; k++) {
+		d[k] = __dsub_rn(rq_[k], rp_[k]);
+		const double t = d[k] * ib[k], n = rint(t);
+		if(fabs(t - n) > 0.5 - 1e-9) return DEC64_EXACT; /* rint of d / box could round the other way */
+		d[k] = __dsub_rn(d[k], __dmul_rn(box[k], n));
+	}
+	const double dist2 = __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])), __dmul_rn(d[2], d[2]));
+	if(dist2 < 1.) return -1;
+	if(!(dist2 < rp.sqr_rcut)) return 0;
+	const double in = rsqrt64(dist2);
+	const double u[3] = { d[0] * in, d[1] * in, d[2] * in };
+	const double cmax = rp.cosmax;
+	int p_yes = 0, p_unsure = 0, q_yes = 0, q_unsure = 0;
+#pragma unroll
+	for(int a = 0; a < 4; a++) {
+		const double *b = rp.base[a];
+		double c = 0.;
+#pragma unroll
+		for(int k = 0; k < 3; k++) c = fma(u[k], fma(Rp[3 * k], b[0], fma(Rp[3 * k + 1], b[1], Rp[3 * k + 2] * b[2])), c);
+		p_yes |= c > cmax + DEC64_TOL;
+		p_unsure |= fabs(c - cmax) <= DEC64_TOL;
+		double e = 0.;
+#pragma unroll
+		for(int k = 0; k < 3; k++) e = fma(u[k], fma(Rq[3 * k], b[0], fma(Rq[3 * k + 1], b[1], Rq[3 * k + 2] * b[2])), e);
+		e = -e;
+		q_yes |= e > cmax + DEC64_TOL;
+		q_unsure |= fabs(e - cmax) <= DEC64_TOL;
+	}
+	/* bond iff some patch of p and some patch of q point at each other (MC.c:255-263) */
+	if(p_yes && q_yes) return 1;
+	if((!p_yes && !p_unsure) || (!q_yes && !q_unsure)) return 0;
+	return DEC64_EXACT;
+}
+
 /* ------------------------------------------------------------------------------------------------ */
 /* FP32 classification with guard band                                                              */
 /* ------------------------------------------------------------------------------------------------ */
@@ -619,44 +737,42 @@ __device__ __forceinline__ int wrapi(int v, int n) { return v < 0 ? v + n : (v >
 
 /* the FP32 decision for one pair and one state of p, made exact in the guard band */
 template <int MODE>
-__device__ __forceinline__ int pair_state(const double *rec, const ppi_rparams &rp, ppi_rstate *rs, int pslot, int kind, float4 q, float3 disp, int qslot,
-		float dx, float dy, float dz, const float *cp, const float *cq, float sqr_rcut, float cosmax, float basef, float eps, int vol_dir, double vol_f,
+__device__ __forceinline__ int pair_state(const double *rec, const ppi_rparams &rp, ppi_rstate *rs, const double *inv_box, int pslot, int kind, float4 q, float3 disp,
+		int qslot, float dx, float dy, float dz, const float *cp, const float *cq, float sqr_rcut, float cosmax, float basef, float eps, int vol_dir, double vol_f,
 		double vol_side, unsigned &fallbacks) {
 	PairF f;
 	int cl = classify(dx, dy, dz, cp, cq, sqr_rcut, cosmax, basef, eps, MODE == MODE_AUDIT ? &f : nullptr);
 	if(MODE == MODE_AUDIT) audit_pair(rec, &rp, rs, rs->box, pslot, kind, q, disp, qslot, vol_dir, vol_f, vol_side, cl, f);
 	if(cl == CL_UNSURE) {
 		fallbacks++;
-		int ex = exact_pair(rec, &rp, rs->box, pslot, kind, q, disp, qslot, vol_dir, vol_f, vol_side, nullptr, nullptr, nullptr);
+		int ex = decide64(rec, rp, rs->box, inv_box, pslot, kind, q, disp, qslot, vol_dir, vol_f, vol_side);
+		if(ex == DEC64_EXACT) ex = exact_pair(rec, &rp, rs->box, pslot, kind, q, disp, qslot, vol_dir, vol_f, vol_side, nullptr, nullptr, nullptr);
 		cl = ex == -1 ? CL_OVER : (ex == 1 ? CL_BOND : CL_NONE);
 	}
 	return cl;
 }
 
-/* The rare exact paths (rescans of an attempt or of a particle) are inline code that receives the
- * device pointers it needs one by one (COLD_PARAMS / COLD_ARGS) and returns its counts; the only
- * out-of-line call of the hot kernels is exact_pair, whose arguments are scalars and pointers. */
-#define COLD_PARAMS const float4 *__restrict__ c_spos, const float4 *__restrict__ c_sori, const int *__restrict__ c_cs, const double *c_rec, const ppi_rparams *c_rp, \
-		const ppi_grid *c_grid, ppi_rstate *c_rs
-#define COLD_ARGS(d) (d).spos, (d).sori, (d).cell_start, (d).rec, (d).rp, (d).grid, (d).rs
 
 /* Colour pass design. A warp takes TA = 64 list entries at a time; lane l owns attempts l and l + 32
  * for the per-attempt work (draws, proposal, decision, commit). The neighbour pairs of the 64 attempts
  * are flattened, one neighbour plane (dz) at a time, into a shared pair list (a warp scan of the lanes'
- * plane lengths gives each attempt its slice), and the lanes then walk that list 32 pairs per step:
- * every lane executes the same instructions on its own pair, so the warp does not serialise the
- * attempts' differently sized neighbourhoods, and each step has 32 independent candidate loads in
- * flight. Pairs within the bonding range are compacted (ballot) into a second list whose steps run the
- * patch tests. Guard-band pairs go to a third list resolved after the planes by the out-of-line FP64
- * test, so no call site sits in the hot loops. The per-attempt state kept in shared memory is small
- * (~120 B), so that a colour of a million-particle system fits into one wave of resident warps. */
+ * plane lengths gives each attempt its slice), and the lanes then walk that list 32 pairs per step,
+ * PSTEP steps' candidate loads in flight together: every lane executes the same instructions on its own
+ * pair, so the warp does not serialise the attempts' differently sized neighbourhoods. Pairs within the
+ * bonding range are compacted (ballot) into a second list whose steps run the patch tests.
+ * An attempt with a pair inside the guard band (or whose pairs do not fit the list) is not decided in
+ * the loop: it is deferred to the end of the warp's share of the colour, where it is re-run on its own
+ * with the FP64 fallback (attempt_exact). Same-colour attempts never see each other, so the order does
+ * not matter; keeping the out-of-line FP64 code out of the loop keeps the loop free of spills. */
 #define TA 64          /* attempts per warp and iteration (2 per lane) */
 #define TILE_PCAP 768  /* pair list capacity per neighbour plane */
 #define TILE_CCAP 128  /* close-pair list capacity (flushed before it can overflow) */
-#define TILE_UCAP 32   /* guard-band list capacity (overflow -> the attempt is rescanned exactly) */
+#define TILE_DCAP 16   /* deferred attempts a warp keeps in shared memory (more: flags in global memory) */
+#define TILE_UCAP 32   /* guard-band pairs per iteration resolved in place (more: the attempt is deferred) */
+#define PSTEP 4        /* pair steps whose candidate loads are issued together */
 #define TILE_OFF_MAX (1 << 21) /* |candidate - mover| sorted-position distance that a packed entry holds */
 #define TF_OVER 1      /* the candidate state overlaps: rejected */
-#define TF_RESCAN 2    /* evaluate the whole neighbourhood again with the exact fallback inline */
+#define TF_DEFER 2     /* decided at the end, exactly (guard-band pair, or pairs beyond the list) */
 #define TF_CLOSED 4    /* no attempt (empty slot or move out of the cell) */
 
 struct __align__(16) TileSmem {
@@ -671,9 +787,165 @@ struct __align__(16) TileSmem {
 	int flag[TA], bo[TA], bn[TA];
 	int pbuf[TILE_PCAP]; /* (candidate - mover) << 10 | attempt << 4 | row */
 	int cbuf[TILE_CCAP]; /* same packing, pairs within the bonding range */
-	int2 uns[TILE_UCAP]; /* (sorted position, attempt << 1 | kind) */
-	int nc, nu;
+	int dl[TILE_DCAP];   /* list indices of deferred attempts */
+	int2 uns[TILE_UCAP]; /* guard-band pairs of this iteration: (sorted position, attempt << 1 | kind) */
+	int nc, nd, dov, nu;
 };
+
+/* the proposal of one attempt: particle, displacement, rotation (MC_move_rototranslate, MC.c:311-340) */
+struct Proposal {
+	int i, r, local, pslot, inside;
+	float4 po, q;
+	float3 disp;
+	float cpo[9];
+};
+
+__device__ __forceinline__ void propose(const ppi_dev &d, const int4 ent, long long round, Proposal &P) {
+	const int gc = ent.x, c0 = ent.y, cnt = ent.z;
+	P.r = ent.w;
+	const ppi_rparams &rp = d.rp[P.r];
+	const ppi_grid &g = d.grid[P.r];
+	P.local = gc - rp.cell_base;
+	/* the attempt's Philox draws: particle + displacement, rotation (acceptance only when needed) */
+	const U4 r1 = rng(rp, round, P.r, TAG_MOVE, (uint32_t) P.local, 0u), r2 = rng(rp, round, P.r, TAG_MOVE, (uint32_t) P.local, 1u);
+	P.i = c0 + (int) __umulhi(r1.x, (uint32_t) cnt);
+	P.po = d.spos[P.i];
+	const float dm = rp.disp_max_f;
+	P.disp = make_float3((u01(r1.y) - 0.5f) * dm, (u01(r1.z) - 0.5f) * dm, (u01(r1.w) - 0.5f) * dm);
+	const float nx = P.po.x + P.disp.x, ny = P.po.y + P.disp.y, nz = P.po.z + P.disp.z;
+	/* a move that leaves the cell is rejected: cells stay valid and same-colour cells stay independent */
+	P.inside = nx >= 0.f && nx < g.wf[0] && ny >= 0.f && ny < g.wf[1] && nz >= 0.f && nz < g.wf[2];
+	P.pslot = 0;
+	P.q = make_float4(1.f, 0.f, 0.f, 0.f);
+	if(P.inside) {
+		const float4 ob = d.sori[3 * (size_t) P.i], oc = d.sori[3 * (size_t) P.i + 1], od = d.sori[3 * (size_t) P.i + 2];
+		P.pslot = __float_as_int(od.w);
+		/* rotation: angle uniform in [0, Theta_max), axis uniform on the sphere (inversion method) */
+		const float theta = u01(r2.x) * rp.theta_max_f;
+		const float zc = 1.f - 2.f * u01(r2.y);
+		const float phi = 6.283185307179586f * u01(r2.z);
+		const float sr = sqrtf(fmaxf(0.f, 1.f - zc * zc));
+		float sp, cph, sh, ch;
+		__sincosf(phi, &sp, &cph);
+		__sincosf(0.5f * theta, &sh, &ch);
+		P.q = make_float4(ch, sh * sr * cph, sh * sr * sp, sh * zc);
+		P.cpo[0] = ob.x;
+		P.cpo[1] = ob.y;
+		P.cpo[2] = ob.z;
+		P.cpo[3] = ob.w;
+		P.cpo[4] = oc.x;
+		P.cpo[5] = oc.y;
+		P.cpo[6] = oc.z;
+		P.cpo[7] = oc.w;
+		P.cpo[8] = od.x;
+	}
+}
+
+/* FP32 rotation matrix of a unit quaternion (w, x, y, z), rows */
+__device__ __forceinline__ void quatmat32(float4 q, float *Q) {
+	const float w = q.x, x = q.y, y = q.z, z = q.w;
+	Q[0] = 1.f - 2.f * (y * y + z * z);
+	Q[1] = 2.f * (x * y - w * z);
+	Q[2] = 2.f * (x * z + w * y);
+	Q[3] = 2.f * (x * y + w * z);
+	Q[4] = 1.f - 2.f * (x * x + z * z);
+	Q[5] = 2.f * (y * z - w * x);
+	Q[6] = 2.f * (x * z - w * y);
+	Q[7] = 2.f * (y * z + w * x);
+	Q[8] = 1.f - 2.f * (x * x + y * y);
+}
+
+/* candidate orientation columns cpn = R . Q of the old columns cpo */
+__device__ __forceinline__ void cols_new(const float *cpo, float4 q, float *cpn) {
+	float Q[9];
+	quatmat32(q, Q);
+#pragma unroll
+	for(int jj = 0; jj < 3; jj++)
+#pragma unroll
+		for(int k3 = 0; k3 < 3; k3++) cpn[3 * jj + k3] = fmaf(cpo[k3], Q[jj], fmaf(cpo[3 + k3], Q[3 + jj], cpo[6 + k3] * Q[6 + jj]));
+}
+
+/* accepted move: FP64 q' = q (x) dq and r' = r + disp (state64 defines the same bits), FP32 record */
+__device__ __forceinline__ void commit_move(const ppi_dev &d, int i, int pslot, float4 po, float3 disp, float4 q, const float *cpn) {
+	double *rec = d.rec + (size_t) pslot * PPI_REC;
+	const double2 r01 = *(const double2 *) rec, r23 = *(const double2 *) (rec + 2), r45 = *(const double2 *) (rec + 4);
+	const double r6 = rec[6];
+	const double qv[4] = { r23.y, r45.x, r45.y, r6 };
+	const double b[4] = { f2d(q.x), f2d(q.y), f2d(q.z), f2d(q.w) };
+	double qn[4];
+#pragma unroll
+	for(int c = 0; c < 4; c++) qn[c] = qcomp64(qv[c], qv[c ^ 1], qv[c ^ 2], qv[c ^ 3], b, c);
+	*(double2 *) rec = make_double2(__dadd_rn(r01.x, f2d(disp.x)), __dadd_rn(r01.y, f2d(disp.y)));
+	*(double2 *) (rec + 2) = make_double2(__dadd_rn(r23.x, f2d(disp.z)), qn[0]);
+	*(double2 *) (rec + 4) = make_double2(qn[1], qn[2]);
+	rec[6] = qn[3];
+	d.spos[i] = make_float4(po.x + disp.x, po.y + disp.y, po.z + disp.z, po.w);
+	d.sori[3 * (size_t) i] = make_float4(cpn[0], cpn[1], cpn[2], cpn[3]);
+	d.sori[3 * (size_t) i + 1] = make_float4(cpn[4], cpn[5], cpn[6], cpn[7]);
+	((float *) (d.sori + 3 * (size_t) i + 2))[0] = cpn[8];
+}
+
+/* Metropolis on dE = -(bn - bo) (MC.c:330-339) */
+__device__ __forceinline__ bool metropolis(const ppi_rparams &rp, long long round, int r, int local, int bo, int bn) {
+	const int dE = bo - bn; /* E = -bonds */
+	if(dE <= 0) return true;
+	const U4 u3 = rng(rp, round, r, TAG_MOVE, (uint32_t) local, 2u);
+	const uint64_t U = ((uint64_t) u3.x << 21) | (u3.y >> 11);
+	return U < rp.acc_thr[dE < 31 ? dE : 31];
+}
+
+/* one whole attempt on its own, every guard-band pair decided exactly on the spot (the deferred
+ * attempts; the proposal is drawn again from the same counters, so it is the same proposal) */
+template <int MODE>
+__device__ __forceinline__ void attempt_exact(const ppi_dev &d, const int4 ent, long long round, Acc &A) {
+	Proposal P;
+	propose(d, ent, round, P);
+	if(!P.inside) return;
+	const ppi_rparams &rp = d.rp[P.r];
+	const ppi_grid &g = d.grid[P.r];
+	ppi_rstate *rs = d.rs + P.r;
+	const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+	const int cx = P.local % nx, cy = (P.local / nx) % ny, cz = P.local / (nx * ny);
+	const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
+	const float rc2e = rp.sqr_rcut_f + eps, ovl = 1.f - eps;
+	float cpn[9];
+	cols_new(P.cpo, P.q, cpn);
+	const float4 pn = make_float4(P.po.x + P.disp.x, P.po.y + P.disp.y, P.po.z + P.disp.z, 0.f);
+	int bo = 0, bn = 0;
+	for(int t = 0; t < 27; t++) {
+		const int dx = t % 3 - 1, dy = (t / 3) % 3 - 1, dz = t / 9 - 1;
+		const int cell = rp.cell_base + (wrapi(cz + dz, nz) * ny + wrapi(cy + dy, ny)) * nx + wrapi(cx + dx, nx);
+		const float ox = dx * g.wf[0], oy = dy * g.wf[1], oz = dz * g.wf[2];
+		for(int jq = d.cell_start[cell]; jq < d.cell_start[cell + 1]; jq++) {
+			if(jq == P.i) continue;
+			const float4 qa = d.spos[jq];
+			const float dxo = (qa.x - P.po.x) + ox, dyo = (qa.y - P.po.y) + oy, dzo = (qa.z - P.po.z) + oz;
+			const float dxn = (qa.x - pn.x) + ox, dyn = (qa.y - pn.y) + oy, dzn = (qa.z - pn.z) + oz;
+			const float r2o = fmaf(dxo, dxo, fmaf(dyo, dyo, dzo * dzo)), r2n = fmaf(dxn, dxn, fmaf(dyn, dyn, dzn * dzn));
+			A.pairs += 2;
+			if(MODE != MODE_AUDIT && r2n < ovl) return;
+			if(!(MODE == MODE_AUDIT || r2o < rc2e || r2n < rc2e)) continue;
+			const float4 qb = d.sori[3 * (size_t) jq], qc = d.sori[3 * (size_t) jq + 1], qd = d.sori[3 * (size_t) jq + 2];
+			const float cq[9] = { qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w, qd.x };
+			const int qslot = __float_as_int(qd.w);
+			const int clo = pair_state<MODE>(d.rec, rp, rs, g.inv_L, P.pslot, 0, P.q, P.disp, qslot, dxo, dyo, dzo, P.cpo, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0.,
+					A.fallbacks);
+			const int cln = pair_state<MODE>(d.rec, rp, rs, g.inv_L, P.pslot, 1, P.q, P.disp, qslot, dxn, dyn, dzn, cpn, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0.,
+					A.fallbacks);
+			if(cln == CL_OVER) return;
+			bo += (clo == CL_BOND);
+			bn += (cln == CL_BOND);
+		}
+	}
+	if(!metropolis(rp, round, P.r, P.local, bo, bn)) return;
+	if(P.r != A.r) {
+		flush_thread(d, A);
+		A.r = P.r;
+	}
+	A.acc++;
+	A.dbonds += bn - bo;
+	commit_move(d, P.i, P.pslot, P.po, P.disp, P.q, cpn);
+}
 
 /* pair geometry: d = q - p in p's cell frame for the old (o) and candidate (n) state of attempt a */
 struct PairGeo {
@@ -696,30 +968,11 @@ __device__ __forceinline__ PairGeo pair_geo(const TileSmem &S, int a, int t, flo
 	return G;
 }
 
-/* FP32 rotation matrix of a unit quaternion (w, x, y, z), rows */
-__device__ __forceinline__ void quatmat32(float4 q, float *Q) {
-	const float w = q.x, x = q.y, y = q.z, z = q.w;
-	Q[0] = 1.f - 2.f * (y * y + z * z);
-	Q[1] = 2.f * (x * y - w * z);
-	Q[2] = 2.f * (x * z + w * y);
-	Q[3] = 2.f * (x * y + w * z);
-	Q[4] = 1.f - 2.f * (x * x + z * z);
-	Q[5] = 2.f * (y * z - w * x);
-	Q[6] = 2.f * (x * z - w * y);
-	Q[7] = 2.f * (y * z + w * x);
-	Q[8] = 1.f - 2.f * (x * x + y * y);
-}
-
-/* old (cpo) and candidate (cpn = R . Q) orientation columns of attempt a */
+/* old (cpo) and candidate (cpn) orientation columns of attempt a */
 __device__ __forceinline__ void mover_cols(const TileSmem &S, int a, float *cpo, float *cpn) {
 #pragma unroll
 	for(int k = 0; k < 9; k++) cpo[k] = S.cpo[k][a];
-	float Q[9];
-	quatmat32(S.qr[a], Q);
-#pragma unroll
-	for(int jj = 0; jj < 3; jj++)
-#pragma unroll
-		for(int k3 = 0; k3 < 3; k3++) cpn[3 * jj + k3] = fmaf(cpo[k3], Q[jj], fmaf(cpo[3 + k3], Q[3 + jj], cpo[6 + k3] * Q[6 + jj]));
+	cols_new(cpo, S.qr[a], cpn);
 }
 
 /* patch tests of the listed close pairs, 32 per step */
@@ -729,7 +982,7 @@ __device__ __forceinline__ void tile_close(const ppi_dev &d, TileSmem &S, int la
 	for(int c = lane; c < nc; c += 32) {
 		const int en = S.cbuf[c];
 		const int a = (en >> 4) & 63, t = en & 15;
-		if(S.flag[a] & (TF_OVER | TF_RESCAN)) continue;
+		if(S.flag[a] & (TF_OVER | TF_DEFER)) continue;
 		const int jq = S.mi[a] + (en >> 10);
 		const ppi_rparams &rp = d.rp[S.rep[a]];
 		const float4 qa = d.spos[jq], qb = d.sori[3 * (size_t) jq], qc = d.sori[3 * (size_t) jq + 1], qd = d.sori[3 * (size_t) jq + 2];
@@ -739,26 +992,28 @@ __device__ __forceinline__ void tile_close(const ppi_dev &d, TileSmem &S, int la
 		float cpo[9], cpn[9];
 		mover_cols(S, a, cpo, cpn);
 		int clo, cln;
-		if(MODE == MODE_AUDIT) {
+		if(MODE == MODE_AUDIT) { /* test mode: every pair also through the FP64 comparison */
 			ppi_rstate *rs = d.rs + S.rep[a];
 			const float4 md = S.md[a];
 			const int pslot = __float_as_int(md.w), qslot = __float_as_int(qd.w);
 			const float3 disp = make_float3(md.x, md.y, md.z);
-			clo = pair_state<MODE>(d.rec, rp, rs, pslot, 0, S.qr[a], disp, qslot, G.dxo, G.dyo, G.dzo, cpo, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0., A.fallbacks);
-			cln = pair_state<MODE>(d.rec, rp, rs, pslot, 1, S.qr[a], disp, qslot, G.dxn, G.dyn, G.dzn, cpn, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0., A.fallbacks);
+			clo = pair_state<MODE>(d.rec, rp, rs, d.grid[S.rep[a]].inv_L, pslot, 0, S.qr[a], disp, qslot, G.dxo, G.dyo, G.dzo, cpo, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0., A.fallbacks);
+			cln = pair_state<MODE>(d.rec, rp, rs, d.grid[S.rep[a]].inv_L, pslot, 1, S.qr[a], disp, qslot, G.dxn, G.dyn, G.dzn, cpn, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0., A.fallbacks);
 		}
 		else {
 			clo = classify(G.dxo, G.dyo, G.dzo, cpo, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, nullptr);
 			cln = classify(G.dxn, G.dyn, G.dzn, cpn, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, nullptr);
+			/* guard band: recorded, decided after the planes by the certified FP64 test */
 			const int nu = (clo == CL_UNSURE) + (cln == CL_UNSURE);
 			if(nu) {
 				const int k = atomicAdd(&S.nu, nu);
-				if(k + nu > TILE_UCAP) atomicOr(&S.flag[a], TF_RESCAN);
-				else {
-					int kk = k;
-					if(clo == CL_UNSURE) S.uns[kk++] = make_int2(jq, a << 1);
-					if(cln == CL_UNSURE) S.uns[kk] = make_int2(jq, (a << 1) | 1);
+				if(k + nu > TILE_UCAP) {
+					atomicOr(&S.flag[a], TF_DEFER);
+					continue;
 				}
+				int kk = k;
+				if(clo == CL_UNSURE) S.uns[kk++] = make_int2(jq, a << 1);
+				if(cln == CL_UNSURE) S.uns[kk] = make_int2(jq, (a << 1) | 1);
 			}
 		}
 		if(clo == CL_BOND) atomicAdd(&S.bo[a], 1);
@@ -770,148 +1025,42 @@ __device__ __forceinline__ void tile_close(const ppi_dev &d, TileSmem &S, int la
 	__syncwarp();
 }
 
-/* cold path: attempt a's neighbourhood again, every guard-band pair decided exactly on the spot;
- * returns the number of exact re-evaluations */
-__device__ __forceinline__ unsigned tile_rescan(COLD_PARAMS, TileSmem &S, int a) {
-	const float4 md = S.md[a];
-	const int mslot = __float_as_int(md.w);
-	const int i = S.mi[a];
-	const int r = S.rep[a];
-	const ppi_rparams &rp = c_rp[r];
-	const ppi_grid &g = c_grid[r];
-	ppi_rstate *rs = c_rs + r;
-	const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
-	const int ccp = S.cc[a];
-	const int cx = ccp & 1023, cy = (ccp >> 10) & 1023, cz = ccp >> 20;
-	const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
-	const float rc2e = rp.sqr_rcut_f + eps;
-	const float4 mq = S.qr[a];
-	const float3 disp = make_float3(md.x, md.y, md.z);
-	float cpo[9], cpn[9];
-	mover_cols(S, a, cpo, cpn);
-	int bo = 0, bn = 0, over = 0;
-	unsigned fallbacks = 0;
-	for(int t = 0; t < 9 && !over; t++) {
-		const int row = rp.cell_base + (wrapi(cz + t / 3 - 1, nz) * ny + wrapi(cy + t % 3 - 1, ny)) * nx;
-		for(int c = 0; c < 3 && !over; c++) {
-			const int cell = row + wrapi(cx + c - 1, nx);
-			for(int jq = c_cs[cell]; jq < c_cs[cell + 1]; jq++) {
-				if(jq == i) continue;
-				const float4 qa = c_spos[jq];
-				const PairGeo G = pair_geo(S, a, t, qa);
-				const float r2o = fmaf(G.dxo, G.dxo, fmaf(G.dyo, G.dyo, G.dzo * G.dzo)), r2n = fmaf(G.dxn, G.dxn, fmaf(G.dyn, G.dyn, G.dzn * G.dzn));
-				if(!(r2o < rc2e || r2n < rc2e)) continue;
-				const float4 qb = c_sori[3 * (size_t) jq], qc = c_sori[3 * (size_t) jq + 1], qd = c_sori[3 * (size_t) jq + 2];
-				const float cq[9] = { qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w, qd.x };
-				const int qslot = __float_as_int(qd.w);
-				const int clo = pair_state<MODE_FAST>(c_rec, rp, rs, mslot, 0, mq, disp, qslot, G.dxo, G.dyo, G.dzo, cpo, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0.,
-						fallbacks);
-				const int cln = pair_state<MODE_FAST>(c_rec, rp, rs, mslot, 1, mq, disp, qslot, G.dxn, G.dyn, G.dzn, cpn, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0.,
-						fallbacks);
-				bo += (clo == CL_BOND);
-				bn += (cln == CL_BOND);
-				if(cln == CL_OVER) {
-					over = 1;
-					break;
-				}
-			}
-		}
-	}
-	S.bo[a] = bo;
-	S.bn[a] = bn;
-	S.flag[a] = over ? TF_OVER : 0;
-	return fallbacks;
-}
-
-/* the rare exact work of a tile iteration: guard-band pairs of the list, then attempts to rescan */
-__device__ __forceinline__ unsigned tile_exact(COLD_PARAMS, TileSmem &S, int lane) {
-	unsigned fallbacks = 0;
-	const int nu = S.nu < TILE_UCAP ? S.nu : TILE_UCAP;
-	for(int u = lane; u < nu; u += 32) {
-		const int2 v = S.uns[u];
-		const int jq = v.x, a = v.y >> 1, kind = v.y & 1;
-		if(S.flag[a] & (TF_OVER | TF_RESCAN)) continue;
-		const float4 md = S.md[a];
-		const int rr = S.rep[a];
-		fallbacks++;
-		const int ex = exact_pair(c_rec, c_rp + rr, c_rs[rr].box, __float_as_int(md.w), kind, S.qr[a], make_float3(md.x, md.y, md.z),
-				__float_as_int(c_sori[3 * (size_t) jq + 2].w), -1, 1., 0., nullptr, nullptr, nullptr);
-		if(ex == 1) atomicAdd(kind ? &S.bn[a] : &S.bo[a], 1);
-		else if(ex == -1 && kind) atomicOr(&S.flag[a], TF_OVER);
-	}
-	__syncwarp();
-	for(int k = 0; k < 2; k++) {
-		const int a = lane + 32 * k;
-		if(S.flag[a] & TF_RESCAN) fallbacks += tile_rescan(c_spos, c_sori, c_cs, c_rec, c_rp, c_grid, c_rs, S, a);
-	}
-	__syncwarp();
-	return fallbacks;
-}
-
-/* proposal of attempt a = (list entry ent): mover, displacement, rotation; returns the attempt's local
- * cell index (its draws' counter) */
+/* proposal of attempt a = (list entry ent) into the tile's shared state */
 __device__ __forceinline__ int tile_setup(const ppi_dev &d, TileSmem &S, int a, const int4 ent, long long round, Acc &A) {
-	int flag = TF_CLOSED, i = 0, r = 0, local = 0, pslot = 0;
-	float4 po = make_float4(0.f, 0.f, 0.f, 0.f), q = make_float4(1.f, 0.f, 0.f, 0.f), wv = make_float4(1.f, 1.f, 1.f, __int_as_float(4));
-	float3 disp = make_float3(0.f, 0.f, 0.f);
+	int flag = TF_CLOSED;
+	Proposal P;
+	P.i = P.r = P.local = P.pslot = 0;
+	P.po = make_float4(0.f, 0.f, 0.f, 0.f);
+	P.q = make_float4(1.f, 0.f, 0.f, 0.f);
+	P.disp = make_float3(0.f, 0.f, 0.f);
+	float4 wv = make_float4(1.f, 1.f, 1.f, __int_as_float(4));
 	if(ent.x >= 0) {
-		const int gc = ent.x, c0 = ent.y, cnt = ent.z;
-		r = ent.w;
-		if(r != A.r) {
+		if(ent.w != A.r) {
 			flush_thread(d, A);
-			A.r = r;
-		}
-		const ppi_rparams &rp = d.rp[r];
-		const ppi_grid &g = d.grid[r];
-		local = gc - rp.cell_base;
-		{
-			const int cx = local % g.n[0], cy = (local / g.n[0]) % g.n[1], cz = local / (g.n[0] * g.n[1]);
-			S.cc[a] = cx | (cy << 10) | (cz << 20);
+			A.r = ent.w;
 		}
 		A.tries++;
-		/* the attempt's Philox draws: particle + displacement, rotation (acceptance only when needed) */
-		const U4 r1 = rng(rp, round, r, TAG_MOVE, (uint32_t) local, 0u), r2 = rng(rp, round, r, TAG_MOVE, (uint32_t) local, 1u);
-		i = c0 + (int) __umulhi(r1.x, (uint32_t) cnt);
-		po = d.spos[i];
-		const float dm = rp.disp_max_f;
-		disp = make_float3((u01(r1.y) - 0.5f) * dm, (u01(r1.z) - 0.5f) * dm, (u01(r1.w) - 0.5f) * dm);
+		propose(d, ent, round, P);
+		const ppi_grid &g = d.grid[P.r];
 		wv = make_float4(g.wf[0], g.wf[1], g.wf[2], __int_as_float(g.n[0]));
-		const float nx = po.x + disp.x, ny = po.y + disp.y, nz = po.z + disp.z;
-		/* a move that leaves the cell is rejected: cells stay valid and same-colour cells stay independent */
-		if(nx >= 0.f && nx < wv.x && ny >= 0.f && ny < wv.y && nz >= 0.f && nz < wv.z) {
+		const int cx = P.local % g.n[0], cy = (P.local / g.n[0]) % g.n[1], cz = P.local / (g.n[0] * g.n[1]);
+		S.cc[a] = cx | (cy << 10) | (cz << 20);
+		if(P.inside) {
 			flag = 0;
-			const float4 ob = d.sori[3 * (size_t) i], oc = d.sori[3 * (size_t) i + 1], od = d.sori[3 * (size_t) i + 2];
-			pslot = __float_as_int(od.w);
-			/* rotation: angle uniform in [0, Theta_max), axis uniform on the sphere (inversion method) */
-			const float theta = u01(r2.x) * rp.theta_max_f;
-			const float zc = 1.f - 2.f * u01(r2.y);
-			const float phi = 6.283185307179586f * u01(r2.z);
-			const float sr = sqrtf(fmaxf(0.f, 1.f - zc * zc));
-			float sp, cph, sh, ch;
-			__sincosf(phi, &sp, &cph);
-			__sincosf(0.5f * theta, &sh, &ch);
-			q = make_float4(ch, sh * sr * cph, sh * sr * sp, sh * zc);
-			S.cpo[0][a] = ob.x;
-			S.cpo[1][a] = ob.y;
-			S.cpo[2][a] = ob.z;
-			S.cpo[3][a] = ob.w;
-			S.cpo[4][a] = oc.x;
-			S.cpo[5][a] = oc.y;
-			S.cpo[6][a] = oc.z;
-			S.cpo[7][a] = oc.w;
-			S.cpo[8][a] = od.x;
+#pragma unroll
+			for(int k = 0; k < 9; k++) S.cpo[k][a] = P.cpo[k];
 		}
 	}
-	S.pos[a] = po;
-	S.md[a] = make_float4(disp.x, disp.y, disp.z, __int_as_float(pslot));
+	S.pos[a] = P.po;
+	S.md[a] = make_float4(P.disp.x, P.disp.y, P.disp.z, __int_as_float(P.pslot));
 	S.wv[a] = wv;
-	S.qr[a] = q;
-	S.mi[a] = i;
-	S.rep[a] = r;
+	S.qr[a] = P.q;
+	S.mi[a] = P.i;
+	S.rep[a] = P.r;
 	S.bo[a] = 0;
 	S.bn[a] = 0;
 	S.flag[a] = flag;
-	return local;
+	return P.local;
 }
 
 /* the three rows (dy = -1, 0, 1) of plane dz of attempt a's neighbourhood: each row is one or two
@@ -924,7 +1073,7 @@ __device__ __forceinline__ int plane_ranges(const ppi_dev &d, const TileSmem &S,
 	int n = 0;
 #pragma unroll
 	for(int k = 0; k < 6; k++) P.s[k] = P.e[k] = 0;
-	if(S.flag[a] & (TF_OVER | TF_CLOSED | TF_RESCAN)) return 0;
+	if(S.flag[a] & (TF_OVER | TF_CLOSED | TF_DEFER)) return 0;
 	const int r = S.rep[a];
 	const ppi_grid &g = d.grid[r];
 	const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
@@ -958,7 +1107,7 @@ __device__ __forceinline__ void write_pairs(TileSmem &S, int a, int pz, const Pl
 		for(int jq = P.s[sg]; jq < P.e[sg]; jq++) {
 			const int off = jq - i;
 			if(off >= TILE_OFF_MAX || off <= -TILE_OFF_MAX) {
-				atomicOr(&S.flag[a], TF_RESCAN);
+				atomicOr(&S.flag[a], TF_DEFER);
 				S.pbuf[pos++] = tag; /* offset 0 = the mover itself: skipped */
 			}
 			else S.pbuf[pos++] = (int) ((unsigned) off << 10) | tag;
@@ -966,9 +1115,19 @@ __device__ __forceinline__ void write_pairs(TileSmem &S, int a, int pz, const Pl
 	}
 }
 
-/* the TA attempts of list entries e0 (lane's first) and e1 (lane's second); ent.x < 0: none */
+/* remembers deferred attempt list index e */
+__device__ __forceinline__ void defer_attempt(const ppi_dev &d, TileSmem &S, int col, int e) {
+	const int k = atomicAdd(&S.nd, 1);
+	if(k < TILE_DCAP) S.dl[k] = e;
+	else {
+		d.dflag[(size_t) col * d.clist_cap + e] = 1;
+		S.dov = 1;
+	}
+}
+
+/* the TA attempts of list positions b + lane (e0) and b + 32 + lane (e1); ent.x < 0: none */
 template <int MODE>
-__device__ __forceinline__ void tile_round(const ppi_dev &d, TileSmem &S, const int lane, const int4 e0, const int4 e1, long long round, Acc &A) {
+__device__ __forceinline__ void tile_round(const ppi_dev &d, TileSmem &S, const int lane, const int4 e0, const int4 e1, int b, int col, long long round, Acc &A) {
 	const int loc0 = tile_setup(d, S, lane, e0, round, A);
 	const int loc1 = tile_setup(d, S, lane + 32, e1, round, A);
 	if(lane == 0) {
@@ -990,12 +1149,12 @@ __device__ __forceinline__ void tile_round(const ppi_dev &d, TileSmem &S, const 
 			if(lane >= o) incl += v;
 		}
 		if(__shfl_sync(0xffffffffu, incl, 31) == 0) continue;
-		/* the lanes whose slices fit into the list; the others are rescanned exactly (dense corner case) */
+		/* the lanes whose slices fit into the list; the others' attempts are deferred (dense corner case) */
 		const unsigned fit = __ballot_sync(0xffffffffu, incl <= TILE_PCAP);
 		const int np = fit ? __shfl_sync(0xffffffffu, incl, 31 - __clz(fit)) : 0;
 		if(incl > TILE_PCAP) {
-			if(n0) atomicOr(&S.flag[lane], TF_RESCAN);
-			if(n1) atomicOr(&S.flag[lane + 32], TF_RESCAN);
+			if(n0) atomicOr(&S.flag[lane], TF_DEFER);
+			if(n1) atomicOr(&S.flag[lane + 32], TF_DEFER);
 		}
 		else {
 			const int pos = incl - n;
@@ -1003,16 +1162,30 @@ __device__ __forceinline__ void tile_round(const ppi_dev &d, TileSmem &S, const 
 			write_pairs(S, lane + 32, pz, P1, pos + n0);
 		}
 		__syncwarp();
-		for(int p0 = 0; p0 < np; p0 += 32) {
-			const int p = p0 + lane;
-			int close = 0, en = 0;
-			if(p < np) {
-				en = S.pbuf[p];
-				const int a = (en >> 4) & 63, off = en >> 10;
-				if(off != 0 && !(S.flag[a] & (TF_OVER | TF_RESCAN))) {
-					const int jq = S.mi[a] + off;
-					const float4 qa = d.spos[jq];
-					const PairGeo G = pair_geo(S, a, en & 15, qa);
+		/* PSTEP steps of 32 pairs at a time: the candidate loads of all of them are issued before any is
+		 * used, so that a step group costs one memory latency instead of PSTEP */
+		for(int p0 = 0; p0 < np; p0 += 32 * PSTEP) {
+			int en[PSTEP], ok[PSTEP];
+			float4 qa[PSTEP];
+#pragma unroll
+			for(int u = 0; u < PSTEP; u++) {
+				const int p = p0 + 32 * u + lane;
+				en[u] = 0;
+				ok[u] = 0;
+				qa[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+				if(p < np) {
+					en[u] = S.pbuf[p];
+					const int a = (en[u] >> 4) & 63, off = en[u] >> 10;
+					ok[u] = off != 0 && !(S.flag[a] & (TF_OVER | TF_DEFER));
+					if(ok[u]) qa[u] = d.spos[S.mi[a] + off];
+				}
+			}
+#pragma unroll
+			for(int u = 0; u < PSTEP; u++) {
+				int close = 0;
+				if(ok[u]) {
+					const int a = (en[u] >> 4) & 63;
+					const PairGeo G = pair_geo(S, a, en[u] & 15, qa[u]);
 					const float r2o = fmaf(G.dxo, G.dxo, fmaf(G.dyo, G.dyo, G.dzo * G.dzo));
 					const float r2n = fmaf(G.dxn, G.dxn, fmaf(G.dyn, G.dyn, G.dzn * G.dzn));
 					const ppi_rparams &rp = d.rp[S.rep[a]];
@@ -1021,65 +1194,60 @@ __device__ __forceinline__ void tile_round(const ppi_dev &d, TileSmem &S, const 
 					if(MODE != MODE_AUDIT && r2n < 1.f - eps) atomicOr(&S.flag[a], TF_OVER); /* certain overlap of the candidate state */
 					else close = MODE == MODE_AUDIT || r2o < rp.sqr_rcut_f + eps || r2n < rp.sqr_rcut_f + eps;
 				}
-			}
-			/* compact the close pairs into the patch-test list */
-			const unsigned m = __ballot_sync(0xffffffffu, close);
-			if(m) {
-				if(S.nc + __popc(m) > TILE_CCAP) tile_close<MODE>(d, S, lane, A);
-				if(close) S.cbuf[S.nc + __popc(m & lt)] = en;
-				__syncwarp();
-				if(lane == 0) S.nc += __popc(m);
-				__syncwarp();
+				/* compact the close pairs into the patch-test list */
+				const unsigned m = __ballot_sync(0xffffffffu, close);
+				if(m) {
+					if(S.nc + __popc(m) > TILE_CCAP) tile_close<MODE>(d, S, lane, A);
+					if(close) S.cbuf[S.nc + __popc(m & lt)] = en[u];
+					__syncwarp();
+					if(lane == 0) S.nc += __popc(m);
+					__syncwarp();
+				}
 			}
 		}
 	}
 	if(S.nc) tile_close<MODE>(d, S, lane, A);
-	/* guard-band pairs and rescans: exact decisions, out of line */
-	const int need = (S.nu > 0) | ((S.flag[lane] | S.flag[lane + 32]) & TF_RESCAN);
-	if(__any_sync(0xffffffffu, need)) A.fallbacks += tile_exact(COLD_ARGS(d), S, lane);
+	/* guard-band pairs: certified FP64 decisions (no division chain); an undecided one defers its attempt */
+	if(MODE == MODE_FAST) {
+		const int nu = S.nu < TILE_UCAP ? S.nu : TILE_UCAP;
+		for(int u = lane; u < nu; u += 32) {
+			const int2 v = S.uns[u];
+			const int jq = v.x, a = v.y >> 1, kind = v.y & 1;
+			if(S.flag[a] & (TF_OVER | TF_DEFER)) continue;
+			const int r = S.rep[a];
+			const float4 md = S.md[a];
+			A.fallbacks++;
+			const int ex = decide64(d.rec, d.rp[r], d.rs[r].box, d.grid[r].inv_L, __float_as_int(md.w), kind, S.qr[a], make_float3(md.x, md.y, md.z),
+					__float_as_int(d.sori[3 * (size_t) jq + 2].w), -1, 1., 0.);
+			if(ex == DEC64_EXACT) atomicOr(&S.flag[a], TF_DEFER);
+			else if(ex == 1) atomicAdd(kind ? &S.bn[a] : &S.bo[a], 1);
+			else if(ex == -1 && kind) atomicOr(&S.flag[a], TF_OVER);
+		}
+		__syncwarp();
+	}
+	/* decisions and commits of the attempts that are not deferred */
 #pragma unroll 1
 	for(int k = 0; k < 2; k++) {
 		const int a = lane + 32 * k;
 		const int flag = S.flag[a];
 		if(flag & (TF_OVER | TF_CLOSED)) continue;
-		/* Metropolis on dE = -(bn - bo) (MC.c:330-339) */
-		const int r = S.rep[a];
-		const ppi_rparams &rp = d.rp[r];
-		const int bo = S.bo[a], bn = S.bn[a];
-		const int dE = bo - bn;
-		if(dE > 0) {
-			const U4 u3 = rng(rp, round, r, TAG_MOVE, (uint32_t) (k ? loc1 : loc0), 2u);
-			const uint64_t U = ((uint64_t) u3.x << 21) | (u3.y >> 11);
-			if(!(U < rp.acc_thr[dE < 31 ? dE : 31])) continue;
+		if(flag & TF_DEFER) {
+			defer_attempt(d, S, col, b + a);
+			continue;
 		}
+		const int r = S.rep[a];
+		const int bo = S.bo[a], bn = S.bn[a];
+		if(!metropolis(d.rp[r], round, r, k ? loc1 : loc0, bo, bn)) continue;
 		if(r != A.r) {
 			flush_thread(d, A);
 			A.r = r;
 		}
 		A.acc++;
 		A.dbonds += bn - bo;
-		/* commit: FP64 q' = q (x) dq and r' = r + disp (state64 defines the same bits), FP32 record */
-		const float4 mq = S.qr[a], md = S.md[a];
-		const int i = S.mi[a];
-		double *rec = d.rec + (size_t) __float_as_int(md.w) * PPI_REC;
-		const double2 r01 = *(const double2 *) rec, r23 = *(const double2 *) (rec + 2), r45 = *(const double2 *) (rec + 4);
-		const double r6 = rec[6];
-		const double qv[4] = { r23.y, r45.x, r45.y, r6 };
-		const double b[4] = { f2d(mq.x), f2d(mq.y), f2d(mq.z), f2d(mq.w) };
-		double qn[4];
-#pragma unroll
-		for(int c = 0; c < 4; c++) qn[c] = qcomp64(qv[c], qv[c ^ 1], qv[c ^ 2], qv[c ^ 3], b, c);
-		*(double2 *) rec = make_double2(__dadd_rn(r01.x, f2d(md.x)), __dadd_rn(r01.y, f2d(md.y)));
-		*(double2 *) (rec + 2) = make_double2(__dadd_rn(r23.x, f2d(md.z)), qn[0]);
-		*(double2 *) (rec + 4) = make_double2(qn[1], qn[2]);
-		rec[6] = qn[3];
-		const float4 po = S.pos[a];
-		d.spos[i] = make_float4(po.x + md.x, po.y + md.y, po.z + md.z, po.w);
 		float cpo[9], cpn[9];
 		mover_cols(S, a, cpo, cpn);
-		d.sori[3 * (size_t) i] = make_float4(cpn[0], cpn[1], cpn[2], cpn[3]);
-		d.sori[3 * (size_t) i + 1] = make_float4(cpn[4], cpn[5], cpn[6], cpn[7]);
-		((float *) (d.sori + 3 * (size_t) i + 2))[0] = cpn[8];
+		const float4 md = S.md[a];
+		commit_move(d, S.mi[a], __float_as_int(md.w), S.pos[a], make_float3(md.x, md.y, md.z), S.qr[a], cpn);
 	}
 }
 
@@ -1101,12 +1269,29 @@ __global__ void __launch_bounds__(32 * TILE_WARPS, MODE == MODE_FAST ? PPI_TILE_
 	 * working CTAs of a partly filled grid evenly over the SMs) */
 	const int lo = (int) ((long long) warp * cnt / nwarp), hi = (int) ((long long) (warp + 1) * cnt / nwarp);
 	const int4 none = make_int4(-1, 0, 0, 0);
+	if(lane == 0) {
+		S.nd = 0;
+		S.dov = 0;
+	}
+	__syncwarp();
 	for(int b = lo; b < hi; b += TA) {
 		const int4 e0 = (b + lane < hi) ? list[b + lane] : none;
 		const int4 e1 = (b + 32 + lane < hi) ? list[b + 32 + lane] : none;
-		tile_round<MODE>(d, S, lane, e0, e1, round, A);
+		tile_round<MODE>(d, S, lane, e0, e1, b, col, round, A);
 		__syncwarp();
 	}
+	/* the deferred attempts, one per lane, exactly */
+	const int nd = S.nd < TILE_DCAP ? S.nd : TILE_DCAP;
+	for(int k = lane; k < nd; k += 32) attempt_exact<MODE>(d, list[S.dl[k]], round, A);
+	if(S.dov) {
+		unsigned char *fl = d.dflag + (size_t) col * d.clist_cap;
+		for(int e = lo + lane; e < hi; e += 32)
+			if(fl[e]) {
+				fl[e] = 0;
+				attempt_exact<MODE>(d, list[e], round, A);
+			}
+	}
+	__syncwarp();
 	flush_block(d, A);
 }
 
@@ -1125,33 +1310,6 @@ __device__ __forceinline__ int group_sum(unsigned gm, int v) {
 #pragma unroll
 	for(int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(gm, v, o);
 	return v;
-}
-
-/* Guard-band pairs met in the hot loops are not evaluated there: a call to the out-of-line FP64 test
- * inside the loop would make the compiler keep the loop's state in local memory around it. Each lane
- * records up to UNS_CAP of them in registers (a shift register, no indexed arrays) and resolves them
- * after its loop; a lane with more re-runs its share of the neighbourhood on a cold path. */
-#define UNS_CAP 4
-struct Unsure {
-	int n;
-	int v0, v1, v2, v3; /* (sorted position << 1) | kind */
-	__device__ __forceinline__ void push(int v) {
-		v3 = v2;
-		v2 = v1;
-		v1 = v0;
-		v0 = v;
-		n++;
-	}
-};
-
-/* exact decision of a recorded pair: p's state `kind` against the particle at sorted position jq */
-__device__ __forceinline__ int resolve_exact(const ppi_dev &d, const ppi_rparams &rp, ppi_rstate *rs, int pslot, int v, float4 q, float3 disp, int vol_dir,
-		double vol_f, double vol_side, Acc &A) {
-	const int jq = v >> 1, kind = v & 1;
-	const int qslot = __float_as_int(d.sori[3 * (size_t) jq + 2].w);
-	A.fallbacks++;
-	const int ex = exact_pair(d.rec, &rp, rs->box, pslot, kind, q, disp, qslot, vol_dir, vol_f, vol_side, nullptr, nullptr, nullptr);
-	return ex == -1 ? CL_OVER : (ex == 1 ? CL_BOND : CL_NONE);
 }
 
 /* ------------------------------------------------------------------------------------------------ */
@@ -1200,64 +1358,88 @@ __device__ __forceinline__ void energy_flush_block(const ppi_dev &d, Acc &A) {
 	}
 }
 
-/* what a lane needs to re-run its share of a particle's neighbourhood in the energy pass */
-struct EnergyCtx {
-	float pl[3], w[3], cp[9];
-	float sf;
-	int k, pslot, cx, cy, cz, nx, ny, nz, cell_base, sdir;
-	double vf, vside;
-	int *partners;
-};
-
-/* cold path of a lane that met more than UNS_CAP guard-band pairs in the energy pass: its rows again,
- * every guard-band pair decided exactly on the spot. Returns bonds | overlaps << 16 | exact
- * re-evaluations << 32. */
-template <int G>
-__device__ __forceinline__ unsigned long long energy_lane_exact(COLD_PARAMS, int r, const EnergyCtx &E, int sub) {
-	const ppi_rparams &rp = c_rp[r];
-	ppi_rstate *rs = c_rs + r;
+/* energy of particle k (sorted position) on its own, every guard-band pair decided exactly on the spot
+ * (the deferred particles of the energy pass) */
+__device__ __forceinline__ void energy_exact(const ppi_dev &d, int mode, int k, Acc &A) {
+	const float4 pa = d.spos[k], pb = d.sori[3 * (size_t) k], pc = d.sori[3 * (size_t) k + 1], pd = d.sori[3 * (size_t) k + 2];
+	const int gc = __float_as_int(pd.z);
+	const int r = d.cell_rep[gc];
+	if(r != A.r) {
+		energy_flush_thread(d, A);
+		A.r = r;
+	}
+	const ppi_rparams &rp = d.rp[r];
+	const ppi_grid &g = d.grid[r];
+	ppi_rstate *rs = d.rs + r;
+	int sdir = -1;
+	float sf = 1.f;
+	double vf = 1.0, vside = 0.0;
+	if(mode == PPI_EN_VOLUME) {
+		if(g.vol_dir < 0 || rs->vol_overlap) return;
+		sdir = g.vol_dir;
+		sf = g.vol_ff;
+		vf = g.vol_f;
+		vside = g.vol_side;
+	}
+	float w[3] = { g.wf[0], g.wf[1], g.wf[2] };
+	float pl[3] = { pa.x, pa.y, pa.z };
+	if(sdir >= 0) {
+		w[sdir] *= sf;
+		pl[sdir] *= sf;
+	}
+	const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+	const int local = gc - rp.cell_base;
+	const int cx = local % nx, cy = (local / nx) % ny, cz = local / (nx * ny);
 	const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
-	const float sqr_rcut = rp.sqr_rcut_f, cosmax = rp.cosmax_f, basef = rp.base_f, rc2e = sqr_rcut + eps;
-	const int *cs = c_cs;
-	unsigned fallbacks = 0;
+	const float rc2e = rp.sqr_rcut_f + eps;
+	const int pslot = __float_as_int(pd.w);
+	const float cp[9] = { pb.x, pb.y, pb.z, pb.w, pc.x, pc.y, pc.z, pc.w, pd.x };
+	int *partners = (mode == PPI_EN_PARTNERS) ? d.out_partners + (size_t) pslot * PPI_MAX_PARTNERS : nullptr;
 	const float4 q0 = make_float4(1.f, 0.f, 0.f, 0.f);
 	const float3 d0 = make_float3(0.f, 0.f, 0.f);
 	int nb = 0, no = 0;
-	for(int t = sub; t < 9; t += G) {
-		const int dy = t % 3 - 1, dz = t / 3 - 1;
-		const int row = E.cell_base + (wrapi(E.cz + dz, E.nz) * E.ny + wrapi(E.cy + dy, E.ny)) * E.nx;
-		for(int c = 0; c < 3; c++) {
-			const int cell = row + wrapi(E.cx + c - 1, E.nx);
-			const float ox = (c - 1) * E.w[0], oy = dy * E.w[1], oz = dz * E.w[2];
-			for(int jq = cs[cell]; jq < cs[cell + 1]; jq++) {
-				if(jq == E.k) continue;
-				const float4 qa = c_spos[jq];
-				float ql[3] = { qa.x, qa.y, qa.z };
-				if(E.sdir >= 0) ql[E.sdir] *= E.sf;
-				const float ddx = (ql[0] - E.pl[0]) + ox, ddy = (ql[1] - E.pl[1]) + oy, ddz = (ql[2] - E.pl[2]) + oz;
-				const float r2 = fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz));
-				if(r2 >= rc2e) continue;
-				const float4 qb = c_sori[3 * (size_t) jq], qc = c_sori[3 * (size_t) jq + 1], qd = c_sori[3 * (size_t) jq + 2];
-				const float cq[9] = { qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w, qd.x };
-				const int cl = pair_state<MODE_FAST>(c_rec, rp, rs, E.pslot, 0, q0, d0, __float_as_int(qd.w), ddx, ddy, ddz, E.cp, cq, sqr_rcut, cosmax, basef, eps, E.sdir,
-						E.vf, E.vside, fallbacks);
-				if(cl == CL_BOND) {
-					if(E.partners && nb < PPI_MAX_PARTNERS) E.partners[nb] = __float_as_int(qd.y);
-					nb++;
-				}
-				no += (cl == CL_OVER);
+	for(int t = 0; t < 27 && !(mode == PPI_EN_VOLUME && no); t++) {
+		const int dx = t % 3 - 1, dy = (t / 3) % 3 - 1, dz = t / 9 - 1;
+		const int cell = rp.cell_base + (wrapi(cz + dz, nz) * ny + wrapi(cy + dy, ny)) * nx + wrapi(cx + dx, nx);
+		const float ox = dx * w[0], oy = dy * w[1], oz = dz * w[2];
+		for(int jq = d.cell_start[cell]; jq < d.cell_start[cell + 1]; jq++) {
+			if(jq == k) continue;
+			const float4 qa = d.spos[jq];
+			float ql[3] = { qa.x, qa.y, qa.z };
+			if(sdir >= 0) ql[sdir] *= sf;
+			const float ddx = (ql[0] - pl[0]) + ox, ddy = (ql[1] - pl[1]) + oy, ddz = (ql[2] - pl[2]) + oz;
+			const float r2 = fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz));
+			A.pairs++;
+			if(r2 >= rc2e) continue;
+			const float4 qb = d.sori[3 * (size_t) jq], qc = d.sori[3 * (size_t) jq + 1], qd = d.sori[3 * (size_t) jq + 2];
+			const float cq[9] = { qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w, qd.x };
+			const int cl = pair_state<MODE_FAST>(d.rec, rp, rs, g.inv_L, pslot, 0, q0, d0, __float_as_int(qd.w), ddx, ddy, ddz, cp, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps,
+					sdir, vf, vside, A.fallbacks);
+			if(cl == CL_BOND) {
+				if(partners && nb < PPI_MAX_PARTNERS) partners[nb] = __float_as_int(qd.y);
+				nb++;
+			}
+			if(cl == CL_OVER) {
+				no++;
+				if(mode == PPI_EN_VOLUME) break;
 			}
 		}
 	}
-	return (unsigned long long) (nb & 0xffff) | ((unsigned long long) (no & 0xffff) << 16) | ((unsigned long long) fallbacks << 32);
+	if(mode != PPI_EN_VOLUME) {
+		d.out_bonds[pslot] = nb;
+		d.out_overlaps[pslot] = no;
+	}
+	if(no && !rs->vol_overlap) atomicExch(&rs->vol_overlap, 1);
+	if(!(mode == PPI_EN_VOLUME && no)) A.tries += nb;
 }
 
 /* energy of one particle from scratch, G lanes: bond and overlap counts over all partners (MC_energy,
  * MC.c:272-309, without the early exit, as output_print_bonds counts them, output.c:213-268), or its
  * share of the NPT candidate box's energy (MC.c:487-495). G = 1 in PPI_EN_PARTNERS mode, which also
- * lists the bonded partners. */
+ * lists the bonded partners. Returns 1 if a pair fell inside the guard band: the particle is then
+ * computed again on its own, exactly, at the end of the pass (energy_exact), and nothing is written. */
 template <int MODE, int G>
-__device__ __forceinline__ void energy_particle(const ppi_dev &d, int mode, int k, Acc &A, const int sub, const unsigned gm) {
+__device__ __forceinline__ int energy_particle(const ppi_dev &d, int mode, int k, Acc &A, const int sub, const unsigned gm) {
 	const float4 pa = d.spos[k];
 	const float4 pd = d.sori[3 * (size_t) k + 2];
 	const int gc = __float_as_int(pd.z);
@@ -1273,11 +1455,11 @@ __device__ __forceinline__ void energy_particle(const ppi_dev &d, int mode, int 
 	float sf = 1.f;
 	double vf = 1.0, vside = 0.0;
 	if(mode == PPI_EN_VOLUME) {
-		if(g.vol_dir < 0) return;
+		if(g.vol_dir < 0) return 0;
 		/* one overlap already rejects the candidate box: skip (one read per group, shared) */
 		int skip = sub == 0 ? *(volatile int *) &rs->vol_overlap : 0;
 		skip = __shfl_sync(gm, skip, 0, G);
-		if(skip) return;
+		if(skip) return 0;
 		sdir = g.vol_dir;
 		sf = g.vol_ff;
 		vf = g.vol_f;
@@ -1295,7 +1477,7 @@ __device__ __forceinline__ void energy_particle(const ppi_dev &d, int mode, int 
 	const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
 	const float sqr_rcut = rp.sqr_rcut_f, cosmax = rp.cosmax_f, basef = rp.base_f, rc2e = sqr_rcut + eps, ovl = 1.f - eps;
 	const int pslot = __float_as_int(pd.w);
-	int nb = 0, no = 0;
+	int nb = 0, no = 0, uns = 0, u0 = 0, u1 = 0; /* guard-band pairs: count, first two candidates */
 	int *partners = (mode == PPI_EN_PARTNERS) ? d.out_partners + (size_t) pslot * PPI_MAX_PARTNERS : nullptr;
 	const int *cs = d.cell_start;
 	float cp[9];
@@ -1315,15 +1497,13 @@ __device__ __forceinline__ void energy_particle(const ppi_dev &d, int mode, int 
 	const float3 d0 = make_float3(0.f, 0.f, 0.f);
 	const int xm = wrapi(cx - 1, nx), xp = wrapi(cx + 1, nx);
 	const int stop_on_overlap = (mode == PPI_EN_VOLUME);
-	Unsure U;
-	U.n = U.v0 = U.v1 = U.v2 = U.v3 = 0;
-	for(int t = sub; t < 9 && !(stop_on_overlap && no); t += G) {
+	for(int t = sub; t < 9 && !(stop_on_overlap && no) && uns <= 2; t += G) {
 		const int dy = t % 3 - 1, dz = t / 3 - 1;
 		const int row = rp.cell_base + (wrapi(cz + dz, nz) * ny + wrapi(cy + dy, ny)) * nx;
 		const int a0 = cs[row + xm], a1 = cs[row + xm + 1], m0 = cs[row + cx], m1 = cs[row + cx + 1], p0 = cs[row + xp], p1 = cs[row + xp + 1];
 		const float oy = dy * w[1], oz = dz * w[2];
 #pragma unroll 1
-		for(int c = 0; c < 3 && !(stop_on_overlap && no); c++) {
+		for(int c = 0; c < 3 && !(stop_on_overlap && no) && uns <= 2; c++) {
 			const float ox = (c - 1) * w[0];
 			const int j1 = c == 0 ? a1 : (c == 1 ? m1 : p1);
 			for(int jq = (c == 0 ? a0 : (c == 1 ? m0 : p0)); jq < j1; jq++) {
@@ -1342,10 +1522,15 @@ __device__ __forceinline__ void energy_particle(const ppi_dev &d, int mode, int 
 					const float4 qd = d.sori[3 * (size_t) jq + 2];
 					const float cq[9] = { qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w, qd.x };
 					if(MODE == MODE_AUDIT)
-						cl = pair_state<MODE>(d.rec, rp, rs, pslot, 0, q0, d0, __float_as_int(qd.w), ddx, ddy, ddz, cp, cq, sqr_rcut, cosmax, basef, eps, sdir, vf, vside, A.fallbacks);
+						cl = pair_state<MODE>(d.rec, rp, rs, g.inv_L, pslot, 0, q0, d0, __float_as_int(qd.w), ddx, ddy, ddz, cp, cq, sqr_rcut, cosmax, basef, eps, sdir, vf, vside, A.fallbacks);
 					else {
 						cl = classify(ddx, ddy, ddz, cp, cq, sqr_rcut, cosmax, basef, eps, nullptr);
-						if(cl == CL_UNSURE) U.push(jq << 1);
+						if(cl == CL_UNSURE) { /* decided after the loop by the certified FP64 test */
+							if(uns == 0) u0 = jq;
+							else u1 = jq;
+							if(++uns > 2) break;
+							continue;
+						}
 					}
 					if(cl == CL_BOND && partners && nb < PPI_MAX_PARTNERS) partners[nb] = __float_as_int(qd.y);
 				}
@@ -1357,46 +1542,26 @@ __device__ __forceinline__ void energy_particle(const ppi_dev &d, int mode, int 
 			}
 		}
 	}
-	if(MODE == MODE_FAST && U.n && !(stop_on_overlap && no)) {
-		if(U.n > UNS_CAP) {
-			EnergyCtx E;
-			for(int a = 0; a < 3; a++) {
-				E.pl[a] = pl[a];
-				E.w[a] = w[a];
-			}
-			for(int a = 0; a < 9; a++) E.cp[a] = cp[a];
-			E.sf = sf;
-			E.k = k;
-			E.pslot = pslot;
-			E.cx = cx;
-			E.cy = cy;
-			E.cz = cz;
-			E.nx = nx;
-			E.ny = ny;
-			E.nz = nz;
-			E.cell_base = rp.cell_base;
-			E.sdir = sdir;
-			E.vf = vf;
-			E.vside = vside;
-			E.partners = partners;
-			const unsigned long long res = energy_lane_exact<G>(COLD_ARGS(d), r, E, sub);
-			nb = (int) (res & 0xffff);
-			no = (int) ((res >> 16) & 0xffff);
-			A.fallbacks += (unsigned) (res >> 32);
-		}
-		else {
-#pragma unroll 1
-			for(int kk = 0; kk < U.n; kk++) {
-				const int v = kk == 0 ? U.v0 : (kk == 1 ? U.v1 : (kk == 2 ? U.v2 : U.v3));
-				const int cl = resolve_exact(d, rp, rs, pslot, v, q0, d0, sdir, vf, vside, A);
-				if(cl == CL_BOND) {
-					if(partners && nb < PPI_MAX_PARTNERS) partners[nb] = __float_as_int(d.sori[3 * (size_t) (v >> 1) + 2].y);
+	if(MODE == MODE_FAST && uns && !(stop_on_overlap && no)) {
+		if(uns > 2) uns = -1; /* more than this lane keeps: the particle is computed exactly at the end */
+		else
+			for(int k2 = 0; k2 < uns; k2++) {
+				const int jq = k2 ? u1 : u0;
+				const float4 qd = d.sori[3 * (size_t) jq + 2];
+				A.fallbacks++;
+				const int ex = decide64(d.rec, rp, rs->box, g.inv_L, pslot, 0, q0, d0, __float_as_int(qd.w), sdir, vf, vside);
+				if(ex == DEC64_EXACT) {
+					uns = -1;
+					break;
+				}
+				if(ex == 1) {
+					if(partners && nb < PPI_MAX_PARTNERS) partners[nb] = __float_as_int(qd.y);
 					nb++;
 				}
-				no += (cl == CL_OVER);
+				no += (ex == -1);
 			}
-		}
 	}
+	if(MODE == MODE_FAST && __any_sync(gm, uns < 0)) return 1;
 	nb = group_sum<G>(gm, nb);
 	no = group_sum<G>(gm, no);
 	if(sub == 0) {
@@ -1407,23 +1572,52 @@ __device__ __forceinline__ void energy_particle(const ppi_dev &d, int mode, int 
 		if(no && !rs->vol_overlap) atomicExch(&rs->vol_overlap, 1); /* visible at once: lets the others skip work */
 		if(!(mode == PPI_EN_VOLUME && no)) A.tries += nb;
 	}
+	return 0;
 }
+
+#define ENERGY_DCAP 16 /* deferred particles a warp keeps in shared memory (more: flags in global memory) */
 
 template <int MODE, int G>
 __global__ void __launch_bounds__(128, MODE == MODE_FAST ? PPI_FAST_MIN_BLOCKS : 1) k_energy(ppi_dev d, int mode) {
+	__shared__ int s_dl[4][ENERGY_DCAP];
+	__shared__ int s_nd[4], s_dov[4];
 	constexpr int PW = 32 / G;
 	if(blockIdx.x * (blockDim.x / G) >= d.ntot) return;
 	Acc A; /* A.tries = bonds counted, pairs, fallbacks */
 	A.r = -1;
 	A.tries = A.acc = A.pairs = A.fallbacks = 0;
 	A.dbonds = 0;
+	const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
 	const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarp = (gridDim.x * blockDim.x) >> 5;
 	const int sub = threadIdx.x & (G - 1), slot = (threadIdx.x & 31) / G;
 	const unsigned gm = group_mask<G>();
+	if(lane == 0) {
+		s_nd[wi] = 0;
+		s_dov[wi] = 0;
+	}
+	__syncwarp();
 	for(int b = warp * PW; b < d.ntot; b += nwarp * PW) {
 		const int k = b + slot;
-		if(k < d.ntot) energy_particle<MODE, G>(d, mode, k, A, sub, gm);
+		if(k < d.ntot && energy_particle<MODE, G>(d, mode, k, A, sub, gm) && sub == 0) {
+			const int i = atomicAdd(&s_nd[wi], 1);
+			if(i < ENERGY_DCAP) s_dl[wi][i] = k;
+			else {
+				d.eflag[k] = 1;
+				s_dov[wi] = 1;
+			}
+		}
 	}
+	__syncwarp();
+	/* the deferred particles, one per lane, exactly */
+	const int nd = s_nd[wi] < ENERGY_DCAP ? s_nd[wi] : ENERGY_DCAP;
+	for(int i = lane; i < nd; i += 32) energy_exact(d, mode, s_dl[wi][i], A);
+	if(s_dov[wi])
+		for(int b = warp * PW; b < d.ntot; b += nwarp * PW)
+			if(sub == 0 && b + slot < d.ntot && d.eflag[b + slot]) {
+				d.eflag[b + slot] = 0;
+				energy_exact(d, mode, b + slot, A);
+			}
+	__syncwarp();
 	energy_flush_block(d, A);
 }
 
@@ -1723,7 +1917,8 @@ extern "C" int ppi_export(const ppi_dev *d, int first, int count, cudaStream_t s
 #define NA_AUX (NA_CREP + NA_ALIGN((size_t) NOALLOC_CELLS * sizeof(int)))
 #define NA_CLIST (NA_AUX + NA_ALIGN((size_t) (NOALLOC_CELLS / 1024 + 2) * sizeof(int)))
 #define NA_COLCOUNT (NA_CLIST + NA_ALIGN((size_t) 8 * (NOALLOC_CELLS / 8 + 8) * sizeof(int4)))
-#define NA_RP (NA_COLCOUNT + NA_ALIGN(8 * sizeof(int)))
+#define NA_EFLAG (NA_COLCOUNT + NA_ALIGN(8 * sizeof(int)))
+#define NA_RP (NA_EFLAG + NA_ALIGN((size_t) NOALLOC_N))
 #define NA_RS (NA_RP + NA_ALIGN(sizeof(ppi_rparams)))
 #define NA_GRID (NA_RS + NA_ALIGN(sizeof(ppi_rstate)))
 #define NA_TOTAL (NA_GRID + NA_ALIGN(sizeof(ppi_grid)))
@@ -1820,6 +2015,7 @@ extern "C" int pp_gpu_energy_noalloc(int N, const double *r_dev, const double *R
 	d.scan_aux = (int *) (base + NA_AUX);
 	d.clist = (int4 *) (base + NA_CLIST);
 	d.ccount = (int *) (base + NA_COLCOUNT);
+	d.eflag = (unsigned char *) (base + NA_EFLAG);
 	d.audit_any = 0;
 	d.lanes = 0;
 	d.rp = (ppi_rparams *) (base + NA_RP);
@@ -1832,7 +2028,8 @@ extern "C" int pp_gpu_energy_noalloc(int N, const double *r_dev, const double *R
 	rs.V = box[0] * box[1] * box[2];
 	if((c = cudaMemcpy(d.rp, &rp, sizeof(rp), cudaMemcpyHostToDevice)) != cudaSuccess ||
 			(c = cudaMemcpy(d.rs, &rs, sizeof(rs), cudaMemcpyHostToDevice)) != cudaSuccess ||
-			(c = cudaMemset(d.grid, 0, sizeof(ppi_grid))) != cudaSuccess || (c = cudaMemset(d.cell_rep, 0, sizeof(int) * (size_t) cells)) != cudaSuccess)
+			(c = cudaMemset(d.grid, 0, sizeof(ppi_grid))) != cudaSuccess || (c = cudaMemset(d.cell_rep, 0, sizeof(int) * (size_t) cells)) != cudaSuccess ||
+			(c = cudaMemset(d.eflag, 0, (size_t) (N > 0 ? N : 1))) != cudaSuccess)
 		return na_fail(err, err_len, PP_ERR_CUDA, "scratch set-up", cudaGetErrorString(c));
 	long long nl = 0;
 	if(N > 0) k_noalloc_pack<<<(N + 255) / 256, 256>>>(d, r_dev, R_dev);
