@@ -332,7 +332,10 @@ static int read_states(pp_engine *e) {
 	CU(cudaMemcpyAsync(e->h_rs, e->d.rs, sizeof(ppi_rstate) * e->nrep, cudaMemcpyDeviceToHost, e->stream));
 	CU(cudaStreamSynchronize(e->stream));
 	for(int r = 0; r < e->nrep; r++)
-		if(e->h_rs[r].error) return set_err(e, PP_ERR_CAPACITY, "replica %d: the box no longer fits an even cell grid of edge >= r_cut (device error %d)", r, e->h_rs[r].error);
+		if(e->h_rs[r].error == PPI_E_EXACT)
+			return set_err(e, PP_ERR_STATE, "replica %d: more pairs within 1e-12 of a bonding threshold than one warp keeps for the exact test", r);
+		else if(e->h_rs[r].error)
+			return set_err(e, PP_ERR_CAPACITY, "replica %d: the box no longer fits an even cell grid of edge >= r_cut (device error %d)", r, e->h_rs[r].error);
 	return PP_OK;
 }
 

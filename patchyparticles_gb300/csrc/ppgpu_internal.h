@@ -38,7 +38,8 @@ extern "C" {
 #define PPI_MAX_AXIS_CELLS 1024
 
 /* error codes written by kernels into ppi_rstate.error */
-#define PPI_E_GRID 2 /* the box became too small for an even cell grid of edge >= r_cut */
+#define PPI_E_GRID 2  /* the box became too small for an even cell grid of edge >= r_cut */
+#define PPI_E_EXACT 3 /* more undecidable pairs in one warp's share of a volume pass than it keeps */
 
 typedef struct ppi_rparams {
 	int N;           /* particles of this replica */

@@ -402,13 +402,15 @@ __device__ __forceinline__ void atomicMaxFloatBits(unsigned int *addr, float v) 
 	if(v > 0.f) atomicMax(addr, __float_as_uint(v)); /* positive floats order like their bit patterns */
 }
 
-/* audit: compare an FP32 decision with the exact one */
-__device__ __noinline__ void audit_pair(const double *rec_all, const ppi_rparams *rp, ppi_rstate *rs, const double *box, int ps, int kind, float4 q,
-		float3 disp, int qs, int vol_dir, double vol_f, double vol_side, int cl, PairF f) {
+/* audit: compare an FP32 decision, and the certified FP64 decision, with the exact one */
+__device__ __noinline__ void audit_pair(const double *rec_all, const ppi_rparams *rp, ppi_rstate *rs, const double *box, const double *inv_box, int ps, int kind,
+		float4 q, float3 disp, int qs, int vol_dir, double vol_f, double vol_side, int cl, PairF f) {
 	double d2, pm = -2., qm = -2.;
 	int ex = exact_pair(rec_all, rp, box, ps, kind, q, disp, qs, vol_dir, vol_f, vol_side, &d2, &pm, &qm);
 	int exc = ex == -1 ? CL_OVER : (ex == 1 ? CL_BOND : CL_NONE);
 	if(cl != CL_UNSURE && cl != exc) atomicAdd(&rs->mismatches, 1ull);
+	const int dc = decide64(rec_all, *rp, box, inv_box, ps, kind, q, disp, qs, vol_dir, vol_f, vol_side);
+	if(dc != DEC64_EXACT && dc != ex) atomicAdd(&rs->mismatches, 1ull);
 	if(d2 < (double) rp->sqr_rcut + 0.5) atomicMaxFloatBits(&rs->max_err_r2_bits, (float) fabs((double) f.r2 - d2));
 	if(pm > -1.5 && f.pmax > -1.5f) {
 		atomicMaxFloatBits(&rs->max_err_cos_bits, (float) fabs((double) f.pmax - pm));
@@ -742,7 +744,7 @@ __device__ __forceinline__ int pair_state(const double *rec, const ppi_rparams &
 		double vol_side, unsigned &fallbacks) {
 	PairF f;
 	int cl = classify(dx, dy, dz, cp, cq, sqr_rcut, cosmax, basef, eps, MODE == MODE_AUDIT ? &f : nullptr);
-	if(MODE == MODE_AUDIT) audit_pair(rec, &rp, rs, rs->box, pslot, kind, q, disp, qslot, vol_dir, vol_f, vol_side, cl, f);
+	if(MODE == MODE_AUDIT) audit_pair(rec, &rp, rs, rs->box, inv_box, pslot, kind, q, disp, qslot, vol_dir, vol_f, vol_side, cl, f);
 	if(cl == CL_UNSURE) {
 		fallbacks++;
 		int ex = decide64(rec, rp, rs->box, inv_box, pslot, kind, q, disp, qslot, vol_dir, vol_f, vol_side);
@@ -1621,6 +1623,349 @@ __global__ void __launch_bounds__(128, MODE == MODE_FAST ? PPI_FAST_MIN_BLOCKS :
 	energy_flush_block(d, A);
 }
 
+/* ------------------------------------------------------------------------------------------------ */
+/* NPT candidate box: bonds and overlaps of all pairs, one warp tile of 64 particles at a time       */
+/* ------------------------------------------------------------------------------------------------ */
+/* The volume move needs only the candidate box's total bond count and whether any pair overlaps
+ * (MC.c:487-495), so every pair is evaluated once, from its particle with the lower sorted position
+ * (a half shell: each row range of the neighbourhood is clamped to positions above the particle's).
+ * Same pair-list layout as the colour pass: lanes own particles for the set-up, the pairs of a plane are
+ * flattened and walked 32 per step, pairs within the bonding range get their patch test, guard-band pairs
+ * the certified FP64 test and, in the rare undecided case, exact_pair at the end of the warp's share. */
+#define EV_UCAP 32
+
+struct __align__(16) VolSmem {
+	float4 pos[TA];   /* scaled cell-local position, .w = cell x index */
+	float4 wv[TA];    /* scaled cell edges, .w = number of x cells */
+	float4 vs[TA];    /* (scale factor, scaled axis as int bits, -, -) */
+	float cp[9][TA];  /* orientation columns */
+	int ki[TA];       /* sorted position */
+	int rep[TA];
+	int cc[TA];       /* cell coordinates cx | cy << 10 | cz << 20, -1: no particle */
+	int pbuf[TILE_PCAP]; /* (candidate - particle) << 10 | particle << 4 | row */
+	int cbuf[TILE_CCAP];
+	int2 uns[EV_UCAP];  /* guard-band pairs: (candidate, particle) */
+	int2 exl[EV_UCAP];  /* pairs left to exact_pair: (candidate, particle), decided at the end of the share */
+	int nc, nu, nex;
+};
+
+__device__ __forceinline__ void vol_exact_later(const ppi_dev &d, VolSmem &S, int jq, int k);
+
+__device__ __forceinline__ void vol_setup(const ppi_dev &d, VolSmem &S, int a, int k) {
+	int cc = -1, r = 0;
+	float4 pos = make_float4(0.f, 0.f, 0.f, 0.f), wv = make_float4(1.f, 1.f, 1.f, __int_as_float(4)), vs = make_float4(1.f, __int_as_float(-1), 0.f, 0.f);
+	if(k >= 0) {
+		const float4 pa = d.spos[k], pb = d.sori[3 * (size_t) k], pc = d.sori[3 * (size_t) k + 1], pd = d.sori[3 * (size_t) k + 2];
+		const int gc = __float_as_int(pd.z);
+		r = d.cell_rep[gc];
+		const ppi_grid &g = d.grid[r];
+		if(g.vol_dir >= 0) {
+			const int sdir = g.vol_dir;
+			const float sf = g.vol_ff;
+			pos = make_float4(sdir == 0 ? pa.x * sf : pa.x, sdir == 1 ? pa.y * sf : pa.y, sdir == 2 ? pa.z * sf : pa.z, pa.w);
+			wv = make_float4(sdir == 0 ? g.wf[0] * sf : g.wf[0], sdir == 1 ? g.wf[1] * sf : g.wf[1], sdir == 2 ? g.wf[2] * sf : g.wf[2], __int_as_float(g.n[0]));
+			vs = make_float4(sf, __int_as_float(sdir), 0.f, 0.f);
+			const int local = gc - d.rp[r].cell_base;
+			cc = (local % g.n[0]) | (((local / g.n[0]) % g.n[1]) << 10) | ((local / (g.n[0] * g.n[1])) << 20);
+			const float c9[9] = { pb.x, pb.y, pb.z, pb.w, pc.x, pc.y, pc.z, pc.w, pd.x };
+#pragma unroll
+			for(int j = 0; j < 9; j++) S.cp[j][a] = c9[j];
+		}
+	}
+	S.pos[a] = pos;
+	S.wv[a] = wv;
+	S.vs[a] = vs;
+	S.ki[a] = k;
+	S.rep[a] = r;
+	S.cc[a] = cc;
+}
+
+/* half-shell ranges of plane pz of particle a (candidates above its sorted position) */
+__device__ __forceinline__ int vol_ranges(const ppi_dev &d, const VolSmem &S, int a, int pz, PlaneRanges &P) {
+#pragma unroll
+	for(int j = 0; j < 6; j++) P.s[j] = P.e[j] = 0;
+	const int ccp = S.cc[a];
+	if(ccp < 0) return 0;
+	const int r = S.rep[a];
+	if(*(volatile int *) &d.rs[r].vol_overlap) return 0; /* the candidate box is rejected already */
+	const ppi_grid &g = d.grid[r];
+	const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+	const int cb = d.rp[r].cell_base;
+	const int cx = ccp & 1023, cy = (ccp >> 10) & 1023, cz = ccp >> 20;
+	const bool inner = cx >= 1 && cx <= nx - 2;
+	const int xa0 = inner ? cx - 1 : (cx == 0 ? nx - 1 : nx - 2), xa1 = inner ? cx + 2 : nx;
+	const int xb1 = cx == 0 ? 2 : 1;
+	const int kmin = S.ki[a] + 1;
+	int n = 0;
+#pragma unroll
+	for(int ry = 0; ry < 3; ry++) {
+		const int *cs = d.cell_start + cb + (wrapi(cz + pz - 1, nz) * ny + wrapi(cy + ry - 1, ny)) * nx;
+		P.s[2 * ry] = max(cs[xa0], kmin);
+		P.e[2 * ry] = max(cs[xa1], P.s[2 * ry]);
+		if(!inner) {
+			P.s[2 * ry + 1] = max(cs[0], kmin);
+			P.e[2 * ry + 1] = max(cs[xb1], P.s[2 * ry + 1]);
+		}
+	}
+#pragma unroll
+	for(int j = 0; j < 6; j++) n += P.e[j] - P.s[j];
+	return n;
+}
+
+__device__ __forceinline__ int vol_far(const VolSmem &S, int a, const PlaneRanges &P) {
+	int m = 0;
+#pragma unroll
+	for(int j = 0; j < 6; j++) m = max(m, P.e[j]);
+	return m - S.ki[a] >= TILE_OFF_MAX;
+}
+
+__device__ __forceinline__ void vol_write(VolSmem &S, int a, int pz, const PlaneRanges &P, int pos) {
+	const int k = S.ki[a];
+#pragma unroll
+	for(int sg = 0; sg < 6; sg++) {
+		const int tag = (a << 4) | (3 * pz + (sg >> 1));
+		for(int jq = P.s[sg]; jq < P.e[sg]; jq++) {
+			const int off = jq - k;
+			S.pbuf[pos++] = (int) ((unsigned) off << 10) | tag;
+		}
+	}
+}
+
+/* candidate position in particle a's scaled cell frame, relative to a */
+__device__ __forceinline__ float3 vol_geo(const VolSmem &S, int a, int t, float4 qa) {
+	const float4 p = S.pos[a], w = S.wv[a], v = S.vs[a];
+	const int sdir = __float_as_int(v.y);
+	const float qx = sdir == 0 ? qa.x * v.x : qa.x, qy = sdir == 1 ? qa.y * v.x : qa.y, qz = sdir == 2 ? qa.z * v.x : qa.z;
+	const int nxc = __float_as_int(w.w);
+	int dxc = __float_as_int(qa.w) - __float_as_int(p.w);
+	dxc = dxc > 1 ? dxc - nxc : (dxc < -1 ? dxc + nxc : dxc);
+	return make_float3((qx - p.x) + dxc * w.x, (qy - p.y) + (t % 3 - 1) * w.y, (qz - p.z) + (t / 3 - 1) * w.z);
+}
+
+__device__ __forceinline__ void vol_close(const ppi_dev &d, VolSmem &S, int lane, Acc &A) {
+	const int nc = S.nc;
+	for(int c = lane; c < nc; c += 32) {
+		const int en = S.cbuf[c];
+		const int a = (en >> 4) & 63, t = en & 15;
+		const int jq = S.ki[a] + (en >> 10);
+		const int r = S.rep[a];
+		const ppi_rparams &rp = d.rp[r];
+		const float4 qa = d.spos[jq], qb = d.sori[3 * (size_t) jq], qc = d.sori[3 * (size_t) jq + 1], qd = d.sori[3 * (size_t) jq + 2];
+		const float cq[9] = { qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w, qd.x };
+		float cp[9];
+#pragma unroll
+		for(int j = 0; j < 9; j++) cp[j] = S.cp[j][a];
+		const float3 dv = vol_geo(S, a, t, qa);
+		const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
+		const int cl = classify(dv.x, dv.y, dv.z, cp, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, nullptr);
+		if(cl == CL_UNSURE) {
+			const int k = atomicAdd(&S.nu, 1);
+			if(k < EV_UCAP) S.uns[k] = make_int2(jq, a);
+			else vol_exact_later(d, S, jq, S.ki[a]); /* list full: decided exactly at the end */
+			continue;
+		}
+		if(r != A.r) {
+			energy_flush_thread(d, A);
+			A.r = r;
+		}
+		if(cl == CL_BOND) A.tries += 2; /* the box total counts every bond from both sides */
+		else if(cl == CL_OVER && !d.rs[r].vol_overlap) atomicExch(&d.rs[r].vol_overlap, 1);
+	}
+	__syncwarp();
+	if(lane == 0) S.nc = 0;
+	__syncwarp();
+}
+
+/* a pair for exact_pair at the end of the warp's share; more than EV_UCAP of them in one share (pairs
+ * within 1e-12 of a threshold, or guard-band overflow) is reported as PPI_E_EXACT instead */
+__device__ __forceinline__ void vol_exact_later(const ppi_dev &d, VolSmem &S, int jq, int k) {
+	const int x = atomicAdd(&S.nex, 1);
+	if(x < EV_UCAP) S.exl[x] = make_int2(jq, k);
+	else d.rs[d.cell_rep[__float_as_int(d.sori[3 * (size_t) k + 2].z)]].error = PPI_E_EXACT;
+}
+
+/* the decision of pair (candidate jq, particle k): certified FP64, or (exact = 1) the bit-identical
+ * exact_pair */
+__device__ __forceinline__ void vol_pair_decide(const ppi_dev &d, VolSmem &S, int jq, int k, int exact, Acc &A) {
+	const int r = d.cell_rep[__float_as_int(d.sori[3 * (size_t) k + 2].z)];
+	const ppi_grid &g = d.grid[r];
+	const int ps = __float_as_int(d.sori[3 * (size_t) k + 2].w), qs = __float_as_int(d.sori[3 * (size_t) jq + 2].w);
+	const float4 q0 = make_float4(1.f, 0.f, 0.f, 0.f);
+	const float3 d0 = make_float3(0.f, 0.f, 0.f);
+	A.fallbacks++;
+	int ex = exact ? exact_pair(d.rec, d.rp + r, d.rs[r].box, ps, 0, q0, d0, qs, g.vol_dir, g.vol_f, g.vol_side, nullptr, nullptr, nullptr)
+				   : decide64(d.rec, d.rp[r], d.rs[r].box, g.inv_L, ps, 0, q0, d0, qs, g.vol_dir, g.vol_f, g.vol_side);
+	if(ex == DEC64_EXACT) {
+		vol_exact_later(d, S, jq, k);
+		return;
+	}
+	if(r != A.r) {
+		energy_flush_thread(d, A);
+		A.r = r;
+	}
+	if(ex == 1) A.tries += 2; /* the box total counts every bond from both sides */
+	else if(ex == -1 && !d.rs[r].vol_overlap) atomicExch(&d.rs[r].vol_overlap, 1);
+}
+
+/* the pairs of a lane whose plane slice alone exceeds the pair list (cells far denser than a hard-sphere
+ * packing allows; kept for completeness): evaluated one by one */
+__device__ __forceinline__ void vol_lane_pairs(const ppi_dev &d, VolSmem &S, int a, int pz, const PlaneRanges &P, Acc &A) {
+	const int k = S.ki[a];
+	const int r = S.rep[a];
+	const ppi_rparams &rp = d.rp[r];
+	const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
+	float cp[9];
+#pragma unroll
+	for(int j = 0; j < 9; j++) cp[j] = S.cp[j][a];
+	for(int sg = 0; sg < 6; sg++)
+		for(int jq = P.s[sg]; jq < P.e[sg]; jq++) {
+			const float4 qa = d.spos[jq], qb = d.sori[3 * (size_t) jq], qc = d.sori[3 * (size_t) jq + 1];
+			const float cq[9] = { qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w, d.sori[3 * (size_t) jq + 2].x };
+			const float3 dv = vol_geo(S, a, 3 * pz + (sg >> 1), qa);
+			A.pairs++;
+			const int cl = classify(dv.x, dv.y, dv.z, cp, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, nullptr);
+			if(cl == CL_UNSURE) vol_pair_decide(d, S, jq, k, 0, A);
+			else {
+				if(r != A.r) {
+					energy_flush_thread(d, A);
+					A.r = r;
+				}
+				if(cl == CL_BOND) A.tries += 2;
+				else if(cl == CL_OVER && !d.rs[r].vol_overlap) atomicExch(&d.rs[r].vol_overlap, 1);
+			}
+		}
+}
+
+__global__ void __launch_bounds__(32 * TILE_WARPS, PPI_TILE_MIN_BLOCKS) k_energy_vol(ppi_dev d) {
+	__shared__ VolSmem s_vol[TILE_WARPS];
+	VolSmem &S = s_vol[threadIdx.x >> 5];
+	const int lane = threadIdx.x & 31;
+	Acc A;
+	A.r = -1;
+	A.tries = A.acc = A.pairs = A.fallbacks = 0;
+	A.dbonds = 0;
+	const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarp = (gridDim.x * blockDim.x) >> 5;
+	const int lo = (int) ((long long) warp * d.ntot / nwarp), hi = (int) ((long long) (warp + 1) * d.ntot / nwarp);
+	const unsigned lt = (1u << lane) - 1u;
+	if(lane == 0) S.nex = 0;
+	__syncwarp();
+	for(int b = lo; b < hi; b += TA) {
+		vol_setup(d, S, lane, b + lane < hi ? b + lane : -1);
+		vol_setup(d, S, lane + 32, b + 32 + lane < hi ? b + 32 + lane : -1);
+		if(lane == 0) {
+			S.nc = 0;
+			S.nu = 0;
+		}
+		__syncwarp();
+#pragma unroll 1
+		for(int pz = 0; pz < 3; pz++) {
+			PlaneRanges P0, P1;
+			int n0 = vol_ranges(d, S, lane, pz, P0), n1 = vol_ranges(d, S, lane + 32, pz, P1);
+			/* candidates farther than a packed entry can hold (planes of more than ~2M particles): one by one */
+			if(n0 && vol_far(S, lane, P0)) {
+				vol_lane_pairs(d, S, lane, pz, P0, A);
+				n0 = 0;
+#pragma unroll
+				for(int j = 0; j < 6; j++) P0.s[j] = P0.e[j] = 0;
+			}
+			if(n1 && vol_far(S, lane + 32, P1)) {
+				vol_lane_pairs(d, S, lane + 32, pz, P1, A);
+				n1 = 0;
+#pragma unroll
+				for(int j = 0; j < 6; j++) P1.s[j] = P1.e[j] = 0;
+			}
+			const int n = n0 + n1;
+			int incl = n;
+#pragma unroll
+			for(int o = 1; o < 32; o <<= 1) {
+				const int v = __shfl_up_sync(0xffffffffu, incl, o);
+				if(lane >= o) incl += v;
+			}
+			const int total = __shfl_sync(0xffffffffu, incl, 31);
+			if(total == 0) continue;
+			/* a plane that does not fit is walked in slices of whole lanes */
+			int done = 0;
+			while(done < total) {
+				const int start = incl - n;
+				const int mine = n > 0 && start >= done && incl - done <= TILE_PCAP;
+				const unsigned take = __ballot_sync(0xffffffffu, mine);
+				if(take == 0) { /* the next lane's slice alone exceeds the list */
+					const int big = n > 0 && start == done;
+					if(big) {
+						vol_lane_pairs(d, S, lane, pz, P0, A);
+						vol_lane_pairs(d, S, lane + 32, pz, P1, A);
+					}
+					const unsigned bm = __ballot_sync(0xffffffffu, big);
+					done = __shfl_sync(0xffffffffu, incl, __ffs(bm) - 1);
+					continue;
+				}
+				if(mine) {
+					const int pos = start - done;
+					vol_write(S, lane, pz, P0, pos);
+					vol_write(S, lane + 32, pz, P1, pos + n0);
+				}
+				const int end = __shfl_sync(0xffffffffu, incl, 31 - __clz(take));
+				const int np = end - done;
+				__syncwarp();
+				for(int p0 = 0; p0 < np; p0 += 32 * PSTEP) {
+					int en[PSTEP], ok[PSTEP];
+					float4 qa[PSTEP];
+#pragma unroll
+					for(int u = 0; u < PSTEP; u++) {
+						const int p = p0 + 32 * u + lane;
+						en[u] = 0;
+						ok[u] = 0;
+						qa[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+						if(p < np) {
+							en[u] = S.pbuf[p];
+							const int a = (en[u] >> 4) & 63, off = en[u] >> 10;
+							ok[u] = off != 0;
+							if(ok[u]) qa[u] = d.spos[S.ki[a] + off];
+						}
+					}
+#pragma unroll
+					for(int u = 0; u < PSTEP; u++) {
+						int close = 0;
+						if(ok[u]) {
+							const int a = (en[u] >> 4) & 63;
+							const float3 dv = vol_geo(S, a, en[u] & 15, qa[u]);
+							const float r2 = fmaf(dv.x, dv.x, fmaf(dv.y, dv.y, dv.z * dv.z));
+							const int r = S.rep[a];
+							const ppi_rparams &rp = d.rp[r];
+							const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
+							A.pairs++;
+							if(r2 < 1.f - eps) {
+								if(!d.rs[r].vol_overlap) atomicExch(&d.rs[r].vol_overlap, 1);
+							}
+							else close = r2 < rp.sqr_rcut_f + eps;
+						}
+						const unsigned m = __ballot_sync(0xffffffffu, close);
+						if(m) {
+							if(S.nc + __popc(m) > TILE_CCAP) vol_close(d, S, lane, A);
+							if(close) S.cbuf[S.nc + __popc(m & lt)] = en[u];
+							__syncwarp();
+							if(lane == 0) S.nc += __popc(m);
+							__syncwarp();
+						}
+					}
+				}
+				done = end;
+				__syncwarp();
+			}
+		}
+		if(S.nc) vol_close(d, S, lane, A);
+		/* guard-band pairs: certified FP64 decisions */
+		const int nu = S.nu < EV_UCAP ? S.nu : EV_UCAP;
+		for(int u = lane; u < nu; u += 32) vol_pair_decide(d, S, S.uns[u].x, S.ki[S.uns[u].y], 0, A);
+		__syncwarp();
+	}
+	/* pairs within 1e-12 of a threshold (rare): the bit-identical exact_pair, after the loop */
+	const int nex = S.nex < EV_UCAP ? S.nex : EV_UCAP;
+	for(int u = lane; u < nex; u += 32) vol_pair_decide(d, S, S.exl[u].x, S.exl[u].y, 1, A);
+	__syncwarp();
+	energy_flush_block(d, A);
+}
+
 __global__ void k_energy_reset(ppi_dev d) {
 	int r = blockIdx.x * blockDim.x + threadIdx.x;
 	if(r >= d.nrep) return;
@@ -1844,6 +2189,10 @@ static void launch_energy(const ppi_dev *d, int mode, cudaStream_t s, long long 
 		else k_energy<MODE_FAST, 1><<<resident_grid(k_energy<MODE_FAST, 1>, &g_f1), 128, 0, s>>>(*d, mode);
 	}
 	else if(audit) k_energy<MODE_AUDIT, 4><<<resident_grid(k_energy<MODE_AUDIT, 4>, &g_a4), 128, 0, s>>>(*d, mode);
+	else if(mode == PPI_EN_VOLUME) {
+		static int g_vol = 0;
+		k_energy_vol<<<resident_grid(k_energy_vol, &g_vol, 32 * TILE_WARPS), 32 * TILE_WARPS, 0, s>>>(*d);
+	}
 	else if(lanes_of(d) == 8) k_energy<MODE_FAST, 8><<<resident_grid(k_energy<MODE_FAST, 8>, &g_f8), 128, 0, s>>>(*d, mode);
 	else k_energy<MODE_FAST, 4><<<resident_grid(k_energy<MODE_FAST, 4>, &g_f4), 128, 0, s>>>(*d, mode);
 	*nl += 1;
