@@ -33,7 +33,9 @@ import numpy as np  # noqa: E402
 
 METRIC = "MC move attempts/sec at N=1M (frac of HBM peak); eff. samples/sec learned vs plain"
 UNIT = "attempts/s"
-BYTES_PER_ATTEMPT = 192  # read + write of the FP64 canonical state r (24 B) + R (72 B) per attempt
+# algorithmic bytes of one attempt: read + write of one particle's FP64 state as the reference keeps it,
+# position (24 B) + orientation matrix (72 B); the unit of the HBM roofline of the sweep kernel
+BYTES_PER_ATTEMPT = 192
 
 WORKLOADS = {
     "c5": dict(N=1048576, rho=0.3, T=0.11, P=0.05, ensemble=5, rescale=0.01, disp=0.05, theta=0.1, seed=1005,
@@ -280,7 +282,8 @@ def run_gpu(args, wl, ws, rank, local, dist):
         el = allreduce(dist, el, _max_op(dist))
         att_e2e = allreduce(dist, att_e2e, _sum_op(dist))
         N = wl["N"]
-        e2e = {"value": att_e2e / el, "unit": UNIT, "h2d_bytes_per_step": N * (96 + 4), "d2h_bytes_per_step": N * (96 + 4),
+        # upload: 16-double canonical records + particle index; download: x y z R (12 doubles) + index
+        e2e = {"value": att_e2e / el, "unit": UNIT, "h2d_bytes_per_step": N * (128 + 4), "d2h_bytes_per_step": N * (96 + 4),
                "sweeps_per_step": args.e2e_sweeps, "steps": e2e_steps}
 
     cpu = None
@@ -297,7 +300,7 @@ def run_gpu(args, wl, ws, rank, local, dist):
         "ms_per_step": 1000.0 * t_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64", "data": "synthetic (seeded random insertion, uniform orientations)",
         "config": {"workload": wl["name"], "N": wl["N"], "sweeps_per_step": spsw, "proposal": "plain",
-                   "l2": "inputs larger than L2 (FP64 state %.0f MB + FP32 mirror %.0f MB per GPU)" % (wl["N"] * 96 / 1e6, wl["N"] * 64 / 1e6),
+                   "l2": "inputs larger than L2 (FP64 state %.0f MB + FP32 mirror %.0f MB per GPU)" % (wl["N"] * 128 / 1e6, wl["N"] * 64 / 1e6),
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "acceptance": acc[pp.MOVE_ROTO_TRASL] / max(1, tries[pp.MOVE_ROTO_TRASL]),
         "volume_acceptance": acc[pp.MOVE_VOLUME] / max(1, tries[pp.MOVE_VOLUME]) if tries[pp.MOVE_VOLUME] else None,

@@ -82,6 +82,8 @@ typedef struct ppi_grid {
 	double inv_w[3], inv_L[3];
 	float wf[3];
 	float pad;
+	float inv_wf[3], inv_Lf[3], Lf[3]; /* FP32 copies for the cell assignment's guesses */
+	float pad4;
 	/* NPT candidate of the current sweep (MC.c:456-472) */
 	int vol_dir;
 	int pad2;

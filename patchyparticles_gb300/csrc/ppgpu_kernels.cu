@@ -461,40 +461,58 @@ __global__ void k_grid(ppi_dev d, long long epoch) {
 		g->shift[a] = (double) us[a] * w;
 		g->inv_w[a] = 1.0 / w;
 		g->inv_L[a] = 1.0 / rs->box[a];
+		g->inv_wf[a] = (float) g->inv_w[a];
+		g->inv_Lf[a] = (float) g->inv_L[a];
+		g->Lf[a] = (float) rs->box[a];
 	}
 	g->ncells = n[0] * n[1] * n[2];
 }
 
-/* cell of a slot in the current grid (FP64) and its cell-local coordinates (rounded to FP32) */
+/* d2f truncated toward zero (the guesses below only need ~1e-7) */
+__device__ __forceinline__ float d2f_trunc(double x) {
+	const unsigned long long u = (unsigned long long) __double_as_longlong(x);
+	const int e = (int) ((u >> 52) & 0x7ff) - 896;
+	if(e <= 0) return 0.f;
+	return __uint_as_float(((uint32_t) (u >> 32) & 0x80000000u) | ((uint32_t) e << 23) | ((uint32_t) (u >> 29) & 0x7fffffu));
+}
+
+/* cell of a slot in the current grid and its cell-local coordinates (FP32). Per axis: the periodic
+ * image and the cell index are guessed in FP32 and the FP64 work is four operations (image, grid origin,
+ * cell origin, local offset); the FP32 local coordinate is then checked to lie in [0, w) and the cell
+ * index corrected if it does not (the FP64 pipe is the scarce resource on this GPU). */
 __global__ void k_assign(ppi_dev d, float4 *tmp) {
 	int s = blockIdx.x * blockDim.x + threadIdx.x;
 	if(s >= d.ntot) return;
-	int r = d.rep[s];
-	const ppi_grid g = d.grid[r];
+	const int r = d.rep[s];
+	const ppi_grid &g = d.grid[r];
 	const double *x = d.rec + (size_t) s * PPI_REC;
+	const double2 x01 = *(const double2 *) x;
+	const double xs[3] = { x01.x, x01.y, x[2] };
 	int c[3];
 	float l[3];
+#pragma unroll
 	for(int a = 0; a < 3; a++) {
-		double L = d.rs[r].box[a];
-		double xw = x[a] - L * floor(x[a] * g.inv_L[a]);
-		if(xw >= L) xw -= L; /* the reciprocal may round floor() one step off */
-		else if(xw < 0.) xw += L;
-		double u = (xw - g.shift[a]) * g.inv_w[a];
-		int ci;
-		double lo;
-		if(u < 0.) {
-			ci = g.n[a] - 1; /* below the shifted origin: the last cell, across the periodic boundary */
-			lo = (xw + L) - (g.shift[a] + ci * g.w[a]);
-		}
-		else {
-			ci = (int) floor(u);
-			if(ci > g.n[a] - 1) ci = g.n[a] - 1;
-			lo = xw - (g.shift[a] + ci * g.w[a]);
-		}
+		const double L = d.rs[r].box[a], w = g.w[a];
+		const int n = g.n[a];
+		const float Lf = g.Lf[a], wf = g.wf[a];
+		/* periodic image: x - k L in [0, L) */
+		const float kf = floorf(d2f_trunc(xs[a]) * g.inv_Lf[a]);
+		double y = __fma_rn(-f2d(kf), L, xs[a]) - g.shift[a];
+		float yf = d2f_trunc(y);
+		if(yf < 0.f) y += L;
+		else if(yf >= Lf) y -= L;
+		yf = d2f_trunc(y);
+		if(yf < 0.f) y += L; /* a guess of k off by one in both steps: one more image */
+		else if(yf >= Lf) y -= L;
+		int ci = (int) (d2f_trunc(y) * g.inv_wf[a]);
+		ci = ci < 0 ? 0 : (ci > n - 1 ? n - 1 : ci);
+		float lf = d2f(y - f2d((float) ci) * w);
+		if(lf < 0.f && ci > 0) lf = d2f(y - f2d((float) --ci) * w);
+		else if(lf >= wf && ci < n - 1) lf = d2f(y - f2d((float) ++ci) * w);
 		c[a] = ci;
-		l[a] = (float) lo;
+		l[a] = lf;
 	}
-	int gc = d.rp[r].cell_base + (c[2] * g.n[1] + c[1]) * g.n[0] + c[0];
+	const int gc = d.rp[r].cell_base + (c[2] * g.n[1] + c[1]) * g.n[0] + c[0];
 	d.cellof[s] = gc;
 	tmp[s] = make_float4(l[0], l[1], l[2], __int_as_float(gc));
 	atomicAdd(d.cell_count + gc, 1);
@@ -768,7 +786,7 @@ __device__ __forceinline__ int pair_state(const double *rec, const ppi_rparams &
  * not matter; keeping the out-of-line FP64 code out of the loop keeps the loop free of spills. */
 #define TA 64          /* attempts per warp and iteration (2 per lane) */
 #define TILE_PCAP 768  /* pair list capacity per neighbour plane */
-#define TILE_CCAP 128  /* close-pair list capacity (flushed before it can overflow) */
+#define TILE_CCAP 128  /* close-pair list capacity, >= 32 * PSTEP (flushed before it can overflow) */
 #define TILE_DCAP 16   /* deferred attempts a warp keeps in shared memory (more: flags in global memory) */
 #define TILE_UCAP 32   /* guard-band pairs per iteration resolved in place (more: the attempt is deferred) */
 #define PSTEP 4        /* pair steps whose candidate loads are issued together */
@@ -783,6 +801,7 @@ struct __align__(16) TileSmem {
 	float4 wv[TA];    /* cell edges (wx, wy, wz), .w = number of x cells */
 	float4 qr[TA];    /* proposed rotation quaternion */
 	float cpo[9][TA]; /* mover's old orientation columns */
+	float2 lim[TA];   /* (1 - eps, r_cut^2 + eps): certain overlap below, certainly unbonded above */
 	int mi[TA];       /* mover sorted position */
 	int rep[TA];      /* replica */
 	int cc[TA];       /* mover cell coordinates cx | cy << 10 | cz << 20 */
@@ -1036,6 +1055,7 @@ __device__ __forceinline__ int tile_setup(const ppi_dev &d, TileSmem &S, int a, 
 	P.q = make_float4(1.f, 0.f, 0.f, 0.f);
 	P.disp = make_float3(0.f, 0.f, 0.f);
 	float4 wv = make_float4(1.f, 1.f, 1.f, __int_as_float(4));
+	float2 lim = make_float2(0.f, 0.f);
 	if(ent.x >= 0) {
 		if(ent.w != A.r) {
 			flush_thread(d, A);
@@ -1044,6 +1064,9 @@ __device__ __forceinline__ int tile_setup(const ppi_dev &d, TileSmem &S, int a, 
 		A.tries++;
 		propose(d, ent, round, P);
 		const ppi_grid &g = d.grid[P.r];
+		const ppi_rparams &rp = d.rp[P.r];
+		const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
+		lim = make_float2(1.f - eps, rp.sqr_rcut_f + eps);
 		wv = make_float4(g.wf[0], g.wf[1], g.wf[2], __int_as_float(g.n[0]));
 		const int cx = P.local % g.n[0], cy = (P.local / g.n[0]) % g.n[1], cz = P.local / (g.n[0] * g.n[1]);
 		S.cc[a] = cx | (cy << 10) | (cz << 20);
@@ -1058,6 +1081,7 @@ __device__ __forceinline__ int tile_setup(const ppi_dev &d, TileSmem &S, int a, 
 	S.wv[a] = wv;
 	S.qr[a] = P.q;
 	S.mi[a] = P.i;
+	S.lim[a] = lim;
 	S.rep[a] = P.r;
 	S.bo[a] = 0;
 	S.bn[a] = 0;
@@ -1182,29 +1206,40 @@ __device__ __forceinline__ void tile_round(const ppi_dev &d, TileSmem &S, const 
 					if(ok[u]) qa[u] = d.spos[S.mi[a] + off];
 				}
 			}
+			int close[PSTEP];
 #pragma unroll
 			for(int u = 0; u < PSTEP; u++) {
-				int close = 0;
+				close[u] = 0;
 				if(ok[u]) {
 					const int a = (en[u] >> 4) & 63;
 					const PairGeo G = pair_geo(S, a, en[u] & 15, qa[u]);
 					const float r2o = fmaf(G.dxo, G.dxo, fmaf(G.dyo, G.dyo, G.dzo * G.dzo));
 					const float r2n = fmaf(G.dxn, G.dxn, fmaf(G.dyn, G.dyn, G.dzn * G.dzn));
-					const ppi_rparams &rp = d.rp[S.rep[a]];
-					const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
+					const float2 lim = S.lim[a];
 					A.pairs += 2;
-					if(MODE != MODE_AUDIT && r2n < 1.f - eps) atomicOr(&S.flag[a], TF_OVER); /* certain overlap of the candidate state */
-					else close = MODE == MODE_AUDIT || r2o < rp.sqr_rcut_f + eps || r2n < rp.sqr_rcut_f + eps;
+					if(MODE != MODE_AUDIT && r2n < lim.x) atomicOr(&S.flag[a], TF_OVER); /* certain overlap of the candidate state */
+					else close[u] = MODE == MODE_AUDIT || r2o < lim.y || r2n < lim.y;
 				}
-				/* compact the close pairs into the patch-test list */
-				const unsigned m = __ballot_sync(0xffffffffu, close);
-				if(m) {
-					if(S.nc + __popc(m) > TILE_CCAP) tile_close<MODE>(d, S, lane, A);
-					if(close) S.cbuf[S.nc + __popc(m & lt)] = en[u];
-					__syncwarp();
-					if(lane == 0) S.nc += __popc(m);
-					__syncwarp();
+			}
+			/* compact the group's close pairs into the patch-test list */
+			unsigned m[PSTEP];
+			int tot = 0;
+#pragma unroll
+			for(int u = 0; u < PSTEP; u++) {
+				m[u] = __ballot_sync(0xffffffffu, close[u]);
+				tot += __popc(m[u]);
+			}
+			if(tot) {
+				if(S.nc + tot > TILE_CCAP) tile_close<MODE>(d, S, lane, A);
+				int base = S.nc;
+#pragma unroll
+				for(int u = 0; u < PSTEP; u++) {
+					if(close[u]) S.cbuf[base + __popc(m[u] & lt)] = en[u];
+					base += __popc(m[u]);
 				}
+				__syncwarp();
+				if(lane == 0) S.nc = base;
+				__syncwarp();
 			}
 		}
 	}
@@ -1637,7 +1672,7 @@ __global__ void __launch_bounds__(128, MODE == MODE_FAST ? PPI_FAST_MIN_BLOCKS :
 struct __align__(16) VolSmem {
 	float4 pos[TA];   /* scaled cell-local position, .w = cell x index */
 	float4 wv[TA];    /* scaled cell edges, .w = number of x cells */
-	float4 vs[TA];    /* (scale factor, scaled axis as int bits, -, -) */
+	float4 vs[TA];    /* (scale factor, scaled axis as int bits, 1 - eps, r_cut^2 + eps) */
 	float cp[9][TA];  /* orientation columns */
 	int ki[TA];       /* sorted position */
 	int rep[TA];
@@ -1664,7 +1699,9 @@ __device__ __forceinline__ void vol_setup(const ppi_dev &d, VolSmem &S, int a, i
 			const float sf = g.vol_ff;
 			pos = make_float4(sdir == 0 ? pa.x * sf : pa.x, sdir == 1 ? pa.y * sf : pa.y, sdir == 2 ? pa.z * sf : pa.z, pa.w);
 			wv = make_float4(sdir == 0 ? g.wf[0] * sf : g.wf[0], sdir == 1 ? g.wf[1] * sf : g.wf[1], sdir == 2 ? g.wf[2] * sf : g.wf[2], __int_as_float(g.n[0]));
-			vs = make_float4(sf, __int_as_float(sdir), 0.f, 0.f);
+			const ppi_rparams &rp = d.rp[r];
+			const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
+			vs = make_float4(sf, __int_as_float(sdir), 1.f - eps, rp.sqr_rcut_f + eps);
 			const int local = gc - d.rp[r].cell_base;
 			cc = (local % g.n[0]) | (((local / g.n[0]) % g.n[1]) << 10) | ((local / (g.n[0] * g.n[1])) << 20);
 			const float c9[9] = { pb.x, pb.y, pb.z, pb.w, pc.x, pc.y, pc.z, pc.w, pd.x };
@@ -1784,20 +1821,24 @@ __device__ __forceinline__ void vol_exact_later(const ppi_dev &d, VolSmem &S, in
 	else d.rs[d.cell_rep[__float_as_int(d.sori[3 * (size_t) k + 2].z)]].error = PPI_E_EXACT;
 }
 
-/* the decision of pair (candidate jq, particle k): certified FP64, or (exact = 1) the bit-identical
- * exact_pair */
-__device__ __forceinline__ void vol_pair_decide(const ppi_dev &d, VolSmem &S, int jq, int k, int exact, Acc &A) {
+/* the decision of pair (candidate jq, particle k): certified FP64 (in the loop), or the bit-identical
+ * exact_pair (after the loop, for the pairs the certified test leaves undecided) */
+template <bool EXACT>
+__device__ __forceinline__ void vol_pair_decide(const ppi_dev &d, VolSmem &S, int jq, int k, Acc &A) {
 	const int r = d.cell_rep[__float_as_int(d.sori[3 * (size_t) k + 2].z)];
 	const ppi_grid &g = d.grid[r];
 	const int ps = __float_as_int(d.sori[3 * (size_t) k + 2].w), qs = __float_as_int(d.sori[3 * (size_t) jq + 2].w);
 	const float4 q0 = make_float4(1.f, 0.f, 0.f, 0.f);
 	const float3 d0 = make_float3(0.f, 0.f, 0.f);
 	A.fallbacks++;
-	int ex = exact ? exact_pair(d.rec, d.rp + r, d.rs[r].box, ps, 0, q0, d0, qs, g.vol_dir, g.vol_f, g.vol_side, nullptr, nullptr, nullptr)
-				   : decide64(d.rec, d.rp[r], d.rs[r].box, g.inv_L, ps, 0, q0, d0, qs, g.vol_dir, g.vol_f, g.vol_side);
-	if(ex == DEC64_EXACT) {
-		vol_exact_later(d, S, jq, k);
-		return;
+	int ex;
+	if(EXACT) ex = exact_pair(d.rec, d.rp + r, d.rs[r].box, ps, 0, q0, d0, qs, g.vol_dir, g.vol_f, g.vol_side, nullptr, nullptr, nullptr);
+	else {
+		ex = decide64(d.rec, d.rp[r], d.rs[r].box, g.inv_L, ps, 0, q0, d0, qs, g.vol_dir, g.vol_f, g.vol_side);
+		if(ex == DEC64_EXACT) {
+			vol_exact_later(d, S, jq, k);
+			return;
+		}
 	}
 	if(r != A.r) {
 		energy_flush_thread(d, A);
@@ -1824,7 +1865,7 @@ __device__ __forceinline__ void vol_lane_pairs(const ppi_dev &d, VolSmem &S, int
 			const float3 dv = vol_geo(S, a, 3 * pz + (sg >> 1), qa);
 			A.pairs++;
 			const int cl = classify(dv.x, dv.y, dv.z, cp, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, nullptr);
-			if(cl == CL_UNSURE) vol_pair_decide(d, S, jq, k, 0, A);
+			if(cl == CL_UNSURE) vol_pair_decide<false>(d, S, jq, k, A);
 			else {
 				if(r != A.r) {
 					energy_flush_thread(d, A);
@@ -1930,14 +1971,13 @@ __global__ void __launch_bounds__(32 * TILE_WARPS, PPI_TILE_MIN_BLOCKS) k_energy
 							const int a = (en[u] >> 4) & 63;
 							const float3 dv = vol_geo(S, a, en[u] & 15, qa[u]);
 							const float r2 = fmaf(dv.x, dv.x, fmaf(dv.y, dv.y, dv.z * dv.z));
-							const int r = S.rep[a];
-							const ppi_rparams &rp = d.rp[r];
-							const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
+							const float4 v = S.vs[a];
 							A.pairs++;
-							if(r2 < 1.f - eps) {
+							if(r2 < v.z) {
+								const int r = S.rep[a];
 								if(!d.rs[r].vol_overlap) atomicExch(&d.rs[r].vol_overlap, 1);
 							}
-							else close = r2 < rp.sqr_rcut_f + eps;
+							else close = r2 < v.w;
 						}
 						const unsigned m = __ballot_sync(0xffffffffu, close);
 						if(m) {
@@ -1956,12 +1996,12 @@ __global__ void __launch_bounds__(32 * TILE_WARPS, PPI_TILE_MIN_BLOCKS) k_energy
 		if(S.nc) vol_close(d, S, lane, A);
 		/* guard-band pairs: certified FP64 decisions */
 		const int nu = S.nu < EV_UCAP ? S.nu : EV_UCAP;
-		for(int u = lane; u < nu; u += 32) vol_pair_decide(d, S, S.uns[u].x, S.ki[S.uns[u].y], 0, A);
+		for(int u = lane; u < nu; u += 32) vol_pair_decide<false>(d, S, S.uns[u].x, S.ki[S.uns[u].y], A);
 		__syncwarp();
 	}
 	/* pairs within 1e-12 of a threshold (rare): the bit-identical exact_pair, after the loop */
 	const int nex = S.nex < EV_UCAP ? S.nex : EV_UCAP;
-	for(int u = lane; u < nex; u += 32) vol_pair_decide(d, S, S.exl[u].x, S.exl[u].y, 1, A);
+	for(int u = lane; u < nex; u += 32) vol_pair_decide<true>(d, S, S.exl[u].x, S.exl[u].y, A);
 	__syncwarp();
 	energy_flush_block(d, A);
 }
@@ -2032,6 +2072,9 @@ __global__ void k_vol_decide(ppi_dev d, long long sweep) {
 		g->wf[a] = (float) g->w[a];
 		g->inv_w[a] = 1.0 / g->w[a];
 		g->inv_L[a] = 1.0 / rs->box[a];
+		g->inv_wf[a] = (float) g->inv_w[a];
+		g->inv_Lf[a] = (float) g->inv_L[a];
+		g->Lf[a] = (float) rs->box[a];
 	}
 }
 
