@@ -750,7 +750,10 @@ __device__ __forceinline__ void flush_block(const ppi_dev &d, Acc &A) {
 #endif
 #define TILE_WARPS 3 /* warps per CTA of the colour kernel (shared memory: ~12 KB per warp) */
 #ifndef PPI_TILE_MIN_BLOCKS
-#define PPI_TILE_MIN_BLOCKS 6 /* resident CTAs per SM of the colour kernel */
+#define PPI_TILE_MIN_BLOCKS 5 /* resident CTAs per SM of the colour kernel (measured: 5 beats 6, 128 registers) */
+#endif
+#ifndef PPI_VOL_MIN_BLOCKS
+#define PPI_VOL_MIN_BLOCKS 6 /* resident CTAs per SM of the candidate-box energy kernel */
 #endif
 
 __device__ __forceinline__ int wrapi(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
@@ -1877,7 +1880,7 @@ __device__ __forceinline__ void vol_lane_pairs(const ppi_dev &d, VolSmem &S, int
 		}
 }
 
-__global__ void __launch_bounds__(32 * TILE_WARPS, PPI_TILE_MIN_BLOCKS) k_energy_vol(ppi_dev d) {
+__global__ void __launch_bounds__(32 * TILE_WARPS, PPI_VOL_MIN_BLOCKS) k_energy_vol(ppi_dev d) {
 	__shared__ VolSmem s_vol[TILE_WARPS];
 	VolSmem &S = s_vol[threadIdx.x >> 5];
 	const int lane = threadIdx.x & 31;
