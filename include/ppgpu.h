@@ -167,7 +167,7 @@ int pp_gpu_time_sweeps(pp_engine *e, long long n, double *ms);
  * FP32 pair tests with the FP64 guard band (eps = 1e-5), bit-identical decisions to the reference.
  *
  * Nothing is allocated: all scratch (cell grid, sort buffers, working records) lives in one static
- * device array of about 8.8 MB, which every GPU that loads the library holds until the process exits.
+ * device array of about 11.2 MiB, which every GPU that loads the library holds until the process exits.
  * Limits: N <= 32768 particles and at most 131072 cells (even cell count >= 4 per axis, cell edge >=
  * 1 + KF_delta, i.e. roughly a 57^3 box at delta = 0.12); larger inputs return PP_ERR_CAPACITY with a
  * message in err (err may be NULL). The first call on a device looks up the array's device address with
