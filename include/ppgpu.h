@@ -178,6 +178,25 @@ int pp_gpu_time_sweeps(pp_engine *e, long long n, double *ms);
 int pp_gpu_energy_noalloc(int N, const double *r_dev, const double *R_dev, const double box[3], double kf_delta, double kf_cosmax,
 		int *n_bonds_dev, int *n_overlaps_dev, double *E, int *overlap, char *err, int err_len);
 
+/* ------------------------------------------------------------------ learned proposal: the network */
+/* Per-particle MLP 36 -> 64 -> 64 -> 4 (ReLU), BF16 operands on the tensor cores, FP32 accumulation.
+ * No counterpart in the reference: the spec addition whose plain fallback is MC_move_rototranslate.
+ * Parameters are FP32, laid out W1[64][36] b1[64] W2[64][64] b2[64] W3[4][64] b3[4] (PP_MLP_NPARAMS). */
+#define PP_MLP_IN 36
+#define PP_MLP_HIDDEN 64
+#define PP_MLP_OUT 4
+#define PP_MLP_NPARAMS 6788
+#define PP_MLP_SAMPLE 40 /* floats per training sample: 36 features + 4 component utilities */
+
+/* z[n][4] = network(x[n][36]) on the current device (host arrays; allocates device scratch). */
+int pp_mlp_forward(const float *params, int n, const float *x, float *z);
+
+/* Gradient of L = -(1/n) sum_s J_s over n training samples (samples[n][40]: features, utilities u_k),
+ * J = sum_k pi_k u_k + tau H(softmax z), pi = (1 - floor) softmax(z) + floor e_0, into grad[PP_MLP_NPARAMS]
+ * (same layout as params); *objective (may be NULL) receives the mean J. tiles_per_cta: 128-sample tiles
+ * each CTA accumulates in tensor memory before its atomics (the engine's training uses the same kernel). */
+int pp_mlp_grad(const float *params, int n, const float *samples, double floor, double tau, int tiles_per_cta, float *grad, double *objective);
+
 /* Number of replicas, particles of a replica, current box of a replica. */
 int pp_gpu_num_replicas(const pp_engine *e);
 int pp_gpu_num_particles(const pp_engine *e, int replica);

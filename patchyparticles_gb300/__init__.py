@@ -93,7 +93,7 @@ EXPORTED = [
     "pp_gpu_bond_lists", "pp_gpu_guard_stats", "pp_gpu_num_replicas", "pp_gpu_num_particles", "pp_gpu_box",
     "pp_gpu_launch_count", "pp_gpu_last_error", "pp_gpu_destroy", "pp_rrr_header", "pp_rrr_read", "pp_rrr_write",
     "pp_generate", "pp_gpu_select_device", "pp_gpu_set_timing", "pp_gpu_kernel_stats", "pp_gpu_time_sweeps",
-    "pp_gpu_energy_noalloc",
+    "pp_gpu_energy_noalloc", "pp_mlp_forward", "pp_mlp_grad",
 ]
 
 
@@ -108,6 +108,7 @@ def load_library(path=None):
     lib = ctypes.CDLL(p)
     dp = ctypes.POINTER(ctypes.c_double)
     ip = ctypes.POINTER(ctypes.c_int)
+    fp = ctypes.POINTER(ctypes.c_float)
     vp = ctypes.c_void_p
     sig = {
         "pp_default_params": (None, [ctypes.POINTER(PPParams)]),
@@ -141,6 +142,8 @@ def load_library(path=None):
         "pp_gpu_set_timing": (ctypes.c_int, [vp, ctypes.c_int]),
         "pp_gpu_kernel_stats": (ctypes.c_int, [vp, ctypes.POINTER(PPKernelStats), ctypes.c_int]),
         "pp_gpu_time_sweeps": (ctypes.c_int, [vp, ctypes.c_longlong, dp]),
+        "pp_mlp_forward": (ctypes.c_int, [fp, ctypes.c_int, fp, fp]),
+        "pp_mlp_grad": (ctypes.c_int, [fp, ctypes.c_int, fp, ctypes.c_double, ctypes.c_double, ctypes.c_int, fp, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -157,6 +160,10 @@ def _dp(a):
 
 def _ip(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+def _fp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
 
 
 def default_params(**kw):
@@ -345,3 +352,36 @@ def generate(N, density, seed, round_like_file=True):
     if rc != PP_OK:
         raise PPError(rc, "generation failed (density must be in (0, 0.7])")
     return r, R, b
+
+
+# ---------------------------------------------------------------- learned proposal: the network
+MLP_IN = 36
+MLP_HIDDEN = 64
+MLP_OUT = 4
+MLP_NPARAMS = 6788
+MLP_SAMPLE = 40
+
+
+def mlp_forward(params, x):
+    """Logits z[n][4] of the per-particle network on the tensor cores (x: n x 36 FP32)."""
+    lib = load_library()
+    P = np.ascontiguousarray(params, dtype=np.float32).reshape(MLP_NPARAMS)
+    x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, MLP_IN)
+    z = np.zeros((x.shape[0], MLP_OUT), dtype=np.float32)
+    rc = lib.pp_mlp_forward(_fp(P), x.shape[0], _fp(x), _fp(z))
+    if rc != PP_OK:
+        raise PPError(rc, "pp_mlp_forward failed")
+    return z
+
+
+def mlp_grad(params, samples, floor=0.1, tau=0.01, tiles_per_cta=1):
+    """(gradient[6788], mean objective) of one training batch (samples: n x 40) on the tensor cores."""
+    lib = load_library()
+    P = np.ascontiguousarray(params, dtype=np.float32).reshape(MLP_NPARAMS)
+    S = np.ascontiguousarray(samples, dtype=np.float32).reshape(-1, MLP_SAMPLE)
+    g = np.zeros(MLP_NPARAMS, dtype=np.float32)
+    obj = ctypes.c_double()
+    rc = lib.pp_mlp_grad(_fp(P), S.shape[0], _fp(S), floor, tau, tiles_per_cta, _fp(g), ctypes.byref(obj))
+    if rc != PP_OK:
+        raise PPError(rc, "pp_mlp_grad failed")
+    return g, obj.value

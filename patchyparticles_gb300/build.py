@@ -50,9 +50,9 @@ def build(force=False, verbose=False):
     if not os.path.exists(nvcc):
         nvcc = "nvcc"
     inc = ["-I", INCLUDE, "-I", CSRC, "-I", os.path.join(cuda, "include")]
-    headers = [os.path.join(CSRC, "ppgpu_internal.h"), os.path.join(INCLUDE, "ppgpu.h")]
+    headers = [os.path.join(CSRC, "ppgpu_internal.h"), os.path.join(CSRC, "ppgpu_umma.cuh"), os.path.join(INCLUDE, "ppgpu.h")]
     units = []
-    cu_srcs = ["ppgpu_kernels.cu"]
+    cu_srcs = ["ppgpu_kernels.cu", "ppgpu_mlp.cu"]
     c_srcs = ["ppgpu_host.c"]
     cmds = []
     objs = []
