@@ -197,6 +197,61 @@ int pp_mlp_forward(const float *params, int n, const float *x, float *z);
  * each CTA accumulates in tensor memory before its atomics (the engine's training uses the same kernel). */
 int pp_mlp_grad(const float *params, int n, const float *samples, double floor, double tau, int tiles_per_cta, float *grad, double *objective);
 
+/* ------------------------------------------------------------------ learned proposal: the engine */
+/* With the learned proposal on, every attempt of pp_gpu_sweeps draws its move from a four-component
+ * mixture: component k displaces uniformly in a cube of edge scale_disp[k] * Disp_max and rotates by an
+ * angle uniform below scale_theta[k] * Theta_max (capped below pi) about a uniform axis; component 0 is
+ * the plain move (scales 1). The weights are pi = (1 - floor) softmax(network(features)) + floor e_0,
+ * where the features are up to 12 neighbour patch sites (3 nearest neighbours within 1 + KF_delta, 4
+ * patches each, centre + 0.5 patch direction) in the particle's frame, zero-padded. Acceptance is
+ * Metropolis-Hastings with the reverse-move density, so the Boltzmann distribution is kept exactly.
+ * The network is trained on the GPU (pp_gpu_learned_train) on samples of configurations generated by
+ * the plain move (pp_gpu_learned_collect); per sample and component the utility is the mean over
+ * `draws` proposals of acc (|d|^2 / Disp_max^2 + angle^2 / Theta_max^2 + kappa |bond change|). */
+#define PP_PROPOSAL_PLAIN 0
+#define PP_PROPOSAL_LEARNED 1
+#define PP_MIX 4
+
+typedef struct pp_learned_params {
+	double scale_disp[PP_MIX];  /* cube edge of component k in units of Disp_max (scale_disp[0] = 1) */
+	double scale_theta[PP_MIX]; /* maximum angle of component k in units of Theta_max (scale_theta[0] = 1) */
+	double floor;               /* weight of the plain component always mixed in, (0, 1] */
+	double entropy;             /* training: entropy bonus tau of the objective (>= 0) */
+	double kappa;               /* training: weight of the bond-count change in the utility (>= 0) */
+	int draws;                  /* training: proposals per component and sample, [1, 64] */
+	uint64_t seed;              /* initial weights and the training order */
+} pp_learned_params;
+
+void pp_default_learned_params(pp_learned_params *p);
+
+/* Allocates the network (seeded initial weights: uniform fan-in hidden layers, zero output layer, i.e.
+ * the uniform mixture) and the training state; may be called again to reset. */
+int pp_gpu_learned_init(pp_engine *e, const pp_learned_params *p);
+int pp_gpu_learned_set_weights(pp_engine *e, const float *params); /* PP_MLP_NPARAMS floats */
+int pp_gpu_learned_get_weights(pp_engine *e, float *params);
+
+/* PP_PROPOSAL_PLAIN (default) or PP_PROPOSAL_LEARNED (needs pp_gpu_learned_init) for the following sweeps. */
+int pp_gpu_set_proposal(pp_engine *e, int proposal);
+
+/* n_configs times: sweeps_between sweeps with the plain move, then samples_per_config training samples of
+ * the current configuration appended to the engine's sample buffer (one checkerboard colour's attempts,
+ * spread over its list). */
+int pp_gpu_learned_collect(pp_engine *e, int n_configs, int sweeps_between, int samples_per_config);
+
+/* epochs passes over the sample buffer in shuffled 128-sample tiles, one Adam step (learning rate lr)
+ * per batch of tiles_per_cta x (SMs) tiles; *objective (may be NULL) = mean J over the last epoch. */
+int pp_gpu_learned_train(pp_engine *e, int epochs, int tiles_per_cta, double lr, double *objective);
+
+/* Number of samples in the buffer; if out is not NULL, copies them (count x PP_MLP_SAMPLE floats). */
+int pp_gpu_learned_samples(pp_engine *e, long long *count, float *out);
+int pp_gpu_learned_clear_samples(pp_engine *e);
+
+/* The 36 features of every particle of a replica in the current state (N x 36, particle order). */
+int pp_gpu_learned_features(pp_engine *e, int replica, float *features);
+
+/* Attempts and acceptances of learned moves per mixture component since the last reset (all replicas). */
+int pp_gpu_learned_stats(pp_engine *e, long long tries[PP_MIX], long long accepted[PP_MIX], int reset);
+
 /* Number of replicas, particles of a replica, current box of a replica. */
 int pp_gpu_num_replicas(const pp_engine *e);
 int pp_gpu_num_particles(const pp_engine *e, int replica);

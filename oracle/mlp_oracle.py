@@ -161,3 +161,67 @@ def random_samples(n, seed=0):
     X[rng.random((n, IN)) < 0.3] = 0.0  # zero padding of absent neighbours
     U = rng.uniform(0, 3, (n, OUT)).astype(np.float32)
     return np.concatenate([X, U], axis=1)
+
+
+# ---------------------------------------------------------------- features of the learned proposal
+def base_patches():
+    """The four tetrahedral patch directions as the reference builds them (system.c:20-31): +-0.5/sqrt(3)
+    components, each vector then normalised."""
+    h = 0.5 / np.sqrt(3.0)
+    v = np.array([[-h, -h, h], [h, -h, -h], [h, h, h], [-h, h, -h]], dtype=np.float64)
+    for i in range(4):
+        n = np.sqrt((v[i, 0] * v[i, 0] + v[i, 1] * v[i, 1]) + v[i, 2] * v[i, 2])
+        v[i] = v[i] / n
+    return v
+
+
+def canonical_image(r, R, box):
+    """FP32 image of the canonical state: positions wrapped into [0, L) (x - floor(x / L) L), orientation
+    rows; both rounded to FP32."""
+    r = np.asarray(r, dtype=np.float64).reshape(-1, 3)
+    box = np.asarray(box, dtype=np.float64)
+    k = np.floor(r / box)
+    y = r - k * box
+    return y.astype(np.float32), np.asarray(R, dtype=np.float64).reshape(-1, 3, 3).astype(np.float32)
+
+
+def features(r, R, box, kf_delta, nb=3):
+    """features[N][36] of every particle: patch sites (centre + 0.5 patch direction) of its `nb` nearest
+    neighbours within (1 + delta) sqrt(1 - 1e-4), nearest first (ties by index), minimum image, in the
+    particle's frame (R^T . site), zero-padded. FP32 arithmetic operation by operation, as the engine."""
+    pos, Rf = canonical_image(r, R, box)
+    N = pos.shape[0]
+    L = np.asarray(box, dtype=np.float64).astype(np.float32)
+    iL = np.float32(1.0) / L
+    rf2 = np.float32(np.float32((1.0 + kf_delta) * (1.0 + kf_delta)) * np.float32(0.9999))
+    b32 = base_patches().astype(np.float32)
+    half = np.float32(0.5)
+    out = np.zeros((N, 12 * nb), dtype=np.float32)
+    for i in range(N):
+        v = pos - pos[i]
+        v = v - L * np.rint(v * iL)
+        r2 = (v[:, 0] * v[:, 0] + v[:, 1] * v[:, 1]) + v[:, 2] * v[:, 2]
+        r2[i] = np.float32(np.inf)
+        cand = np.nonzero(r2 < rf2)[0]
+        if cand.size == 0:
+            continue
+        order = cand[np.lexsort((cand, r2[cand]))][:nb]
+        Ri = Rf[i]
+        for n, j in enumerate(order):
+            dl = v[j]
+            Rj = Rf[j]
+            for m in range(4):
+                p = (Rj[:, 0] * b32[m, 0] + Rj[:, 1] * b32[m, 1]) + Rj[:, 2] * b32[m, 2]
+                site = dl + half * p
+                f = (Ri[0, :] * site[0] + Ri[1, :] * site[1]) + Ri[2, :] * site[2]
+                out[i, 12 * n + 3 * m:12 * n + 3 * m + 3] = f
+    return out
+
+
+def mixture_density_ratio(pi_new, pi_old, scale_disp, scale_theta, disp_max, theta_max, d, theta):
+    """q(x' -> x) / q(x -> x') of one move (displacement d, angle theta) under the four-component mixture."""
+    a = np.array([disp_max * s for s in scale_disp])
+    t = np.minimum(np.array([theta_max * s for s in scale_theta]), np.pi)
+    m = np.max(np.abs(d))
+    c = np.where((m <= a / 2) & (theta < t), 1.0 / (a ** 3 * t), 0.0)
+    return float(np.dot(pi_new, c) / np.dot(pi_old, c))

@@ -76,6 +76,22 @@ class PPKernelStats(ctypes.Structure):
     ]
 
 
+class PPLearnedParams(ctypes.Structure):
+    _fields_ = [
+        ("scale_disp", ctypes.c_double * 4),
+        ("scale_theta", ctypes.c_double * 4),
+        ("floor", ctypes.c_double),
+        ("entropy", ctypes.c_double),
+        ("kappa", ctypes.c_double),
+        ("draws", ctypes.c_int),
+        ("seed", ctypes.c_uint64),
+    ]
+
+
+PROPOSAL_PLAIN = 0
+PROPOSAL_LEARNED = 1
+
+
 class PPError(RuntimeError):
     def __init__(self, code, message):
         super().__init__(f"ppgpu error {code}: {message}")
@@ -93,7 +109,10 @@ EXPORTED = [
     "pp_gpu_bond_lists", "pp_gpu_guard_stats", "pp_gpu_num_replicas", "pp_gpu_num_particles", "pp_gpu_box",
     "pp_gpu_launch_count", "pp_gpu_last_error", "pp_gpu_destroy", "pp_rrr_header", "pp_rrr_read", "pp_rrr_write",
     "pp_generate", "pp_gpu_select_device", "pp_gpu_set_timing", "pp_gpu_kernel_stats", "pp_gpu_time_sweeps",
-    "pp_gpu_energy_noalloc", "pp_mlp_forward", "pp_mlp_grad",
+    "pp_gpu_energy_noalloc", "pp_mlp_forward", "pp_mlp_grad", "pp_default_learned_params", "pp_gpu_learned_init",
+    "pp_gpu_learned_set_weights", "pp_gpu_learned_get_weights", "pp_gpu_set_proposal", "pp_gpu_learned_collect",
+    "pp_gpu_learned_train", "pp_gpu_learned_samples", "pp_gpu_learned_clear_samples", "pp_gpu_learned_features",
+    "pp_gpu_learned_stats",
 ]
 
 
@@ -143,6 +162,17 @@ def load_library(path=None):
         "pp_gpu_kernel_stats": (ctypes.c_int, [vp, ctypes.POINTER(PPKernelStats), ctypes.c_int]),
         "pp_gpu_time_sweeps": (ctypes.c_int, [vp, ctypes.c_longlong, dp]),
         "pp_mlp_forward": (ctypes.c_int, [fp, ctypes.c_int, fp, fp]),
+        "pp_default_learned_params": (None, [ctypes.POINTER(PPLearnedParams)]),
+        "pp_gpu_learned_init": (ctypes.c_int, [vp, ctypes.POINTER(PPLearnedParams)]),
+        "pp_gpu_learned_set_weights": (ctypes.c_int, [vp, fp]),
+        "pp_gpu_learned_get_weights": (ctypes.c_int, [vp, fp]),
+        "pp_gpu_set_proposal": (ctypes.c_int, [vp, ctypes.c_int]),
+        "pp_gpu_learned_collect": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+        "pp_gpu_learned_train": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, dp]),
+        "pp_gpu_learned_samples": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_longlong), fp]),
+        "pp_gpu_learned_clear_samples": (ctypes.c_int, [vp]),
+        "pp_gpu_learned_features": (ctypes.c_int, [vp, ctypes.c_int, fp]),
+        "pp_gpu_learned_stats": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
         "pp_mlp_grad": (ctypes.c_int, [fp, ctypes.c_int, fp, ctypes.c_double, ctypes.c_double, ctypes.c_int, fp, dp]),
     }
     for name, (res, args) in sig.items():
@@ -299,6 +329,69 @@ class Engine:
         ms = ctypes.c_double()
         self._check(self.lib.pp_gpu_time_sweeps(self.h, n, ctypes.byref(ms)))
         return ms.value
+
+    # ---------------------------------------------------------------- learned proposal
+    def learned_init(self, **kw):
+        p = default_learned_params(**kw)
+        self._check(self.lib.pp_gpu_learned_init(self.h, ctypes.byref(p)))
+
+    def set_proposal(self, learned):
+        self._check(self.lib.pp_gpu_set_proposal(self.h, PROPOSAL_LEARNED if learned else PROPOSAL_PLAIN))
+
+    def learned_weights(self):
+        P = np.zeros(MLP_NPARAMS, dtype=np.float32)
+        self._check(self.lib.pp_gpu_learned_get_weights(self.h, _fp(P)))
+        return P
+
+    def set_learned_weights(self, P):
+        P = np.ascontiguousarray(P, dtype=np.float32).reshape(MLP_NPARAMS)
+        self._check(self.lib.pp_gpu_learned_set_weights(self.h, _fp(P)))
+
+    def learned_collect(self, n_configs, sweeps_between, samples_per_config):
+        self._check(self.lib.pp_gpu_learned_collect(self.h, n_configs, sweeps_between, samples_per_config))
+
+    def learned_train(self, epochs, lr=3e-3, tiles_per_cta=2):
+        obj = ctypes.c_double()
+        self._check(self.lib.pp_gpu_learned_train(self.h, epochs, tiles_per_cta, lr, ctypes.byref(obj)))
+        return obj.value
+
+    def learned_samples(self):
+        n = ctypes.c_longlong()
+        self._check(self.lib.pp_gpu_learned_samples(self.h, ctypes.byref(n), None))
+        out = np.zeros((n.value, MLP_SAMPLE), dtype=np.float32)
+        if n.value:
+            self._check(self.lib.pp_gpu_learned_samples(self.h, ctypes.byref(n), _fp(out)))
+        return out
+
+    def learned_clear_samples(self):
+        self._check(self.lib.pp_gpu_learned_clear_samples(self.h))
+
+    def learned_features(self, replica=0):
+        N = self.num_particles(replica)
+        f = np.zeros((N, MLP_IN), dtype=np.float32)
+        self._check(self.lib.pp_gpu_learned_features(self.h, replica, _fp(f)))
+        return f
+
+    def learned_stats(self, reset=False):
+        t = (ctypes.c_longlong * 4)()
+        a = (ctypes.c_longlong * 4)()
+        self._check(self.lib.pp_gpu_learned_stats(self.h, t, a, 1 if reset else 0))
+        return list(t), list(a)
+
+
+def default_learned_params(**kw):
+    lib = load_library()
+    p = PPLearnedParams()
+    lib.pp_default_learned_params(ctypes.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise KeyError(k)
+        if k in ("scale_disp", "scale_theta"):
+            for i, x in enumerate(v):
+                getattr(p, k)[i] = x
+        else:
+            setattr(p, k, v)
+    return p
 
 
 def select_device(dev):

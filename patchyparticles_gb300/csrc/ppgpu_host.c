@@ -50,6 +50,22 @@ struct pp_engine {
 	int *ev_kind;      /* 0 sort, 1 sweep, 2 volume */
 	int ev_cap;
 	pp_kernel_stats kstats;
+	/* learned proposal */
+	int learn_ready;              /* network buffers allocated (pp_gpu_learned_init) */
+	int proposal;                 /* PP_PROPOSAL_PLAIN or PP_PROPOSAL_LEARNED */
+	pp_learned_params lprm;
+	ppi_learn h_learn;
+	float *l_P, *l_m1, *l_m2, *l_grad; /* FP32 master weights, Adam moments, gradient (device) */
+	unsigned char *l_img;         /* packed BF16 operands (device) */
+	ppi_learn *l_learn;
+	unsigned long long *l_stats;
+	int *l_err;
+	double *l_obj;
+	int *l_tiles;
+	int l_tiles_cap;
+	long long n_samples;
+	int adam_step;
+	long long collect_snap;
 	/* pinned staging */
 	double *pin_rec;
 	int *pin_id;
@@ -214,12 +230,34 @@ static void free_device(pp_engine *e) {
 	e->pin_rec = NULL;
 	e->pin_id = e->pin_i1 = e->pin_i2 = NULL;
 	e->pin_n = 0;
+	/* layout-sized buffers of the learned proposal */
+	if(e->d.wimg) cudaFree(e->d.wimg);
+	if(e->d.feat) cudaFree(e->d.feat);
+	e->d.wimg = NULL;
+	e->d.feat = NULL;
+}
+
+static void free_learned(pp_engine *e) {
+	void *ptrs[] = { e->l_P, e->l_m1, e->l_m2, e->l_grad, e->l_img, e->l_learn, e->l_stats, e->l_err, e->l_obj, e->l_tiles, e->d.samples };
+	for(size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); i++)
+		if(ptrs[i]) cudaFree(ptrs[i]);
+	e->l_P = e->l_m1 = e->l_m2 = e->l_grad = NULL;
+	e->l_img = NULL;
+	e->l_learn = NULL;
+	e->l_stats = NULL;
+	e->l_err = NULL;
+	e->l_obj = NULL;
+	e->l_tiles = NULL;
+	e->d.samples = NULL;
+	e->d.sample_cap = 0;
+	e->learn_ready = 0;
 }
 
 void pp_gpu_destroy(pp_engine *e) {
 	if(e == NULL) return;
 	if(e->stream) cudaStreamSynchronize(e->stream);
 	free_device(e);
+	free_learned(e);
 	if(e->stream) cudaStreamDestroy(e->stream);
 	for(int i = 0; i < e->nrep; i++) {
 		free(e->h_r[i]);
@@ -330,7 +368,10 @@ static int ensure_pinned(pp_engine *e, size_t n) {
 
 static int read_states(pp_engine *e) {
 	CU(cudaMemcpyAsync(e->h_rs, e->d.rs, sizeof(ppi_rstate) * e->nrep, cudaMemcpyDeviceToHost, e->stream));
+	int lerr = 0;
+	if(e->learn_ready) CU(cudaMemcpyAsync(&lerr, e->l_err, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
 	CU(cudaStreamSynchronize(e->stream));
+	if(lerr) return set_err(e, PP_ERR_CUDA, "a tensor-core wait of the learned proposal timed out");
 	for(int r = 0; r < e->nrep; r++)
 		if(e->h_rs[r].error == PPI_E_EXACT)
 			return set_err(e, PP_ERR_STATE, "replica %d: more pairs within 1e-12 of a bonding threshold than one warp keeps for the exact test", r);
@@ -352,6 +393,7 @@ static int do_resort(pp_engine *e) {
 		CK(ppi_reorder(&e->d, e->stream, &nl));
 	}
 	CK(ppi_resort(&e->d, e->epoch, e->stream, &nl));
+	if(e->proposal == PP_PROPOSAL_LEARNED && e->d.wimg) CK(ppi_canon(&e->d, e->stream, &nl));
 	e->launches += nl;
 	e->epoch++;
 	return PP_OK;
@@ -675,7 +717,8 @@ int pp_gpu_sweeps(pp_engine *e, long long n) {
 			int colours[8];
 			colour_order(e->round_counter, colours);
 			if((rc = ev_begin(e, 1, &ev)) != PP_OK) return rc;
-			CK(ppi_round(&e->d, e->round_counter, colours, e->any_audit, e->stream, &nl));
+			if(e->proposal == PP_PROPOSAL_LEARNED) CK(ppi_round_learned(&e->d, e->round_counter, colours, e->any_audit, e->stream, &nl));
+			else CK(ppi_round(&e->d, e->round_counter, colours, e->any_audit, e->stream, &nl));
 			if((rc = ev_end(e, ev)) != PP_OK) return rc;
 			e->round_counter++;
 			e->launches += nl;
@@ -684,6 +727,7 @@ int pp_gpu_sweeps(pp_engine *e, long long n) {
 			long long nl = 0;
 			if((rc = ev_begin(e, 2, &ev)) != PP_OK) return rc;
 			CK(ppi_volume(&e->d, s, e->stream, &nl));
+			if(e->proposal == PP_PROPOSAL_LEARNED) CK(ppi_canon(&e->d, e->stream, &nl)); /* positions and box may have changed */
 			if((rc = ev_end(e, ev)) != PP_OK) return rc;
 			e->launches += nl;
 		}
@@ -1169,5 +1213,315 @@ int pp_generate(int N, double density, int seed, int round_like_file, double *r,
 			h_gram_schmidt(Ri, Ri + 3, Ri + 6);
 		}
 	}
+	return PP_OK;
+}
+
+/* ------------------------------------------------------------------------------------------------ */
+/* learned proposal                                                                                 */
+/* ------------------------------------------------------------------------------------------------ */
+void pp_default_learned_params(pp_learned_params *p) {
+	memset(p, 0, sizeof(*p));
+	const double sd[PP_MIX] = { 1., 3., 8., 2. }, st[PP_MIX] = { 1., 3., 8., 25. };
+	for(int k = 0; k < PP_MIX; k++) {
+		p->scale_disp[k] = sd[k];
+		p->scale_theta[k] = st[k];
+	}
+	p->floor = 0.1;
+	p->entropy = 0.01;
+	p->kappa = 100.;
+	p->draws = 2;
+	p->seed = 12345;
+}
+
+static uint64_t splitmix64(uint64_t *s) {
+	uint64_t z = (*s += 0x9E3779B97F4A7C15ULL);
+	z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+	z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+	return z ^ (z >> 31);
+}
+
+static double u01_sm(uint64_t *s) { return (double) (splitmix64(s) >> 11) * 0x1p-53; }
+
+/* layout-sized buffers (canonical images, features); valid after the layout exists */
+static int ensure_learn_layout(pp_engine *e) {
+	if(!e->committed) return set_err(e, PP_ERR_STATE, "no configuration uploaded for every replica");
+	size_t n1 = e->d.ntot > 0 ? (size_t) e->d.ntot : 1;
+	if(!e->d.wimg) CU(cudaMalloc((void **) &e->d.wimg, sizeof(float) * 12 * n1));
+	if(!e->d.feat) CU(cudaMalloc((void **) &e->d.feat, sizeof(float) * PP_MLP_IN * n1));
+	return PP_OK;
+}
+
+static int learn_check(pp_engine *e) {
+	if(e == NULL) return PP_ERR_ARG;
+	if(!e->learn_ready) return set_err(e, PP_ERR_STATE, "learned proposal not initialised (pp_gpu_learned_init)");
+	return PP_OK;
+}
+
+int pp_gpu_learned_init(pp_engine *e, const pp_learned_params *p) {
+	if(e == NULL || p == NULL) return PP_ERR_ARG;
+	if(p->scale_disp[0] != 1. || p->scale_theta[0] != 1.) return set_err(e, PP_ERR_ARG, "component 0 is the plain move: its scales must be 1");
+	for(int k = 0; k < PP_MIX; k++)
+		if(!(p->scale_disp[k] > 0.) || !(p->scale_theta[k] > 0.) || p->scale_disp[k] > 1e3 || p->scale_theta[k] > 1e3)
+			return set_err(e, PP_ERR_ARG, "component scales must lie in (0, 1000]");
+	if(!(p->floor > 0. && p->floor <= 1.)) return set_err(e, PP_ERR_ARG, "floor must lie in (0, 1]");
+	if(!(p->entropy >= 0.) || !(p->kappa >= 0.)) return set_err(e, PP_ERR_ARG, "entropy and kappa must be >= 0");
+	if(p->draws < 1 || p->draws > 64) return set_err(e, PP_ERR_ARG, "draws must lie in [1, 64]");
+	e->lprm = *p;
+	for(int k = 0; k < PP_MIX; k++) {
+		e->h_learn.sdisp[k] = (float) p->scale_disp[k];
+		e->h_learn.stheta[k] = (float) p->scale_theta[k];
+	}
+	e->h_learn.floor0 = (float) p->floor;
+	e->h_learn.kappa = (float) p->kappa;
+	e->h_learn.draws = p->draws;
+	if(!e->learn_ready) {
+		CU(cudaMalloc((void **) &e->l_P, sizeof(float) * PP_MLP_NPARAMS));
+		CU(cudaMalloc((void **) &e->l_m1, sizeof(float) * PP_MLP_NPARAMS));
+		CU(cudaMalloc((void **) &e->l_m2, sizeof(float) * PP_MLP_NPARAMS));
+		CU(cudaMalloc((void **) &e->l_grad, sizeof(float) * PP_MLP_NPARAMS));
+		CU(cudaMalloc((void **) &e->l_img, 32768));
+		CU(cudaMalloc((void **) &e->l_learn, sizeof(ppi_learn)));
+		CU(cudaMalloc((void **) &e->l_stats, sizeof(unsigned long long) * 2 * PP_MIX));
+		CU(cudaMalloc((void **) &e->l_err, sizeof(int)));
+		CU(cudaMalloc((void **) &e->l_obj, sizeof(double)));
+		e->learn_ready = 1;
+	}
+	e->d.mlp_img = e->l_img;
+	e->d.learn = e->l_learn;
+	e->d.lstats = e->l_stats;
+	e->d.lerr = e->l_err;
+	CU(cudaMemcpyAsync(e->l_learn, &e->h_learn, sizeof(ppi_learn), cudaMemcpyHostToDevice, e->stream));
+	CU(cudaMemsetAsync(e->l_stats, 0, sizeof(unsigned long long) * 2 * PP_MIX, e->stream));
+	CU(cudaMemsetAsync(e->l_err, 0, sizeof(int), e->stream));
+	/* initial weights: uniform fan-in hidden layers, zero biases and output layer (uniform mixture) */
+	float *P = calloc(PP_MLP_NPARAMS, sizeof(float));
+	if(!P) return set_err(e, PP_ERR_ARG, "out of host memory");
+	uint64_t st = p->seed;
+	const double a1 = sqrt(6.0 / PP_MLP_IN), a2 = sqrt(6.0 / PP_MLP_HIDDEN);
+	for(int i = 0; i < PP_MLP_HIDDEN * PP_MLP_IN; i++) P[i] = (float) ((2. * u01_sm(&st) - 1.) * a1);
+	const int w2 = PP_MLP_HIDDEN * PP_MLP_IN + PP_MLP_HIDDEN;
+	for(int i = 0; i < PP_MLP_HIDDEN * PP_MLP_HIDDEN; i++) P[w2 + i] = (float) ((2. * u01_sm(&st) - 1.) * a2);
+	int rc = pp_gpu_learned_set_weights(e, P);
+	free(P);
+	return rc;
+}
+
+int pp_gpu_learned_set_weights(pp_engine *e, const float *params) {
+	int rc = learn_check(e);
+	if(rc != PP_OK) return rc;
+	if(params == NULL) return set_err(e, PP_ERR_ARG, "null weights");
+	for(int i = 0; i < PP_MLP_NPARAMS; i++)
+		if(!isfinite(params[i])) return set_err(e, PP_ERR_ARG, "weight %d is not finite", i);
+	CU(cudaMemcpyAsync(e->l_P, params, sizeof(float) * PP_MLP_NPARAMS, cudaMemcpyHostToDevice, e->stream));
+	CU(cudaMemsetAsync(e->l_m1, 0, sizeof(float) * PP_MLP_NPARAMS, e->stream));
+	CU(cudaMemsetAsync(e->l_m2, 0, sizeof(float) * PP_MLP_NPARAMS, e->stream));
+	CU(cudaMemsetAsync(e->l_grad, 0, sizeof(float) * PP_MLP_NPARAMS, e->stream));
+	e->adam_step = 0;
+	CK(ppi_mlp_pack(e->l_P, e->l_img, e->stream));
+	e->launches++;
+	CU(cudaStreamSynchronize(e->stream));
+	return PP_OK;
+}
+
+int pp_gpu_learned_get_weights(pp_engine *e, float *params) {
+	int rc = learn_check(e);
+	if(rc != PP_OK) return rc;
+	if(params == NULL) return set_err(e, PP_ERR_ARG, "null weights");
+	CU(cudaMemcpyAsync(params, e->l_P, sizeof(float) * PP_MLP_NPARAMS, cudaMemcpyDeviceToHost, e->stream));
+	CU(cudaStreamSynchronize(e->stream));
+	return PP_OK;
+}
+
+int pp_gpu_set_proposal(pp_engine *e, int proposal) {
+	int rc = ready(e);
+	if(rc != PP_OK) return rc;
+	if(proposal == PP_PROPOSAL_PLAIN) {
+		e->proposal = proposal;
+		return PP_OK;
+	}
+	if(proposal != PP_PROPOSAL_LEARNED) return set_err(e, PP_ERR_ARG, "unknown proposal %d", proposal);
+	rc = learn_check(e);
+	if(rc != PP_OK) return rc;
+	rc = ensure_learn_layout(e);
+	if(rc != PP_OK) return rc;
+	long long nl = 0;
+	CK(ppi_canon(&e->d, e->stream, &nl));
+	e->launches += nl;
+	e->proposal = proposal;
+	return PP_OK;
+}
+
+/* grows the device sample buffer to hold at least n samples (existing samples kept) */
+static int ensure_samples(pp_engine *e, long long n) {
+	if(n <= e->d.sample_cap) return PP_OK;
+	if(n > (1LL << 30)) return set_err(e, PP_ERR_CAPACITY, "too many training samples");
+	long long cap = e->d.sample_cap > 0 ? 2LL * e->d.sample_cap : 1024;
+	while(cap < n) cap *= 2;
+	float *buf = NULL;
+	CU(cudaMalloc((void **) &buf, sizeof(float) * PP_MLP_SAMPLE * (size_t) cap));
+	if(e->n_samples > 0) CU(cudaMemcpyAsync(buf, e->d.samples, sizeof(float) * PP_MLP_SAMPLE * (size_t) e->n_samples, cudaMemcpyDeviceToDevice, e->stream));
+	CU(cudaStreamSynchronize(e->stream));
+	if(e->d.samples) cudaFree(e->d.samples);
+	e->d.samples = buf;
+	e->d.sample_cap = (int) cap;
+	return PP_OK;
+}
+
+int pp_gpu_learned_collect(pp_engine *e, int n_configs, int sweeps_between, int samples_per_config) {
+	int rc = ready(e);
+	if(rc != PP_OK) return rc;
+	rc = learn_check(e);
+	if(rc != PP_OK) return rc;
+	if(n_configs < 0 || sweeps_between < 0 || samples_per_config < 1) return set_err(e, PP_ERR_ARG, "bad collection arguments");
+	rc = ensure_learn_layout(e);
+	if(rc != PP_OK) return rc;
+	rc = ensure_samples(e, e->n_samples + (long long) n_configs * samples_per_config);
+	if(rc != PP_OK) return rc;
+	const int saved = e->proposal;
+	e->proposal = PP_PROPOSAL_PLAIN; /* the training configurations come from the plain move */
+	for(int c = 0; c < n_configs; c++) {
+		rc = pp_gpu_sweeps(e, sweeps_between);
+		if(rc != PP_OK) break;
+		long long nl = 0;
+		int order[8];
+		colour_order(e->collect_snap, order);
+		if((rc = ppi_canon(&e->d, e->stream, &nl)) != 0 ||
+				(rc = ppi_learn_collect(&e->d, e->collect_snap, order[0], (int) e->n_samples, samples_per_config, e->stream, &nl)) != 0) {
+			rc = set_err(e, PP_ERR_CUDA, "sample collection: %s", cudaGetErrorString((cudaError_t) rc));
+			break;
+		}
+		e->launches += nl;
+		e->collect_snap++;
+		e->n_samples += samples_per_config;
+	}
+	e->proposal = saved;
+	if(rc != PP_OK) return rc;
+	CU(cudaStreamSynchronize(e->stream));
+	return read_states(e);
+}
+
+int pp_gpu_learned_samples(pp_engine *e, long long *count, float *out) {
+	int rc = learn_check(e);
+	if(rc != PP_OK) return rc;
+	if(count) *count = e->n_samples;
+	if(out && e->n_samples > 0) {
+		CU(cudaMemcpyAsync(out, e->d.samples, sizeof(float) * PP_MLP_SAMPLE * (size_t) e->n_samples, cudaMemcpyDeviceToHost, e->stream));
+		CU(cudaStreamSynchronize(e->stream));
+	}
+	return PP_OK;
+}
+
+int pp_gpu_learned_clear_samples(pp_engine *e) {
+	int rc = learn_check(e);
+	if(rc != PP_OK) return rc;
+	e->n_samples = 0;
+	return PP_OK;
+}
+
+int pp_gpu_learned_train(pp_engine *e, int epochs, int tiles_per_cta, double lr, double *objective) {
+	int rc = learn_check(e);
+	if(rc != PP_OK) return rc;
+	if(epochs < 0 || tiles_per_cta < 1 || tiles_per_cta > 64 || !(lr > 0.) || lr > 1.) return set_err(e, PP_ERR_ARG, "bad training arguments");
+	if(e->n_samples == 0) return set_err(e, PP_ERR_STATE, "no training samples (pp_gpu_learned_collect)");
+	const int ntiles = (int) ((e->n_samples + 127) / 128);
+	if(e->l_tiles_cap < ntiles) {
+		if(e->l_tiles) cudaFree(e->l_tiles);
+		e->l_tiles = NULL;
+		CU(cudaMalloc((void **) &e->l_tiles, sizeof(int) * (size_t) ntiles));
+		e->l_tiles_cap = ntiles;
+	}
+	int *perm = malloc(sizeof(int) * (size_t) ntiles);
+	if(!perm) return set_err(e, PP_ERR_ARG, "out of host memory");
+	int ctas = ppi_sm_count();
+	if(ctas * tiles_per_cta > ntiles) ctas = (ntiles + tiles_per_cta - 1) / tiles_per_cta;
+	const int per_step = ctas * tiles_per_cta;
+	double obj_sum = 0.;
+	long long obj_n = 0;
+	uint64_t st = e->lprm.seed ^ 0xA5A5A5A5DEADBEEFULL;
+	for(int ep = 0; ep < epochs && rc == PP_OK; ep++) {
+		for(int i = 0; i < ntiles; i++) perm[i] = i;
+		for(int i = ntiles - 1; i > 0; i--) {
+			int j = (int) (splitmix64(&st) % (uint64_t) (i + 1));
+			int t = perm[i];
+			perm[i] = perm[j];
+			perm[j] = t;
+		}
+		if(cudaMemcpyAsync(e->l_tiles, perm, sizeof(int) * (size_t) ntiles, cudaMemcpyHostToDevice, e->stream) != cudaSuccess) {
+			rc = set_err(e, PP_ERR_CUDA, "tile order upload failed");
+			break;
+		}
+		const int last = ep == epochs - 1;
+		if(last) cudaMemsetAsync(e->l_obj, 0, sizeof(double), e->stream);
+		for(int s0 = 0; s0 < ntiles; s0 += per_step) {
+			const int nt = ntiles - s0 < per_step ? ntiles - s0 : per_step;
+			int c = ppi_mlp_train_step(e->l_img, e->d.samples, (int) e->n_samples, e->l_tiles + s0, nt, tiles_per_cta, (float) e->lprm.floor, (float) e->lprm.entropy,
+					1.f / (float) (nt * 128), e->l_grad, e->l_obj, e->l_err, e->stream);
+			if(c == 0) c = ppi_mlp_adam(e->l_P, e->l_grad, e->l_m1, e->l_m2, e->l_img, ++e->adam_step, (float) lr, e->stream);
+			if(c != 0) {
+				rc = set_err(e, PP_ERR_CUDA, "training step: %s", cudaGetErrorString((cudaError_t) c));
+				break;
+			}
+			e->launches += 2;
+		}
+		/* the copy of perm must finish before the next epoch overwrites it */
+		if(cudaStreamSynchronize(e->stream) != cudaSuccess) rc = set_err(e, PP_ERR_CUDA, "training failed");
+		if(last) obj_n = e->n_samples;
+	}
+	free(perm);
+	if(rc != PP_OK) return rc;
+	CU(cudaMemcpyAsync(&obj_sum, e->l_obj, sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+	int lerr = 0;
+	CU(cudaMemcpyAsync(&lerr, e->l_err, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+	CU(cudaStreamSynchronize(e->stream));
+	if(lerr) return set_err(e, PP_ERR_CUDA, "a tensor-core wait of the training step timed out");
+	if(objective) *objective = obj_n > 0 ? obj_sum / (double) obj_n : 0.;
+	return PP_OK;
+}
+
+int pp_gpu_learned_features(pp_engine *e, int r, float *features) {
+	int rc = ready(e);
+	if(rc != PP_OK) return rc;
+	if(r < 0 || r >= e->nrep || features == NULL) return set_err(e, PP_ERR_ARG, "bad arguments");
+	rc = learn_check(e);
+	if(rc != PP_OK) return rc;
+	rc = ensure_learn_layout(e);
+	if(rc != PP_OK) return rc;
+	long long nl = 0;
+	CK(ppi_canon(&e->d, e->stream, &nl));
+	CK(ppi_learn_features(&e->d, e->stream, &nl));
+	e->launches += nl;
+	ppi_rparams *rp = e->h_rp + r;
+	const int N = rp->N;
+	float *tmp = malloc(sizeof(float) * PP_MLP_IN * (size_t) (N > 0 ? N : 1));
+	if(!tmp) return set_err(e, PP_ERR_ARG, "out of host memory");
+	if(cudaMemcpyAsync(tmp, e->d.feat + (size_t) rp->p0 * PP_MLP_IN, sizeof(float) * PP_MLP_IN * (size_t) N, cudaMemcpyDeviceToHost, e->stream) != cudaSuccess ||
+			cudaMemcpyAsync(e->pin_id, e->d.id + rp->p0, sizeof(int) * N, cudaMemcpyDeviceToHost, e->stream) != cudaSuccess ||
+			cudaStreamSynchronize(e->stream) != cudaSuccess) {
+		free(tmp);
+		return set_err(e, PP_ERR_CUDA, "feature download failed");
+	}
+	for(int k = 0; k < N; k++) {
+		const int i = e->pin_id[k];
+		if(i < 0 || i >= N) {
+			free(tmp);
+			return set_err(e, PP_ERR_STATE, "corrupt particle ids");
+		}
+		memcpy(features + (size_t) i * PP_MLP_IN, tmp + (size_t) k * PP_MLP_IN, sizeof(float) * PP_MLP_IN);
+	}
+	free(tmp);
+	return PP_OK;
+}
+
+int pp_gpu_learned_stats(pp_engine *e, long long tries[PP_MIX], long long accepted[PP_MIX], int reset) {
+	int rc = learn_check(e);
+	if(rc != PP_OK) return rc;
+	unsigned long long v[2 * PP_MIX];
+	CU(cudaMemcpyAsync(v, e->l_stats, sizeof(v), cudaMemcpyDeviceToHost, e->stream));
+	CU(cudaStreamSynchronize(e->stream));
+	for(int k = 0; k < PP_MIX; k++) {
+		if(tries) tries[k] = (long long) v[k];
+		if(accepted) accepted[k] = (long long) v[PP_MIX + k];
+	}
+	if(reset) CU(cudaMemsetAsync(e->l_stats, 0, sizeof(v), e->stream));
 	return PP_OK;
 }

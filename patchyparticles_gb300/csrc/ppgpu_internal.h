@@ -92,6 +92,17 @@ typedef struct ppi_grid {
 	float pad3;
 } ppi_grid;
 
+/* learned proposal: the four mixture components (component 0 is the plain move) and training knobs */
+#define PPI_MIX 4
+typedef struct ppi_learn {
+	float sdisp[PPI_MIX];  /* component k draws its displacement in a cube of edge sdisp[k] * Disp_max */
+	float stheta[PPI_MIX]; /* ... and its rotation angle uniformly below stheta[k] * Theta_max (capped below pi) */
+	float floor0;          /* weight of the plain component added to the network's softmax */
+	float kappa;           /* training utility: weight of the accepted bond-count change */
+	int draws;             /* training utility: proposals per component and sample */
+	int pad;
+} ppi_learn;
+
 /* all device pointers, passed by value to every kernel */
 typedef struct ppi_dev {
 	int nrep;
@@ -125,6 +136,17 @@ typedef struct ppi_dev {
 	int *out_partners; /* bond lists: per slot up to PPI_MAX_PARTNERS */
 	double *tmp_rec;   /* reorder / export scratch (ntot records) */
 	int *tmp_id;
+	/* learned proposal (allocated when it is first configured) */
+	float4 *wimg;                 /* per slot, 3 x float4: FP32 image of the canonical state (position wrapped into
+	                                 the box, orientation rows), a function of rec and the box only */
+	const unsigned char *mlp_img; /* packed BF16 network operands (ppgpu_umma.cuh) */
+	const ppi_learn *learn;
+	float *samples;               /* training samples [sample_cap][40] */
+	float *feat;                  /* per slot features [ntot][36] (pp_gpu_learned_features) */
+	unsigned long long *lstats;   /* per component: tries [0..3], accepted [4..7] */
+	int *lerr;                    /* tensor-core barrier timeouts of the learned passes */
+	int sample_cap;
+	int pad2;
 } ppi_dev;
 
 #define PPI_MAX_PARTNERS 24
@@ -139,6 +161,18 @@ int ppi_reorder(const ppi_dev *d, cudaStream_t s, long long *nl);
 /* writes x y z R00..R22 (12 doubles) of slots [first, first + count) into d->tmp_rec */
 int ppi_export(const ppi_dev *d, int first, int count, cudaStream_t s, long long *nl);
 int ppi_sm_count(void);
+
+/* learned proposal (ppgpu_kernels.cu): canonical images of all slots; one round of learned moves; the
+ * features of every slot; training samples of the current state for colour col into rows [base, base + count) */
+int ppi_canon(const ppi_dev *d, cudaStream_t s, long long *nl);
+int ppi_round_learned(const ppi_dev *d, long long round, const int *colours, int audit, cudaStream_t s, long long *nl);
+int ppi_learn_features(const ppi_dev *d, cudaStream_t s, long long *nl);
+int ppi_learn_collect(const ppi_dev *d, long long snap, int col, int base, int count, cudaStream_t s, long long *nl);
+/* the network (ppgpu_mlp.cu) */
+int ppi_mlp_pack(const float *P_dev, unsigned char *img_dev, cudaStream_t s);
+int ppi_mlp_train_step(const unsigned char *img, const float *samples, int n_samples, const int *tile_ids, int n_tiles, int tiles_per_cta, float floor0,
+		float tau, float inv_batch, float *grad, double *objective, int *err_dev, cudaStream_t s);
+int ppi_mlp_adam(float *P, float *grad, float *m1, float *m2, unsigned char *img, int step, float lr, cudaStream_t s);
 
 /* model parameters of one NVT system of N particles (exact FP64 base patches, FP32 thresholds),
  * without cell capacities; defined in ppgpu_host.c (compiled with -ffp-contract=off) */

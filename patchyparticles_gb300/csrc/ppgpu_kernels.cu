@@ -18,6 +18,7 @@
  */
 #include "ppgpu.h"
 #include "ppgpu_internal.h"
+#include "ppgpu_umma.cuh"
 
 #include <cuda_runtime.h>
 #include <math.h>
@@ -181,15 +182,18 @@ __device__ __forceinline__ void quatmat64(const double *q, double *Q) {
 /* orientation R = R0 . Q(q) of a canonical record. With q the identity (every particle after upload or
  * orthonormalisation) the result is R0 bit for bit (up to the sign of zero entries, which no test of
  * MC_would_interact can see). */
-__device__ __noinline__ void orient64(const double *R0, const double *q, double *R) {
+__device__ __forceinline__ void orient64_ops(const double *R0, const double *q, double *R) {
 	double Q[9];
 	quatmat64(q, Q);
-#pragma unroll 1
+#pragma unroll
 	for(int i = 0; i < 3; i++)
-#pragma unroll 1
+#pragma unroll
 		for(int j = 0; j < 3; j++)
 			R[3 * i + j] = __dadd_rn(__dadd_rn(__dmul_rn(R0[3 * i], Q[j]), __dmul_rn(R0[3 * i + 1], Q[3 + j])), __dmul_rn(R0[3 * i + 2], Q[6 + j]));
 }
+
+/* the same explicitly rounded operations out of line (the exact pair test's state) */
+__device__ __noinline__ void orient64(const double *R0, const double *q, double *R) { orient64_ops(R0, q, R); }
 
 /* Canonical state of particle slot ps as (x y z R00..R22): kind 0 = stored state, kind 1 = the candidate
  * of the current move, r + disp and q (x) dq with disp and dq the FP32 proposal widened exactly. This is
@@ -1336,6 +1340,478 @@ __global__ void __launch_bounds__(32 * TILE_WARPS, MODE == MODE_FAST ? PPI_TILE_
 }
 
 /* ------------------------------------------------------------------------------------------------ */
+/* learned proposal                                                                                 */
+/* ------------------------------------------------------------------------------------------------ */
+/* A learned attempt draws its move from a four-component mixture q(x -> .) = sum_k pi_k(x) K_k, where
+ * K_k displaces uniformly in a cube of edge a_k and rotates by an angle uniform in [0, t_k) about a
+ * uniform axis (component 0 is the plain move of MC_move_rototranslate, MC.c:311-340: a_0 = Disp_max,
+ * t_0 = Theta_max), and pi(x) = (1 - floor) softmax(MLP(features(x))) + floor e_0. The reverse of the
+ * move (d, axis, angle) is (-d, -axis, angle): the same |d| and angle, so every K_k has the same density
+ * c_k = [|d|_inf <= a_k / 2] [angle < t_k] / (a_k^3 t_k) both ways (relative to a measure common to all
+ * components), and Metropolis-Hastings accepts with probability
+ *     min(1, exp(-dE / T) sum_k pi_k(x') c_k / sum_k pi_k(x) c_k),     evaluated in FP64.
+ * pi is a deterministic function of the particle's canonical state and its neighbours' canonical states:
+ * the features read the FP32 image of the FP64 state (wimg), never the FP32 working records, and every
+ * operation on the way is explicitly rounded. The forward density computed for a move therefore equals
+ * the one the reverse move would compute, and the chain keeps the Boltzmann distribution exactly. */
+#define TAG_LEARN 7u
+#define TAG_COLLECT 8u
+#define LEARN_NB 3            /* neighbours in the feature vector (12 patch sites) */
+#define PI_BELOW 3.1415925f   /* largest FP32 value below pi: rotation angles stay below pi */
+#define LEARN_RF2_SCALE 0.9999f /* feature radius^2 = (1 + delta)^2 (1 - 1e-4): inside the 27 cells */
+#define LEARN_LOOSE 1e-3f     /* slack of the working-record pre-filter on r^2 */
+
+/* FP32 image of a canonical state: position wrapped into [0, L), orientation rows */
+__device__ __forceinline__ void canon_image(const double *r, const double *R, const double *box, float *img) {
+#pragma unroll
+	for(int a = 0; a < 3; a++) {
+		const double k = floor(__ddiv_rn(r[a], box[a]));
+		img[a] = d2f(__fma_rn(-k, box[a], r[a]));
+	}
+#pragma unroll
+	for(int k = 0; k < 9; k++) img[3 + k] = d2f(R[k]);
+}
+
+__device__ __forceinline__ void load_image(const float4 *wimg, int slot, float *img) {
+	const float4 a = wimg[3 * (size_t) slot], b = wimg[3 * (size_t) slot + 1], c = wimg[3 * (size_t) slot + 2];
+	img[0] = a.x, img[1] = a.y, img[2] = a.z, img[3] = a.w;
+	img[4] = b.x, img[5] = b.y, img[6] = b.z, img[7] = b.w;
+	img[8] = c.x, img[9] = c.y, img[10] = c.z, img[11] = c.w;
+}
+
+__device__ __forceinline__ void store_image(float4 *wimg, int slot, const float *img) {
+	wimg[3 * (size_t) slot] = make_float4(img[0], img[1], img[2], img[3]);
+	wimg[3 * (size_t) slot + 1] = make_float4(img[4], img[5], img[6], img[7]);
+	wimg[3 * (size_t) slot + 2] = make_float4(img[8], img[9], img[10], img[11]);
+}
+
+struct BoxF {
+	float L[3], iL[3];
+};
+
+__device__ __forceinline__ BoxF box_f(const double *box) {
+	BoxF B;
+#pragma unroll
+	for(int a = 0; a < 3; a++) {
+		B.L[a] = __double2float_rn(box[a]);
+		B.iL[a] = __fdiv_rn(1.f, B.L[a]);
+	}
+	return B;
+}
+
+__device__ __forceinline__ float min_image(float v, float L, float iL) { return __fsub_rn(v, __fmul_rn(L, rintf(__fmul_rn(v, iL)))); }
+
+/* the up to LEARN_NB nearest neighbours, ordered by (r^2, slot) */
+struct NbSel {
+	float r2[LEARN_NB];
+	int slot[LEARN_NB];
+};
+
+__device__ __forceinline__ bool nb_less(float r2a, int sa, float r2b, int sb) { return r2a < r2b || (r2a == r2b && sa < sb); }
+
+__device__ __forceinline__ void nb_insert(NbSel &S, float r2, int slot) {
+	if(!nb_less(r2, slot, S.r2[2], S.slot[2])) return;
+	S.r2[2] = r2;
+	S.slot[2] = slot;
+	if(nb_less(S.r2[2], S.slot[2], S.r2[1], S.slot[1])) {
+		float tr = S.r2[1];
+		int ts = S.slot[1];
+		S.r2[1] = S.r2[2], S.slot[1] = S.slot[2];
+		S.r2[2] = tr, S.slot[2] = ts;
+		if(nb_less(S.r2[1], S.slot[1], S.r2[0], S.slot[0])) {
+			tr = S.r2[0], ts = S.slot[0];
+			S.r2[0] = S.r2[1], S.slot[0] = S.slot[1];
+			S.r2[1] = tr, S.slot[1] = ts;
+		}
+	}
+}
+
+/* Neighbours for the feature vector of a particle with canonical image pimg, at cell-local position pl in
+ * cell (cx, cy, cz) of replica r (sorted position self is skipped): every particle whose canonical
+ * distance is below the feature radius. The 27 cells are scanned with a loose pre-filter on the working
+ * records; membership is decided on the canonical images only. */
+__device__ __forceinline__ void nb_select(const ppi_dev &d, const ppi_rparams &rp, const ppi_grid &g, int cx, int cy, int cz, int self, float plx, float ply, float plz,
+		const float *pimg, const BoxF &B, NbSel &S) {
+	const float rf2 = __fmul_rn(rp.sqr_rcut_f, LEARN_RF2_SCALE), loose = rf2 + LEARN_LOOSE;
+#pragma unroll
+	for(int n = 0; n < LEARN_NB; n++) {
+		S.r2[n] = 3.0e38f;
+		S.slot[n] = 0x7fffffff;
+	}
+	const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+#pragma unroll 1
+	for(int t = 0; t < 27; t++) {
+		const int dx = t % 3 - 1, dy = (t / 3) % 3 - 1, dz = t / 9 - 1;
+		const int cell = rp.cell_base + (wrapi(cz + dz, nz) * ny + wrapi(cy + dy, ny)) * nx + wrapi(cx + dx, nx);
+		const float ox = dx * g.wf[0], oy = dy * g.wf[1], oz = dz * g.wf[2];
+		const int j1 = d.cell_start[cell + 1];
+		for(int jq = d.cell_start[cell]; jq < j1; jq++) {
+			if(jq == self) continue;
+			const float4 qa = d.spos[jq];
+			const float ex = (qa.x - plx) + ox, ey = (qa.y - ply) + oy, ez = (qa.z - plz) + oz;
+			if(fmaf(ex, ex, fmaf(ey, ey, ez * ez)) >= loose) continue;
+			const int slot = __float_as_int(d.sori[3 * (size_t) jq + 2].w);
+			const float4 qp = d.wimg[3 * (size_t) slot];
+			const float vx = min_image(__fsub_rn(qp.x, pimg[0]), B.L[0], B.iL[0]);
+			const float vy = min_image(__fsub_rn(qp.y, pimg[1]), B.L[1], B.iL[1]);
+			const float vz = min_image(__fsub_rn(qp.z, pimg[2]), B.L[2], B.iL[2]);
+			const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(vx, vx), __fmul_rn(vy, vy)), __fmul_rn(vz, vz));
+			if(r2 < rf2) nb_insert(S, r2, slot);
+		}
+	}
+}
+
+/* f[12 n + 3 m + c]: patch site m of neighbour n (centre + 0.5 patch direction, minimum image, relative
+ * to the particle) in the particle's frame (component c = column c of its orientation . site); zero
+ * for absent neighbours */
+__device__ __forceinline__ void site_features(const ppi_dev &d, const ppi_rparams &rp, const float *pimg, const NbSel &S, const BoxF &B, float *f) {
+#pragma unroll
+	for(int n = 0; n < LEARN_NB; n++) {
+		if(S.slot[n] == 0x7fffffff) {
+#pragma unroll
+			for(int e = 0; e < 12; e++) f[12 * n + e] = 0.f;
+			continue;
+		}
+		float q[12];
+		load_image(d.wimg, S.slot[n], q);
+		float dl[3];
+#pragma unroll
+		for(int a = 0; a < 3; a++) dl[a] = min_image(__fsub_rn(q[a], pimg[a]), B.L[a], B.iL[a]);
+#pragma unroll
+		for(int m = 0; m < 4; m++) {
+			const float b0 = (float) rp.base[m][0], b1 = (float) rp.base[m][1], b2 = (float) rp.base[m][2];
+			float site[3];
+#pragma unroll
+			for(int a = 0; a < 3; a++) {
+				const float p = __fadd_rn(__fadd_rn(__fmul_rn(q[3 + 3 * a], b0), __fmul_rn(q[4 + 3 * a], b1)), __fmul_rn(q[5 + 3 * a], b2));
+				site[a] = __fadd_rn(dl[a], __fmul_rn(0.5f, p));
+			}
+#pragma unroll
+			for(int c = 0; c < 3; c++)
+				f[12 * n + 3 * m + c] = __fadd_rn(__fadd_rn(__fmul_rn(pimg[3 + c], site[0]), __fmul_rn(pimg[6 + c], site[1])), __fmul_rn(pimg[9 + c], site[2]));
+		}
+	}
+}
+
+/* bonds of the mover's old (bo) and candidate (bn) state; false if the candidate overlaps. The plain
+ * attempt's pair loop (attempt_exact) with every guard-band pair decided exactly on the spot. */
+template <int MODE>
+__device__ __forceinline__ bool move_bonds(const ppi_dev &d, const Proposal &P, const float *cpn, int cx, int cy, int cz, int &bo, int &bn, Acc &A) {
+	const ppi_rparams &rp = d.rp[P.r];
+	const ppi_grid &g = d.grid[P.r];
+	ppi_rstate *rs = d.rs + P.r;
+	const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+	const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
+	const float rc2e = rp.sqr_rcut_f + eps, ovl = 1.f - eps;
+	const float4 pn = make_float4(P.po.x + P.disp.x, P.po.y + P.disp.y, P.po.z + P.disp.z, 0.f);
+	bo = bn = 0;
+#pragma unroll 1
+	for(int t = 0; t < 27; t++) {
+		const int dx = t % 3 - 1, dy = (t / 3) % 3 - 1, dz = t / 9 - 1;
+		const int cell = rp.cell_base + (wrapi(cz + dz, nz) * ny + wrapi(cy + dy, ny)) * nx + wrapi(cx + dx, nx);
+		const float ox = dx * g.wf[0], oy = dy * g.wf[1], oz = dz * g.wf[2];
+		const int j1 = d.cell_start[cell + 1];
+		for(int jq = d.cell_start[cell]; jq < j1; jq++) {
+			if(jq == P.i) continue;
+			const float4 qa = d.spos[jq];
+			const float dxo = (qa.x - P.po.x) + ox, dyo = (qa.y - P.po.y) + oy, dzo = (qa.z - P.po.z) + oz;
+			const float dxn = (qa.x - pn.x) + ox, dyn = (qa.y - pn.y) + oy, dzn = (qa.z - pn.z) + oz;
+			const float r2o = fmaf(dxo, dxo, fmaf(dyo, dyo, dzo * dzo)), r2n = fmaf(dxn, dxn, fmaf(dyn, dyn, dzn * dzn));
+			A.pairs += 2;
+			if(MODE != MODE_AUDIT && r2n < ovl) return false;
+			if(!(MODE == MODE_AUDIT || r2o < rc2e || r2n < rc2e)) continue;
+			const float4 qb = d.sori[3 * (size_t) jq], qc = d.sori[3 * (size_t) jq + 1], qd = d.sori[3 * (size_t) jq + 2];
+			const float cq[9] = { qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w, qd.x };
+			const int qslot = __float_as_int(qd.w);
+			const int clo = pair_state<MODE>(d.rec, rp, rs, g.inv_L, P.pslot, 0, P.q, P.disp, qslot, dxo, dyo, dzo, P.cpo, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0.,
+					A.fallbacks);
+			const int cln = pair_state<MODE>(d.rec, rp, rs, g.inv_L, P.pslot, 1, P.q, P.disp, qslot, dxn, dyn, dzn, cpn, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0.,
+					A.fallbacks);
+			if(cln == CL_OVER) return false;
+			bo += (clo == CL_BOND);
+			bn += (cln == CL_BOND);
+		}
+	}
+	return true;
+}
+
+/* edges and angles of the four components for replica parameters rp */
+__device__ __forceinline__ void mix_scales(const ppi_rparams &rp, const ppi_learn &L, float *a, float *t) {
+#pragma unroll
+	for(int k = 0; k < PPI_MIX; k++) {
+		a[k] = k == 0 ? rp.disp_max_f : __fmul_rn(rp.disp_max_f, L.sdisp[k]);
+		t[k] = fminf(k == 0 ? rp.theta_max_f : __fmul_rn(rp.theta_max_f, L.stheta[k]), PI_BELOW);
+	}
+}
+
+/* move of component k from two Philox blocks: displacement (rd.x, rd.y, rd.z), angle rd.w, axis (ra.x, ra.y);
+ * component 0 reproduces the plain move's arithmetic */
+__device__ __forceinline__ void mix_draw(float a, float t, U4 rd, U4 ra, float3 &disp, float &theta, float4 &q) {
+	disp = make_float3((u01(rd.x) - 0.5f) * a, (u01(rd.y) - 0.5f) * a, (u01(rd.z) - 0.5f) * a);
+	theta = u01(rd.w) * t;
+	const float zc = 1.f - 2.f * u01(ra.x);
+	const float phi = 6.283185307179586f * u01(ra.y);
+	const float sr = sqrtf(fmaxf(0.f, 1.f - zc * zc));
+	float sp, cph, sh, ch;
+	__sincosf(phi, &sp, &cph);
+	__sincosf(0.5f * theta, &sh, &ch);
+	q = make_float4(ch, sh * sr * cph, sh * sr * sp, sh * zc);
+}
+
+/* sum_k pi_k c_k of a move (FP64) */
+__device__ __forceinline__ double mix_density(const float *pi, const float *a, const float *t, float3 dsp, float theta) {
+	const float m = fmaxf(fabsf(dsp.x), fmaxf(fabsf(dsp.y), fabsf(dsp.z)));
+	double s = 0.;
+#pragma unroll
+	for(int k = 0; k < PPI_MIX; k++)
+		if(m <= 0.5f * a[k] && theta < t[k]) {
+			const double ak = (double) a[k];
+			s += (double) pi[k] / (ak * ak * ak * (double) t[k]);
+		}
+	return s;
+}
+
+/* canonical state of slot ps after the move (dq, disp): commit_move's FP64 operations, then R0 . Q(q') */
+__device__ __forceinline__ void moved_image(const ppi_dev &d, int ps, float4 dq, float3 disp, const double *box, float *img) {
+	const double *rec = d.rec + (size_t) ps * PPI_REC;
+	const double qv[4] = { rec[PPI_Q], rec[PPI_Q + 1], rec[PPI_Q + 2], rec[PPI_Q + 3] };
+	const double b[4] = { f2d(dq.x), f2d(dq.y), f2d(dq.z), f2d(dq.w) };
+	double qn[4], R0[9], R[9];
+#pragma unroll
+	for(int c = 0; c < 4; c++) qn[c] = qcomp64(qv[c], qv[c ^ 1], qv[c ^ 2], qv[c ^ 3], b, c);
+	const double rn[3] = { __dadd_rn(rec[0], f2d(disp.x)), __dadd_rn(rec[1], f2d(disp.y)), __dadd_rn(rec[2], f2d(disp.z)) };
+#pragma unroll
+	for(int k = 0; k < 9; k++) R0[k] = rec[PPI_R0 + k];
+	orient64_ops(R0, qn, R);
+	canon_image(rn, R, box, img);
+}
+
+/* the mover of a list entry: particle choice (draw x), working record, canonical image, cell */
+__device__ __forceinline__ void learn_mover(const ppi_dev &d, const int4 ent, uint32_t draw, Proposal &P, float *img, int &cx, int &cy, int &cz) {
+	P.r = ent.w;
+	const ppi_rparams &rp = d.rp[P.r];
+	const ppi_grid &g = d.grid[P.r];
+	P.local = ent.x - rp.cell_base;
+	P.i = ent.y + (int) __umulhi(draw, (uint32_t) ent.z);
+	P.po = d.spos[P.i];
+	const float4 ob = d.sori[3 * (size_t) P.i], oc = d.sori[3 * (size_t) P.i + 1], od = d.sori[3 * (size_t) P.i + 2];
+	P.pslot = __float_as_int(od.w);
+	P.cpo[0] = ob.x, P.cpo[1] = ob.y, P.cpo[2] = ob.z, P.cpo[3] = ob.w;
+	P.cpo[4] = oc.x, P.cpo[5] = oc.y, P.cpo[6] = oc.z, P.cpo[7] = oc.w;
+	P.cpo[8] = od.x;
+	load_image(d.wimg, P.pslot, img);
+	cx = P.local % g.n[0];
+	cy = (P.local / g.n[0]) % g.n[1];
+	cz = P.local / (g.n[0] * g.n[1]);
+}
+
+__device__ __forceinline__ bool inside_cell(const ppi_grid &g, float4 po, float3 disp) {
+	const float nx = po.x + disp.x, ny = po.y + disp.y, nz = po.z + disp.z;
+	return nx >= 0.f && nx < g.wf[0] && ny >= 0.f && ny < g.wf[1] && nz >= 0.f && nz < g.wf[2];
+}
+
+/* One checkerboard colour of learned moves: 128 attempts per CTA tile, one per thread; the network runs
+ * twice per tile on the tensor cores (current and candidate states). */
+template <int MODE>
+__global__ void __launch_bounds__(MLP_ROWS) k_colour_learned(ppi_dev d, long long round, int col) {
+	extern __shared__ __align__(128) unsigned char smem_raw[];
+	MlpFwdSmem &S = *(MlpFwdSmem *) smem_raw;
+	mlp_fwd_begin(S, d.mlp_img);
+	const ppi_learn L = *d.learn;
+	uint32_t phase = 0;
+	Acc A;
+	A.r = -1;
+	A.tries = A.acc = A.pairs = A.fallbacks = 0;
+	A.dbonds = 0;
+	unsigned ctr[PPI_MIX] = { 0u, 0u, 0u, 0u }, cac[PPI_MIX] = { 0u, 0u, 0u, 0u };
+	const int4 *list = d.clist + (size_t) col * d.clist_cap;
+	int cnt = d.ccount[col];
+	if(cnt > d.clist_cap) cnt = d.clist_cap;
+	const int ntiles = (cnt + MLP_ROWS - 1) / MLP_ROWS;
+#pragma unroll 1
+	for(int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+		const int idx = tile * MLP_ROWS + threadIdx.x;
+		bool live = idx < cnt;
+		Proposal P;
+		P.r = 0;
+		float img0[12], f[MLP_IN];
+		int cx = 0, cy = 0, cz = 0;
+		U4 r1 = U4{ 0u, 0u, 0u, 0u };
+#pragma unroll
+		for(int e = 0; e < MLP_IN; e++) f[e] = 0.f;
+		if(live) {
+			const int4 ent = list[idx];
+			const ppi_rparams &rp = d.rp[ent.w];
+			r1 = rng(rp, round, ent.w, TAG_LEARN, (uint32_t) (ent.x - rp.cell_base), 0u);
+			learn_mover(d, ent, r1.x, P, img0, cx, cy, cz);
+			if(P.r != A.r) {
+				flush_thread(d, A);
+				A.r = P.r;
+			}
+			A.tries++;
+			const BoxF B = box_f(d.rs[P.r].box);
+			NbSel sel;
+			nb_select(d, rp, d.grid[P.r], cx, cy, cz, P.i, P.po.x, P.po.y, P.po.z, img0, B, sel);
+			site_features(d, rp, img0, sel, B, f);
+		}
+		mlp_put_x(S, f);
+		float z[MLP_OUT], pi0[PPI_MIX], pi1[PPI_MIX], a[PPI_MIX], t[PPI_MIX];
+		mlp_forward_tile(S, &phase, z);
+		mix_weights(z, L.floor0, pi0);
+		int comp = 0, bo = 0, bn = 0;
+		float theta = 0.f, img1[12], cpn[9];
+		if(live) {
+			const ppi_rparams &rp = d.rp[P.r];
+			mix_scales(rp, L, a, t);
+			const float uc = u01(r1.y);
+			float cum = pi0[0];
+			while(comp < PPI_MIX - 1 && uc >= cum) cum = __fadd_rn(cum, pi0[++comp]);
+			const U4 rd = rng(rp, round, P.r, TAG_LEARN, (uint32_t) P.local, 1u), ra = rng(rp, round, P.r, TAG_LEARN, (uint32_t) P.local, 2u);
+			mix_draw(a[comp], t[comp], rd, ra, P.disp, theta, P.q);
+			ctr[comp]++;
+			live = inside_cell(d.grid[P.r], P.po, P.disp);
+		}
+		if(live) {
+			cols_new(P.cpo, P.q, cpn);
+			live = move_bonds<MODE>(d, P, cpn, cx, cy, cz, bo, bn, A);
+		}
+#pragma unroll
+		for(int e = 0; e < MLP_IN; e++) f[e] = 0.f;
+		if(live) {
+			const ppi_rparams &rp = d.rp[P.r];
+			const BoxF B = box_f(d.rs[P.r].box);
+			moved_image(d, P.pslot, P.q, P.disp, d.rs[P.r].box, img1);
+			NbSel sel;
+			nb_select(d, rp, d.grid[P.r], cx, cy, cz, P.i, P.po.x + P.disp.x, P.po.y + P.disp.y, P.po.z + P.disp.z, img1, B, sel);
+			site_features(d, rp, img1, sel, B, f);
+		}
+		mlp_put_x(S, f);
+		mlp_forward_tile(S, &phase, z);
+		mix_weights(z, L.floor0, pi1);
+		if(live) {
+			const ppi_rparams &rp = d.rp[P.r];
+			const double ratio = mix_density(pi1, a, t, P.disp, theta) / mix_density(pi0, a, t, P.disp, theta);
+			const double p = exp(-(double) (bo - bn) / rp.T) * ratio;
+			if(u01d(r1.z, r1.w) < p) {
+				commit_move(d, P.i, P.pslot, P.po, P.disp, P.q, cpn);
+				store_image(d.wimg, P.pslot, img1);
+				A.acc++;
+				A.dbonds += bn - bo;
+				cac[comp]++;
+			}
+		}
+	}
+	flush_thread(d, A);
+#pragma unroll
+	for(int k = 0; k < PPI_MIX; k++) {
+		const unsigned tk = __reduce_add_sync(0xffffffffu, ctr[k]), ak = __reduce_add_sync(0xffffffffu, cac[k]);
+		if((threadIdx.x & 31) == 0 && tk) {
+			atomicAdd(d.lstats + k, (unsigned long long) tk);
+			if(ak) atomicAdd(d.lstats + PPI_MIX + k, (unsigned long long) ak);
+		}
+	}
+	mlp_fwd_end(S);
+	if(threadIdx.x == 0 && S.err) atomicExch(d.lerr, 1);
+}
+
+/* Training samples of the current state: row j of [base, base + count) takes list entry j * n / count of
+ * colour col, its particle's features and, per component k, the mean over `draws` proposals of
+ *     u_k = acc (|d|^2 / Disp_max^2 + angle^2 / Theta_max^2 + kappa |bonds_new - bonds_old|),
+ * acc = min(1, exp(-dE / T)) for a candidate inside the cell without overlap, else 0. */
+template <int MODE>
+__global__ void __launch_bounds__(128) k_learn_collect(ppi_dev d, long long snap, int col, int base, int count) {
+	const int j = blockIdx.x * blockDim.x + threadIdx.x;
+	if(j >= count) return;
+	float *out = d.samples + (size_t) (base + j) * MLP_SAMPLE;
+	int cnt = d.ccount[col];
+	if(cnt > d.clist_cap) cnt = d.clist_cap;
+	if(cnt == 0) {
+		for(int e = 0; e < MLP_SAMPLE; e++) out[e] = 0.f;
+		return;
+	}
+	const ppi_learn L = *d.learn;
+	const int4 ent = d.clist[(size_t) col * d.clist_cap + (int) (((long long) j * cnt) / count)];
+	const ppi_rparams &rp = d.rp[ent.w];
+	const U4 r1 = rng(rp, snap, ent.w, TAG_COLLECT, (uint32_t) (ent.x - rp.cell_base), 0u);
+	Proposal P;
+	float img0[12], f[MLP_IN];
+	int cx, cy, cz;
+	learn_mover(d, ent, r1.x, P, img0, cx, cy, cz);
+	const BoxF B = box_f(d.rs[P.r].box);
+	NbSel sel;
+	nb_select(d, rp, d.grid[P.r], cx, cy, cz, P.i, P.po.x, P.po.y, P.po.z, img0, B, sel);
+	site_features(d, rp, img0, sel, B, f);
+#pragma unroll
+	for(int e = 0; e < MLP_IN; e++) out[e] = f[e];
+	float a[PPI_MIX], t[PPI_MIX];
+	mix_scales(rp, L, a, t);
+	const float idm2 = 1.f / (rp.disp_max_f * rp.disp_max_f), ith2 = 1.f / (rp.theta_max_f * rp.theta_max_f);
+	Acc A;
+	A.r = -1;
+	A.tries = A.acc = A.pairs = A.fallbacks = 0;
+	A.dbonds = 0;
+#pragma unroll 1
+	for(int k = 0; k < PPI_MIX; k++) {
+		float u = 0.f;
+#pragma unroll 1
+		for(int q = 0; q < L.draws; q++) {
+			const uint32_t sub = 1u + 2u * (uint32_t) (k * L.draws + q);
+			const U4 rd = rng(rp, snap, P.r, TAG_COLLECT, (uint32_t) P.local, sub), ra = rng(rp, snap, P.r, TAG_COLLECT, (uint32_t) P.local, sub + 1u);
+			float theta;
+			mix_draw(a[k], t[k], rd, ra, P.disp, theta, P.q);
+			if(!inside_cell(d.grid[P.r], P.po, P.disp)) continue;
+			float cpn[9];
+			cols_new(P.cpo, P.q, cpn);
+			int bo, bn;
+			if(!move_bonds<MODE>(d, P, cpn, cx, cy, cz, bo, bn, A)) continue;
+			const int dE = bo - bn;
+			const float acc = dE <= 0 ? 1.f : expf(-(float) dE / (float) rp.T);
+			const float d2 = P.disp.x * P.disp.x + P.disp.y * P.disp.y + P.disp.z * P.disp.z;
+			u += acc * (d2 * idm2 + theta * theta * ith2 + L.kappa * (float) abs(bn - bo));
+		}
+		out[MLP_IN + k] = L.draws > 0 ? u / (float) L.draws : 0.f;
+	}
+}
+
+/* features of the particle at every sorted position, stored by slot (d.feat[slot][36]) */
+__global__ void k_learn_features(ppi_dev d) {
+	const int k = blockIdx.x * blockDim.x + threadIdx.x;
+	if(k >= d.ntot) return;
+	const float4 od = d.sori[3 * (size_t) k + 2];
+	const int gc = __float_as_int(od.z), slot = __float_as_int(od.w);
+	const int r = d.cell_rep[gc];
+	const ppi_rparams &rp = d.rp[r];
+	const ppi_grid &g = d.grid[r];
+	const int local = gc - rp.cell_base;
+	const int cx = local % g.n[0], cy = (local / g.n[0]) % g.n[1], cz = local / (g.n[0] * g.n[1]);
+	const float4 po = d.spos[k];
+	float img[12], f[MLP_IN];
+	load_image(d.wimg, slot, img);
+	const BoxF B = box_f(d.rs[r].box);
+	NbSel sel;
+	nb_select(d, rp, g, cx, cy, cz, k, po.x, po.y, po.z, img, B, sel);
+	site_features(d, rp, img, sel, B, f);
+	for(int e = 0; e < MLP_IN; e++) d.feat[(size_t) slot * MLP_IN + e] = f[e];
+}
+
+/* canonical images of every slot from the FP64 records and the current boxes */
+__global__ void k_canon(ppi_dev d) {
+	const int s = blockIdx.x * blockDim.x + threadIdx.x;
+	if(s >= d.ntot) return;
+	const double *rec = d.rec + (size_t) s * PPI_REC;
+	double q[4], R0[9], R[9];
+	const double r[3] = { rec[0], rec[1], rec[2] };
+#pragma unroll
+	for(int c = 0; c < 4; c++) q[c] = rec[PPI_Q + c];
+#pragma unroll
+	for(int k = 0; k < 9; k++) R0[k] = rec[PPI_R0 + k];
+	orient64_ops(R0, q, R);
+	float img[12];
+	canon_image(r, R, d.rs[d.rep[s]].box, img);
+	store_image(d.wimg, s, img);
+}
+
+/* ------------------------------------------------------------------------------------------------ */
 /* lane groups (energy pass)                                                                        */
 /* ------------------------------------------------------------------------------------------------ */
 #define PPI_DEFAULT_LANES 4
@@ -2275,6 +2751,58 @@ extern "C" int ppi_reorder(const ppi_dev *d, cudaStream_t s, long long *nl) {
 	*nl += 1;
 	cudaMemcpyAsync(d->rec, d->tmp_rec, sizeof(double) * PPI_REC * (size_t) d->ntot, cudaMemcpyDeviceToDevice, s);
 	cudaMemcpyAsync(d->id, d->tmp_id, sizeof(int) * (size_t) d->ntot, cudaMemcpyDeviceToDevice, s);
+	return (int) cudaGetLastError();
+}
+
+extern "C" int ppi_canon(const ppi_dev *d, cudaStream_t s, long long *nl) {
+	if(d->ntot <= 0) return 0;
+	k_canon<<<(d->ntot + 255) / 256, 256, 0, s>>>(*d);
+	*nl += 1;
+	return (int) cudaGetLastError();
+}
+
+/* one wave of resident CTAs of a learned-move kernel (dynamic shared memory: the network's tile) */
+template <typename F>
+static int learned_grid(F f, int *cache) {
+	if(*cache == 0) {
+		if(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sizeof(MlpFwdSmem)) != cudaSuccess) return -1;
+		int nb = 0;
+		if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f, MLP_ROWS, sizeof(MlpFwdSmem)) != cudaSuccess || nb <= 0) nb = 1;
+		/* tensor memory: MLP_FWD_TMEM_COLS columns per CTA out of 512 per SM */
+		if(nb > 512 / MLP_FWD_TMEM_COLS) nb = 512 / MLP_FWD_TMEM_COLS;
+		*cache = nb * ppi_sm_count();
+	}
+	return *cache;
+}
+
+extern "C" int ppi_round_learned(const ppi_dev *d, long long round, const int *colours, int audit, cudaStream_t s, long long *nl) {
+	static int g_audit = 0, g_fast = 0;
+	if(audit || d->audit_any) {
+		const int grid = learned_grid(k_colour_learned<MODE_AUDIT>, &g_audit);
+		if(grid < 0) return (int) cudaGetLastError();
+		for(int ci = 0; ci < 8; ci++) k_colour_learned<MODE_AUDIT><<<grid, MLP_ROWS, sizeof(MlpFwdSmem), s>>>(*d, round, colours[ci]);
+	}
+	else {
+		const int grid = learned_grid(k_colour_learned<MODE_FAST>, &g_fast);
+		if(grid < 0) return (int) cudaGetLastError();
+		for(int ci = 0; ci < 8; ci++) k_colour_learned<MODE_FAST><<<grid, MLP_ROWS, sizeof(MlpFwdSmem), s>>>(*d, round, colours[ci]);
+	}
+	*nl += 8;
+	return (int) cudaGetLastError();
+}
+
+extern "C" int ppi_learn_features(const ppi_dev *d, cudaStream_t s, long long *nl) {
+	if(d->ntot <= 0) return 0;
+	k_learn_features<<<(d->ntot + 127) / 128, 128, 0, s>>>(*d);
+	*nl += 1;
+	return (int) cudaGetLastError();
+}
+
+extern "C" int ppi_learn_collect(const ppi_dev *d, long long snap, int col, int base, int count, cudaStream_t s, long long *nl) {
+	if(count <= 0) return 0;
+	if(d->audit_any) k_learn_collect<MODE_AUDIT><<<(count + 127) / 128, 128, 0, s>>>(*d, snap, col, base, count);
+	else k_learn_collect<MODE_FAST><<<(count + 127) / 128, 128, 0, s>>>(*d, snap, col, base, count);
+	*nl += 1;
 	return (int) cudaGetLastError();
 }
 

@@ -31,6 +31,7 @@
 #include <string.h>
 
 #include "ppgpu.h"
+#include "ppgpu_internal.h"
 
 /* ------------------------------------------------------------------------------------------------ */
 /* operand image                                                                                     */
@@ -97,7 +98,6 @@ __global__ void __launch_bounds__(MLP_ROWS) k_mlp_forward(const unsigned char *i
 /* ------------------------------------------------------------------------------------------------ */
 /* training step                                                                                     */
 /* ------------------------------------------------------------------------------------------------ */
-#define MLP_SAMPLE 40 /* floats per training sample: 36 features, 4 component utilities */
 #define MLP_WG_N 112  /* weight-gradient GEMM: N = 64 (H1^T) + 48 (X^T) */
 #define MLP_W3G_N 80  /* dW3 GEMM: N = 64 (H2^T) + ones row + padding */
 #define MLP_ONES_X 100 /* row of the weight-gradient B operand holding ones (X^T row 36) */

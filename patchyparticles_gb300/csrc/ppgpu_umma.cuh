@@ -30,6 +30,7 @@
 #define MLP_OUT 4      /* mixture logits */
 #define MLP_N3 16      /* layer-3 N padded to the smallest legal N for M = 128 */
 #define MLP_ROWS 128   /* particles per tensor-core tile */
+#define MLP_SAMPLE 40  /* floats per training sample: 36 features, 4 component utilities */
 
 /* FP32 master parameters, the layout the C-ABI exposes: W1[64][36] b1[64] W2[64][64] b2[64] W3[4][64] b3[4] */
 #define MLP_OFF_W1 0
