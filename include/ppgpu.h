@@ -207,7 +207,9 @@ int pp_mlp_grad(const float *params, int n, const float *samples, double floor, 
  * Metropolis-Hastings with the reverse-move density, so the Boltzmann distribution is kept exactly.
  * The network is trained on the GPU (pp_gpu_learned_train) on samples of configurations generated by
  * the plain move (pp_gpu_learned_collect); per sample and component the utility is the mean over
- * `draws` proposals of acc (|d|^2 / Disp_max^2 + angle^2 / Theta_max^2 + kappa |bond change|). */
+ * `draws` proposals of acc (kappa |bond change| + jump (|d|^2 / Disp_max^2 + angle^2 / Theta_max^2)),
+ * acc = min(1, exp(-dE / T)) (0 for an overlap or a move out of the cell), divided by the sample's
+ * largest utility (so every environment's preference counts alike). */
 #define PP_PROPOSAL_PLAIN 0
 #define PP_PROPOSAL_LEARNED 1
 #define PP_MIX 4
@@ -218,6 +220,7 @@ typedef struct pp_learned_params {
 	double floor;               /* weight of the plain component always mixed in, (0, 1] */
 	double entropy;             /* training: entropy bonus tau of the objective (>= 0) */
 	double kappa;               /* training: weight of the bond-count change in the utility (>= 0) */
+	double jump;                /* training: weight of the squared jump in the utility (>= 0; a tie-break) */
 	int draws;                  /* training: proposals per component and sample, [1, 64] */
 	uint64_t seed;              /* initial weights and the training order */
 } pp_learned_params;

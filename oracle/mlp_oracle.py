@@ -176,11 +176,14 @@ def base_patches():
 
 
 def canonical_image(r, R, box):
-    """FP32 image of the canonical state: positions wrapped into [0, L) (x - floor(x / L) L), orientation
-    rows; both rounded to FP32."""
+    """FP32 image of the canonical state as the engine forms it: the position wrapped into the box with an
+    FP32 guess of the image index (x - k L in float64, k = floor(fl(x) / fl(L)) in float32) and rounded to
+    FP32; the orientation rows rounded to FP32 (the engine evaluates R0 . Q(q) in FP32, which equals the
+    rounded R while q is the identity -- right after an upload)."""
     r = np.asarray(r, dtype=np.float64).reshape(-1, 3)
     box = np.asarray(box, dtype=np.float64)
-    k = np.floor(r / box)
+    Lf = box.astype(np.float32)
+    k = np.floor(r.astype(np.float32) * (np.float32(1.0) / Lf)).astype(np.float64)
     y = r - k * box
     return y.astype(np.float32), np.asarray(R, dtype=np.float64).reshape(-1, 3, 3).astype(np.float32)
 
@@ -205,7 +208,7 @@ def features(r, R, box, kf_delta, nb=3):
         cand = np.nonzero(r2 < rf2)[0]
         if cand.size == 0:
             continue
-        order = cand[np.lexsort((cand, r2[cand]))][:nb]
+        order = cand[np.lexsort((cand, r2[cand]))][:nb]  # ties by particle index, as the engine
         Ri = Rf[i]
         for n, j in enumerate(order):
             dl = v[j]

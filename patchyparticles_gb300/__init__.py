@@ -83,6 +83,7 @@ class PPLearnedParams(ctypes.Structure):
         ("floor", ctypes.c_double),
         ("entropy", ctypes.c_double),
         ("kappa", ctypes.c_double),
+        ("jump", ctypes.c_double),
         ("draws", ctypes.c_int),
         ("seed", ctypes.c_uint64),
     ]

@@ -58,6 +58,7 @@ struct pp_engine {
 	float *l_P, *l_m1, *l_m2, *l_grad; /* FP32 master weights, Adam moments, gradient (device) */
 	unsigned char *l_img;         /* packed BF16 operands (device) */
 	ppi_learn *l_learn;
+	ppi_lrep *l_rep;              /* per replica mixture tables (device) */
 	unsigned long long *l_stats;
 	int *l_err;
 	double *l_obj;
@@ -231,19 +232,21 @@ static void free_device(pp_engine *e) {
 	e->pin_id = e->pin_i1 = e->pin_i2 = NULL;
 	e->pin_n = 0;
 	/* layout-sized buffers of the learned proposal */
-	if(e->d.wimg) cudaFree(e->d.wimg);
+	if(e->d.simg) cudaFree(e->d.simg);
 	if(e->d.feat) cudaFree(e->d.feat);
-	e->d.wimg = NULL;
+	e->d.simg = NULL;
 	e->d.feat = NULL;
 }
 
 static void free_learned(pp_engine *e) {
-	void *ptrs[] = { e->l_P, e->l_m1, e->l_m2, e->l_grad, e->l_img, e->l_learn, e->l_stats, e->l_err, e->l_obj, e->l_tiles, e->d.samples };
+	void *ptrs[] = { e->l_P, e->l_m1, e->l_m2, e->l_grad, e->l_img, e->l_learn, e->l_rep, e->l_stats, e->l_err, e->l_obj, e->l_tiles, e->d.samples };
 	for(size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); i++)
 		if(ptrs[i]) cudaFree(ptrs[i]);
 	e->l_P = e->l_m1 = e->l_m2 = e->l_grad = NULL;
 	e->l_img = NULL;
 	e->l_learn = NULL;
+	e->l_rep = NULL;
+	e->d.lrep = NULL;
 	e->l_stats = NULL;
 	e->l_err = NULL;
 	e->l_obj = NULL;
@@ -393,7 +396,7 @@ static int do_resort(pp_engine *e) {
 		CK(ppi_reorder(&e->d, e->stream, &nl));
 	}
 	CK(ppi_resort(&e->d, e->epoch, e->stream, &nl));
-	if(e->proposal == PP_PROPOSAL_LEARNED && e->d.wimg) CK(ppi_canon(&e->d, e->stream, &nl));
+	if(e->proposal == PP_PROPOSAL_LEARNED && e->d.simg) CK(ppi_canon(&e->d, e->stream, &nl));
 	e->launches += nl;
 	e->epoch++;
 	return PP_OK;
@@ -1228,8 +1231,9 @@ void pp_default_learned_params(pp_learned_params *p) {
 	}
 	p->floor = 0.1;
 	p->entropy = 0.01;
-	p->kappa = 100.;
-	p->draws = 2;
+	p->kappa = 1.;
+	p->jump = 1e-9;
+	p->draws = 4;
 	p->seed = 12345;
 }
 
@@ -1246,7 +1250,7 @@ static double u01_sm(uint64_t *s) { return (double) (splitmix64(s) >> 11) * 0x1p
 static int ensure_learn_layout(pp_engine *e) {
 	if(!e->committed) return set_err(e, PP_ERR_STATE, "no configuration uploaded for every replica");
 	size_t n1 = e->d.ntot > 0 ? (size_t) e->d.ntot : 1;
-	if(!e->d.wimg) CU(cudaMalloc((void **) &e->d.wimg, sizeof(float) * 12 * n1));
+	if(!e->d.simg) CU(cudaMalloc((void **) &e->d.simg, sizeof(float) * 16 * n1));
 	if(!e->d.feat) CU(cudaMalloc((void **) &e->d.feat, sizeof(float) * PP_MLP_IN * n1));
 	return PP_OK;
 }
@@ -1264,7 +1268,7 @@ int pp_gpu_learned_init(pp_engine *e, const pp_learned_params *p) {
 		if(!(p->scale_disp[k] > 0.) || !(p->scale_theta[k] > 0.) || p->scale_disp[k] > 1e3 || p->scale_theta[k] > 1e3)
 			return set_err(e, PP_ERR_ARG, "component scales must lie in (0, 1000]");
 	if(!(p->floor > 0. && p->floor <= 1.)) return set_err(e, PP_ERR_ARG, "floor must lie in (0, 1]");
-	if(!(p->entropy >= 0.) || !(p->kappa >= 0.)) return set_err(e, PP_ERR_ARG, "entropy and kappa must be >= 0");
+	if(!(p->entropy >= 0.) || !(p->kappa >= 0.) || !(p->jump >= 0.)) return set_err(e, PP_ERR_ARG, "entropy, kappa and jump must be >= 0");
 	if(p->draws < 1 || p->draws > 64) return set_err(e, PP_ERR_ARG, "draws must lie in [1, 64]");
 	e->lprm = *p;
 	for(int k = 0; k < PP_MIX; k++) {
@@ -1273,6 +1277,7 @@ int pp_gpu_learned_init(pp_engine *e, const pp_learned_params *p) {
 	}
 	e->h_learn.floor0 = (float) p->floor;
 	e->h_learn.kappa = (float) p->kappa;
+	e->h_learn.jump = (float) p->jump;
 	e->h_learn.draws = p->draws;
 	if(!e->learn_ready) {
 		CU(cudaMalloc((void **) &e->l_P, sizeof(float) * PP_MLP_NPARAMS));
@@ -1281,6 +1286,7 @@ int pp_gpu_learned_init(pp_engine *e, const pp_learned_params *p) {
 		CU(cudaMalloc((void **) &e->l_grad, sizeof(float) * PP_MLP_NPARAMS));
 		CU(cudaMalloc((void **) &e->l_img, 32768));
 		CU(cudaMalloc((void **) &e->l_learn, sizeof(ppi_learn)));
+		CU(cudaMalloc((void **) &e->l_rep, sizeof(ppi_lrep) * (size_t) e->nrep));
 		CU(cudaMalloc((void **) &e->l_stats, sizeof(unsigned long long) * 2 * PP_MIX));
 		CU(cudaMalloc((void **) &e->l_err, sizeof(int)));
 		CU(cudaMalloc((void **) &e->l_obj, sizeof(double)));
@@ -1288,7 +1294,31 @@ int pp_gpu_learned_init(pp_engine *e, const pp_learned_params *p) {
 	}
 	e->d.mlp_img = e->l_img;
 	e->d.learn = e->l_learn;
+	e->d.lrep = e->l_rep;
 	e->d.lstats = e->l_stats;
+	{ /* per replica tables: the component edges and angles as the kernels' FP32 values, their densities */
+		ppi_lrep *M = calloc((size_t) e->nrep, sizeof(ppi_lrep));
+		if(!M) return set_err(e, PP_ERR_ARG, "out of host memory");
+		for(int r = 0; r < e->nrep; r++) {
+			const float dm = (float) e->prm[r].disp_max, tm = (float) e->prm[r].theta_max;
+			for(int k = 0; k < PP_MIX; k++) {
+				const float a = k == 0 ? dm : dm * e->h_learn.sdisp[k];
+				float t = k == 0 ? tm : tm * e->h_learn.stheta[k];
+				if(t > 3.1415925f) t = 3.1415925f; /* rotation angles stay below pi */
+				M[r].a[k] = a;
+				M[r].t[k] = t;
+				M[r].v[k] = 1.0 / ((double) a * (double) a * (double) a * (double) t);
+			}
+			for(int k = -PPI_LEXP; k <= PPI_LEXP; k++) M[r].expk[k + PPI_LEXP] = exp(-(double) k / e->prm[r].temperature);
+			if(!(M[r].a[0] > 0.f) || !(M[r].t[0] > 0.f)) {
+				free(M);
+				return set_err(e, PP_ERR_ARG, "replica %d: the learned proposal needs Disp_max > 0 and Theta_max > 0", r);
+			}
+		}
+		cudaError_t c = cudaMemcpy(e->l_rep, M, sizeof(ppi_lrep) * (size_t) e->nrep, cudaMemcpyHostToDevice);
+		free(M);
+		if(c != cudaSuccess) return set_err(e, PP_ERR_CUDA, "mixture tables: %s", cudaGetErrorString(c));
+	}
 	e->d.lerr = e->l_err;
 	CU(cudaMemcpyAsync(e->l_learn, &e->h_learn, sizeof(ppi_learn), cudaMemcpyHostToDevice, e->stream));
 	CU(cudaMemsetAsync(e->l_stats, 0, sizeof(unsigned long long) * 2 * PP_MIX, e->stream));

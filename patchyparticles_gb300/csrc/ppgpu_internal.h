@@ -99,9 +99,18 @@ typedef struct ppi_learn {
 	float stheta[PPI_MIX]; /* ... and its rotation angle uniformly below stheta[k] * Theta_max (capped below pi) */
 	float floor0;          /* weight of the plain component added to the network's softmax */
 	float kappa;           /* training utility: weight of the accepted bond-count change */
+	float jump;            /* training utility: weight of the accepted squared jump (tie-break) */
 	int draws;             /* training utility: proposals per component and sample */
-	int pad;
 } ppi_learn;
+
+/* per replica, the learned mixture in that replica's units (host-computed, the kernels' own FP32 values) */
+#define PPI_LEXP 8
+typedef struct ppi_lrep {
+	double v[PPI_MIX];           /* 1 / (a_k^3 t_k): density of component k inside its support */
+	double expk[2 * PPI_LEXP + 1]; /* exp(-k / T), k = -8..8 */
+	float a[PPI_MIX];            /* cube edge of component k: Disp_max * sdisp[k] (FP32) */
+	float t[PPI_MIX];            /* maximum angle: min(Theta_max * stheta[k], largest FP32 below pi) */
+} ppi_lrep;
 
 /* all device pointers, passed by value to every kernel */
 typedef struct ppi_dev {
@@ -137,8 +146,10 @@ typedef struct ppi_dev {
 	double *tmp_rec;   /* reorder / export scratch (ntot records) */
 	int *tmp_id;
 	/* learned proposal (allocated when it is first configured) */
-	float4 *wimg;                 /* per slot, 3 x float4: FP32 image of the canonical state (position wrapped into
-	                                 the box, orientation rows), a function of rec and the box only */
+	float4 *simg;                 /* per sorted position, 4 x float4: FP32 image of the canonical state (position
+	                                 wrapped into the box, particle id, orientation rows), a function of rec, id
+	                                 and the box only */
+	const struct ppi_lrep *lrep;  /* per replica: the mixture components' edges, angles, densities */
 	const unsigned char *mlp_img; /* packed BF16 network operands (ppgpu_umma.cuh) */
 	const ppi_learn *learn;
 	float *samples;               /* training samples [sample_cap][40] */

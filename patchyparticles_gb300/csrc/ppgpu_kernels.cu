@@ -1350,39 +1350,64 @@ __global__ void __launch_bounds__(32 * TILE_WARPS, MODE == MODE_FAST ? PPI_TILE_
  * c_k = [|d|_inf <= a_k / 2] [angle < t_k] / (a_k^3 t_k) both ways (relative to a measure common to all
  * components), and Metropolis-Hastings accepts with probability
  *     min(1, exp(-dE / T) sum_k pi_k(x') c_k / sum_k pi_k(x) c_k),     evaluated in FP64.
- * pi is a deterministic function of the particle's canonical state and its neighbours' canonical states:
- * the features read the FP32 image of the FP64 state (wimg), never the FP32 working records, and every
- * operation on the way is explicitly rounded. The forward density computed for a move therefore equals
- * the one the reverse move would compute, and the chain keeps the Boltzmann distribution exactly. */
+ * pi is a deterministic function of the particle's canonical state and its neighbours' canonical
+ * states: the features read an FP32 image of the FP64 state (simg, computed from rec by explicitly
+ * rounded operations), never the FP32 working records. The forward density computed for a move
+ * therefore equals the one the reverse move would compute, and the chain keeps the Boltzmann
+ * distribution exactly. */
 #define TAG_LEARN 7u
 #define TAG_COLLECT 8u
-#define LEARN_NB 3            /* neighbours in the feature vector (12 patch sites) */
-#define PI_BELOW 3.1415925f   /* largest FP32 value below pi: rotation angles stay below pi */
+#define LEARN_NB 3              /* neighbours in the feature vector (12 patch sites) */
+#define PI_BELOW 3.1415925f     /* largest FP32 value below pi: rotation angles stay below pi */
 #define LEARN_RF2_SCALE 0.9999f /* feature radius^2 = (1 + delta)^2 (1 - 1e-4): inside the 27 cells */
-#define LEARN_LOOSE 1e-3f     /* slack of the working-record pre-filter on r^2 */
+#define LEARN_LOOSE 1e-3f       /* slack of the working-record pre-filter on r^2 */
+#define LIMG 4                  /* float4 per canonical image */
+#define LBATCH 4                /* candidates whose loads a lane issues together */
 
-/* FP32 image of a canonical state: position wrapped into [0, L), orientation rows */
-__device__ __forceinline__ void canon_image(const double *r, const double *R, const double *box, float *img) {
+/* Canonical FP32 image of the state (r, q, R0) of particle id: img[0..2] the position wrapped into the
+ * box (FP32 guess of the image index, one FP64 operation), img[3] the id, img[4 + 3 i + j] = R_ij of
+ * R0 . Q(q / |q|) evaluated in FP32 from the FP32 roundings of q and R0, operation by operation. A
+ * deterministic function of the FP64 state; after upload (q the identity) the rows are R0's. */
+__device__ __forceinline__ void canon_image(const double *r, const double *q, const double *R0, const double *box, int id, float *img) {
 #pragma unroll
 	for(int a = 0; a < 3; a++) {
-		const double k = floor(__ddiv_rn(r[a], box[a]));
-		img[a] = d2f(__fma_rn(-k, box[a], r[a]));
+		const float Lf = __double2float_rn(box[a]);
+		const float kf = floorf(__fmul_rn(d2f(r[a]), __fdiv_rn(1.f, Lf)));
+		img[a] = d2f(__fma_rn(-(double) kf, box[a], r[a]));
 	}
+	img[3] = __int_as_float(id);
+	const float w = d2f(q[0]), x = d2f(q[1]), y = d2f(q[2]), z = d2f(q[3]);
+	const float s = __fdiv_rn(2.f, __fadd_rn(__fadd_rn(__fmul_rn(w, w), __fmul_rn(x, x)), __fadd_rn(__fmul_rn(y, y), __fmul_rn(z, z))));
+	float Q[9];
+	Q[0] = __fsub_rn(1.f, __fmul_rn(s, __fadd_rn(__fmul_rn(y, y), __fmul_rn(z, z))));
+	Q[1] = __fmul_rn(s, __fsub_rn(__fmul_rn(x, y), __fmul_rn(w, z)));
+	Q[2] = __fmul_rn(s, __fadd_rn(__fmul_rn(x, z), __fmul_rn(w, y)));
+	Q[3] = __fmul_rn(s, __fadd_rn(__fmul_rn(x, y), __fmul_rn(w, z)));
+	Q[4] = __fsub_rn(1.f, __fmul_rn(s, __fadd_rn(__fmul_rn(x, x), __fmul_rn(z, z))));
+	Q[5] = __fmul_rn(s, __fsub_rn(__fmul_rn(y, z), __fmul_rn(w, x)));
+	Q[6] = __fmul_rn(s, __fsub_rn(__fmul_rn(x, z), __fmul_rn(w, y)));
+	Q[7] = __fmul_rn(s, __fadd_rn(__fmul_rn(y, z), __fmul_rn(w, x)));
+	Q[8] = __fsub_rn(1.f, __fmul_rn(s, __fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y))));
 #pragma unroll
-	for(int k = 0; k < 9; k++) img[3 + k] = d2f(R[k]);
+	for(int i = 0; i < 3; i++) {
+		const float a0 = d2f(R0[3 * i]), a1 = d2f(R0[3 * i + 1]), a2 = d2f(R0[3 * i + 2]);
+#pragma unroll
+		for(int j = 0; j < 3; j++) img[4 + 3 * i + j] = __fadd_rn(__fadd_rn(__fmul_rn(a0, Q[j]), __fmul_rn(a1, Q[3 + j])), __fmul_rn(a2, Q[6 + j]));
+	}
+	img[13] = img[14] = img[15] = 0.f;
 }
 
-__device__ __forceinline__ void load_image(const float4 *wimg, int slot, float *img) {
-	const float4 a = wimg[3 * (size_t) slot], b = wimg[3 * (size_t) slot + 1], c = wimg[3 * (size_t) slot + 2];
-	img[0] = a.x, img[1] = a.y, img[2] = a.z, img[3] = a.w;
-	img[4] = b.x, img[5] = b.y, img[6] = b.z, img[7] = b.w;
-	img[8] = c.x, img[9] = c.y, img[10] = c.z, img[11] = c.w;
+__device__ __forceinline__ void load_image(const float4 *simg, int k, float *img) {
+#pragma unroll
+	for(int c = 0; c < LIMG; c++) {
+		const float4 v = simg[LIMG * (size_t) k + c];
+		img[4 * c] = v.x, img[4 * c + 1] = v.y, img[4 * c + 2] = v.z, img[4 * c + 3] = v.w;
+	}
 }
 
-__device__ __forceinline__ void store_image(float4 *wimg, int slot, const float *img) {
-	wimg[3 * (size_t) slot] = make_float4(img[0], img[1], img[2], img[3]);
-	wimg[3 * (size_t) slot + 1] = make_float4(img[4], img[5], img[6], img[7]);
-	wimg[3 * (size_t) slot + 2] = make_float4(img[8], img[9], img[10], img[11]);
+__device__ __forceinline__ void store_image(float4 *simg, int k, const float *img) {
+#pragma unroll
+	for(int c = 0; c < LIMG; c++) simg[LIMG * (size_t) k + c] = make_float4(img[4 * c], img[4 * c + 1], img[4 * c + 2], img[4 * c + 3]);
 }
 
 struct BoxF {
@@ -1401,147 +1426,233 @@ __device__ __forceinline__ BoxF box_f(const double *box) {
 
 __device__ __forceinline__ float min_image(float v, float L, float iL) { return __fsub_rn(v, __fmul_rn(L, rintf(__fmul_rn(v, iL)))); }
 
-/* the up to LEARN_NB nearest neighbours, ordered by (r^2, slot) */
+/* the up to LEARN_NB nearest neighbours, ordered by (r^2, particle id); pos = sorted position */
 struct NbSel {
 	float r2[LEARN_NB];
-	int slot[LEARN_NB];
+	int key[LEARN_NB];
+	int pos[LEARN_NB];
 };
 
-__device__ __forceinline__ bool nb_less(float r2a, int sa, float r2b, int sb) { return r2a < r2b || (r2a == r2b && sa < sb); }
+__device__ __forceinline__ bool nb_less(float r2a, int ka, float r2b, int kb) { return r2a < r2b || (r2a == r2b && ka < kb); }
 
-__device__ __forceinline__ void nb_insert(NbSel &S, float r2, int slot) {
-	if(!nb_less(r2, slot, S.r2[2], S.slot[2])) return;
-	S.r2[2] = r2;
-	S.slot[2] = slot;
-	if(nb_less(S.r2[2], S.slot[2], S.r2[1], S.slot[1])) {
+__device__ __forceinline__ void nb_clear(NbSel &S) {
+#pragma unroll
+	for(int n = 0; n < LEARN_NB; n++) {
+		S.r2[n] = 3.0e38f;
+		S.key[n] = 0x7fffffff;
+		S.pos[n] = -1;
+	}
+}
+
+__device__ __forceinline__ void nb_insert(NbSel &S, float r2, int key, int pos) {
+	if(!nb_less(r2, key, S.r2[2], S.key[2])) return;
+	S.r2[2] = r2, S.key[2] = key, S.pos[2] = pos;
+	if(nb_less(S.r2[2], S.key[2], S.r2[1], S.key[1])) {
 		float tr = S.r2[1];
-		int ts = S.slot[1];
-		S.r2[1] = S.r2[2], S.slot[1] = S.slot[2];
-		S.r2[2] = tr, S.slot[2] = ts;
-		if(nb_less(S.r2[1], S.slot[1], S.r2[0], S.slot[0])) {
-			tr = S.r2[0], ts = S.slot[0];
-			S.r2[0] = S.r2[1], S.slot[0] = S.slot[1];
-			S.r2[1] = tr, S.slot[1] = ts;
+		int tk = S.key[1], tp = S.pos[1];
+		S.r2[1] = S.r2[2], S.key[1] = S.key[2], S.pos[1] = S.pos[2];
+		S.r2[2] = tr, S.key[2] = tk, S.pos[2] = tp;
+		if(nb_less(S.r2[1], S.key[1], S.r2[0], S.key[0])) {
+			tr = S.r2[0], tk = S.key[0], tp = S.pos[0];
+			S.r2[0] = S.r2[1], S.key[0] = S.key[1], S.pos[0] = S.pos[1];
+			S.r2[1] = tr, S.key[1] = tk, S.pos[1] = tp;
 		}
 	}
 }
 
-/* Neighbours for the feature vector of a particle with canonical image pimg, at cell-local position pl in
- * cell (cx, cy, cz) of replica r (sorted position self is skipped): every particle whose canonical
- * distance is below the feature radius. The 27 cells are scanned with a loose pre-filter on the working
- * records; membership is decided on the canonical images only. */
-__device__ __forceinline__ void nb_select(const ppi_dev &d, const ppi_rparams &rp, const ppi_grid &g, int cx, int cy, int cz, int self, float plx, float ply, float plz,
-		const float *pimg, const BoxF &B, NbSel &S) {
-	const float rf2 = __fmul_rn(rp.sqr_rcut_f, LEARN_RF2_SCALE), loose = rf2 + LEARN_LOOSE;
-#pragma unroll
-	for(int n = 0; n < LEARN_NB; n++) {
-		S.r2[n] = 3.0e38f;
-		S.slot[n] = 0x7fffffff;
-	}
-	const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
-#pragma unroll 1
-	for(int t = 0; t < 27; t++) {
-		const int dx = t % 3 - 1, dy = (t / 3) % 3 - 1, dz = t / 9 - 1;
-		const int cell = rp.cell_base + (wrapi(cz + dz, nz) * ny + wrapi(cy + dy, ny)) * nx + wrapi(cx + dx, nx);
-		const float ox = dx * g.wf[0], oy = dy * g.wf[1], oz = dz * g.wf[2];
-		const int j1 = d.cell_start[cell + 1];
-		for(int jq = d.cell_start[cell]; jq < j1; jq++) {
-			if(jq == self) continue;
-			const float4 qa = d.spos[jq];
-			const float ex = (qa.x - plx) + ox, ey = (qa.y - ply) + oy, ez = (qa.z - plz) + oz;
-			if(fmaf(ex, ex, fmaf(ey, ey, ez * ez)) >= loose) continue;
-			const int slot = __float_as_int(d.sori[3 * (size_t) jq + 2].w);
-			const float4 qp = d.wimg[3 * (size_t) slot];
-			const float vx = min_image(__fsub_rn(qp.x, pimg[0]), B.L[0], B.iL[0]);
-			const float vy = min_image(__fsub_rn(qp.y, pimg[1]), B.L[1], B.iL[1]);
-			const float vz = min_image(__fsub_rn(qp.z, pimg[2]), B.L[2], B.iL[2]);
-			const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(vx, vx), __fmul_rn(vy, vy)), __fmul_rn(vz, vz));
-			if(r2 < rf2) nb_insert(S, r2, slot);
-		}
-	}
+/* candidate at sorted position k (first float4 of its image: qp) for the feature neighbours of a particle
+ * with image pimg: inserted if its canonical distance is below the feature radius. Every kernel decides
+ * membership with this function. */
+__device__ __forceinline__ void nb_consider(float4 qp, int k, const float *pimg, const BoxF &B, float rf2, NbSel &S) {
+	const float vx = min_image(__fsub_rn(qp.x, pimg[0]), B.L[0], B.iL[0]);
+	const float vy = min_image(__fsub_rn(qp.y, pimg[1]), B.L[1], B.iL[1]);
+	const float vz = min_image(__fsub_rn(qp.z, pimg[2]), B.L[2], B.iL[2]);
+	const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(vx, vx), __fmul_rn(vy, vy)), __fmul_rn(vz, vz));
+	if(r2 < rf2) nb_insert(S, r2, __float_as_int(qp.w), k);
 }
 
 /* f[12 n + 3 m + c]: patch site m of neighbour n (centre + 0.5 patch direction, minimum image, relative
  * to the particle) in the particle's frame (component c = column c of its orientation . site); zero
  * for absent neighbours */
 __device__ __forceinline__ void site_features(const ppi_dev &d, const ppi_rparams &rp, const float *pimg, const NbSel &S, const BoxF &B, float *f) {
+	float q[LEARN_NB][16];
+#pragma unroll
+	for(int n = 0; n < LEARN_NB; n++)
+		if(S.pos[n] >= 0) load_image(d.simg, S.pos[n], q[n]); /* the three loads in flight together */
 #pragma unroll
 	for(int n = 0; n < LEARN_NB; n++) {
-		if(S.slot[n] == 0x7fffffff) {
+		if(S.pos[n] < 0) {
 #pragma unroll
 			for(int e = 0; e < 12; e++) f[12 * n + e] = 0.f;
 			continue;
 		}
-		float q[12];
-		load_image(d.wimg, S.slot[n], q);
 		float dl[3];
 #pragma unroll
-		for(int a = 0; a < 3; a++) dl[a] = min_image(__fsub_rn(q[a], pimg[a]), B.L[a], B.iL[a]);
+		for(int a = 0; a < 3; a++) dl[a] = min_image(__fsub_rn(q[n][a], pimg[a]), B.L[a], B.iL[a]);
 #pragma unroll
 		for(int m = 0; m < 4; m++) {
 			const float b0 = (float) rp.base[m][0], b1 = (float) rp.base[m][1], b2 = (float) rp.base[m][2];
 			float site[3];
 #pragma unroll
 			for(int a = 0; a < 3; a++) {
-				const float p = __fadd_rn(__fadd_rn(__fmul_rn(q[3 + 3 * a], b0), __fmul_rn(q[4 + 3 * a], b1)), __fmul_rn(q[5 + 3 * a], b2));
+				const float p = __fadd_rn(__fadd_rn(__fmul_rn(q[n][4 + 3 * a], b0), __fmul_rn(q[n][5 + 3 * a], b1)), __fmul_rn(q[n][6 + 3 * a], b2));
 				site[a] = __fadd_rn(dl[a], __fmul_rn(0.5f, p));
 			}
 #pragma unroll
 			for(int c = 0; c < 3; c++)
-				f[12 * n + 3 * m + c] = __fadd_rn(__fadd_rn(__fmul_rn(pimg[3 + c], site[0]), __fmul_rn(pimg[6 + c], site[1])), __fmul_rn(pimg[9 + c], site[2]));
+				f[12 * n + 3 * m + c] = __fadd_rn(__fadd_rn(__fmul_rn(pimg[4 + c], site[0]), __fmul_rn(pimg[7 + c], site[1])), __fmul_rn(pimg[10 + c], site[2]));
 		}
 	}
 }
 
-/* bonds of the mover's old (bo) and candidate (bn) state; false if the candidate overlaps. The plain
- * attempt's pair loop (attempt_exact) with every guard-band pair decided exactly on the spot. */
+/* The 27 cells around (cx, cy, cz) as one stream of candidates: 9 rows (dy, dz), each the contiguous
+ * cells max(cx-1, 0) .. min(cx+1, nx-1) plus the periodic wrap-around cell; range r covers candidates
+ * base[r] .. base[r+1]-1 at sorted positions lo[r] + (c - base[r]). The 36 boundary loads are independent. */
+struct Cands {
+	int lo[18];
+	int base[19];
+};
+
+__device__ __forceinline__ int cands_build(const ppi_dev &d, const ppi_rparams &rp, const ppi_grid &g, int cx, int cy, int cz, Cands &C) {
+	const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+	const int xa = cx > 0 ? cx - 1 : 0, xb = cx < nx - 1 ? cx + 1 : nx - 1;
+	const int xw = cx == 0 ? nx - 1 : (cx == nx - 1 ? 0 : -1);
+	int l0[9], h0[9], l1[9], h1[9];
+#pragma unroll
+	for(int r = 0; r < 9; r++) {
+		const int row = rp.cell_base + (wrapi(cz + r / 3 - 1, nz) * ny + wrapi(cy + r % 3 - 1, ny)) * nx;
+		l0[r] = d.cell_start[row + xa];
+		h0[r] = d.cell_start[row + xb + 1];
+		l1[r] = xw >= 0 ? d.cell_start[row + xw] : 0;
+		h1[r] = xw >= 0 ? d.cell_start[row + xw + 1] : 0;
+	}
+	int b = 0;
+#pragma unroll
+	for(int r = 0; r < 9; r++) {
+		C.lo[2 * r] = l0[r];
+		C.base[2 * r] = b;
+		b += h0[r] - l0[r];
+		C.lo[2 * r + 1] = l1[r];
+		C.base[2 * r + 1] = b;
+		b += h1[r] - l1[r];
+	}
+	C.base[18] = b;
+	return b;
+}
+
+/* sorted position of candidate c; the range cursor r only moves forward */
+__device__ __forceinline__ int cand_at(const Cands &C, int c, int &r) {
+	while(c >= C.base[r + 1]) r++;
+	return C.lo[r] + (c - C.base[r]);
+}
+
+/* x offset (in cells, -1, 0 or 1) of a candidate in cell column qx seen from column cx */
+__device__ __forceinline__ int cell_dx(int qx, int cx, int nx) {
+	int v = qx - cx;
+	return v > 1 ? v - nx : (v < -1 ? v + nx : v);
+}
+
+/* feature neighbours of the particle at sorted position self, cell-local position pl, image pimg */
+__device__ __forceinline__ void scan_features(const ppi_dev &d, const ppi_rparams &rp, const ppi_grid &g, const Cands &C, int total, int cx, int self, float4 pl,
+		const float *pimg, const BoxF &B, NbSel &S) {
+	const float rf2 = __fmul_rn(rp.sqr_rcut_f, LEARN_RF2_SCALE), loose = rf2 + LEARN_LOOSE;
+	nb_clear(S);
+	int r = 0;
+#pragma unroll 1
+	for(int c0 = 0; c0 < total; c0 += LBATCH) {
+		int jq[LBATCH], rr[LBATCH];
+#pragma unroll
+		for(int u = 0; u < LBATCH; u++) {
+			jq[u] = c0 + u < total ? cand_at(C, c0 + u, r) : -1;
+			rr[u] = r >> 1;
+		}
+		float4 qa[LBATCH];
+#pragma unroll
+		for(int u = 0; u < LBATCH; u++) qa[u] = jq[u] >= 0 ? d.spos[jq[u]] : make_float4(1e30f, 1e30f, 1e30f, 0.f);
+		bool near[LBATCH];
+#pragma unroll
+		for(int u = 0; u < LBATCH; u++) {
+			const float ox = cell_dx(__float_as_int(qa[u].w), cx, g.n[0]) * g.wf[0], oy = (rr[u] % 3 - 1) * g.wf[1], oz = (rr[u] / 3 - 1) * g.wf[2];
+			const float ex = (qa[u].x - pl.x) + ox, ey = (qa[u].y - pl.y) + oy, ez = (qa[u].z - pl.z) + oz;
+			near[u] = jq[u] >= 0 && jq[u] != self && fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < loose;
+		}
+		float4 qp[LBATCH];
+#pragma unroll
+		for(int u = 0; u < LBATCH; u++)
+			if(near[u]) qp[u] = d.simg[LIMG * (size_t) jq[u]];
+#pragma unroll
+		for(int u = 0; u < LBATCH; u++)
+			if(near[u]) nb_consider(qp[u], jq[u], pimg, B, rf2, S);
+	}
+}
+
+/* One scan for the candidate state: bonds of the old (bo) and candidate (bn) state and the feature
+ * neighbours of the candidate (image img1). False if the candidate overlaps. */
 template <int MODE>
-__device__ __forceinline__ bool move_bonds(const ppi_dev &d, const Proposal &P, const float *cpn, int cx, int cy, int cz, int &bo, int &bn, Acc &A) {
+__device__ __forceinline__ bool scan_move(const ppi_dev &d, const Proposal &P, const Cands &C, int total, int cx, const float *cpn, const float *img1, const BoxF &B,
+		NbSel &S, int &bo, int &bn, Acc &A) {
 	const ppi_rparams &rp = d.rp[P.r];
 	const ppi_grid &g = d.grid[P.r];
 	ppi_rstate *rs = d.rs + P.r;
-	const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
 	const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
 	const float rc2e = rp.sqr_rcut_f + eps, ovl = 1.f - eps;
+	const float rf2 = __fmul_rn(rp.sqr_rcut_f, LEARN_RF2_SCALE), loose = rf2 + LEARN_LOOSE;
 	const float4 pn = make_float4(P.po.x + P.disp.x, P.po.y + P.disp.y, P.po.z + P.disp.z, 0.f);
+	nb_clear(S);
 	bo = bn = 0;
+	int r = 0;
 #pragma unroll 1
-	for(int t = 0; t < 27; t++) {
-		const int dx = t % 3 - 1, dy = (t / 3) % 3 - 1, dz = t / 9 - 1;
-		const int cell = rp.cell_base + (wrapi(cz + dz, nz) * ny + wrapi(cy + dy, ny)) * nx + wrapi(cx + dx, nx);
-		const float ox = dx * g.wf[0], oy = dy * g.wf[1], oz = dz * g.wf[2];
-		const int j1 = d.cell_start[cell + 1];
-		for(int jq = d.cell_start[cell]; jq < j1; jq++) {
-			if(jq == P.i) continue;
-			const float4 qa = d.spos[jq];
-			const float dxo = (qa.x - P.po.x) + ox, dyo = (qa.y - P.po.y) + oy, dzo = (qa.z - P.po.z) + oz;
-			const float dxn = (qa.x - pn.x) + ox, dyn = (qa.y - pn.y) + oy, dzn = (qa.z - pn.z) + oz;
-			const float r2o = fmaf(dxo, dxo, fmaf(dyo, dyo, dzo * dzo)), r2n = fmaf(dxn, dxn, fmaf(dyn, dyn, dzn * dzn));
-			A.pairs += 2;
-			if(MODE != MODE_AUDIT && r2n < ovl) return false;
-			if(!(MODE == MODE_AUDIT || r2o < rc2e || r2n < rc2e)) continue;
-			const float4 qb = d.sori[3 * (size_t) jq], qc = d.sori[3 * (size_t) jq + 1], qd = d.sori[3 * (size_t) jq + 2];
-			const float cq[9] = { qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w, qd.x };
-			const int qslot = __float_as_int(qd.w);
-			const int clo = pair_state<MODE>(d.rec, rp, rs, g.inv_L, P.pslot, 0, P.q, P.disp, qslot, dxo, dyo, dzo, P.cpo, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0.,
-					A.fallbacks);
-			const int cln = pair_state<MODE>(d.rec, rp, rs, g.inv_L, P.pslot, 1, P.q, P.disp, qslot, dxn, dyn, dzn, cpn, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0.,
-					A.fallbacks);
+	for(int c0 = 0; c0 < total; c0 += LBATCH) {
+		int jq[LBATCH], rr[LBATCH];
+#pragma unroll
+		for(int u = 0; u < LBATCH; u++) {
+			jq[u] = c0 + u < total ? cand_at(C, c0 + u, r) : -1;
+			rr[u] = r >> 1;
+		}
+		float4 qa[LBATCH];
+#pragma unroll
+		for(int u = 0; u < LBATCH; u++) qa[u] = jq[u] >= 0 ? d.spos[jq[u]] : make_float4(1e30f, 1e30f, 1e30f, 0.f);
+		float go[LBATCH][3], gn[LBATCH][3];
+		bool feat[LBATCH], pair[LBATCH];
+#pragma unroll
+		for(int u = 0; u < LBATCH; u++) {
+			const float ox = cell_dx(__float_as_int(qa[u].w), cx, g.n[0]) * g.wf[0], oy = (rr[u] % 3 - 1) * g.wf[1], oz = (rr[u] / 3 - 1) * g.wf[2];
+			go[u][0] = (qa[u].x - P.po.x) + ox, go[u][1] = (qa[u].y - P.po.y) + oy, go[u][2] = (qa[u].z - P.po.z) + oz;
+			gn[u][0] = (qa[u].x - pn.x) + ox, gn[u][1] = (qa[u].y - pn.y) + oy, gn[u][2] = (qa[u].z - pn.z) + oz;
+			const float r2o = fmaf(go[u][0], go[u][0], fmaf(go[u][1], go[u][1], go[u][2] * go[u][2]));
+			const float r2n = fmaf(gn[u][0], gn[u][0], fmaf(gn[u][1], gn[u][1], gn[u][2] * gn[u][2]));
+			const bool live = jq[u] >= 0 && jq[u] != P.i;
+			if(live) A.pairs += 2;
+			if(MODE != MODE_AUDIT && live && r2n < ovl) return false;
+			feat[u] = live && r2n < loose;
+			pair[u] = live && (MODE == MODE_AUDIT || r2o < rc2e || r2n < rc2e);
+		}
+		float4 qp[LBATCH], qb[LBATCH], qc[LBATCH], qd[LBATCH];
+#pragma unroll
+		for(int u = 0; u < LBATCH; u++) {
+			if(feat[u]) qp[u] = d.simg[LIMG * (size_t) jq[u]];
+			if(pair[u]) {
+				qb[u] = d.sori[3 * (size_t) jq[u]];
+				qc[u] = d.sori[3 * (size_t) jq[u] + 1];
+				qd[u] = d.sori[3 * (size_t) jq[u] + 2];
+			}
+		}
+#pragma unroll
+		for(int u = 0; u < LBATCH; u++) {
+			if(feat[u]) nb_consider(qp[u], jq[u], img1, B, rf2, S);
+			if(!pair[u]) continue;
+			const float cq[9] = { qb[u].x, qb[u].y, qb[u].z, qb[u].w, qc[u].x, qc[u].y, qc[u].z, qc[u].w, qd[u].x };
+			const int qslot = __float_as_int(qd[u].w);
+			const int clo = pair_state<MODE>(d.rec, rp, rs, g.inv_L, P.pslot, 0, P.q, P.disp, qslot, go[u][0], go[u][1], go[u][2], P.cpo, cq, rp.sqr_rcut_f, rp.cosmax_f,
+					rp.base_f, eps, -1, 1., 0., A.fallbacks);
+			const int cln = pair_state<MODE>(d.rec, rp, rs, g.inv_L, P.pslot, 1, P.q, P.disp, qslot, gn[u][0], gn[u][1], gn[u][2], cpn, cq, rp.sqr_rcut_f, rp.cosmax_f,
+					rp.base_f, eps, -1, 1., 0., A.fallbacks);
 			if(cln == CL_OVER) return false;
 			bo += (clo == CL_BOND);
 			bn += (cln == CL_BOND);
 		}
 	}
 	return true;
-}
-
-/* edges and angles of the four components for replica parameters rp */
-__device__ __forceinline__ void mix_scales(const ppi_rparams &rp, const ppi_learn &L, float *a, float *t) {
-#pragma unroll
-	for(int k = 0; k < PPI_MIX; k++) {
-		a[k] = k == 0 ? rp.disp_max_f : __fmul_rn(rp.disp_max_f, L.sdisp[k]);
-		t[k] = fminf(k == 0 ? rp.theta_max_f : __fmul_rn(rp.theta_max_f, L.stheta[k]), PI_BELOW);
-	}
 }
 
 /* move of component k from two Philox blocks: displacement (rd.x, rd.y, rd.z), angle rd.w, axis (ra.x, ra.y);
@@ -1558,35 +1669,31 @@ __device__ __forceinline__ void mix_draw(float a, float t, U4 rd, U4 ra, float3 
 	q = make_float4(ch, sh * sr * cph, sh * sr * sp, sh * zc);
 }
 
-/* sum_k pi_k c_k of a move (FP64) */
-__device__ __forceinline__ double mix_density(const float *pi, const float *a, const float *t, float3 dsp, float theta) {
+/* sum_k pi_k c_k of a move (FP64; the component densities of the replica precomputed, ppi_lrep) */
+__device__ __forceinline__ double mix_density(const float *pi, const ppi_lrep &M, float3 dsp, float theta) {
 	const float m = fmaxf(fabsf(dsp.x), fmaxf(fabsf(dsp.y), fabsf(dsp.z)));
 	double s = 0.;
 #pragma unroll
 	for(int k = 0; k < PPI_MIX; k++)
-		if(m <= 0.5f * a[k] && theta < t[k]) {
-			const double ak = (double) a[k];
-			s += (double) pi[k] / (ak * ak * ak * (double) t[k]);
-		}
+		if(m <= 0.5f * M.a[k] && theta < M.t[k]) s = fma((double) pi[k], M.v[k], s);
 	return s;
 }
 
-/* canonical state of slot ps after the move (dq, disp): commit_move's FP64 operations, then R0 . Q(q') */
-__device__ __forceinline__ void moved_image(const ppi_dev &d, int ps, float4 dq, float3 disp, const double *box, float *img) {
+/* canonical state of the mover after the move (dq, disp): commit_move's FP64 operations, then its image */
+__device__ __forceinline__ void moved_image(const ppi_dev &d, int ps, int id, float4 dq, float3 disp, const double *box, float *img) {
 	const double *rec = d.rec + (size_t) ps * PPI_REC;
 	const double qv[4] = { rec[PPI_Q], rec[PPI_Q + 1], rec[PPI_Q + 2], rec[PPI_Q + 3] };
 	const double b[4] = { f2d(dq.x), f2d(dq.y), f2d(dq.z), f2d(dq.w) };
-	double qn[4], R0[9], R[9];
+	double qn[4], R0[9];
 #pragma unroll
 	for(int c = 0; c < 4; c++) qn[c] = qcomp64(qv[c], qv[c ^ 1], qv[c ^ 2], qv[c ^ 3], b, c);
 	const double rn[3] = { __dadd_rn(rec[0], f2d(disp.x)), __dadd_rn(rec[1], f2d(disp.y)), __dadd_rn(rec[2], f2d(disp.z)) };
 #pragma unroll
 	for(int k = 0; k < 9; k++) R0[k] = rec[PPI_R0 + k];
-	orient64_ops(R0, qn, R);
-	canon_image(rn, R, box, img);
+	canon_image(rn, qn, R0, box, id, img);
 }
 
-/* the mover of a list entry: particle choice (draw x), working record, canonical image, cell */
+/* the mover of a list entry: particle choice (draw), working record, canonical image, cell */
 __device__ __forceinline__ void learn_mover(const ppi_dev &d, const int4 ent, uint32_t draw, Proposal &P, float *img, int &cx, int &cy, int &cz) {
 	P.r = ent.w;
 	const ppi_rparams &rp = d.rp[P.r];
@@ -1595,11 +1702,11 @@ __device__ __forceinline__ void learn_mover(const ppi_dev &d, const int4 ent, ui
 	P.i = ent.y + (int) __umulhi(draw, (uint32_t) ent.z);
 	P.po = d.spos[P.i];
 	const float4 ob = d.sori[3 * (size_t) P.i], oc = d.sori[3 * (size_t) P.i + 1], od = d.sori[3 * (size_t) P.i + 2];
+	load_image(d.simg, P.i, img);
 	P.pslot = __float_as_int(od.w);
 	P.cpo[0] = ob.x, P.cpo[1] = ob.y, P.cpo[2] = ob.z, P.cpo[3] = ob.w;
 	P.cpo[4] = oc.x, P.cpo[5] = oc.y, P.cpo[6] = oc.z, P.cpo[7] = oc.w;
 	P.cpo[8] = od.x;
-	load_image(d.wimg, P.pslot, img);
 	cx = P.local % g.n[0];
 	cy = (P.local / g.n[0]) % g.n[1];
 	cz = P.local / (g.n[0] * g.n[1]);
@@ -1610,13 +1717,40 @@ __device__ __forceinline__ bool inside_cell(const ppi_grid &g, float4 po, float3
 	return nx >= 0.f && nx < g.wf[0] && ny >= 0.f && ny < g.wf[1] && nz >= 0.f && nz < g.wf[2];
 }
 
-/* One checkerboard colour of learned moves: 128 attempts per CTA tile, one per thread; the network runs
- * twice per tile on the tensor cores (current and candidate states). */
+/* warp-wide flush of the per-lane counters (one atomic per counter when the lanes share a replica) */
+__device__ __forceinline__ void flush_warp(const ppi_dev &d, Acc &A) {
+	const unsigned same = __match_any_sync(0xffffffffu, A.r);
+	if(same != 0xffffffffu || A.r < 0) {
+		flush_thread(d, A);
+		return;
+	}
+	const unsigned t = __reduce_add_sync(0xffffffffu, A.tries), ac = __reduce_add_sync(0xffffffffu, A.acc);
+	const unsigned p = __reduce_add_sync(0xffffffffu, A.pairs), f = __reduce_add_sync(0xffffffffu, A.fallbacks);
+	const int db = __reduce_add_sync(0xffffffffu, A.dbonds);
+	if((threadIdx.x & 31) == 0) {
+		ppi_rstate *rs = d.rs + A.r;
+		if(t) atomicAdd(&rs->tries[0], (unsigned long long) t);
+		if(ac) atomicAdd(&rs->accepted[0], (unsigned long long) ac);
+		if(p) atomicAdd(&rs->pairs, (unsigned long long) p);
+		if(f) atomicAdd(&rs->fallbacks, (unsigned long long) f);
+		if(db) atomicAdd((unsigned long long *) &rs->bonds, (unsigned long long) (long long) db);
+	}
+	A.tries = A.acc = A.pairs = A.fallbacks = 0;
+	A.dbonds = 0;
+}
+
+/* One checkerboard colour of learned moves: one warp per CTA, 32 attempts per tile (one per lane); the
+ * network runs twice per tile on the tensor cores (current and candidate states). */
 template <int MODE>
-__global__ void __launch_bounds__(MLP_ROWS) k_colour_learned(ppi_dev d, long long round, int col) {
+__global__ void __launch_bounds__(32) k_colour_learned(ppi_dev d, long long round, int col) {
+	const int4 *list = d.clist + (size_t) col * d.clist_cap;
+	int cnt = d.ccount[col];
+	if(cnt > d.clist_cap) cnt = d.clist_cap;
+	const int ntiles = (cnt + 31) / 32;
+	if((int) blockIdx.x >= ntiles) return; /* the whole CTA: no tensor memory taken */
 	extern __shared__ __align__(128) unsigned char smem_raw[];
-	MlpFwdSmem &S = *(MlpFwdSmem *) smem_raw;
-	mlp_fwd_begin(S, d.mlp_img);
+	MlpWarpSmem &S = *(MlpWarpSmem *) smem_raw;
+	mlpw_begin(S, d.mlp_img);
 	const ppi_learn L = *d.learn;
 	uint32_t phase = 0;
 	Acc A;
@@ -1624,19 +1758,16 @@ __global__ void __launch_bounds__(MLP_ROWS) k_colour_learned(ppi_dev d, long lon
 	A.tries = A.acc = A.pairs = A.fallbacks = 0;
 	A.dbonds = 0;
 	unsigned ctr[PPI_MIX] = { 0u, 0u, 0u, 0u }, cac[PPI_MIX] = { 0u, 0u, 0u, 0u };
-	const int4 *list = d.clist + (size_t) col * d.clist_cap;
-	int cnt = d.ccount[col];
-	if(cnt > d.clist_cap) cnt = d.clist_cap;
-	const int ntiles = (cnt + MLP_ROWS - 1) / MLP_ROWS;
 #pragma unroll 1
 	for(int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-		const int idx = tile * MLP_ROWS + threadIdx.x;
+		const int idx = tile * 32 + threadIdx.x;
 		bool live = idx < cnt;
 		Proposal P;
 		P.r = 0;
-		float img0[12], f[MLP_IN];
-		int cx = 0, cy = 0, cz = 0;
+		float img0[16], f[MLP_IN];
+		int cx = 0, cy = 0, cz = 0, total = 0;
 		U4 r1 = U4{ 0u, 0u, 0u, 0u };
+		Cands C;
 #pragma unroll
 		for(int e = 0; e < MLP_IN; e++) f[e] = 0.f;
 		if(live) {
@@ -1649,75 +1780,75 @@ __global__ void __launch_bounds__(MLP_ROWS) k_colour_learned(ppi_dev d, long lon
 				A.r = P.r;
 			}
 			A.tries++;
+			const ppi_grid &g = d.grid[P.r];
+			total = cands_build(d, rp, g, cx, cy, cz, C);
 			const BoxF B = box_f(d.rs[P.r].box);
 			NbSel sel;
-			nb_select(d, rp, d.grid[P.r], cx, cy, cz, P.i, P.po.x, P.po.y, P.po.z, img0, B, sel);
+			scan_features(d, rp, g, C, total, cx, P.i, P.po, img0, B, sel);
 			site_features(d, rp, img0, sel, B, f);
 		}
-		mlp_put_x(S, f);
-		float z[MLP_OUT], pi0[PPI_MIX], pi1[PPI_MIX], a[PPI_MIX], t[PPI_MIX];
-		mlp_forward_tile(S, &phase, z);
+		mlpw_put_x(S, f);
+		float z[MLP_OUT], pi0[PPI_MIX], pi1[PPI_MIX];
+		mlpw_forward(S, &phase, z);
 		mix_weights(z, L.floor0, pi0);
 		int comp = 0, bo = 0, bn = 0;
-		float theta = 0.f, img1[12], cpn[9];
-		if(live) {
-			const ppi_rparams &rp = d.rp[P.r];
-			mix_scales(rp, L, a, t);
-			const float uc = u01(r1.y);
-			float cum = pi0[0];
-			while(comp < PPI_MIX - 1 && uc >= cum) cum = __fadd_rn(cum, pi0[++comp]);
-			const U4 rd = rng(rp, round, P.r, TAG_LEARN, (uint32_t) P.local, 1u), ra = rng(rp, round, P.r, TAG_LEARN, (uint32_t) P.local, 2u);
-			mix_draw(a[comp], t[comp], rd, ra, P.disp, theta, P.q);
-			ctr[comp]++;
-			live = inside_cell(d.grid[P.r], P.po, P.disp);
-		}
-		if(live) {
-			cols_new(P.cpo, P.q, cpn);
-			live = move_bonds<MODE>(d, P, cpn, cx, cy, cz, bo, bn, A);
-		}
+		float theta = 0.f, img1[16], cpn[9];
 #pragma unroll
 		for(int e = 0; e < MLP_IN; e++) f[e] = 0.f;
 		if(live) {
 			const ppi_rparams &rp = d.rp[P.r];
-			const BoxF B = box_f(d.rs[P.r].box);
-			moved_image(d, P.pslot, P.q, P.disp, d.rs[P.r].box, img1);
-			NbSel sel;
-			nb_select(d, rp, d.grid[P.r], cx, cy, cz, P.i, P.po.x + P.disp.x, P.po.y + P.disp.y, P.po.z + P.disp.z, img1, B, sel);
-			site_features(d, rp, img1, sel, B, f);
+			const ppi_lrep &M = d.lrep[P.r];
+			const float uc = u01(r1.y);
+			float cum = pi0[0];
+			while(comp < PPI_MIX - 1 && uc >= cum) cum = __fadd_rn(cum, pi0[++comp]);
+			const U4 rd = rng(rp, round, P.r, TAG_LEARN, (uint32_t) P.local, 1u), ra = rng(rp, round, P.r, TAG_LEARN, (uint32_t) P.local, 2u);
+			mix_draw(M.a[comp], M.t[comp], rd, ra, P.disp, theta, P.q);
+			ctr[comp]++;
+			live = inside_cell(d.grid[P.r], P.po, P.disp);
+			if(live) {
+				const BoxF B = box_f(d.rs[P.r].box);
+				moved_image(d, P.pslot, __float_as_int(img0[3]), P.q, P.disp, d.rs[P.r].box, img1);
+				cols_new(P.cpo, P.q, cpn);
+				NbSel sel;
+				live = scan_move<MODE>(d, P, C, total, cx, cpn, img1, B, sel, bo, bn, A);
+				if(live) site_features(d, rp, img1, sel, B, f);
+			}
 		}
-		mlp_put_x(S, f);
-		mlp_forward_tile(S, &phase, z);
+		mlpw_put_x(S, f);
+		mlpw_forward(S, &phase, z);
 		mix_weights(z, L.floor0, pi1);
 		if(live) {
-			const ppi_rparams &rp = d.rp[P.r];
-			const double ratio = mix_density(pi1, a, t, P.disp, theta) / mix_density(pi0, a, t, P.disp, theta);
-			const double p = exp(-(double) (bo - bn) / rp.T) * ratio;
-			if(u01d(r1.z, r1.w) < p) {
+			const ppi_lrep &M = d.lrep[P.r];
+			const int dE = bo - bn;
+			const double bz = (dE >= -PPI_LEXP && dE <= PPI_LEXP) ? M.expk[dE + PPI_LEXP] : exp(-(double) dE / d.rp[P.r].T);
+			/* accept iff U < exp(-dE / T) q(x' -> x) / q(x -> x'), without the division */
+			if(u01d(r1.z, r1.w) * mix_density(pi0, M, P.disp, theta) < bz * mix_density(pi1, M, P.disp, theta)) {
 				commit_move(d, P.i, P.pslot, P.po, P.disp, P.q, cpn);
-				store_image(d.wimg, P.pslot, img1);
+				store_image(d.simg, P.i, img1);
 				A.acc++;
 				A.dbonds += bn - bo;
 				cac[comp]++;
 			}
 		}
 	}
-	flush_thread(d, A);
+	flush_warp(d, A);
 #pragma unroll
 	for(int k = 0; k < PPI_MIX; k++) {
 		const unsigned tk = __reduce_add_sync(0xffffffffu, ctr[k]), ak = __reduce_add_sync(0xffffffffu, cac[k]);
-		if((threadIdx.x & 31) == 0 && tk) {
+		if(threadIdx.x == 0 && tk) {
 			atomicAdd(d.lstats + k, (unsigned long long) tk);
 			if(ak) atomicAdd(d.lstats + PPI_MIX + k, (unsigned long long) ak);
 		}
 	}
-	mlp_fwd_end(S);
+	mlpw_end(S);
 	if(threadIdx.x == 0 && S.err) atomicExch(d.lerr, 1);
 }
 
 /* Training samples of the current state: row j of [base, base + count) takes list entry j * n / count of
  * colour col, its particle's features and, per component k, the mean over `draws` proposals of
- *     u_k = acc (|d|^2 / Disp_max^2 + angle^2 / Theta_max^2 + kappa |bonds_new - bonds_old|),
- * acc = min(1, exp(-dE / T)) for a candidate inside the cell without overlap, else 0. */
+ *     u_k = acc (kappa |bonds_new - bonds_old| + jump (|d|^2 / Disp_max^2 + angle^2 / Theta_max^2)),
+ * acc = min(1, exp(-dE / T)) for a candidate inside the cell without overlap, else 0 (the acceptance
+ * probability, not a coin: a smooth estimate). The four utilities are stored divided by the largest. */
 template <int MODE>
 __global__ void __launch_bounds__(128) k_learn_collect(ppi_dev d, long long snap, int col, int base, int count) {
 	const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1732,24 +1863,28 @@ __global__ void __launch_bounds__(128) k_learn_collect(ppi_dev d, long long snap
 	const ppi_learn L = *d.learn;
 	const int4 ent = d.clist[(size_t) col * d.clist_cap + (int) (((long long) j * cnt) / count)];
 	const ppi_rparams &rp = d.rp[ent.w];
+	const ppi_lrep &M = d.lrep[ent.w];
 	const U4 r1 = rng(rp, snap, ent.w, TAG_COLLECT, (uint32_t) (ent.x - rp.cell_base), 0u);
 	Proposal P;
-	float img0[12], f[MLP_IN];
+	float img0[16], f[MLP_IN];
 	int cx, cy, cz;
 	learn_mover(d, ent, r1.x, P, img0, cx, cy, cz);
+	const ppi_grid &g = d.grid[P.r];
+	Cands C;
+	const int total = cands_build(d, rp, g, cx, cy, cz, C);
 	const BoxF B = box_f(d.rs[P.r].box);
 	NbSel sel;
-	nb_select(d, rp, d.grid[P.r], cx, cy, cz, P.i, P.po.x, P.po.y, P.po.z, img0, B, sel);
+	scan_features(d, rp, g, C, total, cx, P.i, P.po, img0, B, sel);
 	site_features(d, rp, img0, sel, B, f);
 #pragma unroll
 	for(int e = 0; e < MLP_IN; e++) out[e] = f[e];
-	float a[PPI_MIX], t[PPI_MIX];
-	mix_scales(rp, L, a, t);
 	const float idm2 = 1.f / (rp.disp_max_f * rp.disp_max_f), ith2 = 1.f / (rp.theta_max_f * rp.theta_max_f);
 	Acc A;
 	A.r = -1;
 	A.tries = A.acc = A.pairs = A.fallbacks = 0;
 	A.dbonds = 0;
+	float uk[PPI_MIX];
+	float img1[16];
 #pragma unroll 1
 	for(int k = 0; k < PPI_MIX; k++) {
 		float u = 0.f;
@@ -1758,19 +1893,24 @@ __global__ void __launch_bounds__(128) k_learn_collect(ppi_dev d, long long snap
 			const uint32_t sub = 1u + 2u * (uint32_t) (k * L.draws + q);
 			const U4 rd = rng(rp, snap, P.r, TAG_COLLECT, (uint32_t) P.local, sub), ra = rng(rp, snap, P.r, TAG_COLLECT, (uint32_t) P.local, sub + 1u);
 			float theta;
-			mix_draw(a[k], t[k], rd, ra, P.disp, theta, P.q);
-			if(!inside_cell(d.grid[P.r], P.po, P.disp)) continue;
+			mix_draw(M.a[k], M.t[k], rd, ra, P.disp, theta, P.q);
+			if(!inside_cell(g, P.po, P.disp)) continue;
 			float cpn[9];
 			cols_new(P.cpo, P.q, cpn);
 			int bo, bn;
-			if(!move_bonds<MODE>(d, P, cpn, cx, cy, cz, bo, bn, A)) continue;
+			NbSel s2;
+			img1[0] = img1[1] = img1[2] = 0.f; /* the candidate's features are not needed here */
+			if(!scan_move<MODE>(d, P, C, total, cx, cpn, img1, B, s2, bo, bn, A)) continue;
 			const int dE = bo - bn;
-			const float acc = dE <= 0 ? 1.f : expf(-(float) dE / (float) rp.T);
+			const float acc = dE <= 0 ? 1.f : (float) ((dE <= PPI_LEXP) ? M.expk[dE + PPI_LEXP] : exp(-(double) dE / rp.T));
 			const float d2 = P.disp.x * P.disp.x + P.disp.y * P.disp.y + P.disp.z * P.disp.z;
-			u += acc * (d2 * idm2 + theta * theta * ith2 + L.kappa * (float) abs(bn - bo));
+			u += acc * (L.kappa * (float) abs(bn - bo) + L.jump * (d2 * idm2 + theta * theta * ith2));
 		}
-		out[MLP_IN + k] = L.draws > 0 ? u / (float) L.draws : 0.f;
+		uk[k] = u / (float) L.draws;
 	}
+	const float um = fmaxf(fmaxf(uk[0], uk[1]), fmaxf(uk[2], uk[3]));
+#pragma unroll
+	for(int k = 0; k < PPI_MIX; k++) out[MLP_IN + k] = um > 0.f ? uk[k] / um : 0.f;
 }
 
 /* features of the particle at every sorted position, stored by slot (d.feat[slot][36]) */
@@ -1785,30 +1925,32 @@ __global__ void k_learn_features(ppi_dev d) {
 	const int local = gc - rp.cell_base;
 	const int cx = local % g.n[0], cy = (local / g.n[0]) % g.n[1], cz = local / (g.n[0] * g.n[1]);
 	const float4 po = d.spos[k];
-	float img[12], f[MLP_IN];
-	load_image(d.wimg, slot, img);
+	float img[16], f[MLP_IN];
+	load_image(d.simg, k, img);
 	const BoxF B = box_f(d.rs[r].box);
+	Cands C;
+	const int total = cands_build(d, rp, g, cx, cy, cz, C);
 	NbSel sel;
-	nb_select(d, rp, g, cx, cy, cz, k, po.x, po.y, po.z, img, B, sel);
+	scan_features(d, rp, g, C, total, cx, k, po, img, B, sel);
 	site_features(d, rp, img, sel, B, f);
 	for(int e = 0; e < MLP_IN; e++) d.feat[(size_t) slot * MLP_IN + e] = f[e];
 }
 
-/* canonical images of every slot from the FP64 records and the current boxes */
+/* canonical images of every sorted position from the FP64 records and the current boxes */
 __global__ void k_canon(ppi_dev d) {
-	const int s = blockIdx.x * blockDim.x + threadIdx.x;
-	if(s >= d.ntot) return;
+	const int k = blockIdx.x * blockDim.x + threadIdx.x;
+	if(k >= d.ntot) return;
+	const int s = __float_as_int(d.sori[3 * (size_t) k + 2].w);
 	const double *rec = d.rec + (size_t) s * PPI_REC;
-	double q[4], R0[9], R[9];
+	double q[4], R0[9];
 	const double r[3] = { rec[0], rec[1], rec[2] };
 #pragma unroll
 	for(int c = 0; c < 4; c++) q[c] = rec[PPI_Q + c];
 #pragma unroll
-	for(int k = 0; k < 9; k++) R0[k] = rec[PPI_R0 + k];
-	orient64_ops(R0, q, R);
-	float img[12];
-	canon_image(r, R, d.rs[d.rep[s]].box, img);
-	store_image(d.wimg, s, img);
+	for(int j = 0; j < 9; j++) R0[j] = rec[PPI_R0 + j];
+	float img[16];
+	canon_image(r, q, R0, d.rs[d.rep[s]].box, d.id[s], img);
+	store_image(d.simg, k, img);
 }
 
 /* ------------------------------------------------------------------------------------------------ */
@@ -2761,15 +2903,15 @@ extern "C" int ppi_canon(const ppi_dev *d, cudaStream_t s, long long *nl) {
 	return (int) cudaGetLastError();
 }
 
-/* one wave of resident CTAs of a learned-move kernel (dynamic shared memory: the network's tile) */
+/* one wave of resident CTAs of a learned-move kernel (one warp each; dynamic shared memory: the
+ * network's tile; tensor memory: MLP_WARP_TMEM_COLS columns per CTA of the SM's 512) */
 template <typename F>
 static int learned_grid(F f, int *cache) {
 	if(*cache == 0) {
-		if(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sizeof(MlpFwdSmem)) != cudaSuccess) return -1;
+		if(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sizeof(MlpWarpSmem)) != cudaSuccess) return -1;
 		int nb = 0;
-		if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f, MLP_ROWS, sizeof(MlpFwdSmem)) != cudaSuccess || nb <= 0) nb = 1;
-		/* tensor memory: MLP_FWD_TMEM_COLS columns per CTA out of 512 per SM */
-		if(nb > 512 / MLP_FWD_TMEM_COLS) nb = 512 / MLP_FWD_TMEM_COLS;
+		if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f, 32, sizeof(MlpWarpSmem)) != cudaSuccess || nb <= 0) nb = 1;
+		if(nb > 512 / MLP_WARP_TMEM_COLS) nb = 512 / MLP_WARP_TMEM_COLS;
 		*cache = nb * ppi_sm_count();
 	}
 	return *cache;
@@ -2780,12 +2922,12 @@ extern "C" int ppi_round_learned(const ppi_dev *d, long long round, const int *c
 	if(audit || d->audit_any) {
 		const int grid = learned_grid(k_colour_learned<MODE_AUDIT>, &g_audit);
 		if(grid < 0) return (int) cudaGetLastError();
-		for(int ci = 0; ci < 8; ci++) k_colour_learned<MODE_AUDIT><<<grid, MLP_ROWS, sizeof(MlpFwdSmem), s>>>(*d, round, colours[ci]);
+		for(int ci = 0; ci < 8; ci++) k_colour_learned<MODE_AUDIT><<<grid, 32, sizeof(MlpWarpSmem), s>>>(*d, round, colours[ci]);
 	}
 	else {
 		const int grid = learned_grid(k_colour_learned<MODE_FAST>, &g_fast);
 		if(grid < 0) return (int) cudaGetLastError();
-		for(int ci = 0; ci < 8; ci++) k_colour_learned<MODE_FAST><<<grid, MLP_ROWS, sizeof(MlpFwdSmem), s>>>(*d, round, colours[ci]);
+		for(int ci = 0; ci < 8; ci++) k_colour_learned<MODE_FAST><<<grid, 32, sizeof(MlpWarpSmem), s>>>(*d, round, colours[ci]);
 	}
 	*nl += 8;
 	return (int) cudaGetLastError();

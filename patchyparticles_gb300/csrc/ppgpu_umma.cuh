@@ -21,6 +21,7 @@
 #define PPGPU_UMMA_CUH_
 
 #include <cuda_bf16.h>
+#include <stddef.h>
 #include <stdint.h>
 
 /* ---------------------------------------------------------------- network shape (fixed) */
@@ -296,6 +297,97 @@ __device__ __forceinline__ bool mlp_forward_tile(MlpFwdSmem &S, uint32_t *phase,
 	for(int e = 0; e < MLP_OUT; e++) z[e] = v[e] + S.b3[e];
 	tc_fence_before();
 	__syncthreads();
+	if(!ok) S.err = 1;
+	return ok;
+}
+
+/* ---------------------------------------------------------------- MLP forward, one warp and 32 rows */
+/* The move kernel runs one warp per CTA (32 attempts, one per lane) so that a colour of a few thousand
+ * attempts spreads over the whole GPU. The MMA is still M = 128: its A operand is a 128-row view whose
+ * rows 32..127 run on into the following buffers (their D rows are never read), and the warp reads
+ * tensor-memory lanes 0..31. D1, D2 and D3 reuse columns 0..63 (each is read before the next MMA). */
+struct __align__(128) MlpWarpSmem {
+	__nv_bfloat16 x[32 * MLP_K1];
+	__nv_bfloat16 h1[32 * MLP_HID];
+	__nv_bfloat16 h2[32 * MLP_HID];
+	unsigned char w[MLPI_FWD_BYTES];
+	float b1[MLP_HID], b2[MLP_HID], b3[MLP_N3];
+	uint64_t bar;
+	uint32_t tmem;
+	int err;
+};
+#define MLP_WARP_TMEM_COLS 64
+/* the 128-row A views of x, h1 and h2 stay inside the structure */
+static_assert(offsetof(MlpWarpSmem, x) + 128 * MLP_K1 * 2 <= sizeof(MlpWarpSmem), "x view");
+static_assert(offsetof(MlpWarpSmem, h1) + 128 * MLP_HID * 2 <= sizeof(MlpWarpSmem), "h1 view");
+static_assert(offsetof(MlpWarpSmem, h2) + 128 * MLP_HID * 2 <= sizeof(MlpWarpSmem), "h2 view");
+
+/* setup (the whole warp) */
+__device__ __forceinline__ void mlpw_begin(MlpWarpSmem &S, const unsigned char *img) {
+	const uint4 *src = (const uint4 *) img;
+	uint4 *dst = (uint4 *) S.w;
+	for(int i = threadIdx.x; i < MLPI_FWD_BYTES / 16; i += 32) dst[i] = src[i];
+	const float *bias = (const float *) (img + MLPI_BIAS);
+	for(int i = threadIdx.x; i < MLP_HID; i += 32) {
+		S.b1[i] = bias[i];
+		S.b2[i] = bias[MLP_HID + i];
+	}
+	if(threadIdx.x < MLP_N3) S.b3[threadIdx.x] = threadIdx.x < MLP_OUT ? bias[2 * MLP_HID + threadIdx.x] : 0.f;
+	if(threadIdx.x == 0) {
+		mbar_init(&S.bar, 1);
+		S.err = 0;
+	}
+	tmem_alloc(&S.tmem, MLP_WARP_TMEM_COLS);
+	tc_fence_before();
+	__syncwarp();
+	tc_fence_after();
+}
+
+__device__ __forceinline__ void mlpw_end(MlpWarpSmem &S) {
+	tc_fence_before();
+	__syncwarp();
+	tc_fence_after();
+	tmem_dealloc(S.tmem, MLP_WARP_TMEM_COLS);
+}
+
+__device__ __forceinline__ void mlpw_put_x(MlpWarpSmem &S, const float *f) {
+	float v[8];
+#pragma unroll
+	for(int c = 0; c < MLP_K1 / 8; c++) {
+#pragma unroll
+		for(int e = 0; e < 8; e++) v[e] = (8 * c + e < MLP_IN) ? f[8 * c + e] : 0.f;
+		store_row8(S.x, threadIdx.x, 8 * c, MLP_K1, v);
+	}
+}
+
+/* lane 0 issues D[0..63] = A . B^T and commits; the warp waits */
+__device__ __forceinline__ bool mlpw_mma(MlpWarpSmem &S, uint32_t *phase, const void *A, const void *B, int K, int N) {
+	fence_async_smem();
+	tc_fence_before();
+	__syncwarp();
+	tc_fence_after();
+	if(threadIdx.x == 0) {
+		umma_gemm(S.tmem, A, B, K, N);
+		umma_commit(&S.bar);
+	}
+	__syncwarp();
+	const bool ok = mbar_wait(&S.bar, *phase);
+	*phase ^= 1u;
+	tc_fence_after();
+	return ok;
+}
+
+/* logits of this lane's row (after every lane wrote its row with mlpw_put_x) */
+__device__ __forceinline__ bool mlpw_forward(MlpWarpSmem &S, uint32_t *phase, float *z) {
+	bool ok = mlpw_mma(S, phase, S.x, S.w + MLPI_W1, MLP_K1, MLP_HID);
+	mlp_hidden_epilogue(S.tmem, 0, S.b1, S.h1);
+	ok &= mlpw_mma(S, phase, S.h1, S.w + MLPI_W2, MLP_HID, MLP_HID);
+	mlp_hidden_epilogue(S.tmem, 0, S.b2, S.h2);
+	ok &= mlpw_mma(S, phase, S.h2, S.w + MLPI_W3, MLP_HID, MLP_N3);
+	float v[16];
+	tmem_ld16(tmem_lane_addr(S.tmem, 0), v);
+#pragma unroll
+	for(int e = 0; e < MLP_OUT; e++) z[e] = v[e] + S.b3[e];
 	if(!ok) S.err = 1;
 	return ok;
 }
