@@ -207,9 +207,11 @@ int pp_mlp_grad(const float *params, int n, const float *samples, double floor, 
  * Metropolis-Hastings with the reverse-move density, so the Boltzmann distribution is kept exactly.
  * The network is trained on the GPU (pp_gpu_learned_train) on samples of configurations generated by
  * the plain move (pp_gpu_learned_collect); per sample and component the utility is the mean over
- * `draws` proposals of acc (kappa |bond change| + jump (|d|^2 / Disp_max^2 + angle^2 / Theta_max^2)),
- * acc = min(1, exp(-dE / T)) (0 for an overlap or a move out of the cell), divided by the sample's
- * largest utility (so every environment's preference counts alike). */
+ * `draws` proposals of kappa |bond change| min(1, exp(-(dE - 1) / T)) + jump acc (|d|^2 / Disp_max^2 +
+ * angle^2 / Theta_max^2), acc = min(1, exp(-dE / T)) (0 for an overlap or a move out of the cell): how
+ * often the component proposes a change of the particle's bond count that is no less likely to be
+ * accepted than breaking one bond, with the squared jump as a tie-break; divided by the sample's largest
+ * utility (so every environment's preference counts alike). */
 #define PP_PROPOSAL_PLAIN 0
 #define PP_PROPOSAL_LEARNED 1
 #define PP_MIX 4

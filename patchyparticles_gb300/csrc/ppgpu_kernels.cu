@@ -1846,9 +1846,13 @@ __global__ void __launch_bounds__(32) k_colour_learned(ppi_dev d, long long roun
 
 /* Training samples of the current state: row j of [base, base + count) takes list entry j * n / count of
  * colour col, its particle's features and, per component k, the mean over `draws` proposals of
- *     u_k = acc (kappa |bonds_new - bonds_old| + jump (|d|^2 / Disp_max^2 + angle^2 / Theta_max^2)),
- * acc = min(1, exp(-dE / T)) for a candidate inside the cell without overlap, else 0 (the acceptance
- * probability, not a coin: a smooth estimate). The four utilities are stored divided by the largest. */
+ *     u_k = kappa |bonds_new - bonds_old| min(1, exp(-(dE - 1) / T)) + jump acc (|d|^2 / Disp_max^2 + angle^2 / Theta_max^2)
+ * for a candidate inside the cell without overlap (else 0), acc = min(1, exp(-dE / T)). The first term
+ * counts proposals that change the particle's bond count, weighted by their acceptance relative to that
+ * of breaking one bond: in a bonded network bond turnover is limited by breaking, which every component
+ * accepts with the same exp(-1 / T), so what a component adds is how often it proposes one. The second is
+ * a tie-break for particles without partners in reach (acceptance-weighted squared jump). The four
+ * utilities are stored divided by the largest. */
 template <int MODE>
 __global__ void __launch_bounds__(128) k_learn_collect(ppi_dev d, long long snap, int col, int base, int count) {
 	const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1903,8 +1907,9 @@ __global__ void __launch_bounds__(128) k_learn_collect(ppi_dev d, long long snap
 			if(!scan_move<MODE>(d, P, C, total, cx, cpn, img1, B, s2, bo, bn, A)) continue;
 			const int dE = bo - bn;
 			const float acc = dE <= 0 ? 1.f : (float) ((dE <= PPI_LEXP) ? M.expk[dE + PPI_LEXP] : exp(-(double) dE / rp.T));
+			const float acc1 = dE <= 1 ? 1.f : (float) ((dE - 1 <= PPI_LEXP) ? M.expk[dE - 1 + PPI_LEXP] : exp(-(double) (dE - 1) / rp.T));
 			const float d2 = P.disp.x * P.disp.x + P.disp.y * P.disp.y + P.disp.z * P.disp.z;
-			u += acc * (L.kappa * (float) abs(bn - bo) + L.jump * (d2 * idm2 + theta * theta * ith2));
+			u += L.kappa * (float) abs(bn - bo) * acc1 + L.jump * acc * (d2 * idm2 + theta * theta * ith2);
 		}
 		uk[k] = u / (float) L.draws;
 	}
