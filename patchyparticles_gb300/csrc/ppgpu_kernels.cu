@@ -1471,37 +1471,55 @@ __device__ __forceinline__ void nb_consider(float4 qp, int k, const float *pimg,
 	if(r2 < rf2) nb_insert(S, r2, __float_as_int(qp.w), k);
 }
 
-/* f[12 n + 3 m + c]: patch site m of neighbour n (centre + 0.5 patch direction, minimum image, relative
- * to the particle) in the particle's frame (component c = column c of its orientation . site); zero
- * for absent neighbours */
+/* the three features of patch site m of a neighbour with image q (centre + 0.5 patch direction, minimum
+ * image, relative to the particle with image pimg) in the particle's frame: component c = column c of
+ * its orientation . site */
+__device__ __forceinline__ void site_feature(const ppi_rparams &rp, const float *pimg, const float *q, int m, const BoxF &B, float *out) {
+	float dl[3];
+#pragma unroll
+	for(int a = 0; a < 3; a++) dl[a] = min_image(__fsub_rn(q[a], pimg[a]), B.L[a], B.iL[a]);
+	const float b0 = (float) rp.base[m][0], b1 = (float) rp.base[m][1], b2 = (float) rp.base[m][2];
+	float site[3];
+#pragma unroll
+	for(int a = 0; a < 3; a++) {
+		const float p = __fadd_rn(__fadd_rn(__fmul_rn(q[4 + 3 * a], b0), __fmul_rn(q[5 + 3 * a], b1)), __fmul_rn(q[6 + 3 * a], b2));
+		site[a] = __fadd_rn(dl[a], __fmul_rn(0.5f, p));
+	}
+#pragma unroll
+	for(int c = 0; c < 3; c++) out[c] = __fadd_rn(__fadd_rn(__fmul_rn(pimg[4 + c], site[0]), __fmul_rn(pimg[7 + c], site[1])), __fmul_rn(pimg[10 + c], site[2]));
+}
+
+/* f[12 n + 3 m + c]: patch site m of neighbour n in the particle's frame; zero for absent neighbours */
 __device__ __forceinline__ void site_features(const ppi_dev &d, const ppi_rparams &rp, const float *pimg, const NbSel &S, const BoxF &B, float *f) {
 	float q[LEARN_NB][16];
 #pragma unroll
 	for(int n = 0; n < LEARN_NB; n++)
 		if(S.pos[n] >= 0) load_image(d.simg, S.pos[n], q[n]); /* the three loads in flight together */
 #pragma unroll
-	for(int n = 0; n < LEARN_NB; n++) {
-		if(S.pos[n] < 0) {
-#pragma unroll
-			for(int e = 0; e < 12; e++) f[12 * n + e] = 0.f;
-			continue;
-		}
-		float dl[3];
-#pragma unroll
-		for(int a = 0; a < 3; a++) dl[a] = min_image(__fsub_rn(q[n][a], pimg[a]), B.L[a], B.iL[a]);
+	for(int n = 0; n < LEARN_NB; n++)
 #pragma unroll
 		for(int m = 0; m < 4; m++) {
-			const float b0 = (float) rp.base[m][0], b1 = (float) rp.base[m][1], b2 = (float) rp.base[m][2];
-			float site[3];
-#pragma unroll
-			for(int a = 0; a < 3; a++) {
-				const float p = __fadd_rn(__fadd_rn(__fmul_rn(q[n][4 + 3 * a], b0), __fmul_rn(q[n][5 + 3 * a], b1)), __fmul_rn(q[n][6 + 3 * a], b2));
-				site[a] = __fadd_rn(dl[a], __fmul_rn(0.5f, p));
-			}
-#pragma unroll
-			for(int c = 0; c < 3; c++)
-				f[12 * n + 3 * m + c] = __fadd_rn(__fadd_rn(__fmul_rn(pimg[4 + c], site[0]), __fmul_rn(pimg[7 + c], site[1])), __fmul_rn(pimg[10 + c], site[2]));
+			if(S.pos[n] >= 0) site_feature(rp, pimg, q[n], m, B, f + 12 * n + 3 * m);
+			else f[12 * n + 3 * m] = f[12 * n + 3 * m + 1] = f[12 * n + 3 * m + 2] = 0.f;
 		}
+}
+
+/* merge the selections of the G lanes of a group (butterfly; every lane ends with the group's result).
+ * The order (r^2, id) is total, so the result does not depend on how candidates were split. */
+template <int G>
+__device__ __forceinline__ void nb_merge(NbSel &S) {
+#pragma unroll
+	for(int o = 1; o < G; o <<= 1) {
+		NbSel T;
+#pragma unroll
+		for(int n = 0; n < LEARN_NB; n++) {
+			T.r2[n] = __shfl_xor_sync(0xffffffffu, S.r2[n], o);
+			T.key[n] = __shfl_xor_sync(0xffffffffu, S.key[n], o);
+			T.pos[n] = __shfl_xor_sync(0xffffffffu, S.pos[n], o);
+		}
+#pragma unroll
+		for(int n = 0; n < LEARN_NB; n++)
+			if(T.pos[n] >= 0) nb_insert(S, T.r2[n], T.key[n], T.pos[n]);
 	}
 }
 
@@ -1552,18 +1570,20 @@ __device__ __forceinline__ int cell_dx(int qx, int cx, int nx) {
 	return v > 1 ? v - nx : (v < -1 ? v + nx : v);
 }
 
-/* feature neighbours of the particle at sorted position self, cell-local position pl, image pimg */
+/* feature neighbours of the particle at sorted position self, cell-local position pl, image pimg: this
+ * lane takes candidates sub, sub + G, ... (G lanes per particle; merged with nb_merge<G>) */
+template <int G>
 __device__ __forceinline__ void scan_features(const ppi_dev &d, const ppi_rparams &rp, const ppi_grid &g, const Cands &C, int total, int cx, int self, float4 pl,
-		const float *pimg, const BoxF &B, NbSel &S) {
+		const float *pimg, const BoxF &B, NbSel &S, int sub) {
 	const float rf2 = __fmul_rn(rp.sqr_rcut_f, LEARN_RF2_SCALE), loose = rf2 + LEARN_LOOSE;
 	nb_clear(S);
 	int r = 0;
 #pragma unroll 1
-	for(int c0 = 0; c0 < total; c0 += LBATCH) {
+	for(int c0 = sub; c0 < total; c0 += G * LBATCH) {
 		int jq[LBATCH], rr[LBATCH];
 #pragma unroll
 		for(int u = 0; u < LBATCH; u++) {
-			jq[u] = c0 + u < total ? cand_at(C, c0 + u, r) : -1;
+			jq[u] = c0 + G * u < total ? cand_at(C, c0 + G * u, r) : -1;
 			rr[u] = r >> 1;
 		}
 		float4 qa[LBATCH];
@@ -1587,10 +1607,11 @@ __device__ __forceinline__ void scan_features(const ppi_dev &d, const ppi_rparam
 }
 
 /* One scan for the candidate state: bonds of the old (bo) and candidate (bn) state and the feature
- * neighbours of the candidate (image img1). False if the candidate overlaps. */
-template <int MODE>
+ * neighbours of the candidate (image img1) over this lane's candidates sub, sub + G, ... False if one of
+ * them overlaps the candidate state. */
+template <int MODE, int G>
 __device__ __forceinline__ bool scan_move(const ppi_dev &d, const Proposal &P, const Cands &C, int total, int cx, const float *cpn, const float *img1, const BoxF &B,
-		NbSel &S, int &bo, int &bn, Acc &A) {
+		NbSel &S, int &bo, int &bn, Acc &A, int sub) {
 	const ppi_rparams &rp = d.rp[P.r];
 	const ppi_grid &g = d.grid[P.r];
 	ppi_rstate *rs = d.rs + P.r;
@@ -1602,11 +1623,11 @@ __device__ __forceinline__ bool scan_move(const ppi_dev &d, const Proposal &P, c
 	bo = bn = 0;
 	int r = 0;
 #pragma unroll 1
-	for(int c0 = 0; c0 < total; c0 += LBATCH) {
+	for(int c0 = sub; c0 < total; c0 += G * LBATCH) {
 		int jq[LBATCH], rr[LBATCH];
 #pragma unroll
 		for(int u = 0; u < LBATCH; u++) {
-			jq[u] = c0 + u < total ? cand_at(C, c0 + u, r) : -1;
+			jq[u] = c0 + G * u < total ? cand_at(C, c0 + G * u, r) : -1;
 			rr[u] = r >> 1;
 		}
 		float4 qa[LBATCH];
@@ -1784,7 +1805,7 @@ __global__ void __launch_bounds__(32) k_colour_learned(ppi_dev d, long long roun
 			total = cands_build(d, rp, g, cx, cy, cz, C);
 			const BoxF B = box_f(d.rs[P.r].box);
 			NbSel sel;
-			scan_features(d, rp, g, C, total, cx, P.i, P.po, img0, B, sel);
+			scan_features<1>(d, rp, g, C, total, cx, P.i, P.po, img0, B, sel, 0);
 			site_features(d, rp, img0, sel, B, f);
 		}
 		mlpw_put_x(S, f);
@@ -1810,7 +1831,7 @@ __global__ void __launch_bounds__(32) k_colour_learned(ppi_dev d, long long roun
 				moved_image(d, P.pslot, __float_as_int(img0[3]), P.q, P.disp, d.rs[P.r].box, img1);
 				cols_new(P.cpo, P.q, cpn);
 				NbSel sel;
-				live = scan_move<MODE>(d, P, C, total, cx, cpn, img1, B, sel, bo, bn, A);
+				live = scan_move<MODE, 1>(d, P, C, total, cx, cpn, img1, B, sel, bo, bn, A, 0);
 				if(live) site_features(d, rp, img1, sel, B, f);
 			}
 		}
@@ -1878,7 +1899,7 @@ __global__ void __launch_bounds__(128) k_learn_collect(ppi_dev d, long long snap
 	const int total = cands_build(d, rp, g, cx, cy, cz, C);
 	const BoxF B = box_f(d.rs[P.r].box);
 	NbSel sel;
-	scan_features(d, rp, g, C, total, cx, P.i, P.po, img0, B, sel);
+	scan_features<1>(d, rp, g, C, total, cx, P.i, P.po, img0, B, sel, 0);
 	site_features(d, rp, img0, sel, B, f);
 #pragma unroll
 	for(int e = 0; e < MLP_IN; e++) out[e] = f[e];
@@ -1904,7 +1925,7 @@ __global__ void __launch_bounds__(128) k_learn_collect(ppi_dev d, long long snap
 			int bo, bn;
 			NbSel s2;
 			img1[0] = img1[1] = img1[2] = 0.f; /* the candidate's features are not needed here */
-			if(!scan_move<MODE>(d, P, C, total, cx, cpn, img1, B, s2, bo, bn, A)) continue;
+			if(!scan_move<MODE, 1>(d, P, C, total, cx, cpn, img1, B, s2, bo, bn, A, 0)) continue;
 			const int dE = bo - bn;
 			const float acc = dE <= 0 ? 1.f : (float) ((dE <= PPI_LEXP) ? M.expk[dE + PPI_LEXP] : exp(-(double) dE / rp.T));
 			const float acc1 = dE <= 1 ? 1.f : (float) ((dE - 1 <= PPI_LEXP) ? M.expk[dE - 1 + PPI_LEXP] : exp(-(double) (dE - 1) / rp.T));
@@ -1936,7 +1957,7 @@ __global__ void k_learn_features(ppi_dev d) {
 	Cands C;
 	const int total = cands_build(d, rp, g, cx, cy, cz, C);
 	NbSel sel;
-	scan_features(d, rp, g, C, total, cx, k, po, img, B, sel);
+	scan_features<1>(d, rp, g, C, total, cx, k, po, img, B, sel, 0);
 	site_features(d, rp, img, sel, B, f);
 	for(int e = 0; e < MLP_IN; e++) d.feat[(size_t) slot * MLP_IN + e] = f[e];
 }

@@ -132,11 +132,14 @@ static_assert(sizeof(((MlpTrainSmem *) 0)->dzt) + sizeof(((MlpTrainSmem *) 0)->b
 
 __device__ __forceinline__ void put_t(__nv_bfloat16 *M, int row, int col, float v) { M[cl_off(row, col, MLP_ROWS)] = __float2bfloat16_rn(v); }
 
-/* one commit + wait; false on timeout */
+/* one commit + wait; false on timeout (the CTA then stops issuing tensor-core work: S.err) */
 __device__ __forceinline__ bool tc_sync(MlpTrainSmem &S, uint32_t &phase) {
 	if(threadIdx.x == 0) umma_commit(&S.bar);
-	const bool ok = mbar_wait(&S.bar, phase);
+	bool ok = mbar_wait(&S.bar, phase);
 	phase ^= 1u;
+	if(!ok) S.err = 1;
+	__syncthreads();
+	ok = S.err == 0;
 	tc_fence_after();
 	return ok;
 }
@@ -234,7 +237,7 @@ __global__ void __launch_bounds__(MLP_ROWS, 1) k_mlp_train(const unsigned char *
 			for(int i = 0; i < MLP_K1; i++) put_t(S.bw, MLP_HID + i, t, i < MLP_IN ? f[i] : (i == MLP_IN ? 1.f : 0.f));
 		}
 		operands_ready();
-		if(t == 0) umma_gemm(tm + TT_D1, S.x, S.w + MLPI_W1, MLP_K1, MLP_HID);
+		if(t == 0 && !S.err) umma_gemm(tm + TT_D1, S.x, S.w + MLPI_W1, MLP_K1, MLP_HID);
 		ok &= tc_sync(S, phase);
 		/* layer-1 epilogue: H1 row, H1^T column, ReLU mask */
 		uint64_t mask1 = 0ull, mask2 = 0ull;
@@ -253,7 +256,7 @@ __global__ void __launch_bounds__(MLP_ROWS, 1) k_mlp_train(const unsigned char *
 			store_row8(S.h1, t, 16 * c + 8, MLP_HID, v + 8);
 		}
 		operands_ready();
-		if(t == 0) umma_gemm(tm + TT_D2, S.h1, S.w + MLPI_W2, MLP_HID, MLP_HID);
+		if(t == 0 && !S.err) umma_gemm(tm + TT_D2, S.h1, S.w + MLPI_W2, MLP_HID, MLP_HID);
 		ok &= tc_sync(S, phase);
 #pragma unroll
 		for(int c = 0; c < MLP_HID / 16; c++) {
@@ -272,7 +275,7 @@ __global__ void __launch_bounds__(MLP_ROWS, 1) k_mlp_train(const unsigned char *
 #pragma unroll
 		for(int i = MLP_HID; i < MLP_W3G_N; i++) put_t(S.b3m, i, t, i == MLP_HID ? 1.f : 0.f);
 		operands_ready();
-		if(t == 0) umma_gemm(tm + TT_D3, S.h2, S.w + MLPI_W3, MLP_HID, MLP_N3);
+		if(t == 0 && !S.err) umma_gemm(tm + TT_D3, S.h2, S.w + MLPI_W3, MLP_HID, MLP_N3);
 		ok &= tc_sync(S, phase);
 		float z[MLP_OUT], dz[MLP_OUT];
 		{
@@ -296,7 +299,7 @@ __global__ void __launch_bounds__(MLP_ROWS, 1) k_mlp_train(const unsigned char *
 			for(int e = 0; e < MLP_N3; e++) put_t(S.dzt, e, t, v[e]);
 		}
 		operands_ready();
-		if(t == 0) umma_gemm(tm + TT_D1, S.dz, S.w + MLPI_W3T, MLP_N3, MLP_HID);
+		if(t == 0 && !S.err) umma_gemm(tm + TT_D1, S.dz, S.w + MLPI_W3T, MLP_N3, MLP_HID);
 		ok &= tc_sync(S, phase);
 		/* dA2 = dH2 * relu'(a2): row (A of dH1) and column (weight-gradient A rows 0..63) */
 #pragma unroll
@@ -312,7 +315,7 @@ __global__ void __launch_bounds__(MLP_ROWS, 1) k_mlp_train(const unsigned char *
 			store_row8(S.da2, t, 16 * c + 8, MLP_HID, v + 8);
 		}
 		operands_ready();
-		if(t == 0) umma_gemm(tm + TT_D2, S.da2, S.w + MLPI_W2T, MLP_HID, MLP_HID);
+		if(t == 0 && !S.err) umma_gemm(tm + TT_D2, S.da2, S.w + MLPI_W2T, MLP_HID, MLP_HID);
 		ok &= tc_sync(S, phase);
 #pragma unroll
 		for(int c = 0; c < MLP_HID / 16; c++) {
@@ -322,7 +325,7 @@ __global__ void __launch_bounds__(MLP_ROWS, 1) k_mlp_train(const unsigned char *
 			for(int e = 0; e < 16; e++) put_t(S.aw, MLP_HID + 16 * c + e, t, ((mask1 >> (16 * c + e)) & 1ull) ? v[e] : 0.f);
 		}
 		operands_ready();
-		if(t == 0) {
+		if(t == 0 && !S.err) {
 			const uint32_t a = smem_u32(S.aw), b = smem_u32(S.bw), a3 = smem_u32(S.dzt), b3 = smem_u32(S.b3m);
 			const uint32_t idw = umma_idesc_bf16(128, MLP_WG_N), id3 = umma_idesc_bf16(128, MLP_W3G_N);
 			for(int k = 0; k < MLP_ROWS / 16; k++) {

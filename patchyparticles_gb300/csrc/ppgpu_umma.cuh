@@ -80,13 +80,16 @@ __device__ __forceinline__ uint64_t umma_sdesc(uint32_t saddr, uint32_t lbo, uin
 __device__ __forceinline__ uint64_t umma_kmajor(uint32_t saddr, int K) { return umma_sdesc(saddr, 128u, (uint32_t) (K >> 3) * 128u); }
 
 /* ---------------------------------------------------------------- tensor memory */
-/* executed by one whole warp; the allocated base address is written to *dst (shared memory) */
+/* executed by one whole warp (converged first: .sync.aligned); the allocated base address is written to
+ * *dst (shared memory) */
 __device__ __forceinline__ void tmem_alloc(uint32_t *dst, uint32_t ncols) {
+	__syncwarp();
 	asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)), "r"(ncols) : "memory");
 	asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
 }
 
 __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+	__syncwarp();
 	asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
 }
 
@@ -113,13 +116,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 	return ok != 0u;
 }
 
-#define UMMA_WAIT_LIMIT (1 << 22) /* try_wait rounds (each suspends for a hardware-chosen time) */
+#define UMMA_WAIT_CYCLES (1ll << 31) /* ~1 s at the SM clock: a wait that long has failed */
 
-/* wait for the phase with the given parity to complete; false when the limit expired */
+/* wait for the phase with the given parity to complete; false when the time limit expired. Lanes may
+ * leave the loop in different rounds: callers reconverge before any .sync.aligned instruction. */
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-	for(int it = 0; it < UMMA_WAIT_LIMIT; it++)
-		if(mbar_try_wait(bar, parity)) return true;
-	return false;
+	const long long t0 = clock64();
+	while(!mbar_try_wait(bar, parity))
+		if(clock64() - t0 > UMMA_WAIT_CYCLES) return false;
+	return true;
 }
 
 /* ---------------------------------------------------------------- MMA issue (one thread) */
@@ -145,9 +150,11 @@ __device__ __forceinline__ void umma_gemm(uint32_t d_tmem, const void *A, const 
 	for(int k = 0; k < K / 16; k++) umma_bf16(d_tmem, umma_kmajor(a + 256u * k, K), umma_kmajor(b + 256u * k, K), idesc, k > 0 ? 1u : 0u);
 }
 
-/* 16 consecutive FP32 columns of this thread's lane, the load completed before returning */
+/* 16 consecutive FP32 columns of this thread's lane, the load completed before returning (warp-collective:
+ * the warp reconverges first) */
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
 	uint32_t r[16];
+	__syncwarp();
 	asm volatile(
 			"tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];\n\t"
 			"tcgen05.wait::ld.sync.aligned;"
@@ -259,6 +266,11 @@ __device__ __forceinline__ bool mlp_forward_tile(MlpFwdSmem &S, uint32_t *phase,
 	bool ok = true;
 	fence_async_smem();
 	__syncthreads();
+	if(S.err) { /* an earlier wait expired: no further tensor-core work in this CTA */
+#pragma unroll
+		for(int e = 0; e < MLP_OUT; e++) z[e] = 0.f;
+		return false;
+	}
 	if(threadIdx.x == 0) {
 		tc_fence_after();
 		umma_gemm(t, S.x, S.w + MLPI_W1, MLP_K1, MLP_HID);
@@ -295,9 +307,9 @@ __device__ __forceinline__ bool mlp_forward_tile(MlpFwdSmem &S, uint32_t *phase,
 	tmem_ld16(tmem_lane_addr(t, 0), v);
 #pragma unroll
 	for(int e = 0; e < MLP_OUT; e++) z[e] = v[e] + S.b3[e];
+	if(!ok) S.err = 1;
 	tc_fence_before();
 	__syncthreads();
-	if(!ok) S.err = 1;
 	return ok;
 }
 
@@ -360,19 +372,24 @@ __device__ __forceinline__ void mlpw_put_x(MlpWarpSmem &S, const float *f) {
 	}
 }
 
-/* lane 0 issues D[0..63] = A . B^T and commits; the warp waits */
+/* lane 0 issues D[0..63] = A . B^T and commits; the warp waits. Once a wait has expired (S.err) the CTA
+ * issues no further tensor-core work and its results are void (the host reports the error). */
 __device__ __forceinline__ bool mlpw_mma(MlpWarpSmem &S, uint32_t *phase, const void *A, const void *B, int K, int N) {
 	fence_async_smem();
 	tc_fence_before();
 	__syncwarp();
 	tc_fence_after();
+	if(S.err) return false;
 	if(threadIdx.x == 0) {
 		umma_gemm(S.tmem, A, B, K, N);
 		umma_commit(&S.bar);
 	}
 	__syncwarp();
-	const bool ok = mbar_wait(&S.bar, *phase);
+	bool ok = mbar_wait(&S.bar, *phase);
+	ok = __all_sync(0xffffffffu, ok);
 	*phase ^= 1u;
+	if(!ok && threadIdx.x == 0) S.err = 1;
+	__syncwarp();
 	tc_fence_after();
 	return ok;
 }
@@ -387,8 +404,7 @@ __device__ __forceinline__ bool mlpw_forward(MlpWarpSmem &S, uint32_t *phase, fl
 	float v[16];
 	tmem_ld16(tmem_lane_addr(S.tmem, 0), v);
 #pragma unroll
-	for(int e = 0; e < MLP_OUT; e++) z[e] = v[e] + S.b3[e];
-	if(!ok) S.err = 1;
+	for(int e = 0; e < MLP_OUT; e++) z[e] = ok ? v[e] + S.b3[e] : 0.f;
 	return ok;
 }
 
