@@ -286,6 +286,11 @@ def run_gpu(args, wl, ws, rank, local, dist):
         e2e = {"value": att_e2e / el, "unit": UNIT, "h2d_bytes_per_step": N * (128 + 4), "d2h_bytes_per_step": N * (96 + 4),
                "sweeps_per_step": args.e2e_sweeps, "steps": e2e_steps}
 
+    learned = None
+    if rank == 0 and ws == 1 and not args.no_learned:
+        e.close()
+        learned = learned_comparison(args)
+
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -313,8 +318,99 @@ def run_gpu(args, wl, ws, rank, local, dist):
         "e2e": e2e,
         "cpu_baseline": cpu,
         "gpu_launches": launches,
+        "learned": learned,
     }
     print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- learned proposal vs plain (N=32768, T=0.09)
+def _acf_particles(B):
+    """Autocorrelation of per-particle bond counts B[t][i] (the per-time mean over particles removed, so a
+    slow drift of the whole system does not count as correlation)."""
+    d = B.astype(np.float64)
+    d -= d.mean(axis=1, keepdims=True)
+    T = d.shape[0]
+    f = np.fft.rfft(d, 2 * T, axis=0)
+    a = np.fft.irfft(f * np.conj(f), axis=0)[:T].sum(axis=1)
+    a /= np.arange(T, 0, -1)
+    return a / a[0]
+
+
+def _tau_sokal(acf, c=5.0):
+    tau = 1.0
+    for M in range(1, len(acf)):
+        tau = 1 + 2 * acf[1:M + 1].sum()
+        if M >= c * tau:
+            return tau, M, False
+    return tau, len(acf), True
+
+
+def _chain(e, sweeps, every, learned):
+    """Per-particle bond counts every `every` sweeps; device time of the sweeps only."""
+    import patchyparticles_gb300 as pp
+
+    e.set_proposal(learned)
+    N = e.num_particles()
+    n = sweeps // every
+    B = np.zeros((n, N), dtype=np.int8)
+    ms = 0.0
+    for k in range(n):
+        ms += e.time_sweeps(every)
+        nb, _ = e.bonds()
+        B[k] = nb
+    acf = _acf_particles(B)
+    lags = np.arange(1, min(6, len(acf)))
+    # initial decorrelation: C(k every) ~ 1 - k every / tau for an exponential autocorrelation
+    slope = float(np.polyfit(lags * every, 1.0 - acf[lags], 1)[0]) if len(lags) >= 2 else float("nan")
+    tau_exp = 1.0 / slope if slope > 0 else float("inf")
+    tau_w, win, limited = _tau_sokal(acf)
+    ms_sweep = ms / sweeps
+    sps = 1000.0 / ms_sweep
+    out = {"ms_per_sweep": ms_sweep, "sweeps": sweeps, "snapshot_every": every,
+           "bonds_per_particle": [float(B[0].mean() / 2), float(B[-1].mean() / 2)],
+           "bond_change_rate_per_sweep": float((B[1:] != B[:-1]).mean() / every),
+           "tau_exp_sweeps": tau_exp, "tau_int_window_sweeps": tau_w * every, "tau_window_limited": bool(limited),
+           "ess_per_s": N * sps / (2.0 * tau_exp)}
+    if learned:
+        t, a = e.learned_stats(reset=True)
+        tt = max(1, sum(t))
+        out["component_share"] = [x / tt for x in t]
+        out["component_acceptance"] = [a[k] / max(1, t[k]) for k in range(len(t))]
+    return out
+
+
+def learned_comparison(args):
+    """The learned proposal against the plain move at N=32768, rho=0.1, T=0.09: the network is trained on
+    the GPU on samples of configurations generated by the plain move, then both chains run from the same
+    configuration; effective samples/s of the per-particle bond count = N x sweeps/s / (2 tau), tau from the
+    initial decay of its autocorrelation (the windowed estimate is reported too: at T=0.09 the chains age
+    and a run of bench length does not reach the window)."""
+    import patchyparticles_gb300 as pp
+
+    wl = WORKLOADS["c4"]
+    r, R, box = make_config(wl)
+    e = pp.Engine(pp.default_params(temperature=wl["T"], disp_max=wl["disp"], theta_max=wl["theta"], seed=wl["seed"]))
+    e.upload(r, R, box)
+    e.learned_init(seed=7)
+    t0 = time.perf_counter()
+    e.learned_collect(args.learn_configs, args.learn_sweeps_between, 128)
+    t1 = time.perf_counter()
+    obj = e.learned_train(args.learn_epochs, lr=3e-3)
+    e.sync()
+    t2 = time.perf_counter()
+    r0, R0, b0 = e.download()
+    res = {"workload": "N=32768 NVT rho=0.1 T=0.09 KF_delta=0.12 KF_cosmax=0.92, Disp_max=0.05, Theta_max=0.1 (plain component)",
+           "training": {"configs": args.learn_configs, "sweeps_between": args.learn_sweeps_between, "samples": args.learn_configs * 128,
+                        "epochs": args.learn_epochs, "objective": obj, "collect_s": t1 - t0, "train_s": t2 - t1,
+                        "network": "36-64-64-4 ReLU, BF16 tcgen05 GEMMs, FP32 accumulation"}}
+    for name, learned in (("plain", False), ("learned", True)):
+        e.upload(r0, R0, b0)
+        e.learned_stats(reset=True)
+        res[name] = _chain(e, args.learn_measure_sweeps, 40, learned)
+    e.close()
+    res["ess_ratio"] = res["learned"]["ess_per_s"] / res["plain"]["ess_per_s"]
+    res["per_sweep_ratio"] = res["plain"]["tau_exp_sweeps"] / res["learned"]["tau_exp_sweeps"]
+    return res
 
 
 def _max_op(dist):
@@ -342,6 +438,11 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-plain effective-sample comparison")
+    ap.add_argument("--learn-configs", type=int, default=10000)
+    ap.add_argument("--learn-sweeps-between", type=int, default=5)
+    ap.add_argument("--learn-epochs", type=int, default=30)
+    ap.add_argument("--learn-measure-sweeps", type=int, default=16000)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
