@@ -1760,6 +1760,145 @@ __device__ __forceinline__ void flush_warp(const ppi_dev &d, Acc &A) {
 	A.dbonds = 0;
 }
 
+/* Per-lane candidate cache of the learned colour kernel (shared memory, [slot][lane] so that a warp's
+ * accesses to one slot are conflict-free): the scans gather the working-record positions of up to LCAP
+ * candidates, then the canonical positions of the close ones and the orientations of the bonding-range
+ * ones, each batch with asynchronous copies that are all in flight together (one memory latency per
+ * batch instead of one per candidate). */
+#define LCAP 16
+#define LPB 4 /* pairs per orientation batch */
+#define LEARN_CACHE_OFF ((sizeof(MlpWarpSmem) + 127) / 128 * 128)
+#define LEARN_SMEM (LEARN_CACHE_OFF + sizeof(LearnCache))
+struct __align__(16) LearnCache {
+	float4 pos[LCAP][32];
+	float4 img[LCAP][32];
+	float4 ori[LPB][3][32];
+	int jq[LCAP][32]; /* sorted position << 4 | row (0..8) */
+};
+
+/* gathers the working-record positions of candidates c0 .. c0 + n - 1 of this lane */
+__device__ __forceinline__ void cache_positions(const ppi_dev &d, LearnCache &K, const Cands &C, int c0, int n, int &r) {
+	const int l = threadIdx.x;
+	for(int k = 0; k < n; k++) {
+		const int jq = cand_at(C, c0 + k, r);
+		K.jq[k][l] = (jq << 4) | (r >> 1);
+		cp_async16(&K.pos[k][l], d.spos + jq);
+	}
+	cp_async_wait_all();
+}
+
+/* feature neighbours of the current state from the cache (see scan_features) */
+__device__ __forceinline__ int scan_features_cached(const ppi_dev &d, LearnCache &K, const ppi_rparams &rp, const ppi_grid &g, const Cands &C, int total, int cx, int self,
+		float4 pl, const float *pimg, const BoxF &B, NbSel &S) {
+	const int l = threadIdx.x;
+	const float rf2 = __fmul_rn(rp.sqr_rcut_f, LEARN_RF2_SCALE), loose = rf2 + LEARN_LOOSE;
+	nb_clear(S);
+	int r = 0, last = 0;
+	for(int c0 = 0; c0 < total; c0 += LCAP) {
+		const int n = min(LCAP, total - c0);
+		cache_positions(d, K, C, c0, n, r);
+		last = n;
+		unsigned near = 0u;
+		for(int k = 0; k < n; k++) {
+			const float4 qa = K.pos[k][l];
+			const int e = K.jq[k][l], jq = e >> 4, rr = e & 15;
+			const float ox = cell_dx(__float_as_int(qa.w), cx, g.n[0]) * g.wf[0], oy = (rr % 3 - 1) * g.wf[1], oz = (rr / 3 - 1) * g.wf[2];
+			const float ex = (qa.x - pl.x) + ox, ey = (qa.y - pl.y) + oy, ez = (qa.z - pl.z) + oz;
+			if(jq != self && fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < loose) {
+				near |= 1u << k;
+				cp_async16(&K.img[k][l], d.simg + LIMG * (size_t) jq);
+			}
+		}
+		cp_async_wait_all();
+		while(near) {
+			const int k = __ffs(near) - 1;
+			near &= near - 1u;
+			nb_consider(K.img[k][l], K.jq[k][l] >> 4, pimg, B, rf2, S);
+		}
+	}
+	return total <= LCAP ? last : -1; /* candidates still in the cache (all of them), or -1 */
+}
+
+/* bonds of the old and candidate state and the candidate's feature neighbours from the cache (see
+ * scan_move); cached = number of candidates the feature scan left in the cache (-1: reload) */
+template <int MODE>
+__device__ __forceinline__ bool scan_move_cached(const ppi_dev &d, LearnCache &K, const Proposal &P, const Cands &C, int total, int cached, int cx, const float *cpn,
+		const float *img1, const BoxF &B, NbSel &S, int &bo, int &bn, Acc &A) {
+	const int l = threadIdx.x;
+	const ppi_rparams &rp = d.rp[P.r];
+	const ppi_grid &g = d.grid[P.r];
+	ppi_rstate *rs = d.rs + P.r;
+	const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
+	const float rc2e = rp.sqr_rcut_f + eps, ovl = 1.f - eps;
+	const float rf2 = __fmul_rn(rp.sqr_rcut_f, LEARN_RF2_SCALE), loose = rf2 + LEARN_LOOSE;
+	const float4 pn = make_float4(P.po.x + P.disp.x, P.po.y + P.disp.y, P.po.z + P.disp.z, 0.f);
+	nb_clear(S);
+	bo = bn = 0;
+	int r = 0;
+	for(int c0 = 0; c0 < total; c0 += LCAP) {
+		const int n = min(LCAP, total - c0);
+		if(cached < 0) cache_positions(d, K, C, c0, n, r);
+		unsigned feat = 0u, pair = 0u;
+		for(int k = 0; k < n; k++) {
+			const float4 qa = K.pos[k][l];
+			const int e = K.jq[k][l], jq = e >> 4, rr = e & 15;
+			if(jq == P.i) continue;
+			const float ox = cell_dx(__float_as_int(qa.w), cx, g.n[0]) * g.wf[0], oy = (rr % 3 - 1) * g.wf[1], oz = (rr / 3 - 1) * g.wf[2];
+			const float dxo = (qa.x - P.po.x) + ox, dyo = (qa.y - P.po.y) + oy, dzo = (qa.z - P.po.z) + oz;
+			const float dxn = (qa.x - pn.x) + ox, dyn = (qa.y - pn.y) + oy, dzn = (qa.z - pn.z) + oz;
+			const float r2o = fmaf(dxo, dxo, fmaf(dyo, dyo, dzo * dzo)), r2n = fmaf(dxn, dxn, fmaf(dyn, dyn, dzn * dzn));
+			A.pairs += 2;
+			if(MODE != MODE_AUDIT && r2n < ovl) {
+				cp_async_wait_all();
+				return false;
+			}
+			if(r2n < loose) {
+				feat |= 1u << k;
+				cp_async16(&K.img[k][l], d.simg + LIMG * (size_t) jq);
+			}
+			if(MODE == MODE_AUDIT || r2o < rc2e || r2n < rc2e) pair |= 1u << k;
+		}
+		cp_async_wait_all();
+		while(feat) {
+			const int k = __ffs(feat) - 1;
+			feat &= feat - 1u;
+			nb_consider(K.img[k][l], K.jq[k][l] >> 4, img1, B, rf2, S);
+		}
+		/* pair tests, LPB orientation gathers in flight at a time */
+		while(pair) {
+			int ks[LPB], nb = 0;
+			while(pair && nb < LPB) {
+				ks[nb] = __ffs(pair) - 1;
+				pair &= pair - 1u;
+				const int jq = K.jq[ks[nb]][l] >> 4;
+#pragma unroll
+				for(int c = 0; c < 3; c++) cp_async16(&K.ori[nb][c][l], d.sori + 3 * (size_t) jq + c);
+				nb++;
+			}
+			cp_async_wait_all();
+			for(int b = 0; b < nb; b++) {
+				const int k = ks[b];
+				const float4 qa = K.pos[k][l];
+				const int rr = K.jq[k][l] & 15;
+				const float ox = cell_dx(__float_as_int(qa.w), cx, g.n[0]) * g.wf[0], oy = (rr % 3 - 1) * g.wf[1], oz = (rr / 3 - 1) * g.wf[2];
+				const float dxo = (qa.x - P.po.x) + ox, dyo = (qa.y - P.po.y) + oy, dzo = (qa.z - P.po.z) + oz;
+				const float dxn = (qa.x - pn.x) + ox, dyn = (qa.y - pn.y) + oy, dzn = (qa.z - pn.z) + oz;
+				const float4 qb = K.ori[b][0][l], qc = K.ori[b][1][l], qd = K.ori[b][2][l];
+				const float cq[9] = { qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w, qd.x };
+				const int qslot = __float_as_int(qd.w);
+				const int clo = pair_state<MODE>(d.rec, rp, rs, g.inv_L, P.pslot, 0, P.q, P.disp, qslot, dxo, dyo, dzo, P.cpo, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1.,
+						0., A.fallbacks);
+				const int cln = pair_state<MODE>(d.rec, rp, rs, g.inv_L, P.pslot, 1, P.q, P.disp, qslot, dxn, dyn, dzn, cpn, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0.,
+						A.fallbacks);
+				if(cln == CL_OVER) return false;
+				bo += (clo == CL_BOND);
+				bn += (cln == CL_BOND);
+			}
+		}
+	}
+	return true;
+}
+
 /* One checkerboard colour of learned moves: one warp per CTA, 32 attempts per tile (one per lane); the
  * network runs twice per tile on the tensor cores (current and candidate states). */
 template <int MODE>
@@ -1771,6 +1910,7 @@ __global__ void __launch_bounds__(32) k_colour_learned(ppi_dev d, long long roun
 	if((int) blockIdx.x >= ntiles) return; /* the whole CTA: no tensor memory taken */
 	extern __shared__ __align__(128) unsigned char smem_raw[];
 	MlpWarpSmem &S = *(MlpWarpSmem *) smem_raw;
+	LearnCache &K = *(LearnCache *) (smem_raw + LEARN_CACHE_OFF);
 	mlpw_begin(S, d.mlp_img);
 	const ppi_learn L = *d.learn;
 	uint32_t phase = 0;
@@ -1786,7 +1926,7 @@ __global__ void __launch_bounds__(32) k_colour_learned(ppi_dev d, long long roun
 		Proposal P;
 		P.r = 0;
 		float img0[16], f[MLP_IN];
-		int cx = 0, cy = 0, cz = 0, total = 0;
+		int cx = 0, cy = 0, cz = 0, total = 0, cached = -1;
 		U4 r1 = U4{ 0u, 0u, 0u, 0u };
 		Cands C;
 #pragma unroll
@@ -1805,7 +1945,7 @@ __global__ void __launch_bounds__(32) k_colour_learned(ppi_dev d, long long roun
 			total = cands_build(d, rp, g, cx, cy, cz, C);
 			const BoxF B = box_f(d.rs[P.r].box);
 			NbSel sel;
-			scan_features<1>(d, rp, g, C, total, cx, P.i, P.po, img0, B, sel, 0);
+			cached = scan_features_cached(d, K, rp, g, C, total, cx, P.i, P.po, img0, B, sel);
 			site_features(d, rp, img0, sel, B, f);
 		}
 		mlpw_put_x(S, f);
@@ -1831,7 +1971,7 @@ __global__ void __launch_bounds__(32) k_colour_learned(ppi_dev d, long long roun
 				moved_image(d, P.pslot, __float_as_int(img0[3]), P.q, P.disp, d.rs[P.r].box, img1);
 				cols_new(P.cpo, P.q, cpn);
 				NbSel sel;
-				live = scan_move<MODE, 1>(d, P, C, total, cx, cpn, img1, B, sel, bo, bn, A, 0);
+				live = scan_move_cached<MODE>(d, K, P, C, total, cached, cx, cpn, img1, B, sel, bo, bn, A);
 				if(live) site_features(d, rp, img1, sel, B, f);
 			}
 		}
@@ -2934,9 +3074,9 @@ extern "C" int ppi_canon(const ppi_dev *d, cudaStream_t s, long long *nl) {
 template <typename F>
 static int learned_grid(F f, int *cache) {
 	if(*cache == 0) {
-		if(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sizeof(MlpWarpSmem)) != cudaSuccess) return -1;
+		if(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) LEARN_SMEM) != cudaSuccess) return -1;
 		int nb = 0;
-		if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f, 32, sizeof(MlpWarpSmem)) != cudaSuccess || nb <= 0) nb = 1;
+		if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f, 32, LEARN_SMEM) != cudaSuccess || nb <= 0) nb = 1;
 		if(nb > 512 / MLP_WARP_TMEM_COLS) nb = 512 / MLP_WARP_TMEM_COLS;
 		*cache = nb * ppi_sm_count();
 	}
@@ -2948,12 +3088,12 @@ extern "C" int ppi_round_learned(const ppi_dev *d, long long round, const int *c
 	if(audit || d->audit_any) {
 		const int grid = learned_grid(k_colour_learned<MODE_AUDIT>, &g_audit);
 		if(grid < 0) return (int) cudaGetLastError();
-		for(int ci = 0; ci < 8; ci++) k_colour_learned<MODE_AUDIT><<<grid, 32, sizeof(MlpWarpSmem), s>>>(*d, round, colours[ci]);
+		for(int ci = 0; ci < 8; ci++) k_colour_learned<MODE_AUDIT><<<grid, 32, LEARN_SMEM, s>>>(*d, round, colours[ci]);
 	}
 	else {
 		const int grid = learned_grid(k_colour_learned<MODE_FAST>, &g_fast);
 		if(grid < 0) return (int) cudaGetLastError();
-		for(int ci = 0; ci < 8; ci++) k_colour_learned<MODE_FAST><<<grid, 32, sizeof(MlpWarpSmem), s>>>(*d, round, colours[ci]);
+		for(int ci = 0; ci < 8; ci++) k_colour_learned<MODE_FAST><<<grid, 32, LEARN_SMEM, s>>>(*d, round, colours[ci]);
 	}
 	*nl += 8;
 	return (int) cudaGetLastError();

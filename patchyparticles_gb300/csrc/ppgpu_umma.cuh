@@ -334,11 +334,15 @@ static_assert(offsetof(MlpWarpSmem, x) + 128 * MLP_K1 * 2 <= sizeof(MlpWarpSmem)
 static_assert(offsetof(MlpWarpSmem, h1) + 128 * MLP_HID * 2 <= sizeof(MlpWarpSmem), "h1 view");
 static_assert(offsetof(MlpWarpSmem, h2) + 128 * MLP_HID * 2 <= sizeof(MlpWarpSmem), "h2 view");
 
+/* 16-byte asynchronous global -> shared copies (each thread waits for its own) */
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc) {
+	asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(smem_dst)), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 /* setup (the whole warp) */
 __device__ __forceinline__ void mlpw_begin(MlpWarpSmem &S, const unsigned char *img) {
-	const uint4 *src = (const uint4 *) img;
-	uint4 *dst = (uint4 *) S.w;
-	for(int i = threadIdx.x; i < MLPI_FWD_BYTES / 16; i += 32) dst[i] = src[i];
+	for(int i = threadIdx.x; i < MLPI_FWD_BYTES / 16; i += 32) cp_async16(S.w + 16 * i, img + 16 * i);
 	const float *bias = (const float *) (img + MLPI_BIAS);
 	for(int i = threadIdx.x; i < MLP_HID; i += 32) {
 		S.b1[i] = bias[i];
@@ -350,6 +354,7 @@ __device__ __forceinline__ void mlpw_begin(MlpWarpSmem &S, const unsigned char *
 		S.err = 0;
 	}
 	tmem_alloc(&S.tmem, MLP_WARP_TMEM_COLS);
+	cp_async_wait_all();
 	tc_fence_before();
 	__syncwarp();
 	tc_fence_after();
