@@ -439,6 +439,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-plain effective-sample comparison")
+    ap.add_argument("--learned-only", action="store_true", help="run only the learned-vs-plain comparison (one JSON object)")
     ap.add_argument("--learn-configs", type=int, default=10000)
     ap.add_argument("--learn-sweeps-between", type=int, default=5)
     ap.add_argument("--learn-epochs", type=int, default=30)
@@ -450,6 +451,11 @@ def main():
     ws, rank, local, dist = dist_setup()
     if args.impl == "reference":
         run_reference(args, wl, ws, rank, dist)
+    elif args.learned_only:
+        from patchyparticles_gb300 import build
+
+        build.build()
+        print(json.dumps({"learned": learned_comparison(args)}), flush=True)
     else:
         run_gpu(args, wl, ws, rank, local, dist)
     if dist is not None:
