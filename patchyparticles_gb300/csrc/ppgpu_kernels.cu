@@ -3076,7 +3076,15 @@ static int learned_grid(F f, int *cache) {
 	if(*cache == 0) {
 		if(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) LEARN_SMEM) != cudaSuccess) return -1;
 		int nb = 0;
-		if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f, 32, LEARN_SMEM) != cudaSuccess || nb <= 0) nb = 1;
+		if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f, 32, LEARN_SMEM) != cudaSuccess || nb <= 1) {
+			/* the shared-memory bound from the device limits (a grid beyond residency only queues) */
+			int dev = 0, smem_sm = 0;
+			cudaGetLastError();
+			cudaGetDevice(&dev);
+			cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+			nb = smem_sm / (int) (LEARN_SMEM + 1024);
+			if(nb < 1) nb = 1;
+		}
 		if(nb > 512 / MLP_WARP_TMEM_COLS) nb = 512 / MLP_WARP_TMEM_COLS;
 		*cache = nb * ppi_sm_count();
 	}
