@@ -391,7 +391,7 @@ def learned_comparison(args):
     r, R, box = make_config(wl)
     e = pp.Engine(pp.default_params(temperature=wl["T"], disp_max=wl["disp"], theta_max=wl["theta"], seed=wl["seed"]))
     e.upload(r, R, box)
-    e.learned_init(seed=7)
+    e.learned_init(seed=7, **json.loads(args.learn_params))
     t0 = time.perf_counter()
     e.learned_collect(args.learn_configs, args.learn_sweeps_between, 128)
     t1 = time.perf_counter()
@@ -441,6 +441,7 @@ def main():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-plain effective-sample comparison")
     ap.add_argument("--learned-only", action="store_true", help="run only the learned-vs-plain comparison (one JSON object)")
     ap.add_argument("--learn-configs", type=int, default=10000)
+    ap.add_argument("--learn-params", default="{}", help="JSON overrides of pp_learned_params (e.g. {\"jump\": 1e-3})")
     ap.add_argument("--learn-sweeps-between", type=int, default=5)
     ap.add_argument("--learn-epochs", type=int, default=30)
     ap.add_argument("--learn-measure-sweeps", type=int, default=16000)

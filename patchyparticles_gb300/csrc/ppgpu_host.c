@@ -1224,7 +1224,7 @@ int pp_generate(int N, double density, int seed, int round_like_file, double *r,
 /* ------------------------------------------------------------------------------------------------ */
 void pp_default_learned_params(pp_learned_params *p) {
 	memset(p, 0, sizeof(*p));
-	const double sd[PP_MIX] = { 1., 3., 8., 8. }, st[PP_MIX] = { 1., 3., 8., 25. };
+	const double sd[PP_MIX] = { 1., 4., 8., 8. }, st[PP_MIX] = { 1., 4., 8., 25. };
 	for(int k = 0; k < PP_MIX; k++) {
 		p->scale_disp[k] = sd[k];
 		p->scale_theta[k] = st[k];

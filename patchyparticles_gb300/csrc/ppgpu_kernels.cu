@@ -913,6 +913,24 @@ __device__ __forceinline__ void commit_move(const ppi_dev &d, int i, int pslot, 
 	((float *) (d.sori + 3 * (size_t) i + 2))[0] = cpn[8];
 }
 
+/* commit_move with the mover's FP64 record already in registers (rec = its 16 doubles) */
+__device__ __forceinline__ void commit_from(const ppi_dev &d, const double *rec, int i, int pslot, float4 po, float3 disp, float4 q, const float *cpn) {
+	double *out = d.rec + (size_t) pslot * PPI_REC;
+	const double qv[4] = { rec[PPI_Q], rec[PPI_Q + 1], rec[PPI_Q + 2], rec[PPI_Q + 3] };
+	const double b[4] = { f2d(q.x), f2d(q.y), f2d(q.z), f2d(q.w) };
+	double qn[4];
+#pragma unroll
+	for(int c = 0; c < 4; c++) qn[c] = qcomp64(qv[c], qv[c ^ 1], qv[c ^ 2], qv[c ^ 3], b, c);
+	*(double2 *) out = make_double2(__dadd_rn(rec[0], f2d(disp.x)), __dadd_rn(rec[1], f2d(disp.y)));
+	*(double2 *) (out + 2) = make_double2(__dadd_rn(rec[2], f2d(disp.z)), qn[0]);
+	*(double2 *) (out + 4) = make_double2(qn[1], qn[2]);
+	out[6] = qn[3];
+	d.spos[i] = make_float4(po.x + disp.x, po.y + disp.y, po.z + disp.z, po.w);
+	d.sori[3 * (size_t) i] = make_float4(cpn[0], cpn[1], cpn[2], cpn[3]);
+	d.sori[3 * (size_t) i + 1] = make_float4(cpn[4], cpn[5], cpn[6], cpn[7]);
+	((float *) (d.sori + 3 * (size_t) i + 2))[0] = cpn[8];
+}
+
 /* Metropolis on dE = -(bn - bo) (MC.c:330-339) */
 __device__ __forceinline__ bool metropolis(const ppi_rparams &rp, long long round, int r, int local, int bo, int bn) {
 	const int dE = bo - bn; /* E = -bonds */
@@ -1701,8 +1719,7 @@ __device__ __forceinline__ double mix_density(const float *pi, const ppi_lrep &M
 }
 
 /* canonical state of the mover after the move (dq, disp): commit_move's FP64 operations, then its image */
-__device__ __forceinline__ void moved_image(const ppi_dev &d, int ps, int id, float4 dq, float3 disp, const double *box, float *img) {
-	const double *rec = d.rec + (size_t) ps * PPI_REC;
+__device__ __forceinline__ void moved_image(const double *rec, int id, float4 dq, float3 disp, const double *box, float *img) {
 	const double qv[4] = { rec[PPI_Q], rec[PPI_Q + 1], rec[PPI_Q + 2], rec[PPI_Q + 3] };
 	const double b[4] = { f2d(dq.x), f2d(dq.y), f2d(dq.z), f2d(dq.w) };
 	double qn[4], R0[9];
@@ -1771,10 +1788,50 @@ __device__ __forceinline__ void flush_warp(const ppi_dev &d, Acc &A) {
 #define LEARN_SMEM (LEARN_CACHE_OFF + sizeof(LearnCache))
 struct __align__(16) LearnCache {
 	float4 pos[LCAP][32];
-	float4 img[LCAP][32];
+	float4 img[LCAP][LIMG][32]; /* canonical images of the close candidates */
 	float4 ori[LPB][3][32];
-	int jq[LCAP][32]; /* sorted position << 4 | row (0..8) */
+	double2 rec[PPI_REC / 2][32]; /* the mover's FP64 record */
+	int jq[LCAP][32];             /* sorted position << 4 | row (0..8) */
 };
+
+/* all four float4 of the canonical image of sorted position jq into cache slot k */
+__device__ __forceinline__ void cache_image(const ppi_dev &d, LearnCache &K, int k, int jq) {
+	const int l = threadIdx.x;
+#pragma unroll
+	for(int c = 0; c < LIMG; c++) cp_async16(&K.img[k][c][l], d.simg + LIMG * (size_t) jq + c);
+}
+
+/* features from the images the scan left in the cache (ncached candidates of its last chunk); a
+ * neighbour outside it (scans of more than LCAP candidates) is read from global memory */
+__device__ __forceinline__ void site_features_cached(const ppi_dev &d, const LearnCache &K, int ncached, const ppi_rparams &rp, const float *pimg, const NbSel &S, const BoxF &B,
+		float *f) {
+	const int l = threadIdx.x;
+#pragma unroll
+	for(int n = 0; n < LEARN_NB; n++) {
+		if(S.pos[n] < 0) {
+#pragma unroll
+			for(int e = 0; e < 12; e++) f[12 * n + e] = 0.f;
+			continue;
+		}
+		int slot = -1;
+		for(int k = 0; k < ncached; k++)
+			if((K.jq[k][l] >> 4) == S.pos[n]) {
+				slot = k;
+				break;
+			}
+		float q[16];
+		if(slot >= 0) {
+#pragma unroll
+			for(int c = 0; c < LIMG; c++) {
+				const float4 v = K.img[slot][c][l];
+				q[4 * c] = v.x, q[4 * c + 1] = v.y, q[4 * c + 2] = v.z, q[4 * c + 3] = v.w;
+			}
+		}
+		else load_image(d.simg, S.pos[n], q);
+#pragma unroll
+		for(int m = 0; m < 4; m++) site_feature(rp, pimg, q, m, B, f + 12 * n + 3 * m);
+	}
+}
 
 /* gathers the working-record positions of candidates c0 .. c0 + n - 1 of this lane */
 __device__ __forceinline__ void cache_positions(const ppi_dev &d, LearnCache &K, const Cands &C, int c0, int n, int &r) {
@@ -1789,7 +1846,7 @@ __device__ __forceinline__ void cache_positions(const ppi_dev &d, LearnCache &K,
 
 /* feature neighbours of the current state from the cache (see scan_features) */
 __device__ __forceinline__ int scan_features_cached(const ppi_dev &d, LearnCache &K, const ppi_rparams &rp, const ppi_grid &g, const Cands &C, int total, int cx, int self,
-		float4 pl, const float *pimg, const BoxF &B, NbSel &S) {
+		float4 pl, const float *pimg, const BoxF &B, NbSel &S, int *ncached) {
 	const int l = threadIdx.x;
 	const float rf2 = __fmul_rn(rp.sqr_rcut_f, LEARN_RF2_SCALE), loose = rf2 + LEARN_LOOSE;
 	nb_clear(S);
@@ -1806,16 +1863,17 @@ __device__ __forceinline__ int scan_features_cached(const ppi_dev &d, LearnCache
 			const float ex = (qa.x - pl.x) + ox, ey = (qa.y - pl.y) + oy, ez = (qa.z - pl.z) + oz;
 			if(jq != self && fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < loose) {
 				near |= 1u << k;
-				cp_async16(&K.img[k][l], d.simg + LIMG * (size_t) jq);
+				cache_image(d, K, k, jq);
 			}
 		}
 		cp_async_wait_all();
 		while(near) {
 			const int k = __ffs(near) - 1;
 			near &= near - 1u;
-			nb_consider(K.img[k][l], K.jq[k][l] >> 4, pimg, B, rf2, S);
+			nb_consider(K.img[k][0][l], K.jq[k][l] >> 4, pimg, B, rf2, S);
 		}
 	}
+	*ncached = last;
 	return total <= LCAP ? last : -1; /* candidates still in the cache (all of them), or -1 */
 }
 
@@ -1823,7 +1881,7 @@ __device__ __forceinline__ int scan_features_cached(const ppi_dev &d, LearnCache
  * scan_move); cached = number of candidates the feature scan left in the cache (-1: reload) */
 template <int MODE>
 __device__ __forceinline__ bool scan_move_cached(const ppi_dev &d, LearnCache &K, const Proposal &P, const Cands &C, int total, int cached, int cx, const float *cpn,
-		const float *img1, const BoxF &B, NbSel &S, int &bo, int &bn, Acc &A) {
+		const float *img1, const BoxF &B, NbSel &S, int &bo, int &bn, Acc &A, int *ncached) {
 	const int l = threadIdx.x;
 	const ppi_rparams &rp = d.rp[P.r];
 	const ppi_grid &g = d.grid[P.r];
@@ -1835,9 +1893,11 @@ __device__ __forceinline__ bool scan_move_cached(const ppi_dev &d, LearnCache &K
 	nb_clear(S);
 	bo = bn = 0;
 	int r = 0;
+	*ncached = 0;
 	for(int c0 = 0; c0 < total; c0 += LCAP) {
 		const int n = min(LCAP, total - c0);
 		if(cached < 0) cache_positions(d, K, C, c0, n, r);
+		*ncached = n;
 		unsigned feat = 0u, pair = 0u;
 		for(int k = 0; k < n; k++) {
 			const float4 qa = K.pos[k][l];
@@ -1854,7 +1914,7 @@ __device__ __forceinline__ bool scan_move_cached(const ppi_dev &d, LearnCache &K
 			}
 			if(r2n < loose) {
 				feat |= 1u << k;
-				cp_async16(&K.img[k][l], d.simg + LIMG * (size_t) jq);
+				cache_image(d, K, k, jq);
 			}
 			if(MODE == MODE_AUDIT || r2o < rc2e || r2n < rc2e) pair |= 1u << k;
 		}
@@ -1862,7 +1922,7 @@ __device__ __forceinline__ bool scan_move_cached(const ppi_dev &d, LearnCache &K
 		while(feat) {
 			const int k = __ffs(feat) - 1;
 			feat &= feat - 1u;
-			nb_consider(K.img[k][l], K.jq[k][l] >> 4, img1, B, rf2, S);
+			nb_consider(K.img[k][0][l], K.jq[k][l] >> 4, img1, B, rf2, S);
 		}
 		/* pair tests, LPB orientation gathers in flight at a time */
 		while(pair) {
@@ -1945,8 +2005,12 @@ __global__ void __launch_bounds__(32) k_colour_learned(ppi_dev d, long long roun
 			total = cands_build(d, rp, g, cx, cy, cz, C);
 			const BoxF B = box_f(d.rs[P.r].box);
 			NbSel sel;
-			cached = scan_features_cached(d, K, rp, g, C, total, cx, P.i, P.po, img0, B, sel);
-			site_features(d, rp, img0, sel, B, f);
+			/* the mover's FP64 record, in flight while the features are formed */
+#pragma unroll
+			for(int c = 0; c < PPI_REC / 2; c++) cp_async16(&K.rec[c][threadIdx.x], d.rec + (size_t) P.pslot * PPI_REC + 2 * c);
+			int nc = 0;
+			cached = scan_features_cached(d, K, rp, g, C, total, cx, P.i, P.po, img0, B, sel, &nc);
+			site_features_cached(d, K, nc, rp, img0, sel, B, f);
 		}
 		mlpw_put_x(S, f);
 		float z[MLP_OUT], pi0[PPI_MIX], pi1[PPI_MIX];
@@ -1954,6 +2018,7 @@ __global__ void __launch_bounds__(32) k_colour_learned(ppi_dev d, long long roun
 		mix_weights(z, L.floor0, pi0);
 		int comp = 0, bo = 0, bn = 0;
 		float theta = 0.f, img1[16], cpn[9];
+		double recl[PPI_REC];
 #pragma unroll
 		for(int e = 0; e < MLP_IN; e++) f[e] = 0.f;
 		if(live) {
@@ -1968,11 +2033,19 @@ __global__ void __launch_bounds__(32) k_colour_learned(ppi_dev d, long long roun
 			live = inside_cell(d.grid[P.r], P.po, P.disp);
 			if(live) {
 				const BoxF B = box_f(d.rs[P.r].box);
-				moved_image(d, P.pslot, __float_as_int(img0[3]), P.q, P.disp, d.rs[P.r].box, img1);
+				cp_async_wait_all();
+#pragma unroll
+				for(int c = 0; c < PPI_REC / 2; c++) {
+					const double2 v = K.rec[c][threadIdx.x];
+					recl[2 * c] = v.x;
+					recl[2 * c + 1] = v.y;
+				}
+				moved_image(recl, __float_as_int(img0[3]), P.q, P.disp, d.rs[P.r].box, img1);
 				cols_new(P.cpo, P.q, cpn);
 				NbSel sel;
-				live = scan_move_cached<MODE>(d, K, P, C, total, cached, cx, cpn, img1, B, sel, bo, bn, A);
-				if(live) site_features(d, rp, img1, sel, B, f);
+				int nc = 0;
+				live = scan_move_cached<MODE>(d, K, P, C, total, cached, cx, cpn, img1, B, sel, bo, bn, A, &nc);
+				if(live) site_features_cached(d, K, nc, rp, img1, sel, B, f);
 			}
 		}
 		mlpw_put_x(S, f);
@@ -1984,13 +2057,14 @@ __global__ void __launch_bounds__(32) k_colour_learned(ppi_dev d, long long roun
 			const double bz = (dE >= -PPI_LEXP && dE <= PPI_LEXP) ? M.expk[dE + PPI_LEXP] : exp(-(double) dE / d.rp[P.r].T);
 			/* accept iff U < exp(-dE / T) q(x' -> x) / q(x -> x'), without the division */
 			if(u01d(r1.z, r1.w) * mix_density(pi0, M, P.disp, theta) < bz * mix_density(pi1, M, P.disp, theta)) {
-				commit_move(d, P.i, P.pslot, P.po, P.disp, P.q, cpn);
+				commit_from(d, recl, P.i, P.pslot, P.po, P.disp, P.q, cpn);
 				store_image(d.simg, P.i, img1);
 				A.acc++;
 				A.dbonds += bn - bo;
 				cac[comp]++;
 			}
 		}
+		cp_async_wait_all(); /* no copy of this tile may land in the next tile's buffers */
 	}
 	flush_warp(d, A);
 #pragma unroll
