@@ -229,6 +229,7 @@ def run_gpu(args, wl, ws, rank, local, dist):
     e = pp.Engine(prm)
     e.upload(r, R, box)
     spsw = args.sweeps_per_step
+    tune = e.autotune(args.tune_sweeps) if args.tune_sweeps > 0 else None  # schedule choice, before the timed region
     # warm-up
     for _ in range(args.warmup):
         e.sweeps(spsw)
@@ -306,7 +307,8 @@ def run_gpu(args, wl, ws, rank, local, dist):
         "dtype": "f32+f64", "data": "synthetic (seeded random insertion, uniform orientations)",
         "config": {"workload": wl["name"], "N": wl["N"], "sweeps_per_step": spsw, "proposal": "plain",
                    "l2": "inputs larger than L2 (FP64 state %.0f MB + FP32 mirror %.0f MB per GPU)" % (wl["N"] * 128 / 1e6, wl["N"] * 64 / 1e6),
-                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+                   "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "schedule": tune if tune else "defaults (resort_every 4, reorder_every 16, cell_scale 1.0)"},
         "acceptance": acc[pp.MOVE_ROTO_TRASL] / max(1, tries[pp.MOVE_ROTO_TRASL]),
         "volume_acceptance": acc[pp.MOVE_VOLUME] / max(1, tries[pp.MOVE_VOLUME]) if tries[pp.MOVE_VOLUME] else None,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -439,6 +441,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-plain effective-sample comparison")
+    ap.add_argument("--tune-sweeps", type=int, default=10, help="sweeps per autotuner trial before the run (0: default schedule)")
     ap.add_argument("--learned-only", action="store_true", help="run only the learned-vs-plain comparison (one JSON object)")
     ap.add_argument("--learn-configs", type=int, default=10000)
     ap.add_argument("--learn-params", default="{}", help="JSON overrides of pp_learned_params (e.g. {\"jump\": 1e-3})")

@@ -257,6 +257,25 @@ int pp_gpu_learned_features(pp_engine *e, int replica, float *features);
 /* Attempts and acceptances of learned moves per mixture component since the last reset (all replicas). */
 int pp_gpu_learned_stats(pp_engine *e, long long tries[PP_MIX], long long accepted[PP_MIX], int reset);
 
+/* ------------------------------------------------------------------ autotuner */
+/* Chooses the engine's schedule on the live system by timing it: the checkerboard rounds between cell-grid
+ * re-sorts (2, 4, 8, 16), the re-sorts between physical reorders of the FP64 state (4, 16, 64) and the cell
+ * edge as a multiple of its minimum (1.0, 1.2, 1.5: the cell occupancy, hence attempts per round and
+ * neighbours per attempt). Each candidate runs 2 + trial_sweeps ordinary sweeps (they are part of the
+ * trajectory) timed with CUDA events; the one with the most move attempts per second is kept. NPT replicas
+ * keep the compression margin of their cell edge for every candidate period. No counterpart in the
+ * reference. */
+typedef struct pp_tune_result {
+	int resort_every;                /* chosen */
+	int reorder_every;               /* chosen */
+	double cell_scale;               /* chosen */
+	double attempts_per_s;           /* of the chosen schedule */
+	double baseline_attempts_per_s;  /* of the schedule before tuning */
+	int n_tried;
+} pp_tune_result;
+
+int pp_gpu_autotune(pp_engine *e, int trial_sweeps, pp_tune_result *out);
+
 /* Number of replicas, particles of a replica, current box of a replica. */
 int pp_gpu_num_replicas(const pp_engine *e);
 int pp_gpu_num_particles(const pp_engine *e, int replica);

@@ -93,6 +93,17 @@ PROPOSAL_PLAIN = 0
 PROPOSAL_LEARNED = 1
 
 
+class PPTuneResult(ctypes.Structure):
+    _fields_ = [
+        ("resort_every", ctypes.c_int),
+        ("reorder_every", ctypes.c_int),
+        ("cell_scale", ctypes.c_double),
+        ("attempts_per_s", ctypes.c_double),
+        ("baseline_attempts_per_s", ctypes.c_double),
+        ("n_tried", ctypes.c_int),
+    ]
+
+
 class PPError(RuntimeError):
     def __init__(self, code, message):
         super().__init__(f"ppgpu error {code}: {message}")
@@ -113,7 +124,7 @@ EXPORTED = [
     "pp_gpu_energy_noalloc", "pp_mlp_forward", "pp_mlp_grad", "pp_default_learned_params", "pp_gpu_learned_init",
     "pp_gpu_learned_set_weights", "pp_gpu_learned_get_weights", "pp_gpu_set_proposal", "pp_gpu_learned_collect",
     "pp_gpu_learned_train", "pp_gpu_learned_samples", "pp_gpu_learned_clear_samples", "pp_gpu_learned_features",
-    "pp_gpu_learned_stats",
+    "pp_gpu_learned_stats", "pp_gpu_autotune",
 ]
 
 
@@ -174,6 +185,7 @@ def load_library(path=None):
         "pp_gpu_learned_clear_samples": (ctypes.c_int, [vp]),
         "pp_gpu_learned_features": (ctypes.c_int, [vp, ctypes.c_int, fp]),
         "pp_gpu_learned_stats": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
+        "pp_gpu_autotune": (ctypes.c_int, [vp, ctypes.c_int, ctypes.POINTER(PPTuneResult)]),
         "pp_mlp_grad": (ctypes.c_int, [fp, ctypes.c_int, fp, ctypes.c_double, ctypes.c_double, ctypes.c_int, fp, dp]),
     }
     for name, (res, args) in sig.items():
@@ -330,6 +342,11 @@ class Engine:
         ms = ctypes.c_double()
         self._check(self.lib.pp_gpu_time_sweeps(self.h, n, ctypes.byref(ms)))
         return ms.value
+
+    def autotune(self, trial_sweeps=20):
+        t = PPTuneResult()
+        self._check(self.lib.pp_gpu_autotune(self.h, trial_sweeps, ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in PPTuneResult._fields_}
 
     # ---------------------------------------------------------------- learned proposal
     def learned_init(self, **kw):

@@ -41,6 +41,7 @@ struct pp_engine {
 	int resort_every;     /* rounds between cell-grid re-sorts (new random shift, records rebuilt from FP64) */
 	int rounds_per_sweep; /* checkerboard rounds per MC step */
 	int reorder_every;    /* re-sorts between physical reorders of the FP64 state */
+	double cell_scale;    /* cell edge / minimum edge (autotuner) */
 	int any_npt;
 	int any_audit;
 	/* event timing */
@@ -195,6 +196,7 @@ static int create_common(const pp_params *prms, int n, pp_engine **out) {
 	e->resort_every = 4;
 	e->rounds_per_sweep = 1;
 	e->reorder_every = 16;
+	e->cell_scale = 1.0;
 	for(int i = 0; i < n; i++) {
 		if(e->prm[i].guard_eps <= 0.) e->prm[i].guard_eps = 1e-5;
 		if(e->prm[i].ensemble == PP_NPT) e->any_npt = 1;
@@ -323,7 +325,7 @@ static int derive_rparams(pp_engine *e, int r, ppi_rparams *rp) {
 	 * the accepted compressions between two re-sorts (each shrinks one side by at most exp(-max/2)) */
 	double wm = rp->r_cut + 1e-5;
 	if(p->ensemble == PP_NPT) wm /= exp(-0.5 * p->rescale_factor_max * (e->resort_every + 1));
-	rp->w_min = wm;
+	rp->w_min = wm * (e->cell_scale > 1.0 ? e->cell_scale : 1.0);
 	for(int k = 0; k < 32; k++) {
 		double pk = exp(-(double) k / p->temperature);
 		double t = ceil(pk * 9007199254740992.0);
@@ -1553,5 +1555,90 @@ int pp_gpu_learned_stats(pp_engine *e, long long tries[PP_MIX], long long accept
 		if(accepted) accepted[k] = (long long) v[PP_MIX + k];
 	}
 	if(reset) CU(cudaMemsetAsync(e->l_stats, 0, sizeof(v), e->stream));
+	return PP_OK;
+}
+
+/* ------------------------------------------------------------------------------------------------ */
+/* autotuner                                                                                        */
+/* ------------------------------------------------------------------------------------------------ */
+/* minimum cell edge of replica r for the engine's current period and scale (as derive_rparams) */
+static double tuned_w_min(const pp_engine *e, int r) {
+	const pp_params *p = e->prm + r;
+	double wm = (1. + p->kf_delta) + 1e-5;
+	if(p->ensemble == PP_NPT) wm /= exp(-0.5 * p->rescale_factor_max * (e->resort_every + 1));
+	return wm * e->cell_scale;
+}
+
+/* installs a schedule; the next round re-sorts onto the new grid */
+static int apply_schedule(pp_engine *e, int resort, int reorder, double scale) {
+	e->resort_every = resort;
+	e->reorder_every = reorder;
+	e->cell_scale = scale;
+	for(int r = 0; r < e->nrep; r++) e->h_rp[r].w_min = tuned_w_min(e, r);
+	CU(cudaMemcpyAsync(e->d.rp, e->h_rp, sizeof(ppi_rparams) * e->nrep, cudaMemcpyHostToDevice, e->stream));
+	e->round_counter += (resort - e->round_counter % resort) % resort;
+	return PP_OK;
+}
+
+static long long total_tries(pp_engine *e) {
+	long long t = 0;
+	for(int r = 0; r < e->nrep; r++) t += (long long) e->h_rs[r].tries[PP_MOVE_ROTO_TRASL] + (long long) e->h_rs[r].tries[PP_MOVE_VOLUME];
+	return t;
+}
+
+/* attempts per second of the installed schedule over `sweeps` sweeps after two warm-up sweeps */
+static int time_schedule(pp_engine *e, int sweeps, double *aps) {
+	int rc = pp_gpu_sweeps(e, 2);
+	if(rc == PP_OK) rc = read_states(e);
+	if(rc != PP_OK) return rc;
+	const long long t0 = total_tries(e);
+	double ms = 0.;
+	rc = pp_gpu_time_sweeps(e, sweeps, &ms);
+	if(rc != PP_OK) return rc;
+	const long long t1 = total_tries(e);
+	*aps = ms > 0. ? (double) (t1 - t0) / (ms * 1e-3) : 0.;
+	return PP_OK;
+}
+
+int pp_gpu_autotune(pp_engine *e, int trial_sweeps, pp_tune_result *out) {
+	int rc = ready(e);
+	if(rc != PP_OK) return rc;
+	if(trial_sweeps < 1 || trial_sweeps > 100000) return set_err(e, PP_ERR_ARG, "trial_sweeps must lie in [1, 100000]");
+	const int resorts[] = { 2, 4, 8, 16 }, reorders[] = { 4, 16, 64 };
+	const double scales[] = { 1.0, 1.2, 1.5 };
+	const int r0 = e->resort_every, o0 = e->reorder_every;
+	const double s0 = e->cell_scale;
+	double base = 0.;
+	if((rc = time_schedule(e, trial_sweeps, &base)) != PP_OK) return rc;
+	int best_r = r0, best_o = o0, tried = 1;
+	double best_s = s0, best = base;
+	for(int a = 0; a < 4; a++)
+		for(int b = 0; b < 3; b++)
+			for(int c = 0; c < 3; c++) {
+				if(resorts[a] == r0 && reorders[b] == o0 && scales[c] == s0) continue;
+				if((rc = apply_schedule(e, resorts[a], reorders[b], scales[c])) != PP_OK) return rc;
+				double v = 0.;
+				rc = time_schedule(e, trial_sweeps, &v);
+				if(rc != PP_OK) { /* a schedule the boxes cannot hold: fall back to the best so far */
+					apply_schedule(e, best_r, best_o, best_s);
+					return rc;
+				}
+				tried++;
+				if(v > best) {
+					best = v;
+					best_r = resorts[a];
+					best_o = reorders[b];
+					best_s = scales[c];
+				}
+			}
+	if((rc = apply_schedule(e, best_r, best_o, best_s)) != PP_OK) return rc;
+	if(out) {
+		out->resort_every = best_r;
+		out->reorder_every = best_o;
+		out->cell_scale = best_s;
+		out->attempts_per_s = best;
+		out->baseline_attempts_per_s = base;
+		out->n_tried = tried;
+	}
 	return PP_OK;
 }
