@@ -152,6 +152,71 @@ def allreduce(dist, value, op):
     return float(t.item())
 
 
+def batch_configs(n=256, seed=3000):
+    """The batched-replica workload: n NVT replicas, N log-uniform in [500, 8000], T uniform in [0.09, 0.20],
+    rho uniform in [0.05, 0.6], KF_cosmax uniform in [0.89, 0.95] (seeded), each a seeded random insertion."""
+    import patchyparticles_gb300 as pp
+
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        N = int(round(np.exp(rng.uniform(np.log(500), np.log(8000)))))
+        T, rho, cm = rng.uniform(0.09, 0.20), rng.uniform(0.05, 0.6), rng.uniform(0.89, 0.95)
+        r, R, box = pp.generate(N, rho, seed + k, round_like_file=False)
+        out.append(dict(N=N, T=T, rho=rho, cosmax=cm, seed=seed + k, arrays=(r, R, box)))
+    return out
+
+
+def run_batch(args, ws, rank, local, dist):
+    """Batched replicas in one engine: every launch advances all of them."""
+    import patchyparticles_gb300 as pp
+    from patchyparticles_gb300 import build
+
+    if rank == 0 or ws == 1:
+        build.build()
+    barrier(dist)
+    pp.select_device(local)
+    reps = batch_configs(seed=3000 + 1000 * rank)
+    prm = [pp.default_params(temperature=c["T"], kf_cosmax=c["cosmax"], seed=c["seed"]) for c in reps]
+    e = pp.Engine(prm)
+    for k, c in enumerate(reps):
+        e.upload(*c["arrays"], replica=k)
+    tune = e.autotune(args.tune_sweeps) if args.tune_sweeps > 0 else None
+    for _ in range(args.warmup):
+        e.sweeps(args.sweeps_per_step)
+    e.sync()
+    for k in range(len(reps)):
+        e.counters(replica=k, reset=True)
+    launches0 = e.launch_count()
+    sampler = ClockSampler(local)
+    barrier(dist)
+    sampler.start()
+    ms = e.time_sweeps(args.steps * args.sweeps_per_step)
+    clocks = sampler.stop()
+    barrier(dist)
+    att = sum(e.counters(replica=k)[0][pp.MOVE_ROTO_TRASL] for k in range(len(reps)))
+    t_max = allreduce(dist, ms / 1000.0, _max_op(dist))
+    att = allreduce(dist, att, _sum_op(dist))
+    ntot = sum(c["N"] for c in reps)
+    launches = e.launch_count() - launches0
+    e.close()
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peaks()
+    achieved = att / t_max * BYTES_PER_ATTEMPT / 1e9
+    line = {
+        "metric": "MC move attempts/sec, 256 batched replicas", "value": att / t_max, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * t_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64", "data": "synthetic (seeded random insertion per replica)",
+        "config": {"workload": "256 NVT replicas, N log-uniform 500-8000 (%d particles), T U[0.09,0.20], rho U[0.05,0.6], KF_cosmax U[0.89,0.95]" % ntot,
+                   "schedule": tune, "l2": "the whole batch (%.0f MB of FP64 state) fits in L2" % (ntot * 128 / 1e6)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "peak_source": peak_kind, "bytes_per_attempt": BYTES_PER_ATTEMPT, "note": "whole sweep, not one kernel"},
+        "clocks": clocks, "e2e": None, "cpu_baseline": None, "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def make_config(wl, seed_offset=0):
     import patchyparticles_gb300 as pp
 
@@ -433,7 +498,7 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c5", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="c5", choices=sorted(WORKLOADS) + ["c3"])
     ap.add_argument("--sweeps-per-step", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--e2e-sweeps", type=int, default=10)
@@ -451,10 +516,12 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    wl = WORKLOADS[args.workload]
+    wl = WORKLOADS.get(args.workload, WORKLOADS["c2"])
     ws, rank, local, dist = dist_setup()
     if args.impl == "reference":
         run_reference(args, wl, ws, rank, dist)
+    elif args.workload == "c3":
+        run_batch(args, ws, rank, local, dist)
     elif args.learned_only:
         from patchyparticles_gb300 import build
 
