@@ -300,31 +300,35 @@ def run_gpu(args, wl, ws, rank, local, dist):
         e.sweeps(spsw)
     e.sync()
     e.counters(reset=True)
-    e.set_timing(True)
-    e.kernel_stats(reset=True)
     launches0 = e.launch_count()
     sampler = ClockSampler(local)
     barrier(dist)
     e.sync()
     sampler.start()
-    ms = e.time_sweeps(args.steps * spsw)  # CUDA events on the engine's stream around the K steps
+    ms = e.time_sweeps(args.steps * spsw)  # CUDA events on the engine's stream around the K steps (graph replays)
     clocks = sampler.stop()
     barrier(dist)
     launches = e.launch_count() - launches0
     tries, acc = e.counters()
-    ks = e.kernel_stats()
-    e.set_timing(False)
     attempts = tries[pp.MOVE_ROTO_TRASL] + tries[pp.MOVE_VOLUME]
     t_max = allreduce(dist, ms / 1000.0, _max_op(dist))
     att_sum = allreduce(dist, attempts, _sum_op(dist))
     value = att_sum / t_max
 
-    # roofline of the dominant kernel: k_colour (the 8 checkerboard colour launches of a round are timed as one
-    # event group on the engine stream), 192 B per attempt
+    # roofline of the dominant kernel: k_colour. A separate pass of the same sweeps with per-group CUDA events
+    # on the engine stream (stream launches; the 8 colour launches of a round form one group), 192 B per attempt
+    e.counters(reset=True)
+    e.set_timing(True)
+    e.kernel_stats(reset=True)
+    e.sweeps(args.roofline_sweeps)
+    e.sync()
+    ks = e.kernel_stats()
+    e.set_timing(False)
+    rtries, _ = e.counters()
     peak, peak_kind = measured_peaks()
     sweep_launches = max(1, ks["sweep_launches"])
     avg_ms = ks["sweep_ms"] / sweep_launches
-    att_per_launch = tries[pp.MOVE_ROTO_TRASL] / sweep_launches
+    att_per_launch = rtries[pp.MOVE_ROTO_TRASL] / sweep_launches
     achieved = att_per_launch * BYTES_PER_ATTEMPT / (avg_ms / 1000.0) / 1e9
     traffic = profiled_traffic(args.workload)
 
@@ -372,7 +376,7 @@ def run_gpu(args, wl, ws, rank, local, dist):
         "dtype": "f32+f64", "data": "synthetic (seeded random insertion, uniform orientations)",
         "config": {"workload": wl["name"], "N": wl["N"], "sweeps_per_step": spsw, "proposal": "plain",
                    "l2": "inputs larger than L2 (FP64 state %.0f MB + FP32 mirror %.0f MB per GPU)" % (wl["N"] * 128 / 1e6, wl["N"] * 64 / 1e6),
-                   "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "parallelism": "replicas" if ws > 1 else "single GPU", "launch": "CUDA graph per re-sort period",
                    "schedule": tune if tune else "defaults (resort_every 4, reorder_every 16, cell_scale 1.0)"},
         "acceptance": acc[pp.MOVE_ROTO_TRASL] / max(1, tries[pp.MOVE_ROTO_TRASL]),
         "volume_acceptance": acc[pp.MOVE_VOLUME] / max(1, tries[pp.MOVE_VOLUME]) if tries[pp.MOVE_VOLUME] else None,
@@ -507,6 +511,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-plain effective-sample comparison")
     ap.add_argument("--tune-sweeps", type=int, default=10, help="sweeps per autotuner trial before the run (0: default schedule)")
+    ap.add_argument("--roofline-sweeps", type=int, default=32, help="sweeps of the per-kernel event-timed pass")
     ap.add_argument("--learned-only", action="store_true", help="run only the learned-vs-plain comparison (one JSON object)")
     ap.add_argument("--learn-configs", type=int, default=10000)
     ap.add_argument("--learn-params", default="{}", help="JSON overrides of pp_learned_params (e.g. {\"jump\": 1e-3})")

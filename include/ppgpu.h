@@ -151,6 +151,11 @@ int pp_gpu_select_device(int device);
 int pp_gpu_set_timing(pp_engine *e, int enable);
 int pp_gpu_kernel_stats(pp_engine *e, pp_kernel_stats *out, int reset);
 
+/* Whole re-sort periods of pp_gpu_sweeps are replayed from captured CUDA graphs (one launch per period
+ * instead of one per kernel; the launches and the trajectory are the same). enable = 0 turns the graphs
+ * off (every kernel launched on the stream); per-group event timing always uses stream launches. */
+int pp_gpu_set_graphs(pp_engine *e, int enable);
+
 /* Enqueues n sweeps between two CUDA events recorded on the engine's stream, waits, and returns the
  * elapsed device time in *ms. */
 int pp_gpu_time_sweeps(pp_engine *e, long long n, double *ms);

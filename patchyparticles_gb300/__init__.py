@@ -124,7 +124,7 @@ EXPORTED = [
     "pp_gpu_energy_noalloc", "pp_mlp_forward", "pp_mlp_grad", "pp_default_learned_params", "pp_gpu_learned_init",
     "pp_gpu_learned_set_weights", "pp_gpu_learned_get_weights", "pp_gpu_set_proposal", "pp_gpu_learned_collect",
     "pp_gpu_learned_train", "pp_gpu_learned_samples", "pp_gpu_learned_clear_samples", "pp_gpu_learned_features",
-    "pp_gpu_learned_stats", "pp_gpu_autotune",
+    "pp_gpu_learned_stats", "pp_gpu_autotune", "pp_gpu_set_graphs",
 ]
 
 
@@ -186,6 +186,7 @@ def load_library(path=None):
         "pp_gpu_learned_features": (ctypes.c_int, [vp, ctypes.c_int, fp]),
         "pp_gpu_learned_stats": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
         "pp_gpu_autotune": (ctypes.c_int, [vp, ctypes.c_int, ctypes.POINTER(PPTuneResult)]),
+        "pp_gpu_set_graphs": (ctypes.c_int, [vp, ctypes.c_int]),
         "pp_mlp_grad": (ctypes.c_int, [fp, ctypes.c_int, fp, ctypes.c_double, ctypes.c_double, ctypes.c_int, fp, dp]),
     }
     for name, (res, args) in sig.items():
@@ -342,6 +343,9 @@ class Engine:
         ms = ctypes.c_double()
         self._check(self.lib.pp_gpu_time_sweeps(self.h, n, ctypes.byref(ms)))
         return ms.value
+
+    def set_graphs(self, enable=True):
+        self._check(self.lib.pp_gpu_set_graphs(self.h, 1 if enable else 0))
 
     def autotune(self, trial_sweeps=20):
         t = PPTuneResult()

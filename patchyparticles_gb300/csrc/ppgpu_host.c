@@ -51,6 +51,14 @@ struct pp_engine {
 	int *ev_kind;      /* 0 sort, 1 sweep, 2 volume */
 	int ev_cap;
 	pp_kernel_stats kstats;
+	/* captured sweep graphs: one per re-sort period, with and without the physical reorder */
+	int graphs_on;                /* pp_gpu_set_graphs (default 1) */
+	int graphs_broken;            /* capture failed once: stream launches from then on */
+	int graph_gen;                /* bumped whenever device pointers or the schedule change */
+	cudaGraphExec_t gexec[2];
+	cudaGraph_t gph[2];
+	long long gnodes[2];
+	int gkey[2][5];               /* resort_every, proposal, audit, npt, graph_gen of the capture */
 	/* learned proposal */
 	int learn_ready;              /* network buffers allocated (pp_gpu_learned_init) */
 	int proposal;                 /* PP_PROPOSAL_PLAIN or PP_PROPOSAL_LEARNED */
@@ -197,6 +205,7 @@ static int create_common(const pp_params *prms, int n, pp_engine **out) {
 	e->rounds_per_sweep = 1;
 	e->reorder_every = 16;
 	e->cell_scale = 1.0;
+	e->graphs_on = 1;
 	for(int i = 0; i < n; i++) {
 		if(e->prm[i].guard_eps <= 0.) e->prm[i].guard_eps = 1e-5;
 		if(e->prm[i].ensemble == PP_NPT) e->any_npt = 1;
@@ -217,6 +226,8 @@ int pp_gpu_num_replicas(const pp_engine *e) { return e ? e->nrep : 0; }
 int pp_gpu_num_particles(const pp_engine *e, int r) { return (e && r >= 0 && r < e->nrep) ? e->N[r] : -1; }
 long long pp_gpu_launch_count(const pp_engine *e) { return e ? e->launches : 0; }
 
+static void drop_graphs(pp_engine *e);
+
 static void free_device(pp_engine *e) {
 	void **ptrs[] = { (void **) &e->d.rec, (void **) &e->d.spos, (void **) &e->d.sori, (void **) &e->d.id, (void **) &e->d.rep, (void **) &e->d.cellof,
 		(void **) &e->d.cell_count, (void **) &e->d.cell_start, (void **) &e->d.cell_cursor, (void **) &e->d.cell_rep, (void **) &e->d.scan_aux,
@@ -233,11 +244,24 @@ static void free_device(pp_engine *e) {
 	e->pin_rec = NULL;
 	e->pin_id = e->pin_i1 = e->pin_i2 = NULL;
 	e->pin_n = 0;
+	if(e->d.ctr) cudaFree(e->d.ctr);
+	e->d.ctr = NULL;
+	drop_graphs(e);
 	/* layout-sized buffers of the learned proposal */
 	if(e->d.simg) cudaFree(e->d.simg);
 	if(e->d.feat) cudaFree(e->d.feat);
 	e->d.simg = NULL;
 	e->d.feat = NULL;
+}
+
+static void drop_graphs(pp_engine *e) {
+	for(int v = 0; v < 2; v++) {
+		if(e->gexec[v]) cudaGraphExecDestroy(e->gexec[v]);
+		if(e->gph[v]) cudaGraphDestroy(e->gph[v]);
+		e->gexec[v] = NULL;
+		e->gph[v] = NULL;
+	}
+	e->graph_gen++;
 }
 
 static void free_learned(pp_engine *e) {
@@ -468,6 +492,7 @@ static int commit(pp_engine *e) {
 	CU(cudaMalloc((void **) &d->rp, sizeof(ppi_rparams) * e->nrep));
 	CU(cudaMalloc((void **) &d->rs, sizeof(ppi_rstate) * e->nrep));
 	CU(cudaMalloc((void **) &d->grid, sizeof(ppi_grid) * e->nrep));
+	CU(cudaMalloc((void **) &d->ctr, sizeof(ppi_ctr)));
 	CU(cudaMemsetAsync(d->out_bonds, 0, sizeof(int) * n1, e->stream));
 	CU(cudaMemsetAsync(d->out_overlaps, 0, sizeof(int) * n1, e->stream));
 	CU(cudaMemsetAsync(d->grid, 0, sizeof(ppi_grid) * e->nrep, e->stream));
@@ -705,11 +730,103 @@ static void colour_order(long long round, int col[8]) {
 
 /* One MC step: `rounds_per_sweep` checkerboard rounds (one attempt per non-empty cell per round, the
  * grid re-sorted from the FP64 state every resort_every rounds), then one NPT volume attempt. */
+#define GRAPH_UNAVAILABLE 1 /* internal: capture not possible, use stream launches */
+
+/* Captures one re-sort period (the re-sort, with the physical reorder if v, then resort_every rounds, each
+ * followed by the NPT volume attempt) as a CUDA graph whose launches read the round / epoch / sweep
+ * indices from the device counters. The launches are the stream path's, argument for argument. */
+static int capture_period(pp_engine *e, int v) {
+	const int R = e->resort_every, learned = e->proposal == PP_PROPOSAL_LEARNED;
+	static const int slots[8] = { 0, 1, 2, 3, 4, 5, 6, 7 };
+	if(ppi_prepare(&e->d) != 0) {
+		cudaGetLastError();
+		return GRAPH_UNAVAILABLE;
+	}
+	long long nl = 0;
+	cudaGraph_t g = NULL;
+	if(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+		cudaGetLastError();
+		return GRAPH_UNAVAILABLE;
+	}
+	int rc = 0;
+	if(v) {
+		rc |= ppi_resort(&e->d, -1, e->stream, &nl);
+		rc |= ppi_reorder(&e->d, e->stream, &nl);
+	}
+	rc |= ppi_resort(&e->d, -1, e->stream, &nl);
+	if(learned) rc |= ppi_canon(&e->d, e->stream, &nl);
+	for(int r = 0; r < R; r++) {
+		if(learned) rc |= ppi_round_learned(&e->d, -1 - r, slots, e->any_audit, e->stream, &nl);
+		else rc |= ppi_round(&e->d, -1 - r, slots, e->any_audit, e->stream, &nl);
+		if(e->any_npt) {
+			rc |= ppi_volume(&e->d, -1 - r, e->stream, &nl);
+			if(learned) rc |= ppi_canon(&e->d, e->stream, &nl);
+		}
+	}
+	const cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
+	cudaGraphExec_t x = NULL;
+	if(rc != 0 || ce != cudaSuccess || g == NULL || cudaGraphInstantiate(&x, g, 0) != cudaSuccess) {
+		if(g) cudaGraphDestroy(g);
+		cudaGetLastError();
+		return GRAPH_UNAVAILABLE;
+	}
+	e->gexec[v] = x;
+	e->gph[v] = g;
+	e->gnodes[v] = nl;
+	e->gkey[v][0] = R;
+	e->gkey[v][1] = e->proposal;
+	e->gkey[v][2] = e->any_audit;
+	e->gkey[v][3] = e->any_npt;
+	e->gkey[v][4] = e->graph_gen;
+	return PP_OK;
+}
+
+/* one re-sort period (resort_every sweeps) by replaying its graph */
+static int replay_period(pp_engine *e) {
+	const int v = (e->reorder_every > 0 && e->epoch % e->reorder_every == 0) ? 1 : 0;
+	if(e->gexec[v] && (e->gkey[v][0] != e->resort_every || e->gkey[v][1] != e->proposal || e->gkey[v][2] != e->any_audit || e->gkey[v][3] != e->any_npt ||
+							  e->gkey[v][4] != e->graph_gen)) {
+		cudaGraphExecDestroy(e->gexec[v]);
+		cudaGraphDestroy(e->gph[v]);
+		e->gexec[v] = NULL;
+		e->gph[v] = NULL;
+	}
+	if(!e->gexec[v]) {
+		const int rc = capture_period(e, v);
+		if(rc != PP_OK) return rc;
+	}
+	long long nl = 0;
+	CK(ppi_set_counters(&e->d, e->round_counter, e->epoch, e->sweep_counter, e->stream, &nl));
+	CU(cudaGraphLaunch(e->gexec[v], e->stream));
+	e->launches += nl + e->gnodes[v];
+	e->round_counter += e->resort_every;
+	e->sweep_counter += e->resort_every;
+	e->epoch++;
+	return PP_OK;
+}
+
+int pp_gpu_set_graphs(pp_engine *e, int enable) {
+	if(e == NULL) return PP_ERR_ARG;
+	e->graphs_on = enable ? 1 : 0;
+	if(!enable) drop_graphs(e);
+	return PP_OK;
+}
+
 int pp_gpu_sweeps(pp_engine *e, long long n) {
 	int rc = ready(e);
 	if(rc != PP_OK) return rc;
 	if(n < 0) return set_err(e, PP_ERR_ARG, "negative sweep count");
 	for(long long k = 0; k < n; k++) {
+		/* whole re-sort periods from a captured graph (not while per-group event timing is on) */
+		if(e->graphs_on && !e->graphs_broken && !e->timing && e->rounds_per_sweep == 1 && e->round_counter % e->resort_every == 0 && n - k >= e->resort_every) {
+			rc = replay_period(e);
+			if(rc == PP_OK) {
+				k += e->resort_every - 1;
+				continue;
+			}
+			if(rc != GRAPH_UNAVAILABLE) return rc;
+			e->graphs_broken = 1;
+		}
 		long long s = e->sweep_counter++;
 		int ev;
 		for(int rr = 0; rr < e->rounds_per_sweep; rr++) {
@@ -1251,6 +1368,7 @@ static double u01_sm(uint64_t *s) { return (double) (splitmix64(s) >> 11) * 0x1p
 /* layout-sized buffers (canonical images, features); valid after the layout exists */
 static int ensure_learn_layout(pp_engine *e) {
 	if(!e->committed) return set_err(e, PP_ERR_STATE, "no configuration uploaded for every replica");
+	if(!e->d.simg || !e->d.feat) drop_graphs(e); /* captured launches hold the device pointers by value */
 	size_t n1 = e->d.ntot > 0 ? (size_t) e->d.ntot : 1;
 	if(!e->d.simg) CU(cudaMalloc((void **) &e->d.simg, sizeof(float) * 16 * n1));
 	if(!e->d.feat) CU(cudaMalloc((void **) &e->d.feat, sizeof(float) * PP_MLP_IN * n1));
@@ -1294,6 +1412,7 @@ int pp_gpu_learned_init(pp_engine *e, const pp_learned_params *p) {
 		CU(cudaMalloc((void **) &e->l_obj, sizeof(double)));
 		e->learn_ready = 1;
 	}
+	drop_graphs(e);
 	e->d.mlp_img = e->l_img;
 	e->d.learn = e->l_learn;
 	e->d.lrep = e->l_rep;
@@ -1382,6 +1501,7 @@ int pp_gpu_set_proposal(pp_engine *e, int proposal) {
 	e->proposal = proposal;
 	return PP_OK;
 }
+
 
 /* grows the device sample buffer to hold at least n samples (existing samples kept) */
 static int ensure_samples(pp_engine *e, long long n) {
@@ -1571,6 +1691,7 @@ static double tuned_w_min(const pp_engine *e, int r) {
 
 /* installs a schedule; the next round re-sorts onto the new grid */
 static int apply_schedule(pp_engine *e, int resort, int reorder, double scale) {
+	drop_graphs(e);
 	e->resort_every = resort;
 	e->reorder_every = reorder;
 	e->cell_scale = scale;

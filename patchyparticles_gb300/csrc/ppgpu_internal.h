@@ -112,6 +112,12 @@ typedef struct ppi_lrep {
 	float t[PPI_MIX];            /* maximum angle: min(Theta_max * stheta[k], largest FP32 below pi) */
 } ppi_lrep;
 
+/* device counters of the captured sweep graphs: a kernel given a negative round / epoch / sweep argument
+ * (-1 - k) uses the k-th index after these (the host writes them before each replay) */
+typedef struct ppi_ctr {
+	long long round, epoch, sweep;
+} ppi_ctr;
+
 /* all device pointers, passed by value to every kernel */
 typedef struct ppi_dev {
 	int nrep;
@@ -158,6 +164,7 @@ typedef struct ppi_dev {
 	int *lerr;                    /* tensor-core barrier timeouts of the learned passes */
 	int sample_cap;
 	int pad2;
+	ppi_ctr *ctr;                 /* graph-path counters */
 } ppi_dev;
 
 #define PPI_MAX_PARTNERS 24
@@ -172,6 +179,10 @@ int ppi_reorder(const ppi_dev *d, cudaStream_t s, long long *nl);
 /* writes x y z R00..R22 (12 doubles) of slots [first, first + count) into d->tmp_rec */
 int ppi_export(const ppi_dev *d, int first, int count, cudaStream_t s, long long *nl);
 int ppi_sm_count(void);
+/* sizes the launch grids of every pass once (their occupancy queries must not run inside a stream capture) */
+int ppi_prepare(const ppi_dev *d);
+/* writes the graph-path counters (one small kernel on the stream) */
+int ppi_set_counters(const ppi_dev *d, long long round, long long epoch, long long sweep, cudaStream_t s, long long *nl);
 
 /* learned proposal (ppgpu_kernels.cu): canonical images of all slots; one round of learned moves; the
  * features of every slot; training samples of the current state for colour col into rows [base, base + count) */

@@ -56,6 +56,32 @@ __device__ __forceinline__ U4 rng(const ppi_rparams &rp, long long sweep, int re
 	return philox(U4{ (uint32_t) sweep, ((uint32_t) ((unsigned long long) sweep >> 32) << 8) | tag, item, sub }, (uint32_t) rp.seed, (uint32_t) (rp.seed >> 32));
 }
 
+/* index of a launch: a non-negative argument is the index itself, a negative one (-1 - k) the k-th after
+ * the device counter base (the launches of a captured sweep graph) */
+__device__ __forceinline__ long long ctr_index(long long arg, long long base) { return arg >= 0 ? arg : base + (-1 - arg); }
+
+/* colour of slot ci in round `round`: the host's colour_order (ppgpu_host.c), a Fisher-Yates shuffle driven
+ * by splitmix64 of the round index, evaluated on the device for graph launches */
+__device__ __forceinline__ int colour_at(long long round, int ci) {
+	uint64_t z = (uint64_t) round * 0x9E3779B97F4A7C15ULL + 0x632BE59BD9B4E019ULL;
+	int col[8];
+#pragma unroll
+	for(int i = 0; i < 8; i++) col[i] = i;
+#pragma unroll
+	for(int i = 7; i > 0; i--) {
+		z += 0x9E3779B97F4A7C15ULL;
+		uint64_t x = z;
+		x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
+		x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
+		x ^= x >> 31;
+		const int j = (int) (x % (uint64_t) (i + 1));
+		const int t = col[i];
+		col[i] = col[j];
+		col[j] = t;
+	}
+	return col[ci & 7];
+}
+
 __device__ __forceinline__ float u01(uint32_t v) { return (float) (v >> 8) * 0x1p-24f; } /* [0, 1) */
 __device__ __forceinline__ double u01d(uint32_t a, uint32_t b) { return (double) (((uint64_t) a << 21) | (b >> 11)) * 0x1p-53; }
 
@@ -432,6 +458,7 @@ __device__ __noinline__ void audit_pair(const double *rec_all, const ppi_rparams
 __global__ void k_grid(ppi_dev d, long long epoch) {
 	int r = blockIdx.x * blockDim.x + threadIdx.x;
 	if(r >= d.nrep) return;
+	epoch = ctr_index(epoch, epoch < 0 ? d.ctr->epoch : 0);
 	const ppi_rparams &rp = d.rp[r];
 	ppi_rstate *rs = d.rs + r;
 	ppi_grid *g = d.grid + r;
@@ -1316,6 +1343,10 @@ __device__ __forceinline__ void tile_round(const ppi_dev &d, TileSmem &S, const 
 /* one colour of a round: the colour's non-empty cells, TA per warp and iteration */
 template <int MODE>
 __global__ void __launch_bounds__(32 * TILE_WARPS, MODE == MODE_FAST ? PPI_TILE_MIN_BLOCKS : 1) k_colour(ppi_dev d, long long round, int col) {
+	if(round < 0) { /* graph launch: round after the device counter, col = slot in the round's colour order */
+		round = ctr_index(round, d.ctr->round);
+		col = colour_at(round, col);
+	}
 	__shared__ TileSmem s_tile[TILE_WARPS];
 	TileSmem &S = s_tile[threadIdx.x >> 5];
 	const int lane = threadIdx.x & 31;
@@ -1963,6 +1994,10 @@ __device__ __forceinline__ bool scan_move_cached(const ppi_dev &d, LearnCache &K
  * network runs twice per tile on the tensor cores (current and candidate states). */
 template <int MODE>
 __global__ void __launch_bounds__(32) k_colour_learned(ppi_dev d, long long round, int col) {
+	if(round < 0) { /* graph launch (see k_colour) */
+		round = ctr_index(round, d.ctr->round);
+		col = colour_at(round, col);
+	}
 	const int4 *list = d.clist + (size_t) col * d.clist_cap;
 	int cnt = d.ccount[col];
 	if(cnt > d.clist_cap) cnt = d.clist_cap;
@@ -2881,6 +2916,7 @@ __global__ void k_energy_reset(ppi_dev d) {
 __global__ void k_vol_plan(ppi_dev d, long long sweep) {
 	int r = blockIdx.x * blockDim.x + threadIdx.x;
 	if(r >= d.nrep) return;
+	sweep = ctr_index(sweep, sweep < 0 ? d.ctr->sweep : 0);
 	const ppi_rparams &rp = d.rp[r];
 	ppi_rstate *rs = d.rs + r;
 	ppi_grid *g = d.grid + r;
@@ -2910,6 +2946,7 @@ __global__ void k_vol_plan(ppi_dev d, long long sweep) {
 __global__ void k_vol_decide(ppi_dev d, long long sweep) {
 	int r = blockIdx.x * blockDim.x + threadIdx.x;
 	if(r >= d.nrep) return;
+	sweep = ctr_index(sweep, sweep < 0 ? d.ctr->sweep : 0);
 	const ppi_rparams &rp = d.rp[r];
 	ppi_grid *g = d.grid + r;
 	ppi_rstate *rs = d.rs + r;
@@ -3052,6 +3089,10 @@ static int resident_grid(F f, int *cache, int block = 128) {
 	return *cache;
 }
 
+/* cached launch grids (one occupancy query each, made before any stream capture by ppi_prepare) */
+static int g_col_audit = 0, g_col_fast = 0, g_learn_audit = 0, g_learn_fast = 0, g_vol_grid = 0;
+static int g_a1 = 0, g_a4 = 0, g_f1 = 0, g_f4 = 0, g_f8 = 0;
+
 extern "C" int ppi_resort(const ppi_dev *d, long long epoch, cudaStream_t s, long long *nl) {
 	float4 *tmp = (float4 *) d->tmp_rec; /* ntot float4 fit in the reorder scratch */
 	cudaMemsetAsync(d->cell_count, 0, sizeof(int) * (size_t) d->total_cells, s);
@@ -3072,13 +3113,12 @@ extern "C" int ppi_resort(const ppi_dev *d, long long epoch, cudaStream_t s, lon
 static int lanes_of(const ppi_dev *d) { return d->lanes == 8 ? 8 : PPI_DEFAULT_LANES; }
 
 extern "C" int ppi_round(const ppi_dev *d, long long round, const int *colours, int audit, cudaStream_t s, long long *nl) {
-	static int g_audit = 0, g_fast = 0;
 	if(audit || d->audit_any) {
-		int grid = resident_grid(k_colour<MODE_AUDIT>, &g_audit, 32 * TILE_WARPS);
+		int grid = resident_grid(k_colour<MODE_AUDIT>, &g_col_audit, 32 * TILE_WARPS);
 		for(int ci = 0; ci < 8; ci++) k_colour<MODE_AUDIT><<<grid, 32 * TILE_WARPS, 0, s>>>(*d, round, colours[ci]);
 	}
 	else {
-		int grid = resident_grid(k_colour<MODE_FAST>, &g_fast, 32 * TILE_WARPS);
+		int grid = resident_grid(k_colour<MODE_FAST>, &g_col_fast, 32 * TILE_WARPS);
 		for(int ci = 0; ci < 8; ci++) k_colour<MODE_FAST><<<grid, 32 * TILE_WARPS, 0, s>>>(*d, round, colours[ci]);
 	}
 	*nl += 8;
@@ -3086,17 +3126,14 @@ extern "C" int ppi_round(const ppi_dev *d, long long round, const int *colours, 
 }
 
 static void launch_energy(const ppi_dev *d, int mode, cudaStream_t s, long long *nl) {
-	static int g_a1 = 0, g_a4 = 0, g_f1 = 0, g_f4 = 0, g_f8 = 0;
+
 	const int audit = d->audit_any;
 	if(mode == PPI_EN_PARTNERS) { /* one lane per particle: the partner list is written in order */
 		if(audit) k_energy<MODE_AUDIT, 1><<<resident_grid(k_energy<MODE_AUDIT, 1>, &g_a1), 128, 0, s>>>(*d, mode);
 		else k_energy<MODE_FAST, 1><<<resident_grid(k_energy<MODE_FAST, 1>, &g_f1), 128, 0, s>>>(*d, mode);
 	}
 	else if(audit) k_energy<MODE_AUDIT, 4><<<resident_grid(k_energy<MODE_AUDIT, 4>, &g_a4), 128, 0, s>>>(*d, mode);
-	else if(mode == PPI_EN_VOLUME) {
-		static int g_vol = 0;
-		k_energy_vol<<<resident_grid(k_energy_vol, &g_vol, 32 * TILE_WARPS), 32 * TILE_WARPS, 0, s>>>(*d);
-	}
+	else if(mode == PPI_EN_VOLUME) k_energy_vol<<<resident_grid(k_energy_vol, &g_vol_grid, 32 * TILE_WARPS), 32 * TILE_WARPS, 0, s>>>(*d);
 	else if(lanes_of(d) == 8) k_energy<MODE_FAST, 8><<<resident_grid(k_energy<MODE_FAST, 8>, &g_f8), 128, 0, s>>>(*d, mode);
 	else k_energy<MODE_FAST, 4><<<resident_grid(k_energy<MODE_FAST, 4>, &g_f4), 128, 0, s>>>(*d, mode);
 	*nl += 1;
@@ -3136,6 +3173,18 @@ extern "C" int ppi_reorder(const ppi_dev *d, cudaStream_t s, long long *nl) {
 	return (int) cudaGetLastError();
 }
 
+__global__ void k_set_counters(ppi_ctr *c, long long round, long long epoch, long long sweep) {
+	c->round = round;
+	c->epoch = epoch;
+	c->sweep = sweep;
+}
+
+extern "C" int ppi_set_counters(const ppi_dev *d, long long round, long long epoch, long long sweep, cudaStream_t s, long long *nl) {
+	k_set_counters<<<1, 1, 0, s>>>(d->ctr, round, epoch, sweep);
+	*nl += 1;
+	return (int) cudaGetLastError();
+}
+
 extern "C" int ppi_canon(const ppi_dev *d, cudaStream_t s, long long *nl) {
 	if(d->ntot <= 0) return 0;
 	k_canon<<<(d->ntot + 255) / 256, 256, 0, s>>>(*d);
@@ -3165,15 +3214,28 @@ static int learned_grid(F f, int *cache) {
 	return *cache;
 }
 
+extern "C" int ppi_prepare(const ppi_dev *d) {
+	(void) d;
+	resident_grid(k_colour<MODE_AUDIT>, &g_col_audit, 32 * TILE_WARPS);
+	resident_grid(k_colour<MODE_FAST>, &g_col_fast, 32 * TILE_WARPS);
+	resident_grid(k_energy_vol, &g_vol_grid, 32 * TILE_WARPS);
+	resident_grid(k_energy<MODE_AUDIT, 1>, &g_a1);
+	resident_grid(k_energy<MODE_AUDIT, 4>, &g_a4);
+	resident_grid(k_energy<MODE_FAST, 1>, &g_f1);
+	resident_grid(k_energy<MODE_FAST, 4>, &g_f4);
+	resident_grid(k_energy<MODE_FAST, 8>, &g_f8);
+	if(learned_grid(k_colour_learned<MODE_AUDIT>, &g_learn_audit) < 0 || learned_grid(k_colour_learned<MODE_FAST>, &g_learn_fast) < 0) return (int) cudaGetLastError();
+	return (int) cudaGetLastError();
+}
+
 extern "C" int ppi_round_learned(const ppi_dev *d, long long round, const int *colours, int audit, cudaStream_t s, long long *nl) {
-	static int g_audit = 0, g_fast = 0;
 	if(audit || d->audit_any) {
-		const int grid = learned_grid(k_colour_learned<MODE_AUDIT>, &g_audit);
+		const int grid = learned_grid(k_colour_learned<MODE_AUDIT>, &g_learn_audit);
 		if(grid < 0) return (int) cudaGetLastError();
 		for(int ci = 0; ci < 8; ci++) k_colour_learned<MODE_AUDIT><<<grid, 32, LEARN_SMEM, s>>>(*d, round, colours[ci]);
 	}
 	else {
-		const int grid = learned_grid(k_colour_learned<MODE_FAST>, &g_fast);
+		const int grid = learned_grid(k_colour_learned<MODE_FAST>, &g_learn_fast);
 		if(grid < 0) return (int) cudaGetLastError();
 		for(int ci = 0; ci < 8; ci++) k_colour_learned<MODE_FAST><<<grid, 32, LEARN_SMEM, s>>>(*d, round, colours[ci]);
 	}
