@@ -381,7 +381,7 @@ def run_gpu(args, wl, ws, rank, local, dist):
         "acceptance": acc[pp.MOVE_ROTO_TRASL] / max(1, tries[pp.MOVE_ROTO_TRASL]),
         "volume_acceptance": acc[pp.MOVE_VOLUME] / max(1, tries[pp.MOVE_VOLUME]) if tries[pp.MOVE_VOLUME] else None,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "kernel": "k_colour (8 launches per round, one event group)", "peak_source": peak_kind,
+                     "traffic": traffic, "kernel": "k_colour%s (8 launches per round, one event group)" % (" over neighbour lists" if (tune is None or tune.get("neighbour_lists", 1)) else ""), "peak_source": peak_kind,
                      "bytes_per_attempt": BYTES_PER_ATTEMPT, "avg_launch_ms": avg_ms, "attempts_per_launch": att_per_launch},
         "kernel_ms_per_step": {"sort": ks["sort_ms"] / max(1, ks["sort_launches"]), "sweep": avg_ms,
                                "volume": ks["volume_ms"] / max(1, ks["volume_launches"]) if ks["volume_launches"] else 0.0},

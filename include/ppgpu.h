@@ -74,6 +74,7 @@ typedef struct pp_guard_stats {
 	long long mismatches;  /* audit mode: FP32 decisions outside the band that FP64 contradicts (must be 0) */
 	double max_err_r2;     /* audit mode: largest |r^2_fp32 - r^2_fp64| seen */
 	double max_err_cos;    /* audit mode: largest |cos_fp32 - cos_fp64| seen */
+	long long nl_overflows; /* neighbour lists that overflowed their capacity (those moves took the 27-cell path) */
 } pp_guard_stats;
 
 typedef struct pp_engine pp_engine;
@@ -155,6 +156,15 @@ int pp_gpu_kernel_stats(pp_engine *e, pp_kernel_stats *out, int reset);
  * instead of one per kernel; the launches and the trajectory are the same). enable = 0 turns the graphs
  * off (every kernel launched on the stream); per-group event timing always uses stream launches. */
 int pp_gpu_set_graphs(pp_engine *e, int enable);
+
+/* Per-epoch neighbour lists (default on). Between two re-sorts no particle leaves its cell and each moves
+ * at most once per round, so after every re-sort each particle's candidates in the 27 surrounding cells
+ * that lie closer than a radius covering the epoch's largest possible motion (and, for NPT, its accepted
+ * compressions) are listed, and plain moves test only those pairs. A pair left out can neither overlap nor
+ * bond during the epoch, so the decisions, hence the trajectory, are the full 27-cell scan's bit for bit.
+ * enable = 0 scans the 27 cells in every move. No counterpart in the reference, whose MC_energy walks the
+ * 27 cell lists on every call (MC.c:272-309). */
+int pp_gpu_set_neighbour_lists(pp_engine *e, int enable);
 
 /* Enqueues n sweeps between two CUDA events recorded on the engine's stream, waits, and returns the
  * elapsed device time in *ms. */
@@ -264,9 +274,10 @@ int pp_gpu_learned_stats(pp_engine *e, long long tries[PP_MIX], long long accept
 
 /* ------------------------------------------------------------------ autotuner */
 /* Chooses the engine's schedule on the live system by timing it: the checkerboard rounds between cell-grid
- * re-sorts (2, 4, 8, 16), the re-sorts between physical reorders of the FP64 state (4, 16, 64) and the cell
+ * re-sorts (1, 2, 4, 8, 16), the re-sorts between physical reorders of the FP64 state (4, 16, 64), the cell
  * edge as a multiple of its minimum (1.0, 1.2, 1.5: the cell occupancy, hence attempts per round and
- * neighbours per attempt). Each candidate runs 2 + trial_sweeps ordinary sweeps (they are part of the
+ * neighbours per attempt) and, when they are enabled, the neighbour lists on or off (their radius grows
+ * with the re-sort period). Each candidate runs 2 + trial_sweeps ordinary sweeps (they are part of the
  * trajectory) timed with CUDA events; the one with the most move attempts per second is kept. NPT replicas
  * keep the compression margin of their cell edge for every candidate period. No counterpart in the
  * reference. */
@@ -277,6 +288,7 @@ typedef struct pp_tune_result {
 	double attempts_per_s;           /* of the chosen schedule */
 	double baseline_attempts_per_s;  /* of the schedule before tuning */
 	int n_tried;
+	int neighbour_lists;             /* chosen (tried both ways when the lists are enabled) */
 } pp_tune_result;
 
 int pp_gpu_autotune(pp_engine *e, int trial_sweeps, pp_tune_result *out);

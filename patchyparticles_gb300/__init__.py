@@ -62,6 +62,7 @@ class PPGuardStats(ctypes.Structure):
         ("mismatches", ctypes.c_longlong),
         ("max_err_r2", ctypes.c_double),
         ("max_err_cos", ctypes.c_double),
+        ("nl_overflows", ctypes.c_longlong),
     ]
 
 
@@ -101,6 +102,7 @@ class PPTuneResult(ctypes.Structure):
         ("attempts_per_s", ctypes.c_double),
         ("baseline_attempts_per_s", ctypes.c_double),
         ("n_tried", ctypes.c_int),
+        ("neighbour_lists", ctypes.c_int),
     ]
 
 
@@ -124,7 +126,7 @@ EXPORTED = [
     "pp_gpu_energy_noalloc", "pp_mlp_forward", "pp_mlp_grad", "pp_default_learned_params", "pp_gpu_learned_init",
     "pp_gpu_learned_set_weights", "pp_gpu_learned_get_weights", "pp_gpu_set_proposal", "pp_gpu_learned_collect",
     "pp_gpu_learned_train", "pp_gpu_learned_samples", "pp_gpu_learned_clear_samples", "pp_gpu_learned_features",
-    "pp_gpu_learned_stats", "pp_gpu_autotune", "pp_gpu_set_graphs",
+    "pp_gpu_learned_stats", "pp_gpu_autotune", "pp_gpu_set_graphs", "pp_gpu_set_neighbour_lists",
 ]
 
 
@@ -187,6 +189,7 @@ def load_library(path=None):
         "pp_gpu_learned_stats": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
         "pp_gpu_autotune": (ctypes.c_int, [vp, ctypes.c_int, ctypes.POINTER(PPTuneResult)]),
         "pp_gpu_set_graphs": (ctypes.c_int, [vp, ctypes.c_int]),
+        "pp_gpu_set_neighbour_lists": (ctypes.c_int, [vp, ctypes.c_int]),
         "pp_mlp_grad": (ctypes.c_int, [fp, ctypes.c_int, fp, ctypes.c_double, ctypes.c_double, ctypes.c_int, fp, dp]),
     }
     for name, (res, args) in sig.items():
@@ -346,6 +349,9 @@ class Engine:
 
     def set_graphs(self, enable=True):
         self._check(self.lib.pp_gpu_set_graphs(self.h, 1 if enable else 0))
+
+    def set_neighbour_lists(self, enable=True):
+        self._check(self.lib.pp_gpu_set_neighbour_lists(self.h, 1 if enable else 0))
 
     def autotune(self, trial_sweeps=20):
         t = PPTuneResult()

@@ -44,6 +44,8 @@ struct pp_engine {
 	double cell_scale;    /* cell edge / minimum edge (autotuner) */
 	int any_npt;
 	int any_audit;
+	int nl_mode;          /* per-epoch neighbour lists for plain moves (pp_gpu_set_neighbour_lists) */
+	int nl_valid;         /* the current epoch's lists are built and only plain moves ran since */
 	/* event timing */
 	int timing;
 	int n_ev;
@@ -206,6 +208,7 @@ static int create_common(const pp_params *prms, int n, pp_engine **out) {
 	e->reorder_every = 16;
 	e->cell_scale = 1.0;
 	e->graphs_on = 1;
+	e->nl_mode = 1;
 	for(int i = 0; i < n; i++) {
 		if(e->prm[i].guard_eps <= 0.) e->prm[i].guard_eps = 1e-5;
 		if(e->prm[i].ensemble == PP_NPT) e->any_npt = 1;
@@ -246,6 +249,11 @@ static void free_device(pp_engine *e) {
 	e->pin_n = 0;
 	if(e->d.ctr) cudaFree(e->d.ctr);
 	e->d.ctr = NULL;
+	if(e->d.nl) cudaFree(e->d.nl);
+	if(e->d.nl_cnt) cudaFree(e->d.nl_cnt);
+	e->d.nl = e->d.nl_cnt = NULL;
+	e->d.nl_k = 0;
+	e->nl_valid = 0;
 	drop_graphs(e);
 	/* layout-sized buffers of the learned proposal */
 	if(e->d.simg) cudaFree(e->d.simg);
@@ -423,6 +431,11 @@ static int do_resort(pp_engine *e) {
 	}
 	CK(ppi_resort(&e->d, e->epoch, e->stream, &nl));
 	if(e->proposal == PP_PROPOSAL_LEARNED && e->d.simg) CK(ppi_canon(&e->d, e->stream, &nl));
+	e->nl_valid = 0;
+	if(e->proposal == PP_PROPOSAL_PLAIN && e->d.nl_k > 0) {
+		CK(ppi_nlist(&e->d, e->stream, &nl));
+		e->nl_valid = 1;
+	}
 	e->launches += nl;
 	e->epoch++;
 	return PP_OK;
@@ -434,6 +447,73 @@ static int run_energy(pp_engine *e, int mode) {
 	CK(ppi_energy(&e->d, mode, e->stream, &nl));
 	e->launches += nl;
 	return read_states(e);
+}
+
+/* Squared radius of replica r's neighbour lists. Between two re-sorts (at most resort_every rounds) each
+ * particle moves at most once per round by |d| <= sqrt(3)/2 Disp_max, so a pair's separation changes by at
+ * most sqrt(3) Disp_max per round; NPT adds the accepted rescalings (each scales one axis by a factor in
+ * [exp(-max/2), exp(max/2)], at most one per round, and one more for the candidate box). A pair farther
+ * apart than the radius at the re-sort therefore stays beyond r_cut + 1e-3 and outside the FP32 guard band
+ * on r^2 for the whole epoch. FP64-precision replicas get no lists (every pair takes the exact path). */
+static float nl_radius2(const pp_engine *e, int r) {
+	const pp_params *p = e->prm + r;
+	if(p->precision == PP_PREC_FP64) return 0.f;
+	const double E = (double) e->resort_every, rc = 1. + p->kf_delta;
+	const double base = sqrt((rc + 1e-3) * (rc + 1e-3) + p->guard_eps);
+	const double motion = sqrt(3.) * E * p->disp_max;
+	double R = base + motion;
+	if(p->ensemble == PP_NPT) {
+		const double smin = exp(-0.5 * p->rescale_factor_max * (E + 1.)), smax = exp(0.5 * p->rescale_factor_max * E);
+		R = (base + smax * motion) / smin;
+	}
+	R += 1e-3;
+	return (float) (R * R * (1. + 1e-6));
+}
+
+/* Radii of every replica and the per-particle list capacity (a generous bound on the listed count at the
+ * replica's density, 1.5x the density for NPT); (re)allocates the lists when the capacity grows. A list
+ * that overflows anyway sends its particle's attempts to the exact 27-cell path. */
+static int setup_nlists(pp_engine *e) {
+	int K = 0;
+	for(int r = 0; r < e->nrep; r++) {
+		e->h_rp[r].nl_r2f = e->nl_mode ? nl_radius2(e, r) : 0.f;
+		if(!(e->h_rp[r].nl_r2f > 0.f)) continue;
+		const double R = sqrt((double) e->h_rp[r].nl_r2f), *b = e->h_box[r];
+		double rho = e->N[r] / (b[0] * b[1] * b[2]);
+		if(e->prm[r].ensemble == PP_NPT) rho *= 1.5;
+		const double mean = 4.18879020478639 * R * R * R * rho;
+		int k = (int) ceil(mean + 6. * sqrt(mean) + 6.);
+		if(k > K) K = k;
+	}
+	if(K > 0) K = K < 8 ? 8 : (K > 128 ? 128 : (K + 3) & ~3);
+	{ /* a capacity override for tests of the overflow path (PPGPU_NL_CAP, rounded up to a multiple of 4) */
+		const char *v = getenv("PPGPU_NL_CAP");
+		if(K > 0 && v && atoi(v) > 0 && atoi(v) <= 128) K = (atoi(v) + 3) & ~3;
+	}
+	if(!e->nl_mode || e->d.ntot >= (1 << 27)) K = 0; /* a list entry holds sorted positions below 2^27 */
+	if(K == 0) {
+		if(e->d.nl) cudaFree(e->d.nl);
+		if(e->d.nl_cnt) cudaFree(e->d.nl_cnt);
+		e->d.nl = e->d.nl_cnt = NULL;
+		if(e->d.nl_k) e->graph_gen++;
+		e->d.nl_k = 0;
+		e->nl_valid = 0;
+		return PP_OK;
+	}
+	if(K > e->d.nl_k || e->d.nl == NULL) {
+		drop_graphs(e);
+		e->graph_gen++;
+		if(e->d.nl) cudaFree(e->d.nl);
+		if(e->d.nl_cnt) cudaFree(e->d.nl_cnt);
+		e->d.nl = e->d.nl_cnt = NULL;
+		e->d.nl_k = 0;
+		e->nl_valid = 0;
+		const size_t n1 = e->d.ntot > 0 ? (size_t) e->d.ntot : 1;
+		CU(cudaMalloc((void **) &e->d.nl, sizeof(int) * (size_t) K * n1));
+		CU(cudaMalloc((void **) &e->d.nl_cnt, sizeof(int) * n1));
+		e->d.nl_k = K;
+	}
+	return PP_OK;
 }
 
 static int commit(pp_engine *e) {
@@ -497,6 +577,8 @@ static int commit(pp_engine *e) {
 	CU(cudaMemsetAsync(d->out_overlaps, 0, sizeof(int) * n1, e->stream));
 	CU(cudaMemsetAsync(d->grid, 0, sizeof(ppi_grid) * e->nrep, e->stream));
 	int rc = ensure_pinned(e, n1);
+	if(rc != PP_OK) return rc;
+	rc = setup_nlists(e);
 	if(rc != PP_OK) return rc;
 	int *crep = malloc(sizeof(int) * (cells > 0 ? cells : 1));
 	int *rep = malloc(sizeof(int) * n1);
@@ -755,9 +837,11 @@ static int capture_period(pp_engine *e, int v) {
 	}
 	rc |= ppi_resort(&e->d, -1, e->stream, &nl);
 	if(learned) rc |= ppi_canon(&e->d, e->stream, &nl);
+	const int lists = !learned && e->d.nl_k > 0;
+	if(lists) rc |= ppi_nlist(&e->d, e->stream, &nl);
 	for(int r = 0; r < R; r++) {
 		if(learned) rc |= ppi_round_learned(&e->d, -1 - r, slots, e->any_audit, e->stream, &nl);
-		else rc |= ppi_round(&e->d, -1 - r, slots, e->any_audit, e->stream, &nl);
+		else rc |= ppi_round(&e->d, -1 - r, slots, e->any_audit, lists, e->stream, &nl);
 		if(e->any_npt) {
 			rc |= ppi_volume(&e->d, -1 - r, e->stream, &nl);
 			if(learned) rc |= ppi_canon(&e->d, e->stream, &nl);
@@ -798,10 +882,26 @@ static int replay_period(pp_engine *e) {
 	long long nl = 0;
 	CK(ppi_set_counters(&e->d, e->round_counter, e->epoch, e->sweep_counter, e->stream, &nl));
 	CU(cudaGraphLaunch(e->gexec[v], e->stream));
+	e->nl_valid = e->proposal == PP_PROPOSAL_PLAIN && e->d.nl_k > 0;
 	e->launches += nl + e->gnodes[v];
 	e->round_counter += e->resort_every;
 	e->sweep_counter += e->resort_every;
 	e->epoch++;
+	return PP_OK;
+}
+
+int pp_gpu_set_neighbour_lists(pp_engine *e, int enable) {
+	if(e == NULL) return PP_ERR_ARG;
+	enable = enable ? 1 : 0;
+	if(enable == e->nl_mode) return PP_OK;
+	e->nl_mode = enable;
+	if(!e->committed) return PP_OK;
+	int rc = setup_nlists(e);
+	if(rc != PP_OK) return rc;
+	drop_graphs(e);
+	e->graph_gen++;
+	e->nl_valid = 0; /* lists are (re)built at the next re-sort */
+	CU(cudaMemcpyAsync(e->d.rp, e->h_rp, sizeof(ppi_rparams) * e->nrep, cudaMemcpyHostToDevice, e->stream));
 	return PP_OK;
 }
 
@@ -839,8 +939,11 @@ int pp_gpu_sweeps(pp_engine *e, long long n) {
 			int colours[8];
 			colour_order(e->round_counter, colours);
 			if((rc = ev_begin(e, 1, &ev)) != PP_OK) return rc;
-			if(e->proposal == PP_PROPOSAL_LEARNED) CK(ppi_round_learned(&e->d, e->round_counter, colours, e->any_audit, e->stream, &nl));
-			else CK(ppi_round(&e->d, e->round_counter, colours, e->any_audit, e->stream, &nl));
+			if(e->proposal == PP_PROPOSAL_LEARNED) {
+				CK(ppi_round_learned(&e->d, e->round_counter, colours, e->any_audit, e->stream, &nl));
+				e->nl_valid = 0; /* learned moves reach farther than the lists' radius */
+			}
+			else CK(ppi_round(&e->d, e->round_counter, colours, e->any_audit, e->nl_valid, e->stream, &nl));
 			if((rc = ev_end(e, ev)) != PP_OK) return rc;
 			e->round_counter++;
 			e->launches += nl;
@@ -982,6 +1085,7 @@ int pp_gpu_guard_stats(pp_engine *e, pp_guard_stats *out, int reset) {
 		g.pairs += (long long) s->pairs;
 		g.fallbacks += (long long) s->fallbacks;
 		g.mismatches += (long long) s->mismatches;
+		g.nl_overflows += (long long) s->nl_overflow;
 		float a, b;
 		memcpy(&a, &s->max_err_r2_bits, 4);
 		memcpy(&b, &s->max_err_cos_bits, 4);
@@ -990,6 +1094,7 @@ int pp_gpu_guard_stats(pp_engine *e, pp_guard_stats *out, int reset) {
 		if(reset) {
 			s->pairs = s->fallbacks = s->mismatches = 0;
 			s->max_err_r2_bits = s->max_err_cos_bits = 0;
+			s->nl_overflow = 0;
 		}
 	}
 	if(out) *out = g;
@@ -1690,12 +1795,17 @@ static double tuned_w_min(const pp_engine *e, int r) {
 }
 
 /* installs a schedule; the next round re-sorts onto the new grid */
-static int apply_schedule(pp_engine *e, int resort, int reorder, double scale) {
+static int apply_schedule(pp_engine *e, int resort, int reorder, double scale, int lists) {
 	drop_graphs(e);
 	e->resort_every = resort;
 	e->reorder_every = reorder;
 	e->cell_scale = scale;
+	e->nl_mode = lists;
 	for(int r = 0; r < e->nrep; r++) e->h_rp[r].w_min = tuned_w_min(e, r);
+	int rc = setup_nlists(e); /* the lists' radius covers one period of motion */
+	if(rc != PP_OK) return rc;
+	e->nl_valid = 0;
+	e->graph_gen++;
 	CU(cudaMemcpyAsync(e->d.rp, e->h_rp, sizeof(ppi_rparams) * e->nrep, cudaMemcpyHostToDevice, e->stream));
 	e->round_counter += (resort - e->round_counter % resort) % resort;
 	return PP_OK;
@@ -1725,34 +1835,36 @@ int pp_gpu_autotune(pp_engine *e, int trial_sweeps, pp_tune_result *out) {
 	int rc = ready(e);
 	if(rc != PP_OK) return rc;
 	if(trial_sweeps < 1 || trial_sweeps > 100000) return set_err(e, PP_ERR_ARG, "trial_sweeps must lie in [1, 100000]");
-	const int resorts[] = { 2, 4, 8, 16 }, reorders[] = { 4, 16, 64 };
+	const int resorts[] = { 1, 2, 4, 8, 16 }, reorders[] = { 4, 16, 64 };
 	const double scales[] = { 1.0, 1.2, 1.5 };
-	const int r0 = e->resort_every, o0 = e->reorder_every;
+	const int r0 = e->resort_every, o0 = e->reorder_every, l0 = e->nl_mode;
 	const double s0 = e->cell_scale;
 	double base = 0.;
 	if((rc = time_schedule(e, trial_sweeps, &base)) != PP_OK) return rc;
-	int best_r = r0, best_o = o0, tried = 1;
+	int best_r = r0, best_o = o0, best_l = l0, tried = 1;
 	double best_s = s0, best = base;
-	for(int a = 0; a < 4; a++)
-		for(int b = 0; b < 3; b++)
-			for(int c = 0; c < 3; c++) {
-				if(resorts[a] == r0 && reorders[b] == o0 && scales[c] == s0) continue;
-				if((rc = apply_schedule(e, resorts[a], reorders[b], scales[c])) != PP_OK) return rc;
-				double v = 0.;
-				rc = time_schedule(e, trial_sweeps, &v);
-				if(rc != PP_OK) { /* a schedule the boxes cannot hold: fall back to the best so far */
-					apply_schedule(e, best_r, best_o, best_s);
-					return rc;
+	for(int l = l0; l >= 0; l--) /* lists on and off when the caller allows them */
+		for(int a = 0; a < 5; a++)
+			for(int b = 0; b < 3; b++)
+				for(int c = 0; c < 3; c++) {
+					if(resorts[a] == r0 && reorders[b] == o0 && scales[c] == s0 && l == l0) continue;
+					if((rc = apply_schedule(e, resorts[a], reorders[b], scales[c], l)) != PP_OK) return rc;
+					double v = 0.;
+					rc = time_schedule(e, trial_sweeps, &v);
+					if(rc != PP_OK) { /* a schedule the boxes cannot hold: fall back to the best so far */
+						apply_schedule(e, best_r, best_o, best_s, best_l);
+						return rc;
+					}
+					tried++;
+					if(v > best) {
+						best = v;
+						best_r = resorts[a];
+						best_o = reorders[b];
+						best_s = scales[c];
+						best_l = l;
+					}
 				}
-				tried++;
-				if(v > best) {
-					best = v;
-					best_r = resorts[a];
-					best_o = reorders[b];
-					best_s = scales[c];
-				}
-			}
-	if((rc = apply_schedule(e, best_r, best_o, best_s)) != PP_OK) return rc;
+	if((rc = apply_schedule(e, best_r, best_o, best_s, best_l)) != PP_OK) return rc;
 	if(out) {
 		out->resort_every = best_r;
 		out->reorder_every = best_o;
@@ -1760,6 +1872,7 @@ int pp_gpu_autotune(pp_engine *e, int trial_sweeps, pp_tune_result *out) {
 		out->attempts_per_s = best;
 		out->baseline_attempts_per_s = base;
 		out->n_tried = tried;
+		out->neighbour_lists = best_l;
 	}
 	return PP_OK;
 }

@@ -55,7 +55,8 @@ typedef struct ppi_rparams {
 	double base[4][3];     /* tetrahedral base patches, bit-identical to system.c:20-31 */
 	uint64_t acc_thr[32];  /* accept a move with dE = +k iff U53 < acc_thr[k], U53 uniform in [0, 2^53) */
 	float cosmax_f, sqr_rcut_f, eps_f, disp_max_f, theta_max_f, base_f;
-	float pad1[2];
+	float nl_r2f;          /* squared radius of the per-epoch neighbour lists (0: no lists, exact path) */
+	float pad1;
 	uint64_t seed;
 } ppi_rparams;
 
@@ -72,6 +73,7 @@ typedef struct ppi_rstate {
 	int error_info;
 	unsigned long long pairs, fallbacks, mismatches;
 	unsigned int max_err_r2_bits, max_err_cos_bits;
+	unsigned long long nl_overflow; /* particles whose neighbour list overflowed (their attempts take the exact path) */
 } ppi_rstate;
 
 typedef struct ppi_grid {
@@ -142,7 +144,7 @@ typedef struct ppi_dev {
 	int audit_any;     /* some replica audits: every pass runs in audit mode */
 	int lanes;         /* lanes per attempt of the colour and energy passes (4 or 8; 0 = default) */
 	int clist_cap;
-	int pad1;
+	int nl_k;          /* neighbour-list capacity per particle (multiple of 4; 0 = no lists) */
 	ppi_rparams *rp;
 	ppi_rstate *rs;
 	ppi_grid *grid;
@@ -165,13 +167,20 @@ typedef struct ppi_dev {
 	int sample_cap;
 	int pad2;
 	ppi_ctr *ctr;                 /* graph-path counters */
+	/* per-epoch neighbour lists, per sorted position: nl[k * nl_k + j] = candidate sorted position << 5 |
+	 * cell offset code (dx + 1) + 3 (dy + 1) + 9 (dz + 1); nl_cnt[k] = entries (> nl_k: overflow) */
+	int *nl;
+	int *nl_cnt;
 } ppi_dev;
 
 #define PPI_MAX_PARTNERS 24
 
 /* launchers (ppgpu_kernels.cu); each returns a cudaError_t value as int and adds its launches to *nl */
 int ppi_resort(const ppi_dev *d, long long epoch, cudaStream_t s, long long *nl);
-int ppi_round(const ppi_dev *d, long long round, const int *colours, int audit, cudaStream_t s, long long *nl);
+/* use_nl: the epoch's neighbour lists are valid (built by ppi_nlist after the re-sort, plain moves since) */
+int ppi_round(const ppi_dev *d, long long round, const int *colours, int audit, int use_nl, cudaStream_t s, long long *nl);
+/* neighbour lists of every sorted position for the current epoch (after ppi_resort) */
+int ppi_nlist(const ppi_dev *d, cudaStream_t s, long long *nl);
 int ppi_energy(const ppi_dev *d, int mode, cudaStream_t s, long long *nl);
 int ppi_volume(const ppi_dev *d, long long sweep, cudaStream_t s, long long *nl);
 int ppi_gram_schmidt(const ppi_dev *d, int first, int count, cudaStream_t s, long long *nl);

@@ -5,14 +5,16 @@
  * r_cut, random origin shift) and the particles are counting-sorted into cell order as FP32 working
  * records (spos 16 B + sori 48 B) rebuilt from the FP64 canonical state:
  *   k_grid, k_assign, k_scan_*, k_scatter, k_cellfin (deterministic in-cell order, colour lists)
+ * and every particle's neighbour list for the epoch is built (k_nlist: the candidates that can come within
+ * r_cut before the next re-sort).
  * One round = the 8 colours of the 2x2x2 checkerboard, one launch each (k_colour): every non-empty
  * cell of the colour gets one roto-translation attempt on a uniformly chosen particle of the cell
- * (MC_move_rototranslate, MC.c:311-340), run by a group of 4 (or 8) lanes that share the 27-cell
- * neighbourhood. Same-colour cells are never adjacent and a move that leaves its cell is rejected, so
- * concurrent moves never interact and the cell lists stay valid for the whole epoch. The pair test is
- * FP32 with an FP64 re-evaluation inside the guard band, bit-identical to MC_would_interact
- * (MC.c:232-266). Accepted moves update the FP64 state with FP64 arithmetic (r + disp, q (x) dq) and
- * the FP32 record in place.
+ * (MC_move_rototranslate, MC.c:311-340). A warp takes 64 attempts and flattens their neighbour pairs
+ * (from the lists, or from the 27 cells) into one shared pair list that its lanes walk 32 pairs per step.
+ * Same-colour cells are never adjacent and a move that leaves its cell is rejected, so concurrent moves
+ * never interact and the cell lists stay valid for the whole epoch. The pair test is FP32 with an FP64
+ * re-evaluation inside the guard band, bit-identical to MC_would_interact (MC.c:232-266). Accepted moves
+ * update the FP64 state with FP64 arithmetic (r + disp, q (x) dq) and the FP32 record in place.
  * k_energy: energy from scratch (per-particle bonds/overlaps, output.c:213-268) or of the NPT candidate
  * box (MC.c:487-495); k_vol_*: the NPT volume move (MC.c:450-513).
  */
@@ -1203,8 +1205,98 @@ __device__ __forceinline__ void defer_attempt(const ppi_dev &d, TileSmem &S, int
 	}
 }
 
-/* the TA attempts of list positions b + lane (e0) and b + 32 + lane (e1); ent.x < 0: none */
+/* the pair list's np entries, PSTEP steps of 32 pairs at a time: distance filter, certain overlaps,
+ * close pairs compacted into the patch-test list */
 template <int MODE>
+__device__ __forceinline__ void tile_steps(const ppi_dev &d, TileSmem &S, const int lane, const int np, Acc &A) {
+	const unsigned lt = (1u << lane) - 1u;
+	/* PSTEP steps of 32 pairs at a time: the candidate loads of all of them are issued before any is
+	 * used, so that a step group costs one memory latency instead of PSTEP */
+	for(int p0 = 0; p0 < np; p0 += 32 * PSTEP) {
+		int en[PSTEP], ok[PSTEP];
+		float4 qa[PSTEP];
+#pragma unroll
+		for(int u = 0; u < PSTEP; u++) {
+			const int p = p0 + 32 * u + lane;
+			en[u] = 0;
+			ok[u] = 0;
+			qa[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+			if(p < np) {
+				en[u] = S.pbuf[p];
+				const int a = (en[u] >> 4) & 63, off = en[u] >> 10;
+				ok[u] = off != 0 && !(S.flag[a] & (TF_OVER | TF_DEFER));
+				if(ok[u]) qa[u] = d.spos[S.mi[a] + off];
+			}
+		}
+		int close[PSTEP];
+#pragma unroll
+		for(int u = 0; u < PSTEP; u++) {
+			close[u] = 0;
+			if(ok[u]) {
+				const int a = (en[u] >> 4) & 63;
+				const PairGeo G = pair_geo(S, a, en[u] & 15, qa[u]);
+				const float r2o = fmaf(G.dxo, G.dxo, fmaf(G.dyo, G.dyo, G.dzo * G.dzo));
+				const float r2n = fmaf(G.dxn, G.dxn, fmaf(G.dyn, G.dyn, G.dzn * G.dzn));
+				const float2 lim = S.lim[a];
+				A.pairs += 2;
+				if(MODE != MODE_AUDIT && r2n < lim.x) atomicOr(&S.flag[a], TF_OVER); /* certain overlap of the candidate state */
+				else close[u] = MODE == MODE_AUDIT || r2o < lim.y || r2n < lim.y;
+			}
+		}
+		/* compact the group's close pairs into the patch-test list */
+		unsigned m[PSTEP];
+		int tot = 0;
+#pragma unroll
+		for(int u = 0; u < PSTEP; u++) {
+			m[u] = __ballot_sync(0xffffffffu, close[u]);
+			tot += __popc(m[u]);
+		}
+		if(tot) {
+			if(S.nc + tot > TILE_CCAP) tile_close<MODE>(d, S, lane, A);
+			int base = S.nc;
+#pragma unroll
+			for(int u = 0; u < PSTEP; u++) {
+				if(close[u]) S.cbuf[base + __popc(m[u] & lt)] = en[u];
+				base += __popc(m[u]);
+			}
+			__syncwarp();
+			if(lane == 0) S.nc = base;
+			__syncwarp();
+		}
+	}
+}
+
+/* attempt a's pairs from its mover's neighbour list (n entries) into the pair list from position pos, in
+ * the packing of write_pairs: the row tag of an entry with cell offset code c is c / 3 ((dy + 1) +
+ * 3 (dz + 1)); pair_geo recovers dx from the cells' x indices */
+__device__ __forceinline__ void write_list_pairs(const ppi_dev &d, TileSmem &S, int a, int n, int pos) {
+	const int i = S.mi[a];
+	const int4 *L = (const int4 *) (d.nl + (size_t) i * d.nl_k);
+	for(int k0 = 0; k0 < n; k0 += 16) {
+		int4 v[4];
+#pragma unroll
+		for(int c = 0; c < 4; c++) v[c] = (k0 + 4 * c < n) ? L[(k0 >> 2) + c] : make_int4(0, 0, 0, 0);
+#pragma unroll
+		for(int c = 0; c < 4; c++) {
+			const int e4[4] = { v[c].x, v[c].y, v[c].z, v[c].w };
+#pragma unroll
+			for(int u = 0; u < 4; u++) {
+				const int k = k0 + 4 * c + u;
+				if(k >= n) continue;
+				const int jq = (int) ((unsigned) e4[u] >> 5), code = e4[u] & 31;
+				const int off = jq - i, tag = (a << 4) | (code / 3);
+				if(off >= TILE_OFF_MAX || off <= -TILE_OFF_MAX) {
+					atomicOr(&S.flag[a], TF_DEFER);
+					S.pbuf[pos + k] = tag; /* offset 0 = the mover itself: skipped */
+				}
+				else S.pbuf[pos + k] = (int) ((unsigned) off << 10) | tag;
+			}
+		}
+	}
+}
+
+/* the TA attempts of list positions b + lane (e0) and b + 32 + lane (e1); ent.x < 0: none */
+template <int MODE, bool LIST>
 __device__ __forceinline__ void tile_round(const ppi_dev &d, TileSmem &S, const int lane, const int4 e0, const int4 e1, int b, int col, long long round, Acc &A) {
 	const int loc0 = tile_setup(d, S, lane, e0, round, A);
 	const int loc1 = tile_setup(d, S, lane + 32, e1, round, A);
@@ -1213,9 +1305,44 @@ __device__ __forceinline__ void tile_round(const ppi_dev &d, TileSmem &S, const 
 		S.nu = 0;
 	}
 	__syncwarp();
-	const unsigned lt = (1u << lane) - 1u;
+	if(LIST) {
+		/* the pairs come from the movers' neighbour lists, one half of the attempts (a lane each) at a time */
 #pragma unroll 1
-	for(int pz = 0; pz < 3; pz++) {
+		for(int h = 0; h < 2; h++) {
+			const int a = lane + 32 * h;
+			int n = 0;
+			if(!(S.flag[a] & (TF_OVER | TF_CLOSED | TF_DEFER))) {
+				n = d.nl_cnt[S.mi[a]];
+				if(n > d.nl_k) { /* the list overflowed: the exact 27-cell path */
+					atomicOr(&S.flag[a], TF_DEFER);
+					n = 0;
+				}
+			}
+			int incl = n;
+#pragma unroll
+			for(int o = 1; o < 32; o <<= 1) {
+				const int v = __shfl_up_sync(0xffffffffu, incl, o);
+				if(lane >= o) incl += v;
+			}
+			const int total = __shfl_sync(0xffffffffu, incl, 31);
+			/* lanes whose slices fit the pair list together (a slice is at most nl_k <= 128 < TILE_PCAP) */
+			int done = 0;
+			while(done < total) {
+				const int start = incl - n;
+				const int mine = n > 0 && start >= done && incl - done <= TILE_PCAP;
+				const unsigned take = __ballot_sync(0xffffffffu, mine);
+				if(take == 0) break; /* unreachable while nl_k <= TILE_PCAP */
+				if(mine) write_list_pairs(d, S, a, n, start - done);
+				const int end = __shfl_sync(0xffffffffu, incl, 31 - __clz(take));
+				__syncwarp();
+				tile_steps<MODE>(d, S, lane, end - done, A);
+				done = end;
+				__syncwarp();
+			}
+		}
+	}
+#pragma unroll 1
+	for(int pz = 0; pz < (LIST ? 0 : 3); pz++) {
 		PlaneRanges P0, P1;
 		const int n0 = plane_ranges(d, S, lane, pz, P0);
 		const int n1 = plane_ranges(d, S, lane + 32, pz, P1);
@@ -1240,60 +1367,7 @@ __device__ __forceinline__ void tile_round(const ppi_dev &d, TileSmem &S, const 
 			write_pairs(S, lane + 32, pz, P1, pos + n0);
 		}
 		__syncwarp();
-		/* PSTEP steps of 32 pairs at a time: the candidate loads of all of them are issued before any is
-		 * used, so that a step group costs one memory latency instead of PSTEP */
-		for(int p0 = 0; p0 < np; p0 += 32 * PSTEP) {
-			int en[PSTEP], ok[PSTEP];
-			float4 qa[PSTEP];
-#pragma unroll
-			for(int u = 0; u < PSTEP; u++) {
-				const int p = p0 + 32 * u + lane;
-				en[u] = 0;
-				ok[u] = 0;
-				qa[u] = make_float4(0.f, 0.f, 0.f, 0.f);
-				if(p < np) {
-					en[u] = S.pbuf[p];
-					const int a = (en[u] >> 4) & 63, off = en[u] >> 10;
-					ok[u] = off != 0 && !(S.flag[a] & (TF_OVER | TF_DEFER));
-					if(ok[u]) qa[u] = d.spos[S.mi[a] + off];
-				}
-			}
-			int close[PSTEP];
-#pragma unroll
-			for(int u = 0; u < PSTEP; u++) {
-				close[u] = 0;
-				if(ok[u]) {
-					const int a = (en[u] >> 4) & 63;
-					const PairGeo G = pair_geo(S, a, en[u] & 15, qa[u]);
-					const float r2o = fmaf(G.dxo, G.dxo, fmaf(G.dyo, G.dyo, G.dzo * G.dzo));
-					const float r2n = fmaf(G.dxn, G.dxn, fmaf(G.dyn, G.dyn, G.dzn * G.dzn));
-					const float2 lim = S.lim[a];
-					A.pairs += 2;
-					if(MODE != MODE_AUDIT && r2n < lim.x) atomicOr(&S.flag[a], TF_OVER); /* certain overlap of the candidate state */
-					else close[u] = MODE == MODE_AUDIT || r2o < lim.y || r2n < lim.y;
-				}
-			}
-			/* compact the group's close pairs into the patch-test list */
-			unsigned m[PSTEP];
-			int tot = 0;
-#pragma unroll
-			for(int u = 0; u < PSTEP; u++) {
-				m[u] = __ballot_sync(0xffffffffu, close[u]);
-				tot += __popc(m[u]);
-			}
-			if(tot) {
-				if(S.nc + tot > TILE_CCAP) tile_close<MODE>(d, S, lane, A);
-				int base = S.nc;
-#pragma unroll
-				for(int u = 0; u < PSTEP; u++) {
-					if(close[u]) S.cbuf[base + __popc(m[u] & lt)] = en[u];
-					base += __popc(m[u]);
-				}
-				__syncwarp();
-				if(lane == 0) S.nc = base;
-				__syncwarp();
-			}
-		}
+		tile_steps<MODE>(d, S, lane, np, A);
 	}
 	if(S.nc) tile_close<MODE>(d, S, lane, A);
 	/* guard-band pairs: certified FP64 decisions (no division chain); an undecided one defers its attempt */
@@ -1341,7 +1415,7 @@ __device__ __forceinline__ void tile_round(const ppi_dev &d, TileSmem &S, const 
 }
 
 /* one colour of a round: the colour's non-empty cells, TA per warp and iteration */
-template <int MODE>
+template <int MODE, bool LIST>
 __global__ void __launch_bounds__(32 * TILE_WARPS, MODE == MODE_FAST ? PPI_TILE_MIN_BLOCKS : 1) k_colour(ppi_dev d, long long round, int col) {
 	if(round < 0) { /* graph launch: round after the device counter, col = slot in the round's colour order */
 		round = ctr_index(round, d.ctr->round);
@@ -1370,7 +1444,7 @@ __global__ void __launch_bounds__(32 * TILE_WARPS, MODE == MODE_FAST ? PPI_TILE_
 	for(int b = lo; b < hi; b += TA) {
 		const int4 e0 = (b + lane < hi) ? list[b + lane] : none;
 		const int4 e1 = (b + 32 + lane < hi) ? list[b + 32 + lane] : none;
-		tile_round<MODE>(d, S, lane, e0, e1, b, col, round, A);
+		tile_round<MODE, LIST>(d, S, lane, e0, e1, b, col, round, A);
 		__syncwarp();
 	}
 	/* the deferred attempts, one per lane, exactly */
@@ -1386,6 +1460,65 @@ __global__ void __launch_bounds__(32 * TILE_WARPS, MODE == MODE_FAST ? PPI_TILE_
 	}
 	__syncwarp();
 	flush_block(d, A);
+}
+
+/* ------------------------------------------------------------------------------------------------ */
+/* per-epoch neighbour lists                                                                        */
+/* ------------------------------------------------------------------------------------------------ */
+/* Within an epoch (the rounds between two re-sorts) no particle leaves its cell and each moves at most
+ * once per round, by at most sqrt(3)/2 Disp_max (plus the NPT rescalings of accepted volume moves). The
+ * host sizes the list radius (rp.nl_r2f, ppgpu_host.c: nl_radius2) so that a pair farther apart when the
+ * list is built can neither overlap nor bond at any time of the epoch and stays outside the FP32 guard
+ * band. k_colour<MODE, true> then takes its pairs from the movers' lists instead of the 27 cells: the
+ * same decisions, hence the same trajectory, with fewer pair tests and no cell-range lookups. */
+#define NL_B 128 /* threads per CTA of the list build */
+
+/* list of sorted position i: candidates in the 27 cells closer than the replica's list radius */
+__global__ void __launch_bounds__(NL_B) k_nlist(ppi_dev d) {
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= d.ntot) return;
+	const float4 p = d.spos[i];
+	const int gc = __float_as_int(d.sori[3 * (size_t) i + 2].z);
+	const int r = d.cell_rep[gc];
+	const ppi_rparams &rp = d.rp[r];
+	const ppi_grid &g = d.grid[r];
+	const int K = d.nl_k;
+	const float R2 = rp.nl_r2f;
+	if(!(R2 > 0.f)) { /* no lists for this replica: its attempts take the exact path */
+		d.nl_cnt[i] = K + 1;
+		return;
+	}
+	int *out = d.nl + (size_t) i * K;
+	const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+	const int local = gc - rp.cell_base;
+	const int cx = local % nx, cy = (local / nx) % ny, cz = local / (nx * ny);
+	const float wx = g.wf[0], wy = g.wf[1], wz = g.wf[2];
+	int n = 0;
+#pragma unroll 1
+	for(int dz = -1; dz <= 1; dz++)
+#pragma unroll 1
+		for(int dy = -1; dy <= 1; dy++) {
+			const int *cs = d.cell_start + rp.cell_base + (wrapi(cz + dz, nz) * ny + wrapi(cy + dy, ny)) * nx;
+			const float oy = dy * wy, oz = dz * wz;
+#pragma unroll
+			for(int dx = -1; dx <= 1; dx++) {
+				const int c = wrapi(cx + dx, nx);
+				const unsigned code = (unsigned) ((dx + 1) + 3 * (dy + 1) + 9 * (dz + 1));
+				const float ox = dx * wx;
+				const int a = cs[c], b = cs[c + 1];
+				for(int jq = a; jq < b; jq++) {
+					if(jq == i) continue;
+					const float4 q = d.spos[jq];
+					const float ex = (q.x - p.x) + ox, ey = (q.y - p.y) + oy, ez = (q.z - p.z) + oz;
+					if(fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < R2) {
+						if(n < K) out[n] = (int) (((unsigned) jq << 5) | code);
+						n++;
+					}
+				}
+			}
+		}
+	d.nl_cnt[i] = n;
+	if(n > K) atomicAdd(&d.rs[r].nl_overflow, 1ull);
 }
 
 /* ------------------------------------------------------------------------------------------------ */
@@ -3090,7 +3223,7 @@ static int resident_grid(F f, int *cache, int block = 128) {
 }
 
 /* cached launch grids (one occupancy query each, made before any stream capture by ppi_prepare) */
-static int g_col_audit = 0, g_col_fast = 0, g_learn_audit = 0, g_learn_fast = 0, g_vol_grid = 0;
+static int g_col_audit = 0, g_col_fast = 0, g_learn_audit = 0, g_learn_fast = 0, g_vol_grid = 0, g_col_tl = 0, g_col_tla = 0;
 static int g_a1 = 0, g_a4 = 0, g_f1 = 0, g_f4 = 0, g_f8 = 0;
 
 extern "C" int ppi_resort(const ppi_dev *d, long long epoch, cudaStream_t s, long long *nl) {
@@ -3112,14 +3245,30 @@ extern "C" int ppi_resort(const ppi_dev *d, long long epoch, cudaStream_t s, lon
 
 static int lanes_of(const ppi_dev *d) { return d->lanes == 8 ? 8 : PPI_DEFAULT_LANES; }
 
-extern "C" int ppi_round(const ppi_dev *d, long long round, const int *colours, int audit, cudaStream_t s, long long *nl) {
-	if(audit || d->audit_any) {
-		int grid = resident_grid(k_colour<MODE_AUDIT>, &g_col_audit, 32 * TILE_WARPS);
-		for(int ci = 0; ci < 8; ci++) k_colour<MODE_AUDIT><<<grid, 32 * TILE_WARPS, 0, s>>>(*d, round, colours[ci]);
+extern "C" int ppi_nlist(const ppi_dev *d, cudaStream_t s, long long *nl) {
+	if(d->ntot <= 0 || d->nl_k <= 0) return 0;
+	k_nlist<<<(d->ntot + NL_B - 1) / NL_B, NL_B, 0, s>>>(*d);
+	*nl += 1;
+	return (int) cudaGetLastError();
+}
+
+extern "C" int ppi_round(const ppi_dev *d, long long round, const int *colours, int audit, int use_nl, cudaStream_t s, long long *nl) {
+	const int aud = audit || d->audit_any;
+	if(use_nl && d->nl_k > 0 && aud) {
+		int grid = resident_grid(k_colour<MODE_AUDIT, true>, &g_col_tla, 32 * TILE_WARPS);
+		for(int ci = 0; ci < 8; ci++) k_colour<MODE_AUDIT, true><<<grid, 32 * TILE_WARPS, 0, s>>>(*d, round, colours[ci]);
+	}
+	else if(use_nl && d->nl_k > 0) {
+		int grid = resident_grid(k_colour<MODE_FAST, true>, &g_col_tl, 32 * TILE_WARPS);
+		for(int ci = 0; ci < 8; ci++) k_colour<MODE_FAST, true><<<grid, 32 * TILE_WARPS, 0, s>>>(*d, round, colours[ci]);
+	}
+	else if(aud) {
+		int grid = resident_grid(k_colour<MODE_AUDIT, false>, &g_col_audit, 32 * TILE_WARPS);
+		for(int ci = 0; ci < 8; ci++) k_colour<MODE_AUDIT, false><<<grid, 32 * TILE_WARPS, 0, s>>>(*d, round, colours[ci]);
 	}
 	else {
-		int grid = resident_grid(k_colour<MODE_FAST>, &g_col_fast, 32 * TILE_WARPS);
-		for(int ci = 0; ci < 8; ci++) k_colour<MODE_FAST><<<grid, 32 * TILE_WARPS, 0, s>>>(*d, round, colours[ci]);
+		int grid = resident_grid(k_colour<MODE_FAST, false>, &g_col_fast, 32 * TILE_WARPS);
+		for(int ci = 0; ci < 8; ci++) k_colour<MODE_FAST, false><<<grid, 32 * TILE_WARPS, 0, s>>>(*d, round, colours[ci]);
 	}
 	*nl += 8;
 	return (int) cudaGetLastError();
@@ -3216,8 +3365,10 @@ static int learned_grid(F f, int *cache) {
 
 extern "C" int ppi_prepare(const ppi_dev *d) {
 	(void) d;
-	resident_grid(k_colour<MODE_AUDIT>, &g_col_audit, 32 * TILE_WARPS);
-	resident_grid(k_colour<MODE_FAST>, &g_col_fast, 32 * TILE_WARPS);
+	resident_grid(k_colour<MODE_AUDIT, false>, &g_col_audit, 32 * TILE_WARPS);
+	resident_grid(k_colour<MODE_FAST, false>, &g_col_fast, 32 * TILE_WARPS);
+	resident_grid(k_colour<MODE_AUDIT, true>, &g_col_tla, 32 * TILE_WARPS);
+	resident_grid(k_colour<MODE_FAST, true>, &g_col_tl, 32 * TILE_WARPS);
 	resident_grid(k_energy_vol, &g_vol_grid, 32 * TILE_WARPS);
 	resident_grid(k_energy<MODE_AUDIT, 1>, &g_a1);
 	resident_grid(k_energy<MODE_AUDIT, 4>, &g_a4);
