@@ -46,6 +46,7 @@ struct pp_engine {
 	int any_audit;
 	int nl_mode;          /* per-epoch neighbour lists for plain moves (pp_gpu_set_neighbour_lists) */
 	int nl_valid;         /* the current epoch's lists are built and only plain moves ran since */
+	int nl_all;           /* every replica has lists (the volume pass then takes its pairs from them) */
 	/* event timing */
 	int timing;
 	int n_ev;
@@ -475,9 +476,13 @@ static float nl_radius2(const pp_engine *e, int r) {
  * that overflows anyway sends its particle's attempts to the exact 27-cell path. */
 static int setup_nlists(pp_engine *e) {
 	int K = 0;
+	e->nl_all = 1;
 	for(int r = 0; r < e->nrep; r++) {
 		e->h_rp[r].nl_r2f = e->nl_mode ? nl_radius2(e, r) : 0.f;
-		if(!(e->h_rp[r].nl_r2f > 0.f)) continue;
+		if(!(e->h_rp[r].nl_r2f > 0.f)) {
+			e->nl_all = 0;
+			continue;
+		}
 		const double R = sqrt((double) e->h_rp[r].nl_r2f), *b = e->h_box[r];
 		double rho = e->N[r] / (b[0] * b[1] * b[2]);
 		if(e->prm[r].ensemble == PP_NPT) rho *= 1.5;
@@ -843,7 +848,7 @@ static int capture_period(pp_engine *e, int v) {
 		if(learned) rc |= ppi_round_learned(&e->d, -1 - r, slots, e->any_audit, e->stream, &nl);
 		else rc |= ppi_round(&e->d, -1 - r, slots, e->any_audit, lists, e->stream, &nl);
 		if(e->any_npt) {
-			rc |= ppi_volume(&e->d, -1 - r, e->stream, &nl);
+			rc |= ppi_volume(&e->d, -1 - r, lists && e->nl_all, e->stream, &nl);
 			if(learned) rc |= ppi_canon(&e->d, e->stream, &nl);
 		}
 	}
@@ -951,7 +956,7 @@ int pp_gpu_sweeps(pp_engine *e, long long n) {
 		if(e->any_npt) {
 			long long nl = 0;
 			if((rc = ev_begin(e, 2, &ev)) != PP_OK) return rc;
-			CK(ppi_volume(&e->d, s, e->stream, &nl));
+			CK(ppi_volume(&e->d, s, e->nl_valid && e->nl_all, e->stream, &nl));
 			if(e->proposal == PP_PROPOSAL_LEARNED) CK(ppi_canon(&e->d, e->stream, &nl)); /* positions and box may have changed */
 			if((rc = ev_end(e, ev)) != PP_OK) return rc;
 			e->launches += nl;

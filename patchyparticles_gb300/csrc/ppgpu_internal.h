@@ -182,7 +182,8 @@ int ppi_round(const ppi_dev *d, long long round, const int *colours, int audit, 
 /* neighbour lists of every sorted position for the current epoch (after ppi_resort) */
 int ppi_nlist(const ppi_dev *d, cudaStream_t s, long long *nl);
 int ppi_energy(const ppi_dev *d, int mode, cudaStream_t s, long long *nl);
-int ppi_volume(const ppi_dev *d, long long sweep, cudaStream_t s, long long *nl);
+/* use_nl: the candidate-box energy takes its pairs from the epoch's neighbour lists (every replica has them) */
+int ppi_volume(const ppi_dev *d, long long sweep, int use_nl, cudaStream_t s, long long *nl);
 int ppi_gram_schmidt(const ppi_dev *d, int first, int count, cudaStream_t s, long long *nl);
 int ppi_reorder(const ppi_dev *d, cudaStream_t s, long long *nl);
 /* writes x y z R00..R22 (12 doubles) of slots [first, first + count) into d->tmp_rec */

@@ -2906,6 +2906,99 @@ __device__ __forceinline__ void vol_lane_pairs(const ppi_dev &d, VolSmem &S, int
 		}
 }
 
+/* the pair list's np entries, PSTEP steps of 32 pairs at a time: certain overlaps, close pairs compacted
+ * into the patch-test list */
+__device__ __forceinline__ void vol_steps(const ppi_dev &d, VolSmem &S, const int lane, const int np, Acc &A) {
+	const unsigned lt = (1u << lane) - 1u;
+	for(int p0 = 0; p0 < np; p0 += 32 * PSTEP) {
+		int en[PSTEP], ok[PSTEP];
+		float4 qa[PSTEP];
+#pragma unroll
+		for(int u = 0; u < PSTEP; u++) {
+			const int p = p0 + 32 * u + lane;
+			en[u] = 0;
+			ok[u] = 0;
+			qa[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+			if(p < np) {
+				en[u] = S.pbuf[p];
+				const int a = (en[u] >> 4) & 63, off = en[u] >> 10;
+				ok[u] = off != 0;
+				if(ok[u]) qa[u] = d.spos[S.ki[a] + off];
+			}
+		}
+#pragma unroll
+		for(int u = 0; u < PSTEP; u++) {
+			int close = 0;
+			if(ok[u]) {
+				const int a = (en[u] >> 4) & 63;
+				const float3 dv = vol_geo(S, a, en[u] & 15, qa[u]);
+				const float r2 = fmaf(dv.x, dv.x, fmaf(dv.y, dv.y, dv.z * dv.z));
+				const float4 v = S.vs[a];
+				A.pairs++;
+				if(r2 < v.z) {
+					const int r = S.rep[a];
+					if(!d.rs[r].vol_overlap) atomicExch(&d.rs[r].vol_overlap, 1);
+				}
+				else close = r2 < v.w;
+			}
+			const unsigned m = __ballot_sync(0xffffffffu, close);
+			if(m) {
+				if(S.nc + __popc(m) > TILE_CCAP) vol_close(d, S, lane, A);
+				if(close) S.cbuf[S.nc + __popc(m & lt)] = en[u];
+				__syncwarp();
+				if(lane == 0) S.nc += __popc(m);
+				__syncwarp();
+			}
+		}
+	}
+}
+
+/* particle a's pairs from its neighbour list, each pair once (from the lower sorted position): the number
+ * of entries above a's position; far = 1 when a's list overflowed or holds a candidate farther than a
+ * packed entry reaches (a's half shell is then evaluated one by one) */
+__device__ __forceinline__ int vol_list_count(const ppi_dev &d, const VolSmem &S, int a, int &far) {
+	far = 0;
+	const int k = S.ki[a];
+	if(S.cc[a] < 0 || *(volatile int *) &d.rs[S.rep[a]].vol_overlap) return 0;
+	const int n = d.nl_cnt[k];
+	if(n > d.nl_k) {
+		far = 1;
+		return 0;
+	}
+	const int4 *L = (const int4 *) (d.nl + (size_t) k * d.nl_k);
+	int c = 0;
+	for(int k0 = 0; k0 < n; k0 += 4) {
+		const int4 v = L[k0 >> 2];
+		const int e4[4] = { v.x, v.y, v.z, v.w };
+#pragma unroll
+		for(int u = 0; u < 4; u++) {
+			const int jq = (int) ((unsigned) e4[u] >> 5);
+			if(k0 + u < n && jq > k) {
+				c++;
+				far |= jq - k >= TILE_OFF_MAX;
+			}
+		}
+	}
+	return far ? 0 : c;
+}
+
+/* the entries counted by vol_list_count into the pair list from position pos (row tag = code / 3) */
+__device__ __forceinline__ void vol_list_write(const ppi_dev &d, VolSmem &S, int a, int pos) {
+	const int k = S.ki[a];
+	const int n = d.nl_cnt[k];
+	const int4 *L = (const int4 *) (d.nl + (size_t) k * d.nl_k);
+	for(int k0 = 0; k0 < n; k0 += 4) {
+		const int4 v = L[k0 >> 2];
+		const int e4[4] = { v.x, v.y, v.z, v.w };
+#pragma unroll
+		for(int u = 0; u < 4; u++) {
+			const int jq = (int) ((unsigned) e4[u] >> 5);
+			if(k0 + u < n && jq > k) S.pbuf[pos++] = (int) ((unsigned) (jq - k) << 10) | (a << 4) | ((e4[u] & 31) / 3);
+		}
+	}
+}
+
+template <bool LIST>
 __global__ void __launch_bounds__(32 * TILE_WARPS, PPI_VOL_MIN_BLOCKS) k_energy_vol(ppi_dev d) {
 	__shared__ VolSmem s_vol[TILE_WARPS];
 	VolSmem &S = s_vol[threadIdx.x >> 5];
@@ -2916,7 +3009,6 @@ __global__ void __launch_bounds__(32 * TILE_WARPS, PPI_VOL_MIN_BLOCKS) k_energy_
 	A.dbonds = 0;
 	const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarp = (gridDim.x * blockDim.x) >> 5;
 	const int lo = (int) ((long long) warp * d.ntot / nwarp), hi = (int) ((long long) (warp + 1) * d.ntot / nwarp);
-	const unsigned lt = (1u << lane) - 1u;
 	if(lane == 0) S.nex = 0;
 	__syncwarp();
 	for(int b = lo; b < hi; b += TA) {
@@ -2927,8 +3019,44 @@ __global__ void __launch_bounds__(32 * TILE_WARPS, PPI_VOL_MIN_BLOCKS) k_energy_
 			S.nu = 0;
 		}
 		__syncwarp();
+		if(LIST) { /* pairs from the neighbour lists, one half of the particles (a lane each) at a time */
 #pragma unroll 1
-		for(int pz = 0; pz < 3; pz++) {
+			for(int h = 0; h < 2; h++) {
+				const int a = lane + 32 * h;
+				int far;
+				const int n = vol_list_count(d, S, a, far);
+				if(far) {
+#pragma unroll 1
+					for(int pz = 0; pz < 3; pz++) {
+						PlaneRanges P;
+						vol_ranges(d, S, a, pz, P);
+						vol_lane_pairs(d, S, a, pz, P, A);
+					}
+				}
+				int incl = n;
+#pragma unroll
+				for(int o = 1; o < 32; o <<= 1) {
+					const int v = __shfl_up_sync(0xffffffffu, incl, o);
+					if(lane >= o) incl += v;
+				}
+				const int total = __shfl_sync(0xffffffffu, incl, 31);
+				int done = 0;
+				while(done < total) { /* lanes whose slices fit together (a slice is at most nl_k <= TILE_PCAP) */
+					const int start = incl - n;
+					const int mine = n > 0 && start >= done && incl - done <= TILE_PCAP;
+					const unsigned take = __ballot_sync(0xffffffffu, mine);
+					if(take == 0) break; /* unreachable while nl_k <= TILE_PCAP */
+					if(mine) vol_list_write(d, S, a, start - done);
+					const int end = __shfl_sync(0xffffffffu, incl, 31 - __clz(take));
+					__syncwarp();
+					vol_steps(d, S, lane, end - done, A);
+					done = end;
+					__syncwarp();
+				}
+			}
+		}
+#pragma unroll 1
+		for(int pz = 0; pz < (LIST ? 0 : 3); pz++) {
 			PlaneRanges P0, P1;
 			int n0 = vol_ranges(d, S, lane, pz, P0), n1 = vol_ranges(d, S, lane + 32, pz, P1);
 			/* candidates farther than a packed entry can hold (planes of more than ~2M particles): one by one */
@@ -2977,47 +3105,7 @@ __global__ void __launch_bounds__(32 * TILE_WARPS, PPI_VOL_MIN_BLOCKS) k_energy_
 				const int end = __shfl_sync(0xffffffffu, incl, 31 - __clz(take));
 				const int np = end - done;
 				__syncwarp();
-				for(int p0 = 0; p0 < np; p0 += 32 * PSTEP) {
-					int en[PSTEP], ok[PSTEP];
-					float4 qa[PSTEP];
-#pragma unroll
-					for(int u = 0; u < PSTEP; u++) {
-						const int p = p0 + 32 * u + lane;
-						en[u] = 0;
-						ok[u] = 0;
-						qa[u] = make_float4(0.f, 0.f, 0.f, 0.f);
-						if(p < np) {
-							en[u] = S.pbuf[p];
-							const int a = (en[u] >> 4) & 63, off = en[u] >> 10;
-							ok[u] = off != 0;
-							if(ok[u]) qa[u] = d.spos[S.ki[a] + off];
-						}
-					}
-#pragma unroll
-					for(int u = 0; u < PSTEP; u++) {
-						int close = 0;
-						if(ok[u]) {
-							const int a = (en[u] >> 4) & 63;
-							const float3 dv = vol_geo(S, a, en[u] & 15, qa[u]);
-							const float r2 = fmaf(dv.x, dv.x, fmaf(dv.y, dv.y, dv.z * dv.z));
-							const float4 v = S.vs[a];
-							A.pairs++;
-							if(r2 < v.z) {
-								const int r = S.rep[a];
-								if(!d.rs[r].vol_overlap) atomicExch(&d.rs[r].vol_overlap, 1);
-							}
-							else close = r2 < v.w;
-						}
-						const unsigned m = __ballot_sync(0xffffffffu, close);
-						if(m) {
-							if(S.nc + __popc(m) > TILE_CCAP) vol_close(d, S, lane, A);
-							if(close) S.cbuf[S.nc + __popc(m & lt)] = en[u];
-							__syncwarp();
-							if(lane == 0) S.nc += __popc(m);
-							__syncwarp();
-						}
-					}
-				}
+				vol_steps(d, S, lane, np, A);
 				done = end;
 				__syncwarp();
 			}
@@ -3224,7 +3312,7 @@ static int resident_grid(F f, int *cache, int block = 128) {
 
 /* cached launch grids (one occupancy query each, made before any stream capture by ppi_prepare) */
 static int g_col_audit = 0, g_col_fast = 0, g_learn_audit = 0, g_learn_fast = 0, g_vol_grid = 0, g_col_tl = 0, g_col_tla = 0;
-static int g_a1 = 0, g_a4 = 0, g_f1 = 0, g_f4 = 0, g_f8 = 0;
+static int g_a1 = 0, g_a4 = 0, g_f1 = 0, g_f4 = 0, g_f8 = 0, g_vol_list = 0;
 
 extern "C" int ppi_resort(const ppi_dev *d, long long epoch, cudaStream_t s, long long *nl) {
 	float4 *tmp = (float4 *) d->tmp_rec; /* ntot float4 fit in the reorder scratch */
@@ -3274,7 +3362,7 @@ extern "C" int ppi_round(const ppi_dev *d, long long round, const int *colours, 
 	return (int) cudaGetLastError();
 }
 
-static void launch_energy(const ppi_dev *d, int mode, cudaStream_t s, long long *nl) {
+static void launch_energy(const ppi_dev *d, int mode, int use_nl, cudaStream_t s, long long *nl) {
 
 	const int audit = d->audit_any;
 	if(mode == PPI_EN_PARTNERS) { /* one lane per particle: the partner list is written in order */
@@ -3282,7 +3370,9 @@ static void launch_energy(const ppi_dev *d, int mode, cudaStream_t s, long long 
 		else k_energy<MODE_FAST, 1><<<resident_grid(k_energy<MODE_FAST, 1>, &g_f1), 128, 0, s>>>(*d, mode);
 	}
 	else if(audit) k_energy<MODE_AUDIT, 4><<<resident_grid(k_energy<MODE_AUDIT, 4>, &g_a4), 128, 0, s>>>(*d, mode);
-	else if(mode == PPI_EN_VOLUME) k_energy_vol<<<resident_grid(k_energy_vol, &g_vol_grid, 32 * TILE_WARPS), 32 * TILE_WARPS, 0, s>>>(*d);
+	else if(mode == PPI_EN_VOLUME && use_nl && d->nl_k > 0)
+		k_energy_vol<true><<<resident_grid(k_energy_vol<true>, &g_vol_list, 32 * TILE_WARPS), 32 * TILE_WARPS, 0, s>>>(*d);
+	else if(mode == PPI_EN_VOLUME) k_energy_vol<false><<<resident_grid(k_energy_vol<false>, &g_vol_grid, 32 * TILE_WARPS), 32 * TILE_WARPS, 0, s>>>(*d);
 	else if(lanes_of(d) == 8) k_energy<MODE_FAST, 8><<<resident_grid(k_energy<MODE_FAST, 8>, &g_f8), 128, 0, s>>>(*d, mode);
 	else k_energy<MODE_FAST, 4><<<resident_grid(k_energy<MODE_FAST, 4>, &g_f4), 128, 0, s>>>(*d, mode);
 	*nl += 1;
@@ -3293,13 +3383,13 @@ extern "C" int ppi_energy(const ppi_dev *d, int mode, cudaStream_t s, long long 
 		k_energy_reset<<<(d->nrep + 63) / 64, 64, 0, s>>>(*d);
 		*nl += 1;
 	}
-	launch_energy(d, mode, s, nl);
+	launch_energy(d, mode, 0, s, nl);
 	return (int) cudaGetLastError();
 }
 
-extern "C" int ppi_volume(const ppi_dev *d, long long sweep, cudaStream_t s, long long *nl) {
+extern "C" int ppi_volume(const ppi_dev *d, long long sweep, int use_nl, cudaStream_t s, long long *nl) {
 	k_vol_plan<<<(d->nrep + 63) / 64, 64, 0, s>>>(*d, sweep);
-	launch_energy(d, PPI_EN_VOLUME, s, nl);
+	launch_energy(d, PPI_EN_VOLUME, use_nl, s, nl);
 	k_vol_decide<<<(d->nrep + 63) / 64, 64, 0, s>>>(*d, sweep);
 	if(d->ntot > 0) k_vol_apply<<<(d->ntot + 255) / 256, 256, 0, s>>>(*d);
 	*nl += 3;
@@ -3369,7 +3459,8 @@ extern "C" int ppi_prepare(const ppi_dev *d) {
 	resident_grid(k_colour<MODE_FAST, false>, &g_col_fast, 32 * TILE_WARPS);
 	resident_grid(k_colour<MODE_AUDIT, true>, &g_col_tla, 32 * TILE_WARPS);
 	resident_grid(k_colour<MODE_FAST, true>, &g_col_tl, 32 * TILE_WARPS);
-	resident_grid(k_energy_vol, &g_vol_grid, 32 * TILE_WARPS);
+	resident_grid(k_energy_vol<false>, &g_vol_grid, 32 * TILE_WARPS);
+	resident_grid(k_energy_vol<true>, &g_vol_list, 32 * TILE_WARPS);
 	resident_grid(k_energy<MODE_AUDIT, 1>, &g_a1);
 	resident_grid(k_energy<MODE_AUDIT, 4>, &g_a4);
 	resident_grid(k_energy<MODE_FAST, 1>, &g_f1);
