@@ -354,7 +354,8 @@ def run_gpu(args, wl, ws, rank, local, dist):
         N = wl["N"]
         # upload: 16-double canonical records + particle index; download: x y z R (12 doubles) + index
         e2e = {"value": att_e2e / el, "unit": UNIT, "h2d_bytes_per_step": N * (128 + 4), "d2h_bytes_per_step": N * (96 + 4),
-               "sweeps_per_step": args.e2e_sweeps, "steps": e2e_steps}
+               "sweeps_per_step": args.e2e_sweeps, "steps": e2e_steps,
+               "step": "upload (H2D, initial energy check) + sweeps + download (D2H) + tracked energy, through the C-ABI with host arrays"}
 
     learned = None
     if rank == 0 and ws == 1 and not args.no_learned:
@@ -505,7 +506,8 @@ def main():
     ap.add_argument("--workload", default="c5", choices=sorted(WORKLOADS) + ["c3"])
     ap.add_argument("--sweeps-per-step", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--e2e-sweeps", type=int, default=10)
+    ap.add_argument("--e2e-sweeps", type=int, default=1000,
+                    help="sweeps between upload and download of an end-to-end step (1000 = Print_every of the reference's example inputs)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")

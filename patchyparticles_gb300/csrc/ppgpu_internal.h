@@ -118,6 +118,8 @@ typedef struct ppi_lrep {
  * (-1 - k) uses the k-th index after these (the host writes them before each replay) */
 typedef struct ppi_ctr {
 	long long round, epoch, sweep;
+	int vol_any; /* some replica accepted the current volume move (k_vol_apply has work) */
+	int pad;
 } ppi_ctr;
 
 /* all device pointers, passed by value to every kernel */

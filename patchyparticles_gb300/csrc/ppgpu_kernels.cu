@@ -26,6 +26,7 @@
 #include <math.h>
 #include <stdint.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 /* ------------------------------------------------------------------------------------------------ */
@@ -707,6 +708,13 @@ __global__ void __launch_bounds__(CELLFIN_B) k_cellfin(ppi_dev d) {
 /* ------------------------------------------------------------------------------------------------ */
 /* one checkerboard colour: one attempt per non-empty cell of that colour                           */
 /* ------------------------------------------------------------------------------------------------ */
+/* Programmatic dependent launch of the colour passes: colour c + 1 is launched while colour c runs, its
+ * warps draw their first proposals (which read only their own movers, untouched by colour c, and the
+ * epoch's colour and neighbour lists) and then wait for colour c to complete before reading any neighbour
+ * or writing anything. Both are no-ops in a launch without the programmatic attribute. */
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 /* per-thread counters of one launch; reduced per CTA when the CTA serves one replica (the usual case),
  * otherwise flushed per thread */
 struct Acc {
@@ -1297,9 +1305,15 @@ __device__ __forceinline__ void write_list_pairs(const ppi_dev &d, TileSmem &S, 
 
 /* the TA attempts of list positions b + lane (e0) and b + 32 + lane (e1); ent.x < 0: none */
 template <int MODE, bool LIST>
-__device__ __forceinline__ void tile_round(const ppi_dev &d, TileSmem &S, const int lane, const int4 e0, const int4 e1, int b, int col, long long round, Acc &A) {
+__device__ __forceinline__ void tile_round(const ppi_dev &d, TileSmem &S, const int lane, const int4 e0, const int4 e1, int b, int col, long long round, Acc &A,
+		bool &waited) {
 	const int loc0 = tile_setup(d, S, lane, e0, round, A);
 	const int loc1 = tile_setup(d, S, lane + 32, e1, round, A);
+	if(!waited) { /* the proposals are drawn: from here on the previous colour's moves must be complete */
+		grid_dep_wait();
+		grid_dep_release();
+		waited = true;
+	}
 	if(lane == 0) {
 		S.nc = 0;
 		S.nu = 0;
@@ -1441,11 +1455,16 @@ __global__ void __launch_bounds__(32 * TILE_WARPS, MODE == MODE_FAST ? PPI_TILE_
 		S.dov = 0;
 	}
 	__syncwarp();
+	bool waited = false;
 	for(int b = lo; b < hi; b += TA) {
 		const int4 e0 = (b + lane < hi) ? list[b + lane] : none;
 		const int4 e1 = (b + 32 + lane < hi) ? list[b + 32 + lane] : none;
-		tile_round<MODE, LIST>(d, S, lane, e0, e1, b, col, round, A);
+		tile_round<MODE, LIST>(d, S, lane, e0, e1, b, col, round, A, waited);
 		__syncwarp();
+	}
+	if(!waited) {
+		grid_dep_wait();
+		grid_dep_release();
 	}
 	/* the deferred attempts, one per lane, exactly */
 	const int nd = S.nd < TILE_DCAP ? S.nd : TILE_DCAP;
@@ -1473,7 +1492,9 @@ __global__ void __launch_bounds__(32 * TILE_WARPS, MODE == MODE_FAST ? PPI_TILE_
  * same decisions, hence the same trajectory, with fewer pair tests and no cell-range lookups. */
 #define NL_B 128 /* threads per CTA of the list build */
 
-/* list of sorted position i: candidates in the 27 cells closer than the replica's list radius */
+/* list of sorted position i: candidates in the 27 cells closer than the replica's list radius. The 3
+ * cells of a row are one contiguous range of sorted positions (two where the row wraps around the box);
+ * a candidate's x offset comes from its cell's x index (spos.w), as in pair_geo. */
 __global__ void __launch_bounds__(NL_B) k_nlist(ppi_dev d) {
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i >= d.ntot) return;
@@ -1493,30 +1514,30 @@ __global__ void __launch_bounds__(NL_B) k_nlist(ppi_dev d) {
 	const int local = gc - rp.cell_base;
 	const int cx = local % nx, cy = (local / nx) % ny, cz = local / (nx * ny);
 	const float wx = g.wf[0], wy = g.wf[1], wz = g.wf[2];
+	const bool inner = cx >= 1 && cx <= nx - 2;
+	const int xa0 = inner ? cx - 1 : (cx == 0 ? nx - 1 : nx - 2), xa1 = inner ? cx + 2 : nx;
+	const int xb1 = cx == 0 ? 2 : 1;
 	int n = 0;
 #pragma unroll 1
-	for(int dz = -1; dz <= 1; dz++)
-#pragma unroll 1
-		for(int dy = -1; dy <= 1; dy++) {
-			const int *cs = d.cell_start + rp.cell_base + (wrapi(cz + dz, nz) * ny + wrapi(cy + dy, ny)) * nx;
-			const float oy = dy * wy, oz = dz * wz;
-#pragma unroll
-			for(int dx = -1; dx <= 1; dx++) {
-				const int c = wrapi(cx + dx, nx);
-				const unsigned code = (unsigned) ((dx + 1) + 3 * (dy + 1) + 9 * (dz + 1));
-				const float ox = dx * wx;
-				const int a = cs[c], b = cs[c + 1];
-				for(int jq = a; jq < b; jq++) {
-					if(jq == i) continue;
-					const float4 q = d.spos[jq];
-					const float ex = (q.x - p.x) + ox, ey = (q.y - p.y) + oy, ez = (q.z - p.z) + oz;
-					if(fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < R2) {
-						if(n < K) out[n] = (int) (((unsigned) jq << 5) | code);
-						n++;
-					}
-				}
+	for(int row = 0; row < 9; row++) {
+		const int dy = row % 3 - 1, dz = row / 3 - 1;
+		const int *cs = d.cell_start + rp.cell_base + (wrapi(cz + dz, nz) * ny + wrapi(cy + dy, ny)) * nx;
+		const float oy = dy * wy, oz = dz * wz;
+		const int s0 = cs[xa0], e0 = cs[xa1], s1 = inner ? 0 : cs[0], e1 = inner ? 0 : cs[xb1];
+		const int len0 = e0 - s0, tot = len0 + (e1 - s1);
+		for(int t = 0; t < tot; t++) {
+			const int jq = t < len0 ? s0 + t : s1 + (t - len0);
+			if(jq == i) continue;
+			const float4 q = d.spos[jq];
+			int dxc = __float_as_int(q.w) - cx;
+			dxc = dxc > 1 ? dxc - nx : (dxc < -1 ? dxc + nx : dxc);
+			const float ex = (q.x - p.x) + dxc * wx, ey = (q.y - p.y) + oy, ez = (q.z - p.z) + oz;
+			if(fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < R2) {
+				if(n < K) out[n] = (int) (((unsigned) jq << 5) | (unsigned) ((dxc + 1) + 3 * (dy + 1) + 9 * (dz + 1)));
+				n++;
 			}
 		}
+	}
 	d.nl_cnt[i] = n;
 	if(n > K) atomicAdd(&d.rs[r].nl_overflow, 1ull);
 }
@@ -3138,6 +3159,7 @@ __global__ void k_vol_plan(ppi_dev d, long long sweep) {
 	int r = blockIdx.x * blockDim.x + threadIdx.x;
 	if(r >= d.nrep) return;
 	sweep = ctr_index(sweep, sweep < 0 ? d.ctr->sweep : 0);
+	if(r == 0) d.ctr->vol_any = 0;
 	const ppi_rparams &rp = d.rp[r];
 	ppi_rstate *rs = d.rs + r;
 	ppi_grid *g = d.grid + r;
@@ -3181,6 +3203,7 @@ __global__ void k_vol_decide(ppi_dev d, long long sweep) {
 	if(!rs->vol_overlap && u01d(u.x, u.y) < exp(arg)) {
 		int a = g->vol_dir;
 		rs->vol_accept = 1;
+		d.ctr->vol_any = 1;
 		rs->box[a] = g->vol_side;
 		rs->V = g->vol_V1;
 		rs->bonds = nb_new;
@@ -3199,7 +3222,7 @@ __global__ void k_vol_decide(ppi_dev d, long long sweep) {
 
 __global__ void k_vol_apply(ppi_dev d) {
 	int k = blockIdx.x * blockDim.x + threadIdx.x;
-	if(k >= d.ntot) return;
+	if(k >= d.ntot || !d.ctr->vol_any) return; /* every replica rejected its volume move: nothing to rescale */
 	/* canonical positions (slot k) */
 	int r = d.rep[k];
 	if(d.rs[r].vol_accept) {
@@ -3333,6 +3356,27 @@ extern "C" int ppi_resort(const ppi_dev *d, long long epoch, cudaStream_t s, lon
 
 static int lanes_of(const ppi_dev *d) { return d->lanes == 8 ? 8 : PPI_DEFAULT_LANES; }
 
+/* the 8 colour launches of a round; colours 1..7 with programmatic stream serialisation (their proposals
+ * overlap the previous colour's tail, see grid_dep_wait) */
+template <typename K>
+static void launch_round(K kern, int grid, const ppi_dev *d, long long round, const int *colours, cudaStream_t s) {
+	static int pdl = -1;
+	if(pdl < 0) pdl = getenv("PPGPU_NO_PDL") ? 0 : 1;
+	for(int ci = 0; ci < 8; ci++) {
+		cudaLaunchConfig_t cfg;
+		memset(&cfg, 0, sizeof(cfg));
+		cfg.gridDim = dim3(grid);
+		cfg.blockDim = dim3(32 * TILE_WARPS);
+		cfg.stream = s;
+		cudaLaunchAttribute at[1];
+		at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+		at[0].val.programmaticStreamSerializationAllowed = 1;
+		cfg.attrs = at;
+		cfg.numAttrs = (ci > 0 && pdl) ? 1 : 0;
+		cudaLaunchKernelEx(&cfg, kern, *d, round, colours[ci]);
+	}
+}
+
 extern "C" int ppi_nlist(const ppi_dev *d, cudaStream_t s, long long *nl) {
 	if(d->ntot <= 0 || d->nl_k <= 0) return 0;
 	k_nlist<<<(d->ntot + NL_B - 1) / NL_B, NL_B, 0, s>>>(*d);
@@ -3342,22 +3386,10 @@ extern "C" int ppi_nlist(const ppi_dev *d, cudaStream_t s, long long *nl) {
 
 extern "C" int ppi_round(const ppi_dev *d, long long round, const int *colours, int audit, int use_nl, cudaStream_t s, long long *nl) {
 	const int aud = audit || d->audit_any;
-	if(use_nl && d->nl_k > 0 && aud) {
-		int grid = resident_grid(k_colour<MODE_AUDIT, true>, &g_col_tla, 32 * TILE_WARPS);
-		for(int ci = 0; ci < 8; ci++) k_colour<MODE_AUDIT, true><<<grid, 32 * TILE_WARPS, 0, s>>>(*d, round, colours[ci]);
-	}
-	else if(use_nl && d->nl_k > 0) {
-		int grid = resident_grid(k_colour<MODE_FAST, true>, &g_col_tl, 32 * TILE_WARPS);
-		for(int ci = 0; ci < 8; ci++) k_colour<MODE_FAST, true><<<grid, 32 * TILE_WARPS, 0, s>>>(*d, round, colours[ci]);
-	}
-	else if(aud) {
-		int grid = resident_grid(k_colour<MODE_AUDIT, false>, &g_col_audit, 32 * TILE_WARPS);
-		for(int ci = 0; ci < 8; ci++) k_colour<MODE_AUDIT, false><<<grid, 32 * TILE_WARPS, 0, s>>>(*d, round, colours[ci]);
-	}
-	else {
-		int grid = resident_grid(k_colour<MODE_FAST, false>, &g_col_fast, 32 * TILE_WARPS);
-		for(int ci = 0; ci < 8; ci++) k_colour<MODE_FAST, false><<<grid, 32 * TILE_WARPS, 0, s>>>(*d, round, colours[ci]);
-	}
+	if(use_nl && d->nl_k > 0 && aud) launch_round(k_colour<MODE_AUDIT, true>, resident_grid(k_colour<MODE_AUDIT, true>, &g_col_tla, 32 * TILE_WARPS), d, round, colours, s);
+	else if(use_nl && d->nl_k > 0) launch_round(k_colour<MODE_FAST, true>, resident_grid(k_colour<MODE_FAST, true>, &g_col_tl, 32 * TILE_WARPS), d, round, colours, s);
+	else if(aud) launch_round(k_colour<MODE_AUDIT, false>, resident_grid(k_colour<MODE_AUDIT, false>, &g_col_audit, 32 * TILE_WARPS), d, round, colours, s);
+	else launch_round(k_colour<MODE_FAST, false>, resident_grid(k_colour<MODE_FAST, false>, &g_col_fast, 32 * TILE_WARPS), d, round, colours, s);
 	*nl += 8;
 	return (int) cudaGetLastError();
 }
