@@ -421,6 +421,47 @@ static void o_change_volume(orc_system *s) { /* MC_change_volume, MC.c:450-513 *
 	}
 }
 
+/* MC_change_Lx (MC.c:515-567): Lx changes by a uniform amount, Ly = Lz follow at constant volume, every
+ * coordinate is rescaled; accepted with probability min(1, exp(+dE / T)) (MC.c:559) as the reference does;
+ * a rejected move divides the positions back */
+static void o_change_lx(orc_system *s) {
+	s->tries[ORC_LX]++;
+	double dE = -s->energy;
+	double old_sides[3] = { s->box[0], s->box[1], s->box[2] };
+	s->box[0] += (orc_drand(s) - 0.5) * s->prm.lx_change_max;
+	s->box[1] = s->box[2] = sqrt(s->V / s->box[0]);
+	if(s->box[1] < s->prm.lyz_min || s->box[1] > s->prm.lyz_max) { /* early rejection (MC.c:526-530) */
+		memcpy(s->box, old_sides, sizeof(old_sides));
+		return;
+	}
+	double f[3] = { s->box[0] / old_sides[0], s->box[1] / old_sides[1], s->box[2] / old_sides[2] };
+	for(int i = 0; i < s->N; i++)
+		for(int k = 0; k < 3; k++) s->r[3 * i + k] *= f[k];
+	if((s->box[0] / s->nside[0]) < s->r_cut || (s->box[1] / s->nside[1]) < s->r_cut) {
+		o_cells_init(s);
+		o_cells_fill(s);
+	}
+	int overlap_found = 0;
+	for(int i = 0; i < s->N && !overlap_found; i++) {
+		dE += o_energy(s, i) * 0.5;
+		if(s->overlap) overlap_found = 1;
+	}
+	if(!overlap_found && orc_drand(s) < exp(dE / s->prm.T)) {
+		s->energy += dE;
+		s->accepted[ORC_LX]++;
+	}
+	else {
+		for(int i = 0; i < s->N; i++)
+			for(int k = 0; k < 3; k++) s->r[3 * i + k] /= f[k];
+		memcpy(s->box, old_sides, sizeof(old_sides));
+		if((s->box[0] / s->nside[0]) < s->r_cut || (s->box[1] / s->nside[1]) < s->r_cut) {
+			o_cells_init(s);
+			o_cells_fill(s);
+		}
+		s->overlap = 0;
+	}
+}
+
 /* one iteration of the do_NVT (MC.c:19-29) or do_NPT (MC.c:60-68) loop body */
 static void o_attempt(orc_system *s) {
 	if(s->prm.ensemble == ORC_NPT) {
@@ -430,7 +471,8 @@ static void o_attempt(orc_system *s) {
 	else {
 		o_move_rototranslate(s);
 		/* do_NVT always draws the Lx-move number (MC.c:24), even with Lx_move = 0 */
-		(void) orc_drand(s);
+		const double R = orc_drand(s);
+		if(s->prm.lx_move && R < 1. / s->N) o_change_lx(s);
 	}
 }
 

@@ -30,6 +30,7 @@ extern "C" {
 /* move-type slots of the tries/accepted counters, as in defs.h:11-19 */
 #define ORC_ROTO_TRASL 0
 #define ORC_VOLUME 6
+#define ORC_LX 7 /* defs.h:19 */
 #define ORC_N_MOVES 8
 
 typedef struct orc_params {
@@ -42,6 +43,9 @@ typedef struct orc_params {
 	double kf_delta;           /* KF_delta */
 	double kf_cosmax;          /* KF_cosmax */
 	int seed;                  /* Seed (srand48 argument, system.c:71-75) */
+	int lx_move;               /* Lx_move (NVT only, system.c:165-193) */
+	double lx_change_max;      /* Lx_change_max */
+	double lyz_min, lyz_max;   /* Lyz_min, Lyz_max */
 } orc_params;
 
 typedef struct orc_system orc_system;

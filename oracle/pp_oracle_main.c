@@ -130,10 +130,30 @@ int main(int argc, char *argv[]) {
 		prm.rescale_factor_max = atof(get(in, "rescale_factor_max", 1));
 		prm.P = atof(get(in, "P", 1));
 	}
+	else if((v = get(in, "Lx_move", 0)) && atoi(v)) { /* system.c:170-193 (NVT only) */
+		prm.lx_move = 1;
+		prm.lx_change_max = atof(get(in, "Lx_change_max", 1));
+		prm.lyz_min = atof(get(in, "Lyz_min", 1));
+		prm.lyz_max = atof(get(in, "Lyz_max", 1));
+	}
+	/* boxshape.dat is opened whenever the Lx_move key is set (output.c:101-108) */
+	FILE *fb = NULL;
+	if((v = get(in, "Lx_move", 0)) && atoi(v)) {
+		fb = fopen("boxshape.dat", mode);
+		if(fb == NULL) die("boxshape.dat is not writable");
+	}
 	if(dynamics != 0 || (ensemble != ORC_NVT && ensemble != ORC_NPT)) die("only Dynamics = 0 with Ensemble 0 or 5 is restated");
 	char err[512];
 	orc_system *s = orc_load_rrr(conf, &prm, err, sizeof(err));
 	if(s == NULL) die(err);
+	if(prm.lx_move) {
+		double b[3];
+		orc_box(s, b);
+		if(b[1] != b[2]) die("Lx_move = 1 requires Ly = Lz");
+		if(prm.lyz_min >= b[1]) die("Lyz_min should be smaller than box size");
+		if(prm.lyz_max <= b[1]) die("Lyz_max should be larger than box size");
+		fprintf(stderr, "Ly and Lz are allowed to vary between %lf and %lf\n", prm.lyz_min, prm.lyz_max); /* output_log_msg */
+	}
 
 	/* initial energy and overlap check (main.c:55-64) */
 	int N = orc_N(s), ov;
@@ -158,10 +178,17 @@ int main(int argc, char *argv[]) {
 				fprintf(fd, "%lld %lf %d\n", step, N / V, N);
 				fflush(fd);
 			}
+			if(prm.lx_move) {
+				double b[3];
+				orc_box(s, b);
+				fprintf(fb, "%lld %lf %lf %lf\n", step, b[0], b[1], b[2]);
+				fflush(fb);
+			}
 			orc_counters(s, tries, acc);
 			fprintf(fa, "%lld", step);
 			fprintf(fa, " %e", acc[ORC_ROTO_TRASL] / (double) tries[ORC_ROTO_TRASL]);
 			if(ensemble == ORC_NPT) fprintf(fa, " %e", acc[ORC_VOLUME] / (double) tries[ORC_VOLUME]);
+			if(prm.lx_move) fprintf(fa, " %e", acc[ORC_LX] / (double) tries[ORC_LX]);
 			fprintf(fa, "\n");
 			fflush(fa);
 			orc_reset_counters(s);
@@ -190,6 +217,7 @@ int main(int argc, char *argv[]) {
 	fclose(fe);
 	fclose(fa);
 	if(fd) fclose(fd);
+	if(fb) fclose(fb);
 	orc_free(s);
 	free(in);
 	return 0;

@@ -30,6 +30,10 @@ class OrcParams(ctypes.Structure):
         ("kf_delta", ctypes.c_double),
         ("kf_cosmax", ctypes.c_double),
         ("seed", ctypes.c_int),
+        ("lx_move", ctypes.c_int),
+        ("lx_change_max", ctypes.c_double),
+        ("lyz_min", ctypes.c_double),
+        ("lyz_max", ctypes.c_double),
     ]
 
 
@@ -95,8 +99,9 @@ def _ip(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
 
 
-def params(ensemble=NVT, T=0.12, P=0.0, disp_max=0.05, theta_max=0.1, rescale_factor_max=0.01, kf_delta=0.12, kf_cosmax=0.92, seed=1):
-    return OrcParams(ensemble, T, P, disp_max, theta_max, rescale_factor_max, kf_delta, kf_cosmax, seed)
+def params(ensemble=NVT, T=0.12, P=0.0, disp_max=0.05, theta_max=0.1, rescale_factor_max=0.01, kf_delta=0.12, kf_cosmax=0.92, seed=1,
+           lx_move=0, lx_change_max=0.0, lyz_min=0.0, lyz_max=0.0):
+    return OrcParams(ensemble, T, P, disp_max, theta_max, rescale_factor_max, kf_delta, kf_cosmax, seed, lx_move, lx_change_max, lyz_min, lyz_max)
 
 
 class System:

@@ -6,7 +6,7 @@ the reference's own programs:
 
   generator_<N>_<rho>_<seed>.rrr.gz   reference generator seeded with srand48(seed) (oracle/ref_generator_seeded.c)
   probe_<name>.txt.gz                 ref_probe: per-particle MC_energy, overlap flag, bond/overlap partners
-  traj_<name>/                        reference main loop outputs (stdout, energy/acceptance/density, last.rrr)
+  traj_<name>/                        reference main loop outputs (stdout, energy/acceptance/density/boxshape, last.rrr)
   adversarial.rrr.gz                  near-threshold pair configuration (tests/golden/adversarial.py)
 
 The reference is compiled with -O2 -ffp-contract=off (oracle/Makefile); nothing here is used at run time
@@ -58,6 +58,8 @@ TRAJ = [
     ("bcc_npt", "bcc.rrr", 5, 0.12, 400, 50, 12345, "P = 0.05\nrescale_factor_max = 0.01\n"),
     ("small_nvt", "generator_300_0.3_4242.rrr", 0, 0.11, 200, 20, 7, ""),
     ("small_npt", "generator_300_0.3_4242.rrr", 5, 0.11, 300, 30, 9, "P = 0.05\nrescale_factor_max = 0.01\n"),
+    # the box-shape move of NVT (MC.c:515-567): Lx changes, Ly = Lz follow at constant volume
+    ("small_lx", "generator_300_0.3_4242.rrr", 0, 0.11, 400, 40, 11, "Lx_move = 1\nLx_change_max = 0.5\nLyz_min = 8.0\nLyz_max = 12.0\n"),
 ]
 
 PROBE_INPUT = """Dynamics = 0
@@ -116,7 +118,7 @@ def main():
         os.makedirs(dst, exist_ok=True)
         open(os.path.join(dst, "input"), "w").write(TRAJ_INPUT.format(ensemble=ens, seed=seed, T=T, steps=steps, print_every=pe, save_every=pe * 2, conf=conf, extra=extra))
         open(os.path.join(dst, "stdout.txt"), "wb").write(out)
-        for fn in ("energy.dat", "acceptance.dat", "density.dat"):
+        for fn in ("energy.dat", "acceptance.dat", "density.dat", "boxshape.dat"):
             if os.path.exists(os.path.join(d, fn)):
                 shutil.copy(os.path.join(d, fn), os.path.join(dst, fn))
         gz_write(os.path.join(dst, "last.rrr.gz"), open(os.path.join(d, "last.rrr"), "rb").read())

@@ -50,7 +50,7 @@ def test_known_answers(built):
         assert E == want and not ov
 
 
-@pytest.mark.parametrize("name", ["fcc_nvt", "bcc_npt", "small_nvt", "small_npt"])
+@pytest.mark.parametrize("name", ["fcc_nvt", "bcc_npt", "small_nvt", "small_npt", "small_lx"])
 def test_oracle_trajectory_matches_reference(built, name):
     """The restated main loop reproduces the reference's output files line for line."""
     src = helpers.golden_path("traj_" + name)
@@ -61,7 +61,7 @@ def test_oracle_trajectory_matches_reference(built, name):
     helpers.unpack_golden(conf, work)
     out = subprocess.check_output([po.CLI, "input"], cwd=work, stderr=subprocess.DEVNULL).decode()
     assert out == open(os.path.join(src, "stdout.txt")).read()
-    for fn in ("energy.dat", "acceptance.dat", "density.dat"):
+    for fn in ("energy.dat", "acceptance.dat", "density.dat", "boxshape.dat"):
         p = os.path.join(src, fn)
         if os.path.exists(p):
             assert helpers.normalise_nan(open(os.path.join(work, fn)).read()) == helpers.normalise_nan(open(p).read()), fn
