@@ -42,6 +42,7 @@ extern "C" {
 
 #define PP_MOVE_ROTO_TRASL 0 /* tries/accepted slots as System::tries/accepted (defs.h:11-19, 95-96) */
 #define PP_MOVE_VOLUME 6
+#define PP_MOVE_LX 7 /* the NVT box-shape move (defs.h:19) */
 #define PP_N_MOVES 8
 
 #define PP_PREC_FP32_GUARD 0 /* FP32 pair tests, FP64 re-evaluation inside the guard band (default) */
@@ -61,6 +62,12 @@ typedef struct pp_params {
 	double guard_eps;          /* guard half-width on r^2 and on patch cosines; <= 0 selects 1e-5 */
 	int resort_every;          /* checkerboard rounds between cell-grid re-sorts from the FP64 state; 0 = 4 */
 	int audit;                 /* nonzero: re-check every FP32 decision in FP64 and count mismatches */
+	/* Lx_move (system.c:170-193, NVT only; ignored for NPT as in the reference): once per sweep Lx changes by
+	 * (R - 0.5) Lx_change_max and Ly = Lz = sqrt(V / Lx) keep the volume (MC_change_Lx, MC.c:515-567).
+	 * 1 = the reference's acceptance min(1, exp(+dE / T)) (MC.c:559), 2 = the Boltzmann factor exp(-dE / T). */
+	int lx_move;
+	double lx_change_max;      /* Lx_change_max */
+	double lyz_min, lyz_max;   /* Lyz_min, Lyz_max: allowed range of Ly = Lz (absolute lengths) */
 } pp_params;
 
 typedef struct pp_counters {

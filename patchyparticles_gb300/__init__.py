@@ -30,6 +30,7 @@ PREC_FP32_GUARD = 0
 PREC_FP64 = 1
 MOVE_ROTO_TRASL = 0
 MOVE_VOLUME = 6
+MOVE_LX = 7
 N_MOVES = 8
 
 
@@ -48,6 +49,10 @@ class PPParams(ctypes.Structure):
         ("guard_eps", ctypes.c_double),
         ("resort_every", ctypes.c_int),
         ("audit", ctypes.c_int),
+        ("lx_move", ctypes.c_int),
+        ("lx_change_max", ctypes.c_double),
+        ("lyz_min", ctypes.c_double),
+        ("lyz_max", ctypes.c_double),
     ]
 
 

@@ -43,6 +43,7 @@ struct pp_engine {
 	int reorder_every;    /* re-sorts between physical reorders of the FP64 state */
 	double cell_scale;    /* cell edge / minimum edge (autotuner) */
 	int any_npt;
+	int any_lx;           /* some NVT replica has the box-shape move */
 	int any_audit;
 	int nl_mode;          /* per-epoch neighbour lists for plain moves (pp_gpu_set_neighbour_lists) */
 	int nl_valid;         /* the current epoch's lists are built and only plain moves ran since */
@@ -179,6 +180,11 @@ static int check_params(pp_engine *e, const pp_params *p) {
 	if(p->guard_eps > 1e-2) return set_err(e, PP_ERR_ARG, "guard_eps too large");
 	if(p->resort_every < 0 || p->resort_every > 64) return set_err(e, PP_ERR_ARG, "resort_every (re-sort period in rounds) must be 0 or in [1, 64]");
 	if(p->ensemble == PP_NPT && !(p->rescale_factor_max > 0. && p->rescale_factor_max < 1.)) return set_err(e, PP_ERR_ARG, "rescale_factor_max must lie in (0, 1)");
+	if(p->lx_move < 0 || p->lx_move > 2) return set_err(e, PP_ERR_ARG, "Lx_move must be 0, 1 (reference acceptance) or 2 (Boltzmann acceptance)");
+	if(p->ensemble == PP_NVT && p->lx_move) {
+		if(!(p->lx_change_max > 0.)) return set_err(e, PP_ERR_ARG, "Lx_change_max must be > 0");
+		if(!(p->lyz_min > 0.) || !(p->lyz_max > p->lyz_min)) return set_err(e, PP_ERR_ARG, "Lyz_min and Lyz_max must satisfy 0 < Lyz_min < Lyz_max");
+	}
 	return PP_OK;
 }
 
@@ -213,6 +219,7 @@ static int create_common(const pp_params *prms, int n, pp_engine **out) {
 	for(int i = 0; i < n; i++) {
 		if(e->prm[i].guard_eps <= 0.) e->prm[i].guard_eps = 1e-5;
 		if(e->prm[i].ensemble == PP_NPT) e->any_npt = 1;
+		if(e->prm[i].ensemble == PP_NVT && e->prm[i].lx_move) e->any_lx = 1;
 		if(e->prm[i].audit) e->any_audit = 1;
 	}
 	if(e->prm[0].resort_every > 0) e->resort_every = e->prm[0].resort_every;
@@ -338,6 +345,17 @@ void ppi_model_params(int N, double kf_delta, double kf_cosmax, ppi_rparams *rp)
 	rp->seed = 1;
 }
 
+/* Bounds [smin, smax] of the factor by which one accepted box-shape move scales one side of the box of
+ * replica r: an Lx move (MC.c:520-537) scales x by 1 +- Lx_change_max / (2 Lx) and y, z by sqrt(Lx / Lx'),
+ * with Lx >= V / Lyz_max^2 (1, 1 without the move; NPT volume moves use exp(+-rescale_factor_max / 2)). */
+static void lx_move_bounds(const pp_params *p, const double *box, double *smin, double *smax) {
+	*smin = *smax = 1.;
+	if(p->ensemble != PP_NVT || !p->lx_move) return;
+	const double V = box[0] * box[1] * box[2], h = 0.5 * p->lx_change_max / (V / (p->lyz_max * p->lyz_max));
+	*smin = fmin(1. - h, 1. / sqrt(1. + h));
+	*smax = fmax(1. + h, 1. / sqrt(1. - h));
+}
+
 static int derive_rparams(pp_engine *e, int r, ppi_rparams *rp) {
 	const pp_params *p = e->prm + r;
 	memset(rp, 0, sizeof(*rp));
@@ -358,7 +376,14 @@ static int derive_rparams(pp_engine *e, int r, ppi_rparams *rp) {
 	 * the accepted compressions between two re-sorts (each shrinks one side by at most exp(-max/2)) */
 	double wm = rp->r_cut + 1e-5;
 	if(p->ensemble == PP_NPT) wm /= exp(-0.5 * p->rescale_factor_max * (e->resort_every + 1));
+	double lsmin, lsmax;
+	lx_move_bounds(p, e->h_box[r], &lsmin, &lsmax);
+	wm /= pow(lsmin, e->resort_every + 1); /* the Lx moves that can be accepted before the next re-sort */
 	rp->w_min = wm * (e->cell_scale > 1.0 ? e->cell_scale : 1.0);
+	rp->lx_move = (p->ensemble == PP_NVT) ? p->lx_move : 0;
+	rp->lx_change_max = p->lx_change_max;
+	rp->lyz_min = p->lyz_min;
+	rp->lyz_max = p->lyz_max;
 	for(int k = 0; k < 32; k++) {
 		double pk = exp(-(double) k / p->temperature);
 		double t = ceil(pk * 9007199254740992.0);
@@ -379,7 +404,10 @@ static int derive_rparams(pp_engine *e, int r, ppi_rparams *rp) {
 		int n = ((int) floor(box[a] / wm)) & ~1;
 		if(n < 4) return set_err(e, PP_ERR_CAPACITY, "replica %d: box side %g is too small for the cell grid (needs >= 4 cells of edge %g)", r, box[a], wm);
 		if(n > PPI_MAX_AXIS_CELLS) return set_err(e, PP_ERR_CAPACITY, "replica %d: box side %g needs more than %d cells", r, box[a], PPI_MAX_AXIS_CELLS);
-		int nc = ((int) floor(box[a] * grow / wm)) & ~1;
+		double side = box[a] * grow;
+		if(rp->lx_move) /* the largest sides the box-shape move allows: Lx <= V / Lyz_min^2, Ly = Lz <= Lyz_max */
+			side = a == 0 ? box[0] * box[1] * box[2] / (p->lyz_min * p->lyz_min) : p->lyz_max;
+		int nc = ((int) floor(side / wm)) & ~1;
 		if(nc > PPI_MAX_AXIS_CELLS) nc = PPI_MAX_AXIS_CELLS;
 		cap *= nc;
 	}
@@ -466,6 +494,11 @@ static float nl_radius2(const pp_engine *e, int r) {
 	if(p->ensemble == PP_NPT) {
 		const double smin = exp(-0.5 * p->rescale_factor_max * (E + 1.)), smax = exp(0.5 * p->rescale_factor_max * E);
 		R = (base + smax * motion) / smin;
+	}
+	else if(p->lx_move) { /* the same for the Lx moves of the epoch (MC.c:520-545) */
+		double s1, s2;
+		lx_move_bounds(p, e->h_box[r], &s1, &s2);
+		R = (base + pow(s2, E) * motion) / pow(s1, E + 1.);
 	}
 	R += 1e-3;
 	return (float) (R * R * (1. + 1e-6));
@@ -656,6 +689,14 @@ int pp_gpu_upload_replica(pp_engine *e, int r, int N, const double *rr, const do
 	if(e == NULL || r < 0 || r >= e->nrep || N < 0 || (N > 0 && (rr == NULL || RR == NULL)) || box == NULL) return set_err(e, PP_ERR_ARG, "invalid upload arguments");
 	for(int a = 0; a < 3; a++)
 		if(!(box[a] > 0.)) return set_err(e, PP_ERR_ARG, "box sides must be positive");
+	const pp_params *p = e->prm + r;
+	if(p->ensemble == PP_NVT && p->lx_move) { /* system.c:172-188 */
+		if(box[1] != box[2]) return set_err(e, PP_ERR_ARG, "Lx_move = 1 requires Ly = Lz");
+		if(p->lyz_min >= box[1]) return set_err(e, PP_ERR_ARG, "Lyz_min should be smaller than box size");
+		if(p->lyz_max <= box[1]) return set_err(e, PP_ERR_ARG, "Lyz_max should be larger than box size");
+		if(0.5 * p->lx_change_max >= 0.5 * box[0] * box[1] * box[2] / (p->lyz_max * p->lyz_max))
+			return set_err(e, PP_ERR_ARG, "Lx_change_max is too large: one move could halve the smallest Lx that Lyz_max allows");
+	}
 	/* fast path: same layout already on the device -> copy straight into the replica's slots */
 	if(e->committed && e->N[r] == N) {
 		double grow = (e->prm[r].ensemble == PP_NPT) ? 1.15 : 1.0;
@@ -847,7 +888,7 @@ static int capture_period(pp_engine *e, int v) {
 	for(int r = 0; r < R; r++) {
 		if(learned) rc |= ppi_round_learned(&e->d, -1 - r, slots, e->any_audit, e->stream, &nl);
 		else rc |= ppi_round(&e->d, -1 - r, slots, e->any_audit, lists, e->stream, &nl);
-		if(e->any_npt) {
+		if(e->any_npt || e->any_lx) {
 			rc |= ppi_volume(&e->d, -1 - r, lists && e->nl_all, e->stream, &nl);
 			if(learned) rc |= ppi_canon(&e->d, e->stream, &nl);
 		}
@@ -953,7 +994,7 @@ int pp_gpu_sweeps(pp_engine *e, long long n) {
 			e->round_counter++;
 			e->launches += nl;
 		}
-		if(e->any_npt) {
+		if(e->any_npt || e->any_lx) { /* the sweep's NPT volume move or NVT box-shape move */
 			long long nl = 0;
 			if((rc = ev_begin(e, 2, &ev)) != PP_OK) return rc;
 			CK(ppi_volume(&e->d, s, e->nl_valid && e->nl_all, e->stream, &nl));
@@ -1796,6 +1837,9 @@ static double tuned_w_min(const pp_engine *e, int r) {
 	const pp_params *p = e->prm + r;
 	double wm = (1. + p->kf_delta) + 1e-5;
 	if(p->ensemble == PP_NPT) wm /= exp(-0.5 * p->rescale_factor_max * (e->resort_every + 1));
+	double lsmin, lsmax;
+	lx_move_bounds(p, e->h_box[r], &lsmin, &lsmax);
+	wm /= pow(lsmin, e->resort_every + 1);
 	return wm * e->cell_scale;
 }
 

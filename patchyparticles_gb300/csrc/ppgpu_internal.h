@@ -49,7 +49,7 @@ typedef struct ppi_rparams {
 	int audit;
 	int cell_base;   /* first global cell index of this replica */
 	int cell_cap;    /* cells reserved for this replica */
-	int pad0;
+	int lx_move;     /* NVT box-shape move (MC.c:515-567): 0 off, 1 reference acceptance, 2 Boltzmann acceptance */
 	double T, P, disp_max, theta_max, rescale_max;
 	double cosmax, sqr_rcut, r_cut, w_min;
 	double base[4][3];     /* tetrahedral base patches, bit-identical to system.c:20-31 */
@@ -58,6 +58,7 @@ typedef struct ppi_rparams {
 	float nl_r2f;          /* squared radius of the per-epoch neighbour lists (0: no lists, exact path) */
 	float pad1;
 	uint64_t seed;
+	double lx_change_max, lyz_min, lyz_max; /* Lx_change_max, Lyz_min, Lyz_max (system.c:177-179) */
 } ppi_rparams;
 
 typedef struct ppi_rstate {
@@ -86,13 +87,16 @@ typedef struct ppi_grid {
 	float pad;
 	float inv_wf[3], inv_Lf[3], Lf[3]; /* FP32 copies for the cell assignment's guesses */
 	float pad4;
-	/* NPT candidate of the current sweep (MC.c:456-472) */
-	int vol_dir;
-	int pad2;
-	double vol_f, vol_side, vol_V1, vol_V0;
-	float vol_ff;
+	/* candidate box of the current sweep's NPT volume move (MC.c:456-472) or Lx move (MC.c:520-537) */
+	int vol_dir;       /* NPT: the scaled axis; PPI_LX_DIR: Lx move; -1: no candidate */
+	int vol_mask;      /* bit k: axis k is scaled in the candidate box */
+	double vol_f, vol_V1, vol_V0; /* NPT: scale factor of axis vol_dir, volumes before and after */
+	double vol_f3[3];  /* per-axis scale factors of the candidate (1 on unscaled axes) */
+	double vol_box3[3]; /* candidate box sides */
+	float vol_ff3[3];  /* FP32 copies of vol_f3 */
 	float pad3;
 } ppi_grid;
+#define PPI_LX_DIR 3
 
 /* learned proposal: the four mixture components (component 0 is the plain move) and training knobs */
 #define PPI_MIX 4

@@ -250,19 +250,22 @@ __device__ __noinline__ void state64(const double *__restrict__ rec_all, int ps,
 }
 
 /* Exact re-evaluation of one pair. p is the probing particle: kind 0 = its stored state, kind 1 = the
- * candidate of the current move (q, disp). vol_dir >= 0 scales coordinate vol_dir of both positions by
- * vol_f and uses box[vol_dir] = vol_side (the NPT candidate box, MC.c:471-478). */
+ * candidate of the current move (q, disp). Bit k of vol_mask scales coordinate k of both positions by
+ * vol_f3[k] and uses box[k] = vol_box3[k] (the candidate box of an NPT volume move, MC.c:471-478, or of an
+ * Lx move, MC.c:533-545); vol_mask = 0 leaves the box alone (the pointers are then not read). */
 __device__ __noinline__ int exact_pair(const double *__restrict__ rec_all, const ppi_rparams *rp, const double *box_in, int ps, int kind, float4 q,
-		float3 disp, int qs, int vol_dir, double vol_f, double vol_side, double *o_dist2, double *o_pmax, double *o_qmax) {
+		float3 disp, int qs, int vol_mask, const double *vol_f3, const double *vol_box3, double *o_dist2, double *o_pmax, double *o_qmax) {
 	double P[12], Qr[12], box[3];
 	state64(rec_all, ps, kind, q, disp, P);
 	state64(rec_all, qs, 0, q, disp, Qr);
 #pragma unroll 1
-	for(int k = 0; k < 3; k++) box[k] = box_in[k];
-	if(vol_dir >= 0) {
-		P[vol_dir] = __dmul_rn(P[vol_dir], vol_f);
-		Qr[vol_dir] = __dmul_rn(Qr[vol_dir], vol_f);
-		box[vol_dir] = vol_side;
+	for(int k = 0; k < 3; k++) {
+		box[k] = box_in[k];
+		if((vol_mask >> k) & 1) {
+			P[k] = __dmul_rn(P[k], vol_f3[k]);
+			Qr[k] = __dmul_rn(Qr[k], vol_f3[k]);
+			box[k] = vol_box3[k];
+		}
 	}
 	return interact64(P, P + 3, Qr, Qr + 3, rp->base, box, rp->sqr_rcut, rp->cosmax, o_dist2, o_pmax, o_qmax);
 }
@@ -338,16 +341,20 @@ __device__ __forceinline__ void state64_fast(const double *__restrict__ rec_all,
 }
 
 __device__ __forceinline__ int decide64(const double *__restrict__ rec_all, const ppi_rparams &rp, const double *box_in, const double *inv_box_in, int ps, int kind, float4 dq,
-		float3 disp, int qs, int vol_dir, double vol_f, double vol_side) {
+		float3 disp, int qs, int vol_mask, const double *vol_f3, const double *vol_box3) {
 	double rp_[3], Rp[9], rq_[3], Rq[9];
 	state64_fast(rec_all, ps, kind, dq, disp, rp_, Rp);
 	state64_fast(rec_all, qs, 0, dq, disp, rq_, Rq);
 	double box[3] = { box_in[0], box_in[1], box_in[2] }, ib[3] = { inv_box_in[0], inv_box_in[1], inv_box_in[2] };
-	if(vol_dir >= 0) {
-		rp_[vol_dir] = __dmul_rn(rp_[vol_dir], vol_f);
-		rq_[vol_dir] = __dmul_rn(rq_[vol_dir], vol_f);
-		box[vol_dir] = vol_side;
-		ib[vol_dir] = rcp64(vol_side);
+	if(vol_mask) {
+#pragma unroll
+		for(int k = 0; k < 3; k++)
+			if((vol_mask >> k) & 1) {
+				rp_[k] = __dmul_rn(rp_[k], vol_f3[k]);
+				rq_[k] = __dmul_rn(rq_[k], vol_f3[k]);
+				box[k] = vol_box3[k];
+				ib[k] = rcp64(vol_box3[k]);
+			}
 	}
 	double d[3];
 #pragma unroll
@@ -437,12 +444,12 @@ __device__ __forceinline__ void atomicMaxFloatBits(unsigned int *addr, float v) 
 
 /* audit: compare an FP32 decision, and the certified FP64 decision, with the exact one */
 __device__ __noinline__ void audit_pair(const double *rec_all, const ppi_rparams *rp, ppi_rstate *rs, const double *box, const double *inv_box, int ps, int kind,
-		float4 q, float3 disp, int qs, int vol_dir, double vol_f, double vol_side, int cl, PairF f) {
+		float4 q, float3 disp, int qs, int vol_mask, const double *vol_f3, const double *vol_box3, int cl, PairF f) {
 	double d2, pm = -2., qm = -2.;
-	int ex = exact_pair(rec_all, rp, box, ps, kind, q, disp, qs, vol_dir, vol_f, vol_side, &d2, &pm, &qm);
+	int ex = exact_pair(rec_all, rp, box, ps, kind, q, disp, qs, vol_mask, vol_f3, vol_box3, &d2, &pm, &qm);
 	int exc = ex == -1 ? CL_OVER : (ex == 1 ? CL_BOND : CL_NONE);
 	if(cl != CL_UNSURE && cl != exc) atomicAdd(&rs->mismatches, 1ull);
-	const int dc = decide64(rec_all, *rp, box, inv_box, ps, kind, q, disp, qs, vol_dir, vol_f, vol_side);
+	const int dc = decide64(rec_all, *rp, box, inv_box, ps, kind, q, disp, qs, vol_mask, vol_f3, vol_box3);
 	if(dc != DEC64_EXACT && dc != ex) atomicAdd(&rs->mismatches, 1ull);
 	if(d2 < (double) rp->sqr_rcut + 0.5) atomicMaxFloatBits(&rs->max_err_r2_bits, (float) fabs((double) f.r2 - d2));
 	if(pm > -1.5 && f.pmax > -1.5f) {
@@ -802,15 +809,15 @@ __device__ __forceinline__ int wrapi(int v, int n) { return v < 0 ? v + n : (v >
 /* the FP32 decision for one pair and one state of p, made exact in the guard band */
 template <int MODE>
 __device__ __forceinline__ int pair_state(const double *rec, const ppi_rparams &rp, ppi_rstate *rs, const double *inv_box, int pslot, int kind, float4 q, float3 disp,
-		int qslot, float dx, float dy, float dz, const float *cp, const float *cq, float sqr_rcut, float cosmax, float basef, float eps, int vol_dir, double vol_f,
-		double vol_side, unsigned &fallbacks) {
+		int qslot, float dx, float dy, float dz, const float *cp, const float *cq, float sqr_rcut, float cosmax, float basef, float eps, int vol_mask,
+		const double *vol_f3, const double *vol_box3, unsigned &fallbacks) {
 	PairF f;
 	int cl = classify(dx, dy, dz, cp, cq, sqr_rcut, cosmax, basef, eps, MODE == MODE_AUDIT ? &f : nullptr);
-	if(MODE == MODE_AUDIT) audit_pair(rec, &rp, rs, rs->box, inv_box, pslot, kind, q, disp, qslot, vol_dir, vol_f, vol_side, cl, f);
+	if(MODE == MODE_AUDIT) audit_pair(rec, &rp, rs, rs->box, inv_box, pslot, kind, q, disp, qslot, vol_mask, vol_f3, vol_box3, cl, f);
 	if(cl == CL_UNSURE) {
 		fallbacks++;
-		int ex = decide64(rec, rp, rs->box, inv_box, pslot, kind, q, disp, qslot, vol_dir, vol_f, vol_side);
-		if(ex == DEC64_EXACT) ex = exact_pair(rec, &rp, rs->box, pslot, kind, q, disp, qslot, vol_dir, vol_f, vol_side, nullptr, nullptr, nullptr);
+		int ex = decide64(rec, rp, rs->box, inv_box, pslot, kind, q, disp, qslot, vol_mask, vol_f3, vol_box3);
+		if(ex == DEC64_EXACT) ex = exact_pair(rec, &rp, rs->box, pslot, kind, q, disp, qslot, vol_mask, vol_f3, vol_box3, nullptr, nullptr, nullptr);
 		cl = ex == -1 ? CL_OVER : (ex == 1 ? CL_BOND : CL_NONE);
 	}
 	return cl;
@@ -1011,9 +1018,9 @@ __device__ __forceinline__ void attempt_exact(const ppi_dev &d, const int4 ent, 
 			const float4 qb = d.sori[3 * (size_t) jq], qc = d.sori[3 * (size_t) jq + 1], qd = d.sori[3 * (size_t) jq + 2];
 			const float cq[9] = { qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w, qd.x };
 			const int qslot = __float_as_int(qd.w);
-			const int clo = pair_state<MODE>(d.rec, rp, rs, g.inv_L, P.pslot, 0, P.q, P.disp, qslot, dxo, dyo, dzo, P.cpo, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0.,
+			const int clo = pair_state<MODE>(d.rec, rp, rs, g.inv_L, P.pslot, 0, P.q, P.disp, qslot, dxo, dyo, dzo, P.cpo, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, 0, nullptr, nullptr,
 					A.fallbacks);
-			const int cln = pair_state<MODE>(d.rec, rp, rs, g.inv_L, P.pslot, 1, P.q, P.disp, qslot, dxn, dyn, dzn, cpn, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0.,
+			const int cln = pair_state<MODE>(d.rec, rp, rs, g.inv_L, P.pslot, 1, P.q, P.disp, qslot, dxn, dyn, dzn, cpn, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, 0, nullptr, nullptr,
 					A.fallbacks);
 			if(cln == CL_OVER) return;
 			bo += (clo == CL_BOND);
@@ -1080,8 +1087,8 @@ __device__ __forceinline__ void tile_close(const ppi_dev &d, TileSmem &S, int la
 			const float4 md = S.md[a];
 			const int pslot = __float_as_int(md.w), qslot = __float_as_int(qd.w);
 			const float3 disp = make_float3(md.x, md.y, md.z);
-			clo = pair_state<MODE>(d.rec, rp, rs, d.grid[S.rep[a]].inv_L, pslot, 0, S.qr[a], disp, qslot, G.dxo, G.dyo, G.dzo, cpo, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0., A.fallbacks);
-			cln = pair_state<MODE>(d.rec, rp, rs, d.grid[S.rep[a]].inv_L, pslot, 1, S.qr[a], disp, qslot, G.dxn, G.dyn, G.dzn, cpn, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0., A.fallbacks);
+			clo = pair_state<MODE>(d.rec, rp, rs, d.grid[S.rep[a]].inv_L, pslot, 0, S.qr[a], disp, qslot, G.dxo, G.dyo, G.dzo, cpo, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, 0, nullptr, nullptr, A.fallbacks);
+			cln = pair_state<MODE>(d.rec, rp, rs, d.grid[S.rep[a]].inv_L, pslot, 1, S.qr[a], disp, qslot, G.dxn, G.dyn, G.dzn, cpn, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, 0, nullptr, nullptr, A.fallbacks);
 		}
 		else {
 			clo = classify(G.dxo, G.dyo, G.dzo, cpo, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, nullptr);
@@ -1395,7 +1402,7 @@ __device__ __forceinline__ void tile_round(const ppi_dev &d, TileSmem &S, const 
 			const float4 md = S.md[a];
 			A.fallbacks++;
 			const int ex = decide64(d.rec, d.rp[r], d.rs[r].box, d.grid[r].inv_L, __float_as_int(md.w), kind, S.qr[a], make_float3(md.x, md.y, md.z),
-					__float_as_int(d.sori[3 * (size_t) jq + 2].w), -1, 1., 0.);
+					__float_as_int(d.sori[3 * (size_t) jq + 2].w), 0, nullptr, nullptr);
 			if(ex == DEC64_EXACT) atomicOr(&S.flag[a], TF_DEFER);
 			else if(ex == 1) atomicAdd(kind ? &S.bn[a] : &S.bo[a], 1);
 			else if(ex == -1 && kind) atomicOr(&S.flag[a], TF_OVER);
@@ -1868,9 +1875,9 @@ __device__ __forceinline__ bool scan_move(const ppi_dev &d, const Proposal &P, c
 			const float cq[9] = { qb[u].x, qb[u].y, qb[u].z, qb[u].w, qc[u].x, qc[u].y, qc[u].z, qc[u].w, qd[u].x };
 			const int qslot = __float_as_int(qd[u].w);
 			const int clo = pair_state<MODE>(d.rec, rp, rs, g.inv_L, P.pslot, 0, P.q, P.disp, qslot, go[u][0], go[u][1], go[u][2], P.cpo, cq, rp.sqr_rcut_f, rp.cosmax_f,
-					rp.base_f, eps, -1, 1., 0., A.fallbacks);
+					rp.base_f, eps, 0, nullptr, nullptr, A.fallbacks);
 			const int cln = pair_state<MODE>(d.rec, rp, rs, g.inv_L, P.pslot, 1, P.q, P.disp, qslot, gn[u][0], gn[u][1], gn[u][2], cpn, cq, rp.sqr_rcut_f, rp.cosmax_f,
-					rp.base_f, eps, -1, 1., 0., A.fallbacks);
+					rp.base_f, eps, 0, nullptr, nullptr, A.fallbacks);
 			if(cln == CL_OVER) return false;
 			bo += (clo == CL_BOND);
 			bn += (cln == CL_BOND);
@@ -2131,9 +2138,9 @@ __device__ __forceinline__ bool scan_move_cached(const ppi_dev &d, LearnCache &K
 				const float4 qb = K.ori[b][0][l], qc = K.ori[b][1][l], qd = K.ori[b][2][l];
 				const float cq[9] = { qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w, qd.x };
 				const int qslot = __float_as_int(qd.w);
-				const int clo = pair_state<MODE>(d.rec, rp, rs, g.inv_L, P.pslot, 0, P.q, P.disp, qslot, dxo, dyo, dzo, P.cpo, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1.,
-						0., A.fallbacks);
-				const int cln = pair_state<MODE>(d.rec, rp, rs, g.inv_L, P.pslot, 1, P.q, P.disp, qslot, dxn, dyn, dzn, cpn, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, -1, 1., 0.,
+				const int clo = pair_state<MODE>(d.rec, rp, rs, g.inv_L, P.pslot, 0, P.q, P.disp, qslot, dxo, dyo, dzo, P.cpo, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, 0, nullptr,
+						nullptr, A.fallbacks);
+				const int cln = pair_state<MODE>(d.rec, rp, rs, g.inv_L, P.pslot, 1, P.q, P.disp, qslot, dxn, dyn, dzn, cpn, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, 0, nullptr, nullptr,
 						A.fallbacks);
 				if(cln == CL_OVER) return false;
 				bo += (clo == CL_BOND);
@@ -2458,21 +2465,24 @@ __device__ __forceinline__ void energy_exact(const ppi_dev &d, int mode, int k, 
 	const ppi_rparams &rp = d.rp[r];
 	const ppi_grid &g = d.grid[r];
 	ppi_rstate *rs = d.rs + r;
-	int sdir = -1;
-	float sf = 1.f;
-	double vf = 1.0, vside = 0.0;
+	int vmask = 0;
+	float sf3[3] = { 1.f, 1.f, 1.f };
+	const double *vf3 = nullptr, *vb3 = nullptr;
 	if(mode == PPI_EN_VOLUME) {
 		if(g.vol_dir < 0 || rs->vol_overlap) return;
-		sdir = g.vol_dir;
-		sf = g.vol_ff;
-		vf = g.vol_f;
-		vside = g.vol_side;
+		vmask = g.vol_mask;
+		sf3[0] = g.vol_ff3[0];
+		sf3[1] = g.vol_ff3[1];
+		sf3[2] = g.vol_ff3[2];
+		vf3 = g.vol_f3;
+		vb3 = g.vol_box3;
 	}
 	float w[3] = { g.wf[0], g.wf[1], g.wf[2] };
 	float pl[3] = { pa.x, pa.y, pa.z };
-	if(sdir >= 0) {
-		w[sdir] *= sf;
-		pl[sdir] *= sf;
+#pragma unroll
+	for(int a = 0; a < 3; a++) { /* the candidate box (a factor 1 on unscaled axes changes nothing) */
+		w[a] *= sf3[a];
+		pl[a] *= sf3[a];
 	}
 	const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
 	const int local = gc - rp.cell_base;
@@ -2493,7 +2503,9 @@ __device__ __forceinline__ void energy_exact(const ppi_dev &d, int mode, int k, 
 			if(jq == k) continue;
 			const float4 qa = d.spos[jq];
 			float ql[3] = { qa.x, qa.y, qa.z };
-			if(sdir >= 0) ql[sdir] *= sf;
+			ql[0] *= sf3[0];
+			ql[1] *= sf3[1];
+			ql[2] *= sf3[2];
 			const float ddx = (ql[0] - pl[0]) + ox, ddy = (ql[1] - pl[1]) + oy, ddz = (ql[2] - pl[2]) + oz;
 			const float r2 = fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz));
 			A.pairs++;
@@ -2501,7 +2513,7 @@ __device__ __forceinline__ void energy_exact(const ppi_dev &d, int mode, int k, 
 			const float4 qb = d.sori[3 * (size_t) jq], qc = d.sori[3 * (size_t) jq + 1], qd = d.sori[3 * (size_t) jq + 2];
 			const float cq[9] = { qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w, qd.x };
 			const int cl = pair_state<MODE_FAST>(d.rec, rp, rs, g.inv_L, pslot, 0, q0, d0, __float_as_int(qd.w), ddx, ddy, ddz, cp, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps,
-					sdir, vf, vside, A.fallbacks);
+					vmask, vf3, vb3, A.fallbacks);
 			if(cl == CL_BOND) {
 				if(partners && nb < PPI_MAX_PARTNERS) partners[nb] = __float_as_int(qd.y);
 				nb++;
@@ -2538,25 +2550,28 @@ __device__ __forceinline__ int energy_particle(const ppi_dev &d, int mode, int k
 	const ppi_rparams &rp = d.rp[r];
 	const ppi_grid &g = d.grid[r];
 	ppi_rstate *rs = d.rs + r;
-	int sdir = -1;
-	float sf = 1.f;
-	double vf = 1.0, vside = 0.0;
+	int vmask = 0;
+	float sf3[3] = { 1.f, 1.f, 1.f };
+	const double *vf3 = nullptr, *vb3 = nullptr;
 	if(mode == PPI_EN_VOLUME) {
 		if(g.vol_dir < 0) return 0;
 		/* one overlap already rejects the candidate box: skip (one read per group, shared) */
 		int skip = sub == 0 ? *(volatile int *) &rs->vol_overlap : 0;
 		skip = __shfl_sync(gm, skip, 0, G);
 		if(skip) return 0;
-		sdir = g.vol_dir;
-		sf = g.vol_ff;
-		vf = g.vol_f;
-		vside = g.vol_side;
+		vmask = g.vol_mask;
+		sf3[0] = g.vol_ff3[0];
+		sf3[1] = g.vol_ff3[1];
+		sf3[2] = g.vol_ff3[2];
+		vf3 = g.vol_f3;
+		vb3 = g.vol_box3;
 	}
 	float w[3] = { g.wf[0], g.wf[1], g.wf[2] };
 	float pl[3] = { pa.x, pa.y, pa.z };
-	if(sdir >= 0) {
-		w[sdir] *= sf;
-		pl[sdir] *= sf;
+#pragma unroll
+	for(int a = 0; a < 3; a++) { /* the candidate box (a factor 1 on unscaled axes changes nothing) */
+		w[a] *= sf3[a];
+		pl[a] *= sf3[a];
 	}
 	const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
 	const int local = gc - rp.cell_base;
@@ -2597,7 +2612,9 @@ __device__ __forceinline__ int energy_particle(const ppi_dev &d, int mode, int k
 				if(jq == k) continue;
 				const float4 qa = d.spos[jq];
 				float ql[3] = { qa.x, qa.y, qa.z };
-				if(sdir >= 0) ql[sdir] *= sf;
+				ql[0] *= sf3[0];
+				ql[1] *= sf3[1];
+				ql[2] *= sf3[2];
 				const float ddx = (ql[0] - pl[0]) + ox, ddy = (ql[1] - pl[1]) + oy, ddz = (ql[2] - pl[2]) + oz;
 				const float r2 = fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz));
 				A.pairs++;
@@ -2609,7 +2626,7 @@ __device__ __forceinline__ int energy_particle(const ppi_dev &d, int mode, int k
 					const float4 qd = d.sori[3 * (size_t) jq + 2];
 					const float cq[9] = { qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w, qd.x };
 					if(MODE == MODE_AUDIT)
-						cl = pair_state<MODE>(d.rec, rp, rs, g.inv_L, pslot, 0, q0, d0, __float_as_int(qd.w), ddx, ddy, ddz, cp, cq, sqr_rcut, cosmax, basef, eps, sdir, vf, vside, A.fallbacks);
+						cl = pair_state<MODE>(d.rec, rp, rs, g.inv_L, pslot, 0, q0, d0, __float_as_int(qd.w), ddx, ddy, ddz, cp, cq, sqr_rcut, cosmax, basef, eps, vmask, vf3, vb3, A.fallbacks);
 					else {
 						cl = classify(ddx, ddy, ddz, cp, cq, sqr_rcut, cosmax, basef, eps, nullptr);
 						if(cl == CL_UNSURE) { /* decided after the loop by the certified FP64 test */
@@ -2636,7 +2653,7 @@ __device__ __forceinline__ int energy_particle(const ppi_dev &d, int mode, int k
 				const int jq = k2 ? u1 : u0;
 				const float4 qd = d.sori[3 * (size_t) jq + 2];
 				A.fallbacks++;
-				const int ex = decide64(d.rec, rp, rs->box, g.inv_L, pslot, 0, q0, d0, __float_as_int(qd.w), sdir, vf, vside);
+				const int ex = decide64(d.rec, rp, rs->box, g.inv_L, pslot, 0, q0, d0, __float_as_int(qd.w), vmask, vf3, vb3);
 				if(ex == DEC64_EXACT) {
 					uns = -1;
 					break;
@@ -2722,7 +2739,8 @@ __global__ void __launch_bounds__(128, MODE == MODE_FAST ? PPI_FAST_MIN_BLOCKS :
 struct __align__(16) VolSmem {
 	float4 pos[TA];   /* scaled cell-local position, .w = cell x index */
 	float4 wv[TA];    /* scaled cell edges, .w = number of x cells */
-	float4 vs[TA];    /* (scale factor, scaled axis as int bits, 1 - eps, r_cut^2 + eps) */
+	float4 vs[TA];    /* (-, -, 1 - eps, r_cut^2 + eps) */
+	float4 sc[TA];    /* scale factors of the candidate box per axis (1 on unscaled axes) */
 	float cp[9][TA];  /* orientation columns */
 	int ki[TA];       /* sorted position */
 	int rep[TA];
@@ -2738,20 +2756,20 @@ __device__ __forceinline__ void vol_exact_later(const ppi_dev &d, VolSmem &S, in
 
 __device__ __forceinline__ void vol_setup(const ppi_dev &d, VolSmem &S, int a, int k) {
 	int cc = -1, r = 0;
-	float4 pos = make_float4(0.f, 0.f, 0.f, 0.f), wv = make_float4(1.f, 1.f, 1.f, __int_as_float(4)), vs = make_float4(1.f, __int_as_float(-1), 0.f, 0.f);
+	float4 pos = make_float4(0.f, 0.f, 0.f, 0.f), wv = make_float4(1.f, 1.f, 1.f, __int_as_float(4)), vs = make_float4(0.f, 0.f, 0.f, 0.f);
+	float4 sc = make_float4(1.f, 1.f, 1.f, 0.f);
 	if(k >= 0) {
 		const float4 pa = d.spos[k], pb = d.sori[3 * (size_t) k], pc = d.sori[3 * (size_t) k + 1], pd = d.sori[3 * (size_t) k + 2];
 		const int gc = __float_as_int(pd.z);
 		r = d.cell_rep[gc];
 		const ppi_grid &g = d.grid[r];
 		if(g.vol_dir >= 0) {
-			const int sdir = g.vol_dir;
-			const float sf = g.vol_ff;
-			pos = make_float4(sdir == 0 ? pa.x * sf : pa.x, sdir == 1 ? pa.y * sf : pa.y, sdir == 2 ? pa.z * sf : pa.z, pa.w);
-			wv = make_float4(sdir == 0 ? g.wf[0] * sf : g.wf[0], sdir == 1 ? g.wf[1] * sf : g.wf[1], sdir == 2 ? g.wf[2] * sf : g.wf[2], __int_as_float(g.n[0]));
+			sc = make_float4(g.vol_ff3[0], g.vol_ff3[1], g.vol_ff3[2], 0.f);
+			pos = make_float4(pa.x * sc.x, pa.y * sc.y, pa.z * sc.z, pa.w);
+			wv = make_float4(g.wf[0] * sc.x, g.wf[1] * sc.y, g.wf[2] * sc.z, __int_as_float(g.n[0]));
 			const ppi_rparams &rp = d.rp[r];
 			const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
-			vs = make_float4(sf, __int_as_float(sdir), 1.f - eps, rp.sqr_rcut_f + eps);
+			vs = make_float4(0.f, 0.f, 1.f - eps, rp.sqr_rcut_f + eps);
 			const int local = gc - d.rp[r].cell_base;
 			cc = (local % g.n[0]) | (((local / g.n[0]) % g.n[1]) << 10) | ((local / (g.n[0] * g.n[1])) << 20);
 			const float c9[9] = { pb.x, pb.y, pb.z, pb.w, pc.x, pc.y, pc.z, pc.w, pd.x };
@@ -2762,6 +2780,7 @@ __device__ __forceinline__ void vol_setup(const ppi_dev &d, VolSmem &S, int a, i
 	S.pos[a] = pos;
 	S.wv[a] = wv;
 	S.vs[a] = vs;
+	S.sc[a] = sc;
 	S.ki[a] = k;
 	S.rep[a] = r;
 	S.cc[a] = cc;
@@ -2820,9 +2839,8 @@ __device__ __forceinline__ void vol_write(VolSmem &S, int a, int pz, const Plane
 
 /* candidate position in particle a's scaled cell frame, relative to a */
 __device__ __forceinline__ float3 vol_geo(const VolSmem &S, int a, int t, float4 qa) {
-	const float4 p = S.pos[a], w = S.wv[a], v = S.vs[a];
-	const int sdir = __float_as_int(v.y);
-	const float qx = sdir == 0 ? qa.x * v.x : qa.x, qy = sdir == 1 ? qa.y * v.x : qa.y, qz = sdir == 2 ? qa.z * v.x : qa.z;
+	const float4 p = S.pos[a], w = S.wv[a], c = S.sc[a];
+	const float qx = qa.x * c.x, qy = qa.y * c.y, qz = qa.z * c.z;
 	const int nxc = __float_as_int(w.w);
 	int dxc = __float_as_int(qa.w) - __float_as_int(p.w);
 	dxc = dxc > 1 ? dxc - nxc : (dxc < -1 ? dxc + nxc : dxc);
@@ -2882,9 +2900,9 @@ __device__ __forceinline__ void vol_pair_decide(const ppi_dev &d, VolSmem &S, in
 	const float3 d0 = make_float3(0.f, 0.f, 0.f);
 	A.fallbacks++;
 	int ex;
-	if(EXACT) ex = exact_pair(d.rec, d.rp + r, d.rs[r].box, ps, 0, q0, d0, qs, g.vol_dir, g.vol_f, g.vol_side, nullptr, nullptr, nullptr);
+	if(EXACT) ex = exact_pair(d.rec, d.rp + r, d.rs[r].box, ps, 0, q0, d0, qs, g.vol_mask, g.vol_f3, g.vol_box3, nullptr, nullptr, nullptr);
 	else {
-		ex = decide64(d.rec, d.rp[r], d.rs[r].box, g.inv_L, ps, 0, q0, d0, qs, g.vol_dir, g.vol_f, g.vol_side);
+		ex = decide64(d.rec, d.rp[r], d.rs[r].box, g.inv_L, ps, 0, q0, d0, qs, g.vol_mask, g.vol_f3, g.vol_box3);
 		if(ex == DEC64_EXACT) {
 			vol_exact_later(d, S, jq, k);
 			return;
@@ -3155,6 +3173,9 @@ __global__ void k_energy_reset(ppi_dev d) {
 /* ------------------------------------------------------------------------------------------------ */
 /* NPT volume move (MC.c:450-513)                                                                   */
 /* ------------------------------------------------------------------------------------------------ */
+/* the candidate box of the sweep: an NPT volume move (MC.c:456-472) or, for NVT replicas with Lx_move, a
+ * box-shape move (MC_change_Lx, MC.c:515-537): Lx changes by (R - 0.5) Lx_change_max, Ly = Lz =
+ * sqrt(V / Lx) keep the volume, every coordinate is rescaled by its side's factor */
 __global__ void k_vol_plan(ppi_dev d, long long sweep) {
 	int r = blockIdx.x * blockDim.x + threadIdx.x;
 	if(r >= d.nrep) return;
@@ -3167,23 +3188,70 @@ __global__ void k_vol_plan(ppi_dev d, long long sweep) {
 	rs->vol_overlap = 0;
 	rs->vol_accept = 0;
 	g->vol_dir = -1;
-	if(rp.ensemble != 5 || rp.N <= 0) return;
+	g->vol_mask = 0;
+	for(int k = 0; k < 3; k++) {
+		g->vol_f3[k] = 1.0;
+		g->vol_box3[k] = rs->box[k];
+		g->vol_ff3[k] = 1.f;
+	}
+	if(rp.N <= 0) return;
 	U4 u = rng(rp, sweep, r, TAG_VOL, 0, 0);
-	/* random axis, ln V' = ln V + (R - 0.5) rescale_factor_max, one side takes the whole change (MC.c:456-472) */
-	int dir = (int) (u01d(u.x, u.y) * 3.0);
-	if(dir > 2) dir = 2;
-	double V0 = rs->box[0] * rs->box[1] * rs->box[2];
-	double lnV = log(V0) + (u01d(u.z, u.w) - 0.5) * rp.rescale_max;
-	double V1 = exp(lnV);
-	double side = V1;
-	for(int i = 0; i < 3; i++)
-		if(i != dir) side /= rs->box[i];
-	g->vol_dir = dir;
-	g->vol_side = side;
-	g->vol_f = side / rs->box[dir];
-	g->vol_ff = (float) g->vol_f;
-	g->vol_V0 = V0;
-	g->vol_V1 = V1;
+	if(rp.ensemble == 5) {
+		/* random axis, ln V' = ln V + (R - 0.5) rescale_factor_max, one side takes the whole change */
+		int dir = (int) (u01d(u.x, u.y) * 3.0);
+		if(dir > 2) dir = 2;
+		double V0 = rs->box[0] * rs->box[1] * rs->box[2];
+		double lnV = log(V0) + (u01d(u.z, u.w) - 0.5) * rp.rescale_max;
+		double V1 = exp(lnV);
+		double side = V1;
+		for(int i = 0; i < 3; i++)
+			if(i != dir) side /= rs->box[i];
+		g->vol_dir = dir;
+		g->vol_mask = 1 << dir;
+		g->vol_f = side / rs->box[dir];
+		g->vol_f3[dir] = g->vol_f;
+		g->vol_box3[dir] = side;
+		g->vol_ff3[dir] = (float) g->vol_f;
+		g->vol_V0 = V0;
+		g->vol_V1 = V1;
+		return;
+	}
+	if(!rp.lx_move) return;
+	const double lx = rs->box[0] + (u01d(u.x, u.y) - 0.5) * rp.lx_change_max;
+	const double lyz = sqrt(rs->V / lx);
+	/* early rejection (MC.c:526-530); a non-positive Lx (Lx_change_max above twice the side) is rejected too */
+	if(!(lx > 0.) || lyz < rp.lyz_min || lyz > rp.lyz_max) {
+		rs->tries[7]++;
+		return;
+	}
+	const double nb[3] = { lx, lyz, lyz };
+	for(int k = 0; k < 3; k++) {
+		g->vol_box3[k] = nb[k];
+		g->vol_f3[k] = nb[k] / rs->box[k]; /* rescale_factors (MC.c:533-537) */
+		g->vol_ff3[k] = (float) g->vol_f3[k];
+		if(g->w[k] * g->vol_f3[k] < rp.r_cut) { /* the cells of the candidate box would be too small */
+			rs->error = PPI_E_GRID;
+			rs->tries[7]++;
+			return;
+		}
+	}
+	g->vol_dir = PPI_LX_DIR;
+	g->vol_mask = 7;
+	g->vol_V0 = g->vol_V1 = rs->V;
+}
+
+/* an accepted candidate box: the cell grid scales with the box, cell membership is unchanged */
+__device__ void grid_scale_axis(ppi_grid *g, ppi_rstate *rs, int a) {
+	const double f = g->vol_f3[a];
+	rs->box[a] = g->vol_box3[a];
+	g->w[a] *= f;
+	g->shift[a] *= f;
+	g->wf[a] = (float) g->w[a];
+	g->inv_w[a] = 1.0 / g->w[a];
+	g->inv_L[a] = 1.0 / rs->box[a];
+	g->inv_wf[a] = (float) g->inv_w[a];
+	g->inv_Lf[a] = (float) g->inv_L[a];
+	g->Lf[a] = (float) rs->box[a];
 }
 
 __global__ void k_vol_decide(ppi_dev d, long long sweep) {
@@ -3194,41 +3262,45 @@ __global__ void k_vol_decide(ppi_dev d, long long sweep) {
 	ppi_grid *g = d.grid + r;
 	ppi_rstate *rs = d.rs + r;
 	if(g->vol_dir < 0) return;
+	const long long nb_new = rs->vol_bonds / 2; /* every bonded pair was counted from both sides */
+	const double dE = (double) (rs->bonds - nb_new);
+	const U4 u = rng(rp, sweep, r, TAG_VOL, 0, 1);
+	if(g->vol_dir == PPI_LX_DIR) {
+		rs->tries[7]++;
+		/* MC.c:559 accepts with min(1, exp(+dE / T)); lx_move = 2 takes the Boltzmann factor exp(-dE / T) */
+		const double arg = (rp.lx_move == 2 ? -dE : dE) / rp.T;
+		if(!rs->vol_overlap && u01d(u.x, u.y) < exp(arg)) {
+			rs->vol_accept = 1;
+			d.ctr->vol_any = 1;
+			rs->bonds = nb_new;
+			rs->accepted[7]++;
+			for(int a = 0; a < 3; a++) grid_scale_axis(g, rs, a);
+		}
+		return;
+	}
 	rs->tries[6]++;
-	long long nb_new = rs->vol_bonds / 2; /* every bonded pair was counted from both sides */
-	double dE = (double) (rs->bonds - nb_new);
 	double dV = g->vol_V1 - g->vol_V0;
 	double arg = -(rp.P * dV + dE) / rp.T + (double) (rp.N + 1) * log(g->vol_f); /* MC.c:497-498 */
-	U4 u = rng(rp, sweep, r, TAG_VOL, 0, 1);
 	if(!rs->vol_overlap && u01d(u.x, u.y) < exp(arg)) {
-		int a = g->vol_dir;
 		rs->vol_accept = 1;
 		d.ctr->vol_any = 1;
-		rs->box[a] = g->vol_side;
 		rs->V = g->vol_V1;
 		rs->bonds = nb_new;
 		rs->accepted[6]++;
-		/* the cell grid scales with the box: cell membership is unchanged */
-		g->w[a] *= g->vol_f;
-		g->shift[a] *= g->vol_f;
-		g->wf[a] = (float) g->w[a];
-		g->inv_w[a] = 1.0 / g->w[a];
-		g->inv_L[a] = 1.0 / rs->box[a];
-		g->inv_wf[a] = (float) g->inv_w[a];
-		g->inv_Lf[a] = (float) g->inv_L[a];
-		g->Lf[a] = (float) rs->box[a];
+		grid_scale_axis(g, rs, g->vol_dir);
 	}
 }
 
 __global__ void k_vol_apply(ppi_dev d) {
 	int k = blockIdx.x * blockDim.x + threadIdx.x;
-	if(k >= d.ntot || !d.ctr->vol_any) return; /* every replica rejected its volume move: nothing to rescale */
-	/* canonical positions (slot k) */
+	if(k >= d.ntot || !d.ctr->vol_any) return; /* every replica rejected its candidate box: nothing to rescale */
+	/* canonical positions (slot k): p->r[a] *= rescale_factor (MC.c:477, MC.c:541-544) */
 	int r = d.rep[k];
 	if(d.rs[r].vol_accept) {
 		const ppi_grid &g = d.grid[r];
 		double *rec = d.rec + (size_t) k * PPI_REC;
-		rec[g.vol_dir] = __dmul_rn(rec[g.vol_dir], g.vol_f); /* p->r[dir] *= rescale_factor (MC.c:477) */
+		for(int a = 0; a < 3; a++)
+			if((g.vol_mask >> a) & 1) rec[a] = __dmul_rn(rec[a], g.vol_f3[a]);
 	}
 	/* working record (sorted position k) */
 	int gc = __float_as_int(d.sori[3 * (size_t) k + 2].z);
@@ -3236,9 +3308,9 @@ __global__ void k_vol_apply(ppi_dev d) {
 	if(d.rs[r2].vol_accept) {
 		const ppi_grid &g = d.grid[r2];
 		float4 a = d.spos[k];
-		if(g.vol_dir == 0) a.x *= g.vol_ff;
-		else if(g.vol_dir == 1) a.y *= g.vol_ff;
-		else a.z *= g.vol_ff;
+		a.x *= g.vol_ff3[0];
+		a.y *= g.vol_ff3[1];
+		a.z *= g.vol_ff3[2];
 		d.spos[k] = a;
 	}
 }
