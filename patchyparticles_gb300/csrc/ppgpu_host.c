@@ -259,7 +259,13 @@ static void free_device(pp_engine *e) {
 	e->d.ctr = NULL;
 	if(e->d.nl) cudaFree(e->d.nl);
 	if(e->d.nl_cnt) cudaFree(e->d.nl_cnt);
-	e->d.nl = e->d.nl_cnt = NULL;
+	if(e->d.vpairs) cudaFree(e->d.vpairs);
+	if(e->d.vp_count) cudaFree(e->d.vp_count);
+	if(e->d.srep) cudaFree(e->d.srep);
+	if(e->d.vp_over) cudaFree(e->d.vp_over);
+	e->d.nl = e->d.nl_cnt = e->d.vp_count = e->d.srep = e->d.vp_over = NULL;
+	e->d.vpairs = NULL;
+	e->d.vp_cap = 0;
 	e->d.nl_k = 0;
 	e->nl_valid = 0;
 	drop_graphs(e);
@@ -439,7 +445,9 @@ static int read_states(pp_engine *e) {
 	CU(cudaStreamSynchronize(e->stream));
 	if(lerr) return set_err(e, PP_ERR_CUDA, "a tensor-core wait of the learned proposal timed out");
 	for(int r = 0; r < e->nrep; r++)
-		if(e->h_rs[r].error == PPI_E_EXACT)
+		if(e->h_rs[r].error == PPI_E_LISTS)
+			return set_err(e, PP_ERR_CAPACITY, "replica %d: the volume pass's pair list ran out of capacity (neighbour lists overflowing)", r);
+		else if(e->h_rs[r].error == PPI_E_EXACT)
 			return set_err(e, PP_ERR_STATE, "replica %d: more pairs within 1e-12 of a bonding threshold than one warp keeps for the exact test", r);
 		else if(e->h_rs[r].error)
 			return set_err(e, PP_ERR_CAPACITY, "replica %d: the box no longer fits an even cell grid of edge >= r_cut (device error %d)", r, e->h_rs[r].error);
@@ -529,28 +537,37 @@ static int setup_nlists(pp_engine *e) {
 		if(K > 0 && v && atoi(v) > 0 && atoi(v) <= 128) K = (atoi(v) + 3) & ~3;
 	}
 	if(!e->nl_mode || e->d.ntot >= (1 << 27)) K = 0; /* a list entry holds sorted positions below 2^27 */
-	if(K == 0) {
-		if(e->d.nl) cudaFree(e->d.nl);
-		if(e->d.nl_cnt) cudaFree(e->d.nl_cnt);
-		e->d.nl = e->d.nl_cnt = NULL;
-		if(e->d.nl_k) e->graph_gen++;
-		e->d.nl_k = 0;
-		e->nl_valid = 0;
-		return PP_OK;
+	/* (re)allocate when the capacity grows; K == 0 frees the lists */
+	if(K == 0 && e->d.nl_k == 0 && e->d.nl == NULL) return PP_OK;
+	if(K > 0 && K <= e->d.nl_k && e->d.nl != NULL) return PP_OK;
+	drop_graphs(e);
+	e->graph_gen++;
+	if(e->d.nl) cudaFree(e->d.nl);
+	if(e->d.nl_cnt) cudaFree(e->d.nl_cnt);
+	if(e->d.vpairs) cudaFree(e->d.vpairs);
+	if(e->d.vp_count) cudaFree(e->d.vp_count);
+	if(e->d.srep) cudaFree(e->d.srep);
+	if(e->d.vp_over) cudaFree(e->d.vp_over);
+	e->d.nl = e->d.nl_cnt = e->d.vp_count = e->d.srep = e->d.vp_over = NULL;
+	e->d.vpairs = NULL;
+	e->d.vp_cap = 0;
+	e->d.nl_k = 0;
+	e->nl_valid = 0;
+	if(K == 0) return PP_OK;
+	const size_t n1 = e->d.ntot > 0 ? (size_t) e->d.ntot : 1;
+	CU(cudaMalloc((void **) &e->d.nl, sizeof(int) * (size_t) K * n1));
+	CU(cudaMalloc((void **) &e->d.nl_cnt, sizeof(int) * n1));
+	/* the volume pass's flat pair list: at most K pairs above each particle (an overflowing particle goes to
+	 * vp_over), so the capacity cannot run out */
+	if((size_t) K * n1 < (size_t) 1 << 31) {
+		CU(cudaMalloc((void **) &e->d.vpairs, sizeof(int2) * (size_t) K * n1));
+		CU(cudaMalloc((void **) &e->d.vp_count, 2 * sizeof(int)));
+		CU(cudaMalloc((void **) &e->d.srep, sizeof(int) * n1));
+		CU(cudaMalloc((void **) &e->d.vp_over, sizeof(int) * n1));
+		CU(cudaMemsetAsync(e->d.vp_count, 0, 2 * sizeof(int), e->stream));
+		e->d.vp_cap = (int) ((size_t) K * n1);
 	}
-	if(K > e->d.nl_k || e->d.nl == NULL) {
-		drop_graphs(e);
-		e->graph_gen++;
-		if(e->d.nl) cudaFree(e->d.nl);
-		if(e->d.nl_cnt) cudaFree(e->d.nl_cnt);
-		e->d.nl = e->d.nl_cnt = NULL;
-		e->d.nl_k = 0;
-		e->nl_valid = 0;
-		const size_t n1 = e->d.ntot > 0 ? (size_t) e->d.ntot : 1;
-		CU(cudaMalloc((void **) &e->d.nl, sizeof(int) * (size_t) K * n1));
-		CU(cudaMalloc((void **) &e->d.nl_cnt, sizeof(int) * n1));
-		e->d.nl_k = K;
-	}
+	e->d.nl_k = K;
 	return PP_OK;
 }
 

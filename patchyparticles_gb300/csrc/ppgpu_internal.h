@@ -40,6 +40,7 @@ extern "C" {
 /* error codes written by kernels into ppi_rstate.error */
 #define PPI_E_GRID 2  /* the box became too small for an even cell grid of edge >= r_cut */
 #define PPI_E_EXACT 3 /* more undecidable pairs in one warp's share of a volume pass than it keeps */
+#define PPI_E_LISTS 4 /* the flat pair list of the volume pass ran out of capacity */
 
 typedef struct ppi_rparams {
 	int N;           /* particles of this replica */
@@ -177,6 +178,13 @@ typedef struct ppi_dev {
 	 * cell offset code (dx + 1) + 3 (dy + 1) + 9 (dz + 1); nl_cnt[k] = entries (> nl_k: overflow) */
 	int *nl;
 	int *nl_cnt;
+	/* the epoch's pairs for the volume pass, each once: (lower sorted position i, candidate << 5 | code) */
+	int2 *vpairs;
+	int *vp_count;     /* [0] pairs written by the list build, [1] particles in vp_over */
+	int *vp_over;      /* sorted positions whose list overflowed: their half shell is scanned in the cells */
+	int *srep;         /* replica of each sorted position */
+	int vp_cap;
+	int pad5;
 } ppi_dev;
 
 #define PPI_MAX_PARTNERS 24

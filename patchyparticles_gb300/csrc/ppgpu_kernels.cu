@@ -618,6 +618,7 @@ __global__ void k_scatter(ppi_dev d, const float4 *tmp) {
 	{ /* .w = the cell's x index (neighbour offsets in the colour pass) */
 		const int r = d.rep[s];
 		a.w = __int_as_float((gc - d.rp[r].cell_base) % d.grid[r].n[0]);
+		if(d.srep) d.srep[pos] = r;
 	}
 	float R0[9], Q[9];
 #pragma unroll
@@ -1499,54 +1500,91 @@ __global__ void __launch_bounds__(32 * TILE_WARPS, MODE == MODE_FAST ? PPI_TILE_
  * same decisions, hence the same trajectory, with fewer pair tests and no cell-range lookups. */
 #define NL_B 128 /* threads per CTA of the list build */
 
-/* list of sorted position i: candidates in the 27 cells closer than the replica's list radius. The 3
- * cells of a row are one contiguous range of sorted positions (two where the row wraps around the box);
- * a candidate's x offset comes from its cell's x index (spos.w), as in pair_geo. */
-__global__ void __launch_bounds__(NL_B) k_nlist(ppi_dev d) {
-	const int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if(i >= d.ntot) return;
-	const float4 p = d.spos[i];
-	const int gc = __float_as_int(d.sori[3 * (size_t) i + 2].z);
-	const int r = d.cell_rep[gc];
-	const ppi_rparams &rp = d.rp[r];
-	const ppi_grid &g = d.grid[r];
-	const int K = d.nl_k;
-	const float R2 = rp.nl_r2f;
-	if(!(R2 > 0.f)) { /* no lists for this replica: its attempts take the exact path */
-		d.nl_cnt[i] = K + 1;
-		return;
-	}
-	int *out = d.nl + (size_t) i * K;
+/* the candidates of sorted position i in its 27 cells: visit(jq, code) for each, code = (dx + 1) +
+ * 3 (dy + 1) + 9 (dz + 1). The 3 cells of a row are one contiguous range of sorted positions (two where the
+ * row wraps around the box); a candidate's x offset comes from its cell's x index (spos.w). */
+template <typename V>
+__device__ __forceinline__ void nl_rows(const ppi_dev &d, int i, const ppi_rparams &rp, const ppi_grid &g, int cx, int cy, int cz, V visit) {
 	const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
-	const int local = gc - rp.cell_base;
-	const int cx = local % nx, cy = (local / nx) % ny, cz = local / (nx * ny);
-	const float wx = g.wf[0], wy = g.wf[1], wz = g.wf[2];
 	const bool inner = cx >= 1 && cx <= nx - 2;
 	const int xa0 = inner ? cx - 1 : (cx == 0 ? nx - 1 : nx - 2), xa1 = inner ? cx + 2 : nx;
 	const int xb1 = cx == 0 ? 2 : 1;
-	int n = 0;
 #pragma unroll 1
 	for(int row = 0; row < 9; row++) {
 		const int dy = row % 3 - 1, dz = row / 3 - 1;
 		const int *cs = d.cell_start + rp.cell_base + (wrapi(cz + dz, nz) * ny + wrapi(cy + dy, ny)) * nx;
-		const float oy = dy * wy, oz = dz * wz;
 		const int s0 = cs[xa0], e0 = cs[xa1], s1 = inner ? 0 : cs[0], e1 = inner ? 0 : cs[xb1];
 		const int len0 = e0 - s0, tot = len0 + (e1 - s1);
 		for(int t = 0; t < tot; t++) {
 			const int jq = t < len0 ? s0 + t : s1 + (t - len0);
-			if(jq == i) continue;
-			const float4 q = d.spos[jq];
-			int dxc = __float_as_int(q.w) - cx;
-			dxc = dxc > 1 ? dxc - nx : (dxc < -1 ? dxc + nx : dxc);
-			const float ex = (q.x - p.x) + dxc * wx, ey = (q.y - p.y) + oy, ez = (q.z - p.z) + oz;
-			if(fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < R2) {
-				if(n < K) out[n] = (int) (((unsigned) jq << 5) | (unsigned) ((dxc + 1) + 3 * (dy + 1) + 9 * (dz + 1)));
-				n++;
+			if(jq != i) visit(jq, dy, dz);
+		}
+	}
+}
+
+/* List of sorted position i: the candidates in its 27 cells closer than the replica's list radius. With
+ * d.vpairs, also the epoch's flat pair list of the volume pass: every listed candidate above i, one
+ * warp-aggregated reservation per warp (at most nl_k per particle, the list's capacity); a particle whose
+ * list overflowed goes to vp_over instead and the volume pass scans its half shell in the cells. */
+__global__ void __launch_bounds__(NL_B) k_nlist(ppi_dev d) {
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	const int lane = threadIdx.x & 31;
+	int n = 0, h = 0, emit = 0, K = d.nl_k, cx = 0, cy = 0, cz = 0, r = 0;
+	if(i < d.ntot) {
+		const float4 p = d.spos[i];
+		const int gc = __float_as_int(d.sori[3 * (size_t) i + 2].z);
+		r = d.cell_rep[gc];
+		const ppi_rparams &rp = d.rp[r];
+		const ppi_grid &g = d.grid[r];
+		const float R2 = rp.nl_r2f;
+		if(!(R2 > 0.f)) d.nl_cnt[i] = K + 1; /* no lists for this replica: its attempts take the exact path */
+		else {
+			emit = 1;
+			int *out = d.nl + (size_t) i * K;
+			const int nx = g.n[0];
+			const int local = gc - rp.cell_base;
+			cx = local % nx;
+			cy = (local / nx) % g.n[1];
+			cz = local / (nx * g.n[1]);
+			const float wx = g.wf[0], wy = g.wf[1], wz = g.wf[2];
+			nl_rows(d, i, rp, g, cx, cy, cz, [&](int jq, int dy, int dz) {
+				const float4 q = d.spos[jq];
+				int dxc = __float_as_int(q.w) - cx;
+				dxc = dxc > 1 ? dxc - nx : (dxc < -1 ? dxc + nx : dxc);
+				const float ex = (q.x - p.x) + dxc * wx, ey = (q.y - p.y) + dy * wy, ez = (q.z - p.z) + dz * wz;
+				if(fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < R2) {
+					if(n < K) out[n] = (int) (((unsigned) jq << 5) | (unsigned) ((dxc + 1) + 3 * (dy + 1) + 9 * (dz + 1)));
+					n++;
+					h += jq > i;
+				}
+			});
+			d.nl_cnt[i] = n;
+			if(n > K) {
+				atomicAdd(&d.rs[r].nl_overflow, 1ull);
+				h = 0;
+				emit = 0;
+				if(d.vp_over) d.vp_over[atomicAdd(d.vp_count + 1, 1)] = i;
 			}
 		}
 	}
-	d.nl_cnt[i] = n;
-	if(n > K) atomicAdd(&d.rs[r].nl_overflow, 1ull);
+	if(d.vpairs == nullptr) return;
+	int incl = h;
+#pragma unroll
+	for(int o = 1; o < 32; o <<= 1) {
+		const int v = __shfl_up_sync(0xffffffffu, incl, o);
+		if(lane >= o) incl += v;
+	}
+	const int total = __shfl_sync(0xffffffffu, incl, 31);
+	int base = 0;
+	if(lane == 31 && total) base = atomicAdd(d.vp_count, total);
+	base = __shfl_sync(0xffffffffu, base, 31);
+	if(!emit || h == 0) return;
+	int pos = base + incl - h; /* within capacity: at most nl_k pairs per particle */
+	const int *out = d.nl + (size_t) i * K;
+	for(int k = 0; k < n; k++) {
+		const int e = out[k];
+		if((int) ((unsigned) e >> 5) > i) d.vpairs[pos++] = make_int2(i, e);
+	}
 }
 
 /* ------------------------------------------------------------------------------------------------ */
@@ -3162,6 +3200,95 @@ __global__ void __launch_bounds__(32 * TILE_WARPS, PPI_VOL_MIN_BLOCKS) k_energy_
 	energy_flush_block(d, A);
 }
 
+/* decide64 and exact_pair out of line, for the flat volume pass: scalar and pointer arguments only, like
+ * exact_pair; called only for pairs inside the guard band, so the loop's registers stay low */
+__device__ __noinline__ int decide_exact_vol(const double *rec, const ppi_rparams *rp, const double *box, const ppi_grid *g, int ps, int qs) {
+	const float4 q0 = make_float4(1.f, 0.f, 0.f, 0.f);
+	const float3 d0 = make_float3(0.f, 0.f, 0.f);
+	int ex = decide64(rec, *rp, box, g->inv_L, ps, 0, q0, d0, qs, g->vol_mask, g->vol_f3, g->vol_box3);
+	if(ex == DEC64_EXACT) ex = exact_pair(rec, rp, box, ps, 0, q0, d0, qs, g->vol_mask, g->vol_f3, g->vol_box3, nullptr, nullptr, nullptr);
+	return ex;
+}
+
+/* one pair (lower sorted position i, candidate jq, cell offset code) of the candidate box */
+__device__ __forceinline__ void vol_flat_pair(const ppi_dev &d, const int i, const int jq, const int code, Acc &A) {
+	const int r = d.srep[i];
+	const ppi_grid &g = d.grid[r];
+	if(g.vol_dir < 0) return;
+	ppi_rstate *rs = d.rs + r;
+	if(*(volatile int *) &rs->vol_overlap) return; /* the candidate box is rejected already */
+	const float4 pa = d.spos[i], qa = d.spos[jq];
+	const float sx = g.vol_ff3[0], sy = g.vol_ff3[1], sz = g.vol_ff3[2];
+	const float ex = (qa.x * sx - pa.x * sx) + (float) (code % 3 - 1) * (g.wf[0] * sx);
+	const float ey = (qa.y * sy - pa.y * sy) + (float) ((code / 3) % 3 - 1) * (g.wf[1] * sy);
+	const float ez = (qa.z * sz - pa.z * sz) + (float) (code / 9 - 1) * (g.wf[2] * sz);
+	const float r2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+	const ppi_rparams &rp = d.rp[r];
+	const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
+	if(r != A.r) {
+		energy_flush_thread(d, A);
+		A.r = r;
+	}
+	A.pairs++;
+	if(r2 < 1.f - eps) {
+		atomicExch(&rs->vol_overlap, 1);
+		return;
+	}
+	if(!(r2 < rp.sqr_rcut_f + eps)) return;
+	const float4 p0 = d.sori[3 * (size_t) i], p1 = d.sori[3 * (size_t) i + 1], p2 = d.sori[3 * (size_t) i + 2];
+	const float4 q0 = d.sori[3 * (size_t) jq], q1 = d.sori[3 * (size_t) jq + 1], q2 = d.sori[3 * (size_t) jq + 2];
+	const float cp[9] = { p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w, p2.x };
+	const float cq[9] = { q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x };
+	int cl = classify(ex, ey, ez, cp, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, nullptr);
+	if(cl == CL_UNSURE) { /* guard band: the certified FP64 decision, the bit-identical one if needed */
+		A.fallbacks++;
+		const int x = decide_exact_vol(d.rec, &rp, rs->box, &g, __float_as_int(p2.w), __float_as_int(q2.w));
+		cl = x == -1 ? CL_OVER : (x == 1 ? CL_BOND : CL_NONE);
+	}
+	if(cl == CL_BOND) A.tries += 2; /* the box total counts every bond from both sides */
+	else if(cl == CL_OVER) atomicExch(&rs->vol_overlap, 1);
+}
+
+/* Energy of the candidate box of the sweep (NPT volume move or Lx move) over the epoch's flat pair list:
+ * one thread per pair (lower sorted position i, candidate jq), the positions and cell edges scaled axis by
+ * axis as in vol_geo; bonds counted from both sides (rs.vol_bonds = 2 x bonds), any overlap flags the
+ * replica. The list holds every pair that can interact in any candidate box of the epoch. */
+#define VP_B 128
+#ifndef PPI_VP_MIN_BLOCKS
+#define PPI_VP_MIN_BLOCKS 8 /* resident CTAs per SM of the flat volume pass (64 registers) */
+#endif
+__global__ void __launch_bounds__(VP_B, PPI_VP_MIN_BLOCKS) k_energy_vol_pairs(ppi_dev d) {
+	Acc A;
+	A.r = -1;
+	A.tries = A.acc = A.pairs = A.fallbacks = 0;
+	A.dbonds = 0;
+	const int np = d.vp_count[0] < d.vp_cap ? d.vp_count[0] : d.vp_cap;
+	const int nth = gridDim.x * blockDim.x, first = blockIdx.x * blockDim.x + threadIdx.x;
+	for(int p = first; p < np; p += nth) {
+		const int2 pr = d.vpairs[p];
+		vol_flat_pair(d, pr.x, (int) ((unsigned) pr.y >> 5), pr.y & 31, A);
+	}
+	/* particles whose list overflowed: their half shell in the 27 cells, one candidate at a time */
+	const int no = d.vp_count[1];
+	for(int k = first; k < no; k += nth) {
+		const int i = d.vp_over[k];
+		const int gc = __float_as_int(d.sori[3 * (size_t) i + 2].z);
+		const int r = d.cell_rep[gc];
+		const ppi_rparams &rp = d.rp[r];
+		const ppi_grid &g = d.grid[r];
+		if(g.vol_dir < 0) continue;
+		const int nx = g.n[0], local = gc - rp.cell_base;
+		const int cx = local % nx;
+		nl_rows(d, i, rp, g, cx, (local / nx) % g.n[1], local / (nx * g.n[1]), [&](int jq, int dy, int dz) {
+			if(jq <= i) return;
+			int dxc = __float_as_int(d.spos[jq].w) - cx;
+			dxc = dxc > 1 ? dxc - nx : (dxc < -1 ? dxc + nx : dxc);
+			vol_flat_pair(d, i, jq, (dxc + 1) + 3 * (dy + 1) + 9 * (dz + 1), A);
+		});
+	}
+	energy_flush_block(d, A);
+}
+
 __global__ void k_energy_reset(ppi_dev d) {
 	int r = blockIdx.x * blockDim.x + threadIdx.x;
 	if(r >= d.nrep) return;
@@ -3407,7 +3534,7 @@ static int resident_grid(F f, int *cache, int block = 128) {
 
 /* cached launch grids (one occupancy query each, made before any stream capture by ppi_prepare) */
 static int g_col_audit = 0, g_col_fast = 0, g_learn_audit = 0, g_learn_fast = 0, g_vol_grid = 0, g_col_tl = 0, g_col_tla = 0;
-static int g_a1 = 0, g_a4 = 0, g_f1 = 0, g_f4 = 0, g_f8 = 0, g_vol_list = 0;
+static int g_a1 = 0, g_a4 = 0, g_f1 = 0, g_f4 = 0, g_f8 = 0, g_vol_list = 0, g_vol_pairs = 0;
 
 extern "C" int ppi_resort(const ppi_dev *d, long long epoch, cudaStream_t s, long long *nl) {
 	float4 *tmp = (float4 *) d->tmp_rec; /* ntot float4 fit in the reorder scratch */
@@ -3451,6 +3578,7 @@ static void launch_round(K kern, int grid, const ppi_dev *d, long long round, co
 
 extern "C" int ppi_nlist(const ppi_dev *d, cudaStream_t s, long long *nl) {
 	if(d->ntot <= 0 || d->nl_k <= 0) return 0;
+	if(d->vp_count) cudaMemsetAsync(d->vp_count, 0, 2 * sizeof(int), s);
 	k_nlist<<<(d->ntot + NL_B - 1) / NL_B, NL_B, 0, s>>>(*d);
 	*nl += 1;
 	return (int) cudaGetLastError();
@@ -3474,6 +3602,8 @@ static void launch_energy(const ppi_dev *d, int mode, int use_nl, cudaStream_t s
 		else k_energy<MODE_FAST, 1><<<resident_grid(k_energy<MODE_FAST, 1>, &g_f1), 128, 0, s>>>(*d, mode);
 	}
 	else if(audit) k_energy<MODE_AUDIT, 4><<<resident_grid(k_energy<MODE_AUDIT, 4>, &g_a4), 128, 0, s>>>(*d, mode);
+	else if(mode == PPI_EN_VOLUME && use_nl && d->nl_k > 0 && d->vpairs)
+		k_energy_vol_pairs<<<resident_grid(k_energy_vol_pairs, &g_vol_pairs, VP_B), VP_B, 0, s>>>(*d);
 	else if(mode == PPI_EN_VOLUME && use_nl && d->nl_k > 0)
 		k_energy_vol<true><<<resident_grid(k_energy_vol<true>, &g_vol_list, 32 * TILE_WARPS), 32 * TILE_WARPS, 0, s>>>(*d);
 	else if(mode == PPI_EN_VOLUME) k_energy_vol<false><<<resident_grid(k_energy_vol<false>, &g_vol_grid, 32 * TILE_WARPS), 32 * TILE_WARPS, 0, s>>>(*d);
@@ -3565,6 +3695,7 @@ extern "C" int ppi_prepare(const ppi_dev *d) {
 	resident_grid(k_colour<MODE_FAST, true>, &g_col_tl, 32 * TILE_WARPS);
 	resident_grid(k_energy_vol<false>, &g_vol_grid, 32 * TILE_WARPS);
 	resident_grid(k_energy_vol<true>, &g_vol_list, 32 * TILE_WARPS);
+	resident_grid(k_energy_vol_pairs, &g_vol_pairs, VP_B);
 	resident_grid(k_energy<MODE_AUDIT, 1>, &g_a1);
 	resident_grid(k_energy<MODE_AUDIT, 4>, &g_a4);
 	resident_grid(k_energy<MODE_FAST, 1>, &g_f1);

@@ -1,7 +1,7 @@
 """Per-epoch neighbour lists: the colour pass over the lists makes the decisions of the 27-cell scan, so the
 trajectory is the same bit for bit (NVT, NPT with accepted volume moves, re-sort periods 1 to 16, dense and
-crystalline configurations, lists forced to overflow, learned moves mid-epoch),
-and it tests fewer pairs."""
+crystalline configurations, lists forced to overflow, learned moves mid-epoch), and at short periods it tests
+fewer pairs. The NPT cases also cover the volume pass over the epoch's flat pair list."""
 import numpy as np
 import pytest
 
@@ -54,7 +54,8 @@ def test_lists_reproduce_the_cell_scan(built, name, T, ens, P, resort):
     a = _run(name, False, **kw)
     b = _run(name, True, **kw)
     _same(a, b)
-    assert b["guard"]["pairs"] < a["guard"]["pairs"]
+    if resort <= 8:  # at longer periods the radius spans the 27 cells
+        assert b["guard"]["pairs"] < a["guard"]["pairs"]
     assert b["guard"]["nl_overflows"] == 0
     if name == "small":
         tries, acc = b["counters"]
