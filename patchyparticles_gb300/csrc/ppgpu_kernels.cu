@@ -555,48 +555,58 @@ __global__ void k_assign(ppi_dev d, float4 *tmp) {
 	}
 	const int gc = d.rp[r].cell_base + (c[2] * g.n[1] + c[1]) * g.n[0] + c[0];
 	d.cellof[s] = gc;
-	tmp[s] = make_float4(l[0], l[1], l[2], __int_as_float(gc));
-	atomicAdd(d.cell_count + gc, 1);
+	/* .w = the particle's rank among its cell's arrivals (the scatter's offset in the cell; k_cellfin
+	 * then orders each cell by particle id) */
+	tmp[s] = make_float4(l[0], l[1], l[2], __int_as_float(atomicAdd(d.cell_count + gc, 1)));
 }
 
 #define SCAN_B 1024
-__global__ void k_scan_local(const int *in, int *out, int *cursor, int *aux, int n) {
-	__shared__ int s[SCAN_B];
-	int i = blockIdx.x * SCAN_B + threadIdx.x;
-	int v = (i < n) ? in[i] : 0;
-	s[threadIdx.x] = v;
+/* inclusive scan of v over the CTA (SCAN_B threads): warp shuffles, then the warps' totals */
+__device__ __forceinline__ int block_scan_incl(int v, int *ws) {
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+	for(int o = 1; o < 32; o <<= 1) {
+		const int y = __shfl_up_sync(0xffffffffu, v, o);
+		if(lane >= o) v += y;
+	}
+	if(lane == 31) ws[warp] = v;
 	__syncthreads();
-	for(int off = 1; off < SCAN_B; off <<= 1) {
-		int t = (threadIdx.x >= off) ? s[threadIdx.x - off] : 0;
-		__syncthreads();
-		s[threadIdx.x] += t;
-		__syncthreads();
+	if(warp == 0) {
+		int t = ws[lane];
+#pragma unroll
+		for(int o = 1; o < 32; o <<= 1) {
+			const int y = __shfl_up_sync(0xffffffffu, t, o);
+			if(lane >= o) t += y;
+		}
+		ws[lane] = t;
 	}
-	if(i < n) {
-		out[i] = s[threadIdx.x] - v;
-		cursor[i] = 0;
-	}
-	if(threadIdx.x == SCAN_B - 1) aux[blockIdx.x] = s[SCAN_B - 1];
+	__syncthreads();
+	if(warp > 0) v += ws[warp - 1];
+	return v;
 }
 
-__global__ void k_scan_top(int *aux, int nblocks, int *total_out) {
-	__shared__ int s[SCAN_B];
+__global__ void __launch_bounds__(SCAN_B) k_scan_local(const int *in, int *out, int *cursor, int *aux, int n) {
+	__shared__ int ws[SCAN_B / 32];
+	const int i = blockIdx.x * SCAN_B + threadIdx.x;
+	const int v = (i < n) ? in[i] : 0;
+	const int x = block_scan_incl(v, ws);
+	if(i < n) {
+		out[i] = x - v;
+		cursor[i] = 0;
+	}
+	if(threadIdx.x == SCAN_B - 1) aux[blockIdx.x] = x;
+}
+
+__global__ void __launch_bounds__(SCAN_B) k_scan_top(int *aux, int nblocks, int *total_out) {
+	__shared__ int ws[SCAN_B / 32];
 	int carry = 0;
 	for(int base = 0; base < nblocks; base += SCAN_B) {
-		int i = base + threadIdx.x;
-		int v = (i < nblocks) ? aux[i] : 0;
-		s[threadIdx.x] = v;
+		const int i = base + threadIdx.x;
+		const int v = (i < nblocks) ? aux[i] : 0;
+		const int x = block_scan_incl(v, ws);
+		if(i < nblocks) aux[i] = carry + x - v;
+		carry += ws[SCAN_B / 32 - 1]; /* the chunk's total */
 		__syncthreads();
-		for(int off = 1; off < SCAN_B; off <<= 1) {
-			int t = (threadIdx.x >= off) ? s[threadIdx.x - off] : 0;
-			__syncthreads();
-			s[threadIdx.x] += t;
-			__syncthreads();
-		}
-		if(i < nblocks) aux[i] = carry + s[threadIdx.x] - v;
-		int tot = s[SCAN_B - 1];
-		__syncthreads();
-		carry += tot;
 	}
 	if(threadIdx.x == 0) *total_out = carry;
 }
@@ -612,9 +622,9 @@ __global__ void k_scatter(ppi_dev d, const float4 *tmp) {
 	int s = blockIdx.x * blockDim.x + threadIdx.x;
 	if(s >= d.ntot) return;
 	int gc = d.cellof[s];
-	int pos = d.cell_start[gc] + atomicAdd(d.cell_cursor + gc, 1);
-	const double *rec = d.rec + (size_t) s * PPI_REC;
 	float4 a = tmp[s];
+	int pos = d.cell_start[gc] + __float_as_int(a.w);
+	const double *rec = d.rec + (size_t) s * PPI_REC;
 	{ /* .w = the cell's x index (neighbour offsets in the colour pass) */
 		const int r = d.rep[s];
 		a.w = __int_as_float((gc - d.rp[r].cell_base) % d.grid[r].n[0]);
@@ -1514,11 +1524,10 @@ __device__ __forceinline__ void nl_rows(const ppi_dev &d, int i, const ppi_rpara
 		const int dy = row % 3 - 1, dz = row / 3 - 1;
 		const int *cs = d.cell_start + rp.cell_base + (wrapi(cz + dz, nz) * ny + wrapi(cy + dy, ny)) * nx;
 		const int s0 = cs[xa0], e0 = cs[xa1], s1 = inner ? 0 : cs[0], e1 = inner ? 0 : cs[xb1];
-		const int len0 = e0 - s0, tot = len0 + (e1 - s1);
-		for(int t = 0; t < tot; t++) {
-			const int jq = t < len0 ? s0 + t : s1 + (t - len0);
+		for(int jq = s0; jq < e0; jq++)
 			if(jq != i) visit(jq, dy, dz);
-		}
+		for(int jq = s1; jq < e1; jq++)
+			if(jq != i) visit(jq, dy, dz);
 	}
 }
 
