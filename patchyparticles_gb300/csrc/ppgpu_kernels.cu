@@ -2222,6 +2222,7 @@ __global__ void __launch_bounds__(32) k_colour_learned(ppi_dev d, long long roun
 	A.tries = A.acc = A.pairs = A.fallbacks = 0;
 	A.dbonds = 0;
 	unsigned ctr[PPI_MIX] = { 0u, 0u, 0u, 0u }, cac[PPI_MIX] = { 0u, 0u, 0u, 0u };
+	bool waited = false;
 #pragma unroll 1
 	for(int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
 		const int idx = tile * 32 + threadIdx.x;
@@ -2235,22 +2236,32 @@ __global__ void __launch_bounds__(32) k_colour_learned(ppi_dev d, long long roun
 #pragma unroll
 		for(int e = 0; e < MLP_IN; e++) f[e] = 0.f;
 		if(live) {
+			/* what reads only the mover, the epoch's cell ranges and the network: before the wait on the
+			 * previous colour (programmatic dependent launch, see grid_dep_wait) */
 			const int4 ent = list[idx];
 			const ppi_rparams &rp = d.rp[ent.w];
 			r1 = rng(rp, round, ent.w, TAG_LEARN, (uint32_t) (ent.x - rp.cell_base), 0u);
 			learn_mover(d, ent, r1.x, P, img0, cx, cy, cz);
+			total = cands_build(d, rp, d.grid[P.r], cx, cy, cz, C);
+			/* the mover's FP64 record, in flight while the features are formed */
+#pragma unroll
+			for(int c = 0; c < PPI_REC / 2; c++) cp_async16(&K.rec[c][threadIdx.x], d.rec + (size_t) P.pslot * PPI_REC + 2 * c);
+		}
+		if(!waited) {
+			grid_dep_wait();
+			grid_dep_release();
+			waited = true;
+		}
+		if(live) {
+			const ppi_rparams &rp = d.rp[P.r];
 			if(P.r != A.r) {
 				flush_thread(d, A);
 				A.r = P.r;
 			}
 			A.tries++;
 			const ppi_grid &g = d.grid[P.r];
-			total = cands_build(d, rp, g, cx, cy, cz, C);
 			const BoxF B = box_f(d.rs[P.r].box);
 			NbSel sel;
-			/* the mover's FP64 record, in flight while the features are formed */
-#pragma unroll
-			for(int c = 0; c < PPI_REC / 2; c++) cp_async16(&K.rec[c][threadIdx.x], d.rec + (size_t) P.pslot * PPI_REC + 2 * c);
 			int nc = 0;
 			cached = scan_features_cached(d, K, rp, g, C, total, cx, P.i, P.po, img0, B, sel, &nc);
 			site_features_cached(d, K, nc, rp, img0, sel, B, f);
@@ -3567,14 +3578,15 @@ static int lanes_of(const ppi_dev *d) { return d->lanes == 8 ? 8 : PPI_DEFAULT_L
 /* the 8 colour launches of a round; colours 1..7 with programmatic stream serialisation (their proposals
  * overlap the previous colour's tail, see grid_dep_wait) */
 template <typename K>
-static void launch_round(K kern, int grid, const ppi_dev *d, long long round, const int *colours, cudaStream_t s) {
+static void launch_round(K kern, int grid, int block, size_t smem, const ppi_dev *d, long long round, const int *colours, cudaStream_t s) {
 	static int pdl = -1;
 	if(pdl < 0) pdl = getenv("PPGPU_NO_PDL") ? 0 : 1;
 	for(int ci = 0; ci < 8; ci++) {
 		cudaLaunchConfig_t cfg;
 		memset(&cfg, 0, sizeof(cfg));
 		cfg.gridDim = dim3(grid);
-		cfg.blockDim = dim3(32 * TILE_WARPS);
+		cfg.blockDim = dim3(block);
+		cfg.dynamicSmemBytes = smem;
 		cfg.stream = s;
 		cudaLaunchAttribute at[1];
 		at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -3595,10 +3607,10 @@ extern "C" int ppi_nlist(const ppi_dev *d, cudaStream_t s, long long *nl) {
 
 extern "C" int ppi_round(const ppi_dev *d, long long round, const int *colours, int audit, int use_nl, cudaStream_t s, long long *nl) {
 	const int aud = audit || d->audit_any;
-	if(use_nl && d->nl_k > 0 && aud) launch_round(k_colour<MODE_AUDIT, true>, resident_grid(k_colour<MODE_AUDIT, true>, &g_col_tla, 32 * TILE_WARPS), d, round, colours, s);
-	else if(use_nl && d->nl_k > 0) launch_round(k_colour<MODE_FAST, true>, resident_grid(k_colour<MODE_FAST, true>, &g_col_tl, 32 * TILE_WARPS), d, round, colours, s);
-	else if(aud) launch_round(k_colour<MODE_AUDIT, false>, resident_grid(k_colour<MODE_AUDIT, false>, &g_col_audit, 32 * TILE_WARPS), d, round, colours, s);
-	else launch_round(k_colour<MODE_FAST, false>, resident_grid(k_colour<MODE_FAST, false>, &g_col_fast, 32 * TILE_WARPS), d, round, colours, s);
+	if(use_nl && d->nl_k > 0 && aud) launch_round(k_colour<MODE_AUDIT, true>, resident_grid(k_colour<MODE_AUDIT, true>, &g_col_tla, 32 * TILE_WARPS), 32 * TILE_WARPS, 0, d, round, colours, s);
+	else if(use_nl && d->nl_k > 0) launch_round(k_colour<MODE_FAST, true>, resident_grid(k_colour<MODE_FAST, true>, &g_col_tl, 32 * TILE_WARPS), 32 * TILE_WARPS, 0, d, round, colours, s);
+	else if(aud) launch_round(k_colour<MODE_AUDIT, false>, resident_grid(k_colour<MODE_AUDIT, false>, &g_col_audit, 32 * TILE_WARPS), 32 * TILE_WARPS, 0, d, round, colours, s);
+	else launch_round(k_colour<MODE_FAST, false>, resident_grid(k_colour<MODE_FAST, false>, &g_col_fast, 32 * TILE_WARPS), 32 * TILE_WARPS, 0, d, round, colours, s);
 	*nl += 8;
 	return (int) cudaGetLastError();
 }
@@ -3718,12 +3730,12 @@ extern "C" int ppi_round_learned(const ppi_dev *d, long long round, const int *c
 	if(audit || d->audit_any) {
 		const int grid = learned_grid(k_colour_learned<MODE_AUDIT>, &g_learn_audit);
 		if(grid < 0) return (int) cudaGetLastError();
-		for(int ci = 0; ci < 8; ci++) k_colour_learned<MODE_AUDIT><<<grid, 32, LEARN_SMEM, s>>>(*d, round, colours[ci]);
+		launch_round(k_colour_learned<MODE_AUDIT>, grid, 32, LEARN_SMEM, d, round, colours, s);
 	}
 	else {
 		const int grid = learned_grid(k_colour_learned<MODE_FAST>, &g_learn_fast);
 		if(grid < 0) return (int) cudaGetLastError();
-		for(int ci = 0; ci < 8; ci++) k_colour_learned<MODE_FAST><<<grid, 32, LEARN_SMEM, s>>>(*d, round, colours[ci]);
+		launch_round(k_colour_learned<MODE_FAST>, grid, 32, LEARN_SMEM, d, round, colours, s);
 	}
 	*nl += 8;
 	return (int) cudaGetLastError();
