@@ -263,7 +263,11 @@ static void free_device(pp_engine *e) {
 	if(e->d.vp_count) cudaFree(e->d.vp_count);
 	if(e->d.srep) cudaFree(e->d.srep);
 	if(e->d.vp_over) cudaFree(e->d.vp_over);
-	e->d.nl = e->d.nl_cnt = e->d.vp_count = e->d.srep = e->d.vp_over = NULL;
+	if(e->d.vunsure) cudaFree(e->d.vunsure);
+	if(e->d.vun_count) cudaFree(e->d.vun_count);
+	e->d.nl = e->d.nl_cnt = e->d.vp_count = e->d.srep = e->d.vp_over = e->d.vun_count = NULL;
+	e->d.vunsure = NULL;
+	e->d.vun_cap = 0;
 	e->d.vpairs = NULL;
 	e->d.vp_cap = 0;
 	e->d.nl_k = 0;
@@ -446,7 +450,7 @@ static int read_states(pp_engine *e) {
 	if(lerr) return set_err(e, PP_ERR_CUDA, "a tensor-core wait of the learned proposal timed out");
 	for(int r = 0; r < e->nrep; r++)
 		if(e->h_rs[r].error == PPI_E_LISTS)
-			return set_err(e, PP_ERR_CAPACITY, "replica %d: the volume pass's pair list ran out of capacity (neighbour lists overflowing)", r);
+			return set_err(e, PP_ERR_CAPACITY, "replica %d: more guard-band pairs in one volume pass than its buffer holds", r);
 		else if(e->h_rs[r].error == PPI_E_EXACT)
 			return set_err(e, PP_ERR_STATE, "replica %d: more pairs within 1e-12 of a bonding threshold than one warp keeps for the exact test", r);
 		else if(e->h_rs[r].error)
@@ -548,7 +552,11 @@ static int setup_nlists(pp_engine *e) {
 	if(e->d.vp_count) cudaFree(e->d.vp_count);
 	if(e->d.srep) cudaFree(e->d.srep);
 	if(e->d.vp_over) cudaFree(e->d.vp_over);
-	e->d.nl = e->d.nl_cnt = e->d.vp_count = e->d.srep = e->d.vp_over = NULL;
+	if(e->d.vunsure) cudaFree(e->d.vunsure);
+	if(e->d.vun_count) cudaFree(e->d.vun_count);
+	e->d.nl = e->d.nl_cnt = e->d.vp_count = e->d.srep = e->d.vp_over = e->d.vun_count = NULL;
+	e->d.vunsure = NULL;
+	e->d.vun_cap = 0;
 	e->d.vpairs = NULL;
 	e->d.vp_cap = 0;
 	e->d.nl_k = 0;
@@ -566,6 +574,10 @@ static int setup_nlists(pp_engine *e) {
 		CU(cudaMalloc((void **) &e->d.vp_over, sizeof(int) * n1));
 		CU(cudaMemsetAsync(e->d.vp_count, 0, 2 * sizeof(int), e->stream));
 		e->d.vp_cap = (int) ((size_t) K * n1);
+		/* guard-band pairs of one volume pass (a fraction ~eps of the close pairs; FP64 replicas have no lists) */
+		e->d.vun_cap = (int) (n1 + 65536);
+		CU(cudaMalloc((void **) &e->d.vunsure, sizeof(int2) * (size_t) e->d.vun_cap));
+		CU(cudaMalloc((void **) &e->d.vun_count, sizeof(int)));
 	}
 	e->d.nl_k = K;
 	return PP_OK;

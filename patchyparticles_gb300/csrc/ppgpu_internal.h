@@ -40,7 +40,7 @@ extern "C" {
 /* error codes written by kernels into ppi_rstate.error */
 #define PPI_E_GRID 2  /* the box became too small for an even cell grid of edge >= r_cut */
 #define PPI_E_EXACT 3 /* more undecidable pairs in one warp's share of a volume pass than it keeps */
-#define PPI_E_LISTS 4 /* the flat pair list of the volume pass ran out of capacity */
+#define PPI_E_LISTS 4 /* more guard-band pairs in one volume pass than its buffer holds */
 
 typedef struct ppi_rparams {
 	int N;           /* particles of this replica */
@@ -184,7 +184,9 @@ typedef struct ppi_dev {
 	int *vp_over;      /* sorted positions whose list overflowed: their half shell is scanned in the cells */
 	int *srep;         /* replica of each sorted position */
 	int vp_cap;
-	int pad5;
+	int vun_cap;
+	int2 *vunsure;     /* guard-band pairs of the current volume pass, decided in FP64 after it */
+	int *vun_count;
 } ppi_dev;
 
 #define PPI_MAX_PARTNERS 24

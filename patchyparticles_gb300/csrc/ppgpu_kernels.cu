@@ -3230,49 +3230,67 @@ __device__ __noinline__ int decide_exact_vol(const double *rec, const ppi_rparam
 	return ex;
 }
 
-/* one pair (lower sorted position i, candidate jq, cell offset code) of the candidate box */
-__device__ __forceinline__ void vol_flat_pair(const ppi_dev &d, const int i, const int jq, const int code, Acc &A) {
-	const int r = d.srep[i];
+/* the candidate box of one replica as the flat volume pass uses it (kept in registers across pairs) */
+struct VolRep {
+	int r, live;       /* replica; live: it has a candidate box this sweep and no overlap was found yet */
+	float sx, sy, sz;  /* scale factors per axis */
+	float wx, wy, wz;  /* scaled cell edges */
+	float ovl, rc2e;   /* 1 - eps, r_cut^2 + eps */
+	float eps;
+};
+
+__device__ __forceinline__ void vol_rep_load(const ppi_dev &d, int r, VolRep &V) {
 	const ppi_grid &g = d.grid[r];
-	if(g.vol_dir < 0) return;
-	ppi_rstate *rs = d.rs + r;
-	if(*(volatile int *) &rs->vol_overlap) return; /* the candidate box is rejected already */
-	const float4 pa = d.spos[i], qa = d.spos[jq];
-	const float sx = g.vol_ff3[0], sy = g.vol_ff3[1], sz = g.vol_ff3[2];
-	const float ex = (qa.x * sx - pa.x * sx) + (float) (code % 3 - 1) * (g.wf[0] * sx);
-	const float ey = (qa.y * sy - pa.y * sy) + (float) ((code / 3) % 3 - 1) * (g.wf[1] * sy);
-	const float ez = (qa.z * sz - pa.z * sz) + (float) (code / 9 - 1) * (g.wf[2] * sz);
-	const float r2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
 	const ppi_rparams &rp = d.rp[r];
-	const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
-	if(r != A.r) {
-		energy_flush_thread(d, A);
-		A.r = r;
-	}
+	V.r = r;
+	V.live = g.vol_dir >= 0 && !*(volatile int *) &d.rs[r].vol_overlap;
+	V.sx = g.vol_ff3[0];
+	V.sy = g.vol_ff3[1];
+	V.sz = g.vol_ff3[2];
+	V.wx = g.wf[0] * V.sx;
+	V.wy = g.wf[1] * V.sy;
+	V.wz = g.wf[2] * V.sz;
+	V.eps = rp.precision == 1 ? 1e30f : rp.eps_f;
+	V.ovl = 1.f - V.eps;
+	V.rc2e = rp.sqr_rcut_f + V.eps;
+}
+
+/* one pair (lower sorted position i, candidate jq, cell offset code) of the candidate box, the positions
+ * already loaded; the geometry is vol_geo's */
+__device__ __forceinline__ void vol_flat_pair(const ppi_dev &d, const VolRep &V, const int i, const int jq, const int code, const float4 pa, const float4 qa,
+		Acc &A) {
+	const float ex = (qa.x * V.sx - pa.x * V.sx) + (float) (code % 3 - 1) * V.wx;
+	const float ey = (qa.y * V.sy - pa.y * V.sy) + (float) ((code / 3) % 3 - 1) * V.wy;
+	const float ez = (qa.z * V.sz - pa.z * V.sz) + (float) (code / 9 - 1) * V.wz;
+	const float r2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+	ppi_rstate *rs = d.rs + V.r;
 	A.pairs++;
-	if(r2 < 1.f - eps) {
+	if(r2 < V.ovl) {
 		atomicExch(&rs->vol_overlap, 1);
 		return;
 	}
-	if(!(r2 < rp.sqr_rcut_f + eps)) return;
+	if(!(r2 < V.rc2e)) return;
+	const ppi_rparams &rp = d.rp[V.r];
 	const float4 p0 = d.sori[3 * (size_t) i], p1 = d.sori[3 * (size_t) i + 1], p2 = d.sori[3 * (size_t) i + 2];
 	const float4 q0 = d.sori[3 * (size_t) jq], q1 = d.sori[3 * (size_t) jq + 1], q2 = d.sori[3 * (size_t) jq + 2];
 	const float cp[9] = { p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w, p2.x };
 	const float cq[9] = { q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x };
-	int cl = classify(ex, ey, ez, cp, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, nullptr);
-	if(cl == CL_UNSURE) { /* guard band: the certified FP64 decision, the bit-identical one if needed */
-		A.fallbacks++;
-		const int x = decide_exact_vol(d.rec, &rp, rs->box, &g, __float_as_int(p2.w), __float_as_int(q2.w));
-		cl = x == -1 ? CL_OVER : (x == 1 ? CL_BOND : CL_NONE);
+	const int cl = classify(ex, ey, ez, cp, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, V.eps, nullptr);
+	if(cl == CL_UNSURE) { /* guard band: queued for the FP64 decision after the pass (k_vol_unsure) */
+		const int k = atomicAdd(d.vun_count, 1);
+		if(k < d.vun_cap) d.vunsure[k] = make_int2(i, jq);
+		else rs->error = PPI_E_LISTS;
 	}
-	if(cl == CL_BOND) A.tries += 2; /* the box total counts every bond from both sides */
+	else if(cl == CL_BOND) A.tries += 2; /* the box total counts every bond from both sides */
 	else if(cl == CL_OVER) atomicExch(&rs->vol_overlap, 1);
 }
 
 /* Energy of the candidate box of the sweep (NPT volume move or Lx move) over the epoch's flat pair list:
  * one thread per pair (lower sorted position i, candidate jq), the positions and cell edges scaled axis by
  * axis as in vol_geo; bonds counted from both sides (rs.vol_bonds = 2 x bonds), any overlap flags the
- * replica. The list holds every pair that can interact in any candidate box of the epoch. */
+ * replica. The list holds every pair that can interact in any candidate box of the epoch. A thread loads
+ * its next pair while it evaluates the current one, and keeps its replica's candidate box in registers
+ * (the overlap flag is re-read every few steps: a rejected box only saves work). */
 #define VP_B 128
 #ifndef PPI_VP_MIN_BLOCKS
 #define PPI_VP_MIN_BLOCKS 8 /* resident CTAs per SM of the flat volume pass (64 registers) */
@@ -3282,11 +3300,43 @@ __global__ void __launch_bounds__(VP_B, PPI_VP_MIN_BLOCKS) k_energy_vol_pairs(pp
 	A.r = -1;
 	A.tries = A.acc = A.pairs = A.fallbacks = 0;
 	A.dbonds = 0;
+	VolRep V;
+	V.r = -1;
+	V.live = 0;
 	const int np = d.vp_count[0] < d.vp_cap ? d.vp_count[0] : d.vp_cap;
 	const int nth = gridDim.x * blockDim.x, first = blockIdx.x * blockDim.x + threadIdx.x;
-	for(int p = first; p < np; p += nth) {
-		const int2 pr = d.vpairs[p];
-		vol_flat_pair(d, pr.x, (int) ((unsigned) pr.y >> 5), pr.y & 31, A);
+	/* software pipeline: the next pair's loads are in flight while the current pair is evaluated */
+	int p = first, step = 0;
+	int2 c = p < np ? d.vpairs[p] : make_int2(-1, 0);
+	int rc = 0;
+	float4 pc = make_float4(0.f, 0.f, 0.f, 0.f), qc = pc;
+	if(c.x >= 0) {
+		rc = d.srep[c.x];
+		pc = d.spos[c.x];
+		qc = d.spos[(unsigned) c.y >> 5];
+	}
+	while(c.x >= 0) {
+		const int pn = p + nth;
+		int2 n = pn < np ? d.vpairs[pn] : make_int2(-1, 0);
+		int rn = 0;
+		float4 pnx = pc, qnx = qc;
+		if(n.x >= 0) {
+			rn = d.srep[n.x];
+			pnx = d.spos[n.x];
+			qnx = d.spos[(unsigned) n.y >> 5];
+		}
+		if(rc != V.r || (step & 15) == 0) vol_rep_load(d, rc, V);
+		if(rc != A.r) {
+			energy_flush_thread(d, A);
+			A.r = rc;
+		}
+		if(V.live) vol_flat_pair(d, V, c.x, (int) ((unsigned) c.y >> 5), c.y & 31, pc, qc, A);
+		c = n;
+		rc = rn;
+		pc = pnx;
+		qc = qnx;
+		p = pn;
+		step++;
 	}
 	/* particles whose list overflowed: their half shell in the 27 cells, one candidate at a time */
 	const int no = d.vp_count[1];
@@ -3296,17 +3346,40 @@ __global__ void __launch_bounds__(VP_B, PPI_VP_MIN_BLOCKS) k_energy_vol_pairs(pp
 		const int r = d.cell_rep[gc];
 		const ppi_rparams &rp = d.rp[r];
 		const ppi_grid &g = d.grid[r];
-		if(g.vol_dir < 0) continue;
+		vol_rep_load(d, r, V);
+		if(!V.live) continue;
+		if(r != A.r) {
+			energy_flush_thread(d, A);
+			A.r = r;
+		}
 		const int nx = g.n[0], local = gc - rp.cell_base;
 		const int cx = local % nx;
+		const float4 pa = d.spos[i];
 		nl_rows(d, i, rp, g, cx, (local / nx) % g.n[1], local / (nx * g.n[1]), [&](int jq, int dy, int dz) {
 			if(jq <= i) return;
-			int dxc = __float_as_int(d.spos[jq].w) - cx;
+			const float4 qa = d.spos[jq];
+			int dxc = __float_as_int(qa.w) - cx;
 			dxc = dxc > 1 ? dxc - nx : (dxc < -1 ? dxc + nx : dxc);
-			vol_flat_pair(d, i, jq, (dxc + 1) + 3 * (dy + 1) + 9 * (dz + 1), A);
+			vol_flat_pair(d, V, i, jq, (dxc + 1) + 3 * (dy + 1) + 9 * (dz + 1), pa, qa, A);
 		});
 	}
 	energy_flush_block(d, A);
+}
+
+/* the guard-band pairs of the flat volume pass: the certified FP64 decision, the bit-identical exact_pair
+ * where it cannot decide */
+__global__ void k_vol_unsure(ppi_dev d) {
+	const int n = d.vun_count[0] < d.vun_cap ? d.vun_count[0] : d.vun_cap;
+	for(int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+		const int2 pr = d.vunsure[k];
+		const int r = d.srep[pr.x];
+		ppi_rstate *rs = d.rs + r;
+		const int x = decide_exact_vol(d.rec, d.rp + r, rs->box, d.grid + r, __float_as_int(d.sori[3 * (size_t) pr.x + 2].w),
+				__float_as_int(d.sori[3 * (size_t) pr.y + 2].w));
+		atomicAdd(&rs->fallbacks, 1ull);
+		if(x == 1) atomicAdd((unsigned long long *) &rs->vol_bonds, 2ull);
+		else if(x == -1) atomicExch(&rs->vol_overlap, 1);
+	}
 }
 
 __global__ void k_energy_reset(ppi_dev d) {
@@ -3623,8 +3696,12 @@ static void launch_energy(const ppi_dev *d, int mode, int use_nl, cudaStream_t s
 		else k_energy<MODE_FAST, 1><<<resident_grid(k_energy<MODE_FAST, 1>, &g_f1), 128, 0, s>>>(*d, mode);
 	}
 	else if(audit) k_energy<MODE_AUDIT, 4><<<resident_grid(k_energy<MODE_AUDIT, 4>, &g_a4), 128, 0, s>>>(*d, mode);
-	else if(mode == PPI_EN_VOLUME && use_nl && d->nl_k > 0 && d->vpairs)
+	else if(mode == PPI_EN_VOLUME && use_nl && d->nl_k > 0 && d->vpairs) {
+		cudaMemsetAsync(d->vun_count, 0, sizeof(int), s);
 		k_energy_vol_pairs<<<resident_grid(k_energy_vol_pairs, &g_vol_pairs, VP_B), VP_B, 0, s>>>(*d);
+		k_vol_unsure<<<64, 128, 0, s>>>(*d);
+		*nl += 1;
+	}
 	else if(mode == PPI_EN_VOLUME && use_nl && d->nl_k > 0)
 		k_energy_vol<true><<<resident_grid(k_energy_vol<true>, &g_vol_list, 32 * TILE_WARPS), 32 * TILE_WARPS, 0, s>>>(*d);
 	else if(mode == PPI_EN_VOLUME) k_energy_vol<false><<<resident_grid(k_energy_vol<false>, &g_vol_grid, 32 * TILE_WARPS), 32 * TILE_WARPS, 0, s>>>(*d);

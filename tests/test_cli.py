@@ -1,0 +1,83 @@
+"""The ppgpu command-line driver: a reference input file run on the GPU engine writes the reference's output
+files. The checkerboard trajectory differs from the reference's sequential one, so the step-0 lines (the
+uploaded configuration's exact energy, density and box) must equal the reference's own outputs
+(tests/golden/traj_*), and every other line must have the reference's format and cadence. Input errors are
+checked on the CPU (they stop the driver before it touches a GPU)."""
+import gzip
+import os
+import shutil
+import subprocess
+import tempfile
+
+import pytest
+
+from patchyparticles_gb300 import build
+from tests import helpers
+
+CLI = build.CLI
+
+
+def _prepare(name, edit=None):
+    src = helpers.golden_path("traj_" + name)
+    work = tempfile.mkdtemp(prefix="ppcli_")
+    os.makedirs(os.path.join(work, "confs"))
+    text = open(os.path.join(src, "input")).read()
+    if edit:
+        text = edit(text)
+    open(os.path.join(work, "input"), "w").write(text)
+    conf = [l.split("=")[1].strip() for l in text.splitlines() if l.startswith("Initial_conditions_file")][0]
+    helpers.unpack_golden(conf, work)
+    return src, work
+
+
+def _lines(path):
+    return helpers.normalise_nan(open(path).read()).splitlines()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,files", [("small_nvt", ("energy.dat", "acceptance.dat")),
+                                        ("small_npt", ("energy.dat", "acceptance.dat", "density.dat")),
+                                        ("small_lx", ("energy.dat", "acceptance.dat", "boxshape.dat"))])
+def test_driver_writes_the_reference_outputs(built, name, files):
+    src, work = _prepare(name)
+    p = subprocess.run([CLI, "input"], cwd=work, capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr
+    ref_out = open(os.path.join(src, "stdout.txt")).read().splitlines()
+    out = p.stdout.splitlines()
+    assert len(out) == len(ref_out) and out[0] == ref_out[0]
+    assert out[-1].split()[0] == ref_out[-1].split()[0]  # the final step
+    for fn in files:
+        mine, ref = _lines(os.path.join(work, fn)), _lines(os.path.join(src, fn))
+        assert len(mine) == len(ref), fn
+        assert mine[0] == ref[0], fn  # step 0: the uploaded configuration
+        for a, b in zip(mine, ref):
+            assert a.split()[0] == b.split()[0] and len(a.split()) == len(b.split()), fn
+    last = open(os.path.join(work, "last.rrr")).read().splitlines()
+    ref_last = gzip.open(os.path.join(src, "last.rrr.gz"), "rt").read().splitlines()
+    assert len(last) == len(ref_last) and last[0].split()[:2] == ref_last[0].split()[:2]
+    saves = sorted(os.listdir(os.path.join(work, "confs")))
+    assert saves and all(f.startswith("conf_") and f.endswith(".rrr") for f in saves)
+    shutil.rmtree(work)
+
+
+@pytest.mark.gpu
+def test_driver_refuses_an_overlapping_configuration(built):
+    src, work = _prepare("small_nvt", lambda t: t.replace("generator_300_0.3_4242.rrr", "adversarial.rrr"))
+    helpers.unpack_golden("adversarial.rrr", work)
+    p = subprocess.run([CLI, "input"], cwd=work, capture_output=True, text=True, timeout=300)
+    assert p.returncode == 1 and "Initial configuration contains an overlap, aborting" in p.stderr
+    shutil.rmtree(work)
+
+
+def test_driver_reports_a_missing_mandatory_key(built):
+    src, work = _prepare("small_nvt", lambda t: "\n".join(l for l in t.splitlines() if not l.startswith("Temperature")))
+    p = subprocess.run([CLI, "input"], cwd=work, capture_output=True, text=True, timeout=60)
+    assert p.returncode == 255 and "Mandatory key 'Temperature' not found" in p.stderr
+    shutil.rmtree(work)
+
+
+def test_driver_rejects_other_dynamics(built):
+    src, work = _prepare("small_nvt", lambda t: t.replace("Dynamics = 0", "Dynamics = 1"))
+    p = subprocess.run([CLI, "input"], cwd=work, capture_output=True, text=True, timeout=60)
+    assert p.returncode == 1 and "Dynamics = 1" in p.stderr
+    shutil.rmtree(work)
