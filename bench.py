@@ -290,7 +290,8 @@ def run_gpu(args, wl, ws, rank, local, dist):
     pp.select_device(local)
     r, R, box = make_config(wl, seed_offset=rank)
     prm = pp.default_params(ensemble=wl["ensemble"], temperature=wl["T"], pressure=wl["P"], disp_max=wl["disp"],
-                            theta_max=wl["theta"], rescale_factor_max=wl["rescale"], seed=wl["seed"] + rank)
+                            theta_max=wl["theta"], rescale_factor_max=wl["rescale"], seed=wl["seed"] + rank,
+                            precision=pp.PREC_FP64 if args.precision == "fp64" else pp.PREC_FP32_GUARD)
     e = pp.Engine(prm)
     e.upload(r, R, box)
     spsw = args.sweeps_per_step
@@ -374,8 +375,9 @@ def run_gpu(args, wl, ws, rank, local, dist):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * t_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32+f64", "data": "synthetic (seeded random insertion, uniform orientations)",
-        "config": {"workload": wl["name"], "N": wl["N"], "sweeps_per_step": spsw, "proposal": "plain",
+        "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic (seeded random insertion, uniform orientations)",
+        "config": {"workload": wl["name"] if args.precision != "fp64" else wl["name"].replace("FP32+guard", "FP64 pair tests"), "N": wl["N"],
+                   "precision": args.precision, "sweeps_per_step": spsw, "proposal": "plain",
                    "l2": "inputs larger than L2 (FP64 state %.0f MB + FP32 mirror %.0f MB per GPU)" % (wl["N"] * 128 / 1e6, wl["N"] * 64 / 1e6),
                    "parallelism": "replicas" if ws > 1 else "single GPU", "launch": "CUDA graph per re-sort period",
                    "schedule": tune if tune else "defaults (resort_every 4, reorder_every 16, cell_scale 1.0)"},
@@ -504,6 +506,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="c5", choices=sorted(WORKLOADS) + ["c3"])
+    ap.add_argument("--precision", default="fp32-guard", choices=["fp32-guard", "fp64"],
+                    help="pair tests in FP32 with the FP64 guard band (default) or every pair in FP64")
     ap.add_argument("--sweeps-per-step", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--e2e-sweeps", type=int, default=1000,
