@@ -3296,6 +3296,8 @@ __device__ __forceinline__ void vol_flat_pair(const ppi_dev &d, const VolRep &V,
 #define PPI_VP_MIN_BLOCKS 8 /* resident CTAs per SM of the flat volume pass (64 registers) */
 #endif
 __global__ void __launch_bounds__(VP_B, PPI_VP_MIN_BLOCKS) k_energy_vol_pairs(ppi_dev d) {
+	grid_dep_wait();
+	grid_dep_release();
 	Acc A;
 	A.r = -1;
 	A.tries = A.acc = A.pairs = A.fallbacks = 0;
@@ -3369,6 +3371,8 @@ __global__ void __launch_bounds__(VP_B, PPI_VP_MIN_BLOCKS) k_energy_vol_pairs(pp
 /* the guard-band pairs of the flat volume pass: the certified FP64 decision, the bit-identical exact_pair
  * where it cannot decide */
 __global__ void k_vol_unsure(ppi_dev d) {
+	grid_dep_wait();
+	grid_dep_release();
 	const int n = d.vun_count[0] < d.vun_cap ? d.vun_count[0] : d.vun_cap;
 	for(int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
 		const int2 pr = d.vunsure[k];
@@ -3397,10 +3401,15 @@ __global__ void k_energy_reset(ppi_dev d) {
  * box-shape move (MC_change_Lx, MC.c:515-537): Lx changes by (R - 0.5) Lx_change_max, Ly = Lz =
  * sqrt(V / Lx) keep the volume, every coordinate is rescaled by its side's factor */
 __global__ void k_vol_plan(ppi_dev d, long long sweep) {
+	grid_dep_wait(); /* the volume move's kernels are chained by programmatic dependent launch */
+	grid_dep_release();
 	int r = blockIdx.x * blockDim.x + threadIdx.x;
 	if(r >= d.nrep) return;
 	sweep = ctr_index(sweep, sweep < 0 ? d.ctr->sweep : 0);
-	if(r == 0) d.ctr->vol_any = 0;
+	if(r == 0) {
+		d.ctr->vol_any = 0;
+		if(d.vun_count) d.vun_count[0] = 0;
+	}
 	const ppi_rparams &rp = d.rp[r];
 	ppi_rstate *rs = d.rs + r;
 	ppi_grid *g = d.grid + r;
@@ -3475,6 +3484,8 @@ __device__ void grid_scale_axis(ppi_grid *g, ppi_rstate *rs, int a) {
 }
 
 __global__ void k_vol_decide(ppi_dev d, long long sweep) {
+	grid_dep_wait();
+	grid_dep_release();
 	int r = blockIdx.x * blockDim.x + threadIdx.x;
 	if(r >= d.nrep) return;
 	sweep = ctr_index(sweep, sweep < 0 ? d.ctr->sweep : 0);
@@ -3512,6 +3523,8 @@ __global__ void k_vol_decide(ppi_dev d, long long sweep) {
 }
 
 __global__ void k_vol_apply(ppi_dev d) {
+	grid_dep_wait();
+	grid_dep_release();
 	int k = blockIdx.x * blockDim.x + threadIdx.x;
 	if(k >= d.ntot || !d.ctr->vol_any) return; /* every replica rejected its candidate box: nothing to rescale */
 	/* canonical positions (slot k): p->r[a] *= rescale_factor (MC.c:477, MC.c:541-544) */
@@ -3648,12 +3661,34 @@ extern "C" int ppi_resort(const ppi_dev *d, long long epoch, cudaStream_t s, lon
 
 static int lanes_of(const ppi_dev *d) { return d->lanes == 8 ? 8 : PPI_DEFAULT_LANES; }
 
+static int pdl_enabled(void) {
+	static int pdl = -1;
+	if(pdl < 0) pdl = getenv("PPGPU_NO_PDL") ? 0 : 1;
+	return pdl;
+}
+
+/* a launch with programmatic stream serialisation: the kernel may start before its predecessor completes
+ * and waits for it (grid_dep_wait) before its first dependent access */
+template <typename... KArgs, typename... Args>
+static void launch_pdl(void (*kern)(KArgs...), int grid, int block, cudaStream_t s, Args... args) {
+	cudaLaunchConfig_t cfg;
+	memset(&cfg, 0, sizeof(cfg));
+	cfg.gridDim = dim3(grid);
+	cfg.blockDim = dim3(block);
+	cfg.stream = s;
+	cudaLaunchAttribute at[1];
+	at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	at[0].val.programmaticStreamSerializationAllowed = 1;
+	cfg.attrs = at;
+	cfg.numAttrs = pdl_enabled() ? 1 : 0;
+	cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 /* the 8 colour launches of a round; colours 1..7 with programmatic stream serialisation (their proposals
  * overlap the previous colour's tail, see grid_dep_wait) */
 template <typename K>
 static void launch_round(K kern, int grid, int block, size_t smem, const ppi_dev *d, long long round, const int *colours, cudaStream_t s) {
-	static int pdl = -1;
-	if(pdl < 0) pdl = getenv("PPGPU_NO_PDL") ? 0 : 1;
+	const int pdl = pdl_enabled();
 	for(int ci = 0; ci < 8; ci++) {
 		cudaLaunchConfig_t cfg;
 		memset(&cfg, 0, sizeof(cfg));
@@ -3696,10 +3731,9 @@ static void launch_energy(const ppi_dev *d, int mode, int use_nl, cudaStream_t s
 		else k_energy<MODE_FAST, 1><<<resident_grid(k_energy<MODE_FAST, 1>, &g_f1), 128, 0, s>>>(*d, mode);
 	}
 	else if(audit) k_energy<MODE_AUDIT, 4><<<resident_grid(k_energy<MODE_AUDIT, 4>, &g_a4), 128, 0, s>>>(*d, mode);
-	else if(mode == PPI_EN_VOLUME && use_nl && d->nl_k > 0 && d->vpairs) {
-		cudaMemsetAsync(d->vun_count, 0, sizeof(int), s);
-		k_energy_vol_pairs<<<resident_grid(k_energy_vol_pairs, &g_vol_pairs, VP_B), VP_B, 0, s>>>(*d);
-		k_vol_unsure<<<64, 128, 0, s>>>(*d);
+	else if(mode == PPI_EN_VOLUME && use_nl && d->nl_k > 0 && d->vpairs) { /* k_vol_plan cleared the queue */
+		launch_pdl(k_energy_vol_pairs, resident_grid(k_energy_vol_pairs, &g_vol_pairs, VP_B), VP_B, s, *d);
+		launch_pdl(k_vol_unsure, 64, 128, s, *d);
 		*nl += 1;
 	}
 	else if(mode == PPI_EN_VOLUME && use_nl && d->nl_k > 0)
@@ -3720,10 +3754,12 @@ extern "C" int ppi_energy(const ppi_dev *d, int mode, cudaStream_t s, long long 
 }
 
 extern "C" int ppi_volume(const ppi_dev *d, long long sweep, int use_nl, cudaStream_t s, long long *nl) {
-	k_vol_plan<<<(d->nrep + 63) / 64, 64, 0, s>>>(*d, sweep);
+	/* the chain plan -> candidate-box energy -> guard band -> decide -> rescale, each launch overlapping its
+	 * predecessor's tail (programmatic dependent launch; every kernel waits before its first access) */
+	launch_pdl(k_vol_plan, (d->nrep + 63) / 64, 64, s, *d, sweep);
 	launch_energy(d, PPI_EN_VOLUME, use_nl, s, nl);
-	k_vol_decide<<<(d->nrep + 63) / 64, 64, 0, s>>>(*d, sweep);
-	if(d->ntot > 0) k_vol_apply<<<(d->ntot + 255) / 256, 256, 0, s>>>(*d);
+	launch_pdl(k_vol_decide, (d->nrep + 63) / 64, 64, s, *d, sweep);
+	if(d->ntot > 0) launch_pdl(k_vol_apply, (d->ntot + 255) / 256, 256, s, *d);
 	*nl += 3;
 	return (int) cudaGetLastError();
 }
