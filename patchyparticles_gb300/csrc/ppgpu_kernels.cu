@@ -88,6 +88,15 @@ __device__ __forceinline__ int colour_at(long long round, int ci) {
 __device__ __forceinline__ float u01(uint32_t v) { return (float) (v >> 8) * 0x1p-24f; } /* [0, 1) */
 __device__ __forceinline__ double u01d(uint32_t a, uint32_t b) { return (double) (((uint64_t) a << 21) | (b >> 11)) * 0x1p-53; }
 
+/* Programmatic dependent launch. A kernel launched with programmatic stream serialisation may start
+ * before its predecessor completes: grid_dep_wait blocks until the predecessor has completed and its
+ * writes are visible, grid_dep_release lets the next such launch begin. Both are no-ops in an ordinary
+ * launch. The colour passes draw their first proposals (which read only their own movers, untouched by
+ * the previous colour, and the epoch's colour and neighbour lists) before the wait; the chained kernels
+ * of the sort and of the volume move wait first. */
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 /* ------------------------------------------------------------------------------------------------ */
 /* Reference-exact FP64 pair test: MC_would_interact (MC.c:232-266) with the patches of              */
 /* MATRIX_VECTOR_MULTIPLICATION (utils.h:18-22). Every operation is an explicitly rounded IEEE        */
@@ -467,6 +476,10 @@ __device__ __noinline__ void audit_pair(const double *rec_all, const ppi_rparams
 
 __global__ void k_grid(ppi_dev d, long long epoch) {
 	int r = blockIdx.x * blockDim.x + threadIdx.x;
+	if(r == 0 && d.vp_count) { /* the counters of the list build that follows the sort (ppi_nlist) */
+		d.vp_count[0] = 0;
+		d.vp_count[1] = 0;
+	}
 	if(r >= d.nrep) return;
 	epoch = ctr_index(epoch, epoch < 0 ? d.ctr->epoch : 0);
 	const ppi_rparams &rp = d.rp[r];
@@ -522,6 +535,8 @@ __device__ __forceinline__ float d2f_trunc(double x) {
  * cell origin, local offset); the FP32 local coordinate is then checked to lie in [0, w) and the cell
  * index corrected if it does not (the FP64 pipe is the scarce resource on this GPU). */
 __global__ void k_assign(ppi_dev d, float4 *tmp) {
+	grid_dep_wait(); /* chained by programmatic dependent launch (ppi_resort) */
+	grid_dep_release();
 	int s = blockIdx.x * blockDim.x + threadIdx.x;
 	if(s >= d.ntot) return;
 	const int r = d.rep[s];
@@ -586,6 +601,8 @@ __device__ __forceinline__ int block_scan_incl(int v, int *ws) {
 }
 
 __global__ void __launch_bounds__(SCAN_B) k_scan_local(const int *in, int *out, int *cursor, int *aux, int n) {
+	grid_dep_wait(); /* chained by programmatic dependent launch (ppi_resort) */
+	grid_dep_release();
 	__shared__ int ws[SCAN_B / 32];
 	const int i = blockIdx.x * SCAN_B + threadIdx.x;
 	const int v = (i < n) ? in[i] : 0;
@@ -598,6 +615,8 @@ __global__ void __launch_bounds__(SCAN_B) k_scan_local(const int *in, int *out, 
 }
 
 __global__ void __launch_bounds__(SCAN_B) k_scan_top(int *aux, int nblocks, int *total_out) {
+	grid_dep_wait(); /* chained by programmatic dependent launch (ppi_resort) */
+	grid_dep_release();
 	__shared__ int ws[SCAN_B / 32];
 	int carry = 0;
 	for(int base = 0; base < nblocks; base += SCAN_B) {
@@ -612,6 +631,8 @@ __global__ void __launch_bounds__(SCAN_B) k_scan_top(int *aux, int nblocks, int 
 }
 
 __global__ void k_scan_add(int *out, const int *aux, int n) {
+	grid_dep_wait(); /* chained by programmatic dependent launch (ppi_resort) */
+	grid_dep_release();
 	int i = blockIdx.x * SCAN_B + threadIdx.x;
 	if(i < n) out[i] += aux[blockIdx.x];
 }
@@ -619,6 +640,8 @@ __global__ void k_scan_add(int *out, const int *aux, int n) {
 /* FP32 working record of slot s at sorted position pos: cell-local position from k_assign, orientation
  * columns of R0 . Q(q) evaluated in FP32 (error ~1e-7, far inside the guard band) */
 __global__ void k_scatter(ppi_dev d, const float4 *tmp) {
+	grid_dep_wait(); /* chained by programmatic dependent launch (ppi_resort) */
+	grid_dep_release();
 	int s = blockIdx.x * blockDim.x + threadIdx.x;
 	if(s >= d.ntot) return;
 	int gc = d.cellof[s];
@@ -661,6 +684,8 @@ __global__ void k_scatter(ppi_dev d, const float4 *tmp) {
  * attempt needs first: (global cell, first sorted position, particle count, replica). */
 #define CELLFIN_B 256
 __global__ void __launch_bounds__(CELLFIN_B) k_cellfin(ppi_dev d) {
+	grid_dep_wait(); /* chained by programmatic dependent launch (ppi_resort) */
+	grid_dep_release();
 	__shared__ int s_cnt[CELLFIN_B / 32][8];
 	__shared__ int s_base[8];
 	const int gc = blockIdx.x * blockDim.x + threadIdx.x;
@@ -726,13 +751,6 @@ __global__ void __launch_bounds__(CELLFIN_B) k_cellfin(ppi_dev d) {
 /* ------------------------------------------------------------------------------------------------ */
 /* one checkerboard colour: one attempt per non-empty cell of that colour                           */
 /* ------------------------------------------------------------------------------------------------ */
-/* Programmatic dependent launch of the colour passes: colour c + 1 is launched while colour c runs, its
- * warps draw their first proposals (which read only their own movers, untouched by colour c, and the
- * epoch's colour and neighbour lists) and then wait for colour c to complete before reading any neighbour
- * or writing anything. Both are no-ops in a launch without the programmatic attribute. */
-__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void grid_dep_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
-
 /* per-thread counters of one launch; reduced per CTA when the CTA serves one replica (the usual case),
  * otherwise flushed per thread */
 struct Acc {
@@ -1536,6 +1554,8 @@ __device__ __forceinline__ void nl_rows(const ppi_dev &d, int i, const ppi_rpara
  * warp-aggregated reservation per warp (at most nl_k per particle, the list's capacity); a particle whose
  * list overflowed goes to vp_over instead and the volume pass scans its half shell in the cells. */
 __global__ void __launch_bounds__(NL_B) k_nlist(ppi_dev d) {
+	grid_dep_wait(); /* chained by programmatic dependent launch (ppi_resort) */
+	grid_dep_release();
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	const int lane = threadIdx.x & 31;
 	int n = 0, h = 0, emit = 0, K = d.nl_k, cx = 0, cy = 0, cz = 0, r = 0;
@@ -3642,25 +3662,6 @@ static int resident_grid(F f, int *cache, int block = 128) {
 static int g_col_audit = 0, g_col_fast = 0, g_learn_audit = 0, g_learn_fast = 0, g_vol_grid = 0, g_col_tl = 0, g_col_tla = 0;
 static int g_a1 = 0, g_a4 = 0, g_f1 = 0, g_f4 = 0, g_f8 = 0, g_vol_list = 0, g_vol_pairs = 0;
 
-extern "C" int ppi_resort(const ppi_dev *d, long long epoch, cudaStream_t s, long long *nl) {
-	float4 *tmp = (float4 *) d->tmp_rec; /* ntot float4 fit in the reorder scratch */
-	cudaMemsetAsync(d->cell_count, 0, sizeof(int) * (size_t) d->total_cells, s);
-	cudaMemsetAsync(d->ccount, 0, sizeof(int) * 8, s);
-	k_grid<<<(d->nrep + 63) / 64, 64, 0, s>>>(*d, epoch);
-	int nb = (d->ntot + 255) / 256;
-	if(nb > 0) k_assign<<<nb, 256, 0, s>>>(*d, tmp);
-	int sb = (d->total_cells + SCAN_B - 1) / SCAN_B;
-	k_scan_local<<<sb, SCAN_B, 0, s>>>(d->cell_count, d->cell_start, d->cell_cursor, d->scan_aux, d->total_cells);
-	k_scan_top<<<1, SCAN_B, 0, s>>>(d->scan_aux, sb, d->cell_start + d->total_cells);
-	k_scan_add<<<sb, SCAN_B, 0, s>>>(d->cell_start, d->scan_aux, d->total_cells);
-	if(nb > 0) k_scatter<<<nb, 256, 0, s>>>(*d, tmp);
-	k_cellfin<<<(d->total_cells + CELLFIN_B - 1) / CELLFIN_B, CELLFIN_B, 0, s>>>(*d);
-	*nl += 5 + (nb > 0 ? 2 : 0);
-	return (int) cudaGetLastError();
-}
-
-static int lanes_of(const ppi_dev *d) { return d->lanes == 8 ? 8 : PPI_DEFAULT_LANES; }
-
 static int pdl_enabled(void) {
 	static int pdl = -1;
 	if(pdl < 0) pdl = getenv("PPGPU_NO_PDL") ? 0 : 1;
@@ -3683,6 +3684,27 @@ static void launch_pdl(void (*kern)(KArgs...), int grid, int block, cudaStream_t
 	cfg.numAttrs = pdl_enabled() ? 1 : 0;
 	cudaLaunchKernelEx(&cfg, kern, args...);
 }
+
+extern "C" int ppi_resort(const ppi_dev *d, long long epoch, cudaStream_t s, long long *nl) {
+	float4 *tmp = (float4 *) d->tmp_rec; /* ntot float4 fit in the reorder scratch */
+	cudaMemsetAsync(d->cell_count, 0, sizeof(int) * (size_t) d->total_cells, s);
+	cudaMemsetAsync(d->ccount, 0, sizeof(int) * 8, s);
+	k_grid<<<(d->nrep + 63) / 64, 64, 0, s>>>(*d, epoch);
+	/* the rest of the sort is one chain of kernels, each launch overlapping its predecessor's tail
+	 * (programmatic dependent launch; every kernel waits before its first access) */
+	int nb = (d->ntot + 255) / 256;
+	if(nb > 0) launch_pdl(k_assign, nb, 256, s, *d, tmp);
+	int sb = (d->total_cells + SCAN_B - 1) / SCAN_B;
+	launch_pdl(k_scan_local, sb, SCAN_B, s, (const int *) d->cell_count, d->cell_start, d->cell_cursor, d->scan_aux, d->total_cells);
+	launch_pdl(k_scan_top, 1, SCAN_B, s, d->scan_aux, sb, d->cell_start + d->total_cells);
+	launch_pdl(k_scan_add, sb, SCAN_B, s, d->cell_start, (const int *) d->scan_aux, d->total_cells);
+	if(nb > 0) launch_pdl(k_scatter, nb, 256, s, *d, (const float4 *) tmp);
+	launch_pdl(k_cellfin, (d->total_cells + CELLFIN_B - 1) / CELLFIN_B, CELLFIN_B, s, *d);
+	*nl += 5 + (nb > 0 ? 2 : 0);
+	return (int) cudaGetLastError();
+}
+
+static int lanes_of(const ppi_dev *d) { return d->lanes == 8 ? 8 : PPI_DEFAULT_LANES; }
 
 /* the 8 colour launches of a round; colours 1..7 with programmatic stream serialisation (their proposals
  * overlap the previous colour's tail, see grid_dep_wait) */
@@ -3707,8 +3729,7 @@ static void launch_round(K kern, int grid, int block, size_t smem, const ppi_dev
 
 extern "C" int ppi_nlist(const ppi_dev *d, cudaStream_t s, long long *nl) {
 	if(d->ntot <= 0 || d->nl_k <= 0) return 0;
-	if(d->vp_count) cudaMemsetAsync(d->vp_count, 0, 2 * sizeof(int), s);
-	k_nlist<<<(d->ntot + NL_B - 1) / NL_B, NL_B, 0, s>>>(*d);
+	launch_pdl(k_nlist, (d->ntot + NL_B - 1) / NL_B, NL_B, s, *d); /* k_grid zeroed its counters */
 	*nl += 1;
 	return (int) cudaGetLastError();
 }
