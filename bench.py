@@ -502,7 +502,7 @@ def _sum_op(dist):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=2000)  # ~0.85 s timed at N = 1M: the clock sampler sees it
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="c5", choices=sorted(WORKLOADS) + ["c3"])

@@ -202,7 +202,7 @@ int pp_gpu_energy_noalloc(int N, const double *r_dev, const double *R_dev, const
 
 /* ------------------------------------------------------------------ learned proposal: the network */
 /* Per-particle MLP 36 -> 64 -> 64 -> 4 (ReLU), BF16 operands on the tensor cores, FP32 accumulation.
- * No counterpart in the reference: the spec addition whose plain fallback is MC_move_rototranslate.
+ * No counterpart in the reference: an addition to it, whose plain fallback is MC_move_rototranslate.
  * Parameters are FP32, laid out W1[64][36] b1[64] W2[64][64] b2[64] W3[4][64] b3[4] (PP_MLP_NPARAMS). */
 #define PP_MLP_IN 36
 #define PP_MLP_HIDDEN 64
