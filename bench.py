@@ -251,7 +251,7 @@ def run_reference(args, wl, ws, rank, dist):
     r, R, box = make_config(wl)
     threads = os.cpu_count() or 1
     total = args.steps + args.warmup
-    per = max(0.2, min(2.0, 20.0 / max(1, total)))
+    per = max(0.05, min(2.0, 20.0 / max(1, total)))  # the whole arm stays within ~2 minutes
     from oracle import pyoracle as po
 
     po.build(with_reference=False)
