@@ -7,7 +7,9 @@
  * It follows the reference's main loop (main.c:26-143): initial energy and overlap check (main.c:55-64),
  * output_print every Print_every steps (output.c:119-211: energy.dat, density.dat, boxshape.dat,
  * acceptance.dat, the stdout line, last.rrr) with MC_check_energy after it (main.c:86), configurations
- * every Save_every steps (main.c:96-101, output.c:302-317) and the final configuration and line
+ * every Save_every steps (main.c:96-101, output.c:302-317), bond files bonds_<step>.dat with every print when
+ * Print_bonds is set (output.c:206-268; partners in ascending order, where the reference lists them in
+ * the order of its cell walk) and the final configuration and line
  * (main.c:125-143). The input keys are the reference's (parse_input.c: "key = value" lines, '#'
  * comments), with the same mandatory keys and error messages; the sweeps between two outputs are one
  * pp_gpu_sweeps call. Optional engine keys: GPU_resort_every (rounds between cell re-sorts),
@@ -113,6 +115,8 @@ typedef struct {
 	double *r, *R, box[3];
 	FILE *energy, *acc, *density, *boxshape;
 	const char *last;
+	const char *bonds_folder; /* Print_bonds: bonds_<step>.dat into this folder (output.c:88-99) */
+	int *offsets, *partners, cap;
 } run_t;
 
 static void check(run_t *s, int rc) {
@@ -124,6 +128,27 @@ static void check(run_t *s, int rc) {
 static void save(run_t *s, long long step, const char *path) {
 	check(s, pp_gpu_download(s->e, s->r, s->R, s->box));
 	if(pp_rrr_write(path, step, s->N, s->r, s->R, s->box) != PP_OK) die("Configuration file '%s' is not writable", path);
+}
+
+/* output_print_bonds (output.c:213-268): N, then per particle "index n_bonds" and its partners */
+static void print_bonds(run_t *s, long long step) {
+	int n;
+	while((n = pp_gpu_bond_lists(s->e, 0, s->offsets, s->partners, s->cap)) == PP_ERR_CAPACITY) {
+		s->cap *= 2;
+		s->partners = realloc(s->partners, sizeof(int) * (size_t) s->cap);
+	}
+	if(n < 0) die("%s", pp_gpu_last_error(s->e));
+	char name[4 * KEYLEN];
+	snprintf(name, sizeof(name), "%s/bonds_%lld.dat", s->bonds_folder, step);
+	FILE *out = fopen(name, "w");
+	if(out == NULL) die("Cannot create files in directory '%s'", s->bonds_folder);
+	fprintf(out, "%d\n", s->N);
+	for(int i = 0; i < s->N; i++) {
+		fprintf(out, "%d %d\n", i, s->offsets[i + 1] - s->offsets[i]);
+		for(int k = s->offsets[i]; k < s->offsets[i + 1]; k++) fprintf(out, "%d ", s->partners[k]);
+		fprintf(out, "\n");
+	}
+	fclose(out);
 }
 
 /* output_print (output.c:119-211) */
@@ -154,6 +179,7 @@ static void print_step(run_t *s, long long step) {
 	printf("\n");
 	fflush(stdout);
 	save(s, step, s->last);
+	if(s->bonds_folder) print_bonds(s, step);
 }
 
 int main(int argc, char *argv[]) {
@@ -183,6 +209,11 @@ int main(int argc, char *argv[]) {
 	const char *folder = key(in, "Configuration_folder", 1);
 	if(access(folder, W_OK) != 0) die("Cannot create files in directory '%s': please make sure that the directory exists and it is writable", folder);
 	s.last = (v = key(in, "Configuration_last", 0)) ? v : "last.rrr";
+	if((v = key(in, "Print_bonds", 0)) && atoi(v)) {
+		s.bonds_folder = key(in, "Bonds_folder", 1);
+		if(access(s.bonds_folder, W_OK) != 0)
+			die("Cannot create files in directory '%s': please make sure that the directory exists and it is writable", s.bonds_folder);
+	}
 
 	/* system_init (system.c:58-252), Dynamics = 0, NVT or NPT */
 	pp_params p;
@@ -223,6 +254,9 @@ int main(int argc, char *argv[]) {
 	char err[512];
 	if(pp_rrr_read(conf, N, s.r, s.R, s.box, err, sizeof(err)) != PP_OK) die("%s", err);
 	s.N = N;
+	s.cap = 8 * (N > 0 ? N : 1);
+	s.offsets = malloc(sizeof(int) * (size_t) (N + 1));
+	s.partners = malloc(sizeof(int) * (size_t) s.cap);
 	if(pp_gpu_create(&p, &s.e) != PP_OK) die("%s", pp_gpu_last_error(s.e));
 	if((v = key(in, "GPU_neighbour_lists", 0))) check(&s, pp_gpu_set_neighbour_lists(s.e, atoi(v)));
 	/* the upload computes the initial energy and refuses an overlapping configuration (main.c:55-64) */
@@ -274,6 +308,8 @@ int main(int argc, char *argv[]) {
 	pp_gpu_destroy(s.e);
 	free(s.r);
 	free(s.R);
+	free(s.offsets);
+	free(s.partners);
 	free(in);
 	return 0;
 }

@@ -61,6 +61,26 @@ def test_driver_writes_the_reference_outputs(built, name, files):
 
 
 @pytest.mark.gpu
+def test_driver_writes_bond_files(built):
+    """Print_bonds: bonds_<step>.dat at every print; at step 0 the partner sets equal the reference's own
+    per-particle probe of the same configuration (output_print_bonds, output.c:213-268)."""
+    src, work = _prepare("small_nvt", lambda t: t + "Print_bonds = 1\nBonds_folder = bonds\n")
+    os.makedirs(os.path.join(work, "bonds"))
+    p = subprocess.run([CLI, "input"], cwd=work, capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr
+    files = sorted(os.listdir(os.path.join(work, "bonds")))
+    assert "bonds_0.dat" in files and len(files) == len(open(os.path.join(src, "energy.dat")).read().splitlines())
+    lines = open(os.path.join(work, "bonds", "bonds_0.dat")).read().splitlines()
+    N, _, _, _, _, nb, _, bonded = helpers.parse_probe("small")
+    assert int(lines[0]) == N and len(lines) == 1 + 2 * N
+    for i in range(N):
+        idx, n = map(int, lines[1 + 2 * i].split())
+        partners = [int(v) for v in lines[2 + 2 * i].split()]
+        assert idx == i and n == nb[i] == len(partners) and sorted(partners) == sorted(bonded[i])
+    shutil.rmtree(work)
+
+
+@pytest.mark.gpu
 def test_driver_refuses_an_overlapping_configuration(built):
     src, work = _prepare("small_nvt", lambda t: t.replace("generator_300_0.3_4242.rrr", "adversarial.rrr"))
     helpers.unpack_golden("adversarial.rrr", work)
