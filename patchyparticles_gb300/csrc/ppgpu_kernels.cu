@@ -1345,7 +1345,7 @@ __device__ __forceinline__ void tile_round(const ppi_dev &d, TileSmem &S, const 
 		bool &waited) {
 	const int loc0 = tile_setup(d, S, lane, e0, round, A);
 	const int loc1 = tile_setup(d, S, lane + 32, e1, round, A);
-	if(!waited) { /* the proposals are drawn: from here on the previous colour's moves must be complete */
+	if(!waited && !LIST) { /* the proposals are drawn: from here on the previous colour's moves must be complete */
 		grid_dep_wait();
 		grid_dep_release();
 		waited = true;
@@ -1385,6 +1385,11 @@ __device__ __forceinline__ void tile_round(const ppi_dev &d, TileSmem &S, const 
 				if(mine) write_list_pairs(d, S, a, n, start - done);
 				const int end = __shfl_sync(0xffffffffu, incl, 31 - __clz(take));
 				__syncwarp();
+				if(!waited) { /* the epoch's lists are read: the candidates need the previous colour complete */
+					grid_dep_wait();
+					grid_dep_release();
+					waited = true;
+				}
 				tile_steps<MODE>(d, S, lane, end - done, A);
 				done = end;
 				__syncwarp();
@@ -1418,6 +1423,11 @@ __device__ __forceinline__ void tile_round(const ppi_dev &d, TileSmem &S, const 
 		}
 		__syncwarp();
 		tile_steps<MODE>(d, S, lane, np, A);
+	}
+	if(!waited) { /* no pair of this iteration read a neighbour: wait before the decisions and commits */
+		grid_dep_wait();
+		grid_dep_release();
+		waited = true;
 	}
 	if(S.nc) tile_close<MODE>(d, S, lane, A);
 	/* guard-band pairs: certified FP64 decisions (no division chain); an undecided one defers its attempt */
