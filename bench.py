@@ -376,7 +376,7 @@ def run_gpu(args, wl, ws, rank, local, dist):
         "config": {"workload": wl["name"] if args.precision != "fp64" else wl["name"].replace("FP32+guard", "FP64 pair tests"), "N": wl["N"],
                    "precision": args.precision, "sweeps_per_step": spsw, "proposal": "plain",
                    "l2": "inputs larger than L2 (FP64 state %.0f MB + FP32 mirror %.0f MB per GPU)" % (wl["N"] * 128 / 1e6, wl["N"] * 64 / 1e6),
-                   "parallelism": "replicas" if ws > 1 else "single GPU", "launch": "CUDA graph per re-sort period",
+                   "parallelism": "replicas" if ws > 1 else "single GPU", "launch": "CUDA graph per re-sort period, programmatic dependent launch between its kernels",
                    "schedule": tune if tune else "defaults (resort_every 4, reorder_every 16, cell_scale 1.0)"},
         "acceptance": acc[pp.MOVE_ROTO_TRASL] / max(1, tries[pp.MOVE_ROTO_TRASL]),
         "volume_acceptance": acc[pp.MOVE_VOLUME] / max(1, tries[pp.MOVE_VOLUME]) if tries[pp.MOVE_VOLUME] else None,
