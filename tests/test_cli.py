@@ -101,3 +101,18 @@ def test_driver_rejects_other_dynamics(built):
     p = subprocess.run([CLI, "input"], cwd=work, capture_output=True, text=True, timeout=60)
     assert p.returncode == 1 and "Dynamics = 1" in p.stderr
     shutil.rmtree(work)
+
+
+@pytest.mark.parametrize("edit,code,msg", [
+    (lambda t: t.replace("Ensemble = 0", "Ensemble = 2"), 1, "Ensemble = 2"),
+    (lambda t: t.replace("generator_300_0.3_4242.rrr", "missing.rrr"), 1, "missing.rrr"),
+    (lambda t: t + "Print_bonds = 1\n", 255, "Mandatory key 'Bonds_folder' not found"),
+    (lambda t: t + "Print_bonds = 1\nBonds_folder = nowhere\n", 1, "Cannot create files in directory 'nowhere'"),
+])
+def test_driver_input_errors(built, edit, code, msg):
+    src, work = _prepare("small_nvt")
+    path = os.path.join(work, "input")
+    open(path, "w").write(edit(open(path).read()))
+    p = subprocess.run([CLI, "input"], cwd=work, capture_output=True, text=True, timeout=60)
+    assert p.returncode == code and msg in p.stderr, p.stderr
+    shutil.rmtree(work)
