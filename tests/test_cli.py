@@ -112,7 +112,8 @@ def test_driver_rejects_other_dynamics(built):
 def test_driver_input_errors(built, edit, code, msg):
     src, work = _prepare("small_nvt")
     path = os.path.join(work, "input")
-    open(path, "w").write(edit(open(path).read()))
+    text = edit(open(path).read())
+    open(path, "w").write(text)
     p = subprocess.run([CLI, "input"], cwd=work, capture_output=True, text=True, timeout=60)
     assert p.returncode == code and msg in p.stderr, p.stderr
     shutil.rmtree(work)
