@@ -15,8 +15,11 @@
  * never interact and the cell lists stay valid for the whole epoch. The pair test is FP32 with an FP64
  * re-evaluation inside the guard band, bit-identical to MC_would_interact (MC.c:232-266). Accepted moves
  * update the FP64 state with FP64 arithmetic (r + disp, q (x) dq) and the FP32 record in place.
- * k_energy: energy from scratch (per-particle bonds/overlaps, output.c:213-268) or of the NPT candidate
- * box (MC.c:487-495); k_vol_*: the NPT volume move (MC.c:450-513).
+ * k_energy: energy from scratch (per-particle bonds/overlaps, output.c:213-268); the candidate box of the
+ * sweep's NPT volume move (MC.c:487-495) or NVT box-shape move (MC.c:547-555) from the epoch's flat pair
+ * list (k_energy_vol_pairs, k_vol_unsure) or, without lists, per particle (k_energy_vol); k_vol_*: the
+ * volume and box-shape moves (MC.c:450-513, 515-567). The sort, the volume move and the colours of a round
+ * are chained by programmatic dependent launch (grid_dep_wait).
  */
 #include "ppgpu.h"
 #include "ppgpu_internal.h"
