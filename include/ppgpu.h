@@ -63,8 +63,8 @@ typedef struct pp_params {
 	int resort_every;          /* checkerboard rounds between cell-grid re-sorts from the FP64 state; 0 = 4 */
 	int audit;                 /* nonzero: re-check every FP32 decision in FP64 and count mismatches */
 	/* Lx_move (system.c:170-193, NVT only; ignored for NPT as in the reference): once per sweep Lx changes by
-	 * (R - 0.5) Lx_change_max and Ly = Lz = sqrt(V / Lx) keep the volume (MC_change_Lx, MC.c:515-567).
-	 * 1 = the reference's acceptance min(1, exp(+dE / T)) (MC.c:559), 2 = the Boltzmann factor exp(-dE / T). */
+	 * (R - 0.5) Lx_change_max and Ly = Lz = sqrt(V / Lx) keep the volume (MC_change_Lx, MC.c:515-585).
+	 * 1 = the reference's acceptance min(1, exp(+dE / T)) (MC.c:562), 2 = the Boltzmann factor exp(-dE / T). */
 	int lx_move;
 	double lx_change_max;      /* Lx_change_max */
 	double lyz_min, lyz_max;   /* Lyz_min, Lyz_max: allowed range of Ly = Lz (absolute lengths) */

@@ -421,8 +421,8 @@ static void o_change_volume(orc_system *s) { /* MC_change_volume, MC.c:450-513 *
 	}
 }
 
-/* MC_change_Lx (MC.c:515-567): Lx changes by a uniform amount, Ly = Lz follow at constant volume, every
- * coordinate is rescaled; accepted with probability min(1, exp(+dE / T)) (MC.c:559) as the reference does;
+/* MC_change_Lx (MC.c:515-585): Lx changes by a uniform amount, Ly = Lz follow at constant volume, every
+ * coordinate is rescaled; accepted with probability min(1, exp(+dE / T)) (MC.c:562) as the reference does;
  * a rejected move divides the positions back */
 static void o_change_lx(orc_system *s) {
 	s->tries[ORC_LX]++;

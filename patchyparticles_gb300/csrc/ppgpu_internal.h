@@ -50,7 +50,7 @@ typedef struct ppi_rparams {
 	int audit;
 	int cell_base;   /* first global cell index of this replica */
 	int cell_cap;    /* cells reserved for this replica */
-	int lx_move;     /* NVT box-shape move (MC.c:515-567): 0 off, 1 reference acceptance, 2 Boltzmann acceptance */
+	int lx_move;     /* NVT box-shape move (MC.c:515-585): 0 off, 1 reference acceptance, 2 Boltzmann acceptance */
 	double T, P, disp_max, theta_max, rescale_max;
 	double cosmax, sqr_rcut, r_cut, w_min;
 	double base[4][3];     /* tetrahedral base patches, bit-identical to system.c:20-31 */

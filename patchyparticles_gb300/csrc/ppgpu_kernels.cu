@@ -16,9 +16,9 @@
  * re-evaluation inside the guard band, bit-identical to MC_would_interact (MC.c:232-266). Accepted moves
  * update the FP64 state with FP64 arithmetic (r + disp, q (x) dq) and the FP32 record in place.
  * k_energy: energy from scratch (per-particle bonds/overlaps, output.c:213-268); the candidate box of the
- * sweep's NPT volume move (MC.c:487-495) or NVT box-shape move (MC.c:547-555) from the epoch's flat pair
+ * sweep's NPT volume move (MC.c:487-495) or NVT box-shape move (MC.c:554-560) from the epoch's flat pair
  * list (k_energy_vol_pairs, k_vol_unsure) or, without lists, per particle (k_energy_vol); k_vol_*: the
- * volume and box-shape moves (MC.c:450-513, 515-567). The sort, the volume move and the colours of a round
+ * volume and box-shape moves (MC.c:450-513, 515-585). The sort, the volume move and the colours of a round
  * are chained by programmatic dependent launch (grid_dep_wait).
  */
 #include "ppgpu.h"
@@ -3531,7 +3531,7 @@ __global__ void k_vol_decide(ppi_dev d, long long sweep) {
 	const U4 u = rng(rp, sweep, r, TAG_VOL, 0, 1);
 	if(g->vol_dir == PPI_LX_DIR) {
 		rs->tries[7]++;
-		/* MC.c:559 accepts with min(1, exp(+dE / T)); lx_move = 2 takes the Boltzmann factor exp(-dE / T) */
+		/* MC.c:562 accepts with min(1, exp(+dE / T)); lx_move = 2 takes the Boltzmann factor exp(-dE / T) */
 		const double arg = (rp.lx_move == 2 ? -dE : dE) / rp.T;
 		if(!rs->vol_overlap && u01d(u.x, u.y) < exp(arg)) {
 			rs->vol_accept = 1;

@@ -58,7 +58,7 @@ TRAJ = [
     ("bcc_npt", "bcc.rrr", 5, 0.12, 400, 50, 12345, "P = 0.05\nrescale_factor_max = 0.01\n"),
     ("small_nvt", "generator_300_0.3_4242.rrr", 0, 0.11, 200, 20, 7, ""),
     ("small_npt", "generator_300_0.3_4242.rrr", 5, 0.11, 300, 30, 9, "P = 0.05\nrescale_factor_max = 0.01\n"),
-    # the box-shape move of NVT (MC.c:515-567): Lx changes, Ly = Lz follow at constant volume
+    # the box-shape move of NVT (MC.c:515-585): Lx changes, Ly = Lz follow at constant volume
     ("small_lx", "generator_300_0.3_4242.rrr", 0, 0.11, 400, 40, 11, "Lx_move = 1\nLx_change_max = 0.5\nLyz_min = 8.0\nLyz_max = 12.0\n"),
 ]
 

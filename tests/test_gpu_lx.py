@@ -1,4 +1,4 @@
-"""The NVT box-shape move (Lx_move, MC_change_Lx, MC.c:515-567) on the GPU: one attempt per sweep, Ly = Lz at
+"""The NVT box-shape move (Lx_move, MC_change_Lx, MC.c:515-585) on the GPU: one attempt per sweep, Ly = Lz at
 constant volume, the tracked energy equal to the reference routines' energy of the downloaded state,
 the same trajectory with and without neighbour lists and CUDA graphs, the reference's validation errors,
 and box-shape statistics against the reference's sequential MC (the oracle, pinned by a reference
