@@ -62,7 +62,7 @@ typedef struct pp_params {
 	double guard_eps;          /* guard half-width on r^2 and on patch cosines; <= 0 selects 1e-5 */
 	int resort_every;          /* checkerboard rounds between cell-grid re-sorts from the FP64 state; 0 = 4 */
 	int audit;                 /* nonzero: re-check every FP32 decision in FP64 and count mismatches */
-	/* Lx_move (system.c:170-193, NVT only; ignored for NPT as in the reference): once per sweep Lx changes by
+	/* Lx_move (system.c:170-196, NVT only; ignored for NPT as in the reference): once per sweep Lx changes by
 	 * (R - 0.5) Lx_change_max and Ly = Lz = sqrt(V / Lx) keep the volume (MC_change_Lx, MC.c:515-585).
 	 * 1 = the reference's acceptance min(1, exp(+dE / T)) (MC.c:562), 2 = the Boltzmann factor exp(-dE / T). */
 	int lx_move;

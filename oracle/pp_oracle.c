@@ -56,7 +56,7 @@ void orc_drand48_sequence(int seed, int n, double *out) {
 }
 
 /* ---------------------------------------------------------------- vector helpers (utils.c, utils.h) */
-#define O_SCALAR(x, y) ((x)[0] * (y)[0] + (x)[1] * (y)[1] + (x)[2] * (y)[2]) /* utils.h:16 */
+#define O_SCALAR(x, y) ((x)[0] * (y)[0] + (x)[1] * (y)[1] + (x)[2] * (y)[2]) /* utils.h:15 */
 
 static void o_normalize(double *v) { /* utils.c:31-36 */
 	double norm = sqrt(O_SCALAR(v, v));
@@ -87,7 +87,7 @@ static void o_gram_schmidt(double *v1, double *v2, double *v3) { /* utils.c:91-1
 	o_normalize(v3);
 }
 
-/* patches[i] = R . base[i] with the MATRIX_VECTOR_MULTIPLICATION order (utils.h:18-22) */
+/* patches[i] = R . base[i] with the MATRIX_VECTOR_MULTIPLICATION order (utils.h:17-21) */
 static void o_set_patches(orc_system *s, int p) {
 	const double *R = s->R + 9 * p;
 	double *P = s->patch + 12 * p;

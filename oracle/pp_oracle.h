@@ -43,7 +43,7 @@ typedef struct orc_params {
 	double kf_delta;           /* KF_delta */
 	double kf_cosmax;          /* KF_cosmax */
 	int seed;                  /* Seed (srand48 argument, system.c:71-75) */
-	int lx_move;               /* Lx_move (NVT only, system.c:165-193) */
+	int lx_move;               /* Lx_move (NVT only, system.c:165-196) */
 	double lx_change_max;      /* Lx_change_max */
 	double lyz_min, lyz_max;   /* Lyz_min, Lyz_max */
 } orc_params;

@@ -130,7 +130,7 @@ int main(int argc, char *argv[]) {
 		prm.rescale_factor_max = atof(get(in, "rescale_factor_max", 1));
 		prm.P = atof(get(in, "P", 1));
 	}
-	else if((v = get(in, "Lx_move", 0)) && atoi(v)) { /* system.c:170-193 (NVT only) */
+	else if((v = get(in, "Lx_move", 0)) && atoi(v)) { /* system.c:170-196 (NVT only) */
 		prm.lx_move = 1;
 		prm.lx_change_max = atof(get(in, "Lx_change_max", 1));
 		prm.lyz_min = atof(get(in, "Lyz_min", 1));

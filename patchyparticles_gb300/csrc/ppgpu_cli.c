@@ -274,7 +274,7 @@ int main(int argc, char *argv[]) {
 				t.reorder_every, t.cell_scale, t.neighbour_lists, t.attempts_per_s);
 	}
 
-	/* main loop (main.c:76-122): the sweeps between two output steps are one pp_gpu_sweeps call */
+	/* main loop (main.c:78-120): the sweeps between two output steps are one pp_gpu_sweeps call */
 	const long long steps = key_ll(in, "Steps", 1, 0) + start_from;
 	long long step = start_from;
 	char name[4 * KEYLEN];

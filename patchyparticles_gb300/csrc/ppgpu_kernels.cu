@@ -102,10 +102,10 @@ __device__ __forceinline__ void grid_dep_release() { asm volatile("griddepcontro
 
 /* ------------------------------------------------------------------------------------------------ */
 /* Reference-exact FP64 pair test: MC_would_interact (MC.c:232-266) with the patches of              */
-/* MATRIX_VECTOR_MULTIPLICATION (utils.h:18-22). Every operation is an explicitly rounded IEEE        */
+/* MATRIX_VECTOR_MULTIPLICATION (utils.h:17-21). Every operation is an explicitly rounded IEEE        */
 /* operation, so nothing is contracted into an FMA and the result equals the reference's bit for bit. */
 /* ------------------------------------------------------------------------------------------------ */
-/* patch i of an orientation: R . base_i with the MATRIX_VECTOR_MULTIPLICATION order (utils.h:18-22) */
+/* patch i of an orientation: R . base_i with the MATRIX_VECTOR_MULTIPLICATION order (utils.h:17-21) */
 __device__ __forceinline__ void patch64(const double *R, const double *b, double *P) {
 #pragma unroll
 	for(int k = 0; k < 3; k++) P[k] = __dadd_rn(__dadd_rn(__dmul_rn(R[3 * k + 0], b[0]), __dmul_rn(R[3 * k + 1], b[1])), __dmul_rn(R[3 * k + 2], b[2]));
@@ -283,10 +283,10 @@ __device__ __noinline__ int exact_pair(const double *__restrict__ rec_all, const
 }
 
 /* Certified FP64 decision of one pair without the reference's division and square root chain.
- * The distance test is the reference's own operation sequence (MC.c:232-245), so it is bit-identical:
+ * The distance test is the reference's own operation sequence (MC.c:233-240), so it is bit-identical:
  * d = q - p, minimum image d - box * rint(d / box), dist2 = d . d. Only rint's argument is formed with
  * the reciprocal of the box; it can round differently from d / box only within ~1e-15 of a half
- * integer, which is checked. The patch test (MC.c:246-265) is evaluated to ~1e-15 with Newton
+ * integer, which is checked. The patch test (MC.c:242-262) is evaluated to ~1e-15 with Newton
  * reciprocals (norm of d, norm of q); a cosine farther than DEC64_TOL from KF_cosmax is then on the same
  * side of it as the reference's FP64 value. Anything closer returns DEC64_EXACT and the caller runs the
  * bit-identical exact_pair. Returns -1 overlap, 0 no bond, 1 bond. */
@@ -398,7 +398,7 @@ __device__ __forceinline__ int decide64(const double *__restrict__ rec_all, cons
 		q_yes |= e > cmax + DEC64_TOL;
 		q_unsure |= fabs(e - cmax) <= DEC64_TOL;
 	}
-	/* bond iff some patch of p and some patch of q point at each other (MC.c:255-263) */
+	/* bond iff some patch of p and some patch of q point at each other (MC.c:249-262) */
 	if(p_yes && q_yes) return 1;
 	if((!p_yes && !p_unsure) || (!q_yes && !q_unsure)) return 0;
 	return DEC64_EXACT;
@@ -1007,7 +1007,7 @@ __device__ __forceinline__ void commit_from(const ppi_dev &d, const double *rec,
 	((float *) (d.sori + 3 * (size_t) i + 2))[0] = cpn[8];
 }
 
-/* Metropolis on dE = -(bn - bo) (MC.c:330-339) */
+/* Metropolis on dE = -(bn - bo) (MC.c:332-339) */
 __device__ __forceinline__ bool metropolis(const ppi_rparams &rp, long long round, int r, int local, int bo, int bn) {
 	const int dE = bo - bn; /* E = -bonds */
 	if(dE <= 0) return true;
@@ -3428,10 +3428,10 @@ __global__ void k_energy_reset(ppi_dev d) {
 }
 
 /* ------------------------------------------------------------------------------------------------ */
-/* NPT volume move (MC.c:450-513)                                                                   */
+/* NPT volume move (MC.c:450-513) and NVT box-shape move (MC.c:515-585)                             */
 /* ------------------------------------------------------------------------------------------------ */
 /* the candidate box of the sweep: an NPT volume move (MC.c:456-472) or, for NVT replicas with Lx_move, a
- * box-shape move (MC_change_Lx, MC.c:515-537): Lx changes by (R - 0.5) Lx_change_max, Ly = Lz =
+ * box-shape move (MC_change_Lx, MC.c:520-537): Lx changes by (R - 0.5) Lx_change_max, Ly = Lz =
  * sqrt(V / Lx) keep the volume, every coordinate is rescaled by its side's factor */
 __global__ void k_vol_plan(ppi_dev d, long long sweep) {
 	grid_dep_wait(); /* the volume move's kernels are chained by programmatic dependent launch */
