@@ -1343,15 +1343,15 @@ int pp_rrr_read(const char *path, int N, double *r, double *R, double box[3], ch
 	char line[512];
 	char *sr = fgets(line, sizeof(line), f);
 	while(sr != NULL) {
-		if(i >= N) {
+		/* the reference does not check these scans either: a short record keeps the previous values */
+		int got = sscanf(line, "%lf %lf %lf\n", p1, p1 + 1, p1 + 2);
+		got += fscanf(f, "%lf %lf %lf\n", p2, p2 + 1, p2 + 2);
+		got += fscanf(f, "%lf %lf %lf\n", rp, rp + 1, rp + 2);
+		(void) got;
+		if(i >= N) { /* records beyond the header's count are only counted, for the message below */
 			i++;
-			break;
-		}
-		if(sscanf(line, "%lf %lf %lf\n", p1, p1 + 1, p1 + 2) < 0) {
-		}
-		if(fscanf(f, "%lf %lf %lf\n", p2, p2 + 1, p2 + 2) < 0) {
-		}
-		if(fscanf(f, "%lf %lf %lf\n", rp, rp + 1, rp + 2) < 0) {
+			sr = fgets(line, sizeof(line), f);
+			continue;
 		}
 		h_normalize(p1);
 		h_normalize(p2);

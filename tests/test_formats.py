@@ -64,3 +64,46 @@ def test_reader_rejects_short_file(built):
     open(p, "w").write("")
     with pytest.raises(pp.PPError):
         pp.rrr_header(p)
+
+
+def test_reader_messages_are_the_reference_loaders(built):
+    """pp_rrr_read reports the reference loader's three failures with its messages (system.c:77-81, 245):
+    an unreadable file, a malformed header, and a record count different from the header's, in either
+    direction (the reference would write past its particle array for extra records; the reader counts them)."""
+    import ctypes
+    lib = pp.load_library()
+    d = tempfile.mkdtemp()
+    rec = "1 0 0\n0 1 0\n{0} {0} {0}\n"
+
+    def read(path, N):
+        r = np.zeros((max(N, 1), 3))
+        R = np.zeros((max(N, 1), 9))
+        b = np.zeros(3)
+        err = ctypes.create_string_buffer(512)
+        rc = lib.pp_rrr_read(path.encode(), N, pp._dp(r), pp._dp(R), pp._dp(b), err, 512)
+        return rc, err.value.decode()
+
+    missing = os.path.join(d, "missing.rrr")
+    rc, msg = read(missing, 1)
+    assert rc == pp.PP_ERR_IO and msg == f"Initial_conditions_file '{missing}' is not readable"
+
+    empty = os.path.join(d, "empty.rrr")
+    open(empty, "w").close()
+    rc, msg = read(empty, 1)
+    assert rc == pp.PP_ERR_IO and msg == f"The initial configuration file '{empty}' is empty or its headers are malformed"
+
+    short = os.path.join(d, "short.rrr")
+    open(short, "w").write("0 3 10 10 10\n" + rec.format(1))
+    rc, msg = read(short, 3)
+    assert rc == pp.PP_ERR_IO
+    assert msg == "Number of particles found in configuration (1) is different from the value found in the header (3)"
+
+    extra = os.path.join(d, "extra.rrr")
+    open(extra, "w").write("0 1 10 10 10\n" + "".join(rec.format(k + 1) for k in range(3)))
+    rc, msg = read(extra, 1)
+    assert rc == pp.PP_ERR_IO
+    assert msg == "Number of particles found in configuration (3) is different from the value found in the header (1)"
+
+    good = os.path.join(d, "good.rrr")
+    open(good, "w").write("0 2 10 10 10\n" + "".join(rec.format(k + 1) for k in range(2)))
+    assert read(good, 2) == (pp.PP_OK, "")
