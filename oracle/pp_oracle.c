@@ -564,20 +564,22 @@ orc_system *orc_load_rrr(const char *path, const orc_params *prm, char *err, int
 	memcpy(s->box, box, sizeof(box));
 	/* three lines per particle: orientation row 0, row 1, position (system.c:213-243) */
 	int i = 0;
-	double p1[3] = { 0., 0., 0. }, p2[3] = { 0., 0., 0. }, p3[3];
+	double p1[3] = { 0., 0., 0. }, p2[3] = { 0., 0., 0. }, p3[3], extra[3];
 	char line[512];
 	char *sr = fgets(line, sizeof(line), f);
 	while(sr != NULL) {
+		/* records beyond the header's count are only counted, for the message below (the reference writes
+		 * them past its particle array) */
+		double *r = i < N ? s->r + 3 * i : extra;
+		/* the reference does not check these scans either: a short record keeps the previous values */
+		int got = sscanf(line, "%lf %lf %lf\n", p1, p1 + 1, p1 + 2);
+		got += fscanf(f, "%lf %lf %lf\n", p2, p2 + 1, p2 + 2);
+		got += fscanf(f, "%lf %lf %lf\n", r, r + 1, r + 2);
+		(void) got;
 		if(i >= N) {
 			i++;
-			break;
-		}
-		if(sscanf(line, "%lf %lf %lf\n", p1, p1 + 1, p1 + 2)) {
-		}
-		if(fscanf(f, "%lf %lf %lf\n", p2, p2 + 1, p2 + 2)) {
-		}
-		double *r = s->r + 3 * i;
-		if(fscanf(f, "%lf %lf %lf\n", r, r + 1, r + 2)) {
+			sr = fgets(line, sizeof(line), f);
+			continue;
 		}
 		o_normalize(p1);
 		o_normalize(p2);

@@ -107,3 +107,9 @@ def test_reader_messages_are_the_reference_loaders(built):
     good = os.path.join(d, "good.rrr")
     open(good, "w").write("0 2 10 10 10\n" + "".join(rec.format(k + 1) for k in range(2)))
     assert read(good, 2) == (pp.PP_OK, "")
+
+    # the oracle's loader reports the same failures with the same messages
+    for path, N in ((missing, 1), (empty, 1), (short, 3), (extra, 1)):
+        with pytest.raises(RuntimeError) as ex:
+            po.System(po.params(), path=path)
+        assert str(ex.value) == read(path, N)[1]
