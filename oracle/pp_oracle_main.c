@@ -33,6 +33,14 @@ static void trim(char *s) {
 	if(b) memmove(s, s + b, strlen(s + b) + 1);
 }
 
+/* a key or value cut to the table's fixed width (the reference's OPT_MAX_LENGTH strings, parse_input.h:16) */
+static void copy_field(char *dst, const char *src) {
+	size_t n = strlen(src);
+	if(n >= KEYLEN) n = KEYLEN - 1;
+	memcpy(dst, src, n);
+	dst[n] = '\0';
+}
+
 /* loadInput (parse_input.c:30-87): "key = value" lines, '#' comments, surrounding blanks trimmed */
 static int load_input(inp_t *in, const char *path) {
 	FILE *f = fopen(path, "r");
@@ -52,8 +60,8 @@ static int load_input(inp_t *in, const char *path) {
 		}
 		*eq = '\0';
 		if(in->n == MAXKEYS) break;
-		snprintf(in->key[in->n], KEYLEN, "%s", line);
-		snprintf(in->val[in->n], KEYLEN, "%s", eq + 1);
+		copy_field(in->key[in->n], line);
+		copy_field(in->val[in->n], eq + 1);
 		trim(in->key[in->n]);
 		trim(in->val[in->n]);
 		in->n++;
