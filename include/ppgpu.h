@@ -135,7 +135,8 @@ int pp_gpu_download_replica(pp_engine *e, int replica, double *r, double *R, dou
 int pp_gpu_bonds(pp_engine *e, int replica, int *n_bonds, int *n_overlaps);
 
 /* Bonded partner lists in upload order: offsets has N+1 entries, partners capacity `cap`.
- * Returns the total number of entries (sum of n_bonds) or a negative error (PP_ERR_CAPACITY if cap is short).
+ * Returns the total number of entries (sum of n_bonds) or a negative error. If cap is short the call returns
+ * PP_ERR_CAPACITY with offsets filled, so offsets[N] is the capacity needed.
  * Partners of each particle are sorted ascending (output_print_bonds lists them in cell-walk order). */
 int pp_gpu_bond_lists(pp_engine *e, int replica, int *offsets, int *partners, int cap);
 

@@ -132,10 +132,13 @@ static void save(run_t *s, long long step, const char *path) {
 
 /* output_print_bonds (output.c:213-268): N, then per particle "index n_bonds" and its partners */
 static void print_bonds(run_t *s, long long step) {
-	int n;
-	while((n = pp_gpu_bond_lists(s->e, 0, s->offsets, s->partners, s->cap)) == PP_ERR_CAPACITY) {
-		s->cap *= 2;
-		s->partners = realloc(s->partners, sizeof(int) * (size_t) s->cap);
+	int n = pp_gpu_bond_lists(s->e, 0, s->offsets, s->partners, s->cap);
+	if(n == PP_ERR_CAPACITY && s->offsets[s->N] > s->cap) { /* the partner buffer was too small: grow it once */
+		s->cap = s->offsets[s->N];
+		free(s->partners);
+		s->partners = malloc(sizeof(int) * (size_t) s->cap);
+		if(s->partners == NULL) die("out of memory");
+		n = pp_gpu_bond_lists(s->e, 0, s->offsets, s->partners, s->cap);
 	}
 	if(n < 0) die("%s", pp_gpu_last_error(s->e));
 	char name[4 * KEYLEN];
@@ -251,12 +254,14 @@ int main(int argc, char *argv[]) {
 
 	s.r = malloc(sizeof(double) * 3 * (N > 0 ? N : 1));
 	s.R = malloc(sizeof(double) * 9 * (N > 0 ? N : 1));
+	if(s.r == NULL || s.R == NULL) die("out of memory");
 	char err[512];
 	if(pp_rrr_read(conf, N, s.r, s.R, s.box, err, sizeof(err)) != PP_OK) die("%s", err);
 	s.N = N;
 	s.cap = 8 * (N > 0 ? N : 1);
-	s.offsets = malloc(sizeof(int) * (size_t) (N + 1));
+	s.offsets = calloc((size_t) N + 1, sizeof(int));
 	s.partners = malloc(sizeof(int) * (size_t) s.cap);
+	if(s.offsets == NULL || s.partners == NULL) die("out of memory");
 	if(pp_gpu_create(&p, &s.e) != PP_OK) die("%s", pp_gpu_last_error(s.e));
 	if((v = key(in, "GPU_neighbour_lists", 0))) check(&s, pp_gpu_set_neighbour_lists(s.e, atoi(v)));
 	/* the upload computes the initial energy and refuses an overlapping configuration (main.c:55-64) */

@@ -110,6 +110,12 @@ static int set_err(pp_engine *e, int code, const char *fmt, ...) {
 		if(_c != 0) return set_err(e, PP_ERR_CUDA, "kernel launch: %s", cudaGetErrorString((cudaError_t) _c)); \
 	} while(0)
 
+/* a host allocation that failed ends the call with PP_ERR_CAPACITY */
+#define HOST_OK(ptr)                                                                   \
+	do {                                                                               \
+		if((ptr) == NULL) return set_err(e, PP_ERR_CAPACITY, "out of host memory: %s", #ptr); \
+	} while(0)
+
 /* ------------------------------------------------------------------------------------------------ */
 /* small vector helpers with the reference's operation order (utils.c)                              */
 /* ------------------------------------------------------------------------------------------------ */
@@ -192,7 +198,7 @@ static int create_common(const pp_params *prms, int n, pp_engine **out) {
 	*out = NULL;
 	if(n < 1 || prms == NULL) return PP_ERR_ARG;
 	pp_engine *e = calloc(1, sizeof(pp_engine));
-	if(e == NULL) return PP_ERR_ARG;
+	if(e == NULL) return PP_ERR_CAPACITY;
 	for(int i = 0; i < n; i++) {
 		int rc = check_params(e, prms + i);
 		if(rc != PP_OK) {
@@ -201,14 +207,16 @@ static int create_common(const pp_params *prms, int n, pp_engine **out) {
 			return rc;
 		}
 	}
-	e->nrep = n;
+	*out = e; /* from here on the caller can read the message, and destroy frees what was allocated */
 	e->prm = calloc(n, sizeof(pp_params));
-	memcpy(e->prm, prms, sizeof(pp_params) * n);
 	e->N = calloc(n, sizeof(int));
 	e->h_r = calloc(n, sizeof(double *));
 	e->h_R = calloc(n, sizeof(double *));
 	e->h_box = calloc(n, sizeof(double[3]));
 	e->uploaded = calloc(n, sizeof(int));
+	if(!e->prm || !e->N || !e->h_r || !e->h_R || !e->h_box || !e->uploaded) return set_err(e, PP_ERR_CAPACITY, "out of host memory");
+	e->nrep = n;
+	memcpy(e->prm, prms, sizeof(pp_params) * n);
 	e->threads = 128;
 	e->resort_every = 4;
 	e->rounds_per_sweep = 1;
@@ -591,6 +599,8 @@ static int commit(pp_engine *e) {
 	free(e->h_rs);
 	e->h_rp = calloc(e->nrep, sizeof(ppi_rparams));
 	e->h_rs = calloc(e->nrep, sizeof(ppi_rstate));
+	HOST_OK(e->h_rp);
+	HOST_OK(e->h_rs);
 	long long cells = 0;
 	int p0 = 0;
 	for(int r = 0; r < e->nrep; r++) {
@@ -649,6 +659,11 @@ static int commit(pp_engine *e) {
 	if(rc != PP_OK) return rc;
 	int *crep = malloc(sizeof(int) * (cells > 0 ? cells : 1));
 	int *rep = malloc(sizeof(int) * n1);
+	if(crep == NULL || rep == NULL) {
+		free(crep);
+		free(rep);
+		return set_err(e, PP_ERR_CAPACITY, "out of host memory");
+	}
 	for(int r = 0; r < e->nrep; r++) {
 		ppi_rparams *rp = e->h_rp + r;
 		for(int c = 0; c < rp->cell_cap; c++) crep[rp->cell_base + c] = r;
@@ -753,6 +768,8 @@ int pp_gpu_upload_replica(pp_engine *e, int r, int N, const double *rr, const do
 	free(e->h_R[r]);
 	e->h_r[r] = malloc(sizeof(double) * 3 * (N > 0 ? N : 1));
 	e->h_R[r] = malloc(sizeof(double) * 9 * (N > 0 ? N : 1));
+	HOST_OK(e->h_r[r]);
+	HOST_OK(e->h_R[r]);
 	if(N > 0) {
 		memcpy(e->h_r[r], rr, sizeof(double) * 3 * N);
 		memcpy(e->h_R[r], RR, sizeof(double) * 9 * N);
@@ -840,6 +857,14 @@ int pp_gpu_set_timing(pp_engine *e, int enable) {
 		e->ev_cap = 3072;
 		e->ev = calloc(2 * e->ev_cap, sizeof(cudaEvent_t));
 		e->ev_kind = calloc(e->ev_cap, sizeof(int));
+		if(e->ev == NULL || e->ev_kind == NULL) {
+			free(e->ev);
+			free(e->ev_kind);
+			e->ev = NULL;
+			e->ev_kind = NULL;
+			e->ev_cap = 0;
+			return set_err(e, PP_ERR_CAPACITY, "out of host memory");
+		}
 		for(int i = 0; i < 2 * e->ev_cap; i++) CU(cudaEventCreate(&e->ev[i]));
 	}
 	if(!enable) {
@@ -1256,6 +1281,11 @@ int pp_gpu_bond_lists(pp_engine *e, int r, int *offsets, int *partners, int cap)
 	/* counts in upload order, then offsets, then the lists */
 	int *cnt = calloc(N > 0 ? N : 1, sizeof(int));
 	int *where = calloc(N > 0 ? N : 1, sizeof(int));
+	if(cnt == NULL || where == NULL) {
+		free(cnt);
+		free(where);
+		return set_err(e, PP_ERR_CAPACITY, "out of host memory");
+	}
 	for(int k = 0; k < N; k++) {
 		int i = e->pin_id[k];
 		if(i < 0 || i >= N) {
@@ -1457,7 +1487,7 @@ int pp_generate(int N, double density, int seed, int round_like_file, double *r,
 	if(head == NULL || next == NULL) {
 		free(head);
 		free(next);
-		return PP_ERR_ARG;
+		return PP_ERR_CAPACITY;
 	}
 	for(long long c = 0; c < nc; c++) head[c] = -1;
 	double bx[3] = { L, L, L };
@@ -1599,7 +1629,7 @@ int pp_gpu_learned_init(pp_engine *e, const pp_learned_params *p) {
 	e->d.lstats = e->l_stats;
 	{ /* per replica tables: the component edges and angles as the kernels' FP32 values, their densities */
 		ppi_lrep *M = calloc((size_t) e->nrep, sizeof(ppi_lrep));
-		if(!M) return set_err(e, PP_ERR_ARG, "out of host memory");
+		if(!M) return set_err(e, PP_ERR_CAPACITY, "out of host memory");
 		for(int r = 0; r < e->nrep; r++) {
 			const float dm = (float) e->prm[r].disp_max, tm = (float) e->prm[r].theta_max;
 			for(int k = 0; k < PP_MIX; k++) {
@@ -1626,7 +1656,7 @@ int pp_gpu_learned_init(pp_engine *e, const pp_learned_params *p) {
 	CU(cudaMemsetAsync(e->l_err, 0, sizeof(int), e->stream));
 	/* initial weights: uniform fan-in hidden layers, zero biases and output layer (uniform mixture) */
 	float *P = calloc(PP_MLP_NPARAMS, sizeof(float));
-	if(!P) return set_err(e, PP_ERR_ARG, "out of host memory");
+	if(!P) return set_err(e, PP_ERR_CAPACITY, "out of host memory");
 	uint64_t st = p->seed;
 	const double a1 = sqrt(6.0 / PP_MLP_IN), a2 = sqrt(6.0 / PP_MLP_HIDDEN);
 	for(int i = 0; i < PP_MLP_HIDDEN * PP_MLP_IN; i++) P[i] = (float) ((2. * u01_sm(&st) - 1.) * a1);
@@ -1763,7 +1793,7 @@ int pp_gpu_learned_train(pp_engine *e, int epochs, int tiles_per_cta, double lr,
 		e->l_tiles_cap = ntiles;
 	}
 	int *perm = malloc(sizeof(int) * (size_t) ntiles);
-	if(!perm) return set_err(e, PP_ERR_ARG, "out of host memory");
+	if(!perm) return set_err(e, PP_ERR_CAPACITY, "out of host memory");
 	int ctas = ppi_sm_count();
 	if(ctas * tiles_per_cta > ntiles) ctas = (ntiles + tiles_per_cta - 1) / tiles_per_cta;
 	const int per_step = ctas * tiles_per_cta;
@@ -1825,7 +1855,7 @@ int pp_gpu_learned_features(pp_engine *e, int r, float *features) {
 	ppi_rparams *rp = e->h_rp + r;
 	const int N = rp->N;
 	float *tmp = malloc(sizeof(float) * PP_MLP_IN * (size_t) (N > 0 ? N : 1));
-	if(!tmp) return set_err(e, PP_ERR_ARG, "out of host memory");
+	if(!tmp) return set_err(e, PP_ERR_CAPACITY, "out of host memory");
 	if(cudaMemcpyAsync(tmp, e->d.feat + (size_t) rp->p0 * PP_MLP_IN, sizeof(float) * PP_MLP_IN * (size_t) N, cudaMemcpyDeviceToHost, e->stream) != cudaSuccess ||
 			cudaMemcpyAsync(e->pin_id, e->d.id + rp->p0, sizeof(int) * N, cudaMemcpyDeviceToHost, e->stream) != cudaSuccess ||
 			cudaStreamSynchronize(e->stream) != cudaSuccess) {
