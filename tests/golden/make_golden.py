@@ -1,8 +1,9 @@
 """Regenerates the golden fixtures in tests/golden/ from the reference itself.
 
 Run from the repository root in a container where the reference sources are present
-(python tests/golden/make_golden.py [reference_dir]); it builds oracle/_ref with oracle/Makefile and runs
-the reference's own programs:
+(python tests/golden/make_golden.py [reference_dir [output_dir]]); it builds oracle/_ref with
+oracle/Makefile and runs the reference's own programs. The fixtures go to tests/golden/ unless an output
+directory is given (tests/test_golden_regen.py regenerates them into a scratch directory and compares):
 
   generator_<N>_<rho>_<seed>.rrr.gz   reference generator seeded with srand48(seed) (oracle/ref_generator_seeded.c)
   probe_<name>.txt.gz                 ref_probe: per-particle MC_energy, overlap flag, bond/overlap partners
@@ -25,6 +26,7 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, HERE)
 
 REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+OUT = sys.argv[2] if len(sys.argv) > 2 else HERE
 REFOUT = os.path.join(ROOT, "oracle", "_ref")
 
 # synthetic configurations: (name, N, density, seed) -- shapes of the benchmark configurations at sizes the
@@ -75,7 +77,8 @@ KF_cosmax = 0.92
 
 
 def gz_write(path, data):
-    with gzip.open(path, "wb", compresslevel=9) as f:
+    """gzip with a zero timestamp, so that regenerating a fixture reproduces its bytes"""
+    with open(path, "wb") as raw, gzip.GzipFile(filename="", mode="wb", compresslevel=9, fileobj=raw, mtime=0) as f:
         f.write(data)
 
 
@@ -87,18 +90,18 @@ def main():
     # shipped reference fixtures
     for name in ("fcc.rrr", "bcc.rrr"):
         shutil.copy(os.path.join(REF, name), os.path.join(work, name))
-        gz_write(os.path.join(HERE, name + ".gz"), open(os.path.join(REF, name), "rb").read())
+        gz_write(os.path.join(OUT, name + ".gz"), open(os.path.join(REF, name), "rb").read())
     # generated configurations
     for name, N, rho, seed in GENERATED:
         subprocess.check_call([os.path.join(REFOUT, "generator_seeded"), str(N), str(rho), str(seed)], cwd=work, stderr=subprocess.DEVNULL)
         fn = "generator_%d_%s_%d.rrr" % (N, rho, seed)
         os.rename(os.path.join(work, "generated.rrr"), os.path.join(work, fn))
         if N <= 1000:
-            gz_write(os.path.join(HERE, fn + ".gz"), open(os.path.join(work, fn), "rb").read())
+            gz_write(os.path.join(OUT, fn + ".gz"), open(os.path.join(work, fn), "rb").read())
     # adversarial pairs
     r, R, box = adversarial.build(n_pairs=1500)
     adversarial.write_rrr17(os.path.join(work, "adversarial.rrr"), r, R, box)
-    gz_write(os.path.join(HERE, "adversarial.rrr.gz"), open(os.path.join(work, "adversarial.rrr"), "rb").read())
+    gz_write(os.path.join(OUT, "adversarial.rrr.gz"), open(os.path.join(work, "adversarial.rrr"), "rb").read())
     # per-particle probes
     probes = [("fcc", "fcc.rrr"), ("bcc", "bcc.rrr"), ("adversarial", "adversarial.rrr")]
     probes += [(name, "generator_%d_%s_%d.rrr" % (N, rho, seed)) for name, N, rho, seed in GENERATED]
@@ -106,7 +109,7 @@ def main():
         inp = os.path.join(work, "probe_input")
         open(inp, "w").write(PROBE_INPUT.format(conf=conf))
         out = subprocess.check_output([os.path.join(REFOUT, "ref_probe"), inp], cwd=work, stderr=subprocess.DEVNULL)
-        gz_write(os.path.join(HERE, "probe_%s.txt.gz" % name), out)
+        gz_write(os.path.join(OUT, "probe_%s.txt.gz" % name), out)
     # trajectories of the reference main loop
     for name, conf, ens, T, steps, pe, seed, extra in TRAJ:
         d = os.path.join(work, name)
@@ -114,7 +117,7 @@ def main():
         shutil.copy(os.path.join(work, conf), os.path.join(d, conf))
         open(os.path.join(d, "input"), "w").write(TRAJ_INPUT.format(ensemble=ens, seed=seed, T=T, steps=steps, print_every=pe, save_every=pe * 2, conf=conf, extra=extra))
         out = subprocess.check_output([os.path.join(REFOUT, "PatchyParticles"), "input"], cwd=d, stderr=subprocess.DEVNULL)
-        dst = os.path.join(HERE, "traj_" + name)
+        dst = os.path.join(OUT, "traj_" + name)
         os.makedirs(dst, exist_ok=True)
         open(os.path.join(dst, "input"), "w").write(TRAJ_INPUT.format(ensemble=ens, seed=seed, T=T, steps=steps, print_every=pe, save_every=pe * 2, conf=conf, extra=extra))
         open(os.path.join(dst, "stdout.txt"), "wb").write(out)
@@ -123,7 +126,7 @@ def main():
                 shutil.copy(os.path.join(d, fn), os.path.join(dst, fn))
         gz_write(os.path.join(dst, "last.rrr.gz"), open(os.path.join(d, "last.rrr"), "rb").read())
     shutil.rmtree(work)
-    print("golden fixtures written to", HERE)
+    print("golden fixtures written to", OUT)
 
 
 if __name__ == "__main__":
