@@ -71,7 +71,11 @@ static void read_input(input_t *in, const char *path) {
 		strip(line);
 		if(line[0] == '\0' || line[0] == '#') continue;
 		char *eq = strchr(line, '=');
-		if(eq == NULL || in->n == MAXKEYS) continue;
+		if(eq == NULL) {
+			fprintf(stderr, "WARNING: malformed line '%s'\n", line); /* as loadInput does (parse_input.c:30-87) */
+			continue;
+		}
+		if(in->n == MAXKEYS) continue;
 		*eq = '\0';
 		snprintf(in->key[in->n], KEYLEN, "%.*s", KEYLEN - 1, line);
 		snprintf(in->val[in->n], KEYLEN, "%.*s", KEYLEN - 1, eq + 1);
