@@ -817,7 +817,7 @@ __device__ __forceinline__ void flush_block(const ppi_dev &d, Acc &A) {
 }
 
 /* ------------------------------------------------------------------------------------------------ */
-/* one checkerboard colour: one attempt per non-empty cell of that colour, 32 attempts per warp      */
+/* one checkerboard colour: one attempt per non-empty cell of that colour, 64 attempts per warp      */
 /* ------------------------------------------------------------------------------------------------ */
 /* Kernel modes of the colour and energy passes:
  *   MODE_FAST  pair tests in FP32; a pair inside the guard band is re-evaluated exactly (FP64, out of
