@@ -39,13 +39,13 @@ BYTES_PER_ATTEMPT = 192
 
 WORKLOADS = {
     "c5": dict(N=1048576, rho=0.3, T=0.11, P=0.05, ensemble=5, rescale=0.01, disp=0.05, theta=0.1, seed=1005,
-               name="N=1048576 NPT rho0=0.3 T=0.11 P=0.05 rescale_factor_max=0.01, plain roto-translation, FP32+guard"),
+               name="N=1048576 NPT rho0=0.3 T=0.11 P=0.05 rescale_factor_max=0.01, plain roto-translation"),
     "c2": dict(N=32768, rho=0.5, T=0.13, P=0.0, ensemble=0, rescale=0.01, disp=0.05, theta=0.1, seed=1002,
-               name="N=32768 NVT rho=0.5 T=0.13, FP32+guard"),
+               name="N=32768 NVT rho=0.5 T=0.13, plain roto-translation"),
     "c4": dict(N=32768, rho=0.1, T=0.09, P=0.0, ensemble=0, rescale=0.01, disp=0.05, theta=0.1, seed=1004,
-               name="N=32768 NVT rho=0.1 T=0.09, plain proposal, FP32+guard"),
+               name="N=32768 NVT rho=0.1 T=0.09, plain roto-translation"),
     "c1": dict(N=1000, rho=0.1, T=0.12, P=0.0, ensemble=0, rescale=0.01, disp=0.05, theta=0.1, seed=1001,
-               name="N=1000 NVT rho=0.1 T=0.12, FP32+guard"),
+               name="N=1000 NVT rho=0.1 T=0.12, plain roto-translation"),
 }
 
 
@@ -218,9 +218,17 @@ def run_batch(args, ws, rank, local, dist):
 
 
 def make_config(wl, seed_offset=0):
+    """The workload's seeded random insertion, built by the product's generator (the GPU arm)."""
     import patchyparticles_gb300 as pp
 
     return pp.generate(wl["N"], wl["rho"], wl["seed"] + seed_offset, round_like_file=False)
+
+
+def workload_config(wl, args):
+    """The `config` object of both arms' lines: the workload alone (no implementation detail), so that the
+    GPU line and the reference line describe the same thing."""
+    return {"workload": wl["name"], "N": wl["N"], "sweeps_per_step": args.sweeps_per_step, "proposal": "plain",
+            "l2": "inputs larger than L2 (FP64 state %.0f MB + FP32 mirror %.0f MB per GPU)" % (wl["N"] * 128 / 1e6, wl["N"] * 64 / 1e6)}
 
 
 def cpu_reference_impl():
@@ -248,11 +256,13 @@ def cpu_throughput(wl, r, R, box, seconds, threads, samples=1):
 def run_reference(args, wl, ws, rank, dist):
     if rank != 0:
         return
-    r, R, box = make_config(wl)
     threads = os.cpu_count() or 1
     from oracle import pyoracle as po
 
     po.build(with_reference=False)
+    # the input comes from the oracle's restatement of the reference generator (generator.c:43-68), which
+    # equals the product's generator bit for bit: nothing of the GPU engine is loaded on this arm
+    r, R, box = po.generate(wl["N"], wl["rho"], wl["seed"])
     prm = po.params(ensemble=wl["ensemble"], T=wl["T"], P=wl["P"], disp_max=wl["disp"], theta_max=wl["theta"],
                     rescale_factor_max=wl["rescale"], seed=wl["seed"])
     pool = po.Pool(r, R, box, prm, threads)
@@ -268,10 +278,13 @@ def run_reference(args, wl, ws, rank, dist):
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * el / max(1, args.steps), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random insertion)",
-        "config": {"workload": wl["name"], "N": wl["N"], "sample": "one continuous %.1f s all-core sample over the %d steps" % (el, args.steps)},
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random insertion, uniform orientations)",
+        "config": workload_config(wl, args),
+        "implementation": "the reference's sequential CPU Monte Carlo (MC.c do_NVT/do_NPT) as restated by the oracle (oracle/pp_oracle.c, "
+                          "trajectories byte-identical to the reference built from its sources); every pair test in FP64",
+        "sample": "one continuous %.1f s all-core sample over the %d steps" % (el, args.steps),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": cpu_reference_impl(),
-                         "sample": "%d independent %d-particle systems, %.1f s" % (threads, wl["N"], el)},
+                         "sample": "%d independent %d-particle systems (one per host thread), %.1f s" % (threads, wl["N"], el)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -373,11 +386,11 @@ def run_gpu(args, wl, ws, rank, local, dist):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * t_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic (seeded random insertion, uniform orientations)",
-        "config": {"workload": wl["name"] if args.precision != "fp64" else wl["name"].replace("FP32+guard", "FP64 pair tests"), "N": wl["N"],
-                   "precision": args.precision, "sweeps_per_step": spsw, "proposal": "plain",
-                   "l2": "inputs larger than L2 (FP64 state %.0f MB + FP32 mirror %.0f MB per GPU)" % (wl["N"] * 128 / 1e6, wl["N"] * 64 / 1e6),
-                   "parallelism": "replicas" if ws > 1 else "single GPU", "launch": "CUDA graph per re-sort period, programmatic dependent launch between its kernels",
-                   "schedule": tune if tune else "defaults (resort_every 4, reorder_every 16, cell_scale 1.0)"},
+        "config": workload_config(wl, args),
+        "precision": "FP64 pair tests" if args.precision == "fp64" else "FP32 pair tests with the FP64 guard band (eps 1e-5), FP64 state",
+        "parallelism": "independent replicas, one per GPU" if ws > 1 else "single GPU",
+        "launch": "CUDA graph per re-sort period, programmatic dependent launch between its kernels",
+        "schedule": tune if tune else "defaults (resort_every 4, reorder_every 16, cell_scale 1.0)",
         "acceptance": acc[pp.MOVE_ROTO_TRASL] / max(1, tries[pp.MOVE_ROTO_TRASL]),
         "volume_acceptance": acc[pp.MOVE_VOLUME] / max(1, tries[pp.MOVE_VOLUME]) if tries[pp.MOVE_VOLUME] else None,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -496,6 +509,18 @@ def _sum_op(dist):
     return dist.ReduceOp.SUM
 
 
+def _spawn_ranks(n):
+    """Runs this command as n ranks on this node (127.0.0.1 rendezvous) and returns their exit status."""
+    import socket
+
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", str(n), "--master-addr", "127.0.0.1",
+           "--master-port", str(port), os.path.abspath(sys.argv[0])] + sys.argv[1:]
+    return subprocess.call(cmd)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -524,6 +549,13 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # one rank per GPU: relaunch this command under torch.distributed.run (each rank runs an independent
+        # replica; rank 0 prints the aggregate line)
+        sys.exit(_spawn_ranks(args.gpus))
+    ws_env = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws_env != args.gpus:
+        sys.exit("bench.py: --gpus %d but WORLD_SIZE=%d: launch one rank per GPU" % (args.gpus, ws_env))
     wl = WORKLOADS.get(args.workload, WORKLOADS["c2"])
     ws, rank, local, dist = dist_setup()
     if args.impl == "reference":

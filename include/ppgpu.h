@@ -189,15 +189,24 @@ int pp_gpu_time_sweeps(pp_engine *e, long long n, double *ms);
  * (main.c:55-64 semantics; -bonds) and *overlap whether any pair overlaps. Model: KF_delta, KF_cosmax,
  * FP32 pair tests with the FP64 guard band (eps = 1e-5), bit-identical decisions to the reference.
  *
- * Nothing is allocated: all scratch (cell grid, sort buffers, working records) lives in one static
- * device array of about 11.2 MiB, which every GPU that loads the library holds until the process exits.
+ * Nothing is allocated by the call: all scratch (cell grid, sort buffers, working records) lives in one
+ * static device array of about 11.2 MiB. The array comes into existence when the library's kernel module
+ * is loaded on a device -- under CUDA's lazy module loading (the default) that is the first engine or
+ * pp_gpu_energy_noalloc call on that device -- and stays until the process exits. A caller on a tight
+ * device-memory budget should therefore make one call at start-up, outside that budget; a failure to
+ * load the module there is reported as PP_ERR_CUDA "cudaGetSymbolAddress".
  * Limits: N <= 32768 particles and at most 131072 cells (even cell count >= 4 per axis, cell edge >=
  * 1 + KF_delta, i.e. roughly a 57^3 box at delta = 0.12); larger inputs return PP_ERR_CAPACITY with a
- * message in err (err may be NULL). The first call on a device looks up the array's device address with
- * cudaGetSymbolAddress (once per device); make that first call before any stream capture. Calls share
- * the array and run on the legacy default stream and return after the result is on the host: calls that
- * overlap on the GPU (from several host threads) race on the shared scratch and must be serialised by
- * the caller. Returns PP_OK, PP_ERR_ARG, PP_ERR_CAPACITY or PP_ERR_CUDA. */
+ * message in err (err may be NULL). N = 0 is valid (E = 0, no overlap).
+ * Every call looks up the array's device address with cudaGetSymbolAddress, with the calling thread's
+ * current device and context, so a device reset between calls is harmless.
+ * Streams: a call copies with cudaMemcpy/cudaMemset and launches on the legacy default stream, and
+ * returns after the result is on the host. No call may be made while any stream of the process is being
+ * captured. Inputs written on a non-blocking stream (cudaStreamNonBlocking, e.g. a framework's pooled
+ * side streams) are not ordered before the call's reads: synchronise those producers first. Calls share
+ * the array, which keeps the last call's contents (each call writes everything it reads): calls that
+ * overlap on the GPU (from several host threads) race on it and must be serialised by the caller.
+ * Returns PP_OK, PP_ERR_ARG, PP_ERR_CAPACITY or PP_ERR_CUDA. */
 int pp_gpu_energy_noalloc(int N, const double *r_dev, const double *R_dev, const double box[3], double kf_delta, double kf_cosmax,
 		int *n_bonds_dev, int *n_overlaps_dev, double *E, int *overlap, char *err, int err_len);
 

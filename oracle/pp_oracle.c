@@ -87,6 +87,96 @@ static void o_gram_schmidt(double *v1, double *v2, double *v3) { /* utils.c:91-1
 	o_normalize(v3);
 }
 
+static void o_random_vector_on_sphere(orc_system *s, double *res);
+
+/* determinant (utils.c:78-89), same term order */
+static double o_determinant(const double *m) {
+	double det = 0.;
+	det += m[0] * m[4] * m[8];
+	det += m[1] * m[5] * m[6];
+	det += m[2] * m[3] * m[7];
+	det -= m[2] * m[4] * m[6];
+	det -= m[0] * m[5] * m[7];
+	det -= m[1] * m[3] * m[8];
+	return det;
+}
+
+/* random_orientation (utils.c:133-169): three vectors on the sphere, Gram-Schmidt, rows (v3, v1, v2),
+ * rows 0 and 1 swapped back when the determinant is negative */
+static void o_random_orientation(orc_system *s, double *R) {
+	double v1[3], v2[3], v3[3];
+	o_random_vector_on_sphere(s, v1);
+	o_random_vector_on_sphere(s, v2);
+	o_random_vector_on_sphere(s, v3);
+	o_gram_schmidt(v1, v2, v3);
+	memcpy(R, v3, sizeof(v3));
+	memcpy(R + 3, v1, sizeof(v1));
+	memcpy(R + 6, v2, sizeof(v2));
+	if(o_determinant(R) < 0.) {
+		memcpy(R, v1, sizeof(v1));
+		memcpy(R + 3, v3, sizeof(v3));
+	}
+}
+
+/* make_initial_conf (generator.c:43-68) with main's box (generator.c:99-105), random numbers from
+ * srand48(seed): uniform insertion in a cubic box of side (N / density)^(1/3), rejected when it overlaps
+ * (r^2 < 1) an inserted particle in the 27 cells of edge >= 1 around it (cells.c:17-49), orientation from
+ * random_orientation. Returns 0, or -1 for density outside (0, 0.7] (generator.c:99-102) or no memory. */
+int orc_generate(int N, double density, int seed, double *r, double *R, double box[3]) {
+	if(N < 0 || !(density > 0.) || density > 0.7) return -1;
+	const double L = pow(N / density, 1. / 3.);
+	orc_system g;
+	orc_seed(&g, seed);
+	int ns = (int) floor(L / 1.);
+	if(ns < 3) ns = 3;
+	const long long nc = (long long) ns * ns * ns;
+	int *head = malloc(sizeof(int) * nc), *next = malloc(sizeof(int) * (N > 0 ? N : 1));
+	if(head == NULL || next == NULL) {
+		free(head);
+		free(next);
+		return -1;
+	}
+	for(long long c = 0; c < nc; c++) head[c] = -1;
+	const double b[3] = { L, L, L };
+	int inserted = 0;
+	while(inserted < N) {
+		double p[3];
+		p[0] = orc_drand(&g) * L;
+		p[1] = orc_drand(&g) * L;
+		p[2] = orc_drand(&g) * L;
+		int ind[3];
+		for(int k = 0; k < 3; k++) ind[k] = (int) ((p[k] / b[k] - floor(p[k] / b[k])) * (1. - DBL_EPSILON) * ns);
+		int overlap = 0;
+		for(int j = -1; j < 2 && !overlap; j++)
+			for(int k = -1; k < 2 && !overlap; k++)
+				for(int l = -1; l < 2 && !overlap; l++) {
+					const int cx = (ind[0] + j + ns) % ns, cy = (ind[1] + k + ns) % ns, cz = (ind[2] + l + ns) % ns;
+					for(int q = head[((long long) cx * ns + cy) * ns + cz]; q != -1; q = next[q]) {
+						double d[3];
+						for(int a = 0; a < 3; a++) {
+							d[a] = r[3 * (size_t) q + a] - p[a];
+							d[a] -= b[a] * rint(d[a] / b[a]);
+						}
+						if(O_SCALAR(d, d) < 1.) {
+							overlap = 1;
+							break;
+						}
+					}
+				}
+		if(overlap) continue;
+		o_random_orientation(&g, R + 9 * (size_t) inserted);
+		memcpy(r + 3 * (size_t) inserted, p, sizeof(p));
+		const int c = (ind[0] * ns + ind[1]) * ns + ind[2];
+		next[inserted] = head[c];
+		head[c] = inserted;
+		inserted++;
+	}
+	free(head);
+	free(next);
+	box[0] = box[1] = box[2] = L;
+	return 0;
+}
+
 /* patches[i] = R . base[i] with the MATRIX_VECTOR_MULTIPLICATION order (utils.h:17-21) */
 static void o_set_patches(orc_system *s, int p) {
 	const double *R = s->R + 9 * p;

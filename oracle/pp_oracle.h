@@ -86,6 +86,11 @@ int orc_check_energy(orc_system *s);
 /* output_save (output.c:302-317). Returns 0 or -1. */
 int orc_save_rrr(const orc_system *s, long long step, const char *path);
 
+/* The reference generator's random sequential insertion (generator.c:43-68, 99-105) with srand48(seed):
+ * r (N x 3), R (N x 9 rows) and the cubic box, unrounded (generated.rrr holds them printed with %lf /
+ * %.12lf). Returns 0, or -1 for a density outside (0, 0.7] or no memory. */
+int orc_generate(int N, double density, int seed, double *r, double *R, double box[3]);
+
 /* drand48 recurrence check: n draws from a generator seeded as srand48(seed) would be. */
 void orc_drand48_sequence(int seed, int n, double *out);
 

@@ -37,10 +37,20 @@ class OrcParams(ctypes.Structure):
     ]
 
 
+def reference_dir():
+    """Directory of the reference's C sources: $PP_REFERENCE_DIR, else a checkout named `reference` beside
+    this repository; None where neither holds them (e.g. on a machine that only runs the GPU tests)."""
+    for d in (os.environ.get("PP_REFERENCE_DIR"), os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")):
+        if d and os.path.isfile(os.path.join(d, "MC.c")):
+            return os.path.abspath(d)
+    return None
+
+
 def build(with_reference=True):
     subprocess.check_call(["make", "-s", "-C", HERE, "port"])
-    if with_reference:
-        subprocess.check_call(["make", "-s", "-C", HERE, "ref"])
+    ref = reference_dir() if with_reference else None
+    if ref is not None:
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref", "REF=" + ref])
 
 
 _lib = None
@@ -78,6 +88,7 @@ def lib():
             "orc_check_energy": (ctypes.c_int, [vp]),
             "orc_save_rrr": (ctypes.c_int, [vp, ctypes.c_longlong, ctypes.c_char_p]),
             "orc_drand48_sequence": (None, [ctypes.c_int, ctypes.c_int, dp]),
+            "orc_generate": (ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_int, dp, dp, dp]),
             "orc_parallel_throughput": (ctypes.c_double, [ctypes.c_int, dp, dp, dp, ctypes.POINTER(OrcParams), ctypes.c_int, ctypes.c_double, llp]),
             "orc_pool_create": (vp, [ctypes.c_int, dp, dp, dp, ctypes.POINTER(OrcParams), ctypes.c_int]),
             "orc_pool_run": (ctypes.c_double, [vp, ctypes.c_double, llp]),
@@ -200,6 +211,26 @@ class System:
 
     def save(self, path, step=0):
         return self.L.orc_save_rrr(self.h, step, path.encode())
+
+
+def generate(N, density, seed):
+    """The reference generator's seeded random sequential insertion (generator.c:43-68): (r, R, box)."""
+    r = np.zeros((N, 3))
+    R = np.zeros((N, 9))
+    b = np.zeros(3)
+    if lib().orc_generate(N, density, seed, _dp(r), _dp(R), _dp(b)) != 0:
+        raise ValueError("density must be in (0, 0.7]")
+    return r, R, b
+
+
+def generated_text(r, R, box):
+    """generated.rrr as the reference generator prints it (generator.c:70-82)."""
+    out = ["0 %d %f %f %f" % (len(r), box[0], box[1], box[2])]
+    for i in range(len(r)):
+        out.append("%f %f %f" % tuple(R[i, 0:3]))
+        out.append("%f %f %f" % tuple(R[i, 3:6]))
+        out.append("%.12f %.12f %.12f" % tuple(r[i]))
+    return "\n".join(out) + "\n"
 
 
 def drand48_sequence(seed, n):

@@ -3944,11 +3944,9 @@ extern "C" int ppi_export(const ppi_dev *d, int first, int count, cudaStream_t s
 #define NA_TOTAL (NA_GRID + NA_ALIGN(sizeof(ppi_grid)))
 
 /* The scratch. Host code must not use its name as an address: the device address comes from
- * cudaGetSymbolAddress (g_noalloc_base, once per device). */
+ * cudaGetSymbolAddress, looked up on every call with the caller's device and context current (an address
+ * kept from an earlier call could belong to a context that a cudaDeviceReset has since destroyed). */
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_TOTAL];
-
-#define NOALLOC_MAX_DEVICES 64
-static void *g_noalloc_base[NOALLOC_MAX_DEVICES];
 
 __global__ void k_noalloc_pack(ppi_dev d, const double *r, const double *R) {
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -4001,18 +3999,12 @@ extern "C" int pp_gpu_energy_noalloc(int N, const double *r_dev, const double *R
 	rp.cell_base = 0;
 	rp.cell_cap = (int) cells;
 	rp.p0 = 0;
-	/* device address of the scratch, looked up once per device with that device current */
-	int dev = 0;
-	cudaError_t c = cudaGetDevice(&dev);
-	if(c != cudaSuccess) return na_fail(err, err_len, PP_ERR_CUDA, "cudaGetDevice", cudaGetErrorString(c));
-	if(dev < 0 || dev >= NOALLOC_MAX_DEVICES) return na_fail(err, err_len, PP_ERR_CUDA, "device ordinal out of range", NULL);
-	if(g_noalloc_base[dev] == NULL) {
-		void *p = NULL;
-		c = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-		if(c != cudaSuccess || p == NULL) return na_fail(err, err_len, PP_ERR_CUDA, "cudaGetSymbolAddress", cudaGetErrorString(c));
-		g_noalloc_base[dev] = p;
-	}
-	unsigned char *base = (unsigned char *) g_noalloc_base[dev];
+	/* device address of the scratch in the current device's current context, looked up on every call
+	 * (a table lookup once the module is loaded; the first call on a device loads it) */
+	void *sym = NULL;
+	cudaError_t c = cudaGetSymbolAddress(&sym, g_noalloc_scratch);
+	if(c != cudaSuccess || sym == NULL) return na_fail(err, err_len, PP_ERR_CUDA, "cudaGetSymbolAddress", cudaGetErrorString(c));
+	unsigned char *base = (unsigned char *) sym;
 	ppi_dev d;
 	memset(&d, 0, sizeof(d));
 	d.nrep = 1;

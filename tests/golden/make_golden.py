@@ -25,7 +25,11 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, HERE)
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+from oracle.pyoracle import reference_dir  # noqa: E402
+
+REF = sys.argv[1] if len(sys.argv) > 1 else reference_dir()
+if REF is None:
+    sys.exit("reference sources not found: pass their directory or set PP_REFERENCE_DIR")
 OUT = sys.argv[2] if len(sys.argv) > 2 else HERE
 REFOUT = os.path.join(ROOT, "oracle", "_ref")
 

@@ -117,3 +117,32 @@ def test_driver_input_errors(built, edit, code, msg):
     p = subprocess.run([CLI, "input"], cwd=work, capture_output=True, text=True, timeout=60)
     assert p.returncode == code and msg in p.stderr, p.stderr
     shutil.rmtree(work)
+
+
+@pytest.mark.gpu
+def test_sigterm_stops_between_output_blocks_and_writes_the_last_configuration(built):
+    """main.c:15-39: SIGTERM sets the stop flag; the loop ends after the current block of sweeps, the final
+    configuration and line are written and the exit status is 0."""
+    import signal
+
+    src, work = _prepare("small_nvt", lambda t: t.replace("Steps = 200", "Steps = 1000000000").replace("Print_every = 20", "Print_every = 200")
+                         .replace("Save_every = 40", "Save_every = 1000000"))
+    p = subprocess.Popen([CLI, "input"], cwd=work, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+    lines = []
+    try:
+        while len(lines) < 3:  # in the main loop: the handler is installed and several blocks have run
+            line = p.stdout.readline()
+            assert line, p.stderr.read()
+            lines.append(line)
+        p.send_signal(signal.SIGTERM)
+        out, err = p.communicate(timeout=120)
+    finally:
+        if p.poll() is None:
+            p.kill()
+    assert p.returncode == 0, err
+    lines += out.splitlines()
+    final = int(lines[-1].split()[0])
+    assert 400 <= final < 1000000000 and final % 200 == 0
+    last = open(os.path.join(work, "last.rrr")).read().splitlines()
+    assert int(last[0].split()[0]) == final and int(last[0].split()[1]) == 300 and len(last) == 1 + 3 * 300
+    shutil.rmtree(work)

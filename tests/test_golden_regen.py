@@ -1,7 +1,7 @@
 """The committed golden fixtures are the reference's own outputs: tests/golden/make_golden.py rebuilds the
 reference from its sources (oracle/Makefile), reruns its programs into a scratch directory, and every
 fixture it writes must equal the committed one byte for byte. Runs only where the reference sources are
-present (the container that builds the oracle from them)."""
+present (oracle.pyoracle.reference_dir())."""
 import filecmp
 import os
 import shutil
@@ -13,7 +13,9 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-REF = os.environ.get("PP_REFERENCE_DIR", "/root/reference")
+from oracle.pyoracle import reference_dir
+
+REF = reference_dir()
 
 
 def fixture_files(top):
@@ -27,7 +29,7 @@ def fixture_files(top):
     return sorted(out)
 
 
-@pytest.mark.skipif(not os.path.isfile(os.path.join(REF, "MC.c")), reason="reference sources not present")
+@pytest.mark.skipif(REF is None or not os.path.isfile(os.path.join(REF, "MC.c")), reason="reference sources not present")
 def test_fixtures_regenerate_byte_for_byte():
     out = tempfile.mkdtemp(prefix="ppgolden_")
     try:

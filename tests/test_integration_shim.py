@@ -1,9 +1,9 @@
-"""The reference-side shim shown in INTEGRATION.md compiles against the reference's own headers and this
-repository's C-ABI header, and links against the reference's own library sources and libppgpu.so (the
-binding a maintainer would add). Runs only where the reference sources are present (the container that
-builds the oracle from them); it compiles and links them, never runs them."""
+"""The reference-side shim (patchyparticles_gb300/csrc/ppgpu_reference_shim.c, the binding a maintainer
+adds to the reference as gpu_ensemble.c) compiles against the reference's own headers and this
+repository's C-ABI header, and links against the reference's own library sources and libppgpu.so. Runs
+only where the reference sources are present (oracle.pyoracle.reference_dir()); it compiles and links
+them, never runs them."""
 import os
-import re
 import shutil
 import subprocess
 import tempfile
@@ -11,7 +11,9 @@ import tempfile
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("PP_REFERENCE_DIR", "/root/reference")
+from oracle.pyoracle import reference_dir
+
+REF = reference_dir()
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 # the reference's library sources (makefile.common's object list without main.o)
 REF_LIB_SRC = ["parse_input.c", "output.c", "system.c", "MC.c", "utils.c", "avb.c", "vmmc.c", "cells.c"]
@@ -31,15 +33,11 @@ int main(int argc, char *argv[]) {
 }
 """
 
-needs_ref = pytest.mark.skipif(not os.path.isfile(os.path.join(REF, "defs.h")), reason="reference sources not present")
+needs_ref = pytest.mark.skipif(REF is None or not os.path.isfile(os.path.join(REF, "defs.h")), reason="reference sources not present")
 
 
 def shim_source():
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    blocks = re.findall(r"```c\n(.*?)```", text, re.S)
-    shim = [b for b in blocks if "gpu_do_ensemble" in b]
-    assert shim, "the shim is missing from INTEGRATION.md"
-    return shim[0]
+    return open(os.path.join(ROOT, "patchyparticles_gb300", "csrc", "ppgpu_reference_shim.c")).read()
 
 
 def gcc(args):

@@ -1,11 +1,14 @@
 """The multi-rank path of bench.py on the CPU: two gloo ranks reduce the timing (the maximum of the elapsed
-time, the sum of the attempts, as every rank runs an independent replica), and the reference arm under
-torch.distributed.run, where rank 0 alone measures and prints one line and the other rank exits cleanly."""
+time, the sum of the attempts, as every rank runs an independent replica); the GPU arm's whole multi-rank
+path with the engine replaced by a host-side stand-in (tests/multirank_bench_runner.py); `--gpus 2`
+without torchrun spawning its own ranks; and the reference arm under torch.distributed.run, where rank 0
+alone measures and prints one line and the other rank exits cleanly."""
 import json
 import os
 import socket
 import subprocess
 import sys
+import tempfile
 
 import pytest
 
@@ -52,3 +55,34 @@ def test_reference_arm_under_torchrun():
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0 and d["cpu_baseline"]["cores"] >= 1
+
+
+def test_gpu_arm_aggregates_two_ranks_with_distinct_seeds():
+    out = tempfile.mkdtemp(prefix="ppmr_")
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2", "--master-addr", "127.0.0.1", "--master-port",
+           str(_free_port()), os.path.join("tests", "multirank_bench_runner.py"), "--gpus", "2", "--steps", "4", "--warmup", "3",
+           "--no-e2e", "--no-learned", "--no-cpu-baseline", "--tune-sweeps", "0", "--roofline-sweeps", "1"]
+    p = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600, env=dict(os.environ, PP_FAKE_OUT=out))
+    assert p.returncode == 0, p.stderr[-3000:]
+    lines = [l for l in p.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1, p.stdout[-2000:]
+    d = json.loads(lines[0])
+    # rank r: (1000 + r) attempts per sweep, 0.5 (1 + r) ms per sweep; value = all attempts / slowest rank
+    assert d["n_gpus"] == 2 and d["steps"] == 4 and d["scaling"] == "weak"
+    assert abs(d["value"] - (4 * 1000 + 4 * 1001) / 0.004) < 1e-6 * d["value"]
+    assert abs(d["ms_per_step"] - 1.0) < 1e-9
+    seen = [json.load(open(os.path.join(out, "rank%d.json" % r))) for r in (0, 1)]
+    assert [s["device"] for s in seen] == [0, 1]
+    assert seen[0]["engine_seeds"] != seen[1]["engine_seeds"] and seen[0]["generate_seeds"] != seen[1]["generate_seeds"]
+
+
+def test_gpus_flag_without_torchrun_spawns_its_ranks():
+    out = tempfile.mkdtemp(prefix="ppmr_")
+    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")}
+    env["PP_FAKE_OUT"] = out
+    cmd = [sys.executable, os.path.join("tests", "multirank_bench_runner.py"), "--gpus", "2", "--steps", "2", "--warmup", "3",
+           "--no-e2e", "--no-learned", "--no-cpu-baseline", "--tune-sweeps", "0", "--roofline-sweeps", "1"]
+    p = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600, env=env)
+    assert p.returncode == 0, p.stderr[-3000:]
+    lines = [l for l in p.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1 and json.loads(lines[0])["n_gpus"] == 2

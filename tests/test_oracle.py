@@ -79,3 +79,27 @@ def test_check_energy_orthonormalises(built):
     _, R2 = s.state()
     M = R2.reshape(-1, 3, 3)
     assert np.allclose(np.einsum("nij,nkj->nik", M, M), np.eye(3), atol=1e-14)
+
+
+@pytest.mark.parametrize("N,rho,seed", [(300, 0.3, 4242), (1000, 0.1, 1001)])
+def test_oracle_generator_prints_the_reference_generators_file(built, N, rho, seed):
+    """orc_generate (generator.c:43-68 restated) against the seeded reference generator's own output."""
+    import gzip
+
+    want = gzip.open(helpers.golden_path("generator_%d_%s_%d.rrr.gz" % (N, rho, seed)), "rt").read()
+    r, R, box = po.generate(N, rho, seed)
+    assert po.generated_text(r, R, box) == want
+
+
+def test_oracle_generator_equals_the_products(built):
+    """The reference arm of bench.py builds its inputs with the oracle's generator, the GPU arm with the
+    product's: both must give the same configuration bit for bit."""
+    import patchyparticles_gb300 as pp
+
+    for N, rho, seed in ((2000, 0.3, 1005), (500, 0.6, 7)):
+        a = po.generate(N, rho, seed)
+        b = pp.generate(N, rho, seed, round_like_file=False)
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
+    with pytest.raises(ValueError):
+        po.generate(10, 0.75, 1)
