@@ -165,6 +165,20 @@ int pp_gpu_kernel_stats(pp_engine *e, pp_kernel_stats *out, int reset);
  * off (every kernel launched on the stream); per-group event timing always uses stream launches. */
 int pp_gpu_set_graphs(pp_engine *e, int enable);
 
+/* Plain rounds over the neighbour lists as one persistent cooperative kernel (enable = 1): the 8 colours
+ * of a round (the 8 sublattice passes of do_NVT/do_NPT's sweep, MC.c:19-29, 60-68) in one launch, with
+ * a grid barrier between colours. enable = 0 (the default) launches one kernel per colour. The
+ * trajectory is the same bit for bit either way. */
+int pp_gpu_set_persistent(pp_engine *e, int enable);
+
+/* Failure-detection hook of that kernel's grid barrier (no counterpart in the reference). limit_cycles:
+ * SM clock cycles a barrier wait may spin before it gives up (0 = the default, about one second).
+ * unreachable = 1 makes the first barrier of every round wait for one arrival more than the grid makes,
+ * so every wait runs out: the kernel returns early and the next call that reads the engine's state
+ * (counters, energy, download) returns PP_ERR_CUDA, "grid barrier wait timed out". The engine's state is
+ * then incomplete; destroy it. The GPU stays usable: no wait is unbounded. */
+int pp_gpu_set_barrier_test(pp_engine *e, long long limit_cycles, int unreachable);
+
 /* Per-epoch neighbour lists (default on). Between two re-sorts no particle leaves its cell and each moves
  * at most once per round, so after every re-sort each particle's candidates in the 27 surrounding cells
  * that lie closer than a radius covering the epoch's largest possible motion (and, for NPT, its accepted

@@ -132,6 +132,7 @@ EXPORTED = [
     "pp_gpu_learned_set_weights", "pp_gpu_learned_get_weights", "pp_gpu_set_proposal", "pp_gpu_learned_collect",
     "pp_gpu_learned_train", "pp_gpu_learned_samples", "pp_gpu_learned_clear_samples", "pp_gpu_learned_features",
     "pp_gpu_learned_stats", "pp_gpu_autotune", "pp_gpu_set_graphs", "pp_gpu_set_neighbour_lists",
+    "pp_gpu_set_persistent", "pp_gpu_set_barrier_test",
 ]
 
 
@@ -195,6 +196,8 @@ def load_library(path=None):
         "pp_gpu_autotune": (ctypes.c_int, [vp, ctypes.c_int, ctypes.POINTER(PPTuneResult)]),
         "pp_gpu_set_graphs": (ctypes.c_int, [vp, ctypes.c_int]),
         "pp_gpu_set_neighbour_lists": (ctypes.c_int, [vp, ctypes.c_int]),
+        "pp_gpu_set_persistent": (ctypes.c_int, [vp, ctypes.c_int]),
+        "pp_gpu_set_barrier_test": (ctypes.c_int, [vp, ctypes.c_longlong, ctypes.c_int]),
         "pp_mlp_grad": (ctypes.c_int, [fp, ctypes.c_int, fp, ctypes.c_double, ctypes.c_double, ctypes.c_int, fp, dp]),
     }
     for name, (res, args) in sig.items():
@@ -357,6 +360,15 @@ class Engine:
 
     def set_neighbour_lists(self, enable=True):
         self._check(self.lib.pp_gpu_set_neighbour_lists(self.h, 1 if enable else 0))
+
+    def set_persistent(self, enable=True):
+        """Plain rounds over the neighbour lists as one persistent cooperative launch (default) or one launch
+        per colour; the trajectory is the same."""
+        self._check(self.lib.pp_gpu_set_persistent(self.h, 1 if enable else 0))
+
+    def set_barrier_test(self, limit_cycles=0, unreachable=False):
+        """Failure-detection hook of the persistent kernel's grid barrier (see include/ppgpu.h)."""
+        self._check(self.lib.pp_gpu_set_barrier_test(self.h, int(limit_cycles), 1 if unreachable else 0))
 
     def autotune(self, trial_sweeps=20):
         t = PPTuneResult()

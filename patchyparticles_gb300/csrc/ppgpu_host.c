@@ -224,6 +224,10 @@ static int create_common(const pp_params *prms, int n, pp_engine **out) {
 	e->cell_scale = 1.0;
 	e->graphs_on = 1;
 	e->nl_mode = 1;
+	{ /* persistent round kernel: PPGPU_PERSIST=1 turns it on for every engine (pp_gpu_set_persistent per engine) */
+		const char *v = getenv("PPGPU_PERSIST");
+		e->d.persist = (v && atoi(v) == 1) ? 1 : 0;
+	}
 	for(int i = 0; i < n; i++) {
 		if(e->prm[i].guard_eps <= 0.) e->prm[i].guard_eps = 1e-5;
 		if(e->prm[i].ensemble == PP_NPT) e->any_npt = 1;
@@ -265,6 +269,8 @@ static void free_device(pp_engine *e) {
 	e->pin_n = 0;
 	if(e->d.ctr) cudaFree(e->d.ctr);
 	e->d.ctr = NULL;
+	if(e->d.gbar) cudaFree(e->d.gbar);
+	e->d.gbar = NULL;
 	if(e->d.nl) cudaFree(e->d.nl);
 	if(e->d.nl_cnt) cudaFree(e->d.nl_cnt);
 	if(e->d.vpairs) cudaFree(e->d.vpairs);
@@ -452,10 +458,12 @@ static int ensure_pinned(pp_engine *e, size_t n) {
 
 static int read_states(pp_engine *e) {
 	CU(cudaMemcpyAsync(e->h_rs, e->d.rs, sizeof(ppi_rstate) * e->nrep, cudaMemcpyDeviceToHost, e->stream));
-	int lerr = 0;
+	int lerr = 0, berr = 0;
 	if(e->learn_ready) CU(cudaMemcpyAsync(&lerr, e->l_err, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+	if(e->d.gbar) CU(cudaMemcpyAsync(&berr, e->d.gbar + 2, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
 	CU(cudaStreamSynchronize(e->stream));
 	if(lerr) return set_err(e, PP_ERR_CUDA, "a tensor-core wait of the learned proposal timed out");
+	if(berr == PPI_E_BARRIER) return set_err(e, PP_ERR_CUDA, "grid barrier wait timed out in the persistent round kernel (the state is incomplete)");
 	for(int r = 0; r < e->nrep; r++)
 		if(e->h_rs[r].error == PPI_E_LISTS)
 			return set_err(e, PP_ERR_CAPACITY, "replica %d: more guard-band pairs in one volume pass than its buffer holds", r);
@@ -650,6 +658,8 @@ static int commit(pp_engine *e) {
 	CU(cudaMalloc((void **) &d->rs, sizeof(ppi_rstate) * e->nrep));
 	CU(cudaMalloc((void **) &d->grid, sizeof(ppi_grid) * e->nrep));
 	CU(cudaMalloc((void **) &d->ctr, sizeof(ppi_ctr)));
+	CU(cudaMalloc((void **) &d->gbar, 4 * sizeof(int)));
+	CU(cudaMemsetAsync(d->gbar, 0, 4 * sizeof(int), e->stream));
 	CU(cudaMemsetAsync(d->out_bonds, 0, sizeof(int) * n1, e->stream));
 	CU(cudaMemsetAsync(d->out_overlaps, 0, sizeof(int) * n1, e->stream));
 	CU(cudaMemsetAsync(d->grid, 0, sizeof(ppi_grid) * e->nrep, e->stream));
@@ -1002,6 +1012,23 @@ int pp_gpu_set_neighbour_lists(pp_engine *e, int enable) {
 	e->graph_gen++;
 	e->nl_valid = 0; /* lists are (re)built at the next re-sort */
 	CU(cudaMemcpyAsync(e->d.rp, e->h_rp, sizeof(ppi_rparams) * e->nrep, cudaMemcpyHostToDevice, e->stream));
+	return PP_OK;
+}
+
+int pp_gpu_set_persistent(pp_engine *e, int enable) {
+	if(e == NULL) return PP_ERR_ARG;
+	enable = enable ? 1 : 0;
+	if(enable == e->d.persist) return PP_OK;
+	e->d.persist = enable;
+	drop_graphs(e); /* the launches' arguments changed */
+	return PP_OK;
+}
+
+int pp_gpu_set_barrier_test(pp_engine *e, long long limit_cycles, int unreachable) {
+	if(e == NULL || limit_cycles < 0 || unreachable < 0 || unreachable > 1) return PP_ERR_ARG;
+	e->d.bar_limit = limit_cycles;
+	e->d.bar_extra = unreachable;
+	drop_graphs(e);
 	return PP_OK;
 }
 

@@ -41,6 +41,7 @@ extern "C" {
 #define PPI_E_GRID 2  /* the box became too small for an even cell grid of edge >= r_cut */
 #define PPI_E_EXACT 3 /* more undecidable pairs in one warp's share of a volume pass than it keeps */
 #define PPI_E_LISTS 4 /* more guard-band pairs in one volume pass than its buffer holds */
+#define PPI_E_BARRIER 5 /* a grid-barrier wait of the persistent round kernel ran out of its limit */
 
 typedef struct ppi_rparams {
 	int N;           /* particles of this replica */
@@ -187,6 +188,13 @@ typedef struct ppi_dev {
 	int vun_cap;
 	int2 *vunsure;     /* guard-band pairs of the current volume pass, decided in FP64 after it */
 	int *vun_count;
+	/* the persistent round kernel (k_round): the 8 colours of a round in one cooperative launch, a grid
+	 * barrier between colours. gbar[0] = CTA arrivals, gbar[1] = CTAs done (the last one resets both),
+	 * gbar[2] = error: a barrier wait that ran out of its limit (PPI_E_BARRIER) */
+	int *gbar;
+	long long bar_limit; /* SM clock cycles a barrier wait may spin before it gives up (0: default ~1 s) */
+	int bar_extra;       /* test hook: arrivals the first barrier waits for beyond the grid (1 = never completes) */
+	int persist;         /* 1: plain rounds over the neighbour lists use k_round, 0: one launch per colour */
 } ppi_dev;
 
 #define PPI_MAX_PARTNERS 24

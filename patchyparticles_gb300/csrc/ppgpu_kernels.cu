@@ -904,6 +904,52 @@ struct Proposal {
 	float cpo[9];
 };
 
+/* the attempt's Philox draws (particle + displacement, rotation; acceptance only when needed) and its mover */
+__device__ __forceinline__ void propose_draws(const ppi_dev &d, const int4 ent, long long round, Proposal &P, U4 &r1, U4 &r2) {
+	P.r = ent.w;
+	const ppi_rparams &rp = d.rp[P.r];
+	P.local = ent.x - rp.cell_base;
+	r1 = rng(rp, round, P.r, TAG_MOVE, (uint32_t) P.local, 0u);
+	r2 = rng(rp, round, P.r, TAG_MOVE, (uint32_t) P.local, 1u);
+	P.i = ent.y + (int) __umulhi(r1.x, (uint32_t) ent.z);
+}
+
+/* the proposal from the draws and the mover's FP32 record (po = spos, ob oc od = sori) */
+__device__ __forceinline__ void propose_from(const ppi_dev &d, Proposal &P, const U4 r1, const U4 r2, const float4 po, const float4 ob, const float4 oc,
+		const float4 od) {
+	const ppi_rparams &rp = d.rp[P.r];
+	const ppi_grid &g = d.grid[P.r];
+	P.po = po;
+	const float dm = rp.disp_max_f;
+	P.disp = make_float3((u01(r1.y) - 0.5f) * dm, (u01(r1.z) - 0.5f) * dm, (u01(r1.w) - 0.5f) * dm);
+	const float nx = P.po.x + P.disp.x, ny = P.po.y + P.disp.y, nz = P.po.z + P.disp.z;
+	/* a move that leaves the cell is rejected: cells stay valid and same-colour cells stay independent */
+	P.inside = nx >= 0.f && nx < g.wf[0] && ny >= 0.f && ny < g.wf[1] && nz >= 0.f && nz < g.wf[2];
+	P.pslot = 0;
+	P.q = make_float4(1.f, 0.f, 0.f, 0.f);
+	if(P.inside) {
+		P.pslot = __float_as_int(od.w);
+		/* rotation: angle uniform in [0, Theta_max), axis uniform on the sphere (inversion method) */
+		const float theta = u01(r2.x) * rp.theta_max_f;
+		const float zc = 1.f - 2.f * u01(r2.y);
+		const float phi = 6.283185307179586f * u01(r2.z);
+		const float sr = sqrtf(fmaxf(0.f, 1.f - zc * zc));
+		float sp, cph, sh, ch;
+		__sincosf(phi, &sp, &cph);
+		__sincosf(0.5f * theta, &sh, &ch);
+		P.q = make_float4(ch, sh * sr * cph, sh * sr * sp, sh * zc);
+		P.cpo[0] = ob.x;
+		P.cpo[1] = ob.y;
+		P.cpo[2] = ob.z;
+		P.cpo[3] = ob.w;
+		P.cpo[4] = oc.x;
+		P.cpo[5] = oc.y;
+		P.cpo[6] = oc.z;
+		P.cpo[7] = oc.w;
+		P.cpo[8] = od.x;
+	}
+}
+
 __device__ __forceinline__ void propose(const ppi_dev &d, const int4 ent, long long round, Proposal &P) {
 	const int gc = ent.x, c0 = ent.y, cnt = ent.z;
 	P.r = ent.w;
@@ -1074,7 +1120,8 @@ struct PairGeo {
 	float dxo, dyo, dzo, dxn, dyn, dzn;
 };
 
-__device__ __forceinline__ PairGeo pair_geo(const TileSmem &S, int a, int t, float4 qa) {
+template <typename SM>
+__device__ __forceinline__ PairGeo pair_geo(const SM &S, int a, int t, float4 qa) {
 	const float4 p = S.pos[a], m = S.md[a], w = S.wv[a];
 	const int nxc = __float_as_int(w.w);
 	int dxc = __float_as_int(qa.w) - __float_as_int(p.w);
@@ -1525,6 +1572,388 @@ __global__ void __launch_bounds__(32 * TILE_WARPS, MODE == MODE_FAST ? PPI_TILE_
 				fl[e] = 0;
 				attempt_exact<MODE>(d, list[e], round, A);
 			}
+	}
+	__syncwarp();
+	flush_block(d, A);
+}
+
+/* ------------------------------------------------------------------------------------------------ */
+/* persistent round over the neighbour lists (k_round)                                              */
+/* ------------------------------------------------------------------------------------------------ */
+/* The 8 colours of a plain round in one cooperative launch, with a grid barrier between colours. A warp
+ * takes 32 attempts at a time (one per lane) and moves each step's global reads into shared memory with
+ * cp.async before it computes on them, so that a step costs one memory latency however many pairs it has:
+ *   1. proposal: the movers' FP32 records, list lengths and first KR_NL0 list entries, all loaded
+ *      together (registers); the movers' FP64 records start towards shared memory;
+ *   2. the candidate positions of every listed pair -> shared memory; distance filter, certain overlaps,
+ *      close pairs compacted;
+ *   3. the close candidates' orientation records -> shared memory; patch tests; guard-band pairs go to the
+ *      certified FP64 test; decisions; commits from the staged FP64 records.
+ * Step 1 of a colour's first iteration runs before the barrier that closes the previous colour: it reads
+ * only its own movers (the previous colour moves none of them) and the epoch's lists. The per-pair
+ * decisions are k_colour's (the same classify, guard band, decide64 and exact_pair on the same proposals)
+ * and every decision is the exact one, so the trajectory equals k_colour's bit for bit; an attempt
+ * k_colour would defer (list overflow, guard-band pairs beyond KR_UCAP) takes the same exact path.
+ * Barrier: a CTA arrives once per colour (after __syncthreads, a gpu-scope fence and an atomic add); a
+ * CTA waits by one thread spinning with acquire loads, then __syncthreads. Every wait is bounded by
+ * d.bar_limit SM cycles: one that runs out writes PPI_E_BARRIER to gbar[2] and its CTA returns (the others
+ * then run out at their next wait), so a missing CTA can never hang the GPU. The launch is cooperative,
+ * so every CTA of the grid is resident. */
+#define KR_WARPS 4
+#define KR_A 32      /* attempts per warp iteration: one per lane */
+#define KR_PCAP 512  /* staged candidate positions per chunk of an iteration's pairs */
+#define KR_CCAP 128  /* staged close-pair orientation records per chunk */
+#define KR_NL0 16    /* list entries loaded with the proposal (the rest, if any, in the pair step) */
+#define KR_UCAP 32   /* guard-band pairs per iteration decided in place (more: the attempt is deferred) */
+#define KR_DCAP 16   /* deferred attempts a warp keeps in shared memory (more: flags in global memory) */
+#define KR_LIMIT_DEFAULT (1ll << 31) /* SM clock cycles of a barrier wait: ~1 s at 2 GHz */
+
+struct __align__(16) RoundSmem {
+	float4 qpos[KR_PCAP];       /* staged candidate positions (spos) */
+	float4 qori[3 * KR_CCAP];   /* staged close candidates' orientation records (sori) */
+	double mrec[KR_A][8];       /* staged movers' FP64 records, doubles 0..7 (x y z q) */
+	float4 pos[KR_A];           /* old cell-local position, .w = cell x index */
+	float4 md[KR_A];            /* displacement, .w = mover slot */
+	float4 wv[KR_A];            /* cell edges, .w = number of x cells */
+	float4 qr[KR_A];            /* proposed rotation quaternion */
+	float cpo[9][KR_A];         /* mover's old orientation columns */
+	float cpn[9][KR_A];         /* mover's candidate orientation columns */
+	float2 lim[KR_A];           /* (1 - eps, r_cut^2 + eps) */
+	int pj[KR_PCAP];            /* candidate sorted position of pair p */
+	unsigned short pat[KR_PCAP]; /* attempt << 4 | row (dy + 1) + 3 (dz + 1) of pair p */
+	short cl[KR_PCAP];          /* the close pairs (indices p) */
+	int mi[KR_A], rep[KR_A], flag[KR_A], bo[KR_A], bn[KR_A];
+	int2 uns[KR_UCAP];          /* guard-band pairs: (candidate sorted position, attempt << 1 | kind) */
+	int dl[KR_DCAP];            /* list indices of deferred attempts */
+	int nu, nd, dov, total;     /* total: listed pairs of the iteration */
+};
+
+/* 16 bytes global -> shared, through L2 only (cp.async.cg); completed by kr_cp_wait */
+__device__ __forceinline__ void kr_cp16(void *dst, const void *src) {
+	asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned) __cvta_generic_to_shared(dst)), "l"(src) : "memory");
+}
+
+/* waits for every cp.async this thread issued; the caller then __syncwarp()s before other lanes read */
+__device__ __forceinline__ void kr_cp_wait() { asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory"); }
+
+/* list entry (candidate << 5 | cell offset code) of attempt a at pair slot p */
+__device__ __forceinline__ void kr_put(RoundSmem &S, int p, int entry, int a) {
+	const unsigned u = (unsigned) entry;
+	S.pj[p] = (int) (u >> 5);
+	S.pat[p] = (unsigned short) ((a << 4) | ((u & 31u) / 3u));
+}
+
+/* step 1 for the lane's attempt (list entry ent; ent.x < 0: none): the proposal into shared memory, the
+ * mover's FP64 record started towards S.mrec, and the attempt's first KR_NL0 list entries written to the
+ * pair list at the attempt's slice (those that fall into the first chunk). Returns the attempt's number of
+ * listed pairs n (0 if it has none or takes the exact path) and its slice's start; S.total = all pairs. */
+__device__ __forceinline__ int kr_setup(const ppi_dev &d, RoundSmem &S, const int a, const int4 ent, long long round, Acc &A, int &start, int &loc) {
+	int flag = TF_CLOSED, n = 0;
+	int e[KR_NL0];
+	Proposal P;
+	P.i = P.r = P.local = P.pslot = 0;
+	P.po = make_float4(0.f, 0.f, 0.f, 0.f);
+	P.q = make_float4(1.f, 0.f, 0.f, 0.f);
+	P.disp = make_float3(0.f, 0.f, 0.f);
+	float4 wv = make_float4(1.f, 1.f, 1.f, __int_as_float(4));
+	float2 lim = make_float2(0.f, 0.f);
+#pragma unroll
+	for(int k = 0; k < KR_NL0; k++) e[k] = 0;
+	if(ent.x >= 0) {
+		if(ent.w != A.r) {
+			flush_thread(d, A);
+			A.r = ent.w;
+		}
+		A.tries++;
+		U4 r1, r2;
+		propose_draws(d, ent, round, P, r1, r2);
+		const size_t i = (size_t) P.i;
+		const int K = d.nl_k;
+		/* every load of the step at once: they all depend on the mover only */
+		const float4 po = __ldcg(d.spos + i);
+		const float4 ob = __ldcg(d.sori + 3 * i), oc = __ldcg(d.sori + 3 * i + 1), od = __ldcg(d.sori + 3 * i + 2);
+		const int cnt = __ldcg(d.nl_cnt + i);
+		const int4 *L = (const int4 *) (d.nl + i * (size_t) K);
+		int4 v[KR_NL0 / 4];
+#pragma unroll
+		for(int c = 0; c < KR_NL0 / 4; c++) v[c] = (4 * c < K) ? __ldcg(L + c) : make_int4(0, 0, 0, 0);
+		propose_from(d, P, r1, r2, po, ob, oc, od);
+		const ppi_grid &g = d.grid[P.r];
+		const ppi_rparams &rp = d.rp[P.r];
+		const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
+		lim = make_float2(1.f - eps, rp.sqr_rcut_f + eps);
+		wv = make_float4(g.wf[0], g.wf[1], g.wf[2], __int_as_float(g.n[0]));
+		if(P.inside) {
+			float cpn[9];
+			cols_new(P.cpo, P.q, cpn);
+#pragma unroll
+			for(int k = 0; k < 9; k++) {
+				S.cpo[k][a] = P.cpo[k];
+				S.cpn[k][a] = cpn[k];
+			}
+			if(cnt > K) flag = TF_DEFER; /* the list overflowed: the exact 27-cell path */
+			else {
+				flag = 0;
+				n = cnt;
+			}
+			const double *rec = d.rec + (size_t) P.pslot * PPI_REC;
+#pragma unroll
+			for(int c = 0; c < 4; c++) kr_cp16(&S.mrec[a][2 * c], rec + 2 * c);
+		}
+#pragma unroll
+		for(int c = 0; c < KR_NL0 / 4; c++) {
+			e[4 * c] = v[c].x;
+			e[4 * c + 1] = v[c].y;
+			e[4 * c + 2] = v[c].z;
+			e[4 * c + 3] = v[c].w;
+		}
+	}
+	S.pos[a] = P.po;
+	S.md[a] = make_float4(P.disp.x, P.disp.y, P.disp.z, __int_as_float(P.pslot));
+	S.wv[a] = wv;
+	S.qr[a] = P.q;
+	S.mi[a] = P.i;
+	S.lim[a] = lim;
+	S.rep[a] = P.r;
+	S.bo[a] = 0;
+	S.bn[a] = 0;
+	S.flag[a] = flag;
+	loc = P.local;
+	/* the attempts' slices of the pair list: a warp scan of the list lengths */
+	int incl = n;
+#pragma unroll
+	for(int o = 1; o < 32; o <<= 1) {
+		const int v = __shfl_up_sync(0xffffffffu, incl, o);
+		if(a >= o) incl += v;
+	}
+	start = incl - n;
+	if(a == 31) S.total = incl;
+#pragma unroll
+	for(int k = 0; k < KR_NL0; k++)
+		if(k < n && start + k < KR_PCAP) kr_put(S, start + k, e[k], a);
+	return n;
+}
+
+/* patch tests of staged close pair q (pair p) */
+__device__ __forceinline__ void kr_close(const ppi_dev &d, RoundSmem &S, int q, int p, Acc &A) {
+	const int at = S.pat[p], a = at >> 4;
+	if(S.flag[a] & (TF_OVER | TF_DEFER)) return;
+	const float4 qb = S.qori[3 * q], qc = S.qori[3 * q + 1], qd = S.qori[3 * q + 2];
+	const float cq[9] = { qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w, qd.x };
+	const PairGeo G = pair_geo(S, a, at & 15, S.qpos[p]);
+	const ppi_rparams &rp = d.rp[S.rep[a]];
+	const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
+	float cpo[9], cpn[9];
+#pragma unroll
+	for(int k = 0; k < 9; k++) {
+		cpo[k] = S.cpo[k][a];
+		cpn[k] = S.cpn[k][a];
+	}
+	const int clo = classify(G.dxo, G.dyo, G.dzo, cpo, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, nullptr);
+	const int cln = classify(G.dxn, G.dyn, G.dzn, cpn, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, nullptr);
+	const int nu = (clo == CL_UNSURE) + (cln == CL_UNSURE);
+	if(nu) { /* guard band: decided after the pairs by the certified FP64 test */
+		const int k = atomicAdd(&S.nu, nu);
+		if(k + nu > KR_UCAP) {
+			atomicOr(&S.flag[a], TF_DEFER);
+			return;
+		}
+		int kk = k;
+		if(clo == CL_UNSURE) S.uns[kk++] = make_int2(S.pj[p], a << 1);
+		if(cln == CL_UNSURE) S.uns[kk] = make_int2(S.pj[p], (a << 1) | 1);
+	}
+	if(clo == CL_BOND) atomicAdd(&S.bo[a], 1);
+	if(cln == CL_BOND) atomicAdd(&S.bn[a], 1);
+	if(cln == CL_OVER) atomicOr(&S.flag[a], TF_OVER);
+}
+
+__device__ __forceinline__ void kr_defer(const ppi_dev &d, RoundSmem &S, int col, int e) {
+	const int k = atomicAdd(&S.nd, 1);
+	if(k < KR_DCAP) S.dl[k] = e;
+	else {
+		d.dflag[(size_t) col * d.clist_cap + e] = 1;
+		S.dov = 1;
+	}
+}
+
+/* steps 2 and 3 of the iteration whose step 1 left n pairs and list entries e[] in this lane */
+__device__ __forceinline__ void kr_iteration(const ppi_dev &d, RoundSmem &S, const int lane, const int n, const int start, const int loc, const int b,
+		const int col, long long round, Acc &A) {
+	const unsigned lt = (1u << lane) - 1u;
+	__syncwarp();
+	const int total = S.total;
+	if(lane == 0) S.nu = 0;
+	const int *Lg = d.nl + (size_t) S.mi[lane] * d.nl_k;
+	for(int c0 = 0; c0 < total; c0 += KR_PCAP) {
+		const int np = min(total - c0, KR_PCAP);
+		/* this lane's list entries that fall into the chunk and are not written yet (kr_setup wrote the
+		 * first KR_NL0 of each attempt that fall into the first chunk) */
+		const int k0 = max(0, c0 - start), k1 = min(n, c0 + np - start);
+		for(int k = (c0 == 0 ? max(k0, KR_NL0) : k0); k < k1; k++) kr_put(S, start + k - c0, __ldcg(Lg + k), lane);
+		__syncwarp();
+		/* step 2: candidate positions (and, in the first chunk, the movers' FP64 records) */
+		for(int p = lane; p < np; p += 32) kr_cp16(&S.qpos[p], d.spos + S.pj[p]);
+		kr_cp_wait();
+		__syncwarp();
+		int ncl = 0;
+		for(int p0 = 0; p0 < np; p0 += 32) {
+			const int p = p0 + lane;
+			int close = 0;
+			if(p < np) {
+				const int at = S.pat[p], a = at >> 4;
+				if(!(S.flag[a] & (TF_OVER | TF_DEFER))) {
+					const PairGeo G = pair_geo(S, a, at & 15, S.qpos[p]);
+					const float r2o = fmaf(G.dxo, G.dxo, fmaf(G.dyo, G.dyo, G.dzo * G.dzo));
+					const float r2n = fmaf(G.dxn, G.dxn, fmaf(G.dyn, G.dyn, G.dzn * G.dzn));
+					const float2 lim = S.lim[a];
+					A.pairs += 2;
+					if(r2n < lim.x) atomicOr(&S.flag[a], TF_OVER); /* certain overlap of the candidate state */
+					else close = r2o < lim.y || r2n < lim.y;
+				}
+			}
+			const unsigned m = __ballot_sync(0xffffffffu, close);
+			if(close) S.cl[ncl + __popc(m & lt)] = (short) p;
+			ncl += __popc(m);
+		}
+		__syncwarp();
+		/* step 3: the close pairs' orientation records, then their patch tests */
+		for(int q0 = 0; q0 < ncl; q0 += KR_CCAP) {
+			const int nq = min(ncl - q0, KR_CCAP);
+			for(int q = lane; q < nq; q += 32) {
+				const int p = S.cl[q0 + q];
+				if(S.flag[S.pat[p] >> 4] & (TF_OVER | TF_DEFER)) continue;
+				const float4 *src = d.sori + 3 * (size_t) S.pj[p];
+				kr_cp16(S.qori + 3 * q, src);
+				kr_cp16(S.qori + 3 * q + 1, src + 1);
+				kr_cp16(S.qori + 3 * q + 2, src + 2);
+			}
+			kr_cp_wait();
+			__syncwarp();
+			for(int q = lane; q < nq; q += 32) kr_close(d, S, q, S.cl[q0 + q], A);
+			__syncwarp();
+		}
+	}
+	if(total == 0) { /* no pair: the movers' FP64 records still have to arrive */
+		kr_cp_wait();
+		__syncwarp();
+	}
+	/* guard-band pairs: certified FP64 decisions; an undecided one defers its attempt */
+	const int nu = S.nu < KR_UCAP ? S.nu : KR_UCAP;
+	for(int u = lane; u < nu; u += 32) {
+		const int2 v = S.uns[u];
+		const int jq = v.x, a = v.y >> 1, kind = v.y & 1;
+		if(S.flag[a] & (TF_OVER | TF_DEFER)) continue;
+		const int r = S.rep[a];
+		const float4 md = S.md[a];
+		A.fallbacks++;
+		const int ex = decide64(d.rec, d.rp[r], d.rs[r].box, d.grid[r].inv_L, __float_as_int(md.w), kind, S.qr[a], make_float3(md.x, md.y, md.z),
+				__float_as_int(__ldcg(d.sori + 3 * (size_t) jq + 2).w), 0, nullptr, nullptr);
+		if(ex == DEC64_EXACT) atomicOr(&S.flag[a], TF_DEFER);
+		else if(ex == 1) atomicAdd(kind ? &S.bn[a] : &S.bo[a], 1);
+		else if(ex == -1 && kind) atomicOr(&S.flag[a], TF_OVER);
+	}
+	__syncwarp();
+	/* decision and commit of the lane's attempt */
+	const int a = lane, flag = S.flag[a];
+	if(flag & (TF_OVER | TF_CLOSED)) return;
+	if(flag & TF_DEFER) {
+		kr_defer(d, S, col, b + a);
+		return;
+	}
+	const int r = S.rep[a];
+	const int bo = S.bo[a], bn = S.bn[a];
+	if(!metropolis(d.rp[r], round, r, loc, bo, bn)) return;
+	if(r != A.r) {
+		flush_thread(d, A);
+		A.r = r;
+	}
+	A.acc++;
+	A.dbonds += bn - bo;
+	float cpn[9];
+#pragma unroll
+	for(int k = 0; k < 9; k++) cpn[k] = S.cpn[k][a];
+	const float4 md = S.md[a];
+	commit_from(d, S.mrec[a], S.mi[a], __float_as_int(md.w), S.pos[a], make_float3(md.x, md.y, md.z), S.qr[a], cpn);
+}
+
+/* waits until gbar[0] >= target (every CTA has closed the previous colour); false if the wait ran out */
+__device__ __forceinline__ bool kr_barrier_wait(const ppi_dev &d, unsigned target, long long limit, int *s_abort) {
+	if(threadIdx.x == 0) {
+		const long long t0 = clock64();
+		unsigned ns = 32;
+		for(;;) {
+			unsigned v;
+			asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(d.gbar) : "memory");
+			if(v >= target) break;
+			if(clock64() - t0 > limit) {
+				atomicExch(d.gbar + 2, PPI_E_BARRIER);
+				*s_abort = 1;
+				break;
+			}
+			__nanosleep(ns);
+			if(ns < 512) ns <<= 1;
+		}
+	}
+	__syncthreads();
+	return *s_abort == 0;
+}
+
+/* one plain round over the epoch's neighbour lists; colours = the round's colour order, 3 bits per slot
+ * (stream launches), or round < 0 for a captured graph launch (round after the device counter, colour
+ * order computed here) */
+__global__ void __launch_bounds__(32 * KR_WARPS, 2) k_round(ppi_dev d, long long round, int colours) {
+	const bool graph = round < 0;
+	if(graph) round = ctr_index(round, d.ctr->round);
+	extern __shared__ __align__(16) unsigned char kr_smem[];
+	RoundSmem &S = ((RoundSmem *) kr_smem)[threadIdx.x >> 5];
+	__shared__ int s_abort;
+	const int lane = threadIdx.x & 31;
+	const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarp = (gridDim.x * blockDim.x) >> 5;
+	const long long limit = d.bar_limit > 0 ? d.bar_limit : KR_LIMIT_DEFAULT;
+	const int4 none = make_int4(-1, 0, 0, 0);
+	Acc A;
+	A.r = -1;
+	A.tries = A.acc = A.pairs = A.fallbacks = 0;
+	A.dbonds = 0;
+	if(threadIdx.x == 0) s_abort = 0;
+	for(int ci = 0; ci < 8; ci++) {
+		const int col = graph ? colour_at(round, ci) : (colours >> (3 * ci)) & 7;
+		const int4 *list = d.clist + (size_t) col * d.clist_cap;
+		int cnt = d.ccount[col];
+		if(cnt > d.clist_cap) cnt = d.clist_cap;
+		/* every warp an equal share of the colour's list */
+		const int lo = (int) ((long long) warp * cnt / nwarp), hi = (int) ((long long) (warp + 1) * cnt / nwarp);
+		if(lane == 0) {
+			S.nd = 0;
+			S.dov = 0;
+		}
+		__syncwarp();
+		int loc = 0, start = 0;
+		int n = kr_setup(d, S, lane, lo + lane < hi ? list[lo + lane] : none, round, A, start, loc);
+		if(ci > 0 && !kr_barrier_wait(d, (unsigned) (ci * gridDim.x + (ci == 1 ? d.bar_extra : 0)), limit, &s_abort)) return;
+		for(int b = lo; b < hi; b += KR_A) {
+			const int4 next = b + KR_A + lane < hi ? list[b + KR_A + lane] : none;
+			kr_iteration(d, S, lane, n, start, loc, b, col, round, A);
+			__syncwarp();
+			if(b + KR_A < hi) n = kr_setup(d, S, lane, next, round, A, start, loc);
+		}
+		/* the deferred attempts, one per lane, exactly */
+		const int nd = S.nd < KR_DCAP ? S.nd : KR_DCAP;
+		for(int k = lane; k < nd; k += 32) attempt_exact<MODE_FAST>(d, list[S.dl[k]], round, A);
+		if(S.dov) {
+			unsigned char *fl = d.dflag + (size_t) col * d.clist_cap;
+			for(int x = lo + lane; x < hi; x += 32)
+				if(fl[x]) {
+					fl[x] = 0;
+					attempt_exact<MODE_FAST>(d, list[x], round, A);
+				}
+		}
+		/* close the colour: every warp of the CTA is done, its writes are visible at gpu scope */
+		__syncthreads();
+		if(threadIdx.x == 0) {
+			__threadfence();
+			atomicAdd((unsigned *) d.gbar, 1u);
+		}
 	}
 	__syncwarp();
 	flush_block(d, A);
@@ -3747,8 +4176,47 @@ extern "C" int ppi_nlist(const ppi_dev *d, cudaStream_t s, long long *nl) {
 	return (int) cudaGetLastError();
 }
 
+/* the persistent round kernel's grid: every CTA resident (cooperative launch); 0 if it cannot run */
+static int g_round_grid = -1;
+static int round_grid(void) {
+	if(g_round_grid < 0) {
+		const int smem = (int) (sizeof(RoundSmem) * KR_WARPS);
+		int nb = 0;
+		if(cudaFuncSetAttribute(k_round, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess ||
+				cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_round, 32 * KR_WARPS, smem) != cudaSuccess)
+			nb = 0;
+		cudaGetLastError();
+		g_round_grid = nb * ppi_sm_count();
+	}
+	return g_round_grid;
+}
+
+/* one plain round over the lists as one cooperative launch of k_round (the barrier counters cleared first) */
+static int launch_persistent_round(const ppi_dev *d, long long round, const int *colours, cudaStream_t s) {
+	int packed = 0;
+	for(int ci = 0; ci < 8; ci++) packed |= (colours[ci] & 7) << (3 * ci);
+	cudaMemsetAsync(d->gbar, 0, 2 * sizeof(int), s);
+	cudaLaunchConfig_t cfg;
+	memset(&cfg, 0, sizeof(cfg));
+	cfg.gridDim = dim3(round_grid());
+	cfg.blockDim = dim3(32 * KR_WARPS);
+	cfg.dynamicSmemBytes = sizeof(RoundSmem) * KR_WARPS;
+	cfg.stream = s;
+	cudaLaunchAttribute at[1];
+	at[0].id = cudaLaunchAttributeCooperative;
+	at[0].val.cooperative = 1;
+	cfg.attrs = at;
+	cfg.numAttrs = 1;
+	return (int) cudaLaunchKernelEx(&cfg, k_round, *d, round, packed);
+}
+
 extern "C" int ppi_round(const ppi_dev *d, long long round, const int *colours, int audit, int use_nl, cudaStream_t s, long long *nl) {
 	const int aud = audit || d->audit_any;
+	if(use_nl && d->nl_k > 0 && !aud && d->persist && d->gbar && round_grid() > 0) {
+		const int rc = launch_persistent_round(d, round, colours, s);
+		*nl += 1;
+		return rc ? rc : (int) cudaGetLastError();
+	}
 	if(use_nl && d->nl_k > 0 && aud) launch_round(k_colour<MODE_AUDIT, true>, resident_grid(k_colour<MODE_AUDIT, true>, &g_col_tla, 32 * TILE_WARPS), 32 * TILE_WARPS, 0, d, round, colours, s);
 	else if(use_nl && d->nl_k > 0) launch_round(k_colour<MODE_FAST, true>, resident_grid(k_colour<MODE_FAST, true>, &g_col_tl, 32 * TILE_WARPS), 32 * TILE_WARPS, 0, d, round, colours, s);
 	else if(aud) launch_round(k_colour<MODE_AUDIT, false>, resident_grid(k_colour<MODE_AUDIT, false>, &g_col_audit, 32 * TILE_WARPS), 32 * TILE_WARPS, 0, d, round, colours, s);
@@ -3869,6 +4337,7 @@ extern "C" int ppi_prepare(const ppi_dev *d) {
 	resident_grid(k_energy<MODE_FAST, 1>, &g_f1);
 	resident_grid(k_energy<MODE_FAST, 4>, &g_f4);
 	resident_grid(k_energy<MODE_FAST, 8>, &g_f8);
+	round_grid();
 	if(learned_grid(k_colour_learned<MODE_AUDIT>, &g_learn_audit) < 0 || learned_grid(k_colour_learned<MODE_FAST>, &g_learn_fast) < 0) return (int) cudaGetLastError();
 	return (int) cudaGetLastError();
 }
