@@ -227,7 +227,9 @@ def make_config(wl, seed_offset=0):
 def workload_config(wl, args):
     """The `config` object of both arms' lines: the workload alone (no implementation detail), so that the
     GPU line and the reference line describe the same thing."""
-    return {"workload": wl["name"], "N": wl["N"], "sweeps_per_step": args.sweeps_per_step, "proposal": "plain",
+    prop = "plain" if args.proposal == "plain" else "learned mixture (36-64-64-4 network trained at N=32768 rho=0.1 T=0.09)"
+    return {"workload": wl["name"] if args.proposal == "plain" else wl["name"].replace("plain roto-translation", "learned proposal"),
+            "N": wl["N"], "sweeps_per_step": args.sweeps_per_step, "proposal": prop,
             "l2": "inputs larger than L2 (FP64 state %.0f MB + FP32 mirror %.0f MB per GPU)" % (wl["N"] * 128 / 1e6, wl["N"] * 64 / 1e6)}
 
 
@@ -299,12 +301,39 @@ def run_gpu(args, wl, ws, rank, local, dist):
     barrier(dist)
     pp.select_device(local)
     r, R, box = make_config(wl, seed_offset=rank)
+    prep, audit = None, None
+    if args.workload == "c2":
+        # the configuration's 10^3-sweep hard-sphere equilibration (T = 1e9: every move without an overlap is
+        # accepted, bonds do not matter) before the timed run; both precisions start from this state
+        h = pp.Engine(pp.default_params(temperature=1e9, disp_max=wl["disp"], theta_max=wl["theta"], seed=wl["seed"] + 100 + rank))
+        h.upload(r, R, box)
+        h.sweeps(1000)
+        r, R, box = h.download()
+        h.close()
+        prep = "1000 hard-sphere sweeps (T = 1e9) from the seeded random insertion"
+        # the guard band's check on this state: every pair of 5 sweeps decided in FP32 and in FP64 (audit mode)
+        a = pp.Engine(pp.default_params(temperature=wl["T"], disp_max=wl["disp"], theta_max=wl["theta"], seed=wl["seed"] + rank, audit=1))
+        a.upload(r, R, box)
+        a.sweeps(5)
+        g = a.guard_stats()
+        a.close()
+        audit = {"sweeps": 5, "pairs": g["pairs"], "fallbacks": g["fallbacks"], "mismatches": g["mismatches"],
+                 "max_err_r2": g["max_err_r2"], "max_err_cos": g["max_err_cos"]}
     prm = pp.default_params(ensemble=wl["ensemble"], temperature=wl["T"], pressure=wl["P"], disp_max=wl["disp"],
                             theta_max=wl["theta"], rescale_factor_max=wl["rescale"], seed=wl["seed"] + rank,
                             precision=pp.PREC_FP64 if args.precision == "fp64" else pp.PREC_FP32_GUARD)
     e = pp.Engine(prm)
     e.upload(r, R, box)
     spsw = args.sweeps_per_step
+    train = None
+    if args.proposal == "learned":
+        # the large-scale configuration with the learned proposal: the network trained on the GPU on the
+        # learned-comparison workload (N=32768, rho=0.1, T=0.09, plain-move samples), then used here
+        W, train = train_network(args)
+        e.learned_init(seed=7, **json.loads(args.learn_params))
+        e.set_learned_weights(W)
+        e.set_proposal(True)
+        args.tune_sweeps = 0
     tune = e.autotune(args.tune_sweeps) if args.tune_sweeps > 0 else None  # schedule choice, before the timed region
     # warm-up
     for _ in range(args.warmup):
@@ -369,7 +398,7 @@ def run_gpu(args, wl, ws, rank, local, dist):
                "step": "upload (H2D, initial energy check) + sweeps + download (D2H) + tracked energy, through the C-ABI with host arrays"}
 
     learned = None
-    if rank == 0 and ws == 1 and not args.no_learned:
+    if rank == 0 and ws == 1 and not args.no_learned and args.proposal == "plain":
         e.close()
         learned = learned_comparison(args)
 
@@ -394,7 +423,7 @@ def run_gpu(args, wl, ws, rank, local, dist):
         "acceptance": acc[pp.MOVE_ROTO_TRASL] / max(1, tries[pp.MOVE_ROTO_TRASL]),
         "volume_acceptance": acc[pp.MOVE_VOLUME] / max(1, tries[pp.MOVE_VOLUME]) if tries[pp.MOVE_VOLUME] else None,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "kernel": "k_colour%s (8 launches per round, one event group)" % (" over neighbour lists" if (tune is None or tune.get("neighbour_lists", 1)) else ""), "peak_source": peak_kind,
+                     "traffic": traffic, "kernel": sweep_kernel_name(args, tune), "peak_source": peak_kind,
                      "bytes_per_attempt": BYTES_PER_ATTEMPT, "avg_launch_ms": avg_ms, "attempts_per_launch": att_per_launch},
         "kernel_ms_per_step": {"sort": ks["sort_ms"] / max(1, ks["sort_launches"]), "sweep": avg_ms,
                                "volume": ks["volume_ms"] / max(1, ks["volume_launches"]) if ks["volume_launches"] else 0.0},
@@ -403,77 +432,120 @@ def run_gpu(args, wl, ws, rank, local, dist):
         "cpu_baseline": cpu,
         "gpu_launches": launches,
         "learned": learned,
+        "training": train,
+        "preparation": prep,
+        "fp32_vs_fp64_audit": audit,
     }
     print(json.dumps(line), flush=True)
+
+
+def sweep_kernel_name(args, tune):
+    if args.proposal == "learned":
+        return "k_colour_learned (8 launches per round, one event group)"
+    if os.environ.get("PPGPU_PERSIST") == "1":
+        return "k_round (one persistent cooperative launch per round over the neighbour lists)"
+    return "k_colour%s (8 launches per round, one event group)" % (" over neighbour lists" if (tune is None or tune.get("neighbour_lists", 1)) else "")
+
+
+def train_network(args):
+    """Trains the proposal network on the GPU as the learned comparison does (samples of the plain move at
+    N=32768, rho=0.1, T=0.09); returns (weights, training record)."""
+    import patchyparticles_gb300 as pp
+
+    wl = WORKLOADS["c4"]
+    r, R, box = pp.generate(wl["N"], wl["rho"], wl["seed"], round_like_file=False)
+    e = pp.Engine(pp.default_params(temperature=wl["T"], disp_max=wl["disp"], theta_max=wl["theta"], seed=wl["seed"]))
+    e.upload(r, R, box)
+    e.learned_init(seed=7, **json.loads(args.learn_params))
+    t0 = time.perf_counter()
+    e.learned_collect(args.learn_configs, args.learn_sweeps_between, 128)
+    obj = e.learned_train(args.learn_epochs, lr=3e-3)
+    e.sync()
+    W = e.learned_weights()
+    e.close()
+    return W, {"workload": wl["name"], "configs": args.learn_configs, "epochs": args.learn_epochs, "objective": obj, "seconds": time.perf_counter() - t0}
 
 
 # ---------------------------------------------------------------- learned proposal vs plain (N=32768, T=0.09)
 def _acf_particles(B):
     """Autocorrelation of per-particle bond counts B[t][i] (the per-time mean over particles removed, so a
-    slow drift of the whole system does not count as correlation)."""
-    d = B.astype(np.float64)
-    d -= d.mean(axis=1, keepdims=True)
-    T = d.shape[0]
-    f = np.fft.rfft(d, 2 * T, axis=0)
-    a = np.fft.irfft(f * np.conj(f), axis=0)[:T].sum(axis=1)
+    slow drift of the whole system does not count as correlation), averaged over particles."""
+    T = B.shape[0]
+    gm = B.mean(axis=1, keepdims=True)
+    a = np.zeros(T)
+    for c0 in range(0, B.shape[1], 4096):  # particles in chunks (memory)
+        d = B[:, c0:c0 + 4096].astype(np.float64) - gm
+        d -= d.mean(axis=0, keepdims=True)
+        f = np.fft.rfft(d, 2 * T, axis=0)
+        a += np.fft.irfft(f * np.conj(f), axis=0)[:T].sum(axis=1)
     a /= np.arange(T, 0, -1)
     return a / a[0]
 
 
-def _tau_sokal(acf, c=5.0):
-    tau = 1.0
-    for M in range(1, len(acf)):
-        tau = 1 + 2 * acf[1:M + 1].sum()
-        if M >= c * tau:
-            return tau, M, False
-    return tau, len(acf), True
+def tau_int(acf, n, c=5.0):
+    """Sokal's windowed integrated autocorrelation time, in samples: tau = 1 + 2 sum_{t=1..M} C(t) with the
+    window M the smallest lag with M >= c tau. Returns (tau, M, window_limited, sigma): window_limited when
+    no such M exists within the series (tau is then a lower bound) or M > n / 50 (the run is shorter than 50
+    tau windows, Sokal's reliability rule); sigma from Sokal's variance 2 (2M + 1) / n tau^2."""
+    tau, M = 1.0, len(acf) - 1
+    found = False
+    for m in range(1, len(acf)):
+        tau = 1.0 + 2.0 * float(acf[1:m + 1].sum())
+        if m >= c * tau:
+            M, found = m, True
+            break
+    sigma = tau * np.sqrt(2.0 * (2 * M + 1) / n)
+    return tau, M, (not found) or M > n / 50, sigma
 
 
-def _chain(e, sweeps, every, learned):
-    """Per-particle bond counts every `every` sweeps; device time of the sweeps only."""
-    import patchyparticles_gb300 as pp
-
-    e.set_proposal(learned)
-    N = e.num_particles()
+def _chains(engines, sweeps, every):
+    """Runs the chains side by side (each engine on its own stream, so their launches overlap) and samples
+    every particle's bond count every `every` sweeps. Returns one (n, N) int8 array per engine."""
     n = sweeps // every
-    B = np.zeros((n, N), dtype=np.int8)
-    ms = 0.0
+    out = [np.zeros((n, e.num_particles()), dtype=np.int8) for e in engines]
     for k in range(n):
-        ms += e.time_sweeps(every)
-        nb, _ = e.bonds()
-        B[k] = nb
-    acf = _acf_particles(B)
-    lags = np.arange(1, min(6, len(acf)))
-    # initial decorrelation: C(k every) ~ 1 - k every / tau for an exponential autocorrelation
-    slope = float(np.polyfit(lags * every, 1.0 - acf[lags], 1)[0]) if len(lags) >= 2 else float("nan")
-    tau_exp = 1.0 / slope if slope > 0 else float("inf")
-    tau_w, win, limited = _tau_sokal(acf)
-    ms_sweep = ms / sweeps
-    sps = 1000.0 / ms_sweep
-    out = {"ms_per_sweep": ms_sweep, "sweeps": sweeps, "snapshot_every": every,
-           "bonds_per_particle": [float(B[0].mean() / 2), float(B[-1].mean() / 2)],
-           "bond_change_rate_per_sweep": float((B[1:] != B[:-1]).mean() / every),
-           "tau_exp_sweeps": tau_exp, "tau_int_window_sweeps": tau_w * every, "tau_window_limited": bool(limited),
-           "ess_per_s": N * sps / (2.0 * tau_exp)}
-    if learned:
-        t, a = e.learned_stats(reset=True)
-        tt = max(1, sum(t))
-        out["component_share"] = [x / tt for x in t]
-        out["component_acceptance"] = [a[k] / max(1, t[k]) for k in range(len(t))]
+        for e in engines:
+            e.sweeps(every)
+        for e, B in zip(engines, out):
+            B[k] = e.bonds()[0]
     return out
 
 
-def learned_comparison(args):
-    """The learned proposal against the plain move at N=32768, rho=0.1, T=0.09: the network is trained on
-    the GPU on samples of configurations generated by the plain move, then both chains run from the same
-    configuration; effective samples/s of the per-particle bond count = N x sweeps/s / (2 tau), tau from the
-    initial decay of its autocorrelation (the windowed estimate is reported too: at T=0.09 the chains age
-    and a run of bench length does not reach the window)."""
+def _chain_result(B, every, ms_per_sweep, N):
+    acf = _acf_particles(B)
+    tau, M, limited, sig = tau_int(acf, len(B))
+    tau_sw, sig_sw = tau * every, sig * every
+    sps = 1000.0 / ms_per_sweep
+    g = B.mean(axis=1) / 2.0  # bonded pairs per particle at each snapshot
+    half = len(g) // 2
+    m1, m2 = g[:half].mean(), g[half:].mean()
+    # standard error of the difference of the two halves' means, from 20 block averages
+    nb = 20 if len(g) >= 20 else max(2, len(g))
+    blk = g[: len(g) // nb * nb].reshape(nb, -1).mean(axis=1)
+    drift_se = blk.std(ddof=1) / np.sqrt(nb / 2.0) * np.sqrt(2.0)
+    ess = N * sps / (2.0 * tau_sw)
+    return {"ms_per_sweep": ms_per_sweep, "sweeps": len(B) * every, "snapshot_every": every,
+            "bonds_per_particle_halves": [float(m1), float(m2)], "drift": float(m2 - m1), "drift_se_blocks": float(drift_se),
+            "tau_int_sweeps": float(tau_sw), "tau_int_sigma_sweeps": float(sig_sw), "window_sweeps": int(M * every),
+            "tau_window_limited": bool(limited), "ess_per_s": float(ess), "ess_per_s_sigma": float(ess * sig_sw / tau_sw)}
+
+
+def learned_comparison(args, T=None, N=None, rho=None):
+    """The learned proposal against the plain move (default N=32768, rho=0.1, T=0.09). The network is trained
+    on the GPU on samples of configurations generated by the plain move; both chains then start from the
+    same configuration (the plain chain's state after the training samples) and run side by side.
+    Effective samples/s of the per-particle bond count = N x sweeps/s / (2 tau_int), tau_int Sokal's
+    windowed integrated autocorrelation time (with its window flag and error bar); the bonds-per-particle
+    averages of the two halves of each chain show whether it was stationary."""
     import patchyparticles_gb300 as pp
 
-    wl = WORKLOADS["c4"]
-    r, R, box = make_config(wl)
-    e = pp.Engine(pp.default_params(temperature=wl["T"], disp_max=wl["disp"], theta_max=wl["theta"], seed=wl["seed"]))
+    wl = dict(WORKLOADS["c4"])
+    wl["T"] = T if T is not None else args.learn_T
+    wl["N"] = N if N is not None else args.learn_N
+    wl["rho"] = rho if rho is not None else wl["rho"]
+    r, R, box = pp.generate(wl["N"], wl["rho"], wl["seed"], round_like_file=False)
+    prm = pp.default_params(temperature=wl["T"], disp_max=wl["disp"], theta_max=wl["theta"], seed=wl["seed"])
+    e = pp.Engine(prm)
     e.upload(r, R, box)
     e.learned_init(seed=7, **json.loads(args.learn_params))
     t0 = time.perf_counter()
@@ -482,18 +554,39 @@ def learned_comparison(args):
     obj = e.learned_train(args.learn_epochs, lr=3e-3)
     e.sync()
     t2 = time.perf_counter()
+    W = e.learned_weights()
     r0, R0, b0 = e.download()
-    res = {"workload": "N=32768 NVT rho=0.1 T=0.09 KF_delta=0.12 KF_cosmax=0.92, Disp_max=0.05, Theta_max=0.1 (plain component)",
+    e.close()
+    res = {"workload": "N=%d NVT rho=%g T=%g KF_delta=0.12 KF_cosmax=0.92, Disp_max=0.05, Theta_max=0.1 (plain component)" % (wl["N"], wl["rho"], wl["T"]),
+           "start": "both chains from the plain chain's state after %d sweeps (the training samples' run)" % (args.learn_configs * args.learn_sweeps_between),
            "training": {"configs": args.learn_configs, "sweeps_between": args.learn_sweeps_between, "samples": args.learn_configs * 128,
                         "epochs": args.learn_epochs, "objective": obj, "collect_s": t1 - t0, "train_s": t2 - t1,
                         "network": "36-64-64-4 ReLU, BF16 tcgen05 GEMMs, FP32 accumulation"}}
-    for name, learned in (("plain", False), ("learned", True)):
-        e.upload(r0, R0, b0)
-        e.learned_stats(reset=True)
-        res[name] = _chain(e, args.learn_measure_sweeps, 40, learned)
-    e.close()
-    res["ess_ratio"] = res["learned"]["ess_per_s"] / res["plain"]["ess_per_s"]
-    res["per_sweep_ratio"] = res["plain"]["tau_exp_sweeps"] / res["learned"]["tau_exp_sweeps"]
+    engines = []
+    for learned in (False, True):
+        x = pp.Engine(prm)
+        x.upload(r0, R0, b0)
+        x.learned_init(seed=7, **json.loads(args.learn_params))
+        x.set_learned_weights(W)
+        x.set_proposal(learned)
+        engines.append(x)
+    # cost per sweep of each chain on its own (CUDA events on the engine's stream)
+    ms = [x.time_sweeps(args.learn_time_sweeps) / args.learn_time_sweeps for x in engines]
+    engines[1].learned_stats(reset=True)
+    Bs = _chains(engines, args.learn_measure_sweeps, args.learn_every)
+    for name, x, B, m in zip(("plain", "learned"), engines, Bs, ms):
+        res[name] = _chain_result(B, args.learn_every, m, wl["N"])
+    t, a = engines[1].learned_stats(reset=True)
+    tt = max(1, sum(t))
+    res["learned"]["component_share"] = [v / tt for v in t]
+    res["learned"]["component_acceptance"] = [a[k] / max(1, t[k]) for k in range(len(t))]
+    for x in engines:
+        x.close()
+    p, l = res["plain"], res["learned"]
+    res["ess_ratio"] = l["ess_per_s"] / p["ess_per_s"]
+    res["ess_ratio_sigma"] = res["ess_ratio"] * float(np.hypot(p["tau_int_sigma_sweeps"] / p["tau_int_sweeps"], l["tau_int_sigma_sweeps"] / l["tau_int_sweeps"]))
+    res["per_sweep_ratio"] = p["tau_int_sweeps"] / l["tau_int_sweeps"]
+    res["resolved"] = not (p["tau_window_limited"] or l["tau_window_limited"])
     return res
 
 
@@ -528,6 +621,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="c5", choices=sorted(WORKLOADS) + ["c3"])
+    ap.add_argument("--proposal", default="plain", choices=["plain", "learned"],
+                    help="the moves of the timed sweeps: the plain roto-translation (default) or the learned mixture")
     ap.add_argument("--precision", default="fp32-guard", choices=["fp32-guard", "fp64"],
                     help="pair tests in FP32 with the FP64 guard band (default) or every pair in FP64")
     ap.add_argument("--sweeps-per-step", type=int, default=1)
@@ -545,7 +640,11 @@ def main():
     ap.add_argument("--learn-params", default="{}", help="JSON overrides of pp_learned_params (e.g. {\"jump\": 1e-3})")
     ap.add_argument("--learn-sweeps-between", type=int, default=5)
     ap.add_argument("--learn-epochs", type=int, default=30)
-    ap.add_argument("--learn-measure-sweeps", type=int, default=16000)
+    ap.add_argument("--learn-measure-sweeps", type=int, default=200000, help="sweeps of each chain (plain and learned side by side)")
+    ap.add_argument("--learn-every", type=int, default=100, help="sweeps between bond-count snapshots")
+    ap.add_argument("--learn-time-sweeps", type=int, default=2000, help="sweeps of the per-chain cost measurement")
+    ap.add_argument("--learn-T", type=float, default=0.09)
+    ap.add_argument("--learn-N", type=int, default=32768)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

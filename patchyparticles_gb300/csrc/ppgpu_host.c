@@ -460,7 +460,7 @@ static int read_states(pp_engine *e) {
 	CU(cudaMemcpyAsync(e->h_rs, e->d.rs, sizeof(ppi_rstate) * e->nrep, cudaMemcpyDeviceToHost, e->stream));
 	int lerr = 0, berr = 0;
 	if(e->learn_ready) CU(cudaMemcpyAsync(&lerr, e->l_err, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
-	if(e->d.gbar) CU(cudaMemcpyAsync(&berr, e->d.gbar + 2, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+	if(e->d.gbar) CU(cudaMemcpyAsync(&berr, e->d.gbar + 15, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
 	CU(cudaStreamSynchronize(e->stream));
 	if(lerr) return set_err(e, PP_ERR_CUDA, "a tensor-core wait of the learned proposal timed out");
 	if(berr == PPI_E_BARRIER) return set_err(e, PP_ERR_CUDA, "grid barrier wait timed out in the persistent round kernel (the state is incomplete)");
@@ -658,8 +658,8 @@ static int commit(pp_engine *e) {
 	CU(cudaMalloc((void **) &d->rs, sizeof(ppi_rstate) * e->nrep));
 	CU(cudaMalloc((void **) &d->grid, sizeof(ppi_grid) * e->nrep));
 	CU(cudaMalloc((void **) &d->ctr, sizeof(ppi_ctr)));
-	CU(cudaMalloc((void **) &d->gbar, 4 * sizeof(int)));
-	CU(cudaMemsetAsync(d->gbar, 0, 4 * sizeof(int), e->stream));
+	CU(cudaMalloc((void **) &d->gbar, 16 * sizeof(int)));
+	CU(cudaMemsetAsync(d->gbar, 0, 16 * sizeof(int), e->stream));
 	CU(cudaMemsetAsync(d->out_bonds, 0, sizeof(int) * n1, e->stream));
 	CU(cudaMemsetAsync(d->out_overlaps, 0, sizeof(int) * n1, e->stream));
 	CU(cudaMemsetAsync(d->grid, 0, sizeof(ppi_grid) * e->nrep, e->stream));

@@ -189,8 +189,9 @@ typedef struct ppi_dev {
 	int2 *vunsure;     /* guard-band pairs of the current volume pass, decided in FP64 after it */
 	int *vun_count;
 	/* the persistent round kernel (k_round): the 8 colours of a round in one cooperative launch, a grid
-	 * barrier between colours. gbar[0] = CTA arrivals, gbar[1] = CTAs done (the last one resets both),
-	 * gbar[2] = error: a barrier wait that ran out of its limit (PPI_E_BARRIER) */
+	 * barrier between colours. gbar[0] = CTA arrivals, gbar[1 + c] = the work counter of the round's c-th
+	 * colour (both cleared before each launch), gbar[15] = sticky error: a barrier wait that ran out of its
+	 * limit (PPI_E_BARRIER) */
 	int *gbar;
 	long long bar_limit; /* SM clock cycles a barrier wait may spin before it gives up (0: default ~1 s) */
 	int bar_extra;       /* test hook: arrivals the first barrier waits for beyond the grid (1 = never completes) */

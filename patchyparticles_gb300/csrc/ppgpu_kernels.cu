@@ -1366,12 +1366,12 @@ __device__ __forceinline__ void tile_steps(const ppi_dev &d, TileSmem &S, const 
 __device__ __forceinline__ void write_list_pairs(const ppi_dev &d, TileSmem &S, int a, int n, int pos) {
 	const int i = S.mi[a];
 	const int4 *L = (const int4 *) (d.nl + (size_t) i * d.nl_k);
-	for(int k0 = 0; k0 < n; k0 += 16) {
-		int4 v[4];
+	for(int k0 = 0; k0 < n; k0 += 32) { /* up to 32 entries' loads at once: one latency for a list */
+		int4 v[8];
 #pragma unroll
-		for(int c = 0; c < 4; c++) v[c] = (k0 + 4 * c < n) ? L[(k0 >> 2) + c] : make_int4(0, 0, 0, 0);
+		for(int c = 0; c < 8; c++) v[c] = (k0 + 4 * c < n) ? L[(k0 >> 2) + c] : make_int4(0, 0, 0, 0);
 #pragma unroll
-		for(int c = 0; c < 4; c++) {
+		for(int c = 0; c < 8; c++) {
 			const int e4[4] = { v[c].x, v[c].y, v[c].z, v[c].w };
 #pragma unroll
 			for(int u = 0; u < 4; u++) {
@@ -1596,16 +1596,16 @@ __global__ void __launch_bounds__(32 * TILE_WARPS, MODE == MODE_FAST ? PPI_TILE_
  * k_colour would defer (list overflow, guard-band pairs beyond KR_UCAP) takes the same exact path.
  * Barrier: a CTA arrives once per colour (after __syncthreads, a gpu-scope fence and an atomic add); a
  * CTA waits by one thread spinning with acquire loads, then __syncthreads. Every wait is bounded by
- * d.bar_limit SM cycles: one that runs out writes PPI_E_BARRIER to gbar[2] and its CTA returns (the others
+ * d.bar_limit SM cycles: one that runs out writes PPI_E_BARRIER to gbar[15] and its CTA returns (the others
  * then run out at their next wait), so a missing CTA can never hang the GPU. The launch is cooperative,
  * so every CTA of the grid is resident. */
 #define KR_WARPS 4
 #define KR_A 32      /* attempts per warp iteration: one per lane */
 #define KR_PCAP 512  /* staged candidate positions per chunk of an iteration's pairs */
 #define KR_CCAP 128  /* staged close-pair orientation records per chunk */
-#define KR_NL0 16    /* list entries loaded with the proposal (the rest, if any, in the pair step) */
+#define KR_NL0 32    /* list entries loaded with the proposal, all in one step (the rest, if any, in the pair step) */
 #define KR_UCAP 32   /* guard-band pairs per iteration decided in place (more: the attempt is deferred) */
-#define KR_DCAP 16   /* deferred attempts a warp keeps in shared memory (more: flags in global memory) */
+#define KR_DCAP 64   /* deferred attempts a warp keeps (flushed once more than KR_DCAP - KR_A are waiting) */
 #define KR_LIMIT_DEFAULT (1ll << 31) /* SM clock cycles of a barrier wait: ~1 s at 2 GHz */
 
 struct __align__(16) RoundSmem {
@@ -1625,7 +1625,7 @@ struct __align__(16) RoundSmem {
 	int mi[KR_A], rep[KR_A], flag[KR_A], bo[KR_A], bn[KR_A];
 	int2 uns[KR_UCAP];          /* guard-band pairs: (candidate sorted position, attempt << 1 | kind) */
 	int dl[KR_DCAP];            /* list indices of deferred attempts */
-	int nu, nd, dov, total;     /* total: listed pairs of the iteration */
+	int nu, nd, pad, total;     /* total: listed pairs of the iteration */
 };
 
 /* 16 bytes global -> shared, through L2 only (cp.async.cg); completed by kr_cp_wait */
@@ -1767,18 +1767,23 @@ __device__ __forceinline__ void kr_close(const ppi_dev &d, RoundSmem &S, int q, 
 	if(cln == CL_OVER) atomicOr(&S.flag[a], TF_OVER);
 }
 
-__device__ __forceinline__ void kr_defer(const ppi_dev &d, RoundSmem &S, int col, int e) {
-	const int k = atomicAdd(&S.nd, 1);
-	if(k < KR_DCAP) S.dl[k] = e;
-	else {
-		d.dflag[(size_t) col * d.clist_cap + e] = 1;
-		S.dov = 1;
-	}
+/* remembers deferred attempt list index e (the warp flushes its list before it can overflow) */
+__device__ __forceinline__ void kr_defer(RoundSmem &S, int e) { S.dl[atomicAdd(&S.nd, 1)] = e; }
+
+/* the warp's deferred attempts, one per lane, each exactly on its own (same-colour attempts are
+ * independent, so when they run does not matter) */
+__device__ __forceinline__ void kr_flush_deferred(const ppi_dev &d, RoundSmem &S, const int4 *list, const int lane, long long round, Acc &A) {
+	__syncwarp();
+	const int nd = S.nd;
+	for(int k = lane; k < nd; k += 32) attempt_exact<MODE_FAST>(d, list[S.dl[k]], round, A);
+	__syncwarp();
+	if(lane == 0) S.nd = 0;
+	__syncwarp();
 }
 
 /* steps 2 and 3 of the iteration whose step 1 left n pairs and list entries e[] in this lane */
 __device__ __forceinline__ void kr_iteration(const ppi_dev &d, RoundSmem &S, const int lane, const int n, const int start, const int loc, const int b,
-		const int col, long long round, Acc &A) {
+		long long round, Acc &A) {
 	const unsigned lt = (1u << lane) - 1u;
 	__syncwarp();
 	const int total = S.total;
@@ -1857,7 +1862,7 @@ __device__ __forceinline__ void kr_iteration(const ppi_dev &d, RoundSmem &S, con
 	const int a = lane, flag = S.flag[a];
 	if(flag & (TF_OVER | TF_CLOSED)) return;
 	if(flag & TF_DEFER) {
-		kr_defer(d, S, col, b + a);
+		kr_defer(S, b + a);
 		return;
 	}
 	const int r = S.rep[a];
@@ -1886,7 +1891,7 @@ __device__ __forceinline__ bool kr_barrier_wait(const ppi_dev &d, unsigned targe
 			asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(d.gbar) : "memory");
 			if(v >= target) break;
 			if(clock64() - t0 > limit) {
-				atomicExch(d.gbar + 2, PPI_E_BARRIER);
+				atomicExch(d.gbar + 15, PPI_E_BARRIER);
 				*s_abort = 1;
 				break;
 			}
@@ -1921,33 +1926,31 @@ __global__ void __launch_bounds__(32 * KR_WARPS, 2) k_round(ppi_dev d, long long
 		const int4 *list = d.clist + (size_t) col * d.clist_cap;
 		int cnt = d.ccount[col];
 		if(cnt > d.clist_cap) cnt = d.clist_cap;
-		/* every warp an equal share of the colour's list */
-		const int lo = (int) ((long long) warp * cnt / nwarp), hi = (int) ((long long) (warp + 1) * cnt / nwarp);
-		if(lane == 0) {
-			S.nd = 0;
-			S.dov = 0;
-		}
-		__syncwarp();
-		int loc = 0, start = 0;
-		int n = kr_setup(d, S, lane, lo + lane < hi ? list[lo + lane] : none, round, A, start, loc);
+		/* iterations of KR_A list entries, handed out one at a time from the colour's work counter
+		 * (gbar[1 + ci]); a warp fetches its next one while it works on the current one */
+		const int nit = (cnt + KR_A - 1) / KR_A;
+		unsigned *work = (unsigned *) d.gbar + 1 + ci;
+		if(lane == 0) S.nd = 0;
+		/* lane 0 keeps the counter's answer in a register and the warp reads it one iteration later, so
+		 * the atomic's latency hides behind the work */
+		unsigned pend = 0;
+		if(lane == 0) pend = atomicAdd(work, 1u);
+		int it = (int) __shfl_sync(0xffffffffu, pend, 0);
+		if(lane == 0 && it < nit) pend = atomicAdd(work, 1u);
+		int loc = 0, start = 0, n = 0;
+		if(it < nit) n = kr_setup(d, S, lane, it * KR_A + lane < cnt ? list[it * KR_A + lane] : none, round, A, start, loc);
 		if(ci > 0 && !kr_barrier_wait(d, (unsigned) (ci * gridDim.x + (ci == 1 ? d.bar_extra : 0)), limit, &s_abort)) return;
-		for(int b = lo; b < hi; b += KR_A) {
-			const int4 next = b + KR_A + lane < hi ? list[b + KR_A + lane] : none;
-			kr_iteration(d, S, lane, n, start, loc, b, col, round, A);
+		while(it < nit) {
+			const int nxt = (int) __shfl_sync(0xffffffffu, pend, 0);
+			const int4 next = nxt < nit && nxt * KR_A + lane < cnt ? list[nxt * KR_A + lane] : none;
+			if(lane == 0 && nxt < nit) pend = atomicAdd(work, 1u);
+			kr_iteration(d, S, lane, n, start, loc, it * KR_A, round, A);
 			__syncwarp();
-			if(b + KR_A < hi) n = kr_setup(d, S, lane, next, round, A, start, loc);
+			if(S.nd > KR_DCAP - KR_A) kr_flush_deferred(d, S, list, lane, round, A);
+			it = nxt;
+			if(it < nit) n = kr_setup(d, S, lane, next, round, A, start, loc);
 		}
-		/* the deferred attempts, one per lane, exactly */
-		const int nd = S.nd < KR_DCAP ? S.nd : KR_DCAP;
-		for(int k = lane; k < nd; k += 32) attempt_exact<MODE_FAST>(d, list[S.dl[k]], round, A);
-		if(S.dov) {
-			unsigned char *fl = d.dflag + (size_t) col * d.clist_cap;
-			for(int x = lo + lane; x < hi; x += 32)
-				if(fl[x]) {
-					fl[x] = 0;
-					attempt_exact<MODE_FAST>(d, list[x], round, A);
-				}
-		}
+		kr_flush_deferred(d, S, list, lane, round, A);
 		/* close the colour: every warp of the CTA is done, its writes are visible at gpu scope */
 		__syncthreads();
 		if(threadIdx.x == 0) {
@@ -4195,7 +4198,7 @@ static int round_grid(void) {
 static int launch_persistent_round(const ppi_dev *d, long long round, const int *colours, cudaStream_t s) {
 	int packed = 0;
 	for(int ci = 0; ci < 8; ci++) packed |= (colours[ci] & 7) << (3 * ci);
-	cudaMemsetAsync(d->gbar, 0, 2 * sizeof(int), s);
+	cudaMemsetAsync(d->gbar, 0, 9 * sizeof(int), s); /* the arrival counter and the colours' work counters (not the error word) */
 	cudaLaunchConfig_t cfg;
 	memset(&cfg, 0, sizeof(cfg));
 	cfg.gridDim = dim3(round_grid());

@@ -85,7 +85,7 @@ def test_learned_audit_mode_has_no_mismatches(built):
     e.close()
 
 
-def _bonds_series(learned, weights, nrep=8, N=1000, rho=0.3, T=0.2, sweeps=6000, every=20, burn=1500):
+def _bonds_series(learned, weights, nrep=16, N=1000, rho=0.3, T=0.2, sweeps=8000, every=20, burn=1500):
     prm = [pp.default_params(temperature=T, seed=100 + k, disp_max=0.1, theta_max=0.2) for k in range(nrep)]
     e = pp.Engine(prm)
     for k in range(nrep):
@@ -105,7 +105,8 @@ def _bonds_series(learned, weights, nrep=8, N=1000, rho=0.3, T=0.2, sweeps=6000,
 
 def test_learned_chain_samples_the_plain_chains_distribution(built):
     """Exactness of the MH correction: with a network whose mixture depends strongly on the environment,
-    the equilibrium bonds per particle equal the plain move's (8 independent replicas each)."""
+    the equilibrium bonds per particle equal the plain move's within two standard errors (16 independent
+    replicas each, 8000 sweeps after 1500 of burn-in; the per-replica time averages are the samples)."""
     W = mo.init_params(seed=11, out_scale=3.0)
     W[mo.OFF_B3:] = [0.0, 1.0, 1.5, 0.5]
     a = _bonds_series(False, W)
@@ -113,7 +114,8 @@ def test_learned_chain_samples_the_plain_chains_distribution(built):
     ma, mb = a.mean(0), b.mean(0)  # per-replica time averages: independent estimates
     diff = mb.mean() - ma.mean()
     se = np.sqrt(ma.var(ddof=1) / len(ma) + mb.var(ddof=1) / len(mb))
-    assert abs(diff) < 4 * se + 1e-3, (ma.mean(), mb.mean(), se)
+    print("bonds per particle: plain %.5f learned %.5f se %.5f z %.2f" % (ma.mean(), mb.mean(), se, diff / se))
+    assert abs(diff) < 2 * se, (ma.mean(), mb.mean(), se)
 
 
 def test_collect_and_train_on_the_gpu(built):

@@ -87,4 +87,4 @@ def test_box_shape_statistics_match_the_reference(built):
     g = gpu_runs(r, R, box, gkw, 200, 4000, 10, lambda e, k: e.box(k)[0])
     z, se = zscore(g, o)
     print("Lx move <Lx>: gpu %.4f oracle %.4f se %.4f z %.2f" % (g.mean(), o.mean(), se, z))
-    assert abs(z) < 2.5
+    assert abs(z) < 2.0  # two combined standard errors of the 16 + 16 run means

@@ -51,6 +51,7 @@ def test_persistent_round_equals_one_launch_per_colour(built, graphs, names, ens
 def test_persistent_round_state_agrees_with_the_oracle(built):
     r, R, box = config("c5")
     e = pp.Engine(pp.default_params(temperature=0.11, ensemble=pp.NPT, pressure=0.05, seed=5))
+    e.set_persistent(True)
     e.upload(r, R, box)
     e.sweeps(24)
     e.sync()
@@ -64,6 +65,7 @@ def test_persistent_round_state_agrees_with_the_oracle(built):
 def test_barrier_wait_that_runs_out_is_reported_and_the_gpu_stays_usable(built):
     r, R, box = config("c5")
     e = pp.Engine(pp.default_params(temperature=0.11, seed=3))
+    e.set_persistent(True)
     e.upload(r, R, box)
     # ~1 ms per wait; the first barrier of every round waits for one arrival more than the grid makes
     e.set_barrier_test(limit_cycles=2_000_000, unreachable=True)
