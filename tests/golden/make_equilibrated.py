@@ -81,7 +81,7 @@ def cpu_stage(indir, sweeps):
                 rho.append(s.N / np.prod(s.box()))
             tmp = os.path.join(OUT, "%s_%d.rrr" % (name, k))
             s.save(tmp, 0)
-            with open(tmp, "rb") as f, gzip.open(tmp + ".gz", "wb", mtime=0) as g:
+            with open(tmp, "rb") as f, open(tmp + ".gz", "wb") as raw, gzip.GzipFile(fileobj=raw, mode="wb", mtime=0) as g:
                 shutil.copyfileobj(f, g)
             os.remove(tmp)
             res[k] = (np.mean(E[:50]), np.mean(E[50:]), np.mean(rho[:50]), np.mean(rho[50:]))
