@@ -36,6 +36,10 @@ struct orc_system {
 	int *head, *next, *cell, *cell_old;
 	/* drand48 state X (48 bits) */
 	unsigned long long X;
+	/* GC / SUS: particle capacity, SUS histogram, the full-system stop */
+	int cap;
+	long long *sus_hist;
+	int error;
 };
 
 /* ---------------------------------------------------------------- drand48 (POSIX recurrence) */
@@ -552,6 +556,73 @@ static void o_change_lx(orc_system *s) {
 	}
 }
 
+/* MC_add_remove (MC.c:342-448): an insertion at a uniform position with a random orientation, accepted
+ * with exp(-dE / T) z V / (N + 1), or the removal of a uniformly chosen particle, accepted with
+ * exp(-dE / T) N / (V z); the last particle takes the removed one's index (and memory position) */
+static void o_add_remove(orc_system *s) {
+	if(orc_drand(s) < 0.5) {
+		if(s->N == s->prm.n_max) {
+			if(s->prm.ensemble == ORC_GC) s->error = 1; /* output_exit in the reference */
+			return;
+		}
+		s->tries[ORC_ADD]++;
+		const int p = s->N;
+		double *r = s->r + 3 * p;
+		r[0] = orc_drand(s) * s->box[0];
+		r[1] = orc_drand(s) * s->box[1];
+		r[2] = orc_drand(s) * s->box[2];
+		o_random_orientation(s, s->R + 9 * p);
+		o_set_patches(s, p);
+		const double dE = o_energy(s, p);
+		const double acc = exp(-dE / s->prm.T) * s->prm.activity * s->V / (s->N + 1.);
+		if(!s->overlap && orc_drand(s) < acc) {
+			s->energy += dE;
+			int ind[3];
+			const int c = o_cell_index(s, r, ind);
+			s->next[p] = s->head[c];
+			s->head[c] = p;
+			s->cell[p] = s->cell_old[p] = c;
+			s->N++;
+			s->accepted[ORC_ADD]++;
+		}
+		else s->overlap = 0;
+	}
+	else {
+		if(s->N == s->prm.n_min) return;
+		s->tries[ORC_REMOVE]++;
+		const int p = (int) (orc_drand(s) * s->N);
+		const double dE = -o_energy(s, p);
+		const double acc = exp(-dE / s->prm.T) * s->N / (s->V * s->prm.activity);
+		if(orc_drand(s) < acc) {
+			s->energy += dE;
+			s->N--;
+			o_unlink(s, p, s->cell[p]);
+			if(p != s->N) {
+				const int q = s->N;
+				o_unlink(s, q, s->cell[q]);
+				memcpy(s->r + 3 * p, s->r + 3 * q, 3 * sizeof(double));
+				memcpy(s->R + 9 * p, s->R + 9 * q, 9 * sizeof(double));
+				o_set_patches(s, p);
+				s->cell[p] = s->cell[q];
+				s->next[p] = s->head[s->cell[p]];
+				s->head[s->cell[p]] = p;
+			}
+			s->accepted[ORC_REMOVE]++;
+		}
+	}
+}
+
+/* one iteration of the do_GC (MC.c:31-43) / do_SUS (MC.c:45-58) loop body */
+static void o_attempt_gc(orc_system *s) {
+	const double R = orc_drand(s);
+	if(R < 0.01) {
+		o_add_remove(s);
+		if(s->prm.ensemble == ORC_SUS) s->sus_hist[s->N - s->prm.n_min]++;
+	}
+	else if(s->prm.lx_move && R < (0.01 + 1. / s->N)) o_change_lx(s);
+	else if(s->N > 0) o_move_rototranslate(s);
+}
+
 /* one iteration of the do_NVT (MC.c:19-29) or do_NPT (MC.c:60-68) loop body */
 static void o_attempt(orc_system *s) {
 	if(s->prm.ensemble == ORC_NPT) {
@@ -567,7 +638,23 @@ static void o_attempt(orc_system *s) {
 }
 
 void orc_sweep(orc_system *s) {
+	if(s->prm.ensemble == ORC_GC || s->prm.ensemble == ORC_SUS) {
+		for(int i = 0; i < s->prm.n_max && !s->error; i++) o_attempt_gc(s);
+		return;
+	}
 	for(int i = 0; i < s->N; i++) o_attempt(s);
+}
+
+int orc_error(const orc_system *s) { return s->error; }
+
+int orc_sus_hist(orc_system *s, long long *out, int reset) {
+	const int n = s->prm.n_max - s->prm.n_min + 1;
+	if(s->sus_hist == NULL) return 0;
+	for(int i = 0; i < n; i++) {
+		if(out) out[i] = s->sus_hist[i];
+		if(reset) s->sus_hist[i] = 0;
+	}
+	return n;
 }
 
 void orc_sweeps(orc_system *s, long long n) {
@@ -596,7 +683,18 @@ static orc_system *o_alloc(int N, const orc_params *prm) {
 	if(s == NULL) return NULL;
 	s->prm = *prm;
 	s->N = N;
-	size_t n = N > 0 ? (size_t) N : 1;
+	/* GC / SUS systems keep room for n_max particles (system.c:199) */
+	const int gc = prm->ensemble == ORC_GC || prm->ensemble == ORC_SUS;
+	s->cap = gc && prm->n_max > N ? prm->n_max : N;
+	if(prm->ensemble == ORC_GC) s->prm.n_min = 0;
+	size_t n = s->cap > 0 ? (size_t) s->cap : 1;
+	if(prm->ensemble == ORC_SUS) {
+		s->sus_hist = calloc((size_t) (prm->n_max - prm->n_min + 1 > 0 ? prm->n_max - prm->n_min + 1 : 1), sizeof(long long));
+		if(s->sus_hist == NULL) {
+			free(s);
+			return NULL;
+		}
+	}
 	s->r = calloc(3 * n, sizeof(double));
 	s->r_old = calloc(3 * n, sizeof(double));
 	s->R = calloc(9 * n, sizeof(double));
@@ -711,6 +809,7 @@ orc_system *orc_from_arrays(int N, const double *r, const double *R, const doubl
 
 void orc_free(orc_system *s) {
 	if(s == NULL) return;
+	free(s->sus_hist);
 	free(s->r);
 	free(s->r_old);
 	free(s->R);

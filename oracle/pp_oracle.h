@@ -25,10 +25,14 @@ extern "C" {
 #define ORC_PATCH_BOND 1
 
 #define ORC_NVT 0
+#define ORC_GC 1  /* grand canonical (defs.h:22), do_GC (MC.c:31-43) */
+#define ORC_SUS 3 /* successive umbrella sampling (defs.h:23), do_SUS (MC.c:45-58) */
 #define ORC_NPT 5
 
 /* move-type slots of the tries/accepted counters, as in defs.h:11-19 */
 #define ORC_ROTO_TRASL 0
+#define ORC_ADD 2    /* defs.h:14 */
+#define ORC_REMOVE 3 /* defs.h:15 */
 #define ORC_VOLUME 6
 #define ORC_LX 7 /* defs.h:19 */
 #define ORC_N_MOVES 8
@@ -46,6 +50,8 @@ typedef struct orc_params {
 	int lx_move;               /* Lx_move (NVT only, system.c:165-196) */
 	double lx_change_max;      /* Lx_change_max */
 	double lyz_min, lyz_max;   /* Lyz_min, Lyz_max */
+	double activity;           /* Activity z (GC and SUS, system.c:91) */
+	int n_min, n_max;          /* GC: 0 and GC_N_max; SUS: Umbrella_sampling_min / _max (system.c:92-103) */
 } orc_params;
 
 typedef struct orc_system orc_system;
@@ -78,7 +84,8 @@ double orc_energies(orc_system *s, double *E, int *overlap, int *n_bonds, int *n
 /* Bonded partner lists: offsets (N+1) and partners (capacity cap). Returns total or -1 if cap too small. */
 int orc_bond_lists(orc_system *s, int *offsets, int *partners, int cap);
 
-/* One Monte Carlo step of the ensemble: do_NVT (MC.c:19-29) or do_NPT (MC.c:60-68). */
+/* One Monte Carlo step of the ensemble: do_NVT (MC.c:19-29), do_GC (MC.c:31-43), do_SUS (MC.c:45-58) or
+ * do_NPT (MC.c:60-68). GC and SUS systems hold up to n_max particles; orc_N is the current count. */
 void orc_sweep(orc_system *s);
 void orc_sweeps(orc_system *s, long long n);
 /* MC_check_energy (MC.c:766-784). Returns 0, -1 (overlap found) or -2 (energy drift > 1e-5). */
@@ -90,6 +97,13 @@ int orc_save_rrr(const orc_system *s, long long step, const char *path);
  * r (N x 3), R (N x 9 rows) and the cubic box, unrounded (generated.rrr holds them printed with %lf /
  * %.12lf). Returns 0, or -1 for a density outside (0, 0.7] or no memory. */
 int orc_generate(int N, double density, int seed, double *r, double *R, double box[3]);
+
+/* 1 once a GC insertion found the system full (the reference stops there: "increase GC_N_max",
+ * MC.c:346-348; the oracle makes no further move), else 0. */
+int orc_error(const orc_system *s);
+/* SUS histogram of N after every insertion/removal attempt (MC.c:50), bins N_min..N_max; reset = 1 clears
+ * it as output_and_reset_sus does (output.c:343-356). Returns the number of bins. */
+int orc_sus_hist(orc_system *s, long long *out, int reset);
 
 /* drand48 recurrence check: n draws from a generator seeded as srand48(seed) would be. */
 void orc_drand48_sequence(int seed, int n, double *out);

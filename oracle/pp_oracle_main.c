@@ -1,6 +1,6 @@
 /*
  * pp_oracle_main.c -- TEST INFRASTRUCTURE: command-line driver of the oracle restatement, mirroring the
- * reference main loop (main.c:26-143) for Dynamics = 0 in the NVT and NPT ensembles, with the reference
+ * reference main loop (main.c:26-143) for Dynamics = 0 in the NVT, NPT, GC and SUS ensembles, with the reference
  * input-file rules (parse_input.c:18-104) and output files (output.c:19-211, 302-317). Used to show that
  * the restatement reproduces the reference trajectory: same input file -> same energy.dat,
  * acceptance.dat, density.dat, stdout and configuration files.
@@ -115,10 +115,15 @@ int main(int argc, char *argv[]) {
 	if(access(folder, W_OK) != 0) die("Cannot create files in the configuration folder");
 	const char *last = (v = get(in, "Configuration_last", 0)) ? v : "last.rrr";
 	int ensemble = atoi(get(in, "Ensemble", 1));
+	const char *sus_folder = NULL;
 	if(ensemble != 0) {
 		const char *dname = (v = get(in, "Density_file", 0)) ? v : "density.dat";
 		fd = fopen(dname, mode);
 		if(fd == NULL) die("Density file not writable");
+		if(ensemble == ORC_SUS) { /* output.c:79-84 */
+			sus_folder = get(in, "Umbrella_sampling_folder", 1);
+			if(access(sus_folder, W_OK) != 0) die("Cannot create files in the umbrella sampling folder");
+		}
 	}
 
 	/* system_init (system.c:58-252), Dynamics = 0, NVT or NPT */
@@ -134,6 +139,14 @@ int main(int argc, char *argv[]) {
 	prm.seed = atoi(v);
 	prm.kf_delta = atof(get(in, "KF_delta", 1));
 	prm.kf_cosmax = atof(get(in, "KF_cosmax", 1));
+	if(ensemble == ORC_GC || ensemble == ORC_SUS) { /* system.c:90-103 */
+		prm.activity = atof(get(in, "Activity", 1));
+		if(ensemble == ORC_GC) prm.n_max = atoi(get(in, "GC_N_max", 1));
+		else {
+			prm.n_min = atoi(get(in, "Umbrella_sampling_min", 1));
+			prm.n_max = atoi(get(in, "Umbrella_sampling_max", 1));
+		}
+	}
 	if(ensemble == ORC_NPT) {
 		prm.rescale_factor_max = atof(get(in, "rescale_factor_max", 1));
 		prm.P = atof(get(in, "P", 1));
@@ -150,10 +163,22 @@ int main(int argc, char *argv[]) {
 		fb = fopen("boxshape.dat", mode);
 		if(fb == NULL) die("boxshape.dat is not writable");
 	}
-	if(dynamics != 0 || (ensemble != ORC_NVT && ensemble != ORC_NPT)) die("only Dynamics = 0 with Ensemble 0 or 5 is restated");
+	if(dynamics != 0 || (ensemble != ORC_NVT && ensemble != ORC_NPT && ensemble != ORC_GC && ensemble != ORC_SUS))
+		die("only Dynamics = 0 with Ensemble 0, 1, 3 or 5 is restated");
 	char err[512];
 	orc_system *s = orc_load_rrr(conf, &prm, err, sizeof(err));
 	if(s == NULL) die(err);
+	if(ensemble == ORC_SUS) { /* system.c:100-101 */
+		char m[256];
+		if(orc_N(s) < prm.n_min) {
+			snprintf(m, sizeof(m), "Number of particles %d is smaller than Umbrella_sampling_min (%d)", orc_N(s), prm.n_min);
+			die(m);
+		}
+		if(orc_N(s) > prm.n_max) {
+			snprintf(m, sizeof(m), "Number of particles %d is larger than Umbrella_sampling_max (%d)", orc_N(s), prm.n_max);
+			die(m);
+		}
+	}
 	if(prm.lx_move) {
 		double b[3];
 		orc_box(s, b);
@@ -176,6 +201,7 @@ int main(int argc, char *argv[]) {
 	long long tries[ORC_N_MOVES], acc[ORC_N_MOVES];
 	char name[1100];
 	for(step = start_from; step < steps; step++) {
+		N = orc_N(s);
 		if(step % print_every == 0) { /* output_print (output.c:119-211) */
 			double energy = orc_get_energy(s);
 			double E = N > 0 ? energy / N : 0;
@@ -195,6 +221,10 @@ int main(int argc, char *argv[]) {
 			orc_counters(s, tries, acc);
 			fprintf(fa, "%lld", step);
 			fprintf(fa, " %e", acc[ORC_ROTO_TRASL] / (double) tries[ORC_ROTO_TRASL]);
+			if(ensemble == ORC_GC || ensemble == ORC_SUS) {
+				fprintf(fa, " %e", acc[ORC_ADD] / (double) tries[ORC_ADD]);
+				fprintf(fa, " %e", acc[ORC_REMOVE] / (double) tries[ORC_REMOVE]);
+			}
 			if(ensemble == ORC_NPT) fprintf(fa, " %e", acc[ORC_VOLUME] / (double) tries[ORC_VOLUME]);
 			if(prm.lx_move) fprintf(fa, " %e", acc[ORC_LX] / (double) tries[ORC_LX]);
 			fprintf(fa, "\n");
@@ -208,6 +238,18 @@ int main(int argc, char *argv[]) {
 				int rc = orc_check_energy(s);
 				if(rc == -1) die("\nComputing energy from scratch resulted in an overlap, aborting");
 				if(rc == -2) die("\nEnergy check failed");
+				if(ensemble == ORC_SUS) { /* output_and_reset_sus (output.c:343-356) */
+					long long h[4096];
+					const int nb = orc_sus_hist(s, NULL, 0);
+					if(nb > 4096) die("SUS window too wide for this driver");
+					orc_sus_hist(s, h, 1);
+					snprintf(name, sizeof(name), "%s/sus-%lld.dat", sus_folder, step);
+					FILE *fs = fopen(name, "w");
+					if(fs == NULL) die("SUS file not writable");
+					for(int b = 0; b < nb; b++)
+						if(h[b] > 0) fprintf(fs, "%d %lld\n", b + prm.n_min, h[b]);
+					fclose(fs);
+				}
 			}
 		}
 		if(step > 0 && step % save_every == 0) {
@@ -216,7 +258,12 @@ int main(int argc, char *argv[]) {
 			orc_save_rrr(s, step, last);
 		}
 		orc_sweep(s);
+		if(orc_error(s)) { /* MC_add_remove's output_exit */
+			fprintf(stderr, "The system contains the maximum number of particles set in the input file (%d), increase GC_N_max\n", prm.n_max);
+			exit(1);
+		}
 	}
+	N = orc_N(s);
 	orc_save_rrr(s, step, last);
 	double energy = orc_get_energy(s);
 	printf("%lld %lf %lf", step, N > 0 ? energy / N : 0, energy);

@@ -16,6 +16,8 @@ CLI = os.path.join(HERE, "_build", "pporacle")
 REF_DIR = os.path.join(HERE, "_ref")
 
 NVT = 0
+GC = 1
+SUS = 3
 NPT = 5
 
 
@@ -34,6 +36,9 @@ class OrcParams(ctypes.Structure):
         ("lx_change_max", ctypes.c_double),
         ("lyz_min", ctypes.c_double),
         ("lyz_max", ctypes.c_double),
+        ("activity", ctypes.c_double),
+        ("n_min", ctypes.c_int),
+        ("n_max", ctypes.c_int),
     ]
 
 
@@ -89,6 +94,8 @@ def lib():
             "orc_save_rrr": (ctypes.c_int, [vp, ctypes.c_longlong, ctypes.c_char_p]),
             "orc_drand48_sequence": (None, [ctypes.c_int, ctypes.c_int, dp]),
             "orc_generate": (ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_int, dp, dp, dp]),
+            "orc_error": (ctypes.c_int, [vp]),
+            "orc_sus_hist": (ctypes.c_int, [vp, llp, ctypes.c_int]),
             "orc_parallel_throughput": (ctypes.c_double, [ctypes.c_int, dp, dp, dp, ctypes.POINTER(OrcParams), ctypes.c_int, ctypes.c_double, llp]),
             "orc_pool_create": (vp, [ctypes.c_int, dp, dp, dp, ctypes.POINTER(OrcParams), ctypes.c_int]),
             "orc_pool_run": (ctypes.c_double, [vp, ctypes.c_double, llp]),
@@ -111,8 +118,9 @@ def _ip(a):
 
 
 def params(ensemble=NVT, T=0.12, P=0.0, disp_max=0.05, theta_max=0.1, rescale_factor_max=0.01, kf_delta=0.12, kf_cosmax=0.92, seed=1,
-           lx_move=0, lx_change_max=0.0, lyz_min=0.0, lyz_max=0.0):
-    return OrcParams(ensemble, T, P, disp_max, theta_max, rescale_factor_max, kf_delta, kf_cosmax, seed, lx_move, lx_change_max, lyz_min, lyz_max)
+           lx_move=0, lx_change_max=0.0, lyz_min=0.0, lyz_max=0.0, activity=0.0, n_min=0, n_max=0):
+    return OrcParams(ensemble, T, P, disp_max, theta_max, rescale_factor_max, kf_delta, kf_cosmax, seed, lx_move, lx_change_max, lyz_min, lyz_max,
+                     activity, n_min, n_max)
 
 
 class System:
@@ -208,6 +216,19 @@ class System:
 
     def check_energy(self):
         return self.L.orc_check_energy(self.h)
+
+    def num_particles(self):
+        """Current particle count (changes in the GC and SUS ensembles)."""
+        return self.L.orc_N(self.h)
+
+    def error(self):
+        return self.L.orc_error(self.h)
+
+    def sus_histogram(self, reset=False):
+        n = self.L.orc_sus_hist(self.h, None, 0)
+        h = (ctypes.c_longlong * max(n, 1))()
+        self.L.orc_sus_hist(self.h, h, 1 if reset else 0)
+        return list(h)[:n]
 
     def save(self, path, step=0):
         return self.L.orc_save_rrr(self.h, step, path.encode())

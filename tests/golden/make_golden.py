@@ -66,6 +66,11 @@ TRAJ = [
     ("small_npt", "generator_300_0.3_4242.rrr", 5, 0.11, 300, 30, 9, "P = 0.05\nrescale_factor_max = 0.01\n"),
     # the box-shape move of NVT (MC.c:515-585): Lx changes, Ly = Lz follow at constant volume
     ("small_lx", "generator_300_0.3_4242.rrr", 0, 0.11, 400, 40, 11, "Lx_move = 1\nLx_change_max = 0.5\nLyz_min = 8.0\nLyz_max = 12.0\n"),
+    # grand canonical insertions and removals (MC.c:31-43, 342-448) and successive umbrella sampling in an
+    # N window (MC.c:45-58, with its histogram files, output.c:343-356)
+    ("small_gc", "generator_300_0.3_4242.rrr", 1, 0.12, 300, 30, 13, "Activity = 0.1\nGC_N_max = 600\n"),
+    ("small_sus", "generator_300_0.3_4242.rrr", 3, 0.12, 300, 30, 17,
+     "Activity = 0.1\nUmbrella_sampling_min = 295\nUmbrella_sampling_max = 305\nUmbrella_sampling_folder = sus\n"),
 ]
 
 PROBE_INPUT = """Dynamics = 0
@@ -118,6 +123,8 @@ def main():
     for name, conf, ens, T, steps, pe, seed, extra in TRAJ:
         d = os.path.join(work, name)
         os.makedirs(os.path.join(d, "confs"))
+        if "Umbrella_sampling_folder" in extra:
+            os.makedirs(os.path.join(d, "sus"))
         shutil.copy(os.path.join(work, conf), os.path.join(d, conf))
         open(os.path.join(d, "input"), "w").write(TRAJ_INPUT.format(ensemble=ens, seed=seed, T=T, steps=steps, print_every=pe, save_every=pe * 2, conf=conf, extra=extra))
         out = subprocess.check_output([os.path.join(REFOUT, "PatchyParticles"), "input"], cwd=d, stderr=subprocess.DEVNULL)
@@ -129,6 +136,10 @@ def main():
             if os.path.exists(os.path.join(d, fn)):
                 shutil.copy(os.path.join(d, fn), os.path.join(dst, fn))
         gz_write(os.path.join(dst, "last.rrr.gz"), open(os.path.join(d, "last.rrr"), "rb").read())
+        if os.path.isdir(os.path.join(d, "sus")):
+            os.makedirs(os.path.join(dst, "sus"), exist_ok=True)
+            for fn in sorted(os.listdir(os.path.join(d, "sus"))):
+                shutil.copy(os.path.join(d, "sus", fn), os.path.join(dst, "sus", fn))
     shutil.rmtree(work)
     print("golden fixtures written to", OUT)
 

@@ -21,7 +21,8 @@ REF = reference_dir()
 def fixture_files(top):
     out = []
     for d, dirs, files in os.walk(top):
-        dirs[:] = [x for x in dirs if x != "__pycache__"]
+        # equilibrated/ comes from make_equilibrated.py (a GPU pre-equilibration), not from the reference
+        dirs[:] = [x for x in dirs if x not in ("__pycache__", "equilibrated")]
         for f in files:
             if f.endswith((".py", ".pyc")):
                 continue

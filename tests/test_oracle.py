@@ -50,12 +50,15 @@ def test_known_answers(built):
         assert E == want and not ov
 
 
-@pytest.mark.parametrize("name", ["fcc_nvt", "bcc_npt", "small_nvt", "small_npt", "small_lx"])
+@pytest.mark.parametrize("name", ["fcc_nvt", "bcc_npt", "small_nvt", "small_npt", "small_lx", "small_gc", "small_sus"])
 def test_oracle_trajectory_matches_reference(built, name):
-    """The restated main loop reproduces the reference's output files line for line."""
+    """The restated main loop reproduces the reference's output files line for line (NVT, NPT, the Lx
+    move, grand canonical insertions and removals, successive umbrella sampling with its histograms)."""
     src = helpers.golden_path("traj_" + name)
     work = tempfile.mkdtemp(prefix="pptraj_")
     os.makedirs(os.path.join(work, "confs"))
+    if os.path.isdir(os.path.join(src, "sus")):
+        os.makedirs(os.path.join(work, "sus"))
     shutil.copy(os.path.join(src, "input"), work)
     conf = [l.split("=")[1].strip() for l in open(os.path.join(src, "input")) if l.startswith("Initial_conditions_file")][0]
     helpers.unpack_golden(conf, work)
@@ -68,6 +71,11 @@ def test_oracle_trajectory_matches_reference(built, name):
     import gzip
 
     assert open(os.path.join(work, "last.rrr"), "rb").read() == gzip.open(os.path.join(src, "last.rrr.gz")).read()
+    if os.path.isdir(os.path.join(src, "sus")):
+        want = sorted(os.listdir(os.path.join(src, "sus")))
+        assert want and sorted(os.listdir(os.path.join(work, "sus"))) == want
+        for fn in want:
+            assert open(os.path.join(work, "sus", fn)).read() == open(os.path.join(src, "sus", fn)).read(), fn
     shutil.rmtree(work)
 
 
