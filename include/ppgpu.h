@@ -38,9 +38,13 @@ extern "C" {
 
 /* ------------------------------------------------------------------ constants shared with the reference */
 #define PP_NVT 0 /* Ensemble = 0 (defs.h:21) */
+#define PP_GC 1  /* Ensemble = 1, grand canonical (defs.h:22, do_GC MC.c:31-43) */
+#define PP_SUS 3 /* Ensemble = 3, successive umbrella sampling (defs.h:23, do_SUS MC.c:45-58) */
 #define PP_NPT 5 /* Ensemble = 5 (defs.h:24) */
 
 #define PP_MOVE_ROTO_TRASL 0 /* tries/accepted slots as System::tries/accepted (defs.h:11-19, 95-96) */
+#define PP_MOVE_ADD 2        /* GC / SUS insertions (defs.h:14) */
+#define PP_MOVE_REMOVE 3     /* GC / SUS removals (defs.h:15) */
 #define PP_MOVE_VOLUME 6
 #define PP_MOVE_LX 7 /* the NVT box-shape move (defs.h:19) */
 #define PP_N_MOVES 8
@@ -68,6 +72,11 @@ typedef struct pp_params {
 	int lx_move;
 	double lx_change_max;      /* Lx_change_max */
 	double lyz_min, lyz_max;   /* Lyz_min, Lyz_max: allowed range of Ly = Lz (absolute lengths) */
+	/* GC and SUS (system.c:90-103): Activity z; GC_N_max (GC), or Umbrella_sampling_min / _max (SUS).
+	 * An engine holds one GC or SUS system; its particles are 0 .. N-1 at every moment (a removal gives the
+	 * highest index to the removed particle's, as the reference does). */
+	double activity;
+	int n_min, n_max;
 } pp_params;
 
 typedef struct pp_counters {
@@ -164,6 +173,13 @@ int pp_gpu_kernel_stats(pp_engine *e, pp_kernel_stats *out, int reset);
  * instead of one per kernel; the launches and the trajectory are the same). enable = 0 turns the graphs
  * off (every kernel launched on the stream); per-group event timing always uses stream launches. */
 int pp_gpu_set_graphs(pp_engine *e, int enable);
+
+/* SUS (Ensemble = 3): the histogram of N counted after every insertion / removal attempt (MC.c:50), bins
+ * Umbrella_sampling_min .. Umbrella_sampling_max, into hist (may be NULL); reset = 1 clears it, as
+ * output_and_reset_sus does at every print (output.c:343-356, main.c:89). Insertions and removals
+ * (MC_add_remove, MC.c:342-448) run once per re-sort period, N_max x 0.01 attempts per MC step as the
+ * reference makes on average, one after the other with exact FP64 energies. */
+int pp_gpu_sus_histogram(pp_engine *e, long long *hist, int reset);
 
 /* Plain rounds over the neighbour lists as one persistent cooperative kernel (enable = 1): the 8 colours
  * of a round (the 8 sublattice passes of do_NVT/do_NPT's sweep, MC.c:19-29, 60-68) in one launch, with

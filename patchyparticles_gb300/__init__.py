@@ -25,10 +25,14 @@ PP_ERR_STATE = -6
 PP_ERR_DRIFT = -7
 
 NVT = 0
+GC = 1
+SUS = 3
 NPT = 5
 PREC_FP32_GUARD = 0
 PREC_FP64 = 1
 MOVE_ROTO_TRASL = 0
+MOVE_ADD = 2
+MOVE_REMOVE = 3
 MOVE_VOLUME = 6
 MOVE_LX = 7
 N_MOVES = 8
@@ -53,6 +57,9 @@ class PPParams(ctypes.Structure):
         ("lx_change_max", ctypes.c_double),
         ("lyz_min", ctypes.c_double),
         ("lyz_max", ctypes.c_double),
+        ("activity", ctypes.c_double),
+        ("n_min", ctypes.c_int),
+        ("n_max", ctypes.c_int),
     ]
 
 
@@ -132,7 +139,7 @@ EXPORTED = [
     "pp_gpu_learned_set_weights", "pp_gpu_learned_get_weights", "pp_gpu_set_proposal", "pp_gpu_learned_collect",
     "pp_gpu_learned_train", "pp_gpu_learned_samples", "pp_gpu_learned_clear_samples", "pp_gpu_learned_features",
     "pp_gpu_learned_stats", "pp_gpu_autotune", "pp_gpu_set_graphs", "pp_gpu_set_neighbour_lists",
-    "pp_gpu_set_persistent", "pp_gpu_set_barrier_test",
+    "pp_gpu_set_persistent", "pp_gpu_set_barrier_test", "pp_gpu_sus_histogram",
 ]
 
 
@@ -197,6 +204,7 @@ def load_library(path=None):
         "pp_gpu_set_graphs": (ctypes.c_int, [vp, ctypes.c_int]),
         "pp_gpu_set_neighbour_lists": (ctypes.c_int, [vp, ctypes.c_int]),
         "pp_gpu_set_persistent": (ctypes.c_int, [vp, ctypes.c_int]),
+        "pp_gpu_sus_histogram": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
         "pp_gpu_set_barrier_test": (ctypes.c_int, [vp, ctypes.c_longlong, ctypes.c_int]),
         "pp_mlp_grad": (ctypes.c_int, [fp, ctypes.c_int, fp, ctypes.c_double, ctypes.c_double, ctypes.c_int, fp, dp]),
     }
@@ -249,6 +257,7 @@ class Engine:
             self.h = ctypes.c_void_p()
             raise PPError(rc, msg)
         self.nrep = len(plist)
+        self.params = list(plist)
 
     def _check(self, rc):
         if rc != PP_OK:
@@ -301,7 +310,15 @@ class Engine:
         return list(c.tries), list(c.accepted)
 
     def num_particles(self, replica=0):
+        """Current particle count (changes in the GC and SUS ensembles)."""
         return self.lib.pp_gpu_num_particles(self.h, replica)
+
+    def sus_histogram(self, reset=False):
+        """SUS: counts of N after every insertion / removal attempt, bins n_min .. n_max."""
+        n = self.params[0].n_max - self.params[0].n_min + 1
+        h = (ctypes.c_longlong * n)()
+        self._check(self.lib.pp_gpu_sus_histogram(self.h, h, 1 if reset else 0))
+        return list(h)
 
     def box(self, replica=0):
         b = np.zeros(3)

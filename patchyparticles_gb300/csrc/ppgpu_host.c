@@ -176,8 +176,17 @@ void pp_default_params(pp_params *p) {
 	p->audit = 0;
 }
 
+static int is_exchange(const pp_engine *e);
+
 static int check_params(pp_engine *e, const pp_params *p) {
-	if(p->ensemble != PP_NVT && p->ensemble != PP_NPT) return set_err(e, PP_ERR_ARG, "Ensemble %d not supported (0 = NVT, 5 = NPT)", p->ensemble);
+	if(p->ensemble != PP_NVT && p->ensemble != PP_NPT && p->ensemble != PP_GC && p->ensemble != PP_SUS)
+		return set_err(e, PP_ERR_ARG, "Ensemble %d not supported (0 = NVT, 1 = GC, 3 = SUS, 5 = NPT)", p->ensemble);
+	if(p->ensemble == PP_GC || p->ensemble == PP_SUS) {
+		if(!(p->activity > 0.)) return set_err(e, PP_ERR_ARG, "Activity must be > 0");
+		if(p->n_max < 1 || (p->ensemble == PP_SUS && (p->n_min < 0 || p->n_min > p->n_max)))
+			return set_err(e, PP_ERR_ARG, "the particle-number window needs 0 <= Umbrella_sampling_min <= Umbrella_sampling_max and GC_N_max >= 1");
+		if(p->lx_move) return set_err(e, PP_ERR_ARG, "Lx_move is not supported with insertions and removals");
+	}
 	if(!(p->temperature > 0.)) return set_err(e, PP_ERR_ARG, "Temperature must be > 0");
 	if(!(p->disp_max >= 0.) || !(p->theta_max >= 0.)) return set_err(e, PP_ERR_ARG, "Disp_max and Theta_max must be >= 0");
 	if(!(p->kf_delta > 0.) || !(p->kf_delta < 1.)) return set_err(e, PP_ERR_ARG, "KF_delta must lie in (0, 1)");
@@ -235,6 +244,15 @@ static int create_common(const pp_params *prms, int n, pp_engine **out) {
 		if(e->prm[i].audit) e->any_audit = 1;
 	}
 	if(e->prm[0].resort_every > 0) e->resort_every = e->prm[0].resort_every;
+	for(int i = 0; i < n; i++)
+		if((e->prm[i].ensemble == PP_GC || e->prm[i].ensemble == PP_SUS) && n > 1)
+			return set_err(e, PP_ERR_ARG, "a GC or SUS system needs an engine of its own (pp_gpu_create)");
+	if(is_exchange(e)) {
+		/* the particle count changes between re-sorts: stream launches (a captured graph fixes it), and no
+		 * physical reorder (it would interleave the live slots) */
+		e->graphs_on = 0;
+		e->reorder_every = 0;
+	}
 	cudaError_t c = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
 	*out = e;
 	if(c != cudaSuccess) return set_err(e, PP_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(c));
@@ -271,6 +289,8 @@ static void free_device(pp_engine *e) {
 	e->d.ctr = NULL;
 	if(e->d.gbar) cudaFree(e->d.gbar);
 	e->d.gbar = NULL;
+	if(e->d.sus_hist) cudaFree(e->d.sus_hist);
+	e->d.sus_hist = NULL;
 	if(e->d.nl) cudaFree(e->d.nl);
 	if(e->d.nl_cnt) cudaFree(e->d.nl_cnt);
 	if(e->d.vpairs) cudaFree(e->d.vpairs);
@@ -380,6 +400,15 @@ static void lx_move_bounds(const pp_params *p, const double *box, double *smin, 
 	*smax = fmax(1. + h, 1. / sqrt(1. - h));
 }
 
+/* device slots of replica r: its particles, or for GC / SUS room for the largest allowed count */
+static int slot_cap(const pp_engine *e, int r) {
+	const pp_params *p = e->prm + r;
+	if((p->ensemble == PP_GC || p->ensemble == PP_SUS) && p->n_max > e->N[r]) return p->n_max;
+	return e->N[r];
+}
+
+static int is_exchange(const pp_engine *e) { return e->nrep == 1 && (e->prm[0].ensemble == PP_GC || e->prm[0].ensemble == PP_SUS); }
+
 static int derive_rparams(pp_engine *e, int r, ppi_rparams *rp) {
 	const pp_params *p = e->prm + r;
 	memset(rp, 0, sizeof(*rp));
@@ -408,6 +437,9 @@ static int derive_rparams(pp_engine *e, int r, ppi_rparams *rp) {
 	rp->lx_change_max = p->lx_change_max;
 	rp->lyz_min = p->lyz_min;
 	rp->lyz_max = p->lyz_max;
+	rp->activity = p->activity;
+	rp->n_min = p->ensemble == PP_SUS ? p->n_min : 0;
+	rp->n_max = p->n_max;
 	for(int k = 0; k < 32; k++) {
 		double pk = exp(-(double) k / p->temperature);
 		double t = ceil(pk * 9007199254740992.0);
@@ -464,6 +496,9 @@ static int read_states(pp_engine *e) {
 	CU(cudaStreamSynchronize(e->stream));
 	if(lerr) return set_err(e, PP_ERR_CUDA, "a tensor-core wait of the learned proposal timed out");
 	if(berr == PPI_E_BARRIER) return set_err(e, PP_ERR_CUDA, "grid barrier wait timed out in the persistent round kernel (the state is incomplete)");
+	for(int r = 0; r < e->nrep; r++)
+		if(e->h_rs[r].error == PPI_E_GCFULL) /* MC.c:346-348 */
+			return set_err(e, PP_ERR_CAPACITY, "The system contains the maximum number of particles set in the input file (%d), increase GC_N_max", e->prm[r].n_max);
 	for(int r = 0; r < e->nrep; r++)
 		if(e->h_rs[r].error == PPI_E_LISTS)
 			return set_err(e, PP_ERR_CAPACITY, "replica %d: more guard-band pairs in one volume pass than its buffer holds", r);
@@ -545,7 +580,7 @@ static int setup_nlists(pp_engine *e) {
 			continue;
 		}
 		const double R = sqrt((double) e->h_rp[r].nl_r2f), *b = e->h_box[r];
-		double rho = e->N[r] / (b[0] * b[1] * b[2]);
+		double rho = slot_cap(e, r) / (b[0] * b[1] * b[2]);
 		if(e->prm[r].ensemble == PP_NPT) rho *= 1.5;
 		const double mean = 4.18879020478639 * R * R * R * rho;
 		int k = (int) ceil(mean + 6. * sqrt(mean) + 6.);
@@ -578,7 +613,7 @@ static int setup_nlists(pp_engine *e) {
 	e->d.nl_k = 0;
 	e->nl_valid = 0;
 	if(K == 0) return PP_OK;
-	const size_t n1 = e->d.ntot > 0 ? (size_t) e->d.ntot : 1;
+	const size_t n1 = e->ntot_alloc > 0 ? (size_t) e->ntot_alloc : 1;
 	CU(cudaMalloc((void **) &e->d.nl, sizeof(int) * (size_t) K * n1));
 	CU(cudaMalloc((void **) &e->d.nl_cnt, sizeof(int) * n1));
 	/* the volume pass's flat pair list: at most K pairs above each particle (an overflowing particle goes to
@@ -600,8 +635,12 @@ static int setup_nlists(pp_engine *e) {
 }
 
 static int commit(pp_engine *e) {
-	int ntot = 0;
-	for(int r = 0; r < e->nrep; r++) ntot += e->N[r];
+	int ntot = 0, nalloc = 0;
+	for(int r = 0; r < e->nrep; r++) {
+		ntot += e->N[r];
+		nalloc += slot_cap(e, r);
+	}
+	e->ntot_alloc = nalloc;
 	free_device(e);
 	free(e->h_rp);
 	free(e->h_rs);
@@ -616,7 +655,7 @@ static int commit(pp_engine *e) {
 		int rc = derive_rparams(e, r, rp);
 		if(rc != PP_OK) return rc;
 		rp->p0 = p0;
-		p0 += rp->N;
+		p0 += slot_cap(e, r);
 		rp->cell_base = (int) cells;
 		cells += rp->cell_cap;
 	}
@@ -626,7 +665,7 @@ static int commit(pp_engine *e) {
 	d->ntot = ntot;
 	d->total_cells = (int) cells;
 	d->clist_cap = (int) (cells / 8 + e->nrep + 8);
-	size_t n1 = ntot > 0 ? (size_t) ntot : 1;
+	size_t n1 = nalloc > 0 ? (size_t) nalloc : 1;
 	CU(cudaMalloc((void **) &d->rec, sizeof(double) * PPI_REC * n1));
 	CU(cudaMalloc((void **) &d->spos, sizeof(float) * 4 * n1));
 	CU(cudaMalloc((void **) &d->sori, sizeof(float) * 12 * n1));
@@ -677,15 +716,20 @@ static int commit(pp_engine *e) {
 	for(int r = 0; r < e->nrep; r++) {
 		ppi_rparams *rp = e->h_rp + r;
 		for(int c = 0; c < rp->cell_cap; c++) crep[rp->cell_base + c] = r;
-		for(int i = 0; i < rp->N; i++) rep[rp->p0 + i] = r;
+		for(int i = 0; i < slot_cap(e, r); i++) rep[rp->p0 + i] = r;
 	}
 	cudaError_t c1 = cudaMemcpy(d->cell_rep, crep, sizeof(int) * cells, cudaMemcpyHostToDevice);
-	cudaError_t c2 = cudaMemcpy(d->rep, rep, sizeof(int) * ntot, cudaMemcpyHostToDevice);
+	cudaError_t c2 = cudaMemcpy(d->rep, rep, sizeof(int) * n1, cudaMemcpyHostToDevice);
 	free(crep);
 	free(rep);
 	if(c1 != cudaSuccess || c2 != cudaSuccess) return set_err(e, PP_ERR_CUDA, "layout upload failed");
+	if(is_exchange(e)) {
+		const pp_params *p = e->prm;
+		const int nb = (p->ensemble == PP_SUS ? p->n_max - p->n_min : p->n_max) + 1;
+		CU(cudaMalloc((void **) &d->sus_hist, sizeof(unsigned long long) * (size_t) nb));
+		CU(cudaMemsetAsync(d->sus_hist, 0, sizeof(unsigned long long) * (size_t) nb, e->stream));
+	}
 	CU(cudaMemcpy(d->rp, e->h_rp, sizeof(ppi_rparams) * e->nrep, cudaMemcpyHostToDevice));
-	e->ntot_alloc = ntot;
 	e->committed = 1;
 	return PP_OK;
 }
@@ -744,6 +788,11 @@ int pp_gpu_upload_replica(pp_engine *e, int r, int N, const double *rr, const do
 	for(int a = 0; a < 3; a++)
 		if(!(box[a] > 0.)) return set_err(e, PP_ERR_ARG, "box sides must be positive");
 	const pp_params *p = e->prm + r;
+	if(p->ensemble == PP_SUS) { /* system.c:100-101 */
+		if(N < p->n_min) return set_err(e, PP_ERR_ARG, "Number of particles %d is smaller than Umbrella_sampling_min (%d)", N, p->n_min);
+		if(N > p->n_max) return set_err(e, PP_ERR_ARG, "Number of particles %d is larger than Umbrella_sampling_max (%d)", N, p->n_max);
+	}
+	if(p->ensemble == PP_GC && N > p->n_max) return set_err(e, PP_ERR_ARG, "Number of particles %d is larger than GC_N_max (%d)", N, p->n_max);
 	if(p->ensemble == PP_NVT && p->lx_move) { /* system.c:172-188 */
 		if(box[1] != box[2]) return set_err(e, PP_ERR_ARG, "Lx_move = 1 requires Ly = Lz");
 		if(p->lyz_min >= box[1]) return set_err(e, PP_ERR_ARG, "Lyz_min should be smaller than box size");
@@ -767,6 +816,7 @@ int pp_gpu_upload_replica(pp_engine *e, int r, int N, const double *rr, const do
 			memset(s, 0, sizeof(*s));
 			memcpy(s->box, box, sizeof(s->box));
 			s->V = box[0] * box[1] * box[2];
+			s->n_live = N;
 			rc = write_states(e);
 			if(rc != PP_OK) return rc;
 			rc = push_replica(e, r, rr, RR);
@@ -797,6 +847,7 @@ int pp_gpu_upload_replica(pp_engine *e, int r, int N, const double *rr, const do
 		memset(s, 0, sizeof(*s));
 		memcpy(s->box, e->h_box[q], sizeof(s->box));
 		s->V = s->box[0] * s->box[1] * s->box[2];
+		s->n_live = e->N[q];
 	}
 	rc = write_states(e);
 	if(rc != PP_OK) return rc;
@@ -1039,6 +1090,43 @@ int pp_gpu_set_graphs(pp_engine *e, int enable) {
 	return PP_OK;
 }
 
+/* GC / SUS: the insertion and removal attempts of the coming re-sort period -- the reference makes
+ * N_max x 0.01 per MC step on average (MC.c:33-35) -- then the new particle count for the launches that
+ * follow (the re-sort places the particles in slots 0 .. N-1 into the cells) */
+static int exchange_step(pp_engine *e) {
+	const pp_params *p = e->prm;
+	int per = (int) floor(0.01 * p->n_max + 0.5);
+	if(per < 1) per = 1;
+	long long nl = 0;
+	CK(ppi_exchange(&e->d, e->epoch, per * e->resort_every, e->stream, &nl));
+	e->launches += nl;
+	int rc = read_states(e);
+	if(rc != PP_OK) return rc;
+	const int n = e->h_rs[0].n_live;
+	e->N[0] = n;
+	e->h_rp[0].N = n;
+	e->d.ntot = n;
+	return PP_OK;
+}
+
+int pp_gpu_sus_histogram(pp_engine *e, long long *hist, int reset) {
+	int rc = ready(e);
+	if(rc != PP_OK) return rc;
+	if(!is_exchange(e) || e->prm[0].ensemble != PP_SUS || e->d.sus_hist == NULL) return set_err(e, PP_ERR_ARG, "not an SUS engine");
+	const int nb = e->prm[0].n_max - e->prm[0].n_min + 1;
+	if(hist) {
+		unsigned long long *tmp = malloc(sizeof(unsigned long long) * (size_t) nb);
+		HOST_OK(tmp);
+		cudaError_t c = cudaMemcpyAsync(tmp, e->d.sus_hist, sizeof(unsigned long long) * (size_t) nb, cudaMemcpyDeviceToHost, e->stream);
+		if(c == cudaSuccess) c = cudaStreamSynchronize(e->stream);
+		for(int k = 0; k < nb && c == cudaSuccess; k++) hist[k] = (long long) tmp[k];
+		free(tmp);
+		if(c != cudaSuccess) return set_err(e, PP_ERR_CUDA, "SUS histogram copy: %s", cudaGetErrorString(c));
+	}
+	if(reset) CU(cudaMemsetAsync(e->d.sus_hist, 0, sizeof(unsigned long long) * (size_t) nb, e->stream));
+	return PP_OK;
+}
+
 int pp_gpu_sweeps(pp_engine *e, long long n) {
 	int rc = ready(e);
 	if(rc != PP_OK) return rc;
@@ -1058,6 +1146,7 @@ int pp_gpu_sweeps(pp_engine *e, long long n) {
 		int ev;
 		for(int rr = 0; rr < e->rounds_per_sweep; rr++) {
 			if(e->round_counter % e->resort_every == 0) {
+				if(is_exchange(e) && (rc = exchange_step(e)) != PP_OK) return rc;
 				if((rc = ev_begin(e, 0, &ev)) != PP_OK) return rc;
 				if((rc = do_resort(e)) != PP_OK) return rc;
 				if((rc = ev_end(e, ev)) != PP_OK) return rc;
@@ -1606,7 +1695,7 @@ static double u01_sm(uint64_t *s) { return (double) (splitmix64(s) >> 11) * 0x1p
 static int ensure_learn_layout(pp_engine *e) {
 	if(!e->committed) return set_err(e, PP_ERR_STATE, "no configuration uploaded for every replica");
 	if(!e->d.simg || !e->d.feat) drop_graphs(e); /* captured launches hold the device pointers by value */
-	size_t n1 = e->d.ntot > 0 ? (size_t) e->d.ntot : 1;
+	size_t n1 = e->ntot_alloc > 0 ? (size_t) e->ntot_alloc : 1;
 	if(!e->d.simg) CU(cudaMalloc((void **) &e->d.simg, sizeof(float) * 16 * n1));
 	if(!e->d.feat) CU(cudaMalloc((void **) &e->d.feat, sizeof(float) * PP_MLP_IN * n1));
 	return PP_OK;
@@ -1723,6 +1812,7 @@ int pp_gpu_learned_get_weights(pp_engine *e, float *params) {
 int pp_gpu_set_proposal(pp_engine *e, int proposal) {
 	int rc = ready(e);
 	if(rc != PP_OK) return rc;
+	if(proposal != PP_PROPOSAL_PLAIN && is_exchange(e)) return set_err(e, PP_ERR_ARG, "the learned proposal is not available with insertions and removals");
 	if(proposal == PP_PROPOSAL_PLAIN) {
 		e->proposal = proposal;
 		return PP_OK;
@@ -1970,6 +2060,7 @@ int pp_gpu_autotune(pp_engine *e, int trial_sweeps, pp_tune_result *out) {
 	int rc = ready(e);
 	if(rc != PP_OK) return rc;
 	if(trial_sweeps < 1 || trial_sweeps > 100000) return set_err(e, PP_ERR_ARG, "trial_sweeps must lie in [1, 100000]");
+	if(is_exchange(e)) return set_err(e, PP_ERR_ARG, "the autotuner does not run GC or SUS engines (their particle count changes)");
 	const int resorts[] = { 1, 2, 4, 8, 16 }, reorders[] = { 4, 16, 64 };
 	const double scales[] = { 1.0, 1.2, 1.5 };
 	const int r0 = e->resort_every, o0 = e->reorder_every, l0 = e->nl_mode;

@@ -42,11 +42,12 @@ extern "C" {
 #define PPI_E_EXACT 3 /* more undecidable pairs in one warp's share of a volume pass than it keeps */
 #define PPI_E_LISTS 4 /* more guard-band pairs in one volume pass than its buffer holds */
 #define PPI_E_BARRIER 5 /* a grid-barrier wait of the persistent round kernel ran out of its limit */
+#define PPI_E_GCFULL 6  /* a grand-canonical insertion found the system at GC_N_max (the reference stops there) */
 
 typedef struct ppi_rparams {
 	int N;           /* particles of this replica */
 	int p0;          /* first slot */
-	int ensemble;    /* 0 NVT, 5 NPT */
+	int ensemble;    /* 0 NVT, 1 GC, 3 SUS, 5 NPT */
 	int precision;   /* 0 FP32 + guard, 1 FP64 */
 	int audit;
 	int cell_base;   /* first global cell index of this replica */
@@ -61,6 +62,8 @@ typedef struct ppi_rparams {
 	float pad1;
 	uint64_t seed;
 	double lx_change_max, lyz_min, lyz_max; /* Lx_change_max, Lyz_min, Lyz_max (system.c:177-179) */
+	double activity;       /* GC / SUS: Activity z (system.c:91) */
+	int n_min, n_max;      /* GC / SUS: the particle-number window (GC: 0 and GC_N_max) */
 } ppi_rparams;
 
 typedef struct ppi_rstate {
@@ -77,6 +80,8 @@ typedef struct ppi_rstate {
 	unsigned long long pairs, fallbacks, mismatches;
 	unsigned int max_err_r2_bits, max_err_cos_bits;
 	unsigned long long nl_overflow; /* particles whose neighbour list overflowed (their attempts take the exact path) */
+	int n_live;                  /* GC / SUS: current particle count (slots p0 .. p0 + n_live - 1 hold them) */
+	int pad_live;
 } ppi_rstate;
 
 typedef struct ppi_grid {
@@ -196,6 +201,7 @@ typedef struct ppi_dev {
 	long long bar_limit; /* SM clock cycles a barrier wait may spin before it gives up (0: default ~1 s) */
 	int bar_extra;       /* test hook: arrivals the first barrier waits for beyond the grid (1 = never completes) */
 	int persist;         /* 1: plain rounds over the neighbour lists use k_round, 0: one launch per colour */
+	unsigned long long *sus_hist; /* SUS: histogram of N after every insertion/removal attempt, n_max - n_min + 1 bins */
 } ppi_dev;
 
 #define PPI_MAX_PARTNERS 24
@@ -210,6 +216,8 @@ int ppi_energy(const ppi_dev *d, int mode, cudaStream_t s, long long *nl);
 /* use_nl: the candidate-box energy takes its pairs from the epoch's neighbour lists (every replica has them) */
 int ppi_volume(const ppi_dev *d, long long sweep, int use_nl, cudaStream_t s, long long *nl);
 int ppi_gram_schmidt(const ppi_dev *d, int first, int count, cudaStream_t s, long long *nl);
+/* GC / SUS: `attempts` sequential insertion / removal attempts per replica (MC_add_remove, MC.c:342-448) */
+int ppi_exchange(const ppi_dev *d, long long step, int attempts, cudaStream_t s, long long *nl);
 int ppi_reorder(const ppi_dev *d, cudaStream_t s, long long *nl);
 /* writes x y z R00..R22 (12 doubles) of slots [first, first + count) into d->tmp_rec */
 int ppi_export(const ppi_dev *d, int first, int count, cudaStream_t s, long long *nl);

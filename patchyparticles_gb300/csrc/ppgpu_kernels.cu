@@ -4078,6 +4078,167 @@ __global__ void k_export(ppi_dev d, int first, int count) {
 }
 
 /* ------------------------------------------------------------------------------------------------ */
+/* grand canonical and successive-umbrella-sampling insertions and removals (MC_add_remove)          */
+/* ------------------------------------------------------------------------------------------------ */
+/* One CTA per GC / SUS replica makes `attempts` attempts one after the other, as MC_add_remove
+ * (MC.c:342-448) does: with probability 1/2 an insertion at a uniform position with a uniform random
+ * orientation, accepted with min(1, exp(-dE / T) z V / (N + 1)), otherwise the removal of a uniformly
+ * chosen particle, accepted with min(1, exp(-dE / T) N / (V z)); an insertion into a full system is an
+ * error for GC (the reference stops, "increase GC_N_max") and a non-attempt for SUS, as is a removal at
+ * N_min. The replica's particles stay in slots p0 .. p0 + N - 1: an insertion takes slot p0 + N, a removal
+ * moves the particle of the last slot into the freed one, and the particle with the highest index takes
+ * the removed particle's index (the reference's renumbering). The energy of the probe is exact: every
+ * live particle within an FP32 pre-filter radius r_cut + 0.05 goes through interact64 (MC_would_interact
+ * with the probe as p). The caller re-sorts the cells afterwards. SUS adds one histogram count of N after
+ * every attempt (MC.c:50). */
+#define TAG_EXCH 9u
+#define EXCH_B 256
+
+/* sum (orbit = 0) or bitwise or (orbit = 1) of v over the CTA; every thread of the CTA calls it */
+__device__ __forceinline__ int block_sum_or(int v, int *ws, int orbit) {
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	v = orbit ? (int) __reduce_or_sync(0xffffffffu, (unsigned) v) : __reduce_add_sync(0xffffffffu, v);
+	__syncthreads();
+	if(lane == 0) ws[warp] = v;
+	__syncthreads();
+	int t = 0;
+	for(int w = 0; w < (int) (blockDim.x >> 5); w++) t = orbit ? (t | ws[w]) : t + ws[w];
+	__syncthreads();
+	return t;
+}
+
+/* rotation matrix (rows) of the uniform random unit quaternion built from three uniforms (Shoemake 1992) */
+__device__ __forceinline__ void uniform_rotation64(double u1, double u2, double u3, double *R) {
+	const double a = sqrt(1.0 - u1), b = sqrt(u1);
+	const double t2 = 6.283185307179586 * u2, t3 = 6.283185307179586 * u3;
+	const double q[4] = { b * cos(t3), a * sin(t2), a * cos(t2), b * sin(t3) }; /* (w, x, y, z) */
+	quatmat64(q, R);
+}
+
+__global__ void __launch_bounds__(EXCH_B) k_exchange(ppi_dev d, long long step, int attempts) {
+	const int r = blockIdx.x;
+	ppi_rparams *rp = d.rp + r;
+	ppi_rstate *rs = d.rs + r;
+	if(rp->ensemble != 1 && rp->ensemble != 3) return;
+	__shared__ double s_r[3], s_R[9];
+	__shared__ int s_ws[EXCH_B / 32], s_t, s_dn;
+	const int tid = threadIdx.x;
+	const int p0 = rp->p0, gc = rp->ensemble == 1;
+	const double box[3] = { rs->box[0], rs->box[1], rs->box[2] };
+	const double V = rs->V, z = rp->activity, T = rp->T;
+	const float rf2 = (float) ((rp->r_cut + 0.05) * (rp->r_cut + 0.05));
+	const float Lf[3] = { (float) box[0], (float) box[1], (float) box[2] }, iLf[3] = { 1.f / Lf[0], 1.f / Lf[1], 1.f / Lf[2] };
+	int n = rs->n_live;
+	if(tid == 0) s_dn = 0;
+	for(int a = 0; a < attempts; a++) {
+		const U4 u0 = rng(*rp, step, r, TAG_EXCH, (uint32_t) a, 0u), u1 = rng(*rp, step, r, TAG_EXCH, (uint32_t) a, 1u);
+		const bool add = u01d(u0.x, u0.y) < 0.5;
+		const double U = u01d(u0.z, u0.w);
+		int skip = 0, probe = -1;
+		if(add) {
+			if(n == rp->n_max) {
+				skip = 1;
+				if(gc) {
+					if(tid == 0) rs->error = PPI_E_GCFULL;
+					break;
+				}
+			}
+			else if(tid == 0) { /* the candidate: uniform position, uniform orientation */
+				const U4 u2 = rng(*rp, step, r, TAG_EXCH, (uint32_t) a, 2u), u3 = rng(*rp, step, r, TAG_EXCH, (uint32_t) a, 3u);
+				s_r[0] = u01d(u1.x, u1.y) * box[0];
+				s_r[1] = u01d(u1.z, u1.w) * box[1];
+				s_r[2] = u01d(u2.x, u2.y) * box[2];
+				uniform_rotation64(u01d(u2.z, u2.w), u01d(u3.x, u3.y), u01d(u3.z, u3.w), s_R);
+			}
+		}
+		else if(n == rp->n_min) skip = 1;
+		else {
+			const int k = (int) (u01d(u1.x, u1.y) * n);
+			probe = p0 + (k < n ? k : n - 1);
+			if(tid == 0) {
+				const double *rec = d.rec + (size_t) probe * PPI_REC;
+				s_r[0] = rec[0];
+				s_r[1] = rec[1];
+				s_r[2] = rec[2];
+				orient64(rec + PPI_R0, rec + PPI_Q, s_R);
+			}
+		}
+		if(!skip) {
+			__syncthreads();
+			/* the probe's bonds and overlaps with every other live particle; for a removal also the slot
+			 * of the particle with the highest index */
+			int nb = 0, ov = 0;
+			const float px = (float) s_r[0], py = (float) s_r[1], pz = (float) s_r[2];
+			for(int j = tid; j < n; j += EXCH_B) {
+				const int q = p0 + j;
+				if(!add && d.id[q] == n - 1) s_t = q;
+				if(q == probe) continue;
+				const double *rec = d.rec + (size_t) q * PPI_REC;
+				float dx = (float) rec[0] - px, dy = (float) rec[1] - py, dz = (float) rec[2] - pz;
+				dx -= Lf[0] * rintf(dx * iLf[0]);
+				dy -= Lf[1] * rintf(dy * iLf[1]);
+				dz -= Lf[2] * rintf(dz * iLf[2]);
+				if(fmaf(dx, dx, fmaf(dy, dy, dz * dz)) >= rf2) continue;
+				double Rq[9];
+				orient64(rec + PPI_R0, rec + PPI_Q, Rq);
+				const int res = interact64(s_r, s_R, rec, Rq, rp->base, box, rp->sqr_rcut, rp->cosmax, nullptr, nullptr, nullptr);
+				nb += res == 1;
+				ov |= res == -1;
+			}
+			nb = block_sum_or(nb, s_ws, 0);
+			ov = block_sum_or(ov, s_ws, 1);
+			if(tid == 0) {
+				if(add) {
+					rs->tries[2]++; /* ADD (defs.h:14) */
+					const double acc = exp((double) nb / T) * z * V / (n + 1.);
+					if(!ov && U < acc) {
+						const int slot = p0 + n;
+						double *rec = d.rec + (size_t) slot * PPI_REC;
+						rec[0] = s_r[0];
+						rec[1] = s_r[1];
+						rec[2] = s_r[2];
+						rec[PPI_Q] = 1.0;
+						rec[PPI_Q + 1] = rec[PPI_Q + 2] = rec[PPI_Q + 3] = 0.0;
+						for(int k = 0; k < 9; k++) rec[PPI_R0 + k] = s_R[k];
+						d.id[slot] = n;
+						rs->bonds += nb;
+						rs->accepted[2]++;
+						s_dn = 1;
+					}
+				}
+				else {
+					rs->tries[3]++; /* REMOVE (defs.h:15) */
+					const double acc = exp(-(double) nb / T) * n / (V * z);
+					if(U < acc) {
+						const int last = p0 + n - 1;
+						d.id[s_t] = d.id[probe]; /* the highest index takes the removed one's */
+						if(probe != last) {
+							double *dst = d.rec + (size_t) probe * PPI_REC;
+							const double *src = d.rec + (size_t) last * PPI_REC;
+							for(int k = 0; k < PPI_REC; k++) dst[k] = src[k];
+							d.id[probe] = d.id[last];
+						}
+						rs->bonds -= nb;
+						rs->accepted[3]++;
+						s_dn = -1;
+					}
+				}
+			}
+			__syncthreads();
+			n += s_dn; /* +1 inserted, -1 removed, 0 rejected */
+			__syncthreads();
+			if(tid == 0) s_dn = 0;
+		}
+		if(!gc && tid == 0) atomicAdd(d.sus_hist + (n - rp->n_min), 1ull); /* MC.c:50 */
+		__syncthreads();
+	}
+	if(tid == 0) {
+		rs->n_live = n;
+		rp->N = n;
+	}
+}
+
+/* ------------------------------------------------------------------------------------------------ */
 /* launchers                                                                                        */
 /* ------------------------------------------------------------------------------------------------ */
 static int g_sms = 0;
@@ -4272,6 +4433,13 @@ extern "C" int ppi_volume(const ppi_dev *d, long long sweep, int use_nl, cudaStr
 extern "C" int ppi_gram_schmidt(const ppi_dev *d, int first, int count, cudaStream_t s, long long *nl) {
 	if(count <= 0) return 0;
 	k_gram_schmidt<<<(count + 255) / 256, 256, 0, s>>>(*d, first, count);
+	*nl += 1;
+	return (int) cudaGetLastError();
+}
+
+extern "C" int ppi_exchange(const ppi_dev *d, long long step, int attempts, cudaStream_t s, long long *nl) {
+	if(attempts <= 0) return 0;
+	k_exchange<<<d->nrep, EXCH_B, 0, s>>>(*d, step, attempts);
 	*nl += 1;
 	return (int) cudaGetLastError();
 }

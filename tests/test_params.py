@@ -7,7 +7,11 @@ import patchyparticles_gb300 as pp
 
 
 @pytest.mark.parametrize("kw,msg", [
-    (dict(ensemble=3), "Ensemble 3 not supported"),
+    (dict(ensemble=4), "Ensemble 4 not supported"),
+    (dict(ensemble=pp.GC, activity=0.0, n_max=10), "Activity must be > 0"),
+    (dict(ensemble=pp.GC, activity=0.1, n_max=0), "GC_N_max >= 1"),
+    (dict(ensemble=pp.SUS, activity=0.1, n_min=20, n_max=10), "Umbrella_sampling_min <= Umbrella_sampling_max"),
+    (dict(ensemble=pp.GC, activity=0.1, n_max=10, lx_move=1, lx_change_max=0.5, lyz_min=1.0, lyz_max=2.0), "Lx_move is not supported"),
     (dict(temperature=0.0), "Temperature must be > 0"),
     (dict(disp_max=-0.1), "Disp_max and Theta_max must be >= 0"),
     (dict(kf_delta=1.5), "KF_delta must lie in (0, 1)"),
