@@ -1,5 +1,5 @@
 /*
- * ppgpu_cli.c -- command-line driver: runs a PatchyParticles input file (Dynamics = 0, Ensemble 0 or 5)
+ * ppgpu_cli.c -- command-line driver: runs a PatchyParticles input file (Dynamics = 0, Ensemble 0, 1, 3 or 5)
  * on the GB300 engine through the public C-ABI (include/ppgpu.h) and writes the reference's output files.
  *
  *   ppgpu input_file
@@ -116,7 +116,9 @@ static FILE *open_or_die(const char *name, const char *mode) {
 typedef struct {
 	pp_engine *e;
 	int N, ensemble, lx;
-	double *r, *R, box[3];
+	double *r, *R, box[3]; /* room for the largest particle count the ensemble allows */
+	const char *sus_folder; /* SUS: sus-<step>.dat into this folder (output.c:343-356) */
+	int n_min, n_max;
 	FILE *energy, *acc, *density, *boxshape;
 	const char *last;
 	const char *bonds_folder; /* Print_bonds: bonds_<step>.dat into this folder (output.c:88-99) */
@@ -130,6 +132,7 @@ static void check(run_t *s, int rc) {
 }
 
 static void save(run_t *s, long long step, const char *path) {
+	s->N = pp_gpu_num_particles(s->e, 0); /* GC / SUS: the current count */
 	check(s, pp_gpu_download(s->e, s->r, s->R, s->box));
 	if(pp_rrr_write(path, step, s->N, s->r, s->R, s->box) != PP_OK) die("Configuration file '%s' is not writable", path);
 }
@@ -165,6 +168,7 @@ static void print_step(run_t *s, long long step) {
 	check(s, pp_gpu_get_energy(s->e, 0, &energy));
 	check(s, pp_gpu_counters(s->e, 0, &c, 1));
 	check(s, pp_gpu_box(s->e, 0, s->box));
+	s->N = pp_gpu_num_particles(s->e, 0);
 	const double V = s->box[0] * s->box[1] * s->box[2], E = s->N > 0 ? energy / s->N : 0.;
 	fprintf(s->energy, "%lld %lf\n", step, E);
 	fflush(s->energy);
@@ -177,6 +181,10 @@ static void print_step(run_t *s, long long step) {
 		fflush(s->boxshape);
 	}
 	fprintf(s->acc, "%lld %e", step, c.accepted[PP_MOVE_ROTO_TRASL] / (double) c.tries[PP_MOVE_ROTO_TRASL]);
+	if(s->ensemble == PP_GC || s->ensemble == PP_SUS) {
+		fprintf(s->acc, " %e", c.accepted[PP_MOVE_ADD] / (double) c.tries[PP_MOVE_ADD]);
+		fprintf(s->acc, " %e", c.accepted[PP_MOVE_REMOVE] / (double) c.tries[PP_MOVE_REMOVE]);
+	}
 	if(s->ensemble == PP_NPT) fprintf(s->acc, " %e", c.accepted[PP_MOVE_VOLUME] / (double) c.tries[PP_MOVE_VOLUME]);
 	if(s->lx) fprintf(s->acc, " %e", c.accepted[PP_MOVE_LX] / (double) c.tries[PP_MOVE_LX]);
 	fprintf(s->acc, "\n");
@@ -228,8 +236,25 @@ int main(int argc, char *argv[]) {
 	const int dynamics = (int) key_ll(in, "Dynamics", 1, 0);
 	s.ensemble = p.ensemble = (int) key_ll(in, "Ensemble", 1, 0);
 	if(dynamics != 0) die("Dynamics = %d is not run by this engine (only Dynamics = 0, roto-translation)", dynamics);
-	if(s.ensemble != PP_NVT && s.ensemble != PP_NPT) die("Ensemble = %d is not run by this engine (0 NVT, 5 NPT)", s.ensemble);
+	if(s.ensemble != PP_NVT && s.ensemble != PP_NPT && s.ensemble != PP_GC && s.ensemble != PP_SUS)
+		die("Ensemble = %d is not run by this engine (0 NVT, 1 GC, 3 SUS, 5 NPT)", s.ensemble);
 	if(s.ensemble != PP_NVT) s.density = open_or_die((v = key(in, "Density_file", 0)) ? v : "density.dat", mode);
+	if(s.bonds_folder && s.ensemble != PP_NVT) die("The printing of bonds is unavailable in non-canonical ensembles"); /* output.c:90-92 */
+	if(s.ensemble == PP_SUS) { /* output.c:79-84 */
+		s.sus_folder = key(in, "Umbrella_sampling_folder", 1);
+		if(access(s.sus_folder, W_OK) != 0)
+			die("Cannot create files in directory '%s': please make sure that the directory exists and it is writable", s.sus_folder);
+	}
+	if(s.ensemble == PP_GC || s.ensemble == PP_SUS) { /* system.c:90-103 */
+		p.activity = key_d(in, "Activity", 1, 0.);
+		if(s.ensemble == PP_GC) p.n_max = (int) key_ll(in, "GC_N_max", 1, 0);
+		else {
+			p.n_min = (int) key_ll(in, "Umbrella_sampling_min", 1, 0);
+			p.n_max = (int) key_ll(in, "Umbrella_sampling_max", 1, 0);
+		}
+		s.n_min = p.n_min;
+		s.n_max = p.n_max;
+	}
 	p.disp_max = key_d(in, "Disp_max", 1, 0.);
 	p.theta_max = key_d(in, "Theta_max", 1, 0.);
 	p.temperature = key_d(in, "Temperature", 1, 0.);
@@ -256,8 +281,9 @@ int main(int argc, char *argv[]) {
 	p.precision = (int) key_ll(in, "GPU_precision", 0, PP_PREC_FP32_GUARD);
 	if((v = key(in, "GPU_device", 0)) && pp_gpu_select_device(atoi(v)) != PP_OK) die("cannot select GPU %s", v);
 
-	s.r = malloc(sizeof(double) * 3 * (N > 0 ? N : 1));
-	s.R = malloc(sizeof(double) * 9 * (N > 0 ? N : 1));
+	const int room = (N > s.n_max ? N : s.n_max) > 0 ? (N > s.n_max ? N : s.n_max) : 1;
+	s.r = malloc(sizeof(double) * 3 * (size_t) room);
+	s.R = malloc(sizeof(double) * 9 * (size_t) room);
 	if(s.r == NULL || s.R == NULL) die("out of memory");
 	char err[512];
 	if(pp_rrr_read(conf, N, s.r, s.R, s.box, err, sizeof(err)) != PP_OK) die("%s", err);
@@ -290,7 +316,22 @@ int main(int argc, char *argv[]) {
 	while(step < steps && !g_stop) {
 		if(step % print_every == 0) {
 			print_step(&s, step);
-			if(step != 0) check(&s, pp_gpu_check_energy(s.e, 0)); /* MC_check_energy (main.c:86) */
+			if(step != 0) {
+				check(&s, pp_gpu_check_energy(s.e, 0)); /* MC_check_energy (main.c:86) */
+				if(s.ensemble == PP_SUS) { /* output_and_reset_sus (main.c:89, output.c:343-356) */
+					const int nb = s.n_max - s.n_min + 1;
+					long long *h = malloc(sizeof(long long) * (size_t) nb);
+					if(h == NULL) die("out of memory");
+					check(&s, pp_gpu_sus_histogram(s.e, h, 1));
+					snprintf(name, sizeof(name), "%s/sus-%lld.dat", s.sus_folder, step);
+					FILE *fs = fopen(name, "w");
+					if(fs == NULL) die("SUS file '%s' is not writable", name);
+					for(int b = 0; b < nb; b++)
+						if(h[b] > 0) fprintf(fs, "%d %lld\n", b + s.n_min, h[b]);
+					fclose(fs);
+					free(h);
+				}
+			}
 		}
 		if(step > 0 && step % save_every == 0) {
 			snprintf(name, sizeof(name), "%s/conf_%lld.rrr", folder, step);
@@ -307,6 +348,7 @@ int main(int argc, char *argv[]) {
 	save(&s, step, s.last);
 	check(&s, pp_gpu_get_energy(s.e, 0, &energy));
 	check(&s, pp_gpu_box(s.e, 0, s.box));
+	N = s.N;
 	printf("%lld %lf %lf", step, N > 0 ? energy / N : 0., energy);
 	if(s.ensemble != PP_NVT) printf(" %lf", N / (s.box[0] * s.box[1] * s.box[2]));
 	printf("\n");

@@ -25,6 +25,8 @@ def _prepare(name, edit=None):
     if edit:
         text = edit(text)
     open(os.path.join(work, "input"), "w").write(text)
+    if "Umbrella_sampling_folder" in text:
+        os.makedirs(os.path.join(work, "sus"))
     conf = [l.split("=")[1].strip() for l in text.splitlines() if l.startswith("Initial_conditions_file")][0]
     helpers.unpack_golden(conf, work)
     return src, work
@@ -37,7 +39,9 @@ def _lines(path):
 @pytest.mark.gpu
 @pytest.mark.parametrize("name,files", [("small_nvt", ("energy.dat", "acceptance.dat")),
                                         ("small_npt", ("energy.dat", "acceptance.dat", "density.dat")),
-                                        ("small_lx", ("energy.dat", "acceptance.dat", "boxshape.dat"))])
+                                        ("small_lx", ("energy.dat", "acceptance.dat", "boxshape.dat")),
+                                        ("small_gc", ("energy.dat", "acceptance.dat", "density.dat")),
+                                        ("small_sus", ("energy.dat", "acceptance.dat", "density.dat"))])
 def test_driver_writes_the_reference_outputs(built, name, files):
     src, work = _prepare(name)
     p = subprocess.run([CLI, "input"], cwd=work, capture_output=True, text=True, timeout=300)
@@ -57,6 +61,12 @@ def test_driver_writes_the_reference_outputs(built, name, files):
     assert len(last) == len(ref_last) and last[0].split()[:2] == ref_last[0].split()[:2]
     saves = sorted(os.listdir(os.path.join(work, "confs")))
     assert saves and all(f.startswith("conf_") and f.endswith(".rrr") for f in saves)
+    if os.path.isdir(os.path.join(src, "sus")):  # one histogram file per print after step 0 (main.c:89)
+        assert sorted(os.listdir(os.path.join(work, "sus"))) == sorted(os.listdir(os.path.join(src, "sus")))
+        for fn in os.listdir(os.path.join(work, "sus")):
+            for line in open(os.path.join(work, "sus", fn)):
+                n, c = map(int, line.split())
+                assert 295 <= n <= 305 and c > 0
     shutil.rmtree(work)
 
 
