@@ -397,10 +397,14 @@ def run_gpu(args, wl, ws, rank, local, dist):
                "sweeps_per_step": args.e2e_sweeps, "steps": e2e_steps,
                "step": "upload (H2D, initial energy check) + sweeps + download (D2H) + tracked energy, through the C-ABI with host arrays"}
 
-    learned = None
+    learned, learned_large = None, None
     if rank == 0 and ws == 1 and not args.no_learned and args.proposal == "plain":
         e.close()
         learned = learned_comparison(args)
+        if args.workload == "c5":  # the large-scale configuration with the learned proposal, the same network
+            learned_large = large_learned(args, wl, learned.pop("_weights"))
+        else:
+            learned.pop("_weights")
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -432,6 +436,7 @@ def run_gpu(args, wl, ws, rank, local, dist):
         "cpu_baseline": cpu,
         "gpu_launches": launches,
         "learned": learned,
+        "learned_large_scale": learned_large,
         "training": train,
         "preparation": prep,
         "fp32_vs_fp64_audit": audit,
@@ -587,7 +592,49 @@ def learned_comparison(args, T=None, N=None, rho=None):
     res["ess_ratio_sigma"] = res["ess_ratio"] * float(np.hypot(p["tau_int_sigma_sweeps"] / p["tau_int_sweeps"], l["tau_int_sigma_sweeps"] / l["tau_int_sweeps"]))
     res["per_sweep_ratio"] = p["tau_int_sweeps"] / l["tau_int_sweeps"]
     res["resolved"] = not (p["tau_window_limited"] or l["tau_window_limited"])
+    res["_weights"] = W
     return res
+
+
+def large_learned(args, wl, W):
+    """Learned-proposal sweeps of the main workload (N=1M NPT): the network of the learned comparison, its
+    attempts/s through the same timed sweeps as the main line, and the learned colour kernel's roofline."""
+    import patchyparticles_gb300 as pp
+
+    r, R, box = make_config(wl)
+    e = pp.Engine(pp.default_params(ensemble=wl["ensemble"], temperature=wl["T"], pressure=wl["P"], disp_max=wl["disp"],
+                                    theta_max=wl["theta"], rescale_factor_max=wl["rescale"], seed=wl["seed"]))
+    e.upload(r, R, box)
+    e.learned_init(seed=7, **json.loads(args.learn_params))
+    e.set_learned_weights(W)
+    e.set_proposal(True)
+    for _ in range(3):
+        e.sweeps(1)
+    e.sync()
+    e.counters(reset=True)
+    e.learned_stats(reset=True)
+    n = args.learn_large_sweeps
+    ms = e.time_sweeps(n)
+    tries, acc = e.counters()
+    att = tries[pp.MOVE_ROTO_TRASL] + tries[pp.MOVE_VOLUME]
+    e.counters(reset=True)
+    e.set_timing(True)
+    e.kernel_stats(reset=True)
+    e.sweeps(8)
+    e.sync()
+    ks = e.kernel_stats()
+    e.set_timing(False)
+    rt, _ = e.counters()
+    t, a = e.learned_stats()
+    e.close()
+    peak, kind = measured_peaks()
+    avg = ks["sweep_ms"] / max(1, ks["sweep_launches"])
+    achieved = rt[pp.MOVE_ROTO_TRASL] / max(1, ks["sweep_launches"]) * BYTES_PER_ATTEMPT / (avg / 1000.0) / 1e9
+    return {"workload": wl["name"].replace("plain roto-translation", "learned proposal"), "value": att / (ms / 1000.0), "unit": UNIT,
+            "ms_per_sweep": ms / n, "sweeps": n, "acceptance": acc[pp.MOVE_ROTO_TRASL] / max(1, tries[pp.MOVE_ROTO_TRASL]),
+            "component_share": [x / max(1, sum(t)) for x in t],
+            "roofline": {"kernel": "k_colour_learned (8 launches per round)", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": kind, "avg_round_ms": avg}}
 
 
 def _max_op(dist):
@@ -644,6 +691,7 @@ def main():
     ap.add_argument("--learn-every", type=int, default=100, help="sweeps between bond-count snapshots")
     ap.add_argument("--learn-time-sweeps", type=int, default=2000, help="sweeps of the per-chain cost measurement")
     ap.add_argument("--learn-T", type=float, default=0.09)
+    ap.add_argument("--learn-large-sweeps", type=int, default=20, help="timed learned sweeps of the main workload")
     ap.add_argument("--learn-N", type=int, default=32768)
     args = ap.parse_args()
     if args.warmup < 3:
@@ -665,7 +713,9 @@ def main():
         from patchyparticles_gb300 import build
 
         build.build()
-        print(json.dumps({"learned": learned_comparison(args)}), flush=True)
+        res = learned_comparison(args)
+        res.pop("_weights")
+        print(json.dumps({"learned": res}), flush=True)
     else:
         run_gpu(args, wl, ws, rank, local, dist)
     if dist is not None:
