@@ -44,7 +44,11 @@ def _newer(target, sources):
 
 
 def build(force=False, verbose=False):
+    """Builds the library. PPGPU_DEFINES (e.g. "-DPSTEP=8 -DPPI_TILE_MIN_BLOCKS=4") adds preprocessor
+    definitions to the CUDA compile, for tuning measurements; it forces a rebuild."""
     os.makedirs(BUILD, exist_ok=True)
+    defines = os.environ.get("PPGPU_DEFINES", "").split()
+    force = force or bool(defines)
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
     if not os.path.exists(nvcc):
@@ -61,7 +65,7 @@ def build(force=False, verbose=False):
         obj = os.path.join(BUILD, s + ".o")
         objs.append(obj)
         if force or _newer(obj, [src] + headers):
-            cmds.append([nvcc] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--ptxas-options=-v" if verbose else "-w"] + inc + ["-c", src, "-o", obj])
+            cmds.append([nvcc] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--ptxas-options=-v" if verbose else "-w"] + defines + inc + ["-c", src, "-o", obj])
     for s in c_srcs:
         src = os.path.join(CSRC, s)
         obj = os.path.join(BUILD, s + ".o")

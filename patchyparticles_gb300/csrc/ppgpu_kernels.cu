@@ -872,7 +872,9 @@ __device__ __forceinline__ int pair_state(const double *rec, const ppi_rparams &
 #define TILE_CCAP 128  /* close-pair list capacity, >= 32 * PSTEP (flushed before it can overflow) */
 #define TILE_DCAP 16   /* deferred attempts a warp keeps in shared memory (more: flags in global memory) */
 #define TILE_UCAP 32   /* guard-band pairs per iteration resolved in place (more: the attempt is deferred) */
+#ifndef PSTEP
 #define PSTEP 4        /* pair steps whose candidate loads are issued together */
+#endif
 #define TILE_OFF_MAX (1 << 21) /* |candidate - mover| sorted-position distance that a packed entry holds */
 #define TF_OVER 1      /* the candidate state overlaps: rejected */
 #define TF_DEFER 2     /* decided at the end, exactly (guard-band pair, or pairs beyond the list) */
