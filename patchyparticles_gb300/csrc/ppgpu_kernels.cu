@@ -2230,23 +2230,6 @@ __device__ __forceinline__ void site_features(const ppi_dev &d, const ppi_rparam
 
 /* merge the selections of the G lanes of a group (butterfly; every lane ends with the group's result).
  * The order (r^2, id) is total, so the result does not depend on how candidates were split. */
-template <int G>
-__device__ __forceinline__ void nb_merge(NbSel &S) {
-#pragma unroll
-	for(int o = 1; o < G; o <<= 1) {
-		NbSel T;
-#pragma unroll
-		for(int n = 0; n < LEARN_NB; n++) {
-			T.r2[n] = __shfl_xor_sync(0xffffffffu, S.r2[n], o);
-			T.key[n] = __shfl_xor_sync(0xffffffffu, S.key[n], o);
-			T.pos[n] = __shfl_xor_sync(0xffffffffu, S.pos[n], o);
-		}
-#pragma unroll
-		for(int n = 0; n < LEARN_NB; n++)
-			if(T.pos[n] >= 0) nb_insert(S, T.r2[n], T.key[n], T.pos[n]);
-	}
-}
-
 /* The 27 cells around (cx, cy, cz) as one stream of candidates: 9 rows (dy, dz), each the contiguous
  * cells max(cx-1, 0) .. min(cx+1, nx-1) plus the periodic wrap-around cell; range r covers candidates
  * base[r] .. base[r+1]-1 at sorted positions lo[r] + (c - base[r]). The 36 boundary loads are independent. */
@@ -2294,11 +2277,11 @@ __device__ __forceinline__ int cell_dx(int qx, int cx, int nx) {
 	return v > 1 ? v - nx : (v < -1 ? v + nx : v);
 }
 
-/* feature neighbours of the particle at sorted position self, cell-local position pl, image pimg: this
- * lane takes candidates sub, sub + G, ... (G lanes per particle; merged with nb_merge<G>) */
-template <int G>
+/* feature neighbours of the particle at sorted position self, cell-local position pl, image pimg: one lane
+ * per particle takes candidates sub, sub + 1, ... (sub = 0) */
 __device__ __forceinline__ void scan_features(const ppi_dev &d, const ppi_rparams &rp, const ppi_grid &g, const Cands &C, int total, int cx, int self, float4 pl,
 		const float *pimg, const BoxF &B, NbSel &S, int sub) {
+	constexpr int G = 1; /* candidates a lane skips between its own */
 	const float rf2 = __fmul_rn(rp.sqr_rcut_f, LEARN_RF2_SCALE), loose = rf2 + LEARN_LOOSE;
 	nb_clear(S);
 	int r = 0;
@@ -2331,9 +2314,9 @@ __device__ __forceinline__ void scan_features(const ppi_dev &d, const ppi_rparam
 }
 
 /* One scan for the candidate state: bonds of the old (bo) and candidate (bn) state and the feature
- * neighbours of the candidate (image img1) over this lane's candidates sub, sub + G, ... False if one of
+ * neighbours of the candidate (image img1) over this lane's candidates sub, sub + 1, ... False if one of
  * them overlaps the candidate state. */
-template <int MODE, int G>
+template <int MODE>
 __device__ __forceinline__ bool scan_move(const ppi_dev &d, const Proposal &P, const Cands &C, int total, int cx, const float *cpn, const float *img1, const BoxF &B,
 		NbSel &S, int &bo, int &bn, Acc &A, int sub) {
 	const ppi_rparams &rp = d.rp[P.r];
@@ -2343,6 +2326,7 @@ __device__ __forceinline__ bool scan_move(const ppi_dev &d, const Proposal &P, c
 	const float rc2e = rp.sqr_rcut_f + eps, ovl = 1.f - eps;
 	const float rf2 = __fmul_rn(rp.sqr_rcut_f, LEARN_RF2_SCALE), loose = rf2 + LEARN_LOOSE;
 	const float4 pn = make_float4(P.po.x + P.disp.x, P.po.y + P.disp.y, P.po.z + P.disp.z, 0.f);
+	constexpr int G = 1; /* candidates a lane skips between its own */
 	nb_clear(S);
 	bo = bn = 0;
 	int r = 0;
@@ -2834,7 +2818,7 @@ __global__ void __launch_bounds__(128) k_learn_collect(ppi_dev d, long long snap
 	const int total = cands_build(d, rp, g, cx, cy, cz, C);
 	const BoxF B = box_f(d.rs[P.r].box);
 	NbSel sel;
-	scan_features<1>(d, rp, g, C, total, cx, P.i, P.po, img0, B, sel, 0);
+	scan_features(d, rp, g, C, total, cx, P.i, P.po, img0, B, sel, 0);
 	site_features(d, rp, img0, sel, B, f);
 #pragma unroll
 	for(int e = 0; e < MLP_IN; e++) out[e] = f[e];
@@ -2860,7 +2844,7 @@ __global__ void __launch_bounds__(128) k_learn_collect(ppi_dev d, long long snap
 			int bo, bn;
 			NbSel s2;
 			img1[0] = img1[1] = img1[2] = 0.f; /* the candidate's features are not needed here */
-			if(!scan_move<MODE, 1>(d, P, C, total, cx, cpn, img1, B, s2, bo, bn, A, 0)) continue;
+			if(!scan_move<MODE>(d, P, C, total, cx, cpn, img1, B, s2, bo, bn, A, 0)) continue;
 			const int dE = bo - bn;
 			const float acc = dE <= 0 ? 1.f : (float) ((dE <= PPI_LEXP) ? M.expk[dE + PPI_LEXP] : exp(-(double) dE / rp.T));
 			const float acc1 = dE <= 1 ? 1.f : (float) ((dE - 1 <= PPI_LEXP) ? M.expk[dE - 1 + PPI_LEXP] : exp(-(double) (dE - 1) / rp.T));
@@ -2892,7 +2876,7 @@ __global__ void k_learn_features(ppi_dev d) {
 	Cands C;
 	const int total = cands_build(d, rp, g, cx, cy, cz, C);
 	NbSel sel;
-	scan_features<1>(d, rp, g, C, total, cx, k, po, img, B, sel, 0);
+	scan_features(d, rp, g, C, total, cx, k, po, img, B, sel, 0);
 	site_features(d, rp, img, sel, B, f);
 	for(int e = 0; e < MLP_IN; e++) d.feat[(size_t) slot * MLP_IN + e] = f[e];
 }
