@@ -18,7 +18,7 @@ static pp_engine *G = NULL;
 int gpu_ensemble_init(System *syst, Output *IO, int seed) {
 	pp_params p;
 	pp_default_params(&p);
-	p.ensemble = syst->ensemble;            /* 0 or 5 */
+	p.ensemble = syst->ensemble;            /* 0 (NVT), 1 (GC), 3 (SUS) or 5 (NPT) */
 	p.temperature = syst->T;
 	p.pressure = syst->P;
 	p.disp_max = syst->disp_max;
@@ -31,6 +31,11 @@ int gpu_ensemble_init(System *syst, Output *IO, int seed) {
 	p.lyz_min = syst->Lyz_min;
 	p.lyz_max = syst->Lyz_max;
 	p.seed = (uint64_t) seed;
+	if(syst->ensemble == GC || syst->ensemble == SUS) { /* system.c:90-103 */
+		p.activity = syst->z;
+		p.n_min = syst->N_min;
+		p.n_max = syst->N_max;
+	}
 	if(pp_gpu_create(&p, &G) != PP_OK) output_exit(IO, "%s\n", pp_gpu_last_error(G));
 	double *r = malloc(sizeof(double) * 3 * syst->N), *R = malloc(sizeof(double) * 9 * syst->N);
 	for(int i = 0; i < syst->N; i++) {
@@ -53,13 +58,24 @@ void gpu_do_ensemble(System *syst, Output *IO) {
 
 /* before output_print / output_save read the System (main.c:82-104) */
 void gpu_sync_system(System *syst, Output *IO) {
-	double *r = malloc(sizeof(double) * 3 * syst->N), *R = malloc(sizeof(double) * 9 * syst->N);
+	/* GC / SUS: the particle count changes on the device; the reference's particle array holds N_max
+	 * (system.c:199), and particles 0 .. N-1 are the live ones, as after its own MC_add_remove */
+	double *r = malloc(sizeof(double) * 3 * syst->N_max), *R = malloc(sizeof(double) * 9 * syst->N_max);
 	pp_counters c;
 	if(pp_gpu_download(G, r, R, syst->box) != PP_OK || pp_gpu_get_energy(G, 0, &syst->energy) != PP_OK ||
 			pp_gpu_counters(G, 0, &c, 1) != PP_OK)
 		output_exit(IO, "%s\n", pp_gpu_last_error(G));
+	syst->N = pp_gpu_num_particles(G, 0);
+	if(syst->ensemble == SUS) { /* fold the device histogram into SUS_hist, which output_and_reset_sus prints */
+		int nb = syst->N_max - syst->N_min + 1;
+		llint *h = malloc(sizeof(llint) * nb);
+		if(pp_gpu_sus_histogram(G, h, 1) != PP_OK) output_exit(IO, "%s\n", pp_gpu_last_error(G));
+		for(int k = 0; k < nb; k++) syst->SUS_hist[k] += h[k];
+		free(h);
+	}
 	for(int i = 0; i < syst->N; i++) {
 		PatchyParticle *q = syst->particles + i;
+		q->index = i;
 		for(int k = 0; k < 3; k++) q->r[k] = r[3 * i + k];
 		for(int k = 0; k < 9; k++) q->orientation[k / 3][k % 3] = R[9 * i + k];
 		set_patches(syst, q); /* the reference's patch vectors follow the orientation (utils.c:20-23) */
