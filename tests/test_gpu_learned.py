@@ -85,7 +85,7 @@ def test_learned_audit_mode_has_no_mismatches(built):
     e.close()
 
 
-def _bonds_series(learned, weights, nrep=16, N=1000, rho=0.3, T=0.2, sweeps=8000, every=20, burn=1500):
+def _bonds_series(learned, weights, nrep=16, N=1000, rho=0.3, T=0.2, sweeps=8000, every=20, burn=6000):
     prm = [pp.default_params(temperature=T, seed=100 + k, disp_max=0.1, theta_max=0.2) for k in range(nrep)]
     e = pp.Engine(prm)
     for k in range(nrep):
@@ -106,7 +106,10 @@ def _bonds_series(learned, weights, nrep=16, N=1000, rho=0.3, T=0.2, sweeps=8000
 def test_learned_chain_samples_the_plain_chains_distribution(built):
     """Exactness of the MH correction: with a network whose mixture depends strongly on the environment,
     the equilibrium bonds per particle equal the plain move's within two standard errors (16 independent
-    replicas each, 8000 sweeps after 1500 of burn-in; the per-replica time averages are the samples)."""
+    replicas each, 8000 sweeps after 6000 of burn-in; the per-replica time averages are the samples). The
+    burn-in is long enough for the plain chain: after 1500 sweeps from the random insertion its bonds per
+    particle still rise by ~4 % between the two halves of the run, which biases the comparison towards the
+    faster-relaxing learned chain."""
     W = mo.init_params(seed=11, out_scale=3.0)
     W[mo.OFF_B3:] = [0.0, 1.0, 1.5, 0.5]
     a = _bonds_series(False, W)
