@@ -40,6 +40,12 @@ struct orc_system {
 	int cap;
 	long long *sus_hist;
 	int error;
+	/* base_orient (defs.h:71-74, system.c:33-54) and the AVB state (avb.h: avbmc) */
+	double base_orient[9];
+	double avb_vin, avb_vout, avb_p;
+	int avb_status;
+	int avb_nb[4]; /* neighbours[patch of the receiver]: bonded particle, or -1 (avb.c:43-75) */
+	int avb_nn;    /* num_neighbours */
 };
 
 /* ---------------------------------------------------------------- drand48 (POSIX recurrence) */
@@ -207,12 +213,11 @@ static void o_random_vector_on_sphere(orc_system *s, double *res) {
 	res[2] = 1. - 2. * ransq;
 }
 
-/* utils_rotate_matrix (utils.c:204-209): new = old . Rot(axis, t), Rot from get_rotation_matrix (utils.c:186-202) */
-static void o_rotate_matrix(const double *old, double *out, const double *a, double t) {
+/* get_rotation_matrix (utils.c:186-202): rotation by t about the unit axis a, rows */
+static void o_rotation_matrix(const double *a, double t, double *m) {
 	double st = sin(t);
 	double ct = cos(t);
 	double uct = 1. - ct;
-	double m[9];
 	m[0] = a[0] * a[0] + (1. - a[0] * a[0]) * ct;
 	m[1] = a[0] * a[1] * uct - a[2] * st;
 	m[2] = a[0] * a[2] * uct + a[1] * st;
@@ -222,9 +227,71 @@ static void o_rotate_matrix(const double *old, double *out, const double *a, dou
 	m[6] = a[0] * a[2] * uct - a[1] * st;
 	m[7] = a[1] * a[2] * uct + a[0] * st;
 	m[8] = a[2] * a[2] + (1. - a[2] * a[2]) * ct;
-	/* matrix_matrix_multiplication (utils.c:172-184) */
+}
+
+/* matrix_matrix_multiplication (utils.c:172-184): out = m . n (out may not alias m or n) */
+static void o_matmul(const double *m, const double *n, double *out) {
 	for(int i = 0; i < 3; i++)
-		for(int j = 0; j < 3; j++) out[3 * i + j] = old[3 * i + 0] * m[0 + j] + old[3 * i + 1] * m[3 + j] + old[3 * i + 2] * m[6 + j];
+		for(int j = 0; j < 3; j++) out[3 * i + j] = m[3 * i + 0] * n[0 + j] + m[3 * i + 1] * n[3 + j] + m[3 * i + 2] * n[6 + j];
+}
+
+/* MATRIX_VECTOR_MULTIPLICATION (utils.h:17-21): res = m . v */
+static void o_matvec(const double *m, const double *v, double *res) {
+	res[0] = m[0] * v[0] + m[1] * v[1] + m[2] * v[2];
+	res[1] = m[3] * v[0] + m[4] * v[1] + m[5] * v[2];
+	res[2] = m[6] * v[0] + m[7] * v[1] + m[8] * v[2];
+}
+
+/* utils_rotate_matrix (utils.c:204-209): new = old . Rot(axis, t) */
+static void o_rotate_matrix(const double *old, double *out, const double *a, double t) {
+	double m[9];
+	o_rotation_matrix(a, t, m);
+	o_matmul(old, m, out);
+}
+
+/* rotate_vector (utils.c:217-223, get_rotated_vector utils.c:211-215): v = Rot(axis, t) . v */
+static void o_rotate_vector(double *v, const double *axis, double t) {
+	double m[9], tmp[3];
+	o_rotation_matrix(axis, t, m);
+	o_matvec(m, v, tmp);
+	memcpy(v, tmp, sizeof(tmp));
+}
+
+/* get_perpendicular_versor (utils.c:38-50): a random unit vector perpendicular to v */
+static void o_perpendicular_versor(orc_system *s, const double *v, double *res) {
+	o_random_vector_on_sphere(s, res);
+	double v_norm2 = O_SCALAR(v, v);
+	double res_v = O_SCALAR(res, v);
+	double buffer = res_v / v_norm2;
+	res[0] -= buffer * v[0];
+	res[1] -= buffer * v[1];
+	res[2] -= buffer * v[2];
+	o_normalize(res);
+}
+
+/* set_orientation_around_vector (utils.c:225-270): orient = B . orient, B's third column along -v turned by
+ * t about a random axis perpendicular to it */
+static void o_set_orientation_around_vector(orc_system *s, const double *v, double *orient, double t) {
+	double y_tmp[3] = { -v[0], -v[1], -v[2] }, w_tmp[3], z[3];
+	o_random_vector_on_sphere(s, z);
+	o_random_vector_on_sphere(s, w_tmp);
+	o_gram_schmidt(y_tmp, z, w_tmp);
+	double m[9], y[3], w[3];
+	o_rotation_matrix(z, t, m);
+	o_matvec(m, y_tmp, y);
+	o_matvec(m, w_tmp, w);
+	double B[9] = { z[0], w[0], y[0], z[1], w[1], y[1], z[2], w[2], y[2] }; /* columns z, w, y */
+	if(o_determinant(B) < 0) {
+		B[0] = w[0];
+		B[3] = w[1];
+		B[6] = w[2];
+		B[1] = z[0];
+		B[4] = z[1];
+		B[7] = z[2];
+	}
+	double old[9];
+	memcpy(old, orient, sizeof(old));
+	o_matmul(B, old, orient);
 }
 
 void orc_base_patches(double base[4][3]) { /* _init_tetrahedral_patches, system.c:20-31 */
@@ -475,6 +542,168 @@ static void o_move_rototranslate(orc_system *s) { /* MC_move_rototranslate, MC.c
 	}
 }
 
+/* MC_would_interact (MC.c:232-266) with the bonding patches: *pp / *qp receive the first (p patch, q patch)
+ * pair, p's patches outer, that bonds */
+static int o_would_interact_patches(const orc_system *s, int p, const double *r, const double *qpatch, int *pp, int *qp) {
+	const double *rp = s->r + 3 * p;
+	double d[3] = { r[0] - rp[0], r[1] - rp[1], r[2] - rp[2] };
+	d[0] -= s->box[0] * rint(d[0] / s->box[0]);
+	d[1] -= s->box[1] * rint(d[1] / s->box[1]);
+	d[2] -= s->box[2] * rint(d[2] / s->box[2]);
+	double dist2 = O_SCALAR(d, d);
+	if(dist2 < 1.) return ORC_OVERLAP;
+	if(dist2 < s->kf_sqr_rcut) {
+		double norm = sqrt(dist2);
+		d[0] /= norm;
+		d[1] /= norm;
+		d[2] /= norm;
+		const double *pa = s->patch + 12 * p;
+		for(int a = 0; a < 4; a++) {
+			double p_cos = O_SCALAR(d, pa + 3 * a);
+			if(p_cos > s->prm.kf_cosmax) {
+				for(int b = 0; b < 4; b++) {
+					double q_cos = -O_SCALAR(d, qpatch + 3 * b);
+					if(q_cos > s->prm.kf_cosmax) {
+						*pp = a;
+						*qp = b;
+						return ORC_PATCH_BOND;
+					}
+				}
+			}
+		}
+	}
+	return ORC_NO_BOND;
+}
+
+/* _set_neighbours (avb.c:43-75): the particles bonded to p, indexed by p's bonding patch */
+static void o_avb_set_neighbours(orc_system *s, int p) {
+	int ind[3];
+	o_cell_index(s, s->r + 3 * p, ind);
+	s->avb_nn = 0;
+	for(int k = 0; k < 4; k++) s->avb_nb[k] = -1;
+	for(int j = -1; j < 2; j++) {
+		int cx = (ind[0] + j + s->nside[0]) % s->nside[0];
+		for(int k = -1; k < 2; k++) {
+			int cy = (ind[1] + k + s->nside[1]) % s->nside[1];
+			for(int l = -1; l < 2; l++) {
+				int cz = (ind[2] + l + s->nside[2]) % s->nside[2];
+				int q = s->head[(cx * s->nside[1] + cy) * s->nside[2] + cz];
+				while(q != -1) {
+					if(q != p) {
+						int pp = 0, qp = 0;
+						if(o_would_interact_patches(s, p, s->r + 3 * q, s->patch + 12 * q, &pp, &qp) == ORC_PATCH_BOND) {
+							s->avb_nb[pp] = q;
+							s->avb_nn++;
+						}
+					}
+					q = s->next[q];
+				}
+			}
+		}
+	}
+}
+
+/* place_inside_vbonding (utils.c:52-76): a position and orientation inside the bonding volume of patch
+ * target_patch of particle rec */
+static void o_place_inside_vbonding(orc_system *s, int rec, double *r, double *orient, int target_patch) {
+	o_rotate_matrix(s->base_orient, orient, s->base[0], 2 * orc_drand(s) * M_PI);
+	double dir[3];
+	memcpy(dir, s->patch + 12 * rec + 3 * target_patch, sizeof(dir));
+	double norm_vect[3];
+	o_perpendicular_versor(s, dir, norm_vect);
+	double theta = acos(s->prm.kf_cosmax + (1. - s->prm.kf_cosmax) * orc_drand(s));
+	o_rotate_vector(dir, norm_vect, theta);
+	o_normalize(dir);
+	double theta2 = acos(s->prm.kf_cosmax + (1. - s->prm.kf_cosmax) * orc_drand(s));
+	o_set_orientation_around_vector(s, dir, orient, theta2);
+	const double dl = s->prm.kf_delta;
+	double dist = pow(1. + orc_drand(s) * (dl * dl * dl + 3. * (dl * dl) + 3. * dl), 1. / 3.);
+	const double *rr = s->r + 3 * rec;
+	r[0] = dir[0] * dist + rr[0];
+	r[1] = dir[1] * dist + rr[1];
+	r[2] = dir[2] * dist + rr[2];
+}
+
+/* AVBMC_dynamics (avb.c:77-186): with probability avb_p (or for N < 2) a roto-translation, otherwise an
+ * aggregation-volume-bias move of a particle into or out of the bonding volume of a random receiver */
+static void o_avb_dynamics(orc_system *s) {
+	if(orc_drand(s) < s->avb_p || s->N < 2) {
+		o_move_rototranslate(s);
+		return;
+	}
+	s->tries[ORC_AVB]++;
+	const int rec = (int) (orc_drand(s) * s->N);
+	o_avb_set_neighbours(s, rec);
+	int p;
+	if(orc_drand(s) > 0.5) { /* into the bonding volume */
+		if(s->avb_nn == s->N - 1) return;
+		int found;
+		do {
+			p = (int) (orc_drand(s) * s->N);
+			found = 1;
+			for(int i = 0; i < 4 && found; i++)
+				if(s->avb_nb[i] == p) found = 0;
+		} while(!found || p == rec);
+		double new_r[3], new_R[9];
+		int target_patch = (int) (orc_drand(s) * 4);
+		o_place_inside_vbonding(s, rec, new_r, new_R, target_patch);
+		const double *rp = s->r + 3 * p;
+		double disp[3] = { new_r[0] - rp[0], new_r[1] - rp[1], new_r[2] - rp[2] };
+		double dE = -o_energy(s, p);
+		o_rototranslate(s, p, disp, new_R);
+		dE += o_energy(s, p);
+		double acc = exp(-dE / s->prm.T) * (s->N - s->avb_nn - 1.) * s->avb_vin / ((s->avb_nn + 1.) * s->avb_vout);
+		if(!s->overlap && orc_drand(s) < acc) {
+			s->accepted[ORC_AVB]++;
+			s->energy += dE;
+		}
+		else o_rollback(s, p); /* the reference leaves syst->overlap set here; every MC_energy clears it */
+	}
+	else { /* out of the bonding volume */
+		if(s->avb_nn == 0) return;
+		int random_neighbour = (int) (orc_drand(s) * s->avb_nn);
+		int cn = 0, ci = 0;
+		while(cn <= random_neighbour) {
+			if(s->avb_nb[ci] != -1) cn++;
+			ci++;
+		}
+		p = s->avb_nb[ci - 1];
+		double new_r[3], new_R[9], new_patches[12];
+		int buff;
+		do {
+			new_r[0] = orc_drand(s) * s->box[0];
+			new_r[1] = orc_drand(s) * s->box[1];
+			new_r[2] = orc_drand(s) * s->box[2];
+			o_random_orientation(s, new_R);
+			for(int i = 0; i < 4; i++) o_matvec(new_R, s->base[i], new_patches + 3 * i);
+		} while(o_would_interact_patches(s, rec, new_r, new_patches, &buff, &buff) == ORC_PATCH_BOND);
+		const double *rp = s->r + 3 * p;
+		double disp[3] = { new_r[0] - rp[0], new_r[1] - rp[1], new_r[2] - rp[2] };
+		double dE = -o_energy(s, p);
+		o_rototranslate(s, p, disp, new_R);
+		dE += o_energy(s, p);
+		double acc = exp(-dE / s->prm.T) * s->avb_nn * s->avb_vout / ((s->N - s->avb_nn) * s->avb_vin);
+		if(!s->overlap && orc_drand(s) < acc) {
+			s->accepted[ORC_AVB]++;
+			s->energy += dE;
+		}
+		else o_rollback(s, p);
+	}
+}
+
+/* syst->do_dynamics (MC_init, MC.c:115-130) */
+static void o_dynamics(orc_system *s) {
+	if(s->prm.dynamics == ORC_AVBMC) o_avb_dynamics(s);
+	else o_move_rototranslate(s);
+}
+
+int orc_avb_status(const orc_system *s) { return s->avb_status; }
+
+void orc_avb_volumes(const orc_system *s, double *v_in, double *v_out) {
+	*v_in = s->avb_vin;
+	*v_out = s->avb_vout;
+}
+
 static void o_change_volume(orc_system *s) { /* MC_change_volume, MC.c:450-513 */
 	s->tries[ORC_VOLUME]++;
 	double dE = -s->energy;
@@ -620,17 +849,17 @@ static void o_attempt_gc(orc_system *s) {
 		if(s->prm.ensemble == ORC_SUS) s->sus_hist[s->N - s->prm.n_min]++;
 	}
 	else if(s->prm.lx_move && R < (0.01 + 1. / s->N)) o_change_lx(s);
-	else if(s->N > 0) o_move_rototranslate(s);
+	else if(s->N > 0) o_dynamics(s);
 }
 
 /* one iteration of the do_NVT (MC.c:19-29) or do_NPT (MC.c:60-68) loop body */
 static void o_attempt(orc_system *s) {
 	if(s->prm.ensemble == ORC_NPT) {
 		if(orc_drand(s) < 1. / s->N) o_change_volume(s);
-		else if(s->N > 0) o_move_rototranslate(s);
+		else if(s->N > 0) o_dynamics(s);
 	}
 	else {
-		o_move_rototranslate(s);
+		o_dynamics(s);
 		/* do_NVT always draws the Lx-move number (MC.c:24), even with Lx_move = 0 */
 		const double R = orc_drand(s);
 		if(s->prm.lx_move && R < 1. / s->N) o_change_lx(s);
@@ -638,6 +867,7 @@ static void o_attempt(orc_system *s) {
 }
 
 void orc_sweep(orc_system *s) {
+	if(s->prm.dynamics == ORC_AVBMC && s->avb_status != 0) return; /* AVBMC_init refused the geometry */
 	if(s->prm.ensemble == ORC_GC || s->prm.ensemble == ORC_SUS) {
 		for(int i = 0; i < s->prm.n_max && !s->error; i++) o_attempt_gc(s);
 		return;
@@ -711,12 +941,14 @@ static orc_system *o_alloc(int N, const orc_params *prm) {
 	s->kf_sqr_rcut = (1. + prm->kf_delta) * (1. + prm->kf_delta); /* system.c:86 */
 	s->r_cut = 1. + prm->kf_delta;                                /* system.c:249 */
 	orc_seed(s, prm->seed);
-	/* system_init seeds (system.c:75) and then _init_tetrahedral_patches builds base_orient through
-	 * set_orientation_around_vector (system.c:48), which draws two random unit vectors
-	 * (utils.c:232-233). base_orient is not used by roto-translations, but the draws move the stream. */
-	double unused[3];
-	o_random_vector_on_sphere(s, unused);
-	o_random_vector_on_sphere(s, unused);
+	/* system_init seeds (system.c:75) and then _init_tetrahedral_patches builds base_orient
+	 * (system.c:33-54): set_orientation_around_vector(-base_patches[0], identity, 0), transposed. Its two
+	 * random unit vectors (utils.c:232-233) move the stream; the AVB move starts from base_orient. */
+	double my[9] = { 1., 0., 0., 0., 1., 0., 0., 0., 1. };
+	const double first[3] = { -s->base[0][0], -s->base[0][1], -s->base[0][2] };
+	o_set_orientation_around_vector(s, first, my, 0.);
+	for(int i = 0; i < 3; i++)
+		for(int j = 0; j < 3; j++) s->base_orient[3 * i + j] = my[3 * j + i];
 	return s;
 }
 
@@ -726,6 +958,14 @@ static int o_finish(orc_system *s) {
 	if(o_cells_init(s) != 0) return -1;
 	o_cells_fill(s);
 	s->energy = 0.;
+	if(s->prm.dynamics == ORC_AVBMC) { /* AVBMC_init (avb.c:13-36), called from MC_init after system_init */
+		const double dl = s->prm.kf_delta, cm = s->prm.kf_cosmax;
+		double sin_theta = sin(acos(cm));
+		s->avb_status = sin_theta >= 1. / (2. * (1. + dl)) ? -1 : 0;
+		s->avb_vin = 4 * 4 * (M_PI * (dl * dl * dl + 3. * (dl * dl) + 3. * dl) * ((1. - cm) * (1. - cm)) / 3.);
+		s->avb_vout = s->V - s->avb_vin;
+		s->avb_p = s->prm.avb_p > 0. ? s->prm.avb_p : 0.5;
+	}
 	return 0;
 }
 

@@ -29,8 +29,13 @@ extern "C" {
 #define ORC_SUS 3 /* successive umbrella sampling (defs.h:23), do_SUS (MC.c:45-58) */
 #define ORC_NPT 5
 
+/* Dynamics (defs.h:27-29) */
+#define ORC_RTMC 0
+#define ORC_AVBMC 2 /* aggregation-volume-bias moves mixed with roto-translations, avb.c:77-186 */
+
 /* move-type slots of the tries/accepted counters, as in defs.h:11-19 */
 #define ORC_ROTO_TRASL 0
+#define ORC_AVB 1    /* defs.h:13 */
 #define ORC_ADD 2    /* defs.h:14 */
 #define ORC_REMOVE 3 /* defs.h:15 */
 #define ORC_VOLUME 6
@@ -52,6 +57,8 @@ typedef struct orc_params {
 	double lyz_min, lyz_max;   /* Lyz_min, Lyz_max */
 	double activity;           /* Activity z (GC and SUS, system.c:91) */
 	int n_min, n_max;          /* GC: 0 and GC_N_max; SUS: Umbrella_sampling_min / _max (system.c:92-103) */
+	int dynamics;              /* Dynamics: ORC_RTMC or ORC_AVBMC (system.c:63, MC.c:115-130) */
+	double avb_p;              /* avb_p: probability of a roto-translation in AVBMC (avb.c:33-35); <= 0 selects 0.5 */
 } orc_params;
 
 typedef struct orc_system orc_system;
@@ -104,6 +111,12 @@ int orc_error(const orc_system *s);
 /* SUS histogram of N after every insertion/removal attempt (MC.c:50), bins N_min..N_max; reset = 1 clears
  * it as output_and_reset_sus does (output.c:343-356). Returns the number of bins. */
 int orc_sus_hist(orc_system *s, long long *out, int reset);
+
+/* AVBMC: 0, or -1 where AVBMC_init refuses the patch geometry (avb.c:14-17: the single-bond-per-patch
+ * condition). A refused system makes no moves. */
+int orc_avb_status(const orc_system *s);
+/* AVBMC_init's bonding and non-bonding volumes (avb.c:26-28) */
+void orc_avb_volumes(const orc_system *s, double *v_in, double *v_out);
 
 /* drand48 recurrence check: n draws from a generator seeded as srand48(seed) would be. */
 void orc_drand48_sequence(int seed, int n, double *out);

@@ -126,11 +126,13 @@ int main(int argc, char *argv[]) {
 		}
 	}
 
-	/* system_init (system.c:58-252), Dynamics = 0, NVT or NPT */
+	/* system_init (system.c:58-252), Dynamics = 0 or 2 */
 	orc_params prm;
 	memset(&prm, 0, sizeof(prm));
 	int dynamics = atoi(get(in, "Dynamics", 1));
 	prm.ensemble = ensemble;
+	prm.dynamics = dynamics;
+	if(dynamics == ORC_AVBMC && (v = get(in, "avb_p", 0))) prm.avb_p = atof(v); /* avb.c:35 */
 	prm.disp_max = atof(get(in, "Disp_max", 1));
 	prm.theta_max = atof(get(in, "Theta_max", 1));
 	prm.T = atof(get(in, "Temperature", 1));
@@ -163,11 +165,17 @@ int main(int argc, char *argv[]) {
 		fb = fopen("boxshape.dat", mode);
 		if(fb == NULL) die("boxshape.dat is not writable");
 	}
-	if(dynamics != 0 || (ensemble != ORC_NVT && ensemble != ORC_NPT && ensemble != ORC_GC && ensemble != ORC_SUS))
-		die("only Dynamics = 0 with Ensemble 0, 1, 3 or 5 is restated");
+	if((dynamics != ORC_RTMC && dynamics != ORC_AVBMC) || (ensemble != ORC_NVT && ensemble != ORC_NPT && ensemble != ORC_GC && ensemble != ORC_SUS))
+		die("only Dynamics = 0 or 2 with Ensemble 0, 1, 3 or 5 is restated");
 	char err[512];
 	orc_system *s = orc_load_rrr(conf, &prm, err, sizeof(err));
 	if(s == NULL) die(err);
+	if(dynamics == ORC_AVBMC) { /* AVBMC_init (avb.c:13-31) */
+		if(orc_avb_status(s) != 0) die("The AVB move cannot be used with patches that do not fulfill the single-bond-per-patch condition");
+		double vin, vout;
+		orc_avb_volumes(s, &vin, &vout);
+		fprintf(stderr, "Vavb = %lf\n", vin); /* output_log_msg */
+	}
 	if(ensemble == ORC_SUS) { /* system.c:100-101 */
 		char m[256];
 		if(orc_N(s) < prm.n_min) {
@@ -221,6 +229,7 @@ int main(int argc, char *argv[]) {
 			orc_counters(s, tries, acc);
 			fprintf(fa, "%lld", step);
 			fprintf(fa, " %e", acc[ORC_ROTO_TRASL] / (double) tries[ORC_ROTO_TRASL]);
+			if(dynamics == ORC_AVBMC) fprintf(fa, " %e", acc[ORC_AVB] / (double) tries[ORC_AVB]); /* output.c:156-158 */
 			if(ensemble == ORC_GC || ensemble == ORC_SUS) {
 				fprintf(fa, " %e", acc[ORC_ADD] / (double) tries[ORC_ADD]);
 				fprintf(fa, " %e", acc[ORC_REMOVE] / (double) tries[ORC_REMOVE]);

@@ -43,7 +43,7 @@ GENERATED = [
     ("small", 300, 0.3, 4242),
 ]
 
-TRAJ_INPUT = """Dynamics = 0
+TRAJ_INPUT = """Dynamics = {dynamics}
 Ensemble = {ensemble}
 Seed = {seed}
 Temperature = {T}
@@ -71,6 +71,10 @@ TRAJ = [
     ("small_gc", "generator_300_0.3_4242.rrr", 1, 0.12, 300, 30, 13, "Activity = 0.1\nGC_N_max = 600\n"),
     ("small_sus", "generator_300_0.3_4242.rrr", 3, 0.12, 300, 30, 17,
      "Activity = 0.1\nUmbrella_sampling_min = 295\nUmbrella_sampling_max = 305\nUmbrella_sampling_folder = sus\n"),
+    # aggregation-volume-bias moves mixed with roto-translations (Dynamics = 2, avb.c:77-186), NVT with the
+    # default avb_p and NPT with avb_p = 0.3
+    ("small_avb", "generator_300_0.3_4242.rrr", 0, 0.11, 300, 30, 21, "", 2),
+    ("small_avb_npt", "generator_300_0.3_4242.rrr", 5, 0.11, 300, 30, 23, "P = 0.05\nrescale_factor_max = 0.01\navb_p = 0.3\n", 2),
 ]
 
 PROBE_INPUT = """Dynamics = 0
@@ -120,17 +124,19 @@ def main():
         out = subprocess.check_output([os.path.join(REFOUT, "ref_probe"), inp], cwd=work, stderr=subprocess.DEVNULL)
         gz_write(os.path.join(OUT, "probe_%s.txt.gz" % name), out)
     # trajectories of the reference main loop
-    for name, conf, ens, T, steps, pe, seed, extra in TRAJ:
+    for entry in TRAJ:
+        name, conf, ens, T, steps, pe, seed, extra = entry[:8]
+        dyn = entry[8] if len(entry) > 8 else 0
         d = os.path.join(work, name)
         os.makedirs(os.path.join(d, "confs"))
         if "Umbrella_sampling_folder" in extra:
             os.makedirs(os.path.join(d, "sus"))
         shutil.copy(os.path.join(work, conf), os.path.join(d, conf))
-        open(os.path.join(d, "input"), "w").write(TRAJ_INPUT.format(ensemble=ens, seed=seed, T=T, steps=steps, print_every=pe, save_every=pe * 2, conf=conf, extra=extra))
+        open(os.path.join(d, "input"), "w").write(TRAJ_INPUT.format(dynamics=dyn, ensemble=ens, seed=seed, T=T, steps=steps, print_every=pe, save_every=pe * 2, conf=conf, extra=extra))
         out = subprocess.check_output([os.path.join(REFOUT, "PatchyParticles"), "input"], cwd=d, stderr=subprocess.DEVNULL)
         dst = os.path.join(OUT, "traj_" + name)
         os.makedirs(dst, exist_ok=True)
-        open(os.path.join(dst, "input"), "w").write(TRAJ_INPUT.format(ensemble=ens, seed=seed, T=T, steps=steps, print_every=pe, save_every=pe * 2, conf=conf, extra=extra))
+        open(os.path.join(dst, "input"), "w").write(TRAJ_INPUT.format(dynamics=dyn, ensemble=ens, seed=seed, T=T, steps=steps, print_every=pe, save_every=pe * 2, conf=conf, extra=extra))
         open(os.path.join(dst, "stdout.txt"), "wb").write(out)
         for fn in ("energy.dat", "acceptance.dat", "density.dat", "boxshape.dat"):
             if os.path.exists(os.path.join(d, fn)):
