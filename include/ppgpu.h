@@ -42,7 +42,11 @@ extern "C" {
 #define PP_SUS 3 /* Ensemble = 3, successive umbrella sampling (defs.h:23, do_SUS MC.c:45-58) */
 #define PP_NPT 5 /* Ensemble = 5 (defs.h:24) */
 
+#define PP_RTMC 0  /* Dynamics = 0: roto-translations (defs.h:27) */
+#define PP_AVBMC 2 /* Dynamics = 2: aggregation-volume-bias moves and roto-translations (defs.h:29) */
+
 #define PP_MOVE_ROTO_TRASL 0 /* tries/accepted slots as System::tries/accepted (defs.h:11-19, 95-96) */
+#define PP_MOVE_AVB 1        /* aggregation-volume-bias moves (defs.h:13) */
 #define PP_MOVE_ADD 2        /* GC / SUS insertions (defs.h:14) */
 #define PP_MOVE_REMOVE 3     /* GC / SUS removals (defs.h:15) */
 #define PP_MOVE_VOLUME 6
@@ -77,6 +81,13 @@ typedef struct pp_params {
 	 * highest index to the removed particle's, as the reference does). */
 	double activity;
 	int n_min, n_max;
+	/* Dynamics (system.c:63, MC.c:115-130): PP_RTMC, or PP_AVBMC for aggregation-volume-bias moves mixed
+	 * with the roto-translations (avb.c:77-186). An AVB engine makes, per MC step, one checkerboard round of
+	 * roto-translations and round((1 - avb_p) N) AVB moves, the latter one after the other on the device
+	 * before each re-sort (NVT and NPT; the patches must satisfy the single-bond-per-patch condition of
+	 * avb.c:14-17). */
+	int dynamics;
+	double avb_p; /* avb_p (avb.c:33-35): the share of roto-translations among the reference's attempts */
 } pp_params;
 
 typedef struct pp_counters {
@@ -171,7 +182,8 @@ int pp_gpu_kernel_stats(pp_engine *e, pp_kernel_stats *out, int reset);
 
 /* Whole re-sort periods of pp_gpu_sweeps are replayed from captured CUDA graphs (one launch per period
  * instead of one per kernel; the launches and the trajectory are the same). enable = 0 turns the graphs
- * off (every kernel launched on the stream); per-group event timing always uses stream launches. */
+ * off (every kernel launched on the stream); per-group event timing always uses stream launches. GC / SUS
+ * engines and engines with AVB moves launch their kernels one by one: enable = 1 returns PP_ERR_ARG there. */
 int pp_gpu_set_graphs(pp_engine *e, int enable);
 
 /* SUS (Ensemble = 3): the histogram of N counted after every insertion / removal attempt (MC.c:50), bins

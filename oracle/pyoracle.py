@@ -21,6 +21,7 @@ SUS = 3
 NPT = 5
 RTMC = 0  # Dynamics (defs.h:27-29)
 AVBMC = 2
+AVB = 1  # tries / accepted slot of the AVB move (defs.h:13)
 
 
 class OrcParams(ctypes.Structure):

@@ -28,11 +28,14 @@ NVT = 0
 GC = 1
 SUS = 3
 NPT = 5
+RTMC = 0  # Dynamics: roto-translations
+AVBMC = 2  # Dynamics: aggregation-volume-bias moves and roto-translations
 PREC_FP32_GUARD = 0
 PREC_FP64 = 1
 MOVE_ROTO_TRASL = 0
 MOVE_ADD = 2
 MOVE_REMOVE = 3
+MOVE_AVB = 1
 MOVE_VOLUME = 6
 MOVE_LX = 7
 N_MOVES = 8
@@ -60,6 +63,8 @@ class PPParams(ctypes.Structure):
         ("activity", ctypes.c_double),
         ("n_min", ctypes.c_int),
         ("n_max", ctypes.c_int),
+        ("dynamics", ctypes.c_int),
+        ("avb_p", ctypes.c_double),
     ]
 
 

@@ -44,6 +44,7 @@ struct pp_engine {
 	double cell_scale;    /* cell edge / minimum edge (autotuner) */
 	int any_npt;
 	int any_lx;           /* some NVT replica has the box-shape move */
+	int any_avb;          /* some replica makes AVB moves (Dynamics = 2) */
 	int any_audit;
 	int nl_mode;          /* per-epoch neighbour lists for plain moves (pp_gpu_set_neighbour_lists) */
 	int nl_valid;         /* the current epoch's lists are built and only plain moves ran since */
@@ -174,6 +175,8 @@ void pp_default_params(pp_params *p) {
 	p->guard_eps = 1e-5;
 	p->resort_every = 0;
 	p->audit = 0;
+	p->dynamics = PP_RTMC;
+	p->avb_p = 0.5; /* avb.c:30 */
 }
 
 static int is_exchange(const pp_engine *e);
@@ -196,6 +199,13 @@ static int check_params(pp_engine *e, const pp_params *p) {
 	if(p->resort_every < 0 || p->resort_every > 64) return set_err(e, PP_ERR_ARG, "resort_every (re-sort period in rounds) must be 0 or in [1, 64]");
 	if(p->ensemble == PP_NPT && !(p->rescale_factor_max > 0. && p->rescale_factor_max < 1.)) return set_err(e, PP_ERR_ARG, "rescale_factor_max must lie in (0, 1)");
 	if(p->lx_move < 0 || p->lx_move > 2) return set_err(e, PP_ERR_ARG, "Lx_move must be 0, 1 (reference acceptance) or 2 (Boltzmann acceptance)");
+	if(p->dynamics != PP_RTMC && p->dynamics != PP_AVBMC) return set_err(e, PP_ERR_ARG, "Dynamics %d not supported (0 = roto-translations, 2 = AVB)", p->dynamics);
+	if(p->dynamics == PP_AVBMC) {
+		if(p->ensemble != PP_NVT && p->ensemble != PP_NPT) return set_err(e, PP_ERR_ARG, "the AVB move runs in the NVT and NPT ensembles");
+		if(!(p->avb_p >= 0. && p->avb_p <= 1.)) return set_err(e, PP_ERR_ARG, "avb_p must lie in [0, 1]");
+		if(sin(acos(p->kf_cosmax)) >= 1. / (2. * (1. + p->kf_delta))) /* avb.c:14-17 */
+			return set_err(e, PP_ERR_ARG, "The AVB move cannot be used with patches that do not fulfill the single-bond-per-patch condition");
+	}
 	if(p->ensemble == PP_NVT && p->lx_move) {
 		if(!(p->lx_change_max > 0.)) return set_err(e, PP_ERR_ARG, "Lx_change_max must be > 0");
 		if(!(p->lyz_min > 0.) || !(p->lyz_max > p->lyz_min)) return set_err(e, PP_ERR_ARG, "Lyz_min and Lyz_max must satisfy 0 < Lyz_min < Lyz_max");
@@ -242,7 +252,9 @@ static int create_common(const pp_params *prms, int n, pp_engine **out) {
 		if(e->prm[i].ensemble == PP_NPT) e->any_npt = 1;
 		if(e->prm[i].ensemble == PP_NVT && e->prm[i].lx_move) e->any_lx = 1;
 		if(e->prm[i].audit) e->any_audit = 1;
+		if(e->prm[i].dynamics == PP_AVBMC) e->any_avb = 1;
 	}
+	if(e->any_avb) e->graphs_on = 0; /* the AVB batches are launched from the host before each re-sort */
 	if(e->prm[0].resort_every > 0) e->resort_every = e->prm[0].resort_every;
 	for(int i = 0; i < n; i++)
 		if((e->prm[i].ensemble == PP_GC || e->prm[i].ensemble == PP_SUS) && n > 1)
@@ -273,7 +285,8 @@ static void free_device(pp_engine *e) {
 	void **ptrs[] = { (void **) &e->d.rec, (void **) &e->d.spos, (void **) &e->d.sori, (void **) &e->d.id, (void **) &e->d.rep, (void **) &e->d.cellof,
 		(void **) &e->d.cell_count, (void **) &e->d.cell_start, (void **) &e->d.cell_cursor, (void **) &e->d.cell_rep, (void **) &e->d.scan_aux,
 		(void **) &e->d.clist, (void **) &e->d.ccount, (void **) &e->d.dflag, (void **) &e->d.eflag, (void **) &e->d.rp, (void **) &e->d.rs, (void **) &e->d.grid, (void **) &e->d.out_bonds,
-		(void **) &e->d.out_overlaps, (void **) &e->d.out_partners, (void **) &e->d.tmp_rec, (void **) &e->d.tmp_id };
+		(void **) &e->d.out_overlaps, (void **) &e->d.out_partners, (void **) &e->d.tmp_rec, (void **) &e->d.tmp_id, (void **) &e->d.avb_head,
+		(void **) &e->d.avb_next, (void **) &e->d.avb_cell };
 	for(size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); i++) {
 		if(*ptrs[i]) cudaFree(*ptrs[i]);
 		*ptrs[i] = NULL;
@@ -409,6 +422,34 @@ static int slot_cap(const pp_engine *e, int r) {
 
 static int is_exchange(const pp_engine *e) { return e->nrep == 1 && (e->prm[0].ensemble == PP_GC || e->prm[0].ensemble == PP_SUS); }
 
+/* AVB (Dynamics = 2): AVBMC_init's volumes (avb.c:26-28) from the uploaded box, the attempts per MC step,
+ * the linked-cell grid the batches may use, and a rotation base_orient taking base patch 0 to (0, 0, 1)
+ * (system.c:33-54 builds one from random vectors; place_inside_vbonding follows it with a uniform turn
+ * about base patch 0, so which one does not change the distribution of its orientations) */
+static void avb_rparams(const pp_engine *e, int r, ppi_rparams *rp) {
+	const pp_params *p = e->prm + r;
+	const double *box = e->h_box[r];
+	const double dl = p->kf_delta, cm = p->kf_cosmax;
+	rp->avb_vin = 4 * 4 * (M_PI * (dl * dl * dl + 3. * (dl * dl) + 3. * dl) * ((1. - cm) * (1. - cm)) / 3.);
+	rp->avb_vout = box[0] * box[1] * box[2] - rp->avb_vin;
+	rp->avb_per_step = (int) floor((1. - p->avb_p) * e->N[r] + 0.5);
+	const double grow = p->ensemble == PP_NPT ? 1.3 : 1.0;
+	for(int a = 0; a < 3; a++) {
+		int n = (int) floor(box[a] * grow / rp->r_cut);
+		rp->avb_ncap[a] = n < 3 ? 3 : n;
+	}
+	const double *b0 = rp->base[0];
+	double u[3] = { 1. - b0[0] * b0[0], -b0[0] * b0[1], -b0[0] * b0[2] }; /* e_x without its b0 part */
+	const double nu = sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+	for(int k = 0; k < 3; k++) u[k] /= nu;
+	const double v[3] = { b0[1] * u[2] - b0[2] * u[1], b0[2] * u[0] - b0[0] * u[2], b0[0] * u[1] - b0[1] * u[0] };
+	for(int k = 0; k < 3; k++) {
+		rp->base_orient[k] = u[k];
+		rp->base_orient[3 + k] = v[k];
+		rp->base_orient[6 + k] = b0[k];
+	}
+}
+
 static int derive_rparams(pp_engine *e, int r, ppi_rparams *rp) {
 	const pp_params *p = e->prm + r;
 	memset(rp, 0, sizeof(*rp));
@@ -440,6 +481,8 @@ static int derive_rparams(pp_engine *e, int r, ppi_rparams *rp) {
 	rp->activity = p->activity;
 	rp->n_min = p->ensemble == PP_SUS ? p->n_min : 0;
 	rp->n_max = p->n_max;
+	rp->dynamics = p->dynamics;
+	if(p->dynamics == PP_AVBMC) avb_rparams(e, r, rp);
 	for(int k = 0; k < 32; k++) {
 		double pk = exp(-(double) k / p->temperature);
 		double t = ceil(pk * 9007199254740992.0);
@@ -502,6 +545,8 @@ static int read_states(pp_engine *e) {
 	for(int r = 0; r < e->nrep; r++)
 		if(e->h_rs[r].error == PPI_E_LISTS)
 			return set_err(e, PP_ERR_CAPACITY, "replica %d: more guard-band pairs in one volume pass than its buffer holds", r);
+		else if(e->h_rs[r].error == PPI_E_AVB)
+			return set_err(e, PP_ERR_STATE, "replica %d: an AVB move's rejection sampling ran out of draws", r);
 		else if(e->h_rs[r].error == PPI_E_EXACT)
 			return set_err(e, PP_ERR_STATE, "replica %d: more pairs within 1e-12 of a bonding threshold than one warp keeps for the exact test", r);
 		else if(e->h_rs[r].error)
@@ -648,7 +693,7 @@ static int commit(pp_engine *e) {
 	e->h_rs = calloc(e->nrep, sizeof(ppi_rstate));
 	HOST_OK(e->h_rp);
 	HOST_OK(e->h_rs);
-	long long cells = 0;
+	long long cells = 0, avb_cells = 0;
 	int p0 = 0;
 	for(int r = 0; r < e->nrep; r++) {
 		ppi_rparams *rp = e->h_rp + r;
@@ -658,7 +703,12 @@ static int commit(pp_engine *e) {
 		p0 += slot_cap(e, r);
 		rp->cell_base = (int) cells;
 		cells += rp->cell_cap;
+		if(rp->dynamics == PP_AVBMC) {
+			rp->avb_head0 = (int) avb_cells;
+			avb_cells += (long long) rp->avb_ncap[0] * rp->avb_ncap[1] * rp->avb_ncap[2];
+		}
 	}
+	if(avb_cells > (1LL << 30)) return set_err(e, PP_ERR_CAPACITY, "too many AVB cells in total");
 	if(cells > (1LL << 30)) return set_err(e, PP_ERR_CAPACITY, "too many cells in total");
 	ppi_dev *d = &e->d;
 	d->nrep = e->nrep;
@@ -688,6 +738,11 @@ static int commit(pp_engine *e) {
 	CU(cudaMemsetAsync(d->dflag, 0, 8 * (size_t) d->clist_cap, e->stream));
 	CU(cudaMalloc((void **) &d->eflag, n1));
 	CU(cudaMemsetAsync(d->eflag, 0, n1, e->stream));
+	if(avb_cells > 0) {
+		CU(cudaMalloc((void **) &d->avb_head, sizeof(int) * (size_t) avb_cells));
+		CU(cudaMalloc((void **) &d->avb_next, sizeof(int) * n1));
+		CU(cudaMalloc((void **) &d->avb_cell, sizeof(int) * n1));
+	}
 	d->audit_any = e->any_audit;
 	{ /* lanes per attempt: a tuning override for measurements (4 by default) */
 		const char *v = getenv("PPGPU_LANES");
@@ -812,6 +867,13 @@ int pp_gpu_upload_replica(pp_engine *e, int r, int N, const double *rr, const do
 			int rc = read_states(e);
 			if(rc != PP_OK) return rc;
 			memcpy(e->h_box[r], box, sizeof(double) * 3);
+			if(e->prm[r].dynamics == PP_AVBMC) { /* AVBMC_init's V_out follows the uploaded box; the cell grid keeps its reservation */
+				ppi_rparams *rp = e->h_rp + r;
+				int ncap[3] = { rp->avb_ncap[0], rp->avb_ncap[1], rp->avb_ncap[2] };
+				avb_rparams(e, r, rp);
+				for(int a = 0; a < 3; a++) rp->avb_ncap[a] = ncap[a];
+				CU(cudaMemcpy(e->d.rp + r, rp, sizeof(ppi_rparams), cudaMemcpyHostToDevice));
+			}
 			ppi_rstate *s = e->h_rs + r;
 			memset(s, 0, sizeof(*s));
 			memcpy(s->box, box, sizeof(s->box));
@@ -1085,6 +1147,10 @@ int pp_gpu_set_barrier_test(pp_engine *e, long long limit_cycles, int unreachabl
 
 int pp_gpu_set_graphs(pp_engine *e, int enable) {
 	if(e == NULL) return PP_ERR_ARG;
+	/* GC / SUS exchanges and AVB batches are launched from the host between re-sort periods, which a
+	 * captured period would skip */
+	if(enable && (is_exchange(e) || e->any_avb))
+		return set_err(e, PP_ERR_ARG, "engines with insertions and removals or AVB moves launch their kernels one by one (no graphs)");
 	e->graphs_on = enable ? 1 : 0;
 	if(!enable) drop_graphs(e);
 	return PP_OK;
@@ -1147,6 +1213,11 @@ int pp_gpu_sweeps(pp_engine *e, long long n) {
 		for(int rr = 0; rr < e->rounds_per_sweep; rr++) {
 			if(e->round_counter % e->resort_every == 0) {
 				if(is_exchange(e) && (rc = exchange_step(e)) != PP_OK) return rc;
+				if(e->any_avb) { /* the AVB moves of the coming re-sort period (avb.c:77-186) */
+					long long nl = 0;
+					CK(ppi_avb(&e->d, e->epoch, e->resort_every, e->stream, &nl));
+					e->launches += nl;
+				}
 				if((rc = ev_begin(e, 0, &ev)) != PP_OK) return rc;
 				if((rc = do_resort(e)) != PP_OK) return rc;
 				if((rc = ev_end(e, ev)) != PP_OK) return rc;
@@ -1813,6 +1884,7 @@ int pp_gpu_set_proposal(pp_engine *e, int proposal) {
 	int rc = ready(e);
 	if(rc != PP_OK) return rc;
 	if(proposal != PP_PROPOSAL_PLAIN && is_exchange(e)) return set_err(e, PP_ERR_ARG, "the learned proposal is not available with insertions and removals");
+	if(proposal != PP_PROPOSAL_PLAIN && e->any_avb) return set_err(e, PP_ERR_ARG, "the learned proposal is not available with AVB moves");
 	if(proposal == PP_PROPOSAL_PLAIN) {
 		e->proposal = proposal;
 		return PP_OK;
@@ -2061,6 +2133,7 @@ int pp_gpu_autotune(pp_engine *e, int trial_sweeps, pp_tune_result *out) {
 	if(rc != PP_OK) return rc;
 	if(trial_sweeps < 1 || trial_sweeps > 100000) return set_err(e, PP_ERR_ARG, "trial_sweeps must lie in [1, 100000]");
 	if(is_exchange(e)) return set_err(e, PP_ERR_ARG, "the autotuner does not run GC or SUS engines (their particle count changes)");
+	if(e->any_avb) return set_err(e, PP_ERR_ARG, "the autotuner does not run AVB engines");
 	const int resorts[] = { 1, 2, 4, 8, 16 }, reorders[] = { 4, 16, 64 };
 	const double scales[] = { 1.0, 1.2, 1.5 };
 	const int r0 = e->resort_every, o0 = e->reorder_every, l0 = e->nl_mode;

@@ -43,6 +43,7 @@ extern "C" {
 #define PPI_E_LISTS 4 /* more guard-band pairs in one volume pass than its buffer holds */
 #define PPI_E_BARRIER 5 /* a grid-barrier wait of the persistent round kernel ran out of its limit */
 #define PPI_E_GCFULL 6  /* a grand-canonical insertion found the system at GC_N_max (the reference stops there) */
+#define PPI_E_AVB 7     /* an AVB move's rejection sampling ran out of its draw limit (no move made) */
 
 typedef struct ppi_rparams {
 	int N;           /* particles of this replica */
@@ -64,6 +65,13 @@ typedef struct ppi_rparams {
 	double lx_change_max, lyz_min, lyz_max; /* Lx_change_max, Lyz_min, Lyz_max (system.c:177-179) */
 	double activity;       /* GC / SUS: Activity z (system.c:91) */
 	int n_min, n_max;      /* GC / SUS: the particle-number window (GC: 0 and GC_N_max) */
+	/* Dynamics = 2 (avb.c): aggregation-volume-bias moves between the checkerboard rounds */
+	int dynamics;          /* 0 roto-translations only, 2 roto-translations and AVB moves */
+	int avb_head0;         /* first entry of this replica's AVB cell heads */
+	int avb_ncap[3];       /* cells per axis the heads were reserved for */
+	int avb_per_step;      /* AVB attempts per MC step: round((1 - avb_p) N) */
+	double avb_vin, avb_vout; /* AVBMC_init's bonding and non-bonding volumes (avb.c:26-28), fixed at upload */
+	double base_orient[9]; /* a rotation taking base patch 0 to (0, 0, 1) (system.c:33-54) */
 } ppi_rparams;
 
 typedef struct ppi_rstate {
@@ -202,6 +210,10 @@ typedef struct ppi_dev {
 	int bar_extra;       /* test hook: arrivals the first barrier waits for beyond the grid (1 = never completes) */
 	int persist;         /* 1: plain rounds over the neighbour lists use k_round, 0: one launch per colour */
 	unsigned long long *sus_hist; /* SUS: histogram of N after every insertion/removal attempt, n_max - n_min + 1 bins */
+	/* AVB moves: linked cells (cells.c) of the replica's live particles, rebuilt at every AVB batch */
+	int *avb_head;     /* per replica avb_ncap[0] x [1] x [2] entries from avb_head0: first slot offset, -1 */
+	int *avb_next;     /* per slot: next slot offset of its cell, -1 */
+	int *avb_cell;     /* per slot: its AVB cell */
 } ppi_dev;
 
 #define PPI_MAX_PARTNERS 24
@@ -218,6 +230,8 @@ int ppi_volume(const ppi_dev *d, long long sweep, int use_nl, cudaStream_t s, lo
 int ppi_gram_schmidt(const ppi_dev *d, int first, int count, cudaStream_t s, long long *nl);
 /* GC / SUS: `attempts` sequential insertion / removal attempts per replica (MC_add_remove, MC.c:342-448) */
 int ppi_exchange(const ppi_dev *d, long long step, int attempts, cudaStream_t s, long long *nl);
+/* Dynamics = 2: `steps` MC steps' worth of AVB attempts per AVB replica (AVBMC_dynamics, avb.c:77-186) */
+int ppi_avb(const ppi_dev *d, long long step, int steps, cudaStream_t s, long long *nl);
 int ppi_reorder(const ppi_dev *d, cudaStream_t s, long long *nl);
 /* writes x y z R00..R22 (12 doubles) of slots [first, first + count) into d->tmp_rec */
 int ppi_export(const ppi_dev *d, int first, int count, cudaStream_t s, long long *nl);

@@ -26,6 +26,7 @@
 #include "ppgpu_umma.cuh"
 
 #include <cuda_runtime.h>
+#include <float.h>
 #include <math.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -4225,9 +4226,404 @@ __global__ void __launch_bounds__(EXCH_B) k_exchange(ppi_dev d, long long step, 
 }
 
 /* ------------------------------------------------------------------------------------------------ */
+/* aggregation-volume-bias moves (Dynamics = 2, AVBMC_dynamics)                                      */
+/* ------------------------------------------------------------------------------------------------ */
+/* One CTA per AVB replica makes its AVB attempts one after the other, as AVBMC_dynamics (avb.c:77-186)
+ * does for the fraction 1 - avb_p of the reference's attempts (the roto-translations of the other
+ * fraction are the checkerboard rounds): a receiver drawn uniformly and its bonded partners indexed by
+ * its bonding patch (_set_neighbours, avb.c:43-75); with probability 1/2 a particle outside its bonding
+ * volume is placed inside it (place_inside_vbonding, utils.c:52-76) and accepted with
+ * min(1, exp(-dE / T) (N - n - 1) V_in / ((n + 1) V_out)); otherwise one of its n partners goes to a
+ * uniform position and orientation that does not bond to it, accepted with
+ * min(1, exp(-dE / T) n V_out / ((N - n) V_in)). Neighbourhoods come from linked cells of edge >= r_cut
+ * (cells.c:17-63) built from the FP64 state at the start of the batch and kept current as particles
+ * move; every pair is decided in FP64 with the reference's operation order, so the tracked energy stays
+ * exact. The caller re-sorts the engine's cells after the batch. */
+#define AVB_B 64
+#define TAG_AVB 10u
+#define AVB_DRAWS 4096 /* draws a rejection loop may take before the batch stops with an error */
+
+/* successive 53-bit uniforms of one attempt from its own Philox counter (item = attempt) */
+struct AvbRng {
+	const ppi_rparams *rp;
+	long long step;
+	int r;
+	uint32_t item, sub;
+	U4 u;
+	int k;
+	__device__ double next() {
+		if(k == 0) {
+			u = rng(*rp, step, r, TAG_AVB, item, sub++);
+			k = 2;
+		}
+		k--;
+		return k ? u01d(u.x, u.y) : u01d(u.z, u.w);
+	}
+};
+
+/* cells_fill_and_get_idx_from_vector (cells.c:43-49) */
+__device__ __forceinline__ int avb_cell_of(const double *r, const double *box, const int *ns, int *idx) {
+#pragma unroll
+	for(int a = 0; a < 3; a++) {
+		const double f = r[a] / box[a];
+		const int i = (int) ((f - floor(f)) * (1. - DBL_EPSILON) * ns[a]);
+		idx[a] = i < 0 ? 0 : (i >= ns[a] ? ns[a] - 1 : i); /* [0, ns) for every finite position already */
+	}
+	return (idx[0] * ns[1] + idx[1]) * ns[2] + idx[2];
+}
+
+/* MC_would_interact (MC.c:232-266) with the reference's operation order for probe p at (pr, pR) and q at
+ * qr, whose orientation is qR or, when qR is null, R0 . Q(q) of its record qrec: -1 overlap, 0 no bond,
+ * 1 bond; *pa receives p's bonding patch (the first whose cosine passes, the reference's p_patch) */
+__device__ __noinline__ int avb_pair(const double *pr, const double *pR, const double *qr, const double *qrec, const double *qR, const ppi_rparams &rp, const double *box,
+		int *pa) {
+	double d[3];
+#pragma unroll 1
+	for(int k = 0; k < 3; k++) {
+		d[k] = __dsub_rn(qr[k], pr[k]);
+		d[k] = __dsub_rn(d[k], __dmul_rn(box[k], rint(__ddiv_rn(d[k], box[k]))));
+	}
+	const double dist2 = scalar64(d, d);
+	if(dist2 < 1.) return -1;
+	if(!(dist2 < rp.sqr_rcut)) return 0;
+	double Rq[9];
+	if(qR == nullptr) orient64(qrec + PPI_R0, qrec + PPI_Q, Rq);
+	else
+		for(int k = 0; k < 9; k++) Rq[k] = qR[k];
+	const double norm = __dsqrt_rn(dist2);
+	d[0] = __ddiv_rn(d[0], norm);
+	d[1] = __ddiv_rn(d[1], norm);
+	d[2] = __ddiv_rn(d[2], norm);
+	double P[3];
+	int first = -1, qok = 0;
+#pragma unroll 1
+	for(int a = 0; a < 4; a++) {
+		patch64(pR, rp.base[a], P);
+		if(first < 0 && scalar64(d, P) > rp.cosmax) first = a;
+	}
+#pragma unroll 1
+	for(int b = 0; b < 4; b++) {
+		patch64(Rq, rp.base[b], P);
+		if(-scalar64(d, P) > rp.cosmax) qok = 1;
+	}
+	if(first >= 0 && qok) {
+		*pa = first;
+		return 1;
+	}
+	return 0;
+}
+
+struct AvbShared {
+	double pr[3], pR[9];   /* the probe of the next scan */
+	double nr[3], nR[9];   /* the moving particle's candidate state */
+	int nb, ov, nbp[4];    /* scan results: bonds, overlap, partners by the probe's patch */
+	int rec, p, nn, skip, nb_old, in;
+};
+
+/* the 27 cells around S.pr (the reference's MC_energy walk, MC.c:272-309): the probe (S.pr, S.pR) against
+ * every particle there but slot offset `self`; thread t < 27 walks cell t. Every thread of the CTA calls
+ * it after S.nb, S.ov (and S.nbp) were cleared. */
+__device__ void avb_scan(const ppi_dev &d, const ppi_rparams &rp, const double *box, const int *ns, AvbShared &S, int self, bool partners) {
+	const int t = threadIdx.x;
+	if(t < 27) {
+		int idx[3];
+		avb_cell_of(S.pr, box, ns, idx);
+		const int cx = (idx[0] + t % 3 - 1 + ns[0]) % ns[0], cy = (idx[1] + (t / 3) % 3 - 1 + ns[1]) % ns[1], cz = (idx[2] + t / 9 - 1 + ns[2]) % ns[2];
+		int q = d.avb_head[rp.avb_head0 + (cx * ns[1] + cy) * ns[2] + cz];
+		for(int guard = 0; q != -1 && guard < rp.N; guard++) {
+			if(q != self) {
+				const double *qrec = d.rec + (size_t) (rp.p0 + q) * PPI_REC;
+				int pa = 0;
+				const int res = avb_pair(S.pr, S.pR, qrec, qrec, nullptr, rp, box, &pa);
+				if(res == -1) S.ov = 1;
+				else if(res == 1) {
+					atomicAdd(&S.nb, 1);
+					if(partners) S.nbp[pa] = q;
+				}
+			}
+			q = d.avb_next[rp.p0 + q];
+		}
+	}
+	__syncthreads();
+}
+
+/* random_vector_on_sphere (utils.c:115-131), Marsaglia (1972); false when the draws ran out */
+__device__ bool avb_sphere(AvbRng &g, double *res) {
+	for(int k = 0; k < 64; k++) {
+		const double r1 = 1. - 2. * g.next(), r2 = 1. - 2. * g.next(), sq = r1 * r1 + r2 * r2;
+		if(sq < 1.) {
+			const double h = 2. * sqrt(1. - sq);
+			res[0] = r1 * h;
+			res[1] = r2 * h;
+			res[2] = 1. - 2. * sq;
+			return true;
+		}
+	}
+	return false;
+}
+
+/* get_rotation_matrix (utils.c:186-202) */
+__device__ void avb_rot(const double *a, double t, double *m) {
+	double st, ct;
+	sincos(t, &st, &ct);
+	const double uct = 1. - ct;
+	m[0] = a[0] * a[0] + (1. - a[0] * a[0]) * ct;
+	m[1] = a[0] * a[1] * uct - a[2] * st;
+	m[2] = a[0] * a[2] * uct + a[1] * st;
+	m[3] = a[0] * a[1] * uct + a[2] * st;
+	m[4] = a[1] * a[1] + (1. - a[1] * a[1]) * ct;
+	m[5] = a[1] * a[2] * uct - a[0] * st;
+	m[6] = a[0] * a[2] * uct - a[1] * st;
+	m[7] = a[1] * a[2] * uct + a[0] * st;
+	m[8] = a[2] * a[2] + (1. - a[2] * a[2]) * ct;
+}
+
+__device__ void avb_matvec(const double *m, const double *v, double *o) {
+	for(int i = 0; i < 3; i++) o[i] = m[3 * i] * v[0] + m[3 * i + 1] * v[1] + m[3 * i + 2] * v[2];
+}
+
+__device__ void avb_matmul(const double *m, const double *n, double *o) {
+	for(int i = 0; i < 3; i++)
+		for(int j = 0; j < 3; j++) o[3 * i + j] = m[3 * i] * n[j] + m[3 * i + 1] * n[3 + j] + m[3 * i + 2] * n[6 + j];
+}
+
+__device__ void avb_normalize(double *v) {
+	const double n = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+	v[0] /= n;
+	v[1] /= n;
+	v[2] /= n;
+}
+
+/* gram_schmidt (utils.c:91-113) */
+__device__ void avb_gram_schmidt(double *v1, double *v2, double *v3) {
+	const double n1 = v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2];
+	double b1 = (v2[0] * v1[0] + v2[1] * v1[1] + v2[2] * v1[2]) / n1;
+	for(int k = 0; k < 3; k++) v2[k] -= b1 * v1[k];
+	const double n2 = v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2];
+	b1 = (v3[0] * v1[0] + v3[1] * v1[1] + v3[2] * v1[2]) / n1;
+	const double b2 = (v3[0] * v2[0] + v3[1] * v2[1] + v3[2] * v2[2]) / n2;
+	for(int k = 0; k < 3; k++) v3[k] -= b1 * v1[k] + b2 * v2[k];
+	avb_normalize(v1);
+	avb_normalize(v2);
+	avb_normalize(v3);
+}
+
+__device__ double avb_det(const double *m) {
+	return m[0] * m[4] * m[8] + m[1] * m[5] * m[6] + m[2] * m[3] * m[7] - m[2] * m[4] * m[6] - m[0] * m[5] * m[7] - m[1] * m[3] * m[8];
+}
+
+/* set_orientation_around_vector (utils.c:225-270): orient = B . orient, B's third column -v turned by t
+ * about a random axis perpendicular to v */
+__device__ bool avb_orient_around(AvbRng &g, const double *v, double *orient, double t) {
+	double y_tmp[3] = { -v[0], -v[1], -v[2] }, z[3], w_tmp[3];
+	if(!avb_sphere(g, z) || !avb_sphere(g, w_tmp)) return false;
+	avb_gram_schmidt(y_tmp, z, w_tmp);
+	double m[9], y[3], w[3];
+	avb_rot(z, t, m);
+	avb_matvec(m, y_tmp, y);
+	avb_matvec(m, w_tmp, w);
+	double B[9] = { z[0], w[0], y[0], z[1], w[1], y[1], z[2], w[2], y[2] };
+	if(avb_det(B) < 0.)
+		for(int i = 0; i < 3; i++) {
+			B[3 * i] = w[i];
+			B[3 * i + 1] = z[i];
+		}
+	double old[9];
+	for(int k = 0; k < 9; k++) old[k] = orient[k];
+	avb_matmul(B, old, orient);
+	return true;
+}
+
+/* place_inside_vbonding (utils.c:52-76): position nr and orientation nR inside the bonding volume of patch
+ * tp of the particle at (rr, rR) */
+__device__ bool avb_place_inside(const ppi_rparams &rp, AvbRng &g, const double *rr, const double *rR, int tp, double *nr, double *nR) {
+	double m[9];
+	avb_rot(rp.base[0], 2. * g.next() * 3.141592653589793, m);
+	avb_matmul(rp.base_orient, m, nR);
+	double dir[3], nv[3];
+	patch64(rR, rp.base[tp], dir);
+	if(!avb_sphere(g, nv)) return false; /* get_perpendicular_versor (utils.c:38-50) */
+	const double vv = dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2], rv = nv[0] * dir[0] + nv[1] * dir[1] + nv[2] * dir[2];
+	for(int k = 0; k < 3; k++) nv[k] -= rv / vv * dir[k];
+	avb_normalize(nv);
+	const double theta = acos(rp.cosmax + (1. - rp.cosmax) * g.next());
+	avb_rot(nv, theta, m);
+	double tmp[3];
+	avb_matvec(m, dir, tmp);
+	for(int k = 0; k < 3; k++) dir[k] = tmp[k];
+	avb_normalize(dir);
+	const double theta2 = acos(rp.cosmax + (1. - rp.cosmax) * g.next());
+	if(!avb_orient_around(g, dir, nR, theta2)) return false;
+	const double dl = rp.r_cut - 1.;
+	const double dist = pow(1. + g.next() * (dl * dl * dl + 3. * dl * dl + 3. * dl), 1. / 3.);
+	for(int k = 0; k < 3; k++) nr[k] = dir[k] * dist + rr[k];
+	return true;
+}
+
+__global__ void __launch_bounds__(AVB_B) k_avb(ppi_dev d, long long step, int steps) {
+	const int r = blockIdx.x, tid = threadIdx.x;
+	const ppi_rparams &rp = d.rp[r];
+	ppi_rstate *rs = d.rs + r;
+	if(rp.dynamics != 2) return;
+	const int N = rp.N, p0 = rp.p0;
+	const int attempts = rp.avb_per_step * steps;
+	if(N < 2 || attempts <= 0) return;
+	__shared__ AvbShared S;
+	const double box[3] = { rs->box[0], rs->box[1], rs->box[2] };
+	int ns[3];
+	for(int a = 0; a < 3; a++) {
+		int n = (int) floor(box[a] / rp.r_cut); /* cells_init (cells.c:17-37) */
+		n = n < rp.avb_ncap[a] ? n : rp.avb_ncap[a];
+		ns[a] = n < 3 ? 3 : n;
+	}
+	const int ncell = ns[0] * ns[1] * ns[2];
+	/* linked cells of the live particles (cells_fill, cells.c:51-63); the order inside a cell does not
+	 * change any outcome: bonds and overlaps are counted, and each patch bonds at most one partner */
+	for(int c = tid; c < ncell; c += AVB_B) d.avb_head[rp.avb_head0 + c] = -1;
+	__syncthreads();
+	for(int i = tid; i < N; i += AVB_B) {
+		int idx[3];
+		const int c = avb_cell_of(d.rec + (size_t) (p0 + i) * PPI_REC, box, ns, idx);
+		d.avb_cell[p0 + i] = c;
+		d.avb_next[p0 + i] = atomicExch(&d.avb_head[rp.avb_head0 + c], i);
+	}
+	__syncthreads();
+	AvbRng g;
+	for(int a = 0; a < attempts; a++) {
+		if(tid == 0) {
+			g.rp = &rp;
+			g.step = step;
+			g.r = r;
+			g.item = (uint32_t) a;
+			g.sub = 0u;
+			g.k = 0;
+			int rec = (int) (g.next() * N);
+			S.rec = rec < N ? rec : N - 1;
+			const double *q = d.rec + (size_t) (p0 + S.rec) * PPI_REC;
+			for(int k = 0; k < 3; k++) S.pr[k] = q[k];
+			orient64(q + PPI_R0, q + PPI_Q, S.pR);
+			S.nb = S.ov = 0;
+			for(int k = 0; k < 4; k++) S.nbp[k] = -1;
+			rs->tries[1]++; /* AVB (defs.h:13) */
+		}
+		__syncthreads();
+		avb_scan(d, rp, box, ns, S, S.rec, true); /* _set_neighbours of the receiver */
+		if(tid == 0) {
+			S.nn = S.nb;
+			S.skip = 0;
+			const double rr[3] = { S.pr[0], S.pr[1], S.pr[2] };
+			double rR[9];
+			for(int k = 0; k < 9; k++) rR[k] = S.pR[k];
+			S.in = g.next() > 0.5;
+			if(S.in) { /* into the receiver's bonding volume */
+				if(S.nn == N - 1) S.skip = 1;
+				else {
+					int p = -1;
+					for(int k = 0; k < AVB_DRAWS && p < 0; k++) {
+						int c = (int) (g.next() * N);
+						c = c < N ? c : N - 1;
+						if(c != S.rec && c != S.nbp[0] && c != S.nbp[1] && c != S.nbp[2] && c != S.nbp[3]) p = c;
+					}
+					int tp = (int) (g.next() * 4);
+					tp = tp < 4 ? tp : 3;
+					if(p < 0 || !avb_place_inside(rp, g, rr, rR, tp, S.nr, S.nR)) {
+						rs->error = PPI_E_AVB;
+						S.skip = 2;
+					}
+					S.p = p;
+				}
+			}
+			else { /* a partner out of it */
+				if(S.nn == 0) S.skip = 1;
+				else {
+					int k = (int) (g.next() * S.nn), cn = 0, ci = 0;
+					while(cn <= k && ci < 4) {
+						if(S.nbp[ci] != -1) cn++;
+						ci++;
+					}
+					S.p = S.nbp[ci - 1];
+					if(S.p < 0) S.skip = 1; /* only if two partners shared a patch, which overlaps forbid */
+					int tries = 0, pa = 0;
+					for(; tries < AVB_DRAWS; tries++) {
+						for(int c = 0; c < 3; c++) S.nr[c] = g.next() * box[c];
+						const double u1 = g.next(), u2 = g.next(), u3 = g.next();
+						uniform_rotation64(u1, u2, u3, S.nR);
+						if(avb_pair(rr, rR, S.nr, nullptr, S.nR, rp, box, &pa) != 1) break;
+					}
+					if(tries == AVB_DRAWS) {
+						rs->error = PPI_E_AVB;
+						S.skip = 2;
+					}
+				}
+			}
+			if(!S.skip) {
+				/* the mover's current state is the next probe; its candidate position is r + (new_r - r)
+				 * (MC_rototraslate_particle, MC.c:208-230) */
+				const double *q = d.rec + (size_t) (p0 + S.p) * PPI_REC;
+				for(int k = 0; k < 3; k++) {
+					S.pr[k] = q[k];
+					S.nr[k] = __dadd_rn(q[k], __dsub_rn(S.nr[k], q[k]));
+				}
+				orient64(q + PPI_R0, q + PPI_Q, S.pR);
+			}
+			S.nb = S.ov = 0;
+		}
+		__syncthreads();
+		if(S.skip == 2) break;
+		if(S.skip) continue;
+		avb_scan(d, rp, box, ns, S, S.p, false); /* the mover's energy now */
+		if(tid == 0) {
+			S.nb_old = S.nb;
+			for(int k = 0; k < 3; k++) S.pr[k] = S.nr[k];
+			for(int k = 0; k < 9; k++) S.pR[k] = S.nR[k];
+			S.nb = S.ov = 0;
+		}
+		__syncthreads();
+		avb_scan(d, rp, box, ns, S, S.p, false); /* and at the candidate state */
+		if(tid == 0) {
+			const int n = S.nn;
+			const double dE = -(double) (S.nb - S.nb_old);
+			/* avb.c:116 (in) and avb.c:173 (out) */
+			const double ratio = S.in ? (N - n - 1.) * rp.avb_vin / ((n + 1.) * rp.avb_vout) : (double) n * rp.avb_vout / ((N - n) * rp.avb_vin);
+			if(!S.ov && g.next() < exp(-dE / rp.T) * ratio) {
+				double *q = d.rec + (size_t) (p0 + S.p) * PPI_REC;
+				for(int k = 0; k < 3; k++) q[k] = S.nr[k];
+				q[PPI_Q] = 1.0;
+				q[PPI_Q + 1] = q[PPI_Q + 2] = q[PPI_Q + 3] = 0.0;
+				for(int k = 0; k < 9; k++) q[PPI_R0 + k] = S.nR[k];
+				/* MC_change_cell (MC.c:180-206) on the batch's linked cells */
+				int idx[3];
+				const int c_new = avb_cell_of(S.nr, box, ns, idx), c_old = d.avb_cell[p0 + S.p];
+				if(c_new != c_old) {
+					int *h = d.avb_head + rp.avb_head0;
+					if(h[c_old] == S.p) h[c_old] = d.avb_next[p0 + S.p];
+					else {
+						int w = h[c_old];
+						for(int guard = 0; w != -1 && d.avb_next[p0 + w] != S.p && guard < N; guard++) w = d.avb_next[p0 + w];
+						if(w != -1) d.avb_next[p0 + w] = d.avb_next[p0 + S.p];
+					}
+					d.avb_next[p0 + S.p] = h[c_new];
+					h[c_new] = S.p;
+					d.avb_cell[p0 + S.p] = c_new;
+				}
+				rs->bonds += S.nb - S.nb_old;
+				rs->accepted[1]++;
+			}
+		}
+		__syncthreads();
+	}
+}
+
+/* ------------------------------------------------------------------------------------------------ */
 /* launchers                                                                                        */
 /* ------------------------------------------------------------------------------------------------ */
 static int g_sms = 0;
+
+extern "C" int ppi_avb(const ppi_dev *d, long long step, int steps, cudaStream_t s, long long *nl) {
+	k_avb<<<d->nrep, AVB_B, 0, s>>>(*d, step, steps);
+	if(nl) *nl += 1;
+	return (int) cudaGetLastError();
+}
 
 extern "C" int ppi_sm_count(void) {
 	if(g_sms == 0) {
