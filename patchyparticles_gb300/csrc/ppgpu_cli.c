@@ -1,5 +1,5 @@
 /*
- * ppgpu_cli.c -- command-line driver: runs a PatchyParticles input file (Dynamics = 0, Ensemble 0, 1, 3 or 5)
+ * ppgpu_cli.c -- command-line driver: runs a PatchyParticles input file (Dynamics 0 or 2, Ensemble 0, 1, 3 or 5)
  * on the GB300 engine through the public C-ABI (include/ppgpu.h) and writes the reference's output files.
  *
  *   ppgpu input_file
@@ -115,7 +115,7 @@ static FILE *open_or_die(const char *name, const char *mode) {
 
 typedef struct {
 	pp_engine *e;
-	int N, ensemble, lx;
+	int N, ensemble, lx, avb;
 	double *r, *R, box[3]; /* room for the largest particle count the ensemble allows */
 	const char *sus_folder; /* SUS: sus-<step>.dat into this folder (output.c:343-356) */
 	int n_min, n_max;
@@ -181,6 +181,7 @@ static void print_step(run_t *s, long long step) {
 		fflush(s->boxshape);
 	}
 	fprintf(s->acc, "%lld %e", step, c.accepted[PP_MOVE_ROTO_TRASL] / (double) c.tries[PP_MOVE_ROTO_TRASL]);
+	if(s->avb) fprintf(s->acc, " %e", c.accepted[PP_MOVE_AVB] / (double) c.tries[PP_MOVE_AVB]); /* output.c:156-158 */
 	if(s->ensemble == PP_GC || s->ensemble == PP_SUS) {
 		fprintf(s->acc, " %e", c.accepted[PP_MOVE_ADD] / (double) c.tries[PP_MOVE_ADD]);
 		fprintf(s->acc, " %e", c.accepted[PP_MOVE_REMOVE] / (double) c.tries[PP_MOVE_REMOVE]);
@@ -230,12 +231,18 @@ int main(int argc, char *argv[]) {
 			die("Cannot create files in directory '%s': please make sure that the directory exists and it is writable", s.bonds_folder);
 	}
 
-	/* system_init (system.c:58-252), Dynamics = 0, NVT or NPT */
+	/* system_init (system.c:58-252) and MC_init (MC.c:85-131) */
 	pp_params p;
 	pp_default_params(&p);
 	const int dynamics = (int) key_ll(in, "Dynamics", 1, 0);
 	s.ensemble = p.ensemble = (int) key_ll(in, "Ensemble", 1, 0);
-	if(dynamics != 0) die("Dynamics = %d is not run by this engine (only Dynamics = 0, roto-translation)", dynamics);
+	if(dynamics != PP_RTMC && dynamics != PP_AVBMC)
+		die("Dynamics = %d is not run by this engine (0 roto-translations, 2 AVB moves and roto-translations)", dynamics);
+	p.dynamics = dynamics;
+	if(dynamics == PP_AVBMC) { /* AVBMC_init (avb.c:13-36): the optional avb_p */
+		s.avb = 1;
+		p.avb_p = key_d(in, "avb_p", 0, 0.5);
+	}
 	if(s.ensemble != PP_NVT && s.ensemble != PP_NPT && s.ensemble != PP_GC && s.ensemble != PP_SUS)
 		die("Ensemble = %d is not run by this engine (0 NVT, 1 GC, 3 SUS, 5 NPT)", s.ensemble);
 	if(s.ensemble != PP_NVT) s.density = open_or_die((v = key(in, "Density_file", 0)) ? v : "density.dat", mode);

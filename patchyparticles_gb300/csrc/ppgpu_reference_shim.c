@@ -6,11 +6,14 @@
  * print/save synchronisation points of the main loop (main.c:82-104) and MC_check_energy (MC.c:766-784).
  */
 #include "defs.h"
+#include "avb.h"
 #include "cells.h"
 #include "output.h"
 #include "utils.h"
 #include "ppgpu.h"        /* from this repository's include/ */
 #include <stdlib.h>
+
+extern avbmc *avbdata; /* avb.c:11, set by AVBMC_init (MC_init runs before gpu_ensemble_init) */
 
 static pp_engine *G = NULL;
 
@@ -31,6 +34,8 @@ int gpu_ensemble_init(System *syst, Output *IO, int seed) {
 	p.lyz_min = syst->Lyz_min;
 	p.lyz_max = syst->Lyz_max;
 	p.seed = (uint64_t) seed;
+	p.dynamics = syst->dynamics; /* 0, or 2: AVB moves mixed with the roto-translations (avb.c:77-186) */
+	if(syst->dynamics == AVBMC) p.avb_p = avbdata->avb_p;
 	if(syst->ensemble == GC || syst->ensemble == SUS) { /* system.c:90-103 */
 		p.activity = syst->z;
 		p.n_min = syst->N_min;

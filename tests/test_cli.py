@@ -41,7 +41,9 @@ def _lines(path):
                                         ("small_npt", ("energy.dat", "acceptance.dat", "density.dat")),
                                         ("small_lx", ("energy.dat", "acceptance.dat", "boxshape.dat")),
                                         ("small_gc", ("energy.dat", "acceptance.dat", "density.dat")),
-                                        ("small_sus", ("energy.dat", "acceptance.dat", "density.dat"))])
+                                        ("small_sus", ("energy.dat", "acceptance.dat", "density.dat")),
+                                        ("small_avb", ("energy.dat", "acceptance.dat")),
+                                        ("small_avb_npt", ("energy.dat", "acceptance.dat", "density.dat"))])
 def test_driver_writes_the_reference_outputs(built, name, files):
     src, work = _prepare(name)
     p = subprocess.run([CLI, "input"], cwd=work, capture_output=True, text=True, timeout=300)
