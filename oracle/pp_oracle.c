@@ -46,6 +46,19 @@ struct orc_system {
 	int avb_status;
 	int avb_nb[4]; /* neighbours[patch of the receiver]: bonded particle, or -1 (avb.c:43-75) */
 	int avb_nn;    /* num_neighbours */
+	/* VMMC state (vmmc.h: vmmc_d) */
+	int *vm_links;   /* possible_links: pairs (lower index, higher index), capacity 16 cap */
+	int vm_nlinks;
+	int *vm_counter; /* possible_links_counter */
+	int *vm_copies;  /* copies */
+	int *vm_in;      /* is_in_cluster */
+	int *vm_clust, vm_nclust;
+	int *vm_pre, vm_npre;   /* prelinked_particles */
+	int *vm_fail, vm_nfail; /* outright_failed */
+	int vm_rot;             /* which_move: 1 rotation, 0 translation */
+	double vm_R[9];         /* the move's rotation */
+	double vm_move[3];      /* the move's translation */
+	int vm_error;
 };
 
 /* ---------------------------------------------------------------- drand48 (POSIX recurrence) */
@@ -691,9 +704,274 @@ static void o_avb_dynamics(orc_system *s) {
 	}
 }
 
+/* ---------------------------------------------------------------- VMMC (vmmc.c) */
+/* _store_dof / _restore_dof (vmmc.c:58-79) */
+static void o_store_dof(orc_system *s, int p) {
+	memcpy(s->r_old + 3 * p, s->r + 3 * p, 3 * sizeof(double));
+	memcpy(s->R_old + 9 * p, s->R + 9 * p, 9 * sizeof(double));
+}
+
+static void o_restore_dof(orc_system *s, int p) {
+	memcpy(s->r + 3 * p, s->r_old + 3 * p, 3 * sizeof(double));
+	memcpy(s->R + 9 * p, s->R_old + 9 * p, 9 * sizeof(double));
+	o_set_patches(s, p);
+}
+
+/* _pair_energy (vmmc.c:81-95) */
+static double o_pair_energy(orc_system *s, int p, int q) {
+	int val = orc_interact(s, p, q);
+	if(val == ORC_PATCH_BOND) return -1.;
+	if(val == ORC_OVERLAP) s->overlap = 1;
+	return 0.;
+}
+
+/* _compute_cluster_energy (vmmc.c:107-137): the cluster's bonds to particles outside it */
+static double o_cluster_energy(orc_system *s) {
+	double res = 0.;
+	for(int i = 0; i < s->vm_nclust; i++) {
+		int p = s->vm_clust[i];
+		int ind[3];
+		o_cell_index(s, s->r + 3 * p, ind);
+		for(int j = -1; j < 2; j++) {
+			int cx = (ind[0] + j + s->nside[0]) % s->nside[0];
+			for(int k = -1; k < 2; k++) {
+				int cy = (ind[1] + k + s->nside[1]) % s->nside[1];
+				for(int l = -1; l < 2; l++) {
+					int cz = (ind[2] + l + s->nside[2]) % s->nside[2];
+					int q = s->head[(cx * s->nside[1] + cy) * s->nside[2] + cz];
+					while(q != -1) {
+						if(s->vm_in[q] == 0) res += o_pair_energy(s, p, q);
+						q = s->next[q];
+					}
+				}
+			}
+		}
+	}
+	return res;
+}
+
+/* _move_particle (vmmc.c:231-256): the translation, or the rotation about the seed */
+static void o_vmmc_move(orc_system *s, int p) {
+	double *r = s->r + 3 * p;
+	if(!s->vm_rot) {
+		r[0] += s->vm_move[0];
+		r[1] += s->vm_move[1];
+		r[2] += s->vm_move[2];
+		return;
+	}
+	const double *seed = s->r + 3 * s->vm_clust[0];
+	double dr_tmp[3] = { r[0] - seed[0], r[1] - seed[1], r[2] - seed[2] }, dr[3];
+	o_matvec(s->vm_R, dr_tmp, dr);
+	r[0] = seed[0] + dr[0];
+	r[1] = seed[1] + dr[1];
+	r[2] = seed[2] + dr[2];
+	o_matmul(s->vm_R, s->R_old + 9 * p, s->R + 9 * p);
+	o_set_patches(s, p);
+}
+
+/* _populate_possible_links (vmmc.c:148-229): the links p can form at its current (real or virtual)
+ * position, each partner taken at its image closest to p's real position */
+static void o_populate_links(orc_system *s, int p, int *force_reject) {
+	int ind[3];
+	o_cell_index(s, s->r + 3 * p, ind);
+	const double *rp = s->r + 3 * p, *rpo = s->r_old + 3 * p;
+	for(int j = -1; j < 2; j++) {
+		int cx = (ind[0] + j + s->nside[0]) % s->nside[0];
+		for(int k = -1; k < 2; k++) {
+			int cy = (ind[1] + k + s->nside[1]) % s->nside[1];
+			for(int l = -1; l < 2; l++) {
+				int cz = (ind[2] + l + s->nside[2]) % s->nside[2];
+				int q = s->head[(cx * s->nside[1] + cy) * s->nside[2] + cz];
+				while(q != -1) {
+					if(q != p) {
+						double *rq = s->r + 3 * q;
+						double dist[3] = { rq[0] - rp[0], rq[1] - rp[1], rq[2] - rp[2] };
+						dist[0] -= s->box[0] * rint(dist[0] / s->box[0]);
+						dist[1] -= s->box[1] * rint(dist[1] / s->box[1]);
+						dist[2] -= s->box[2] * rint(dist[2] / s->box[2]);
+						double dist2 = O_SCALAR(dist, dist);
+						if(dist2 < s->kf_sqr_rcut) {
+							if(s->vm_nlinks >= 16 * s->cap) { /* output_exit "VMMC: memory exhausted" */
+								s->vm_error = 1;
+								*force_reject = 1;
+								return;
+							}
+							/* normalized_diff_vector (vmmc.c:139-146) from p's real position */
+							dist[0] = rq[0] - rpo[0];
+							dist[1] = rq[1] - rpo[1];
+							dist[2] = rq[2] - rpo[2];
+							dist[0] -= s->box[0] * rint(dist[0] / s->box[0]);
+							dist[1] -= s->box[1] * rint(dist[1] / s->box[1]);
+							dist[2] -= s->box[2] * rint(dist[2] / s->box[2]);
+							double new_pos[3] = { rpo[0] + dist[0], rpo[1] + dist[1], rpo[2] + dist[2] };
+							if(s->vm_copies[q] == 1 || s->vm_in[q] == 1) {
+								if(fabs(new_pos[0] - rq[0]) > 1e-6 || fabs(new_pos[1] - rq[1]) > 1e-6 || fabs(new_pos[2] - rq[2]) > 1e-6) {
+									*force_reject = 1;
+									return;
+								}
+							}
+							if(s->vm_copies[q] == 0 && s->vm_in[q] == 0) {
+								rq[0] = new_pos[0];
+								rq[1] = new_pos[1];
+								rq[2] = new_pos[2];
+								s->vm_copies[q] = 1;
+							}
+							int n = s->vm_nlinks;
+							s->vm_links[2 * n] = p < q ? p : q;
+							s->vm_links[2 * n + 1] = p < q ? q : p;
+							s->vm_nlinks++;
+							s->vm_counter[p]++;
+							s->vm_counter[q]++;
+							/* a link already listed is dropped again (_mycomp, vmmc.c:97-105) */
+							for(int m = 0; m < s->vm_nlinks - 1; m++) {
+								if(s->vm_links[2 * m] == s->vm_links[2 * n] && s->vm_links[2 * m + 1] == s->vm_links[2 * n + 1]) {
+									s->vm_nlinks--;
+									s->vm_counter[p]--;
+									s->vm_counter[q]--;
+									if(s->vm_counter[p] == 0) s->vm_copies[p] = 0;
+									if(s->vm_counter[q] == 0) s->vm_copies[q] = 0;
+									break;
+								}
+							}
+						}
+					}
+					q = s->next[q];
+				}
+			}
+		}
+	}
+}
+
+/* drops link k (the last one takes its place) and releases its particles' copies (vmmc.c:310-318, 386-397) */
+static void o_drop_link(orc_system *s, int k, int p, int q) {
+	s->vm_links[2 * k] = s->vm_links[2 * (s->vm_nlinks - 1)];
+	s->vm_links[2 * k + 1] = s->vm_links[2 * (s->vm_nlinks - 1) + 1];
+	s->vm_nlinks--;
+	s->vm_counter[p]--;
+	s->vm_counter[q]--;
+	if(s->vm_counter[p] == 0) s->vm_copies[p] = 0;
+	if(s->vm_counter[q] == 0) s->vm_copies[q] = 0;
+}
+
+/* VMMC_dynamics (vmmc.c:258-483) */
+static void o_vmmc_dynamics(orc_system *s) {
+	s->tries[ORC_MOVE_VMMC]++;
+	int force_reject = 0;
+	s->vm_nclust = 1;
+	s->vm_nfail = 0;
+	s->vm_nlinks = 0;
+	s->vm_npre = 0;
+	int seed = (int) (orc_drand(s) * s->N);
+	s->vm_in[seed] = 1;
+	s->vm_clust[0] = seed;
+	if(orc_drand(s) < 0.5) {
+		s->vm_rot = 0;
+		s->vm_move[0] = (orc_drand(s) - 0.5) * s->prm.disp_max;
+		s->vm_move[1] = (orc_drand(s) - 0.5) * s->prm.disp_max;
+		s->vm_move[2] = (orc_drand(s) - 0.5) * s->prm.disp_max;
+	}
+	else {
+		s->vm_rot = 1;
+		o_random_vector_on_sphere(s, s->vm_move);
+		double angle = orc_drand(s) * s->prm.theta_max;
+		o_rotation_matrix(s->vm_move, angle, s->vm_R);
+	}
+	o_store_dof(s, seed);
+	o_populate_links(s, seed, &force_reject);
+	if(!force_reject) {
+		o_vmmc_move(s, seed);
+		o_populate_links(s, seed, &force_reject);
+		o_restore_dof(s, seed);
+	}
+	while(s->vm_nlinks > 0 && s->vm_nclust < s->prm.vmmc_max_cluster && !force_reject) {
+		int k = (int) (orc_drand(s) * s->vm_nlinks);
+		int p = s->vm_links[2 * k], q = s->vm_links[2 * k + 1];
+		if(s->vm_in[p] == 1 && s->vm_in[q] == 1) {
+			o_drop_link(s, k, p, q);
+			continue;
+		}
+		if(s->vm_in[p] == 0) {
+			int t = q;
+			q = p;
+			p = t;
+		}
+		double E_old = o_pair_energy(s, p, q);
+		o_store_dof(s, p);
+		o_vmmc_move(s, p);
+		double E_p_moved = o_pair_energy(s, p, q);
+		o_restore_dof(s, p);
+		int force_prelink = s->overlap;
+		s->overlap = 0;
+		double p1 = 1. - exp((1. / s->prm.T) * (E_old - E_p_moved));
+		if(force_prelink == 1 || p1 > orc_drand(s)) {
+			o_store_dof(s, q);
+			o_vmmc_move(s, q);
+			double E_q_moved = o_pair_energy(s, p, q);
+			o_restore_dof(s, q);
+			int force_link = s->overlap;
+			s->overlap = 0;
+			double p2 = 1. - exp((1. / s->prm.T) * (E_old - E_q_moved));
+			if(p2 > 1.) p2 = 1.;
+			if(force_link == 1 || (p2 / p1) > orc_drand(s)) {
+				s->vm_copies[q] = 0;
+				s->vm_in[q] = 1;
+				s->vm_clust[s->vm_nclust++] = q;
+				o_store_dof(s, q);
+				o_populate_links(s, q, &force_reject);
+				if(force_reject) break;
+				o_vmmc_move(s, q);
+				o_populate_links(s, q, &force_reject);
+				o_restore_dof(s, q);
+				if(force_reject) break;
+			}
+			else s->vm_pre[s->vm_npre++] = q;
+		}
+		else s->vm_fail[s->vm_nfail++] = q;
+		o_drop_link(s, k, p, q);
+	}
+	if(s->vm_nclust == s->prm.vmmc_max_cluster) force_reject = 1;
+	for(int i = 0; i < s->vm_npre; i++) {
+		int p = s->vm_pre[i];
+		if(s->vm_in[p] == 0) force_reject = 1;
+		else s->vm_copies[p] = 0;
+	}
+	double deltaE = 0.;
+	if(force_reject == 0) deltaE = -o_cluster_energy(s);
+	if(s->overlap) s->vm_error = 1; /* assert(syst->overlap == 0), vmmc.c:436 */
+	for(int i = 0; i < s->vm_nclust && !force_reject; i++) {
+		int p = s->vm_clust[i];
+		o_store_dof(s, p);
+		o_vmmc_move(s, p);
+		o_change_cell(s, p);
+	}
+	if(force_reject == 0) deltaE += o_cluster_energy(s);
+	if(s->overlap) s->vm_error = 1; /* vmmc.c:446 */
+	if(force_reject == 1)
+		for(int i = 0; i < s->vm_nclust; i++) o_restore_dof(s, s->vm_clust[i]);
+	if(force_reject == 0) {
+		s->accepted[ORC_MOVE_VMMC]++;
+		s->energy += deltaE;
+	}
+	for(int i = 0; i < s->vm_nclust; i++) {
+		int p = s->vm_clust[i];
+		o_change_cell(s, p);
+		s->vm_in[p] = 0;
+	}
+	for(int i = 0; i < s->vm_nfail; i++) s->vm_copies[s->vm_fail[i]] = 0;
+	s->vm_nfail = 0;
+	for(int i = 0; i < s->vm_nlinks; i++) {
+		int p = s->vm_links[2 * i], q = s->vm_links[2 * i + 1];
+		s->vm_copies[p] = s->vm_copies[q] = 0;
+		s->vm_counter[p] = s->vm_counter[q] = 0;
+	}
+}
+
+int orc_vmmc_error(const orc_system *s) { return s->vm_error; }
+
 /* syst->do_dynamics (MC_init, MC.c:115-130) */
 static void o_dynamics(orc_system *s) {
 	if(s->prm.dynamics == ORC_AVBMC) o_avb_dynamics(s);
+	else if(s->prm.dynamics == ORC_VMMC) o_vmmc_dynamics(s);
 	else o_move_rototranslate(s);
 }
 
@@ -868,11 +1146,12 @@ static void o_attempt(orc_system *s) {
 
 void orc_sweep(orc_system *s) {
 	if(s->prm.dynamics == ORC_AVBMC && s->avb_status != 0) return; /* AVBMC_init refused the geometry */
+	if(s->vm_error) return;
 	if(s->prm.ensemble == ORC_GC || s->prm.ensemble == ORC_SUS) {
 		for(int i = 0; i < s->prm.n_max && !s->error; i++) o_attempt_gc(s);
 		return;
 	}
-	for(int i = 0; i < s->N; i++) o_attempt(s);
+	for(int i = 0; i < s->N && !s->vm_error; i++) o_attempt(s);
 }
 
 int orc_error(const orc_system *s) { return s->error; }
@@ -933,6 +1212,19 @@ static orc_system *o_alloc(int N, const orc_params *prm) {
 	s->next = malloc(n * sizeof(int));
 	s->cell = malloc(n * sizeof(int));
 	s->cell_old = malloc(n * sizeof(int));
+	if(prm->dynamics == ORC_VMMC) { /* VMMC_init (vmmc.c:15-45) */
+		s->vm_links = malloc(2 * 16 * n * sizeof(int));
+		s->vm_counter = calloc(n, sizeof(int));
+		s->vm_copies = calloc(n, sizeof(int));
+		s->vm_in = calloc(n, sizeof(int));
+		s->vm_clust = malloc(n * sizeof(int));
+		s->vm_pre = malloc(n * sizeof(int));
+		s->vm_fail = malloc(n * sizeof(int));
+		if(!s->vm_links || !s->vm_counter || !s->vm_copies || !s->vm_in || !s->vm_clust || !s->vm_pre || !s->vm_fail) {
+			orc_free(s);
+			return NULL;
+		}
+	}
 	if(!s->r || !s->r_old || !s->R || !s->R_old || !s->patch || !s->next || !s->cell || !s->cell_old) {
 		orc_free(s);
 		return NULL;
@@ -1059,6 +1351,13 @@ void orc_free(orc_system *s) {
 	free(s->next);
 	free(s->cell);
 	free(s->cell_old);
+	free(s->vm_links);
+	free(s->vm_counter);
+	free(s->vm_copies);
+	free(s->vm_in);
+	free(s->vm_clust);
+	free(s->vm_pre);
+	free(s->vm_fail);
 	free(s);
 }
 

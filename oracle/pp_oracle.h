@@ -31,6 +31,7 @@ extern "C" {
 
 /* Dynamics (defs.h:27-29) */
 #define ORC_RTMC 0
+#define ORC_VMMC 1  /* virtual-move Monte Carlo cluster moves, vmmc.c:258-483 */
 #define ORC_AVBMC 2 /* aggregation-volume-bias moves mixed with roto-translations, avb.c:77-186 */
 
 /* move-type slots of the tries/accepted counters, as in defs.h:11-19 */
@@ -38,6 +39,7 @@ extern "C" {
 #define ORC_AVB 1    /* defs.h:13 */
 #define ORC_ADD 2    /* defs.h:14 */
 #define ORC_REMOVE 3 /* defs.h:15 */
+#define ORC_MOVE_VMMC 5 /* defs.h:17 */
 #define ORC_VOLUME 6
 #define ORC_LX 7 /* defs.h:19 */
 #define ORC_N_MOVES 8
@@ -59,6 +61,7 @@ typedef struct orc_params {
 	int n_min, n_max;          /* GC: 0 and GC_N_max; SUS: Umbrella_sampling_min / _max (system.c:92-103) */
 	int dynamics;              /* Dynamics: ORC_RTMC or ORC_AVBMC (system.c:63, MC.c:115-130) */
 	double avb_p;              /* avb_p: probability of a roto-translation in AVBMC (avb.c:33-35); <= 0 selects 0.5 */
+	int vmmc_max_cluster;      /* vmmc_max_cluster (vmmc.c:25): a cluster that reaches it is rejected */
 } orc_params;
 
 typedef struct orc_system orc_system;
@@ -104,6 +107,10 @@ int orc_save_rrr(const orc_system *s, long long step, const char *path);
  * r (N x 3), R (N x 9 rows) and the cubic box, unrounded (generated.rrr holds them printed with %lf /
  * %.12lf). Returns 0, or -1 for a density outside (0, 0.7] or no memory. */
 int orc_generate(int N, double density, int seed, double *r, double *R, double box[3]);
+
+/* VMMC: 1 once a move ran out of link memory ("VMMC: memory exhausted", vmmc.c:176) or moved a cluster
+ * into an overlap (the reference's assert, vmmc.c:436-446); the oracle then makes no further move */
+int orc_vmmc_error(const orc_system *s);
 
 /* 1 once a GC insertion found the system full (the reference stops there: "increase GC_N_max",
  * MC.c:346-348; the oracle makes no further move), else 0. */

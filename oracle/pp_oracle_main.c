@@ -165,8 +165,14 @@ int main(int argc, char *argv[]) {
 		fb = fopen("boxshape.dat", mode);
 		if(fb == NULL) die("boxshape.dat is not writable");
 	}
-	if((dynamics != ORC_RTMC && dynamics != ORC_AVBMC) || (ensemble != ORC_NVT && ensemble != ORC_NPT && ensemble != ORC_GC && ensemble != ORC_SUS))
-		die("only Dynamics = 0 or 2 with Ensemble 0, 1, 3 or 5 is restated");
+	if(dynamics == ORC_VMMC) { /* VMMC_init (vmmc.c:15-45): both keys are mandatory; vmmc_max_move is read, not used */
+		const double max_move = atof(get(in, "vmmc_max_move", 1));
+		prm.vmmc_max_cluster = atoi(get(in, "vmmc_max_cluster", 1));
+		fprintf(stderr, "Using VMMC dynamics with max_move = %lf, max_clust = %d\n", max_move, prm.vmmc_max_cluster); /* output_log_msg */
+	}
+	if((dynamics != ORC_RTMC && dynamics != ORC_AVBMC && dynamics != ORC_VMMC) ||
+			(ensemble != ORC_NVT && ensemble != ORC_NPT && ensemble != ORC_GC && ensemble != ORC_SUS))
+		die("only Dynamics = 0, 1 or 2 with Ensemble 0, 1, 3 or 5 is restated");
 	char err[512];
 	orc_system *s = orc_load_rrr(conf, &prm, err, sizeof(err));
 	if(s == NULL) die(err);
@@ -228,8 +234,10 @@ int main(int argc, char *argv[]) {
 			}
 			orc_counters(s, tries, acc);
 			fprintf(fa, "%lld", step);
-			fprintf(fa, " %e", acc[ORC_ROTO_TRASL] / (double) tries[ORC_ROTO_TRASL]);
-			if(dynamics == ORC_AVBMC) fprintf(fa, " %e", acc[ORC_AVB] / (double) tries[ORC_AVB]); /* output.c:156-158 */
+			/* output.c:149-162 */
+			if(dynamics == ORC_VMMC) fprintf(fa, " %e", acc[ORC_MOVE_VMMC] / (double) tries[ORC_MOVE_VMMC]);
+			else fprintf(fa, " %e", acc[ORC_ROTO_TRASL] / (double) tries[ORC_ROTO_TRASL]);
+			if(dynamics == ORC_AVBMC) fprintf(fa, " %e", acc[ORC_AVB] / (double) tries[ORC_AVB]);
 			if(ensemble == ORC_GC || ensemble == ORC_SUS) {
 				fprintf(fa, " %e", acc[ORC_ADD] / (double) tries[ORC_ADD]);
 				fprintf(fa, " %e", acc[ORC_REMOVE] / (double) tries[ORC_REMOVE]);
@@ -267,6 +275,7 @@ int main(int argc, char *argv[]) {
 			orc_save_rrr(s, step, last);
 		}
 		orc_sweep(s);
+		if(orc_vmmc_error(s)) die("VMMC: memory exhausted, or a cluster move into an overlap");
 		if(orc_error(s)) { /* MC_add_remove's output_exit */
 			fprintf(stderr, "The system contains the maximum number of particles set in the input file (%d), increase GC_N_max\n", prm.n_max);
 			exit(1);

@@ -22,6 +22,8 @@ NPT = 5
 RTMC = 0  # Dynamics (defs.h:27-29)
 AVBMC = 2
 AVB = 1  # tries / accepted slot of the AVB move (defs.h:13)
+VMMC = 1  # Dynamics = 1: virtual-move cluster moves
+MOVE_VMMC = 5  # its tries / accepted slot (defs.h:17)
 
 
 class OrcParams(ctypes.Structure):
@@ -44,6 +46,7 @@ class OrcParams(ctypes.Structure):
         ("n_max", ctypes.c_int),
         ("dynamics", ctypes.c_int),
         ("avb_p", ctypes.c_double),
+        ("vmmc_max_cluster", ctypes.c_int),
     ]
 
 
@@ -123,9 +126,9 @@ def _ip(a):
 
 
 def params(ensemble=NVT, T=0.12, P=0.0, disp_max=0.05, theta_max=0.1, rescale_factor_max=0.01, kf_delta=0.12, kf_cosmax=0.92, seed=1,
-           lx_move=0, lx_change_max=0.0, lyz_min=0.0, lyz_max=0.0, activity=0.0, n_min=0, n_max=0, dynamics=0, avb_p=0.5):
+           lx_move=0, lx_change_max=0.0, lyz_min=0.0, lyz_max=0.0, activity=0.0, n_min=0, n_max=0, dynamics=0, avb_p=0.5, vmmc_max_cluster=0):
     return OrcParams(ensemble, T, P, disp_max, theta_max, rescale_factor_max, kf_delta, kf_cosmax, seed, lx_move, lx_change_max, lyz_min, lyz_max,
-                     activity, n_min, n_max, dynamics, avb_p)
+                     activity, n_min, n_max, dynamics, avb_p, vmmc_max_cluster)
 
 
 class System:

@@ -75,6 +75,9 @@ TRAJ = [
     # default avb_p and NPT with avb_p = 0.3
     ("small_avb", "generator_300_0.3_4242.rrr", 0, 0.11, 300, 30, 21, "", 2),
     ("small_avb_npt", "generator_300_0.3_4242.rrr", 5, 0.11, 300, 30, 23, "P = 0.05\nrescale_factor_max = 0.01\navb_p = 0.3\n", 2),
+    # virtual-move cluster moves (Dynamics = 1, vmmc.c:258-483), NVT and NPT
+    ("small_vmmc", "generator_300_0.3_4242.rrr", 0, 0.11, 300, 30, 25, "vmmc_max_move = 0.5\nvmmc_max_cluster = 20\n", 1),
+    ("small_vmmc_npt", "generator_300_0.3_4242.rrr", 5, 0.11, 300, 30, 27, "P = 0.05\nrescale_factor_max = 0.01\nvmmc_max_move = 0.5\nvmmc_max_cluster = 10\n", 1),
 ]
 
 PROBE_INPUT = """Dynamics = 0

@@ -50,11 +50,11 @@ def test_known_answers(built):
         assert E == want and not ov
 
 
-@pytest.mark.parametrize("name", ["fcc_nvt", "bcc_npt", "small_nvt", "small_npt", "small_lx", "small_gc", "small_sus", "small_avb", "small_avb_npt"])
+@pytest.mark.parametrize("name", ["fcc_nvt", "bcc_npt", "small_nvt", "small_npt", "small_lx", "small_gc", "small_sus", "small_avb", "small_avb_npt", "small_vmmc", "small_vmmc_npt"])
 def test_oracle_trajectory_matches_reference(built, name):
     """The restated main loop reproduces the reference's output files line for line (NVT, NPT, the Lx
-    move, grand canonical insertions and removals, successive umbrella sampling with its histograms, and
-    the aggregation-volume-bias dynamics in NVT and NPT)."""
+    move, grand canonical insertions and removals, successive umbrella sampling with its histograms, the
+    aggregation-volume-bias dynamics and the virtual-move cluster dynamics in NVT and NPT)."""
     src = helpers.golden_path("traj_" + name)
     work = tempfile.mkdtemp(prefix="pptraj_")
     os.makedirs(os.path.join(work, "confs"))
