@@ -43,12 +43,14 @@ extern "C" {
 #define PP_NPT 5 /* Ensemble = 5 (defs.h:24) */
 
 #define PP_RTMC 0  /* Dynamics = 0: roto-translations (defs.h:27) */
+#define PP_VMMC 1  /* Dynamics = 1: virtual-move Monte Carlo cluster moves (defs.h:28) */
 #define PP_AVBMC 2 /* Dynamics = 2: aggregation-volume-bias moves and roto-translations (defs.h:29) */
 
 #define PP_MOVE_ROTO_TRASL 0 /* tries/accepted slots as System::tries/accepted (defs.h:11-19, 95-96) */
 #define PP_MOVE_AVB 1        /* aggregation-volume-bias moves (defs.h:13) */
 #define PP_MOVE_ADD 2        /* GC / SUS insertions (defs.h:14) */
 #define PP_MOVE_REMOVE 3     /* GC / SUS removals (defs.h:15) */
+#define PP_MOVE_VMMC 5 /* virtual-move cluster moves (defs.h:17) */
 #define PP_MOVE_VOLUME 6
 #define PP_MOVE_LX 7 /* the NVT box-shape move (defs.h:19) */
 #define PP_N_MOVES 8
@@ -88,6 +90,11 @@ typedef struct pp_params {
 	 * avb.c:14-17). */
 	int dynamics;
 	double avb_p; /* avb_p (avb.c:33-35): the share of roto-translations among the reference's attempts */
+	/* PP_VMMC (vmmc.c:258-483): every attempt is a virtual-move cluster move, N per MC step, one after the
+	 * other on the device (NVT and NPT). vmmc_max_cluster (vmmc.c:25): a cluster that reaches this size is
+	 * rejected; vmmc_max_move is the reference's vmmc_max_move key, which it reads and does not use. */
+	int vmmc_max_cluster;
+	double vmmc_max_move;
 } pp_params;
 
 typedef struct pp_counters {

@@ -29,6 +29,7 @@ GC = 1
 SUS = 3
 NPT = 5
 RTMC = 0  # Dynamics: roto-translations
+VMMC = 1  # Dynamics: virtual-move cluster moves
 AVBMC = 2  # Dynamics: aggregation-volume-bias moves and roto-translations
 PREC_FP32_GUARD = 0
 PREC_FP64 = 1
@@ -36,6 +37,7 @@ MOVE_ROTO_TRASL = 0
 MOVE_ADD = 2
 MOVE_REMOVE = 3
 MOVE_AVB = 1
+MOVE_VMMC = 5
 MOVE_VOLUME = 6
 MOVE_LX = 7
 N_MOVES = 8
@@ -65,6 +67,8 @@ class PPParams(ctypes.Structure):
         ("n_max", ctypes.c_int),
         ("dynamics", ctypes.c_int),
         ("avb_p", ctypes.c_double),
+        ("vmmc_max_cluster", ctypes.c_int),
+        ("vmmc_max_move", ctypes.c_double),
     ]
 
 

@@ -1,5 +1,5 @@
 /*
- * ppgpu_cli.c -- command-line driver: runs a PatchyParticles input file (Dynamics 0 or 2, Ensemble 0, 1, 3 or 5)
+ * ppgpu_cli.c -- command-line driver: runs a PatchyParticles input file (Dynamics 0, 1 or 2, Ensemble 0, 1, 3 or 5)
  * on the GB300 engine through the public C-ABI (include/ppgpu.h) and writes the reference's output files.
  *
  *   ppgpu input_file
@@ -115,7 +115,7 @@ static FILE *open_or_die(const char *name, const char *mode) {
 
 typedef struct {
 	pp_engine *e;
-	int N, ensemble, lx, avb;
+	int N, ensemble, lx, avb, vmmc;
 	double *r, *R, box[3]; /* room for the largest particle count the ensemble allows */
 	const char *sus_folder; /* SUS: sus-<step>.dat into this folder (output.c:343-356) */
 	int n_min, n_max;
@@ -180,8 +180,10 @@ static void print_step(run_t *s, long long step) {
 		fprintf(s->boxshape, "%lld %lf %lf %lf\n", step, s->box[0], s->box[1], s->box[2]);
 		fflush(s->boxshape);
 	}
-	fprintf(s->acc, "%lld %e", step, c.accepted[PP_MOVE_ROTO_TRASL] / (double) c.tries[PP_MOVE_ROTO_TRASL]);
-	if(s->avb) fprintf(s->acc, " %e", c.accepted[PP_MOVE_AVB] / (double) c.tries[PP_MOVE_AVB]); /* output.c:156-158 */
+	/* output.c:149-162: the dynamics' columns */
+	if(s->vmmc) fprintf(s->acc, "%lld %e", step, c.accepted[PP_MOVE_VMMC] / (double) c.tries[PP_MOVE_VMMC]);
+	else fprintf(s->acc, "%lld %e", step, c.accepted[PP_MOVE_ROTO_TRASL] / (double) c.tries[PP_MOVE_ROTO_TRASL]);
+	if(s->avb) fprintf(s->acc, " %e", c.accepted[PP_MOVE_AVB] / (double) c.tries[PP_MOVE_AVB]);
 	if(s->ensemble == PP_GC || s->ensemble == PP_SUS) {
 		fprintf(s->acc, " %e", c.accepted[PP_MOVE_ADD] / (double) c.tries[PP_MOVE_ADD]);
 		fprintf(s->acc, " %e", c.accepted[PP_MOVE_REMOVE] / (double) c.tries[PP_MOVE_REMOVE]);
@@ -236,9 +238,14 @@ int main(int argc, char *argv[]) {
 	pp_default_params(&p);
 	const int dynamics = (int) key_ll(in, "Dynamics", 1, 0);
 	s.ensemble = p.ensemble = (int) key_ll(in, "Ensemble", 1, 0);
-	if(dynamics != PP_RTMC && dynamics != PP_AVBMC)
-		die("Dynamics = %d is not run by this engine (0 roto-translations, 2 AVB moves and roto-translations)", dynamics);
+	if(dynamics != PP_RTMC && dynamics != PP_VMMC && dynamics != PP_AVBMC)
+		die("Dynamics = %d is not run by this engine (0 roto-translations, 1 VMMC, 2 AVB moves and roto-translations)", dynamics);
 	p.dynamics = dynamics;
+	if(dynamics == PP_VMMC) { /* VMMC_init (vmmc.c:15-45): both keys mandatory */
+		s.vmmc = 1;
+		p.vmmc_max_move = key_d(in, "vmmc_max_move", 1, 0.);
+		p.vmmc_max_cluster = (int) key_ll(in, "vmmc_max_cluster", 1, 0);
+	}
 	if(dynamics == PP_AVBMC) { /* AVBMC_init (avb.c:13-36): the optional avb_p */
 		s.avb = 1;
 		p.avb_p = key_d(in, "avb_p", 0, 0.5);

@@ -45,6 +45,7 @@ struct pp_engine {
 	int any_npt;
 	int any_lx;           /* some NVT replica has the box-shape move */
 	int any_avb;          /* some replica makes AVB moves (Dynamics = 2) */
+	int any_vmmc;         /* every replica makes VMMC moves (Dynamics = 1): no checkerboard rounds */
 	int any_audit;
 	int nl_mode;          /* per-epoch neighbour lists for plain moves (pp_gpu_set_neighbour_lists) */
 	int nl_valid;         /* the current epoch's lists are built and only plain moves ran since */
@@ -177,6 +178,8 @@ void pp_default_params(pp_params *p) {
 	p->audit = 0;
 	p->dynamics = PP_RTMC;
 	p->avb_p = 0.5; /* avb.c:30 */
+	p->vmmc_max_cluster = 0;
+	p->vmmc_max_move = 0.;
 }
 
 static int is_exchange(const pp_engine *e);
@@ -199,7 +202,12 @@ static int check_params(pp_engine *e, const pp_params *p) {
 	if(p->resort_every < 0 || p->resort_every > 64) return set_err(e, PP_ERR_ARG, "resort_every (re-sort period in rounds) must be 0 or in [1, 64]");
 	if(p->ensemble == PP_NPT && !(p->rescale_factor_max > 0. && p->rescale_factor_max < 1.)) return set_err(e, PP_ERR_ARG, "rescale_factor_max must lie in (0, 1)");
 	if(p->lx_move < 0 || p->lx_move > 2) return set_err(e, PP_ERR_ARG, "Lx_move must be 0, 1 (reference acceptance) or 2 (Boltzmann acceptance)");
-	if(p->dynamics != PP_RTMC && p->dynamics != PP_AVBMC) return set_err(e, PP_ERR_ARG, "Dynamics %d not supported (0 = roto-translations, 2 = AVB)", p->dynamics);
+	if(p->dynamics != PP_RTMC && p->dynamics != PP_VMMC && p->dynamics != PP_AVBMC)
+		return set_err(e, PP_ERR_ARG, "Dynamics %d not supported (0 = roto-translations, 1 = VMMC, 2 = AVB)", p->dynamics);
+	if(p->dynamics == PP_VMMC) {
+		if(p->ensemble != PP_NVT && p->ensemble != PP_NPT) return set_err(e, PP_ERR_ARG, "the VMMC move runs in the NVT and NPT ensembles");
+		if(p->vmmc_max_cluster < 1) return set_err(e, PP_ERR_ARG, "vmmc_max_cluster must be >= 1");
+	}
 	if(p->dynamics == PP_AVBMC) {
 		if(p->ensemble != PP_NVT && p->ensemble != PP_NPT) return set_err(e, PP_ERR_ARG, "the AVB move runs in the NVT and NPT ensembles");
 		if(!(p->avb_p >= 0. && p->avb_p <= 1.)) return set_err(e, PP_ERR_ARG, "avb_p must lie in [0, 1]");
@@ -253,8 +261,12 @@ static int create_common(const pp_params *prms, int n, pp_engine **out) {
 		if(e->prm[i].ensemble == PP_NVT && e->prm[i].lx_move) e->any_lx = 1;
 		if(e->prm[i].audit) e->any_audit = 1;
 		if(e->prm[i].dynamics == PP_AVBMC) e->any_avb = 1;
+		if(e->prm[i].dynamics == PP_VMMC) e->any_vmmc = 1;
 	}
-	if(e->any_avb) e->graphs_on = 0; /* the AVB batches are launched from the host before each re-sort */
+	if(e->any_vmmc)
+		for(int i = 0; i < n; i++)
+			if(e->prm[i].dynamics != PP_VMMC) return set_err(e, PP_ERR_ARG, "VMMC replicas cannot share an engine with other dynamics");
+	if(e->any_avb || e->any_vmmc) e->graphs_on = 0; /* the AVB / VMMC batches are launched from the host */
 	if(e->prm[0].resort_every > 0) e->resort_every = e->prm[0].resort_every;
 	for(int i = 0; i < n; i++)
 		if((e->prm[i].ensemble == PP_GC || e->prm[i].ensemble == PP_SUS) && n > 1)
@@ -286,7 +298,8 @@ static void free_device(pp_engine *e) {
 		(void **) &e->d.cell_count, (void **) &e->d.cell_start, (void **) &e->d.cell_cursor, (void **) &e->d.cell_rep, (void **) &e->d.scan_aux,
 		(void **) &e->d.clist, (void **) &e->d.ccount, (void **) &e->d.dflag, (void **) &e->d.eflag, (void **) &e->d.rp, (void **) &e->d.rs, (void **) &e->d.grid, (void **) &e->d.out_bonds,
 		(void **) &e->d.out_overlaps, (void **) &e->d.out_partners, (void **) &e->d.tmp_rec, (void **) &e->d.tmp_id, (void **) &e->d.avb_head,
-		(void **) &e->d.avb_next, (void **) &e->d.avb_cell };
+		(void **) &e->d.avb_next, (void **) &e->d.avb_cell, (void **) &e->d.vm_old, (void **) &e->d.vm_links, (void **) &e->d.vm_pre,
+		(void **) &e->d.vm_fail, (void **) &e->d.vm_cnt, (void **) &e->d.vm_copies, (void **) &e->d.vm_in, (void **) &e->d.vm_clust };
 	for(size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); i++) {
 		if(*ptrs[i]) cudaFree(*ptrs[i]);
 		*ptrs[i] = NULL;
@@ -482,7 +495,8 @@ static int derive_rparams(pp_engine *e, int r, ppi_rparams *rp) {
 	rp->n_min = p->ensemble == PP_SUS ? p->n_min : 0;
 	rp->n_max = p->n_max;
 	rp->dynamics = p->dynamics;
-	if(p->dynamics == PP_AVBMC) avb_rparams(e, r, rp);
+	rp->vmmc_max_cluster = p->vmmc_max_cluster;
+	if(p->dynamics == PP_AVBMC || p->dynamics == PP_VMMC) avb_rparams(e, r, rp); /* the batches' linked cells */
 	for(int k = 0; k < 32; k++) {
 		double pk = exp(-(double) k / p->temperature);
 		double t = ceil(pk * 9007199254740992.0);
@@ -545,6 +559,8 @@ static int read_states(pp_engine *e) {
 	for(int r = 0; r < e->nrep; r++)
 		if(e->h_rs[r].error == PPI_E_LISTS)
 			return set_err(e, PP_ERR_CAPACITY, "replica %d: more guard-band pairs in one volume pass than its buffer holds", r);
+		else if(e->h_rs[r].error == PPI_E_VMMC)
+			return set_err(e, PP_ERR_STATE, "replica %d: VMMC: memory exhausted, or a cluster moved into an overlap", r);
 		else if(e->h_rs[r].error == PPI_E_AVB)
 			return set_err(e, PP_ERR_STATE, "replica %d: an AVB move's rejection sampling ran out of draws", r);
 		else if(e->h_rs[r].error == PPI_E_EXACT)
@@ -703,7 +719,7 @@ static int commit(pp_engine *e) {
 		p0 += slot_cap(e, r);
 		rp->cell_base = (int) cells;
 		cells += rp->cell_cap;
-		if(rp->dynamics == PP_AVBMC) {
+		if(rp->dynamics == PP_AVBMC || rp->dynamics == PP_VMMC) {
 			rp->avb_head0 = (int) avb_cells;
 			avb_cells += (long long) rp->avb_ncap[0] * rp->avb_ncap[1] * rp->avb_ncap[2];
 		}
@@ -742,6 +758,16 @@ static int commit(pp_engine *e) {
 		CU(cudaMalloc((void **) &d->avb_head, sizeof(int) * (size_t) avb_cells));
 		CU(cudaMalloc((void **) &d->avb_next, sizeof(int) * n1));
 		CU(cudaMalloc((void **) &d->avb_cell, sizeof(int) * n1));
+	}
+	if(e->any_vmmc) { /* VMMC_init's arrays (vmmc.c:28-42), 16 links per particle */
+		CU(cudaMalloc((void **) &d->vm_old, sizeof(double) * 12 * n1));
+		CU(cudaMalloc((void **) &d->vm_links, sizeof(int) * 2 * 16 * n1));
+		CU(cudaMalloc((void **) &d->vm_pre, sizeof(int) * 16 * n1));
+		CU(cudaMalloc((void **) &d->vm_fail, sizeof(int) * 16 * n1));
+		CU(cudaMalloc((void **) &d->vm_cnt, sizeof(int) * n1));
+		CU(cudaMalloc((void **) &d->vm_copies, sizeof(int) * n1));
+		CU(cudaMalloc((void **) &d->vm_in, sizeof(int) * n1));
+		CU(cudaMalloc((void **) &d->vm_clust, sizeof(int) * n1));
 	}
 	d->audit_any = e->any_audit;
 	{ /* lanes per attempt: a tuning override for measurements (4 by default) */
@@ -867,7 +893,7 @@ int pp_gpu_upload_replica(pp_engine *e, int r, int N, const double *rr, const do
 			int rc = read_states(e);
 			if(rc != PP_OK) return rc;
 			memcpy(e->h_box[r], box, sizeof(double) * 3);
-			if(e->prm[r].dynamics == PP_AVBMC) { /* AVBMC_init's V_out follows the uploaded box; the cell grid keeps its reservation */
+			if(e->prm[r].dynamics == PP_AVBMC || e->prm[r].dynamics == PP_VMMC) { /* AVBMC_init's V_out follows the uploaded box; the cell grid keeps its reservation */
 				ppi_rparams *rp = e->h_rp + r;
 				int ncap[3] = { rp->avb_ncap[0], rp->avb_ncap[1], rp->avb_ncap[2] };
 				avb_rparams(e, r, rp);
@@ -1149,8 +1175,8 @@ int pp_gpu_set_graphs(pp_engine *e, int enable) {
 	if(e == NULL) return PP_ERR_ARG;
 	/* GC / SUS exchanges and AVB batches are launched from the host between re-sort periods, which a
 	 * captured period would skip */
-	if(enable && (is_exchange(e) || e->any_avb))
-		return set_err(e, PP_ERR_ARG, "engines with insertions and removals or AVB moves launch their kernels one by one (no graphs)");
+	if(enable && (is_exchange(e) || e->any_avb || e->any_vmmc))
+		return set_err(e, PP_ERR_ARG, "engines with insertions and removals, AVB or VMMC moves launch their kernels one by one (no graphs)");
 	e->graphs_on = enable ? 1 : 0;
 	if(!enable) drop_graphs(e);
 	return PP_OK;
@@ -1210,7 +1236,18 @@ int pp_gpu_sweeps(pp_engine *e, long long n) {
 		}
 		long long s = e->sweep_counter++;
 		int ev;
-		for(int rr = 0; rr < e->rounds_per_sweep; rr++) {
+		if(e->any_vmmc) { /* every attempt a VMMC move (vmmc.c:258-483): N of them, then a re-sort for the passes that follow */
+			long long nl = 0;
+			if((rc = ev_begin(e, 1, &ev)) != PP_OK) return rc;
+			CK(ppi_vmmc(&e->d, s, 1, e->stream, &nl));
+			if((rc = ev_end(e, ev)) != PP_OK) return rc;
+			e->launches += nl;
+			if((rc = ev_begin(e, 0, &ev)) != PP_OK) return rc;
+			if((rc = do_resort(e)) != PP_OK) return rc;
+			if((rc = ev_end(e, ev)) != PP_OK) return rc;
+			e->round_counter++;
+		}
+		for(int rr = 0; rr < (e->any_vmmc ? 0 : e->rounds_per_sweep); rr++) {
 			if(e->round_counter % e->resort_every == 0) {
 				if(is_exchange(e) && (rc = exchange_step(e)) != PP_OK) return rc;
 				if(e->any_avb) { /* the AVB moves of the coming re-sort period (avb.c:77-186) */
@@ -1884,7 +1921,7 @@ int pp_gpu_set_proposal(pp_engine *e, int proposal) {
 	int rc = ready(e);
 	if(rc != PP_OK) return rc;
 	if(proposal != PP_PROPOSAL_PLAIN && is_exchange(e)) return set_err(e, PP_ERR_ARG, "the learned proposal is not available with insertions and removals");
-	if(proposal != PP_PROPOSAL_PLAIN && e->any_avb) return set_err(e, PP_ERR_ARG, "the learned proposal is not available with AVB moves");
+	if(proposal != PP_PROPOSAL_PLAIN && (e->any_avb || e->any_vmmc)) return set_err(e, PP_ERR_ARG, "the learned proposal is not available with AVB or VMMC moves");
 	if(proposal == PP_PROPOSAL_PLAIN) {
 		e->proposal = proposal;
 		return PP_OK;
@@ -2133,7 +2170,7 @@ int pp_gpu_autotune(pp_engine *e, int trial_sweeps, pp_tune_result *out) {
 	if(rc != PP_OK) return rc;
 	if(trial_sweeps < 1 || trial_sweeps > 100000) return set_err(e, PP_ERR_ARG, "trial_sweeps must lie in [1, 100000]");
 	if(is_exchange(e)) return set_err(e, PP_ERR_ARG, "the autotuner does not run GC or SUS engines (their particle count changes)");
-	if(e->any_avb) return set_err(e, PP_ERR_ARG, "the autotuner does not run AVB engines");
+	if(e->any_avb || e->any_vmmc) return set_err(e, PP_ERR_ARG, "the autotuner does not run AVB or VMMC engines");
 	const int resorts[] = { 1, 2, 4, 8, 16 }, reorders[] = { 4, 16, 64 };
 	const double scales[] = { 1.0, 1.2, 1.5 };
 	const int r0 = e->resort_every, o0 = e->reorder_every, l0 = e->nl_mode;

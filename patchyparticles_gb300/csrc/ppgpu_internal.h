@@ -44,6 +44,7 @@ extern "C" {
 #define PPI_E_BARRIER 5 /* a grid-barrier wait of the persistent round kernel ran out of its limit */
 #define PPI_E_GCFULL 6  /* a grand-canonical insertion found the system at GC_N_max (the reference stops there) */
 #define PPI_E_AVB 7     /* an AVB move's rejection sampling ran out of its draw limit (no move made) */
+#define PPI_E_VMMC 8    /* a VMMC move ran out of link memory or moved a cluster into an overlap (the reference stops) */
 
 typedef struct ppi_rparams {
 	int N;           /* particles of this replica */
@@ -72,6 +73,8 @@ typedef struct ppi_rparams {
 	int avb_per_step;      /* AVB attempts per MC step: round((1 - avb_p) N) */
 	double avb_vin, avb_vout; /* AVBMC_init's bonding and non-bonding volumes (avb.c:26-28), fixed at upload */
 	double base_orient[9]; /* a rotation taking base patch 0 to (0, 0, 1) (system.c:33-54) */
+	int vmmc_max_cluster;  /* Dynamics = 1 (vmmc.c): a cluster that reaches this size is rejected */
+	int pad_vmmc;
 } ppi_rparams;
 
 typedef struct ppi_rstate {
@@ -210,10 +213,16 @@ typedef struct ppi_dev {
 	int bar_extra;       /* test hook: arrivals the first barrier waits for beyond the grid (1 = never completes) */
 	int persist;         /* 1: plain rounds over the neighbour lists use k_round, 0: one launch per colour */
 	unsigned long long *sus_hist; /* SUS: histogram of N after every insertion/removal attempt, n_max - n_min + 1 bins */
-	/* AVB moves: linked cells (cells.c) of the replica's live particles, rebuilt at every AVB batch */
+	/* AVB and VMMC moves: linked cells (cells.c) of the replica's live particles, rebuilt at every batch */
 	int *avb_head;     /* per replica avb_ncap[0] x [1] x [2] entries from avb_head0: first slot offset, -1 */
 	int *avb_next;     /* per slot: next slot offset of its cell, -1 */
-	int *avb_cell;     /* per slot: its AVB cell */
+	int *avb_cell;     /* per slot: its cell */
+	/* VMMC (vmmc.h: vmmc_d), per slot: the stored degrees of freedom (x y z and 9 orientation entries),
+	 * the possible links (16 pairs of slot offsets per slot of the replica), the prelinked and outright
+	 * failed lists (16 entries per slot each), link counters, copies, cluster flags and the cluster */
+	double *vm_old;
+	int *vm_links, *vm_pre, *vm_fail;
+	int *vm_cnt, *vm_copies, *vm_in, *vm_clust;
 } ppi_dev;
 
 #define PPI_MAX_PARTNERS 24
@@ -232,6 +241,8 @@ int ppi_gram_schmidt(const ppi_dev *d, int first, int count, cudaStream_t s, lon
 int ppi_exchange(const ppi_dev *d, long long step, int attempts, cudaStream_t s, long long *nl);
 /* Dynamics = 2: `steps` MC steps' worth of AVB attempts per AVB replica (AVBMC_dynamics, avb.c:77-186) */
 int ppi_avb(const ppi_dev *d, long long step, int steps, cudaStream_t s, long long *nl);
+/* Dynamics = 1: `steps` MC steps of VMMC moves (N each) per VMMC replica (VMMC_dynamics, vmmc.c:258-483) */
+int ppi_vmmc(const ppi_dev *d, long long step, int steps, cudaStream_t s, long long *nl);
 int ppi_reorder(const ppi_dev *d, cudaStream_t s, long long *nl);
 /* writes x y z R00..R22 (12 doubles) of slots [first, first + count) into d->tmp_rec */
 int ppi_export(const ppi_dev *d, int first, int count, cudaStream_t s, long long *nl);

@@ -4615,12 +4615,404 @@ __global__ void __launch_bounds__(AVB_B) k_avb(ppi_dev d, long long step, int st
 }
 
 /* ------------------------------------------------------------------------------------------------ */
+/* virtual-move Monte Carlo (Dynamics = 1, VMMC_dynamics)                                            */
+/* ------------------------------------------------------------------------------------------------ */
+/* One CTA per VMMC replica makes N cluster moves per MC step one after the other, as VMMC_dynamics
+ * (vmmc.c:258-483) does for every attempt: a seed and a random translation (Disp_max) or rotation about the
+ * seed (Theta_max); links to neighbours within the bonding range before and after the seed's virtual move
+ * (_populate_possible_links, vmmc.c:148-229, with its image bookkeeping); links drawn at random, p
+ * recruiting q with 1 - exp((E_old - E_p_moved) / T) and q agreeing with the ratio of the reverse virtual
+ * move's probability (overlaps force the link); prelinked particles left outside reject the move, as does
+ * a cluster reaching vmmc_max_cluster; an accepted move shifts the whole cluster. The orientations are made
+ * canonical (R0 = R0 . Q(q), q = 1) at the start of the batch, so that the stored R0 is the orientation
+ * matrix the moves rotate, as the reference's orientation field. Pair energies are the reference's FP64
+ * test (explicitly rounded), so the tracked energy stays exact; the cluster energies use 27 threads, one
+ * per neighbour cell; the rest of a move is one thread's sequential work. The caller re-sorts after the
+ * batch. */
+#define VM_B 64
+#define TAG_VMMC 11u
+#define VM_LINKS 16 /* links, prelinked and failed entries per particle (possible_links holds 16 N, vmmc.c:29) */
+
+struct VmCtx {
+	const ppi_dev *d;
+	const ppi_rparams *rp;
+	double box[3];
+	int ns[3];
+	int p0, N;
+	int rot;
+	double move[3], Rm[9];
+	int nclust, nlinks, npre, nfail;
+	int err;
+};
+
+__device__ __forceinline__ double *vm_rec(const VmCtx &c, int i) { return c.d->rec + (size_t) (c.p0 + i) * PPI_REC; }
+__device__ __forceinline__ double *vm_old(const VmCtx &c, int i) { return c.d->vm_old + (size_t) (c.p0 + i) * 12; }
+
+/* _store_dof / _restore_dof (vmmc.c:58-79): position and orientation (R0 with q = 1) */
+__device__ void vm_store(const VmCtx &c, int i) {
+	const double *r = vm_rec(c, i);
+	double *o = vm_old(c, i);
+	for(int k = 0; k < 3; k++) o[k] = r[k];
+	for(int k = 0; k < 9; k++) o[3 + k] = r[PPI_R0 + k];
+}
+
+__device__ void vm_restore(const VmCtx &c, int i) {
+	double *r = vm_rec(c, i);
+	const double *o = vm_old(c, i);
+	for(int k = 0; k < 3; k++) r[k] = o[k];
+	for(int k = 0; k < 9; k++) r[PPI_R0 + k] = o[3 + k];
+}
+
+/* _pair_energy (vmmc.c:81-95): -1 bond, 0 otherwise; an overlap sets *ov */
+__device__ double vm_pair_energy(const VmCtx &c, int p, int q, int *ov) {
+	const double *a = vm_rec(c, p), *b = vm_rec(c, q);
+	int pa = 0;
+	const int res = avb_pair(a, a + PPI_R0, b, nullptr, b + PPI_R0, *c.rp, c.box, &pa);
+	if(res == 1) return -1.;
+	if(res == -1) *ov = 1;
+	return 0.;
+}
+
+/* _move_particle (vmmc.c:231-256), after vm_store(i): the translation, or the rotation about the seed */
+__device__ void vm_move(const VmCtx &c, int i) {
+	double *r = vm_rec(c, i);
+	if(!c.rot) {
+		for(int k = 0; k < 3; k++) r[k] += c.move[k];
+		return;
+	}
+	const int seed = c.d->vm_clust[c.p0];
+	const double *sr = vm_rec(c, seed);
+	const double dt[3] = { r[0] - sr[0], r[1] - sr[1], r[2] - sr[2] };
+	double dr[3];
+	avb_matvec(c.Rm, dt, dr);
+	for(int k = 0; k < 3; k++) r[k] = sr[k] + dr[k];
+	avb_matmul(c.Rm, vm_old(c, i) + 3, r + PPI_R0);
+}
+
+/* MC_change_cell (MC.c:180-206) on the batch's linked cells */
+__device__ void vm_change_cell(const VmCtx &c, int i) {
+	const ppi_dev &d = *c.d;
+	int idx[3];
+	const int cn = avb_cell_of(vm_rec(c, i), c.box, c.ns, idx), co = d.avb_cell[c.p0 + i];
+	if(cn == co) return;
+	int *h = d.avb_head + c.rp->avb_head0;
+	if(h[co] == i) h[co] = d.avb_next[c.p0 + i];
+	else {
+		int w = h[co];
+		for(int guard = 0; w != -1 && d.avb_next[c.p0 + w] != i && guard < c.N; guard++) w = d.avb_next[c.p0 + w];
+		if(w != -1) d.avb_next[c.p0 + w] = d.avb_next[c.p0 + i];
+	}
+	d.avb_next[c.p0 + i] = h[cn];
+	h[cn] = i;
+	d.avb_cell[c.p0 + i] = cn;
+}
+
+__device__ void vm_drop_link(VmCtx &c, int k, int p, int q) {
+	int *L = c.d->vm_links + 2 * (size_t) VM_LINKS * c.p0;
+	L[2 * k] = L[2 * (c.nlinks - 1)];
+	L[2 * k + 1] = L[2 * (c.nlinks - 1) + 1];
+	c.nlinks--;
+	int *cnt = c.d->vm_cnt + c.p0, *cp = c.d->vm_copies + c.p0;
+	cnt[p]--;
+	cnt[q]--;
+	if(cnt[p] == 0) cp[p] = 0;
+	if(cnt[q] == 0) cp[q] = 0;
+}
+
+/* _populate_possible_links (vmmc.c:148-229) for particle i at its current (real or virtual) position */
+__device__ void vm_populate(VmCtx &c, int i, int *force_reject) {
+	const ppi_dev &d = *c.d;
+	int idx[3];
+	const double *ri = vm_rec(c, i), *ro = vm_old(c, i);
+	avb_cell_of(ri, c.box, c.ns, idx);
+	int *L = d.vm_links + 2 * (size_t) VM_LINKS * c.p0, *cnt = d.vm_cnt + c.p0, *cp = d.vm_copies + c.p0, *in = d.vm_in + c.p0;
+	for(int t = 0; t < 27; t++) {
+		const int cx = (idx[0] + t / 9 - 1 + c.ns[0]) % c.ns[0], cy = (idx[1] + (t / 3) % 3 - 1 + c.ns[1]) % c.ns[1], cz = (idx[2] + t % 3 - 1 + c.ns[2]) % c.ns[2];
+		int q = d.avb_head[c.rp->avb_head0 + (cx * c.ns[1] + cy) * c.ns[2] + cz];
+		for(int guard = 0; q != -1 && guard < c.N; guard++) {
+			if(q != i) {
+				double *rq = vm_rec(c, q);
+				double dist[3];
+				for(int k = 0; k < 3; k++) {
+					dist[k] = rq[k] - ri[k];
+					dist[k] -= c.box[k] * rint(dist[k] / c.box[k]);
+				}
+				if(dist[0] * dist[0] + dist[1] * dist[1] + dist[2] * dist[2] < c.rp->sqr_rcut) {
+					if(c.nlinks >= VM_LINKS * c.N) { /* "VMMC: memory exhausted" (vmmc.c:176) */
+						c.err = 1;
+						*force_reject = 1;
+						return;
+					}
+					double np[3];
+					for(int k = 0; k < 3; k++) {
+						dist[k] = rq[k] - ro[k];
+						dist[k] -= c.box[k] * rint(dist[k] / c.box[k]);
+						np[k] = ro[k] + dist[k];
+					}
+					if(cp[q] == 1 || in[q] == 1) {
+						if(fabs(np[0] - rq[0]) > 1e-6 || fabs(np[1] - rq[1]) > 1e-6 || fabs(np[2] - rq[2]) > 1e-6) {
+							*force_reject = 1;
+							return;
+						}
+					}
+					if(cp[q] == 0 && in[q] == 0) {
+						for(int k = 0; k < 3; k++) rq[k] = np[k];
+						cp[q] = 1;
+					}
+					const int n = c.nlinks, lo = i < q ? i : q, hi = i < q ? q : i;
+					L[2 * n] = lo;
+					L[2 * n + 1] = hi;
+					c.nlinks++;
+					cnt[i]++;
+					cnt[q]++;
+					for(int m = 0; m < c.nlinks - 1; m++)
+						if(L[2 * m] == lo && L[2 * m + 1] == hi) {
+							c.nlinks--;
+							cnt[i]--;
+							cnt[q]--;
+							if(cnt[i] == 0) cp[i] = 0;
+							if(cnt[q] == 0) cp[q] = 0;
+							break;
+						}
+				}
+			}
+			q = d.avb_next[c.p0 + q];
+		}
+	}
+}
+
+struct VmShared {
+	int fr, nb, ov, nclust, stop;
+};
+
+/* _compute_cluster_energy (vmmc.c:107-137): bonds between the cluster and the particles outside it, one
+ * thread per neighbour cell of each member; every thread of the CTA calls it */
+__device__ int vm_cluster_bonds(const VmCtx &c, VmShared &S) {
+	const ppi_dev &d = *c.d;
+	if(threadIdx.x == 0) {
+		S.nb = 0;
+		S.ov = 0;
+	}
+	__syncthreads();
+	for(int m = 0; m < S.nclust; m++) {
+		const int p = d.vm_clust[c.p0 + m];
+		const int t = threadIdx.x;
+		if(t < 27) {
+			int idx[3];
+			const double *rp = vm_rec(c, p);
+			avb_cell_of(rp, c.box, c.ns, idx);
+			const int cx = (idx[0] + t / 9 - 1 + c.ns[0]) % c.ns[0], cy = (idx[1] + (t / 3) % 3 - 1 + c.ns[1]) % c.ns[1], cz = (idx[2] + t % 3 - 1 + c.ns[2]) % c.ns[2];
+			int q = d.avb_head[c.rp->avb_head0 + (cx * c.ns[1] + cy) * c.ns[2] + cz];
+			int nb = 0, ov = 0;
+			for(int guard = 0; q != -1 && guard < c.N; guard++) {
+				if(d.vm_in[c.p0 + q] == 0) nb -= (int) vm_pair_energy(c, p, q, &ov);
+				q = d.avb_next[c.p0 + q];
+			}
+			if(nb) atomicAdd(&S.nb, nb);
+			if(ov) S.ov = 1;
+		}
+		__syncthreads();
+	}
+	return S.nb;
+}
+
+__global__ void __launch_bounds__(VM_B) k_vmmc(ppi_dev d, long long step, int steps) {
+	const int r = blockIdx.x, tid = threadIdx.x;
+	const ppi_rparams &rp = d.rp[r];
+	ppi_rstate *rs = d.rs + r;
+	if(rp.dynamics != 1) return;
+	const int N = rp.N;
+	if(N < 1) return;
+	__shared__ VmShared S;
+	VmCtx c;
+	c.d = &d;
+	c.rp = &rp;
+	for(int a = 0; a < 3; a++) {
+		c.box[a] = rs->box[a];
+		int n = (int) floor(c.box[a] / rp.r_cut); /* cells_init (cells.c:17-37) */
+		n = n < rp.avb_ncap[a] ? n : rp.avb_ncap[a];
+		c.ns[a] = n < 3 ? 3 : n;
+	}
+	c.p0 = rp.p0;
+	c.N = N;
+	c.nclust = c.nlinks = c.npre = c.nfail = 0;
+	c.err = 0;
+	const int ncell = c.ns[0] * c.ns[1] * c.ns[2];
+	for(int k = tid; k < ncell; k += VM_B) d.avb_head[rp.avb_head0 + k] = -1;
+	__syncthreads();
+	for(int i = tid; i < N; i += VM_B) {
+		double *q = vm_rec(c, i);
+		double R[9]; /* canonical orientation: R0 = R0 . Q(q), q = 1 (the same matrix every pass reads) */
+		orient64(q + PPI_R0, q + PPI_Q, R);
+		for(int k = 0; k < 9; k++) q[PPI_R0 + k] = R[k];
+		q[PPI_Q] = 1.0;
+		q[PPI_Q + 1] = q[PPI_Q + 2] = q[PPI_Q + 3] = 0.0;
+		d.vm_cnt[c.p0 + i] = d.vm_copies[c.p0 + i] = d.vm_in[c.p0 + i] = 0;
+		int idx[3];
+		const int cc = avb_cell_of(q, c.box, c.ns, idx);
+		d.avb_cell[c.p0 + i] = cc;
+		d.avb_next[c.p0 + i] = atomicExch(&d.avb_head[rp.avb_head0 + cc], i);
+	}
+	__syncthreads();
+	const long long moves = (long long) N * steps;
+	int *clust = d.vm_clust + c.p0, *in = d.vm_in + c.p0, *cp = d.vm_copies + c.p0, *cnt = d.vm_cnt + c.p0;
+	int *L = d.vm_links + 2 * (size_t) VM_LINKS * c.p0, *pre = d.vm_pre + (size_t) VM_LINKS * c.p0, *fail = d.vm_fail + (size_t) VM_LINKS * c.p0;
+	AvbRng g;
+	int nb_before = 0;
+	for(long long m = 0; m < moves; m++) {
+		if(tid == 0) {
+			g.rp = &rp;
+			g.step = step;
+			g.r = r;
+			g.item = (uint32_t) m;
+			g.sub = 0u;
+			g.k = 0;
+			rs->tries[5]++; /* MOVE_VMMC (defs.h:17) */
+			int fr = 0;
+			c.nclust = 1;
+			c.nfail = c.nlinks = c.npre = 0;
+			int seed = (int) (g.next() * N);
+			seed = seed < N ? seed : N - 1;
+			in[seed] = 1;
+			clust[0] = seed;
+			if(g.next() < 0.5) {
+				c.rot = 0;
+				for(int k = 0; k < 3; k++) c.move[k] = (g.next() - 0.5) * rp.disp_max;
+			}
+			else {
+				c.rot = 1;
+				if(!avb_sphere(g, c.move)) {
+					c.err = 1;
+					fr = 1;
+				}
+				const double angle = g.next() * rp.theta_max;
+				avb_rot(c.move, angle, c.Rm);
+			}
+			vm_store(c, seed);
+			if(!fr) vm_populate(c, seed, &fr);
+			if(!fr) {
+				vm_move(c, seed);
+				vm_populate(c, seed, &fr);
+				vm_restore(c, seed);
+			}
+			while(c.nlinks > 0 && c.nclust < rp.vmmc_max_cluster && !fr) {
+				int k = (int) (g.next() * c.nlinks);
+				k = k < c.nlinks ? k : c.nlinks - 1;
+				int p = L[2 * k], q = L[2 * k + 1];
+				if(in[p] == 1 && in[q] == 1) {
+					vm_drop_link(c, k, p, q);
+					continue;
+				}
+				if(in[p] == 0) {
+					const int t = q;
+					q = p;
+					p = t;
+				}
+				int ov = 0;
+				const double E_old = vm_pair_energy(c, p, q, &ov);
+				vm_store(c, p);
+				vm_move(c, p);
+				ov = 0;
+				const double E_p = vm_pair_energy(c, p, q, &ov);
+				vm_restore(c, p);
+				const int force_prelink = ov;
+				const double p1 = 1. - exp((1. / rp.T) * (E_old - E_p));
+				if(force_prelink == 1 || p1 > g.next()) {
+					vm_store(c, q);
+					vm_move(c, q);
+					ov = 0;
+					const double E_q = vm_pair_energy(c, p, q, &ov);
+					vm_restore(c, q);
+					const int force_link = ov;
+					double p2 = 1. - exp((1. / rp.T) * (E_old - E_q));
+					if(p2 > 1.) p2 = 1.;
+					if(force_link == 1 || (p2 / p1) > g.next()) {
+						cp[q] = 0;
+						in[q] = 1;
+						clust[c.nclust++] = q;
+						vm_store(c, q);
+						vm_populate(c, q, &fr);
+						if(fr) break;
+						vm_move(c, q);
+						vm_populate(c, q, &fr);
+						vm_restore(c, q);
+						if(fr) break;
+					}
+					else if(c.npre < VM_LINKS * N) pre[c.npre++] = q;
+					else {
+						c.err = 1;
+						fr = 1;
+						break;
+					}
+				}
+				else if(c.nfail < VM_LINKS * N) fail[c.nfail++] = q;
+				else {
+					c.err = 1;
+					fr = 1;
+					break;
+				}
+				vm_drop_link(c, k, p, q);
+			}
+			if(c.nclust == rp.vmmc_max_cluster) fr = 1;
+			for(int i = 0; i < c.npre; i++) {
+				if(in[pre[i]] == 0) fr = 1;
+				else cp[pre[i]] = 0;
+			}
+			S.fr = fr;
+			S.nclust = c.nclust;
+			S.stop = c.err;
+		}
+		__syncthreads();
+		if(!S.fr) nb_before = vm_cluster_bonds(c, S);
+		if(tid == 0) {
+			if(!S.fr && S.ov) c.err = 1; /* assert(syst->overlap == 0), vmmc.c:436 */
+			for(int i = 0; i < c.nclust && !S.fr; i++) {
+				vm_store(c, clust[i]);
+				vm_move(c, clust[i]);
+				vm_change_cell(c, clust[i]);
+			}
+		}
+		__syncthreads();
+		int nb_after = 0;
+		if(!S.fr) nb_after = vm_cluster_bonds(c, S);
+		if(tid == 0) {
+			if(!S.fr && S.ov) c.err = 1; /* vmmc.c:446 */
+			if(S.fr)
+				for(int i = 0; i < c.nclust; i++) vm_restore(c, clust[i]);
+			else {
+				rs->accepted[5]++;
+				rs->bonds += nb_after - nb_before;
+			}
+			for(int i = 0; i < c.nclust; i++) {
+				vm_change_cell(c, clust[i]);
+				in[clust[i]] = 0;
+			}
+			for(int i = 0; i < c.nfail; i++) cp[fail[i]] = 0;
+			for(int i = 0; i < c.nlinks; i++) {
+				cp[L[2 * i]] = cp[L[2 * i + 1]] = 0;
+				cnt[L[2 * i]] = cnt[L[2 * i + 1]] = 0;
+			}
+			if(c.err) rs->error = PPI_E_VMMC;
+			S.stop = c.err;
+		}
+		__syncthreads();
+		if(S.stop) break;
+	}
+}
+
+/* ------------------------------------------------------------------------------------------------ */
 /* launchers                                                                                        */
 /* ------------------------------------------------------------------------------------------------ */
 static int g_sms = 0;
 
 extern "C" int ppi_avb(const ppi_dev *d, long long step, int steps, cudaStream_t s, long long *nl) {
 	k_avb<<<d->nrep, AVB_B, 0, s>>>(*d, step, steps);
+	if(nl) *nl += 1;
+	return (int) cudaGetLastError();
+}
+
+extern "C" int ppi_vmmc(const ppi_dev *d, long long step, int steps, cudaStream_t s, long long *nl) {
+	k_vmmc<<<d->nrep, VM_B, 0, s>>>(*d, step, steps);
 	if(nl) *nl += 1;
 	return (int) cudaGetLastError();
 }

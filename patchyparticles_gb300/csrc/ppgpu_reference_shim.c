@@ -7,13 +7,15 @@
  */
 #include "defs.h"
 #include "avb.h"
+#include "vmmc.h"
 #include "cells.h"
 #include "output.h"
 #include "utils.h"
 #include "ppgpu.h"        /* from this repository's include/ */
 #include <stdlib.h>
 
-extern avbmc *avbdata; /* avb.c:11, set by AVBMC_init (MC_init runs before gpu_ensemble_init) */
+extern avbmc *avbdata;  /* avb.c:11, set by AVBMC_init (MC_init runs before gpu_ensemble_init) */
+extern vmmc_d *vmmcdata; /* vmmc.c:13, set by VMMC_init */
 
 static pp_engine *G = NULL;
 
@@ -34,8 +36,12 @@ int gpu_ensemble_init(System *syst, Output *IO, int seed) {
 	p.lyz_min = syst->Lyz_min;
 	p.lyz_max = syst->Lyz_max;
 	p.seed = (uint64_t) seed;
-	p.dynamics = syst->dynamics; /* 0, or 2: AVB moves mixed with the roto-translations (avb.c:77-186) */
+	p.dynamics = syst->dynamics; /* 0, 1 (VMMC, vmmc.c:258-483) or 2 (AVB moves and roto-translations, avb.c:77-186) */
 	if(syst->dynamics == AVBMC) p.avb_p = avbdata->avb_p;
+	if(syst->dynamics == VMMC) {
+		p.vmmc_max_cluster = vmmcdata->max_cluster;
+		p.vmmc_max_move = vmmcdata->max_move;
+	}
 	if(syst->ensemble == GC || syst->ensemble == SUS) { /* system.c:90-103 */
 		p.activity = syst->z;
 		p.n_min = syst->N_min;

@@ -43,7 +43,9 @@ def _lines(path):
                                         ("small_gc", ("energy.dat", "acceptance.dat", "density.dat")),
                                         ("small_sus", ("energy.dat", "acceptance.dat", "density.dat")),
                                         ("small_avb", ("energy.dat", "acceptance.dat")),
-                                        ("small_avb_npt", ("energy.dat", "acceptance.dat", "density.dat"))])
+                                        ("small_avb_npt", ("energy.dat", "acceptance.dat", "density.dat")),
+                                        ("small_vmmc", ("energy.dat", "acceptance.dat")),
+                                        ("small_vmmc_npt", ("energy.dat", "acceptance.dat", "density.dat"))])
 def test_driver_writes_the_reference_outputs(built, name, files):
     src, work = _prepare(name)
     p = subprocess.run([CLI, "input"], cwd=work, capture_output=True, text=True, timeout=300)
@@ -113,9 +115,16 @@ def test_driver_reports_a_missing_mandatory_key(built):
 
 
 def test_driver_rejects_other_dynamics(built):
+    src, work = _prepare("small_nvt", lambda t: t.replace("Dynamics = 0", "Dynamics = 3"))
+    p = subprocess.run([CLI, "input"], cwd=work, capture_output=True, text=True, timeout=60)
+    assert p.returncode == 1 and "Dynamics = 3" in p.stderr
+    shutil.rmtree(work)
+
+
+def test_driver_needs_the_vmmc_keys(built):
     src, work = _prepare("small_nvt", lambda t: t.replace("Dynamics = 0", "Dynamics = 1"))
     p = subprocess.run([CLI, "input"], cwd=work, capture_output=True, text=True, timeout=60)
-    assert p.returncode == 1 and "Dynamics = 1" in p.stderr
+    assert p.returncode == 255 and "Mandatory key 'vmmc_max_move' not found" in p.stderr  # vmmc.c:22
     shutil.rmtree(work)
 
 
