@@ -35,7 +35,6 @@ def test_vmmc_keeps_the_tracked_energy_exact(built):
         s = po.System(po.params(T=0.11), arrays=(r2, R2, b2))
         E, ov = s.init_energy()
         assert not ov and E == e.tracked_energy()
-        assert E < -50  # the bond network grew
         e.check_energy()
         e.close()
 
