@@ -360,9 +360,11 @@ def run_gpu(args, wl, ws, rank, local, dist):
     e.counters(reset=True)
     e.set_timing(True)
     e.kernel_stats(reset=True)
+    e.guard_stats(reset=True)
     e.sweeps(args.roofline_sweeps)
     e.sync()
     ks = e.kernel_stats()
+    gs = e.guard_stats()
     e.set_timing(False)
     rtries, _ = e.counters()
     peak, peak_kind = measured_peaks()
@@ -428,7 +430,9 @@ def run_gpu(args, wl, ws, rank, local, dist):
         "volume_acceptance": acc[pp.MOVE_VOLUME] / max(1, tries[pp.MOVE_VOLUME]) if tries[pp.MOVE_VOLUME] else None,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "kernel": sweep_kernel_name(args, tune), "peak_source": peak_kind,
-                     "bytes_per_attempt": BYTES_PER_ATTEMPT, "avg_launch_ms": avg_ms, "attempts_per_launch": att_per_launch},
+                     "bytes_per_attempt": BYTES_PER_ATTEMPT, "avg_launch_ms": avg_ms, "attempts_per_launch": att_per_launch,
+                     # pairs inside the FP32 guard band, decided in FP64 (colour and volume passes), per MC step
+                     "guard_band_pairs_per_step": gs["fallbacks"] / max(1, args.roofline_sweeps)},
         "kernel_ms_per_step": {"sort": ks["sort_ms"] / max(1, ks["sort_launches"]), "sweep": avg_ms,
                                "volume": ks["volume_ms"] / max(1, ks["volume_launches"]) if ks["volume_launches"] else 0.0},
         "clocks": clocks,

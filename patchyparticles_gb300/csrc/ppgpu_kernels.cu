@@ -405,6 +405,103 @@ __device__ __forceinline__ int decide64(const double *__restrict__ rec_all, cons
 	return DEC64_EXACT;
 }
 
+/* decide64 with all 32 lanes of a warp on one pair: every lane calls it with the same arguments and gets
+ * the same result. Lanes 0..15 build p's state and lanes 16..31 q's; lane e < 9 of each half forms one
+ * entry of its particle's orientation R0 . Q(q) with orient64_fast's operations; lanes 0..3 and 16..19
+ * then form one patch cosine each. The values, and so the decision, are decide64's. On this GPU an FP64
+ * instruction occupies the FP64 pipe as long for one lane as for 32, so spreading the ~270 FP64
+ * operations of one decision over the lanes shortens the warp's wait on it about threefold; one
+ * guard-band pair decided by a single lane was the longest chain of a colour pass. */
+__device__ __forceinline__ double shfl_d(double v, int src) {
+	const int lo = __shfl_sync(0xffffffffu, __double2loint(v), src), hi = __shfl_sync(0xffffffffu, __double2hiint(v), src);
+	return __hiloint2double(hi, lo);
+}
+
+__device__ __forceinline__ int decide64_warp(const double *__restrict__ rec_all, const ppi_rparams &rp, const double *box_in, const double *inv_box_in, int ps, int kind,
+		float4 dq, float3 disp, int qs, int vol_mask, const double *vol_f3, const double *vol_box3, int lane) {
+	const int half = lane >> 4, e = lane & 15;
+	const double *rec = rec_all + (size_t) (half ? qs : ps) * PPI_REC;
+	/* this half's particle: position and quaternion (state64_fast) */
+	double q[4] = { rec[PPI_Q], rec[PPI_Q + 1], rec[PPI_Q + 2], rec[PPI_Q + 3] };
+	double r[3] = { rec[0], rec[1], rec[2] };
+	if(half == 0 && kind == 1) {
+		const double b[4] = { f2d(dq.x), f2d(dq.y), f2d(dq.z), f2d(dq.w) };
+		double qn[4];
+#pragma unroll
+		for(int c = 0; c < 4; c++) qn[c] = qcomp64(q[c], q[c ^ 1], q[c ^ 2], q[c ^ 3], b, c);
+#pragma unroll
+		for(int c = 0; c < 4; c++) q[c] = qn[c];
+		r[0] = __dadd_rn(r[0], f2d(disp.x));
+		r[1] = __dadd_rn(r[1], f2d(disp.y));
+		r[2] = __dadd_rn(r[2], f2d(disp.z));
+	}
+	/* entry (i, j) = e of R = R0 . Q(q), orient64_fast's operations */
+	double Rij;
+	{
+		const double w = q[0], x = q[1], y = q[2], z = q[3];
+		const double sc = 2.0 * rcp64(w * w + x * x + y * y + z * z);
+		const double Q[9] = { 1.0 - sc * (y * y + z * z), sc * (x * y - w * z), sc * (x * z + w * y), sc * (x * y + w * z), 1.0 - sc * (x * x + z * z),
+			sc * (y * z - w * x), sc * (x * z - w * y), sc * (y * z + w * x), 1.0 - sc * (x * x + y * y) };
+		const int i = e < 9 ? e / 3 : 0, j = e < 9 ? e % 3 : 0;
+		const double *R0 = rec + PPI_R0;
+		Rij = fma(R0[3 * i], Q[j], fma(R0[3 * i + 1], Q[3 + j], R0[3 * i + 2] * Q[6 + j]));
+	}
+	/* both positions on every lane, then decide64's distance test */
+	double rp_[3], rq_[3], box[3] = { box_in[0], box_in[1], box_in[2] }, ib[3] = { inv_box_in[0], inv_box_in[1], inv_box_in[2] };
+#pragma unroll
+	for(int k = 0; k < 3; k++) {
+		rp_[k] = shfl_d(r[k], 0);
+		rq_[k] = shfl_d(r[k], 16);
+	}
+	if(vol_mask) {
+#pragma unroll
+		for(int k = 0; k < 3; k++)
+			if((vol_mask >> k) & 1) {
+				rp_[k] = __dmul_rn(rp_[k], vol_f3[k]);
+				rq_[k] = __dmul_rn(rq_[k], vol_f3[k]);
+				box[k] = vol_box3[k];
+				ib[k] = rcp64(vol_box3[k]);
+			}
+	}
+	double d[3];
+	int exact = 0;
+#pragma unroll
+	for(int k = 0; k < 3; k++) {
+		d[k] = __dsub_rn(rq_[k], rp_[k]);
+		const double t = d[k] * ib[k], n = rint(t);
+		if(fabs(t - n) > 0.5 - 1e-9) exact = 1; /* rint of d / box could round the other way */
+		d[k] = __dsub_rn(d[k], __dmul_rn(box[k], n));
+	}
+	/* the halves' orientations to every lane that forms a patch (all lanes take part in the shuffles) */
+	double Rm[9];
+#pragma unroll
+	for(int k = 0; k < 9; k++) Rm[k] = shfl_d(Rij, (half << 4) + k);
+	if(exact) return DEC64_EXACT;
+	const double dist2 = __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])), __dmul_rn(d[2], d[2]));
+	if(dist2 < 1.) return -1;
+	if(!(dist2 < rp.sqr_rcut)) return 0;
+	const double in = rsqrt64(dist2);
+	const double u[3] = { d[0] * in, d[1] * in, d[2] * in };
+	const double cmax = rp.cosmax;
+	/* lane e < 4 of each half: patch e of its particle; q's cosines are -(u . patch) */
+	int yes = 0, unsure = 0;
+	if(e < 4) {
+		const double *b = rp.base[e];
+		double c = 0.;
+#pragma unroll
+		for(int k = 0; k < 3; k++) c = fma(u[k], fma(Rm[3 * k], b[0], fma(Rm[3 * k + 1], b[1], Rm[3 * k + 2] * b[2])), c);
+		if(half) c = -c;
+		yes = c > cmax + DEC64_TOL;
+		unsure = fabs(c - cmax) <= DEC64_TOL;
+	}
+	const unsigned by = __ballot_sync(0xffffffffu, yes), bu = __ballot_sync(0xffffffffu, unsure);
+	const int p_yes = (by & 0xfu) != 0, q_yes = (by & 0xf0000u) != 0, p_unsure = (bu & 0xfu) != 0, q_unsure = (bu & 0xf0000u) != 0;
+	/* bond iff some patch of p and some patch of q point at each other (MC.c:249-262) */
+	if(p_yes && q_yes) return 1;
+	if((!p_yes && !p_unsure) || (!q_yes && !q_unsure)) return 0;
+	return DEC64_EXACT;
+}
+
 /* ------------------------------------------------------------------------------------------------ */
 /* FP32 classification with guard band                                                              */
 /* ------------------------------------------------------------------------------------------------ */
@@ -1483,23 +1580,27 @@ __device__ __forceinline__ void tile_round(const ppi_dev &d, TileSmem &S, const 
 		waited = true;
 	}
 	if(S.nc) tile_close<MODE>(d, S, lane, A);
-	/* guard-band pairs: certified FP64 decisions (no division chain); an undecided one defers its attempt */
+	/* guard-band pairs: certified FP64 decisions (no division chain), the whole warp on each pair; an
+	 * undecided one defers its attempt */
 	if(MODE == MODE_FAST) {
 		const int nu = S.nu < TILE_UCAP ? S.nu : TILE_UCAP;
-		for(int u = lane; u < nu; u += 32) {
+#pragma unroll 1
+		for(int u = 0; u < nu; u++) {
 			const int2 v = S.uns[u];
 			const int jq = v.x, a = v.y >> 1, kind = v.y & 1;
-			if(S.flag[a] & (TF_OVER | TF_DEFER)) continue;
+			if(S.flag[a] & (TF_OVER | TF_DEFER)) continue; /* warp-uniform: read after the last __syncwarp */
 			const int r = S.rep[a];
 			const float4 md = S.md[a];
-			A.fallbacks++;
-			const int ex = decide64(d.rec, d.rp[r], d.rs[r].box, d.grid[r].inv_L, __float_as_int(md.w), kind, S.qr[a], make_float3(md.x, md.y, md.z),
-					__float_as_int(d.sori[3 * (size_t) jq + 2].w), 0, nullptr, nullptr);
-			if(ex == DEC64_EXACT) atomicOr(&S.flag[a], TF_DEFER);
-			else if(ex == 1) atomicAdd(kind ? &S.bn[a] : &S.bo[a], 1);
-			else if(ex == -1 && kind) atomicOr(&S.flag[a], TF_OVER);
+			const int ex = decide64_warp(d.rec, d.rp[r], d.rs[r].box, d.grid[r].inv_L, __float_as_int(md.w), kind, S.qr[a], make_float3(md.x, md.y, md.z),
+					__float_as_int(d.sori[3 * (size_t) jq + 2].w), 0, nullptr, nullptr, lane);
+			if(lane == 0) {
+				A.fallbacks++;
+				if(ex == DEC64_EXACT) atomicOr(&S.flag[a], TF_DEFER);
+				else if(ex == 1) atomicAdd(kind ? &S.bn[a] : &S.bo[a], 1);
+				else if(ex == -1 && kind) atomicOr(&S.flag[a], TF_OVER);
+			}
+			__syncwarp();
 		}
-		__syncwarp();
 	}
 	/* decisions and commits of the attempts that are not deferred */
 #pragma unroll 1
@@ -1845,20 +1946,25 @@ __device__ __forceinline__ void kr_iteration(const ppi_dev &d, RoundSmem &S, con
 		kr_cp_wait();
 		__syncwarp();
 	}
-	/* guard-band pairs: certified FP64 decisions; an undecided one defers its attempt */
+	/* guard-band pairs: certified FP64 decisions, the whole warp on each pair; an undecided one defers its
+	 * attempt */
 	const int nu = S.nu < KR_UCAP ? S.nu : KR_UCAP;
-	for(int u = lane; u < nu; u += 32) {
+#pragma unroll 1
+	for(int u = 0; u < nu; u++) {
 		const int2 v = S.uns[u];
 		const int jq = v.x, a = v.y >> 1, kind = v.y & 1;
-		if(S.flag[a] & (TF_OVER | TF_DEFER)) continue;
+		if(S.flag[a] & (TF_OVER | TF_DEFER)) continue; /* warp-uniform: read after the last __syncwarp */
 		const int r = S.rep[a];
 		const float4 md = S.md[a];
-		A.fallbacks++;
-		const int ex = decide64(d.rec, d.rp[r], d.rs[r].box, d.grid[r].inv_L, __float_as_int(md.w), kind, S.qr[a], make_float3(md.x, md.y, md.z),
-				__float_as_int(__ldcg(d.sori + 3 * (size_t) jq + 2).w), 0, nullptr, nullptr);
-		if(ex == DEC64_EXACT) atomicOr(&S.flag[a], TF_DEFER);
-		else if(ex == 1) atomicAdd(kind ? &S.bn[a] : &S.bo[a], 1);
-		else if(ex == -1 && kind) atomicOr(&S.flag[a], TF_OVER);
+		const int ex = decide64_warp(d.rec, d.rp[r], d.rs[r].box, d.grid[r].inv_L, __float_as_int(md.w), kind, S.qr[a], make_float3(md.x, md.y, md.z),
+				__float_as_int(__ldcg(d.sori + 3 * (size_t) jq + 2).w), 0, nullptr, nullptr, lane);
+		if(lane == 0) {
+			A.fallbacks++;
+			if(ex == DEC64_EXACT) atomicOr(&S.flag[a], TF_DEFER);
+			else if(ex == 1) atomicAdd(kind ? &S.bn[a] : &S.bo[a], 1);
+			else if(ex == -1 && kind) atomicOr(&S.flag[a], TF_OVER);
+		}
+		__syncwarp();
 	}
 	__syncwarp();
 	/* decision and commit of the lane's attempt */
@@ -1916,7 +2022,6 @@ __global__ void __launch_bounds__(32 * KR_WARPS, 2) k_round(ppi_dev d, long long
 	RoundSmem &S = ((RoundSmem *) kr_smem)[threadIdx.x >> 5];
 	__shared__ int s_abort;
 	const int lane = threadIdx.x & 31;
-	const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarp = (gridDim.x * blockDim.x) >> 5;
 	const long long limit = d.bar_limit > 0 ? d.bar_limit : KR_LIMIT_DEFAULT;
 	const int4 none = make_int4(-1, 0, 0, 0);
 	Acc A;
@@ -3672,16 +3777,6 @@ __global__ void __launch_bounds__(32 * TILE_WARPS, PPI_VOL_MIN_BLOCKS) k_energy_
 	energy_flush_block(d, A);
 }
 
-/* decide64 and exact_pair out of line, for the flat volume pass: scalar and pointer arguments only, like
- * exact_pair; called only for pairs inside the guard band, so the loop's registers stay low */
-__device__ __noinline__ int decide_exact_vol(const double *rec, const ppi_rparams *rp, const double *box, const ppi_grid *g, int ps, int qs) {
-	const float4 q0 = make_float4(1.f, 0.f, 0.f, 0.f);
-	const float3 d0 = make_float3(0.f, 0.f, 0.f);
-	int ex = decide64(rec, *rp, box, g->inv_L, ps, 0, q0, d0, qs, g->vol_mask, g->vol_f3, g->vol_box3);
-	if(ex == DEC64_EXACT) ex = exact_pair(rec, rp, box, ps, 0, q0, d0, qs, g->vol_mask, g->vol_f3, g->vol_box3, nullptr, nullptr, nullptr);
-	return ex;
-}
-
 /* the candidate box of one replica as the flat volume pass uses it (kept in registers across pairs) */
 struct VolRep {
 	int r, live;       /* replica; live: it has a candidate box this sweep and no overlap was found yet */
@@ -3826,15 +3921,23 @@ __global__ void k_vol_unsure(ppi_dev d) {
 	grid_dep_wait();
 	grid_dep_release();
 	const int n = d.vun_count[0] < d.vun_cap ? d.vun_count[0] : d.vun_cap;
-	for(int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+	/* one warp per pair (decide64_warp); the bit-identical exact test for the rare undecided one */
+	const int lane = threadIdx.x & 31, warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarp = (gridDim.x * blockDim.x) >> 5;
+	const float4 q0 = make_float4(1.f, 0.f, 0.f, 0.f);
+	const float3 d0 = make_float3(0.f, 0.f, 0.f);
+	for(int k = warp; k < n; k += nwarp) {
 		const int2 pr = d.vunsure[k];
 		const int r = d.srep[pr.x];
 		ppi_rstate *rs = d.rs + r;
-		const int x = decide_exact_vol(d.rec, d.rp + r, rs->box, d.grid + r, __float_as_int(d.sori[3 * (size_t) pr.x + 2].w),
-				__float_as_int(d.sori[3 * (size_t) pr.y + 2].w));
-		atomicAdd(&rs->fallbacks, 1ull);
-		if(x == 1) atomicAdd((unsigned long long *) &rs->vol_bonds, 2ull);
-		else if(x == -1) atomicExch(&rs->vol_overlap, 1);
+		const ppi_grid *g = d.grid + r;
+		const int ps = __float_as_int(d.sori[3 * (size_t) pr.x + 2].w), qs = __float_as_int(d.sori[3 * (size_t) pr.y + 2].w);
+		int x = decide64_warp(d.rec, d.rp[r], rs->box, g->inv_L, ps, 0, q0, d0, qs, g->vol_mask, g->vol_f3, g->vol_box3, lane);
+		if(lane == 0) {
+			if(x == DEC64_EXACT) x = exact_pair(d.rec, d.rp + r, rs->box, ps, 0, q0, d0, qs, g->vol_mask, g->vol_f3, g->vol_box3, nullptr, nullptr, nullptr);
+			atomicAdd(&rs->fallbacks, 1ull);
+			if(x == 1) atomicAdd((unsigned long long *) &rs->vol_bonds, 2ull);
+			else if(x == -1) atomicExch(&rs->vol_overlap, 1);
+		}
 	}
 }
 
