@@ -406,12 +406,13 @@ __device__ __forceinline__ int decide64(const double *__restrict__ rec_all, cons
 }
 
 /* decide64 with all 32 lanes of a warp on one pair: every lane calls it with the same arguments and gets
- * the same result. Lanes 0..15 build p's state and lanes 16..31 q's; lane e < 9 of each half forms one
- * entry of its particle's orientation R0 . Q(q) with orient64_fast's operations; lanes 0..3 and 16..19
- * then form one patch cosine each. The values, and so the decision, are decide64's. On this GPU an FP64
+ * the same result. The distance test runs first on every lane (an overlap or a pair out of range needs no
+ * orientation); then lanes 0..15 build p's orientation and 16..31 q's: lanes 0..3 one component each of
+ * the mover's q (x) dq, lane e < 9 of each half one entry of R0 . Q(q), lanes 0..3
+ * and 16..19 one patch cosine each. The values, and so the decision, are decide64's. On this GPU an FP64
  * instruction occupies the FP64 pipe as long for one lane as for 32, so spreading the ~270 FP64
- * operations of one decision over the lanes shortens the warp's wait on it about threefold; one
- * guard-band pair decided by a single lane was the longest chain of a colour pass. */
+ * operations of one decision over the lanes shortens the warp's wait on it several times; one guard-band
+ * pair decided by a single lane was the longest chain of a colour pass. */
 __device__ __forceinline__ double shfl_d(double v, int src) {
 	const int lo = __shfl_sync(0xffffffffu, __double2loint(v), src), hi = __shfl_sync(0xffffffffu, __double2hiint(v), src);
 	return __hiloint2double(hi, lo);
@@ -421,32 +422,13 @@ __device__ __forceinline__ int decide64_warp(const double *__restrict__ rec_all,
 		float4 dq, float3 disp, int qs, int vol_mask, const double *vol_f3, const double *vol_box3, int lane) {
 	const int half = lane >> 4, e = lane & 15;
 	const double *rec = rec_all + (size_t) (half ? qs : ps) * PPI_REC;
-	/* this half's particle: position and quaternion (state64_fast) */
-	double q[4] = { rec[PPI_Q], rec[PPI_Q + 1], rec[PPI_Q + 2], rec[PPI_Q + 3] };
+	/* positions first: the distance test alone decides an overlap or a pair out of range */
 	double r[3] = { rec[0], rec[1], rec[2] };
 	if(half == 0 && kind == 1) {
-		const double b[4] = { f2d(dq.x), f2d(dq.y), f2d(dq.z), f2d(dq.w) };
-		double qn[4];
-#pragma unroll
-		for(int c = 0; c < 4; c++) qn[c] = qcomp64(q[c], q[c ^ 1], q[c ^ 2], q[c ^ 3], b, c);
-#pragma unroll
-		for(int c = 0; c < 4; c++) q[c] = qn[c];
 		r[0] = __dadd_rn(r[0], f2d(disp.x));
 		r[1] = __dadd_rn(r[1], f2d(disp.y));
 		r[2] = __dadd_rn(r[2], f2d(disp.z));
 	}
-	/* entry (i, j) = e of R = R0 . Q(q), orient64_fast's operations */
-	double Rij;
-	{
-		const double w = q[0], x = q[1], y = q[2], z = q[3];
-		const double sc = 2.0 * rcp64(w * w + x * x + y * y + z * z);
-		const double Q[9] = { 1.0 - sc * (y * y + z * z), sc * (x * y - w * z), sc * (x * z + w * y), sc * (x * y + w * z), 1.0 - sc * (x * x + z * z),
-			sc * (y * z - w * x), sc * (x * z - w * y), sc * (y * z + w * x), 1.0 - sc * (x * x + y * y) };
-		const int i = e < 9 ? e / 3 : 0, j = e < 9 ? e % 3 : 0;
-		const double *R0 = rec + PPI_R0;
-		Rij = fma(R0[3 * i], Q[j], fma(R0[3 * i + 1], Q[3 + j], R0[3 * i + 2] * Q[6 + j]));
-	}
-	/* both positions on every lane, then decide64's distance test */
 	double rp_[3], rq_[3], box[3] = { box_in[0], box_in[1], box_in[2] }, ib[3] = { inv_box_in[0], inv_box_in[1], inv_box_in[2] };
 #pragma unroll
 	for(int k = 0; k < 3; k++) {
@@ -472,14 +454,38 @@ __device__ __forceinline__ int decide64_warp(const double *__restrict__ rec_all,
 		if(fabs(t - n) > 0.5 - 1e-9) exact = 1; /* rint of d / box could round the other way */
 		d[k] = __dsub_rn(d[k], __dmul_rn(box[k], n));
 	}
-	/* the halves' orientations to every lane that forms a patch (all lanes take part in the shuffles) */
-	double Rm[9];
-#pragma unroll
-	for(int k = 0; k < 9; k++) Rm[k] = shfl_d(Rij, (half << 4) + k);
 	if(exact) return DEC64_EXACT;
 	const double dist2 = __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])), __dmul_rn(d[2], d[2]));
 	if(dist2 < 1.) return -1;
 	if(!(dist2 < rp.sqr_rcut)) return 0;
+	/* this half's quaternion (state64_fast): lane c < 4 of half 0 forms component c of q (x) dq */
+	double q[4] = { rec[PPI_Q], rec[PPI_Q + 1], rec[PPI_Q + 2], rec[PPI_Q + 3] };
+	if(kind == 1) {
+		const double b[4] = { f2d(dq.x), f2d(dq.y), f2d(dq.z), f2d(dq.w) };
+		const int c = e & 3;
+		const double qc = qcomp64(q[c], q[c ^ 1], q[c ^ 2], q[c ^ 3], b, c);
+		double qn[4];
+#pragma unroll
+		for(int k = 0; k < 4; k++) qn[k] = shfl_d(qc, k);
+		if(half == 0)
+#pragma unroll
+			for(int k = 0; k < 4; k++) q[k] = qn[k];
+	}
+	/* entry (i, j) = e of R = R0 . Q(q), orient64_fast's operations */
+	double Rij;
+	{
+		const double w = q[0], x = q[1], y = q[2], z = q[3];
+		const double sc = 2.0 * rcp64(w * w + x * x + y * y + z * z);
+		const double Q[9] = { 1.0 - sc * (y * y + z * z), sc * (x * y - w * z), sc * (x * z + w * y), sc * (x * y + w * z), 1.0 - sc * (x * x + z * z),
+			sc * (y * z - w * x), sc * (x * z - w * y), sc * (y * z + w * x), 1.0 - sc * (x * x + y * y) };
+		const int i = e < 9 ? e / 3 : 0, j = e < 9 ? e % 3 : 0;
+		const double *R0 = rec + PPI_R0;
+		Rij = fma(R0[3 * i], Q[j], fma(R0[3 * i + 1], Q[3 + j], R0[3 * i + 2] * Q[6 + j]));
+	}
+	/* the halves' orientations to every lane that forms a patch (all lanes take part in the shuffles) */
+	double Rm[9];
+#pragma unroll
+	for(int k = 0; k < 9; k++) Rm[k] = shfl_d(Rij, (half << 4) + k);
 	const double in = rsqrt64(dist2);
 	const double u[3] = { d[0] * in, d[1] * in, d[2] * in };
 	const double cmax = rp.cosmax;
