@@ -101,6 +101,44 @@ __device__ __forceinline__ double u01d(uint32_t a, uint32_t b) { return (double)
 __device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void grid_dep_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
+/* L2 eviction priorities for the colour pass: the FP32 working records (spos, sori), which every colour
+ * launch gathers again, are loaded with evict_last; the per-launch streams (colour lists, neighbour
+ * lists) with evict_first, so that they do not push the records out of L2 between launches */
+#ifndef PPI_L2HINT
+#define PPI_L2HINT 1
+#endif
+__device__ __forceinline__ uint64_t l2_keep() {
+	uint64_t p;
+	asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+	return p;
+}
+
+__device__ __forceinline__ uint64_t l2_stream() {
+	uint64_t p;
+	asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+	return p;
+}
+
+__device__ __forceinline__ float4 ld_keep(const float4 *a) {
+#if PPI_L2HINT
+	float4 v;
+	asm volatile("ld.global.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(a), "l"(l2_keep()));
+	return v;
+#else
+	return *a;
+#endif
+}
+
+__device__ __forceinline__ int4 ld_stream(const int4 *a) {
+#if PPI_L2HINT
+	int4 v;
+	asm volatile("ld.global.L2::cache_hint.v4.s32 {%0, %1, %2, %3}, [%4], %5;" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(a), "l"(l2_stream()));
+	return v;
+#else
+	return *a;
+#endif
+}
+
 /* ------------------------------------------------------------------------------------------------ */
 /* Reference-exact FP64 pair test: MC_would_interact (MC.c:232-266) with the patches of              */
 /* MATRIX_VECTOR_MULTIPLICATION (utils.h:17-21). Every operation is an explicitly rounded IEEE        */
@@ -1065,7 +1103,7 @@ __device__ __forceinline__ void propose(const ppi_dev &d, const int4 ent, long l
 	/* the attempt's Philox draws: particle + displacement, rotation (acceptance only when needed) */
 	const U4 r1 = rng(rp, round, P.r, TAG_MOVE, (uint32_t) P.local, 0u), r2 = rng(rp, round, P.r, TAG_MOVE, (uint32_t) P.local, 1u);
 	P.i = c0 + (int) __umulhi(r1.x, (uint32_t) cnt);
-	P.po = d.spos[P.i];
+	P.po = ld_keep(d.spos + P.i);
 	const float dm = rp.disp_max_f;
 	P.disp = make_float3((u01(r1.y) - 0.5f) * dm, (u01(r1.z) - 0.5f) * dm, (u01(r1.w) - 0.5f) * dm);
 	const float nx = P.po.x + P.disp.x, ny = P.po.y + P.disp.y, nz = P.po.z + P.disp.z;
@@ -1074,7 +1112,7 @@ __device__ __forceinline__ void propose(const ppi_dev &d, const int4 ent, long l
 	P.pslot = 0;
 	P.q = make_float4(1.f, 0.f, 0.f, 0.f);
 	if(P.inside) {
-		const float4 ob = d.sori[3 * (size_t) P.i], oc = d.sori[3 * (size_t) P.i + 1], od = d.sori[3 * (size_t) P.i + 2];
+		const float4 ob = ld_keep(d.sori + 3 * (size_t) P.i), oc = ld_keep(d.sori + 3 * (size_t) P.i + 1), od = ld_keep(d.sori + 3 * (size_t) P.i + 2);
 		P.pslot = __float_as_int(od.w);
 		/* rotation: angle uniform in [0, Theta_max), axis uniform on the sphere (inversion method) */
 		const float theta = u01(r2.x) * rp.theta_max_f;
@@ -1260,7 +1298,7 @@ __device__ __forceinline__ void tile_close(const ppi_dev &d, TileSmem &S, int la
 		if(S.flag[a] & (TF_OVER | TF_DEFER)) continue;
 		const int jq = S.mi[a] + (en >> 10);
 		const ppi_rparams &rp = d.rp[S.rep[a]];
-		const float4 qa = d.spos[jq], qb = d.sori[3 * (size_t) jq], qc = d.sori[3 * (size_t) jq + 1], qd = d.sori[3 * (size_t) jq + 2];
+		const float4 qa = ld_keep(d.spos + jq), qb = ld_keep(d.sori + 3 * (size_t) jq), qc = ld_keep(d.sori + 3 * (size_t) jq + 1), qd = ld_keep(d.sori + 3 * (size_t) jq + 2);
 		const float cq[9] = { qb.x, qb.y, qb.z, qb.w, qc.x, qc.y, qc.z, qc.w, qd.x };
 		const PairGeo G = pair_geo(S, a, t, qa);
 		const float eps = rp.precision == 1 ? 1e30f : rp.eps_f;
@@ -1425,7 +1463,7 @@ __device__ __forceinline__ void tile_steps(const ppi_dev &d, TileSmem &S, const 
 				en[u] = S.pbuf[p];
 				const int a = (en[u] >> 4) & 63, off = en[u] >> 10;
 				ok[u] = off != 0 && !(S.flag[a] & (TF_OVER | TF_DEFER));
-				if(ok[u]) qa[u] = d.spos[S.mi[a] + off];
+				if(ok[u]) qa[u] = ld_keep(d.spos + (S.mi[a] + off));
 			}
 		}
 		int close[PSTEP];
@@ -1475,7 +1513,7 @@ __device__ __forceinline__ void write_list_pairs(const ppi_dev &d, TileSmem &S, 
 	for(int k0 = 0; k0 < n; k0 += 32) { /* up to 32 entries' loads at once: one latency for a list */
 		int4 v[8];
 #pragma unroll
-		for(int c = 0; c < 8; c++) v[c] = (k0 + 4 * c < n) ? L[(k0 >> 2) + c] : make_int4(0, 0, 0, 0);
+		for(int c = 0; c < 8; c++) v[c] = (k0 + 4 * c < n) ? ld_stream(L + (k0 >> 2) + c) : make_int4(0, 0, 0, 0);
 #pragma unroll
 		for(int c = 0; c < 8; c++) {
 			const int e4[4] = { v[c].x, v[c].y, v[c].z, v[c].w };
@@ -1663,8 +1701,8 @@ __global__ void __launch_bounds__(32 * TILE_WARPS, MODE == MODE_FAST ? PPI_TILE_
 	__syncwarp();
 	bool waited = false;
 	for(int b = lo; b < hi; b += TA) {
-		const int4 e0 = (b + lane < hi) ? list[b + lane] : none;
-		const int4 e1 = (b + 32 + lane < hi) ? list[b + 32 + lane] : none;
+		const int4 e0 = (b + lane < hi) ? ld_stream(list + b + lane) : none;
+		const int4 e1 = (b + 32 + lane < hi) ? ld_stream(list + b + 32 + lane) : none;
 		tile_round<MODE, LIST>(d, S, lane, e0, e1, b, col, round, A, waited);
 		__syncwarp();
 	}
