@@ -56,6 +56,9 @@ class _Engine:
     def kernel_stats(self, reset=False):
         return {"sweep_ms": 1.0, "sweep_launches": 1, "sort_ms": 0.0, "sort_launches": 0, "volume_ms": 0.0, "volume_launches": 0}
 
+    def guard_stats(self, reset=False):
+        return {"pairs": 0, "fallbacks": 0, "mismatches": 0, "max_err_r2": 0.0, "max_err_cos": 0.0, "nl_overflows": 0}
+
     def close(self):
         pass
 
