@@ -295,7 +295,7 @@ static void drop_graphs(pp_engine *e);
 
 static void free_device(pp_engine *e) {
 	void **ptrs[] = { (void **) &e->d.rec, (void **) &e->d.spos, (void **) &e->d.sori, (void **) &e->d.id, (void **) &e->d.rep, (void **) &e->d.cellof,
-		(void **) &e->d.cell_count, (void **) &e->d.cell_start, (void **) &e->d.cell_cursor, (void **) &e->d.cell_rep, (void **) &e->d.scan_aux,
+		(void **) &e->d.cell_count, (void **) &e->d.cell_start, (void **) &e->d.cell_part, (void **) &e->d.cell_rep, (void **) &e->d.scan_aux,
 		(void **) &e->d.clist, (void **) &e->d.ccount, (void **) &e->d.dflag, (void **) &e->d.eflag, (void **) &e->d.rp, (void **) &e->d.rs, (void **) &e->d.grid, (void **) &e->d.out_bonds,
 		(void **) &e->d.out_overlaps, (void **) &e->d.out_partners, (void **) &e->d.tmp_rec, (void **) &e->d.tmp_id, (void **) &e->d.avb_head,
 		(void **) &e->d.avb_next, (void **) &e->d.avb_cell, (void **) &e->d.vm_old, (void **) &e->d.vm_links, (void **) &e->d.vm_pre,
@@ -745,11 +745,11 @@ static int commit(pp_engine *e) {
 	CU(cudaMalloc((void **) &d->tmp_id, sizeof(int) * n1));
 	CU(cudaMalloc((void **) &d->cell_count, sizeof(int) * cells));
 	CU(cudaMalloc((void **) &d->cell_start, sizeof(int) * (cells + 1)));
-	CU(cudaMalloc((void **) &d->cell_cursor, sizeof(int) * cells));
+	CU(cudaMalloc((void **) &d->cell_part, sizeof(int) * cells));
 	CU(cudaMalloc((void **) &d->cell_rep, sizeof(int) * cells));
 	CU(cudaMalloc((void **) &d->scan_aux, sizeof(int) * ((cells + 1023) / 1024 + 1)));
 	CU(cudaMalloc((void **) &d->clist, sizeof(int4) * 8 * (size_t) d->clist_cap));
-	CU(cudaMalloc((void **) &d->ccount, sizeof(int) * 8));
+	CU(cudaMalloc((void **) &d->ccount, sizeof(int) * 16)); /* 8 colour counts, the scan ticket */
 	CU(cudaMalloc((void **) &d->dflag, 8 * (size_t) d->clist_cap));
 	CU(cudaMemsetAsync(d->dflag, 0, 8 * (size_t) d->clist_cap, e->stream));
 	CU(cudaMalloc((void **) &d->eflag, n1));

@@ -105,6 +105,8 @@ typedef struct ppi_grid {
 	float pad;
 	float inv_wf[3], inv_Lf[3], Lf[3]; /* FP32 copies for the cell assignment's guesses */
 	float pad4;
+	float shiftf[3];   /* FP32 copy of shift (the cell assignment's guesses) */
+	float pad5;
 	/* candidate box of the current sweep's NPT volume move (MC.c:456-472) or Lx move (MC.c:520-537) */
 	int vol_dir;       /* NPT: the scaled axis; PPI_LX_DIR: Lx move; -1: no candidate */
 	int vol_mask;      /* bit k: axis k is scaled in the candidate box */
@@ -158,11 +160,11 @@ typedef struct ppi_dev {
 	int *cellof;       /* slot -> global cell (current grid) */
 	int *cell_count;
 	int *cell_start;   /* total_cells + 1 */
-	int *cell_cursor;
+	int *cell_part;    /* k_scan's tile-local exclusive prefix of cell_count */
 	int *cell_rep;     /* global cell -> replica */
 	int *scan_aux;
 	int4 *clist;       /* 8 lists of capacity clist_cap each */
-	int *ccount;       /* 8 counters */
+	int *ccount;       /* 8 colour-list counters, [8]: k_scan's ticket */
 	unsigned char *dflag; /* 8 x clist_cap: deferred attempts a warp could not keep in shared memory */
 	unsigned char *eflag; /* ntot: the same for particles of the energy pass */
 	int audit_any;     /* some replica audits: every pass runs in audit mode */

@@ -658,6 +658,7 @@ __global__ void k_grid(ppi_dev d, long long epoch) {
 		g->w[a] = w;
 		g->wf[a] = (float) w;
 		g->shift[a] = (double) us[a] * w;
+		g->shiftf[a] = (float) g->shift[a];
 		g->inv_w[a] = 1.0 / w;
 		g->inv_L[a] = 1.0 / rs->box[a];
 		g->inv_wf[a] = (float) g->inv_w[a];
@@ -675,10 +676,12 @@ __device__ __forceinline__ float d2f_trunc(double x) {
 	return __uint_as_float(((uint32_t) (u >> 32) & 0x80000000u) | ((uint32_t) e << 23) | ((uint32_t) (u >> 29) & 0x7fffffu));
 }
 
-/* cell of a slot in the current grid and its cell-local coordinates (FP32). Per axis: the periodic
- * image and the cell index are guessed in FP32 and the FP64 work is four operations (image, grid origin,
- * cell origin, local offset); the FP32 local coordinate is then checked to lie in [0, w) and the cell
- * index corrected if it does not (the FP64 pipe is the scarce resource on this GPU). */
+/* cell of a slot in the current grid and its cell-local coordinates (FP32). The FP64 pipe is the scarce
+ * resource on this GPU, so per axis the periodic image and the cell are first estimated in FP32: where
+ * the estimate lies farther than its error bound m from the box and cell boundaries, both are certain and
+ * the FP64 work is three explicitly rounded operations (image, grid origin, cell origin). Otherwise the
+ * image and the cell are found by the careful path: FP32 guesses of both, each checked against the FP64
+ * value and corrected. |estimate - exact| <= 2^-23 |x| + 2^-24 (|k| + 3) L, and m is ~8x that. */
 __global__ void k_assign(ppi_dev d, float4 *tmp) {
 	grid_dep_wait(); /* chained by programmatic dependent launch (ppi_resort) */
 	grid_dep_release();
@@ -697,19 +700,39 @@ __global__ void k_assign(ppi_dev d, float4 *tmp) {
 		const int n = g.n[a];
 		const float Lf = g.Lf[a], wf = g.wf[a];
 		/* periodic image: x - k L in [0, L) */
-		const float kf = floorf(d2f_trunc(xs[a]) * g.inv_Lf[a]);
-		double y = __fma_rn(-f2d(kf), L, xs[a]) - g.shift[a];
-		float yf = d2f_trunc(y);
-		if(yf < 0.f) y += L;
-		else if(yf >= Lf) y -= L;
-		yf = d2f_trunc(y);
-		if(yf < 0.f) y += L; /* a guess of k off by one in both steps: one more image */
-		else if(yf >= Lf) y -= L;
-		int ci = (int) (d2f_trunc(y) * g.inv_wf[a]);
-		ci = ci < 0 ? 0 : (ci > n - 1 ? n - 1 : ci);
-		float lf = d2f(y - f2d((float) ci) * w);
-		if(lf < 0.f && ci > 0) lf = d2f(y - f2d((float) --ci) * w);
-		else if(lf >= wf && ci < n - 1) lf = d2f(y - f2d((float) ++ci) * w);
+		const float xf = d2f_trunc(xs[a]);
+		const float kf = floorf(xf * g.inv_Lf[a]);
+		const float yg = fmaf(-kf, Lf, xf) - g.shiftf[a];
+		const float cg = floorf(yg * g.inv_wf[a]);
+		const float lg = fmaf(-cg, wf, yg);
+		const float m = 1e-6f * (fabsf(xf) + (fabsf(kf) + 3.f) * Lf);
+		int ci;
+		float lf;
+		if(__builtin_expect(yg >= m && yg < Lf - m && lg >= m && lg < wf - m && cg < (float) n, 1)) {
+			ci = (int) cg;
+			const double y = __dadd_rn(__fma_rn(-f2d(kf), L, xs[a]), -g.shift[a]);
+			lf = d2f(__fma_rn(-f2d(cg), w, y));
+		}
+		else {
+			double y = __dadd_rn(__fma_rn(-f2d(kf), L, xs[a]), -g.shift[a]);
+			float yf = d2f_trunc(y);
+			if(yf < 0.f) y += L;
+			else if(yf >= Lf) y -= L;
+			yf = d2f_trunc(y);
+			if(yf < 0.f) y += L; /* a guess of k off by one in both steps: one more image */
+			else if(yf >= Lf) y -= L;
+			ci = (int) (d2f_trunc(y) * g.inv_wf[a]);
+			ci = ci < 0 ? 0 : (ci > n - 1 ? n - 1 : ci);
+			lf = d2f(__fma_rn(-f2d((float) ci), w, y));
+			if(lf < 0.f && ci > 0) {
+				--ci;
+				lf = d2f(__fma_rn(-f2d((float) ci), w, y));
+			}
+			else if(lf >= wf && ci < n - 1) {
+				++ci;
+				lf = d2f(__fma_rn(-f2d((float) ci), w, y));
+			}
+		}
 		c[a] = ci;
 		l[a] = lf;
 	}
@@ -745,41 +768,65 @@ __device__ __forceinline__ int block_scan_incl(int v, int *ws) {
 	return v;
 }
 
-__global__ void __launch_bounds__(SCAN_B) k_scan_local(const int *in, int *out, int *cursor, int *aux, int n) {
-	grid_dep_wait(); /* chained by programmatic dependent launch (ppi_resort) */
-	grid_dep_release();
-	__shared__ int ws[SCAN_B / 32];
-	const int i = blockIdx.x * SCAN_B + threadIdx.x;
-	const int v = (i < n) ? in[i] : 0;
-	const int x = block_scan_incl(v, ws);
-	if(i < n) {
-		out[i] = x - v;
-		cursor[i] = 0;
-	}
-	if(threadIdx.x == SCAN_B - 1) aux[blockIdx.x] = x;
-}
+#define SCAN_T 4                    /* cells per thread of the scan */
+#define SCAN_TILE (SCAN_B * SCAN_T) /* cells per CTA */
+#define SCAN_SHIFT 12               /* log2(SCAN_TILE) */
 
-__global__ void __launch_bounds__(SCAN_B) k_scan_top(int *aux, int nblocks, int *total_out) {
+/* Cell starts in one launch: every CTA scans its tile of SCAN_TILE cell counts (the tile-local exclusive
+ * prefix goes to part) and publishes the tile's total in aux; the CTA that finishes last (a ticket counter,
+ * zeroed before the sort) turns aux into the tiles' exclusive offsets and writes the grand total to
+ * *total_out, the end of the last cell. The start of cell c is then part[c] + aux[c >> SCAN_SHIFT]:
+ * k_scatter reads it so, and k_cellfin writes it to cell_start for every later reader. */
+__global__ void __launch_bounds__(SCAN_B) k_scan(const int *in, int *part, int *aux, int *ticket, int *total_out, int n) {
 	grid_dep_wait(); /* chained by programmatic dependent launch (ppi_resort) */
 	grid_dep_release();
 	__shared__ int ws[SCAN_B / 32];
+	__shared__ int s_last;
+	const int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_T;
+	int v[SCAN_T];
+	const bool full = base + SCAN_T <= n;
+	if(full) {
+		const int4 q = *(const int4 *) (in + base);
+		v[0] = q.x;
+		v[1] = q.y;
+		v[2] = q.z;
+		v[3] = q.w;
+	}
+	else {
+#pragma unroll
+		for(int k = 0; k < SCAN_T; k++) v[k] = base + k < n ? in[base + k] : 0;
+	}
+	const int tsum = v[0] + v[1] + v[2] + v[3];
+	const int x = block_scan_incl(tsum, ws);
+	int p[SCAN_T];
+	p[0] = x - tsum;
+#pragma unroll
+	for(int k = 1; k < SCAN_T; k++) p[k] = p[k - 1] + v[k - 1];
+	if(full) *(int4 *) (part + base) = make_int4(p[0], p[1], p[2], p[3]);
+	else {
+#pragma unroll
+		for(int k = 0; k < SCAN_T; k++)
+			if(base + k < n) part[base + k] = p[k];
+	}
+	if(threadIdx.x == SCAN_B - 1) {
+		aux[blockIdx.x] = x;
+		__threadfence(); /* the tile total is visible before the ticket is taken */
+		s_last = atomicAdd(ticket, 1) == (int) gridDim.x - 1;
+	}
+	__syncthreads();
+	if(!s_last) return;
+	__threadfence(); /* every other tile's total was published before its ticket */
 	int carry = 0;
-	for(int base = 0; base < nblocks; base += SCAN_B) {
-		const int i = base + threadIdx.x;
-		const int v = (i < nblocks) ? aux[i] : 0;
-		const int x = block_scan_incl(v, ws);
-		if(i < nblocks) aux[i] = carry + x - v;
+	const int nblocks = gridDim.x;
+	for(int b0 = 0; b0 < nblocks; b0 += SCAN_B) {
+		const int i = b0 + threadIdx.x;
+		const int t = (i < nblocks) ? __ldcg(aux + i) : 0;
+		const int y = block_scan_incl(t, ws);
+		if(i < nblocks) aux[i] = carry + y - t;
 		carry += ws[SCAN_B / 32 - 1]; /* the chunk's total */
 		__syncthreads();
 	}
 	if(threadIdx.x == 0) *total_out = carry;
-}
-
-__global__ void k_scan_add(int *out, const int *aux, int n) {
-	grid_dep_wait(); /* chained by programmatic dependent launch (ppi_resort) */
-	grid_dep_release();
-	int i = blockIdx.x * SCAN_B + threadIdx.x;
-	if(i < n) out[i] += aux[blockIdx.x];
 }
 
 /* FP32 working record of slot s at sorted position pos: cell-local position from k_assign, orientation
@@ -791,17 +838,20 @@ __global__ void k_scatter(ppi_dev d, const float4 *tmp) {
 	if(s >= d.ntot) return;
 	int gc = d.cellof[s];
 	float4 a = tmp[s];
-	int pos = d.cell_start[gc] + __float_as_int(a.w);
+	int pos = d.cell_part[gc] + d.scan_aux[gc >> SCAN_SHIFT] + __float_as_int(a.w); /* cell start (k_scan) + arrival rank */
 	const double *rec = d.rec + (size_t) s * PPI_REC;
 	{ /* .w = the cell's x index (neighbour offsets in the colour pass) */
 		const int r = d.rep[s];
 		a.w = __int_as_float((gc - d.rp[r].cell_base) % d.grid[r].n[0]);
 		if(d.srep) d.srep[pos] = r;
 	}
-	float R0[9], Q[9];
-#pragma unroll
-	for(int k = 0; k < 9; k++) R0[k] = d2f(rec[PPI_R0 + k]);
-	const float w = d2f(rec[PPI_Q]), x = d2f(rec[PPI_Q + 1]), y = d2f(rec[PPI_Q + 2]), z = d2f(rec[PPI_Q + 3]);
+	static_assert(PPI_Q == 3 && PPI_R0 == 7 && PPI_REC == 16, "record layout");
+	/* doubles 2..15 of the 128 B record in seven 16 B loads: q = 3..6, R0 = 7..15 */
+	const double2 *r2 = (const double2 *) rec;
+	const double2 v1 = r2[1], v2 = r2[2], v3 = r2[3], v4 = r2[4], v5 = r2[5], v6 = r2[6], v7 = r2[7];
+	const float R0[9] = { d2f(v3.y), d2f(v4.x), d2f(v4.y), d2f(v5.x), d2f(v5.y), d2f(v6.x), d2f(v6.y), d2f(v7.x), d2f(v7.y) };
+	float Q[9];
+	const float w = d2f(v1.y), x = d2f(v2.x), y = d2f(v2.y), z = d2f(v3.x);
 	const float sc = 2.f / (w * w + x * x + y * y + z * z);
 	Q[0] = 1.f - sc * (y * y + z * z);
 	Q[1] = sc * (x * y - w * z);
@@ -837,32 +887,19 @@ __global__ void __launch_bounds__(CELLFIN_B) k_cellfin(ppi_dev d) {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	int col = -1, a_out = 0, b_out = 0, rep_out = 0;
 	if(gc < d.total_cells) {
+		/* the cell's start from k_scan's tile prefix and tile offset, written out for every later reader
+		 * (the end of the last cell, cell_start[total_cells], was written by k_scan) */
+		const int a = d.cell_part[gc] + d.scan_aux[gc >> SCAN_SHIFT];
+		const int b = gc + 1 < d.total_cells ? d.cell_part[gc + 1] + d.scan_aux[(gc + 1) >> SCAN_SHIFT] : d.cell_start[gc + 1];
+		d.cell_start[gc] = a;
 		const int r = d.cell_rep[gc];
 		const ppi_grid &g = d.grid[r];
 		const int local = gc - d.rp[r].cell_base;
 		if(local < g.ncells) {
-			const int a = d.cell_start[gc], b = d.cell_start[gc + 1];
 			a_out = a;
 			b_out = b;
 			rep_out = r;
 			if(b > a) {
-				float4 *P = d.spos, *O = d.sori;
-				for(int i = a + 1; i < b; i++) {
-					const float4 x0 = P[i], x1 = O[3 * i], x2 = O[3 * i + 1], x3 = O[3 * i + 2];
-					const int key = __float_as_int(x3.y);
-					int j = i - 1;
-					while(j >= a && __float_as_int(O[3 * j + 2].y) > key) {
-						P[j + 1] = P[j];
-						O[3 * (j + 1)] = O[3 * j];
-						O[3 * (j + 1) + 1] = O[3 * j + 1];
-						O[3 * (j + 1) + 2] = O[3 * j + 2];
-						j--;
-					}
-					P[j + 1] = x0;
-					O[3 * (j + 1)] = x1;
-					O[3 * (j + 1) + 1] = x2;
-					O[3 * (j + 1) + 2] = x3;
-				}
 				const int cx = local % g.n[0], cy = (local / g.n[0]) % g.n[1], cz = local / (g.n[0] * g.n[1]);
 				col = (cx & 1) | ((cy & 1) << 1) | ((cz & 1) << 2);
 			}
@@ -890,6 +927,27 @@ __global__ void __launch_bounds__(CELLFIN_B) k_cellfin(ppi_dev d) {
 	if(col >= 0) {
 		const int idx = s_base[col] + s_cnt[warp][col] + rank;
 		if(idx < d.clist_cap) d.clist[(size_t) col * d.clist_cap + idx] = make_int4(gc, a_out, b_out - a_out, rep_out);
+	}
+	/* the cell's records by ascending id (after the CTA's barriers: the other warps do not wait for it) */
+	if(b_out - a_out > 1) {
+		const int a = a_out, b = b_out;
+		float4 *P = d.spos, *O = d.sori;
+		for(int i = a + 1; i < b; i++) {
+			const float4 x0 = P[i], x1 = O[3 * i], x2 = O[3 * i + 1], x3 = O[3 * i + 2];
+			const int key = __float_as_int(x3.y);
+			int j = i - 1;
+			while(j >= a && __float_as_int(O[3 * j + 2].y) > key) {
+				P[j + 1] = P[j];
+				O[3 * (j + 1)] = O[3 * j];
+				O[3 * (j + 1) + 1] = O[3 * j + 1];
+				O[3 * (j + 1) + 2] = O[3 * j + 2];
+				j--;
+			}
+			P[j + 1] = x0;
+			O[3 * (j + 1)] = x1;
+			O[3 * (j + 1) + 1] = x2;
+			O[3 * (j + 1) + 2] = x3;
+		}
 	}
 }
 
@@ -4074,6 +4132,7 @@ __device__ void grid_scale_axis(ppi_grid *g, ppi_rstate *rs, int a) {
 	rs->box[a] = g->vol_box3[a];
 	g->w[a] *= f;
 	g->shift[a] *= f;
+	g->shiftf[a] = (float) g->shift[a];
 	g->wf[a] = (float) g->w[a];
 	g->inv_w[a] = 1.0 / g->w[a];
 	g->inv_L[a] = 1.0 / rs->box[a];
@@ -4124,26 +4183,27 @@ __global__ void k_vol_decide(ppi_dev d, long long sweep) {
 __global__ void k_vol_apply(ppi_dev d) {
 	grid_dep_wait();
 	grid_dep_release();
-	int k = blockIdx.x * blockDim.x + threadIdx.x;
-	if(k >= d.ntot || !d.ctr->vol_any) return; /* every replica rejected its candidate box: nothing to rescale */
-	/* canonical positions (slot k): p->r[a] *= rescale_factor (MC.c:477, MC.c:541-544) */
-	int r = d.rep[k];
-	if(d.rs[r].vol_accept) {
-		const ppi_grid &g = d.grid[r];
-		double *rec = d.rec + (size_t) k * PPI_REC;
-		for(int a = 0; a < 3; a++)
-			if((g.vol_mask >> a) & 1) rec[a] = __dmul_rn(rec[a], g.vol_f3[a]);
-	}
-	/* working record (sorted position k) */
-	int gc = __float_as_int(d.sori[3 * (size_t) k + 2].z);
-	int r2 = d.cell_rep[gc];
-	if(d.rs[r2].vol_accept) {
-		const ppi_grid &g = d.grid[r2];
-		float4 a = d.spos[k];
-		a.x *= g.vol_ff3[0];
-		a.y *= g.vol_ff3[1];
-		a.z *= g.vol_ff3[2];
-		d.spos[k] = a;
+	if(!d.ctr->vol_any) return; /* every replica rejected its candidate box: nothing to rescale */
+	for(int k = blockIdx.x * blockDim.x + threadIdx.x; k < d.ntot; k += gridDim.x * blockDim.x) {
+		/* canonical positions (slot k): p->r[a] *= rescale_factor (MC.c:477, MC.c:541-544) */
+		int r = d.rep[k];
+		if(d.rs[r].vol_accept) {
+			const ppi_grid &g = d.grid[r];
+			double *rec = d.rec + (size_t) k * PPI_REC;
+			for(int a = 0; a < 3; a++)
+				if((g.vol_mask >> a) & 1) rec[a] = __dmul_rn(rec[a], g.vol_f3[a]);
+		}
+		/* working record (sorted position k) */
+		int gc = __float_as_int(d.sori[3 * (size_t) k + 2].z);
+		int r2 = d.cell_rep[gc];
+		if(d.rs[r2].vol_accept) {
+			const ppi_grid &g = d.grid[r2];
+			float4 a = d.spos[k];
+			a.x *= g.vol_ff3[0];
+			a.y *= g.vol_ff3[1];
+			a.z *= g.vol_ff3[2];
+			d.spos[k] = a;
+		}
 	}
 }
 
@@ -5215,19 +5275,17 @@ static void launch_pdl(void (*kern)(KArgs...), int grid, int block, cudaStream_t
 extern "C" int ppi_resort(const ppi_dev *d, long long epoch, cudaStream_t s, long long *nl) {
 	float4 *tmp = (float4 *) d->tmp_rec; /* ntot float4 fit in the reorder scratch */
 	cudaMemsetAsync(d->cell_count, 0, sizeof(int) * (size_t) d->total_cells, s);
-	cudaMemsetAsync(d->ccount, 0, sizeof(int) * 8, s);
+	cudaMemsetAsync(d->ccount, 0, sizeof(int) * 9, s); /* the 8 colour counts and k_scan's ticket */
 	k_grid<<<(d->nrep + 63) / 64, 64, 0, s>>>(*d, epoch);
 	/* the rest of the sort is one chain of kernels, each launch overlapping its predecessor's tail
 	 * (programmatic dependent launch; every kernel waits before its first access) */
 	int nb = (d->ntot + 255) / 256;
 	if(nb > 0) launch_pdl(k_assign, nb, 256, s, *d, tmp);
-	int sb = (d->total_cells + SCAN_B - 1) / SCAN_B;
-	launch_pdl(k_scan_local, sb, SCAN_B, s, (const int *) d->cell_count, d->cell_start, d->cell_cursor, d->scan_aux, d->total_cells);
-	launch_pdl(k_scan_top, 1, SCAN_B, s, d->scan_aux, sb, d->cell_start + d->total_cells);
-	launch_pdl(k_scan_add, sb, SCAN_B, s, d->cell_start, (const int *) d->scan_aux, d->total_cells);
+	int sb = (d->total_cells + SCAN_TILE - 1) / SCAN_TILE;
+	launch_pdl(k_scan, sb, SCAN_B, s, (const int *) d->cell_count, d->cell_part, d->scan_aux, d->ccount + 8, d->cell_start + d->total_cells, d->total_cells);
 	if(nb > 0) launch_pdl(k_scatter, nb, 256, s, *d, (const float4 *) tmp);
 	launch_pdl(k_cellfin, (d->total_cells + CELLFIN_B - 1) / CELLFIN_B, CELLFIN_B, s, *d);
-	*nl += 5 + (nb > 0 ? 2 : 0);
+	*nl += 3 + (nb > 0 ? 2 : 0);
 	return (int) cudaGetLastError();
 }
 
@@ -5320,7 +5378,7 @@ static void launch_energy(const ppi_dev *d, int mode, int use_nl, cudaStream_t s
 	else if(audit) k_energy<MODE_AUDIT, 4><<<resident_grid(k_energy<MODE_AUDIT, 4>, &g_a4), 128, 0, s>>>(*d, mode);
 	else if(mode == PPI_EN_VOLUME && use_nl && d->nl_k > 0 && d->vpairs) { /* k_vol_plan cleared the queue */
 		launch_pdl(k_energy_vol_pairs, resident_grid(k_energy_vol_pairs, &g_vol_pairs, VP_B), VP_B, s, *d);
-		launch_pdl(k_vol_unsure, 64, 128, s, *d);
+		launch_pdl(k_vol_unsure, 4 * ppi_sm_count(), 128, s, *d); /* a warp per guard-band pair, on every SM's FP64 pipe */
 		*nl += 1;
 	}
 	else if(mode == PPI_EN_VOLUME && use_nl && d->nl_k > 0)
@@ -5346,7 +5404,10 @@ extern "C" int ppi_volume(const ppi_dev *d, long long sweep, int use_nl, cudaStr
 	launch_pdl(k_vol_plan, (d->nrep + 63) / 64, 64, s, *d, sweep);
 	launch_energy(d, PPI_EN_VOLUME, use_nl, s, nl);
 	launch_pdl(k_vol_decide, (d->nrep + 63) / 64, 64, s, *d, sweep);
-	if(d->ntot > 0) launch_pdl(k_vol_apply, (d->ntot + 255) / 256, 256, s, *d);
+	if(d->ntot > 0) { /* one resident wave that loops: when no box is accepted (the usual case) it only reads a flag */
+		const int nb = (d->ntot + 255) / 256, cap = 8 * ppi_sm_count();
+		launch_pdl(k_vol_apply, nb < cap ? nb : cap, 256, s, *d);
+	}
 	*nl += 3;
 	return (int) cudaGetLastError();
 }
@@ -5583,7 +5644,7 @@ extern "C" int pp_gpu_energy_noalloc(int N, const double *r_dev, const double *R
 	d.out_overlaps = n_overlaps_dev ? n_overlaps_dev : (int *) (base + NA_OVER);
 	d.cell_count = (int *) (base + NA_CCOUNT);
 	d.cell_start = (int *) (base + NA_CSTART);
-	d.cell_cursor = (int *) (base + NA_CCURSOR);
+	d.cell_part = (int *) (base + NA_CCURSOR);
 	d.cell_rep = (int *) (base + NA_CREP);
 	d.scan_aux = (int *) (base + NA_AUX);
 	d.clist = (int4 *) (base + NA_CLIST);
