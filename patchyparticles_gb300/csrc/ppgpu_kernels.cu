@@ -4,7 +4,7 @@
  * Every `resort_every` rounds each replica gets a new cell grid (even number of cells per axis, edge >=
  * r_cut, random origin shift) and the particles are counting-sorted into cell order as FP32 working
  * records (spos 16 B + sori 48 B) rebuilt from the FP64 canonical state:
- *   k_grid, k_assign, k_scan_*, k_scatter, k_cellfin (deterministic in-cell order, colour lists)
+ *   k_grid, k_assign, k_scan, k_scatter, k_cellfin (deterministic in-cell order, colour lists)
  * and every particle's neighbour list for the epoch is built (k_nlist: the candidates that can come within
  * r_cut before the next re-sort).
  * One round = the 8 colours of the 2x2x2 checkerboard, one launch each (k_colour): every non-empty
@@ -331,6 +331,11 @@ __device__ __noinline__ int exact_pair(const double *__restrict__ rec_all, const
  * bit-identical exact_pair. Returns -1 overlap, 0 no bond, 1 bond. */
 #define DEC64_TOL 1e-12
 #define DEC64_EXACT 2
+/* what the FP32 test knew about a guard-band pair's patches: nothing certain, certainly not facing each
+ * other, certainly facing each other (then only the distance is decided in FP64) */
+#define PV_FULL 0
+#define PV_NONE 1
+#define PV_BOND 2
 
 __device__ __forceinline__ double rcp64(double x) { /* 1 / x to ~1e-16, x > 0 */
 	double r = (double) (1.0f / (float) x);
@@ -457,7 +462,7 @@ __device__ __forceinline__ double shfl_d(double v, int src) {
 }
 
 __device__ __forceinline__ int decide64_warp(const double *__restrict__ rec_all, const ppi_rparams &rp, const double *box_in, const double *inv_box_in, int ps, int kind,
-		float4 dq, float3 disp, int qs, int vol_mask, const double *vol_f3, const double *vol_box3, int lane) {
+		float4 dq, float3 disp, int qs, int vol_mask, const double *vol_f3, const double *vol_box3, int lane, int pv = 0) {
 	const int half = lane >> 4, e = lane & 15;
 	const double *rec = rec_all + (size_t) (half ? qs : ps) * PPI_REC;
 	/* positions first: the distance test alone decides an overlap or a pair out of range */
@@ -496,6 +501,7 @@ __device__ __forceinline__ int decide64_warp(const double *__restrict__ rec_all,
 	const double dist2 = __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])), __dmul_rn(d[2], d[2]));
 	if(dist2 < 1.) return -1;
 	if(!(dist2 < rp.sqr_rcut)) return 0;
+	if(pv != PV_FULL) return pv == PV_BOND; /* the FP32 patch test was certain: only the distance was in doubt */
 	/* this half's quaternion (state64_fast): lane c < 4 of half 0 forms component c of q (x) dq */
 	double q[4] = { rec[PPI_Q], rec[PPI_Q + 1], rec[PPI_Q + 2], rec[PPI_Q + 3] };
 	if(kind == 1) {
@@ -592,6 +598,33 @@ __device__ __forceinline__ int classify(float dx, float dy, float dz, const floa
 	return CL_UNSURE;
 }
 
+/* classify with the patch verdict of a guard-band pair: the patches are tested in FP32 for every pair
+ * within r_cut^2 + eps, also inside the contact band. A pair near r_cut whose patches certainly do not face
+ * each other is decided here (no bond, and r^2 > 1 + eps rules out an overlap); a guard-band pair whose
+ * patch verdict is certain reports it in *pv, so that the FP64 test only decides the distance. The
+ * patch verdict uses the same bounds as classify's (its error bound does not depend on r^2 >= 1 - eps). */
+__device__ __forceinline__ int classify_pv(float dx, float dy, float dz, const float *cp, const float *cq, float sqr_rcut, float cosmax, float base, float eps, int *pv) {
+	const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+	*pv = PV_FULL;
+	if(r2 < 1.f - eps) return CL_OVER;
+	if(r2 >= sqr_rcut + eps) return CL_NONE;
+	const float inv = rsqrtf(r2) * base;
+	const float a0 = fmaf(dx, cp[0], fmaf(dy, cp[1], dz * cp[2]));
+	const float a1 = fmaf(dx, cp[3], fmaf(dy, cp[4], dz * cp[5]));
+	const float a2 = fmaf(dx, cp[6], fmaf(dy, cp[7], dz * cp[8]));
+	const float pm = fmaxf(fmaxf(-a0 - a1 + a2, a0 - a1 - a2), fmaxf(a0 + a1 + a2, -a0 + a1 - a2)) * inv;
+	const float b0 = fmaf(dx, cq[0], fmaf(dy, cq[1], dz * cq[2]));
+	const float b1 = fmaf(dx, cq[3], fmaf(dy, cq[4], dz * cq[5]));
+	const float b2 = fmaf(dx, cq[6], fmaf(dy, cq[7], dz * cq[8]));
+	const float qm = fmaxf(fmaxf(b0 + b1 - b2, -b0 + b1 + b2), fmaxf(-b0 - b1 - b2, b0 - b1 + b2)) * inv;
+	const bool pnone = pm < cosmax - eps || qm < cosmax - eps, pbond = pm > cosmax + eps && qm > cosmax + eps;
+	const bool near1 = r2 <= 1.f + eps, nearc = r2 > sqr_rcut - eps;
+	if(!near1 && !nearc) return pnone ? CL_NONE : (pbond ? CL_BOND : CL_UNSURE);
+	if(!near1 && pnone) return CL_NONE;
+	*pv = pnone ? PV_NONE : (pbond ? PV_BOND : PV_FULL);
+	return CL_UNSURE;
+}
+
 __device__ __forceinline__ void atomicMaxFloatBits(unsigned int *addr, float v) {
 	if(v > 0.f) atomicMax(addr, __float_as_uint(v)); /* positive floats order like their bit patterns */
 }
@@ -619,45 +652,48 @@ __device__ __noinline__ void audit_pair(const double *rec_all, const ppi_rparams
 #define TAG_VOL 5u
 #define TAG_COLOUR 6u
 
+/* one warp per replica, lane a < 3 for axis a (each axis' FP64 divisions on its own lane) */
 __global__ void k_grid(ppi_dev d, long long epoch) {
-	int r = blockIdx.x * blockDim.x + threadIdx.x;
-	if(r == 0 && d.vp_count) { /* the counters of the list build that follows the sort (ppi_nlist) */
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if(t == 0 && d.vp_count) { /* the counters of the list build that follows the sort (ppi_nlist) */
 		d.vp_count[0] = 0;
 		d.vp_count[1] = 0;
 	}
-	if(r >= d.nrep) return;
+	const int r = t >> 5, lane = t & 31;
+	if(r >= d.nrep) return; /* the whole warp */
 	epoch = ctr_index(epoch, epoch < 0 ? d.ctr->epoch : 0);
 	const ppi_rparams &rp = d.rp[r];
 	ppi_rstate *rs = d.rs + r;
 	ppi_grid *g = d.grid + r;
-	U4 u = rng(rp, epoch, r, TAG_GRID, 0, 0);
-	float us[3] = { u01(u.x), u01(u.y), u01(u.z) };
-	int n[3];
-	for(int a = 0; a < 3; a++) {
-		int k = (int) floor(rs->box[a] / rp.w_min);
-		if(k > PPI_MAX_AXIS_CELLS) k = PPI_MAX_AXIS_CELLS;
-		k &= ~1; /* even: the 2x2x2 checkerboard needs alternating colours across the periodic boundary */
-		if(k < 4) {
-			rs->error = PPI_E_GRID;
-			k = 4;
-		}
-		n[a] = k;
+	const U4 u = rng(rp, epoch, r, TAG_GRID, 0, 0);
+	const int a = lane < 3 ? lane : 0;
+	int err = 0;
+	int k = (int) floor(rs->box[a] / rp.w_min);
+	if(k > PPI_MAX_AXIS_CELLS) k = PPI_MAX_AXIS_CELLS;
+	k &= ~1; /* even: the 2x2x2 checkerboard needs alternating colours across the periodic boundary */
+	if(k < 4) {
+		err = 1;
+		k = 4;
 	}
+	int n[3] = { __shfl_sync(0xffffffffu, k, 0), __shfl_sync(0xffffffffu, k, 1), __shfl_sync(0xffffffffu, k, 2) };
+	err = __shfl_sync(0xffffffffu, err, 0) | __shfl_sync(0xffffffffu, err, 1) | __shfl_sync(0xffffffffu, err, 2);
 	/* stay inside the reserved cell capacity by coarsening the longest axis (coarser cells stay valid) */
 	while((long long) n[0] * n[1] * n[2] > rp.cell_cap) {
-		int a = (n[0] >= n[1] && n[0] >= n[2]) ? 0 : (n[1] >= n[2] ? 1 : 2);
-		if(n[a] <= 4) {
-			rs->error = PPI_E_GRID;
+		int ax = (n[0] >= n[1] && n[0] >= n[2]) ? 0 : (n[1] >= n[2] ? 1 : 2);
+		if(n[ax] <= 4) {
+			err = 1;
 			break;
 		}
-		n[a] -= 2;
+		n[ax] -= 2;
 	}
-	for(int a = 0; a < 3; a++) {
-		double w = rs->box[a] / n[a];
-		g->n[a] = n[a];
+	if(lane < 3) {
+		const int na = lane == 0 ? n[0] : (lane == 1 ? n[1] : n[2]);
+		const float us = u01(lane == 0 ? u.x : (lane == 1 ? u.y : u.z));
+		const double w = rs->box[a] / na;
+		g->n[a] = na;
 		g->w[a] = w;
 		g->wf[a] = (float) w;
-		g->shift[a] = (double) us[a] * w;
+		g->shift[a] = (double) us * w;
 		g->shiftf[a] = (float) g->shift[a];
 		g->inv_w[a] = 1.0 / w;
 		g->inv_L[a] = 1.0 / rs->box[a];
@@ -665,7 +701,10 @@ __global__ void k_grid(ppi_dev d, long long epoch) {
 		g->inv_Lf[a] = (float) g->inv_L[a];
 		g->Lf[a] = (float) rs->box[a];
 	}
-	g->ncells = n[0] * n[1] * n[2];
+	if(lane == 0) {
+		g->ncells = n[0] * n[1] * n[2];
+		if(err) rs->error = PPI_E_GRID;
+	}
 }
 
 /* d2f truncated toward zero (the guesses below only need ~1e-7) */
@@ -710,7 +749,8 @@ __global__ void k_assign(ppi_dev d, float4 *tmp) {
 		float lf;
 		if(__builtin_expect(yg >= m && yg < Lf - m && lg >= m && lg < wf - m && cg < (float) n, 1)) {
 			ci = (int) cg;
-			const double y = __dadd_rn(__fma_rn(-f2d(kf), L, xs[a]), -g.shift[a]);
+			/* k = 0 (the particle's own image, the usual case): fma(-0, L, x) = x */
+			const double y = __dadd_rn(kf == 0.f ? xs[a] : __fma_rn(-f2d(kf), L, xs[a]), -g.shift[a]);
 			lf = d2f(__fma_rn(-f2d(cg), w, y));
 		}
 		else {
@@ -1094,7 +1134,7 @@ struct __align__(16) TileSmem {
 	int pbuf[TILE_PCAP]; /* (candidate - mover) << 10 | attempt << 4 | row */
 	int cbuf[TILE_CCAP]; /* same packing, pairs within the bonding range */
 	int dl[TILE_DCAP];   /* list indices of deferred attempts */
-	int2 uns[TILE_UCAP]; /* guard-band pairs of this iteration: (sorted position, attempt << 1 | kind) */
+	int2 uns[TILE_UCAP]; /* guard-band pairs of this iteration: (sorted position, patch verdict << 7 | attempt << 1 | kind) */
 	int nc, nd, dov, nu;
 };
 
@@ -1372,9 +1412,10 @@ __device__ __forceinline__ void tile_close(const ppi_dev &d, TileSmem &S, int la
 			cln = pair_state<MODE>(d.rec, rp, rs, d.grid[S.rep[a]].inv_L, pslot, 1, S.qr[a], disp, qslot, G.dxn, G.dyn, G.dzn, cpn, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, 0, nullptr, nullptr, A.fallbacks);
 		}
 		else {
-			clo = classify(G.dxo, G.dyo, G.dzo, cpo, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, nullptr);
-			cln = classify(G.dxn, G.dyn, G.dzn, cpn, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, nullptr);
-			/* guard band: recorded, decided after the planes by the certified FP64 test */
+			int pvo, pvn;
+			clo = classify_pv(G.dxo, G.dyo, G.dzo, cpo, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, &pvo);
+			cln = classify_pv(G.dxn, G.dyn, G.dzn, cpn, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, eps, &pvn);
+			/* guard band: recorded with its patch verdict, decided after the planes by the certified FP64 test */
 			const int nu = (clo == CL_UNSURE) + (cln == CL_UNSURE);
 			if(nu) {
 				const int k = atomicAdd(&S.nu, nu);
@@ -1383,8 +1424,8 @@ __device__ __forceinline__ void tile_close(const ppi_dev &d, TileSmem &S, int la
 					continue;
 				}
 				int kk = k;
-				if(clo == CL_UNSURE) S.uns[kk++] = make_int2(jq, a << 1);
-				if(cln == CL_UNSURE) S.uns[kk] = make_int2(jq, (a << 1) | 1);
+				if(clo == CL_UNSURE) S.uns[kk++] = make_int2(jq, (pvo << 7) | (a << 1));
+				if(cln == CL_UNSURE) S.uns[kk] = make_int2(jq, (pvn << 7) | (a << 1) | 1);
 			}
 		}
 		if(clo == CL_BOND) atomicAdd(&S.bo[a], 1);
@@ -1689,12 +1730,12 @@ __device__ __forceinline__ void tile_round(const ppi_dev &d, TileSmem &S, const 
 #pragma unroll 1
 		for(int u = 0; u < nu; u++) {
 			const int2 v = S.uns[u];
-			const int jq = v.x, a = v.y >> 1, kind = v.y & 1;
+			const int jq = v.x, a = (v.y >> 1) & 63, kind = v.y & 1, pv = v.y >> 7;
 			if(S.flag[a] & (TF_OVER | TF_DEFER)) continue; /* warp-uniform: read after the last __syncwarp */
 			const int r = S.rep[a];
 			const float4 md = S.md[a];
 			const int ex = decide64_warp(d.rec, d.rp[r], d.rs[r].box, d.grid[r].inv_L, __float_as_int(md.w), kind, S.qr[a], make_float3(md.x, md.y, md.z),
-					__float_as_int(d.sori[3 * (size_t) jq + 2].w), 0, nullptr, nullptr, lane);
+					__float_as_int(d.sori[3 * (size_t) jq + 2].w), 0, nullptr, nullptr, lane, pv);
 			if(lane == 0) {
 				A.fallbacks++;
 				if(ex == DEC64_EXACT) atomicOr(&S.flag[a], TF_DEFER);
@@ -5276,7 +5317,7 @@ extern "C" int ppi_resort(const ppi_dev *d, long long epoch, cudaStream_t s, lon
 	float4 *tmp = (float4 *) d->tmp_rec; /* ntot float4 fit in the reorder scratch */
 	cudaMemsetAsync(d->cell_count, 0, sizeof(int) * (size_t) d->total_cells, s);
 	cudaMemsetAsync(d->ccount, 0, sizeof(int) * 9, s); /* the 8 colour counts and k_scan's ticket */
-	k_grid<<<(d->nrep + 63) / 64, 64, 0, s>>>(*d, epoch);
+	k_grid<<<(d->nrep + 1) / 2, 64, 0, s>>>(*d, epoch); /* a warp per replica */
 	/* the rest of the sort is one chain of kernels, each launch overlapping its predecessor's tail
 	 * (programmatic dependent launch; every kernel waits before its first access) */
 	int nb = (d->ntot + 255) / 256;
