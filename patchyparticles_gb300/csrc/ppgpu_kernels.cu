@@ -493,9 +493,17 @@ __device__ __forceinline__ int decide64_warp(const double *__restrict__ rec_all,
 #pragma unroll
 	for(int k = 0; k < 3; k++) {
 		d[k] = __dsub_rn(rq_[k], rp_[k]);
-		const double t = d[k] * ib[k], n = rint(t);
-		if(fabs(t - n) > 0.5 - 1e-9) exact = 1; /* rint of d / box could round the other way */
-		d[k] = __dsub_rn(d[k], __dmul_rn(box[k], n));
+		/* the image n = rint(d / box): from an FP32 estimate where it is certain (|tf - t| <= 3 2^-24 |t| < 0.02,
+		 * so a tf within 0.25 of an integer rounds like t, and t is not near a half), else in FP64 */
+		const float tf = d2f(d[k]) * d2f(ib[k]), nf = rintf(tf);
+		if(fabsf(tf - nf) < 0.25f && fabsf(tf) < 1e5f) {
+			if(nf != 0.f) d[k] = __dsub_rn(d[k], __dmul_rn(box[k], f2d(nf)));
+		}
+		else {
+			const double t = d[k] * ib[k], n = rint(t);
+			if(fabs(t - n) > 0.5 - 1e-9) exact = 1; /* rint of d / box could round the other way */
+			d[k] = __dsub_rn(d[k], __dmul_rn(box[k], n));
+		}
 	}
 	if(exact) return DEC64_EXACT;
 	const double dist2 = __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])), __dmul_rn(d[2], d[2]));
@@ -3965,10 +3973,11 @@ __device__ __forceinline__ void vol_flat_pair(const ppi_dev &d, const VolRep &V,
 	const float4 q0 = d.sori[3 * (size_t) jq], q1 = d.sori[3 * (size_t) jq + 1], q2 = d.sori[3 * (size_t) jq + 2];
 	const float cp[9] = { p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w, p2.x };
 	const float cq[9] = { q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x };
-	const int cl = classify(ex, ey, ez, cp, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, V.eps, nullptr);
-	if(cl == CL_UNSURE) { /* guard band: queued for the FP64 decision after the pass (k_vol_unsure) */
+	int pv;
+	const int cl = classify_pv(ex, ey, ez, cp, cq, rp.sqr_rcut_f, rp.cosmax_f, rp.base_f, V.eps, &pv);
+	if(cl == CL_UNSURE) { /* guard band: queued for the FP64 decision after the pass (k_vol_unsure), with its patch verdict */
 		const int k = atomicAdd(d.vun_count, 1);
-		if(k < d.vun_cap) d.vunsure[k] = make_int2(i, jq);
+		if(k < d.vun_cap) d.vunsure[k] = make_int2(i, jq | (pv << 28)); /* sorted positions are below 2^27 */
 		else rs->error = PPI_E_LISTS;
 	}
 	else if(cl == CL_BOND) A.tries += 2; /* the box total counts every bond from both sides */
@@ -4070,11 +4079,12 @@ __global__ void k_vol_unsure(ppi_dev d) {
 	const float3 d0 = make_float3(0.f, 0.f, 0.f);
 	for(int k = warp; k < n; k += nwarp) {
 		const int2 pr = d.vunsure[k];
+		const int jq = pr.y & ((1 << 28) - 1), pv = (unsigned) pr.y >> 28;
 		const int r = d.srep[pr.x];
 		ppi_rstate *rs = d.rs + r;
 		const ppi_grid *g = d.grid + r;
-		const int ps = __float_as_int(d.sori[3 * (size_t) pr.x + 2].w), qs = __float_as_int(d.sori[3 * (size_t) pr.y + 2].w);
-		int x = decide64_warp(d.rec, d.rp[r], rs->box, g->inv_L, ps, 0, q0, d0, qs, g->vol_mask, g->vol_f3, g->vol_box3, lane);
+		const int ps = __float_as_int(d.sori[3 * (size_t) pr.x + 2].w), qs = __float_as_int(d.sori[3 * (size_t) jq + 2].w);
+		int x = decide64_warp(d.rec, d.rp[r], rs->box, g->inv_L, ps, 0, q0, d0, qs, g->vol_mask, g->vol_f3, g->vol_box3, lane, pv);
 		if(lane == 0) {
 			if(x == DEC64_EXACT) x = exact_pair(d.rec, d.rp + r, rs->box, ps, 0, q0, d0, qs, g->vol_mask, g->vol_f3, g->vol_box3, nullptr, nullptr, nullptr);
 			atomicAdd(&rs->fallbacks, 1ull);
