@@ -278,6 +278,16 @@ int pp_mlp_forward(const float *params, int n, const float *x, float *z);
  * each CTA accumulates in tensor memory before its atomics (the engine's training uses the same kernel). */
 int pp_mlp_grad(const float *params, int n, const float *samples, double floor, double tau, int tiles_per_cta, float *grad, double *objective);
 
+/* Failure-detection hook of the tensor-core waits (no counterpart in the reference). The network's kernels
+ * wait for each batch of tcgen05 MMAs on an mbarrier, at most about one second of SM clock cycles; a wait
+ * that runs out sets a sticky error, the kernel stops issuing tensor-core work and returns, and the entry
+ * point returns PP_ERR_CUDA. This runs that same bounded wait in one warp on a barrier of its own, with
+ * limit_cycles (1 .. the one-second default) as its limit: arrive = 1 arrives first, so the wait completes;
+ * arrive = 0 arrives never (and issues no tensor-core work), so the wait runs out. *timed_out and *cycles
+ * (either may be NULL) receive whether it gave up and how long it waited. Returns PP_OK, PP_ERR_CUDA when
+ * the wait ran out (the context stays usable), or PP_ERR_ARG. */
+int pp_mlp_wait_test(long long limit_cycles, int arrive, int *timed_out, long long *cycles);
+
 /* ------------------------------------------------------------------ learned proposal: the engine */
 /* With the learned proposal on, every attempt of pp_gpu_sweeps draws its move from a four-component
  * mixture: component k displaces uniformly in a cube of edge scale_disp[k] * Disp_max and rotates by an

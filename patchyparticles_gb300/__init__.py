@@ -148,7 +148,7 @@ EXPORTED = [
     "pp_gpu_learned_set_weights", "pp_gpu_learned_get_weights", "pp_gpu_set_proposal", "pp_gpu_learned_collect",
     "pp_gpu_learned_train", "pp_gpu_learned_samples", "pp_gpu_learned_clear_samples", "pp_gpu_learned_features",
     "pp_gpu_learned_stats", "pp_gpu_autotune", "pp_gpu_set_graphs", "pp_gpu_set_neighbour_lists",
-    "pp_gpu_set_persistent", "pp_gpu_set_barrier_test", "pp_gpu_sus_histogram",
+    "pp_gpu_set_persistent", "pp_gpu_set_barrier_test", "pp_gpu_sus_histogram", "pp_mlp_wait_test",
 ]
 
 
@@ -216,6 +216,7 @@ def load_library(path=None):
         "pp_gpu_sus_histogram": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
         "pp_gpu_set_barrier_test": (ctypes.c_int, [vp, ctypes.c_longlong, ctypes.c_int]),
         "pp_mlp_grad": (ctypes.c_int, [fp, ctypes.c_int, fp, ctypes.c_double, ctypes.c_double, ctypes.c_int, fp, dp]),
+        "pp_mlp_wait_test": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_longlong)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -549,3 +550,15 @@ def mlp_grad(params, samples, floor=0.1, tau=0.01, tiles_per_cta=1):
     if rc != PP_OK:
         raise PPError(rc, "pp_mlp_grad failed")
     return g, obj.value
+
+
+def mlp_wait_test(limit_cycles, arrive):
+    """Runs the tensor-core kernels' bounded mbarrier wait alone (pp_mlp_wait_test): returns
+    (status code, whether the wait gave up, cycles waited). arrive=False makes the wait run out."""
+    lib = load_library()
+    t = ctypes.c_int(-1)
+    c = ctypes.c_longlong(-1)
+    rc = lib.pp_mlp_wait_test(int(limit_cycles), 1 if arrive else 0, ctypes.byref(t), ctypes.byref(c))
+    if rc not in (PP_OK, PP_ERR_CUDA):
+        raise PPError(rc, "pp_mlp_wait_test failed")
+    return rc, bool(t.value), c.value

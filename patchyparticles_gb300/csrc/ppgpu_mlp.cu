@@ -530,3 +530,47 @@ extern "C" int pp_mlp_grad(const float *params, int n, const float *samples, dou
 	mlp_free(m);
 	return err ? PP_ERR_CUDA : PP_OK;
 }
+
+/* ------------------------------------------------------------------------------------------------ */
+/* failure detection of the tensor-core waits                                                        */
+/* ------------------------------------------------------------------------------------------------ */
+/* One warp waits, the way tc_sync waits for a commit, on an mbarrier of expected count 1. With arrive = 1
+ * thread 0 arrives first and the wait completes; with arrive = 0 nothing arrives and no tensor-core work is
+ * issued, so the wait runs out after limit cycles. out[0] = 1 when any lane gave up, out[1] = the longest
+ * wait in cycles. */
+__global__ void k_mbar_wait_test(long long limit, int arrive, long long *out) {
+	__shared__ uint64_t bar;
+	__shared__ int gave_up;
+	__shared__ unsigned long long longest;
+	if(threadIdx.x == 0) {
+		mbar_init(&bar, 1);
+		gave_up = 0;
+		longest = 0ull;
+	}
+	__syncthreads();
+	if(arrive && threadIdx.x == 0) mbar_arrive(&bar);
+	const long long t0 = clock64();
+	const bool ok = mbar_wait(&bar, 0u, limit);
+	const long long dt = clock64() - t0;
+	if(!ok) gave_up = 1;
+	atomicMax(&longest, (unsigned long long) dt);
+	__syncthreads();
+	if(threadIdx.x == 0) {
+		out[0] = gave_up;
+		out[1] = (long long) longest;
+	}
+}
+
+extern "C" int pp_mlp_wait_test(long long limit_cycles, int arrive, int *timed_out, long long *cycles) {
+	if(limit_cycles <= 0 || limit_cycles > UMMA_WAIT_CYCLES || (arrive != 0 && arrive != 1)) return PP_ERR_ARG;
+	long long *out = NULL, h[2] = {0, 0};
+	if(cudaMalloc(&out, sizeof(h)) != cudaSuccess) return PP_ERR_CUDA;
+	k_mbar_wait_test<<<1, 32>>>(limit_cycles, arrive, out);
+	cudaError_t e = cudaGetLastError();
+	if(e == cudaSuccess) e = cudaMemcpy(h, out, sizeof(h), cudaMemcpyDeviceToHost);
+	cudaFree(out);
+	if(e != cudaSuccess) return PP_ERR_CUDA;
+	if(timed_out) *timed_out = (int) h[0];
+	if(cycles) *cycles = h[1];
+	return h[0] ? PP_ERR_CUDA : PP_OK;
+}

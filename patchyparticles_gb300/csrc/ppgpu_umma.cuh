@@ -118,13 +118,19 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 
 #define UMMA_WAIT_CYCLES (1ll << 31) /* ~1 s at the SM clock: a wait that long has failed */
 
-/* wait for the phase with the given parity to complete; false when the time limit expired. Lanes may
- * leave the loop in different rounds: callers reconverge before any .sync.aligned instruction. */
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+/* wait for the phase with the given parity to complete; false when the time limit (SM clock cycles)
+ * expired. Lanes may leave the loop in different rounds: callers reconverge before any .sync.aligned
+ * instruction. */
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, long long limit = UMMA_WAIT_CYCLES) {
 	const long long t0 = clock64();
 	while(!mbar_try_wait(bar, parity))
-		if(clock64() - t0 > UMMA_WAIT_CYCLES) return false;
+		if(clock64() - t0 > limit) return false;
 	return true;
+}
+
+/* one arrival on *bar from the calling thread */
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+	asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(bar)) : "memory");
 }
 
 /* ---------------------------------------------------------------- MMA issue (one thread) */

@@ -40,3 +40,10 @@ def test_invalid_parameters_are_rejected_before_device_use(built, field, value):
     with pytest.raises(pp.PPError) as ei:
         pp.Engine(p)
     assert ei.value.code == pp.PP_ERR_ARG
+
+
+def test_tensor_core_wait_hook_checks_its_limits_before_device_use(built):
+    lib = pp.load_library()
+    assert lib.pp_mlp_wait_test(0, 0, None, None) == pp.PP_ERR_ARG
+    assert lib.pp_mlp_wait_test(1 << 40, 0, None, None) == pp.PP_ERR_ARG
+    assert lib.pp_mlp_wait_test(1000, 2, None, None) == pp.PP_ERR_ARG

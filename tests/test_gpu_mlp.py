@@ -67,3 +67,19 @@ def test_gradient_of_zero_utilities_with_no_entropy_is_zero(built):
     S[:, mo.IN:] = 0
     g, J = pp.mlp_grad(P, S, floor=0.1, tau=0.0)
     assert np.all(g == 0) and J == 0
+
+
+def test_tensor_core_wait_that_runs_out_is_reported_and_the_gpu_stays_usable(built):
+    """The bounded mbarrier wait of the network's kernels: with an arrival it completes; with none (no
+    tensor-core work issued, a barrier nothing arrives at) it gives up after its limit, the host reads
+    PP_ERR_CUDA, and the context still runs the network."""
+    limit = 2_000_000  # ~1 ms at the SM clock
+    rc, gave_up, cycles = pp.mlp_wait_test(limit, arrive=True)
+    assert rc == pp.PP_OK and not gave_up and 0 <= cycles < limit
+    rc, gave_up, cycles = pp.mlp_wait_test(limit, arrive=False)
+    assert rc == pp.PP_ERR_CUDA and gave_up and cycles > limit
+    P = _params(3)
+    X = mo.random_samples(300, seed=5)[:, :mo.IN]
+    z = pp.mlp_forward(P, X)
+    zr = mo.forward(P, X)
+    assert np.abs(z - zr).max() <= 1e-2 * (1 + np.abs(zr).max())
