@@ -386,10 +386,12 @@ int pp_rrr_header(const char *path, long long *step, int *N, double box[3]);
 
 /* Reads a .rrr configuration exactly as system_init does (system.c:213-243): each particle's two stored
  * orientation rows are normalised, the third row is their cross product and the matrix is passed through
- * gram_schmidt, so R is bit-identical to the reference's. r: N x 3, R: N x 9. */
+ * gram_schmidt, so R is bit-identical to the reference's. r: N x 3, R: N x 9. Returns PP_OK, PP_ERR_IO
+ * (unreadable or malformed file, a particle count other than N; message in err) or PP_ERR_ARG. */
 int pp_rrr_read(const char *path, int N, double *r, double *R, double box[3], char *err, int err_len);
 
-/* Writes a .rrr configuration in output_save's format (output.c:302-317). */
+/* Writes a .rrr configuration in output_save's format (output.c:302-317). Returns PP_OK, PP_ERR_ARG, or
+ * PP_ERR_IO when the file cannot be opened or a write fails (e.g. a full disk). */
 int pp_rrr_write(const char *path, long long step, int N, const double *r, const double *R, const double box[3]);
 
 /* Seeded random sequential insertion of N non-overlapping unit spheres at the given density in a cubic box,

@@ -198,7 +198,7 @@ static int check_params(pp_engine *e, const pp_params *p) {
 	if(!(p->kf_delta > 0.) || !(p->kf_delta < 1.)) return set_err(e, PP_ERR_ARG, "KF_delta must lie in (0, 1)");
 	if(!(p->kf_cosmax > -1.) || !(p->kf_cosmax < 1.)) return set_err(e, PP_ERR_ARG, "KF_cosmax must lie in (-1, 1)");
 	if(p->precision != PP_PREC_FP32_GUARD && p->precision != PP_PREC_FP64) return set_err(e, PP_ERR_ARG, "unknown precision %d", p->precision);
-	if(p->guard_eps > 1e-2) return set_err(e, PP_ERR_ARG, "guard_eps too large");
+	if(!(p->guard_eps <= 1e-2)) return set_err(e, PP_ERR_ARG, "guard_eps too large"); /* NaN too */
 	if(p->resort_every < 0 || p->resort_every > 64) return set_err(e, PP_ERR_ARG, "resort_every (re-sort period in rounds) must be 0 or in [1, 64]");
 	if(p->ensemble == PP_NPT && !(p->rescale_factor_max > 0. && p->rescale_factor_max < 1.)) return set_err(e, PP_ERR_ARG, "rescale_factor_max must lie in (0, 1)");
 	if(p->lx_move < 0 || p->lx_move > 2) return set_err(e, PP_ERR_ARG, "Lx_move must be 0, 1 (reference acceptance) or 2 (Boltzmann acceptance)");
@@ -222,6 +222,7 @@ static int check_params(pp_engine *e, const pp_params *p) {
 }
 
 static int create_common(const pp_params *prms, int n, pp_engine **out) {
+	if(out == NULL) return PP_ERR_ARG;
 	*out = NULL;
 	if(n < 1 || prms == NULL) return PP_ERR_ARG;
 	pp_engine *e = calloc(1, sizeof(pp_engine));
@@ -1574,6 +1575,10 @@ static void set_msg(char *err, int len, const char *fmt, ...) {
 /* system.c:77-245: header "%*d %d %lf %lf %lf", then per particle: row 0 via fgets + sscanf, row 1 and the
  * position via fscanf; rows normalised, row 2 = row0 x row1, gram_schmidt. */
 int pp_rrr_read(const char *path, int N, double *r, double *R, double box[3], char *err, int err_len) {
+	if(path == NULL || N < 0 || (N > 0 && (r == NULL || R == NULL))) {
+		set_msg(err, err_len, "pp_rrr_read: bad arguments");
+		return PP_ERR_ARG;
+	}
 	FILE *f = fopen(path, "r");
 	if(f == NULL) {
 		set_msg(err, err_len, "Initial_conditions_file '%s' is not readable", path);
@@ -1628,6 +1633,7 @@ int pp_rrr_read(const char *path, int N, double *r, double *R, double box[3], ch
 }
 
 int pp_rrr_write(const char *path, long long step, int N, const double *r, const double *R, const double box[3]) {
+	if(path == NULL || box == NULL || N < 0 || (N > 0 && (r == NULL || R == NULL))) return PP_ERR_ARG;
 	FILE *out = fopen(path, "w");
 	if(out == NULL) return PP_ERR_IO;
 	fprintf(out, "%lld %d %.12lf %.12lf %.12lf\n", step, N, box[0], box[1], box[2]); /* output.c:306 */
@@ -1637,7 +1643,8 @@ int pp_rrr_write(const char *path, long long step, int N, const double *r, const
 		fprintf(out, "%lf %lf %lf\n", Ri[3], Ri[4], Ri[5]);
 		fprintf(out, "%.12lf %.12lf %.12lf\n", ri[0], ri[1], ri[2]);
 	}
-	fclose(out);
+	const int bad = ferror(out);
+	if(fclose(out) != 0 || bad) return PP_ERR_IO; /* a short write (full disk) is not a saved configuration */
 	return PP_OK;
 }
 

@@ -113,3 +113,27 @@ def test_reader_messages_are_the_reference_loaders(built):
         with pytest.raises(RuntimeError) as ex:
             po.System(po.params(), path=path)
         assert str(ex.value) == read(path, N)[1]
+
+
+def test_writer_reports_a_failed_write(built):
+    """A configuration that could not be written in full is an error, not a saved file (a full disk:
+    /dev/full accepts the open and fails the writes)."""
+    r = np.zeros((4, 3))
+    R = np.tile(np.eye(3).reshape(9), (4, 1))
+    box = np.full(3, 10.0)
+    if os.path.exists("/dev/full"):
+        with pytest.raises(pp.PPError) as ei:
+            pp.write_rrr("/dev/full", 0, r, R, box)
+        assert ei.value.code == pp.PP_ERR_IO
+    with tempfile.TemporaryDirectory() as d:
+        with pytest.raises(pp.PPError) as ei:
+            pp.write_rrr(os.path.join(d, "missing", "x.rrr"), 0, r, R, box)
+        assert ei.value.code == pp.PP_ERR_IO
+
+
+def test_reader_and_writer_refuse_missing_arrays(built):
+    lib = pp.load_library()
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "c.rrr").encode()
+        assert lib.pp_rrr_write(path, 0, 2, None, None, None) == pp.PP_ERR_ARG
+        assert lib.pp_rrr_read(path, 2, None, None, None, None, 0) == pp.PP_ERR_ARG

@@ -42,3 +42,9 @@ def test_lx_move_is_ignored_for_npt(built):
         pp.Engine(pp.default_params(ensemble=pp.NPT, lx_move=1, lx_change_max=0.0)).close()
     except pp.PPError as ex:  # without a GPU the engine stops at the CUDA stream, not at the parameters
         assert ex.code == pp.PP_ERR_CUDA
+
+
+def test_a_nan_guard_band_is_refused(built):
+    with pytest.raises(pp.PPError) as ex:
+        pp.Engine(pp.default_params(guard_eps=float("nan")))
+    assert ex.value.code == pp.PP_ERR_ARG and "guard_eps" in ex.value.message
