@@ -126,7 +126,9 @@ int pp_gpu_create_batch(const pp_params *prms, int n_replicas, pp_engine **out);
 
 /* Copies one system's state to the device (the System the reference builds in system_init,
  * system.c:213-251, plus the initial energy and overlap check of main.c:55-64: returns PP_ERR_OVERLAP
- * if the configuration contains an overlap). r: N x 3, R: N x 9 row-major, box: Lx Ly Lz. */
+ * if the configuration contains an overlap). r: N x 3, R: N x 9 row-major, box: Lx Ly Lz. A box side that
+ * is not positive and finite, or a position or orientation entry that is not finite, returns PP_ERR_ARG;
+ * after the latter the replica has no configuration until it is uploaded again. */
 int pp_gpu_upload(pp_engine *e, int N, const double *r, const double *R, const double box[3]);
 int pp_gpu_upload_replica(pp_engine *e, int replica, int N, const double *r, const double *R, const double box[3]);
 

@@ -816,10 +816,20 @@ static int commit(pp_engine *e) {
 	return PP_OK;
 }
 
-/* copies replica r's host arrays into its device slots */
+/* all-ones exponent: an infinity or a NaN */
+static inline uint64_t nonfinite_bits(double v) {
+	uint64_t u;
+	memcpy(&u, &v, sizeof(u));
+	return ((u >> 52) & 0x7ff) == 0x7ff;
+}
+
+/* copies replica r's host arrays into its device slots. A non-finite coordinate or orientation entry
+ * (checked in the same pass) refuses the upload: the replica is then without a configuration until the
+ * next upload. */
 static int push_replica(pp_engine *e, int r, const double *rr, const double *RR) {
 	ppi_rparams *rp = e->h_rp + r;
 	int N = rp->N;
+	uint64_t bad = 0;
 	for(int i = 0; i < N; i++) {
 		double *dst = e->pin_rec + (size_t) i * PPI_REC;
 		dst[0] = rr[3 * i];
@@ -830,7 +840,14 @@ static int push_replica(pp_engine *e, int r, const double *rr, const double *RR)
 		dst[PPI_Q + 2] = 0.0;
 		dst[PPI_Q + 3] = 0.0;
 		memcpy(dst + PPI_R0, RR + 9 * (size_t) i, 9 * sizeof(double));
+		for(int k = 0; k < 3; k++) bad |= nonfinite_bits(dst[k]);
+		for(int k = 0; k < 9; k++) bad |= nonfinite_bits(dst[PPI_R0 + k]);
 		e->pin_id[i] = i;
+	}
+	if(bad) {
+		e->committed = 0;
+		e->uploaded[r] = 0;
+		return set_err(e, PP_ERR_ARG, "replica %d: a position or orientation entry is not finite", r);
 	}
 	CU(cudaMemcpyAsync(e->d.rec + (size_t) rp->p0 * PPI_REC, e->pin_rec, sizeof(double) * PPI_REC * N, cudaMemcpyHostToDevice, e->stream));
 	CU(cudaMemcpyAsync(e->d.id + rp->p0, e->pin_id, sizeof(int) * N, cudaMemcpyHostToDevice, e->stream));
@@ -868,7 +885,7 @@ static int finish_upload(pp_engine *e, int only) {
 int pp_gpu_upload_replica(pp_engine *e, int r, int N, const double *rr, const double *RR, const double box[3]) {
 	if(e == NULL || r < 0 || r >= e->nrep || N < 0 || (N > 0 && (rr == NULL || RR == NULL)) || box == NULL) return set_err(e, PP_ERR_ARG, "invalid upload arguments");
 	for(int a = 0; a < 3; a++)
-		if(!(box[a] > 0.)) return set_err(e, PP_ERR_ARG, "box sides must be positive");
+		if(!(box[a] > 0.) || nonfinite_bits(box[a])) return set_err(e, PP_ERR_ARG, "box sides must be positive and finite");
 	const pp_params *p = e->prm + r;
 	if(p->ensemble == PP_SUS) { /* system.c:100-101 */
 		if(N < p->n_min) return set_err(e, PP_ERR_ARG, "Number of particles %d is smaller than Umbrella_sampling_min (%d)", N, p->n_min);
@@ -1325,7 +1342,7 @@ int pp_gpu_get_energy(pp_engine *e, int r, double *E) {
 int pp_gpu_box(pp_engine *e, int r, double box[3]) {
 	int rc = ready(e);
 	if(rc != PP_OK) return rc;
-	if(r < 0 || r >= e->nrep) return set_err(e, PP_ERR_ARG, "bad replica");
+	if(r < 0 || r >= e->nrep || box == NULL) return set_err(e, PP_ERR_ARG, "bad replica or box pointer");
 	rc = read_states(e);
 	if(rc != PP_OK) return rc;
 	memcpy(box, e->h_rs[r].box, sizeof(double) * 3);

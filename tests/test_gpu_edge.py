@@ -6,6 +6,7 @@ import pytest
 
 import patchyparticles_gb300 as pp
 from tests.helpers import config
+from oracle import pyoracle as po
 
 pytestmark = pytest.mark.gpu
 
@@ -57,3 +58,32 @@ def test_batch_with_an_empty_replica(built):
         assert np.array_equal(x, y)
     e.close()
     single.close()
+
+
+@pytest.mark.parametrize("where", ["position", "orientation", "box"])
+def test_non_finite_input_is_refused_and_a_new_upload_recovers(built, where):
+    r, R, box = config("c2")
+    bad_r, bad_R, bad_box = r.copy(), R.copy(), box.copy()
+    if where == "position":
+        bad_r[len(r) // 2, 1] = np.nan
+    elif where == "orientation":
+        bad_R[7, 4] = np.inf
+    else:
+        bad_box[2] = np.inf
+    e = pp.Engine(pp.default_params(temperature=0.2, seed=5))
+    e.upload(r, R, box)
+    with pytest.raises(pp.PPError) as ei:
+        e.upload(bad_r, bad_R, bad_box)
+    assert ei.value.code == pp.PP_ERR_ARG and "finite" in ei.value.message
+    if where != "box":  # a refused configuration leaves the replica without one
+        with pytest.raises(pp.PPError) as ei:
+            e.sweeps(1)
+        assert ei.value.code == pp.PP_ERR_STATE
+    e.upload(r, R, box)
+    e.sweeps(4)
+    e.sync()
+    r2, R2, b2 = e.download()
+    s = po.System(po.params(T=0.2), arrays=(r2, R2, b2))
+    E, ov = s.init_energy()
+    assert not ov and E == e.tracked_energy()
+    e.close()
