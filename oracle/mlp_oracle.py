@@ -1,5 +1,5 @@
 """CPU oracle of the learned proposal's network (test infrastructure only: tests/, smoke() and bench.py's
-CPU leg use it as the checker; the product path never imports it).
+CPU leg compare the GPU network with it; the product path never imports it).
 
 The network and its training objective have no counterpart in the reference (they are the learned
 proposal that the plain MC_move_rototranslate, MC.c:311-340, falls back to). This module restates them

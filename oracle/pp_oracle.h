@@ -3,7 +3,7 @@
  * (Kern-Frenkel four-patch hard spheres, Dynamics = 0, NVT and NPT).
  *
  * TEST INFRASTRUCTURE ONLY. Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may
- * load this library; the product never links, imports or calls it. It is the checker the CUDA path is
+ * load this library; the product never links, imports or calls it. It is what the CUDA path is
  * compared with, and it is itself pinned against the reference compiled from source (oracle/_ref) and
  * against golden outputs of that build committed under tests/golden/.
  *
