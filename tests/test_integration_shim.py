@@ -18,7 +18,8 @@ CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 # the reference's library sources (makefile.common's object list without main.o)
 REF_LIB_SRC = ["parse_input.c", "output.c", "system.c", "MC.c", "utils.c", "avb.c", "vmmc.c", "cells.c"]
 
-# stands in for the reference's main.c and MC_init, which the edits listed in INTEGRATION.md make call these
+# stands in for the reference's main.c and MC_init, which a maintainer's edits (MC_init selects the GPU
+# ensemble, main.c syncs before output) make call these hooks
 DRIVER = r"""
 #include "defs.h"
 #include "output.h"
